@@ -1,0 +1,445 @@
+/*
+ * msx_oracle.c -- CPU restatement of MuPhiSim v1.1's explicit C3D4 step.
+ *
+ * TEST INFRASTRUCTURE ONLY (see msx_oracle.h).  Each routine cites the
+ * reference file:line it restates and keeps the reference's operation order,
+ * so that built with -ffp-contract=off it agrees bit for bit with the
+ * reference compiled without FMA contraction.
+ */
+#include "msx_oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* src/mathematics/maths.cpp:1564-1577 determinantTensor (3x3 branch). */
+static double det3(const double *A)
+{
+    return A[0] * (A[4] * A[8] - A[7] * A[5]) -
+           A[1] * (A[3] * A[8] - A[6] * A[5]) +
+           A[2] * (A[3] * A[7] - A[6] * A[4]);
+}
+
+/* src/mathematics/maths.cpp:2749-2785 inverse (nn == 3 branch). */
+static void inverse3(const double *A, double *Ai)
+{
+    const int nn = 3;
+    double det = det3(A);
+    double idet = 1.0 / det;
+    Ai[0] = idet * (A[nn + 1] * A[nn * 2 + 2] - A[nn * 1 + 2] * A[nn * 2 + 1]);
+    Ai[nn] = -idet * (A[nn * 1 + 0] * A[nn * 2 + 2] - A[nn * 1 + 2] * A[nn * 2 + 0]);
+    Ai[nn * 2] = idet * (A[nn * 1 + 0] * A[nn * 2 + 1] - A[nn * 1 + 1] * A[nn * 2 + 0]);
+    Ai[1] = -idet * (A[nn * 0 + 1] * A[nn * 2 + 2] - A[nn * 0 + 2] * A[nn * 2 + 1]);
+    Ai[nn + 1] = idet * (A[nn * 0 + 0] * A[nn * 2 + 2] - A[nn * 0 + 2] * A[nn * 2 + 0]);
+    Ai[2 * nn + 1] = -idet * (A[nn * 0 + 0] * A[nn * 2 + 1] - A[nn * 0 + 1] * A[nn * 2 + 0]);
+    Ai[2] = idet * (A[nn * 0 + 1] * A[nn * 1 + 2] - A[nn * 0 + 2] * A[nn * 1 + 1]);
+    Ai[nn + 2] = -idet * (A[nn * 0 + 0] * A[nn * 1 + 2] - A[nn * 0 + 2] * A[nn * 1 + 0]);
+    Ai[2 * nn + 2] = idet * (A[nn * 0 + 0] * A[nn * 1 + 1] - A[nn * 0 + 1] * A[nn * 1 + 0]);
+}
+
+/* src/mathematics/geometry.cpp:180-190 crossProduct + :90-136 areaTriangle
+ * (ndim == 3): A = v1 - v3, B = v2 - v3, area = 0.5*|A x B|.  The argument
+ * layout is the reference's {x1,x2,x3, y1,y2,y3, z1,z2,z3}. */
+static double area_triangle(const double *nodes)
+{
+    double A[3], B[3], C[3];
+    for (int i = 0; i < 3; i++) {
+        A[i] = nodes[i * 3] - nodes[i * 3 + 2];
+        B[i] = nodes[i * 3 + 1] - nodes[i * 3 + 2];
+    }
+    C[0] = A[1] * B[2] - A[2] * B[1];
+    C[1] = A[2] * B[0] - A[0] * B[2];
+    C[2] = A[0] * B[1] - A[1] * B[0];
+    return 0.5 * sqrt(C[0] * C[0] + C[1] * C[1] + C[2] * C[2]);
+}
+
+/* src/mathematics/geometry.cpp:264-301 inscribedSphere, times two as in
+ * src/spatialDiscretisation/classLinearTetrahedra.cpp:146-163
+ * characteristicLength.  x[a*3+c] = coordinate c of vertex a. */
+double orc_char_length(const double *x)
+{
+    const double *p0 = x, *p1 = x + 3, *p2 = x + 6, *p3 = x + 9;
+    double arg[9], s1, s2, s3, s4;
+#define TRI(P, Q, R) \
+    arg[0] = P[0]; arg[1] = Q[0]; arg[2] = R[0]; \
+    arg[3] = P[1]; arg[4] = Q[1]; arg[5] = R[1]; \
+    arg[6] = P[2]; arg[7] = Q[2]; arg[8] = R[2];
+    TRI(p0, p1, p2) s1 = area_triangle(arg);
+    TRI(p1, p2, p3) s2 = area_triangle(arg);
+    TRI(p0, p2, p3) s3 = area_triangle(arg);
+    TRI(p0, p1, p3) s4 = area_triangle(arg);
+#undef TRI
+    double A = fabs(s1) + fabs(s2) + fabs(s3) + fabs(s4);
+    double M[9] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2],
+                   p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2],
+                   p3[0] - p0[0], p3[1] - p0[1], p3[2] - p0[2]};
+    double V = 1.0 / 6.0 * fabs(det3(M));
+    double r = 3.0 * V / A;
+    return 2 * r;
+}
+
+/* src/spatialDiscretisation/classLinearTetrahedra.cpp:171-292 defineGPs and
+ * getInterpolationParameters; GPsDistribution.cpp:334-342 (1-point rule,
+ * weight literal 0.166666666667); classGPs.cpp:24-31 (wJ = w*|J|);
+ * maths.cpp:1679-1692 multGeneralMatrices (accumulation from 0). */
+int orc_precompute(int64_t nn, int64_t ne, const double *X, const int32_t *conn,
+                   double *dphi, double *wJ, double *Lref)
+{
+    static const double natDev[12] = {-1.0, -1.0, -1.0, 1.0, 0.0, 0.0,
+                                      0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
+    const double w = 0.166666666667;
+    for (int64_t e = 0; e < ne; e++) {
+        double xyz[12], pts[12], Jac[9], invJ[9];
+        for (int k = 0; k < 4; k++) {
+            int64_t nd = conn[e * 4 + k];
+            if (nd < 0 || nd >= nn) return ORC_ERR_ARG;
+            for (int i = 0; i < 3; i++) {
+                xyz[i * 4 + k] = X[i * nn + nd];
+                pts[k * 3 + i] = X[i * nn + nd];
+            }
+        }
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+                for (int k = 0; k < 4; k++) c += xyz[i * 4 + k] * natDev[k * 3 + j];
+                Jac[i * 3 + j] = c;
+            }
+        double J = det3(Jac);
+        inverse3(Jac, invJ);
+        for (int a = 0; a < 4; a++)
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+                for (int k = 0; k < 3; k++) c += natDev[a * 3 + k] * invJ[k * 3 + j];
+                dphi[e * 12 + a * 3 + j] = c;
+            }
+        wJ[e] = w * fabs(J);
+        Lref[e] = orc_char_length(pts);
+    }
+    return ORC_OK;
+}
+
+/* constitutiveAlgorithms.cpp:135-206 getLumpedMassVector (generic branch),
+ * solverExplicit.cpp:429-459 computeLumpedMassVector (element-order sum). */
+int orc_lumped_mass(int64_t nn, int64_t ne, const int32_t *conn, const double *wJ,
+                    const int32_t *elem_mat, const orc_material *mats, double *mass)
+{
+    const double phi = -1.0 * 0.25 - 1.0 * 0.25 - 1.0 * 0.25 + 1.0;
+    for (int64_t i = 0; i < nn; i++) mass[i] = 0;
+    for (int64_t e = 0; e < ne; e++) {
+        double rho = mats[elem_mat ? elem_mat[e] : 0].rho;
+        double m = 0;
+        for (int b = 0; b < 4; b++) m += wJ[e] * rho * phi * phi;
+        for (int a = 0; a < 4; a++) mass[conn[e * 4 + a]] += m;
+    }
+    return ORC_OK;
+}
+
+/* hyperElasticNeoHookean.cpp:51-54 and hyperElasticStVenantKirchhoff.cpp:50-55. */
+double orc_sound_speed(const orc_material *m)
+{
+    double E = m->young, nu = m->nu;
+    if (m->law == ORC_STVK) return sqrt(E / m->rho);
+    double lambda = (E * nu) / ((1. + nu) * (1. - 2. * nu));
+    double mu = 0.5 * E / (1. + nu);
+    return sqrt((lambda + 2 * mu) / m->rho);
+}
+
+void orc_stress(const orc_material *m, const double *F, double *P)
+{
+    double E = m->young, nu = m->nu;
+    if (m->law == ORC_COMPRESSIBLE_NH) {
+        /* hyperElasticNeoHookean.cpp:221-259; TensorOperations.h:22-75,478-512,215-229 */
+        double lambda = (E * nu) / ((1. + nu) * (1. - 2. * nu));
+        double mu = 0.5 * E / (1. + nu);
+        double J = det3(F), C[9], invC[9], PK2[9];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+                for (int k = 0; k < 3; k++) c += F[k * 3 + i] * F[k * 3 + j];
+                C[i * 3 + j] = c;
+            }
+        inverse3(C, invC);
+        for (int i = 0; i < 9; i++) PK2[i] = 0;
+        for (int i = 0; i < 3; i++) PK2[i * 3 + i] += mu;
+        double alpha = lambda * log(J) - mu;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) PK2[i * 3 + j] += alpha * invC[i * 3 + j];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+                for (int k = 0; k < 3; k++) c += F[i * 3 + k] * PK2[k * 3 + j] * 1.;
+                P[i * 3 + j] = c;
+            }
+    } else if (m->law == ORC_NEO_HOOKEAN) {
+        /* hyperElasticNeoHookean.cpp:23-33 (constants), :70-127 (stress);
+         * TensorOperations.h:517-551 leftCauchy, :577-592 dotSecondTranspose */
+        double mu = 0.5 * E / (1. + nu);
+        double K1 = E / (3 * (1 - 2 * nu));
+        double B[9], invF[9], Ca[9];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+                for (int k = 0; k < 3; k++) c += F[i * 3 + k] * F[j * 3 + k];
+                B[i * 3 + j] = c;
+            }
+        double J = det3(F);
+        inverse3(F, invF);
+        double traceB = 0;
+        for (int i = 0; i < 3; i++) traceB += B[i * 3 + i];
+        double fact1 = pow(J, 5.0 / 3.0);
+        double fact2 = mu / fact1;
+        for (int i = 0; i < 9; i++) Ca[i] = 0;
+        for (int i = 0; i < 9; i++) Ca[i] += fact2 * B[i];
+        double fact3 = -(mu / 3.0) * traceB / fact1 + K1 * (J - 1.0);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) Ca[i * 3 + j] += fact3 * (i == j ? 1.0 : 0.0);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+                for (int k = 0; k < 3; k++) c += Ca[i * 3 + k] * invF[j * 3 + k] * J;
+                P[i * 3 + j] = c;
+            }
+    } else {
+        /* hyperElasticStVenantKirchhoff.cpp:64-101 stress, :203-227;
+         * maths.cpp:1227-1243 computeGL, :1703-1715 multTensorTensor3 */
+        double C[9], Eg[9], S[9];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+                for (int k = 0; k < 3; k++) c += F[k * 3 + i] * F[k * 3 + j];
+                C[i * 3 + j] = c;
+            }
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) Eg[i * 3 + j] = 0.5 * (C[i * 3 + j] - (i == j ? 1.0 : 0.0));
+        double mu2 = E / (1. + nu);
+        double lam = E * nu / ((1. + nu) * (1. - (2 * nu)));
+        double trE = 0;
+        for (int i = 0; i < 3; i++) trE += Eg[i * 3 + i];
+        for (int i = 0; i < 9; i++) S[i] = Eg[i] * mu2;
+        for (int i = 0; i < 3; i++) S[i * 3 + i] += lam * trE;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+                for (int k = 0; k < 3; k++) c += F[i * 3 + k] * S[k * 3 + j];
+                P[i * 3 + j] = c;
+            }
+    }
+}
+
+/* constitutiveManager.cpp:137-164 computeKinematicVariables (F), then the law,
+ * then constitutiveAlgorithms.cpp:33-57 getForceVector; fe[a + 4*i]. */
+static void element_force(const double *dphi, double wJ, const orc_material *m,
+                          const double *ue /* ue[a*3+i] */, double *fe, double *Fo, double *Po)
+{
+    double F[9], P[9];
+    for (int i = 0; i < 9; i++) F[i] = 0.;
+    for (int i = 0; i < 3; i++) {
+        F[i * 3 + i] += 1.;
+        for (int a = 0; a < 4; a++)
+            for (int j = 0; j < 3; j++) F[i * 3 + j] += dphi[a * 3 + j] * ue[a * 3 + i];
+    }
+    orc_stress(m, F, P);
+    for (int a = 0; a < 4; a++)
+        for (int i = 0; i < 3; i++) {
+            double f = 0;
+            for (int J = 0; J < 3; J++) f += wJ * P[i * 3 + J] * dphi[a * 3 + J];
+            fe[a + 4 * i] = 0 + f;
+        }
+    if (Fo) memcpy(Fo, F, sizeof F);
+    if (Po) memcpy(Po, P, sizeof P);
+}
+
+/* solverExplicit.cpp:363-379 computeInternalForce: scatter in element order. */
+int orc_internal_force(int64_t nn, int64_t ne, const int32_t *conn, const double *dphi,
+                       const double *wJ, const int32_t *elem_mat, const orc_material *mats,
+                       const double *u, double *fint, double *F_out, double *P_out, int nthreads)
+{
+    double *fe = (double *)malloc(sizeof(double) * 12 * (size_t)(ne > 0 ? ne : 1));
+    if (!fe) return ORC_ERR_ARG;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+    for (int64_t e = 0; e < ne; e++) {
+        double ue[12];
+        for (int a = 0; a < 4; a++)
+            for (int i = 0; i < 3; i++) ue[a * 3 + i] = u[conn[e * 4 + a] + i * nn];
+        element_force(dphi + 12 * e, wJ[e], &mats[elem_mat ? elem_mat[e] : 0], ue, fe + 12 * e,
+                      F_out ? F_out + 9 * e : 0, P_out ? P_out + 9 * e : 0);
+    }
+    (void)nthreads;
+    for (int64_t i = 0; i < 3 * nn; i++) fint[i] = 0;
+    for (int64_t e = 0; e < ne; e++)
+        for (int i = 0; i < 3; i++)
+            for (int a = 0; a < 4; a++) fint[conn[e * 4 + a] + nn * i] += fe[12 * e + a + 4 * i];
+    free(fe);
+    return ORC_OK;
+}
+
+/* solvers.cpp:296-320 calculateCriticalTimeStep(nod, elem, uK) without the
+ * scale factor; uK == NULL gives the undeformed variant of :276-287. */
+static double critical_dt(int64_t nn, int64_t ne, const double *X, const int32_t *conn,
+                          const double *Lref, const double *cel, const double *uK, int nthreads)
+{
+    double best = INFINITY;
+    (void)nthreads;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(min : best) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+    for (int64_t e = 0; e < ne; e++) {
+        double v;
+        if (!uK) {
+            v = Lref[e] / cel[e];
+        } else {
+            double x[12];
+            for (int a = 0; a < 4; a++)
+                for (int k = 0; k < 3; k++) {
+                    int64_t nd = conn[e * 4 + a];
+                    x[a * 3 + k] = X[k * nn + nd];
+                    x[a * 3 + k] += uK[nn * k + nd];
+                }
+            double dist = orc_char_length(x);
+            double m = (dist < Lref[e]) ? dist : Lref[e]; /* std::min(minDist, dist) */
+            v = m / cel[e];
+        }
+        if (v < best) best = v;
+    }
+    return best;
+}
+
+/* The explicit solve, src/solvers/solverExplicit.cpp:63-338 (sequential build):
+ * time advance with the previous dt (:227-232), dt from the deformed CFL
+ * (:267-276), prediction (nonlinearSystem.cpp:1186-1200), Dirichlet
+ * (solverExplicit.cpp:545-575), internal force, rhs = -fint (:598-628),
+ * a = rhs/m and v += dt*(a_prev + a)/2 (nonlinearSystem.cpp:1034-1117). */
+int orc_run(const orc_problem *p, double *u, double *v, double *a,
+            double *dt_hist, int64_t max_hist, orc_result *res)
+{
+    const int64_t nn = p->nn, ne = p->ne, ndof = 3 * nn;
+    int rc = ORC_OK;
+    double *dphi = malloc(sizeof(double) * 12 * (size_t)ne), *wJ = malloc(sizeof(double) * (size_t)ne);
+    double *Lref = malloc(sizeof(double) * (size_t)ne), *cel = malloc(sizeof(double) * (size_t)ne);
+    double *mass = malloc(sizeof(double) * (size_t)nn), *fint = malloc(sizeof(double) * (size_t)ndof);
+    double *uK = malloc(sizeof(double) * (size_t)ndof), *aprev = malloc(sizeof(double) * (size_t)ndof);
+    char *cons = calloc((size_t)ndof, 1);
+    int32_t *flag = malloc(sizeof(int32_t) * (size_t)(p->nbc > 0 ? p->nbc : 1));
+    double *UU = malloc(sizeof(double) * (size_t)(p->nbc > 0 ? p->nbc : 1));
+    if (!dphi || !wJ || !Lref || !cel || !mass || !fint || !uK || !aprev || !cons || !flag || !UU) {
+        rc = ORC_ERR_ARG;
+        goto done;
+    }
+    if ((rc = orc_precompute(nn, ne, p->X, p->conn, dphi, wJ, Lref)) != ORC_OK) goto done;
+    orc_lumped_mass(nn, ne, p->conn, wJ, p->elem_mat, p->mats, mass);
+    for (int64_t e = 0; e < ne; e++) cel[e] = orc_sound_speed(&p->mats[p->elem_mat ? p->elem_mat[e] : 0]);
+    /* classNodes.cpp:58-74: ramp stores U/duration (flag -1), inst stores U (flag 1) */
+    for (int64_t b = 0; b < p->nbc; b++) {
+        const orc_bc *bc = &p->bcs[b];
+        if (bc->dof < 0 || bc->dof >= ndof) { rc = ORC_ERR_ARG; goto done; }
+        cons[bc->dof] = 1;
+        if (bc->mode == ORC_BC_RAMP) { flag[b] = -1; UU[b] = bc->value / (p->tf - p->t0); }
+        else if (bc->mode == ORC_BC_INST) { flag[b] = 1; UU[b] = bc->value; }
+        else { flag[b] = 2; UU[b] = bc->value; }
+    }
+    /* solverExplicit.cpp:141-149: prev <- current at set-up */
+    memcpy(aprev, a, sizeof(double) * (size_t)ndof);
+    double t = p->t0, tf = p->tf;
+    double dt = critical_dt(nn, ne, p->X, p->conn, Lref, cel, NULL, p->nthreads);
+    dt = dt * p->scale_factor;
+    if (res) res->dt_init = dt;
+    /* :176-177 uK is refreshed from the system only when t0 < 1e-12 */
+    if (t < 1E-12 && !p->first_step_zero_uK) memcpy(uK, u, sizeof(double) * (size_t)ndof);
+    else memset(uK, 0, sizeof(double) * (size_t)ndof);
+    int64_t step = 0;
+    while (t < tf - 1E-12) {
+        if (p->max_steps > 0 && step >= p->max_steps) break;
+        if (t + dt > tf) { dt = tf - t; t = tf; } else { t += dt; }
+        dt = critical_dt(nn, ne, p->X, p->conn, Lref, cel, uK, p->nthreads);
+        dt = dt * p->scale_factor;
+        if (dt < 1E-20) { rc = ORC_ERR_NEG_JACOBIAN; break; }
+        step++;
+        if (dt_hist && step <= max_hist) dt_hist[step - 1] = dt;
+        for (int64_t j = 0; j < ndof; j++)
+            if (!cons[j]) u[j] += dt * v[j] + 0.5 * dt * dt * a[j];
+        for (int64_t b = 0; b < p->nbc; b++) {
+            double Ud = 0, Vd = UU[b];
+            if (flag[b] == 1) { Ud = Vd; flag[b] = 0; }
+            else if (flag[b] == -1) { Ud = Vd * dt; }
+            else if (flag[b] == 2) {
+                double r = p->bcs[b].ramp_steps > 0 && step < p->bcs[b].ramp_steps
+                               ? (double)step / (double)p->bcs[b].ramp_steps : 1.0;
+                Ud = Vd * r * dt;
+            }
+            int64_t d = p->bcs[b].dof;
+            u[d] += Ud;
+            v[d] = Ud;
+            a[d] = 0.;
+        }
+        orc_internal_force(nn, ne, p->conn, dphi, wJ, p->elem_mat, p->mats, u, fint, 0, 0, p->nthreads);
+        for (int64_t j = 0; j < ndof; j++) {
+            if (cons[j]) continue;
+            double val = -fint[j] + 0.0;
+            double rhs = 0;
+            rhs += val;
+            a[j] = rhs / mass[j % nn];
+            v[j] += dt * ((1. - 0.5) * aprev[j] + 0.5 * a[j]);
+        }
+        memcpy(uK, u, sizeof(double) * (size_t)ndof);
+        if (!isfinite(uK[1])) { rc = ORC_ERR_NAN; break; }
+        memcpy(aprev, a, sizeof(double) * (size_t)ndof);
+    }
+    if (res) { res->steps = step; res->t = t; res->dt_last = dt; res->status = rc; }
+done:
+    free(dphi); free(wJ); free(Lref); free(cel); free(mass); free(fint);
+    free(uK); free(aprev); free(cons); free(flag); free(UU);
+    return rc;
+}
+
+/* Cube generator.  Node (i,j,k) has id i + (n+1) j + (n+1)^2 k at (i,j,k)/n;
+ * interior nodes move by jitter*h*(2r-1) per coordinate, r from splitmix64
+ * seeded with `seed`, drawn in node-id order.  Each hex (i fastest) is split
+ * into 6 tets as applications/tools/Hex2Tet-Parallel/Hex2Tet-Partitioning.py
+ * :87-110 does for C3D8 node order N1..N8. */
+static uint64_t splitmix64(uint64_t *s)
+{
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+int orc_cube_mesh(int32_t n, uint64_t seed, double jitter, double *X, int32_t *conn)
+{
+    if (n < 1) return ORC_ERR_ARG;
+    const int64_t m = n + 1, nn = m * m * m;
+    const double h = 1.0 / (double)n;
+    uint64_t s = seed;
+    for (int64_t k = 0; k < m; k++)
+        for (int64_t j = 0; j < m; j++)
+            for (int64_t i = 0; i < m; i++) {
+                int64_t id = i + m * j + m * m * k;
+                double c[3] = {(double)i / (double)n, (double)j / (double)n, (double)k / (double)n};
+                if (i > 0 && i < n && j > 0 && j < n && k > 0 && k < n)
+                    for (int d = 0; d < 3; d++) {
+                        double r = (double)(splitmix64(&s) >> 11) * 0x1.0p-53;
+                        c[d] += (2.0 * r - 1.0) * (jitter * h);
+                    }
+                for (int d = 0; d < 3; d++) X[d * nn + id] = c[d];
+            }
+    int64_t e = 0;
+    for (int64_t k = 0; k < n; k++)
+        for (int64_t j = 0; j < n; j++)
+            for (int64_t i = 0; i < n; i++) {
+                int32_t N[9];
+                N[1] = (int32_t)(i + m * j + m * m * k);
+                N[2] = N[1] + 1;
+                N[3] = N[1] + 1 + (int32_t)m;
+                N[4] = N[1] + (int32_t)m;
+                for (int q = 5; q <= 8; q++) N[q] = N[q - 4] + (int32_t)(m * m);
+                const int T[6][4] = {{1, 3, 4, 7}, {1, 2, 3, 7}, {4, 1, 7, 8},
+                                     {1, 5, 7, 8}, {1, 5, 6, 7}, {2, 1, 6, 7}};
+                for (int t = 0; t < 6; t++, e++)
+                    for (int q = 0; q < 4; q++) conn[e * 4 + q] = N[T[t][q]];
+            }
+    return ORC_OK;
+}

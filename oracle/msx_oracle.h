@@ -1,0 +1,80 @@
+/*
+ * msx_oracle.h -- CPU restatement of MuPhiSim v1.1's explicit C3D4 step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the CUDA path is checked
+ * against; nothing in the product links or calls it.  Only tests/, the smoke
+ * check and bench.py's CPU-baseline leg load it.
+ *
+ * Parity pin: the oracle is validated against the reference itself, built
+ * from its own sources behind a small PETSc/MPI shim (oracle/Makefile,
+ * oracle/ref_harness.cpp), on the golden decks in tests/golden/.
+ *
+ * Every routine follows the reference's arithmetic in the same operation
+ * order (compile with -ffp-contract=off), so on a host without implicit FMA
+ * contraction it reproduces the reference bit for bit.
+ */
+#ifndef MSX_ORACLE_H
+#define MSX_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Constitutive laws, named as in the reference's *HyperElastic keyword. */
+enum { ORC_NEO_HOOKEAN = 0,          /* "Neo-Hookean" (Belytschko form)      */
+       ORC_COMPRESSIBLE_NH = 1,      /* "3D-Compressible-Neo-Hookean"        */
+       ORC_STVK = 2 };               /* "St-Venant-Kirchhoff" (3D isotropic)  */
+
+/* Dirichlet modes: reference *BOUNDARY, TYPE=DISPLACEMENT RAMP / INST, plus
+ * the step-ramped velocity extension (no reference counterpart). */
+enum { ORC_BC_RAMP = 0, ORC_BC_INST = 1, ORC_BC_VEL_RAMP = 2 };
+
+typedef struct { int32_t law; double young, nu, rho; } orc_material;
+typedef struct { int64_t dof; int32_t mode; int32_t ramp_steps; double value; } orc_bc;
+
+typedef struct {
+    int64_t nn, ne;
+    const double *X;          /* 3*nn, X[c*nn + node]                        */
+    const int32_t *conn;      /* 4*ne, 0-based                               */
+    const int32_t *elem_mat;  /* ne material ids, or NULL (all 0)            */
+    const orc_material *mats; int32_t nmat;
+    const orc_bc *bcs; int64_t nbc;
+    double t0, tf, scale_factor;
+    int64_t max_steps;        /* 0: run to tf as the reference does          */
+    int32_t first_step_zero_uK; /* 1: the reference's chained-solver quirk   */
+    int32_t nthreads;
+} orc_problem;
+
+typedef struct { int64_t steps; double t, dt_last, dt_init; int32_t status; } orc_result;
+
+/* status codes */
+enum { ORC_OK = 0, ORC_ERR_NEG_JACOBIAN = 1, ORC_ERR_NAN = 2, ORC_ERR_ARG = 3 };
+
+/* Element set-up: dphi[12*ne] (node-major a*3+j), wJ[ne], Lref[ne]. */
+int orc_precompute(int64_t nn, int64_t ne, const double *X, const int32_t *conn,
+                   double *dphi, double *wJ, double *Lref);
+/* Lumped mass per node (identical for the three components). */
+int orc_lumped_mass(int64_t nn, int64_t ne, const int32_t *conn, const double *wJ,
+                    const int32_t *elem_mat, const orc_material *mats, double *mass);
+/* First Piola stress P(F), row-major 3x3. */
+void orc_stress(const orc_material *m, const double *F, double *P);
+/* Sound speed of a law. */
+double orc_sound_speed(const orc_material *m);
+/* Characteristic length (inscribed-sphere diameter) of one tet; x[a*3+c]. */
+double orc_char_length(const double *x);
+/* Internal force of displacement u: fint[3*nn] (reference scatter order). */
+int orc_internal_force(int64_t nn, int64_t ne, const int32_t *conn, const double *dphi,
+                       const double *wJ, const int32_t *elem_mat, const orc_material *mats,
+                       const double *u, double *fint, double *F_out, double *P_out, int nthreads);
+/* Full explicit solve; u,v,a (3*nn each) in = initial, out = final.
+ * dt_hist (optional) receives one dt per executed step (max_hist entries). */
+int orc_run(const orc_problem *p, double *u, double *v, double *a,
+            double *dt_hist, int64_t max_hist, orc_result *res);
+/* Seeded cube generator: (n+1)^3 nodes, 6 n^3 tets (hex -> 6 tets). */
+int orc_cube_mesh(int32_t n, uint64_t seed, double jitter, double *X, int32_t *conn);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

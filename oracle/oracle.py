@@ -1,0 +1,330 @@
+"""Python access to the oracle (TEST INFRASTRUCTURE ONLY).
+
+Two checkers live here:
+  * the C restatement of MuPhiSim v1.1's explicit C3D4 step (msx_oracle.c,
+    built into _build/liboracle.so), and
+  * the reference MuPhiSim itself, compiled in place from its own sources
+    behind our PETSc/MPI shim (_ref/muphisim_ref, see Makefile), driven through
+    Abaqus-style decks written by `write_deck`.
+
+Only tests/, the smoke check and bench.py's CPU-baseline leg use this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_BIN = os.path.join(HERE, "_ref", "muphisim_ref")
+
+NEO_HOOKEAN, COMPRESSIBLE_NH, STVK = 0, 1, 2
+LAW_NAMES = {NEO_HOOKEAN: "Neo-Hookean", COMPRESSIBLE_NH: "3D-Compressible-Neo-Hookean",
+             STVK: "St-Venant-Kirchhoff"}
+BC_RAMP, BC_INST, BC_VEL_RAMP = 0, 1, 2
+
+
+class _Mat(C.Structure):
+    _fields_ = [("law", C.c_int32), ("young", C.c_double), ("nu", C.c_double), ("rho", C.c_double)]
+
+
+class _BC(C.Structure):
+    _fields_ = [("dof", C.c_int64), ("mode", C.c_int32), ("ramp_steps", C.c_int32), ("value", C.c_double)]
+
+
+class _Problem(C.Structure):
+    _fields_ = [("nn", C.c_int64), ("ne", C.c_int64), ("X", C.c_void_p), ("conn", C.c_void_p),
+                ("elem_mat", C.c_void_p), ("mats", C.c_void_p), ("nmat", C.c_int32),
+                ("bcs", C.c_void_p), ("nbc", C.c_int64), ("t0", C.c_double), ("tf", C.c_double),
+                ("scale_factor", C.c_double), ("max_steps", C.c_int64),
+                ("first_step_zero_uK", C.c_int32), ("nthreads", C.c_int32)]
+
+
+class _Result(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("t", C.c_double), ("dt_last", C.c_double),
+                ("dt_init", C.c_double), ("status", C.c_int32)]
+
+
+_lib = None
+
+
+def build() -> str:
+    """Compile the C restatement (make lib)."""
+    subprocess.run(["make", "-s", "-C", HERE, "lib"], check=True)
+    return LIB_PATH
+
+
+def build_reference() -> str | None:
+    """Compile the reference behind the shim when its sources are mounted."""
+    src = os.environ.get("MSX_REFERENCE_SRC", "/root/reference/src")
+    if not os.path.isdir(src):
+        return None
+    subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF_SRC={src}"], check=True)
+    return REF_BIN
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = C.CDLL(LIB_PATH)
+        _lib.orc_run.argtypes = [C.POINTER(_Problem), C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_int64, C.POINTER(_Result)]
+        _lib.orc_cube_mesh.argtypes = [C.c_int32, C.c_uint64, C.c_double, C.c_void_p, C.c_void_p]
+        _lib.orc_precompute.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_lumped_mass.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_stress.argtypes = [C.POINTER(_Mat), C.c_void_p, C.c_void_p]
+        _lib.orc_sound_speed.argtypes = [C.POINTER(_Mat)]
+        _lib.orc_sound_speed.restype = C.c_double
+        _lib.orc_char_length.argtypes = [C.c_void_p]
+        _lib.orc_char_length.restype = C.c_double
+        _lib.orc_internal_force.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.c_int]
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+@dataclass
+class Material:
+    law: int = COMPRESSIBLE_NH
+    young: float = 1e6
+    nu: float = 0.3
+    rho: float = 1000.0
+
+
+@dataclass
+class Mesh:
+    X: np.ndarray          # (3, nn) float64
+    conn: np.ndarray       # (ne, 4) int32, 0-based
+    elem_mat: np.ndarray | None = None
+
+    @property
+    def nn(self):
+        return self.X.shape[1]
+
+    @property
+    def ne(self):
+        return self.conn.shape[0]
+
+
+@dataclass
+class Solver:
+    """One *SOLVER, EXPLICIT block."""
+    t0: float
+    tf: float
+    scale_factor: float
+    bcs: list = field(default_factory=list)   # (dof, mode, value, ramp_steps)
+    max_steps: int = 0
+
+
+def cube_mesh(n: int, seed: int = 1234, jitter: float = 0.1) -> Mesh:
+    nn, ne = (n + 1) ** 3, 6 * n ** 3
+    X = np.zeros((3, nn))
+    conn = np.zeros((ne, 4), np.int32)
+    rc = lib().orc_cube_mesh(n, seed, jitter, _p(X), _p(conn))
+    assert rc == 0
+    return Mesh(X, conn)
+
+
+def cube_bcs(n: int, top_value: float, mode: int = BC_RAMP, ramp_steps: int = 0):
+    """Bottom face z=0: all DOFs held at zero; top face z=1: z DOF driven.
+    The bottom uses the top's mode when that is INST, since the reference
+    reads one displacement *BOUNDARY block per solver."""
+    m = n + 1
+    nn = m ** 3
+    bcs = []
+    bottom = BC_INST if mode == BC_INST else BC_RAMP
+    for j in range(m):
+        for i in range(m):
+            node = i + m * j
+            for c in range(3):
+                bcs.append((node + c * nn, bottom, 0.0, 0))
+    for j in range(m):
+        for i in range(m):
+            node = i + m * j + m * m * n
+            bcs.append((node + 2 * nn, mode, top_value, ramp_steps))
+    return bcs
+
+
+def precompute(mesh: Mesh):
+    ne = mesh.ne
+    dphi = np.zeros((ne, 12))
+    wJ = np.zeros(ne)
+    Lref = np.zeros(ne)
+    X = np.ascontiguousarray(mesh.X)
+    conn = np.ascontiguousarray(mesh.conn)
+    rc = lib().orc_precompute(mesh.nn, ne, _p(X), _p(conn), _p(dphi), _p(wJ), _p(Lref))
+    assert rc == 0
+    return dphi, wJ, Lref
+
+
+def _mats_array(mats):
+    arr = (_Mat * len(mats))()
+    for k, m in enumerate(mats):
+        arr[k] = _Mat(m.law, m.young, m.nu, m.rho)
+    return arr
+
+
+def lumped_mass(mesh: Mesh, mats, wJ):
+    out = np.zeros(mesh.nn)
+    arr = _mats_array(mats)
+    em = None if mesh.elem_mat is None else np.ascontiguousarray(mesh.elem_mat, np.int32)
+    lib().orc_lumped_mass(mesh.nn, mesh.ne, _p(np.ascontiguousarray(mesh.conn)), _p(wJ), _p(em),
+                          C.cast(arr, C.c_void_p), _p(out))
+    return out
+
+
+def stress(mat: Material, F: np.ndarray) -> np.ndarray:
+    F = np.ascontiguousarray(F, dtype=np.float64).reshape(9)
+    P = np.zeros(9)
+    m = _Mat(mat.law, mat.young, mat.nu, mat.rho)
+    lib().orc_stress(C.byref(m), _p(F), _p(P))
+    return P.reshape(3, 3)
+
+
+def sound_speed(mat: Material) -> float:
+    m = _Mat(mat.law, mat.young, mat.nu, mat.rho)
+    return lib().orc_sound_speed(C.byref(m))
+
+
+def char_length(x: np.ndarray) -> float:
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(12)
+    return lib().orc_char_length(_p(x))
+
+
+def internal_force(mesh: Mesh, mats, u: np.ndarray, nthreads: int = 1):
+    dphi, wJ, _ = precompute(mesh)
+    nn, ne = mesh.nn, mesh.ne
+    f = np.zeros(3 * nn)
+    F = np.zeros((ne, 9))
+    P = np.zeros((ne, 9))
+    arr = _mats_array(mats)
+    em = None if mesh.elem_mat is None else np.ascontiguousarray(mesh.elem_mat, np.int32)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    lib().orc_internal_force(nn, ne, _p(np.ascontiguousarray(mesh.conn)), _p(dphi), _p(wJ), _p(em),
+                             C.cast(arr, C.c_void_p), _p(u), _p(f), _p(F), _p(P), nthreads)
+    return f, F, P
+
+
+@dataclass
+class RunResult:
+    u: np.ndarray
+    v: np.ndarray
+    a: np.ndarray
+    steps: int
+    t: float
+    dt_init: float
+    dt_last: float
+    status: int
+    dt_hist: np.ndarray
+
+
+def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int = 0) -> RunResult:
+    """Run a chain of explicit solver blocks as the reference's main does."""
+    nn = mesh.nn
+    if state is None:
+        u, v, a = np.zeros(3 * nn), np.zeros(3 * nn), np.zeros(3 * nn)
+    else:
+        u, v, a = (np.array(s, dtype=np.float64, copy=True) for s in state)
+    X = np.ascontiguousarray(mesh.X)
+    conn = np.ascontiguousarray(mesh.conn)
+    em = None if mesh.elem_mat is None else np.ascontiguousarray(mesh.elem_mat, np.int32)
+    marr = _mats_array(mats)
+    total = 0
+    res = _Result()
+    hist_all = []
+    for k, s in enumerate(solvers):
+        barr = (_BC * max(1, len(s.bcs)))()
+        for i, (dof, mode, value, ramp) in enumerate(s.bcs):
+            barr[i] = _BC(dof, mode, ramp, value)
+        prob = _Problem(nn, mesh.ne, _p(X), _p(conn), _p(em), C.cast(marr, C.c_void_p), len(mats),
+                        C.cast(barr, C.c_void_p), len(s.bcs), s.t0, s.tf, s.scale_factor, s.max_steps,
+                        0, nthreads)
+        hist = np.zeros(max(1, max_hist))
+        rc = lib().orc_run(C.byref(prob), _p(u), _p(v), _p(a), _p(hist), max_hist, C.byref(res))
+        total += res.steps
+        hist_all.append(hist[: min(res.steps, max_hist)])
+        if rc != 0:
+            break
+    return RunResult(u, v, a, total, res.t, res.dt_init, res.dt_last, res.status,
+                     np.concatenate(hist_all) if hist_all else np.zeros(0))
+
+
+# ---------------------------------------------------------------- the reference
+def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None):
+    """Abaqus-style deck in the keyword subset the reference parses
+    (src/IO/inputFile.cpp: nodes :20-108, C3D4 elements :118-323, materials
+    :838-1029, solver blocks :2253-2831, displacement BCs :2960-3218)."""
+    X, conn = mesh.X, mesh.conn
+    lines = ["*Node"]
+    for i in range(mesh.nn):
+        lines.append("%d, %.17g, %.17g, %.17g" % (i + 1, X[0, i], X[1, i], X[2, i]))
+    lines.append("*Element, type=C3D4")
+    for e in range(mesh.ne):
+        c = conn[e] + 1
+        lines.append("%d, %d, %d, %d, %d" % (e + 1, c[0], c[1], c[2], c[3]))
+    lines += ["*FEM Nodes", "All", "*FEM Elements", "All"]
+    nn = mesh.nn
+    for s in solvers:
+        if any(b[1] == BC_VEL_RAMP for b in s.bcs):
+            raise ValueError("the reference has no velocity-ramp boundary condition")
+        modes = {b[1] for b in s.bcs}
+        if len(modes) > 1:
+            raise ValueError("one *BOUNDARY block per solver: a single mode only")
+        mode = modes.pop() if modes else BC_RAMP
+        lines += ["*SOLVER, EXPLICIT", "*Scale Factor", "%.17g" % s.scale_factor,
+                  "*Outputs", "1", "*Time", "%.17g, %.17g" % (s.t0, s.tf),
+                  "*BOUNDARY, TYPE=DISPLACEMENT " + ("INST" if mode == BC_INST else "RAMP")]
+        for dof, _, value, _ in s.bcs:
+            lines.append("%d,%d,%.17g" % (dof % nn + 1, dof // nn, value))
+        lines.append("*END SOLVER")
+    if mat_elems is None:
+        mat_elems = [None] * len(mats)
+    for k, m in enumerate(mats):
+        lines += ["*MATERIAL, name=Region%d" % (k + 1), "*Density", "%.17g" % m.rho,
+                  "*HyperElastic, " + LAW_NAMES[m.law], "%.17g, %.17g" % (m.young, m.nu)]
+        if mat_elems[k] is None:
+            lines += ["*List of Elements", "All"]
+        else:
+            # the reader takes one element per *List of Elements keyword
+            # (src/IO/inputFile.cpp:2010-2053)
+            for e in mat_elems[k]:
+                lines += ["*List of Elements", str(int(e) + 1)]
+    lines.append("*END")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def run_reference(mesh: Mesh, mats, solvers, workdir: str | None = None, timeout: float = 3600):
+    """Run the shim-built reference on a deck; returns (u, v, a, solve_wall_s)."""
+    if not os.path.exists(REF_BIN):
+        raise FileNotFoundError("reference binary not built: make -C oracle ref")
+    own = workdir is None
+    wd = tempfile.mkdtemp(prefix="msxref_") if own else workdir
+    os.makedirs(os.path.join(wd, "out"), exist_ok=True)
+    mat_elems = None
+    if mesh.elem_mat is not None:
+        mat_elems = [np.nonzero(mesh.elem_mat == k)[0] for k in range(len(mats))]
+    write_deck(os.path.join(wd, "deck.inp"), mesh, mats, solvers, mat_elems)
+    dump, timing = os.path.join(wd, "final.bin"), os.path.join(wd, "timing.txt")
+    r = subprocess.run([REF_BIN, "-input", "deck.inp", "-inputDir", ".", "-outputDir", "out",
+                        "-dump", dump, "-timing", timing], cwd=wd, capture_output=True, text=True,
+                       timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError("reference failed (%d): %s" % (r.returncode, (r.stderr or r.stdout)[-2000:]))
+    data = np.fromfile(dump, dtype=np.float64)
+    n = 3 * mesh.nn
+    wall = float(open(timing).read())
+    return data[:n], data[n:2 * n], data[2 * n:3 * n], wall, r.stdout

@@ -1,0 +1,2 @@
+/* shim: see petsc_shim.h */
+#include "petsc_shim.h"

@@ -1,0 +1,91 @@
+"""Generate the golden fixtures in this folder from the reference MuPhiSim.
+
+Run in a container where the reference sources are mounted:
+    python tests/golden/make_golden.py
+It compiles the reference in place behind our PETSc/MPI shim (oracle/Makefile),
+runs each case below through the reference's own input-deck reader and
+explicit solver, and stores the inputs and the reference's final u, v, a
+(float64, exact bits) as <case>.npz.  The GPU tests and the oracle tests
+compare against these files; nothing here is needed at test time.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
+import oracle as O  # noqa: E402
+
+
+def tet12_mesh(ref_src):
+    """Nodes and C3D4 connectivity of applications/examples/3Dcube.inp."""
+    path = os.path.join(ref_src, "..", "applications", "examples", "3Dcube.inp")
+    nodes, elems, mode = [], [], None
+    for line in open(path):
+        s = line.strip()
+        if s.startswith("*"):
+            mode = "n" if s.startswith("*Node") else ("e" if s.startswith("*Element") else None)
+            continue
+        if mode == "n":
+            nodes.append([float(x) for x in s.split(",")[1:]])
+        elif mode == "e":
+            elems.append([int(x) - 1 for x in s.split(",")[1:]])
+    X = np.ascontiguousarray(np.array(nodes).T)
+    return O.Mesh(X, np.array(elems, np.int32))
+
+
+def cases(ref_src):
+    cnh, nh, stvk = O.COMPRESSIBLE_NH, O.NEO_HOOKEAN, O.STVK
+    out = {}
+    m3 = O.cube_mesh(3)
+    out["cube3_cnh_ramp"] = (m3, [O.Material(cnh)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.002))])
+    m4 = O.cube_mesh(4)
+    out["cube4_nh_ramp"] = (m4, [O.Material(nh)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(4, 0.002))])
+    out["cube4_stvk_ramp"] = (m4, [O.Material(stvk)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(4, 0.002))])
+    out["cube3_cnh_inst"] = (m3, [O.Material(cnh)],
+                             [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.001, O.BC_INST))])
+    out["cube3_cnh_chain"] = (m3, [O.Material(cnh)],
+                              [O.Solver(0.0, 0.01, 0.5, O.cube_bcs(3, 0.001)),
+                               O.Solver(0.01, 0.02, 0.4, O.cube_bcs(3, 0.003))])
+    m2 = O.cube_mesh(2)
+    m2.elem_mat = (np.arange(m2.ne) % 2).astype(np.int32)
+    out["cube2_two_materials"] = (m2, [O.Material(nh, 1e6, 0.3, 1000.0), O.Material(stvk, 3e6, 0.25, 2000.0)],
+                                  [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(2, 0.002))])
+    t12 = tet12_mesh(ref_src)
+    nn = t12.nn
+    bcs = [(node + c * nn, O.BC_RAMP, (-0.5 if (node, c) == (3, 1) else 0.0), 0)
+           for node in (0, 3, 6, 7) for c in range(3)]
+    out["tet12_stvk"] = (t12, [O.Material(stvk, 1e9, 0.3, 1000.0)], [O.Solver(0.0, 0.05, 0.1, bcs)])
+    m10 = O.cube_mesh(10)
+    for name, law in (("cnh", cnh), ("nh", nh), ("stvk", stvk)):
+        out["cube10_%s_S" % name] = (m10, [O.Material(law)], [O.Solver(0.0, 0.5, 0.5, O.cube_bcs(10, 0.05))])
+    return out
+
+
+def pack(mesh, mats, solvers, ref, orc):
+    d = {"X": mesh.X, "conn": mesh.conn,
+         "mats": np.array([[m.law, m.young, m.nu, m.rho] for m in mats]),
+         "solvers": np.array([[s.t0, s.tf, s.scale_factor, len(s.bcs)] for s in solvers]),
+         "bcs": np.array([[b[0], b[1], b[2], b[3]] for s in solvers for b in s.bcs], dtype=np.float64),
+         "u": ref[0], "v": ref[1], "a": ref[2], "steps": np.array(orc.steps)}
+    if mesh.elem_mat is not None:
+        d["elem_mat"] = mesh.elem_mat
+    return d
+
+
+def main():
+    ref_src = os.environ.get("MSX_REFERENCE_SRC", "/root/reference/src")
+    O.build()
+    if O.build_reference() is None:
+        raise SystemExit("reference sources not found at " + ref_src)
+    for name, (mesh, mats, solvers) in cases(ref_src).items():
+        ref = O.run_reference(mesh, mats, solvers)
+        orc = O.run(mesh, mats, solvers)
+        same = all(np.array_equal(x, y) for x, y in zip((orc.u, orc.v, orc.a), ref[:3]))
+        print("%-22s steps %5d  oracle==reference bitwise: %s  ref solve %.2fs" % (name, orc.steps, same, ref[3]))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **pack(mesh, mats, solvers, ref, orc))
+
+
+if __name__ == "__main__":
+    main()

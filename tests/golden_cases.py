@@ -1,0 +1,27 @@
+"""Loader for the golden fixtures made by tests/golden/make_golden.py."""
+import glob
+import os
+
+import numpy as np
+
+import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load(name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    mesh = O.Mesh(d["X"], d["conn"].astype(np.int32),
+                  d["elem_mat"].astype(np.int32) if "elem_mat" in d else None)
+    mats = [O.Material(int(m[0]), float(m[1]), float(m[2]), float(m[3])) for m in d["mats"]]
+    solvers, k = [], 0
+    for t0, tf, sf, nb in d["solvers"]:
+        nb = int(nb)
+        bcs = [(int(b[0]), int(b[1]), float(b[2]), int(b[3])) for b in d["bcs"][k:k + nb]]
+        k += nb
+        solvers.append(O.Solver(float(t0), float(tf), float(sf), bcs))
+    return mesh, mats, solvers, (d["u"], d["v"], d["a"]), int(d["steps"])

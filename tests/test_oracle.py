@@ -1,0 +1,75 @@
+"""The oracle against the reference's own outputs (golden fixtures) and
+against invariants of the element formulation.  CPU only."""
+import numpy as np
+import pytest
+
+import oracle as O
+from golden_cases import load, names
+
+
+@pytest.mark.parametrize("name", names())
+def test_oracle_matches_reference_bitwise(name):
+    mesh, mats, solvers, (u, v, a), steps = load(name)
+    r = O.run(mesh, mats, solvers, nthreads=2)
+    assert r.status == 0 and r.steps == steps
+    # the oracle keeps the reference's operation order: identical bits
+    assert np.array_equal(r.u, u)
+    assert np.array_equal(r.v, v)
+    assert np.array_equal(r.a, a)
+
+
+def test_cube_generator_counts_and_volume():
+    n = 5
+    m = O.cube_mesh(n)
+    assert m.nn == (n + 1) ** 3 and m.ne == 6 * n ** 3
+    dphi, wJ, L = O.precompute(m)
+    # wJ = 0.166666666667*|detJ| = (1+3e-13)*V: the tets tile the unit cube
+    assert abs(wJ.sum() - 1.0) < 1e-9
+    assert (L > 0).all()
+
+
+@pytest.mark.parametrize("law", [O.NEO_HOOKEAN, O.COMPRESSIBLE_NH, O.STVK])
+def test_stress_zero_at_identity_and_rotation(law):
+    mat = O.Material(law)
+    assert np.abs(O.stress(mat, np.eye(3))).max() < 1e-9
+    th = 0.3
+    R = np.array([[np.cos(th), -np.sin(th), 0], [np.sin(th), np.cos(th), 0], [0, 0, 1]])
+    assert np.abs(O.stress(mat, R)).max() < 1e-6 * mat.young
+
+
+@pytest.mark.parametrize("law", [O.COMPRESSIBLE_NH, O.STVK])
+def test_stress_is_energy_gradient(law):
+    """P = dW/dF for the laws whose energy the reference defines
+    (hyperElasticNeoHookean.cpp:291-304, hyperElasticStVenantKirchhoff.cpp:251-274)."""
+    mat = O.Material(law, 1e6, 0.3, 1000.0)
+    lam = mat.young * mat.nu / ((1 + mat.nu) * (1 - 2 * mat.nu))
+    mu = 0.5 * mat.young / (1 + mat.nu)
+
+    def W(F):
+        if law == O.COMPRESSIBLE_NH:
+            J = np.linalg.det(F)
+            return 0.5 * lam * np.log(J) ** 2 - mu * np.log(J) + 0.5 * mu * np.trace(F.T @ F)
+        E = 0.5 * (F.T @ F - np.eye(3))
+        return 0.5 * np.sum((2 * mu * E + lam * np.trace(E) * np.eye(3)) * E)
+
+    rng = np.random.default_rng(3)
+    F = np.eye(3) + 0.05 * rng.standard_normal((3, 3))
+    P = O.stress(mat, F)
+    h = 1e-6
+    G = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(3):
+            Fp, Fm = F.copy(), F.copy()
+            Fp[i, j] += h
+            Fm[i, j] -= h
+            G[i, j] = (W(Fp) - W(Fm)) / (2 * h)
+    assert np.abs(G - P).max() < 1e-5 * np.abs(P).max()
+
+
+def test_rigid_translation_gives_zero_force():
+    m = O.cube_mesh(3)
+    u = np.zeros(3 * m.nn)
+    u[: m.nn] = 0.3
+    u[2 * m.nn:] = -0.1
+    f, F, P = O.internal_force(m, [O.Material(O.COMPRESSIBLE_NH)], u)
+    assert np.abs(f).max() < 1e-9
