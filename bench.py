@@ -1,0 +1,293 @@
+"""Benchmark of the explicit C3D4 step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the large plain-FP64 configuration): unit cube meshed as 100^3 hexes,
+each split into 6 tets -> 6,000,000 C3D4 elements and 1,030,301 nodes; interior
+nodes jittered by a seeded +-0.1 h; 3D-Compressible-Neo-Hookean E=1e6 Pa,
+nu=0.3, rho=1000; bottom face fixed; top face z velocity ramped linearly to
+0.1 m/s over 200 steps; dt = 0.5 x CFL recomputed every step.  One "step" is
+one explicit time step over the whole mesh.  Synthetic, seeded data.
+
+Prints one JSON line: value = element-steps/s of the plain FP64 path with the
+mesh resident in HBM (device time of K steps), e2e = the same through the C ABI
+from host buffers (mesh upload, set-up, K steps and the read-back of u, v, a),
+plus the mixed-precision and reference-order variants, the element kernel's
+roofline and the CPU baseline.  --impl reference times the CPU implementation
+of the path (the oracle's C restatement on all host cores) on a bounded sample.
+Under torchrun each rank runs an independent replica ("replicas only").
+"""
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "v.1.1_gb300"))
+
+N_CUBE = 100
+RAMP_STEPS = 200
+V_TOP = 0.1
+SEED = 1234
+MATERIAL = (1, 1e6, 0.3, 1000.0)   # 3D-Compressible-Neo-Hookean
+METRIC = "element-steps/s on 1 GB300 (plain FP64 vs mixed/batched); p50/p99 solve latency"
+WORKLOAD = ("cube 100^3 hexes -> 6,000,000 C3D4 tets / 1,030,301 nodes, +-0.1h seeded jitter, "
+            "3D-Compressible-Neo-Hookean E=1e6 nu=0.3 rho=1000, bottom fixed, top z-velocity ramped "
+            "to 0.1 m/s over 200 steps, dt=0.5 CFL per step")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per element of the element kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "element_kernel_fp64_cube.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_element:"):
+                return float(line.split(":")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi samples during a timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = [r for r in csv.reader(io.StringIO(self.out or "")) if len(r) >= 9]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = max(float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def make_case(n):
+    import msx
+    X, conn = msx.mesh_cube(n, SEED, 0.1)
+    bcs = msx.cube_bcs(n, V_TOP, msx.BC_VEL_RAMP, RAMP_STEPS)
+    return X, conn, bcs
+
+
+def run_variant(X, conn, bcs, precision, steps, warmup, device):
+    """Create, warm up, then time exactly `steps` steps with the mesh resident."""
+    import msx
+    S = msx.Solver(X, conn, [MATERIAL], bcs, 0.0, 1e30, 0.5, max_steps=0, precision=precision)
+    S.run(warmup)
+    with Clocks(device) as ck:
+        rep = S.run(steps)
+    assert rep.steps == steps, rep
+    prof = S.profile(6)
+    S.close()
+    return rep, prof, ck.summary()
+
+
+def run_e2e(X, conn, bcs, steps):
+    """Whole job through the C ABI from host buffers: upload, set-up, K steps,
+    read back u, v, a.  Inputs come from pinned host memory."""
+    import msx
+    t0 = time.perf_counter()
+    S = msx.Solver(X, conn, [MATERIAL], bcs, 0.0, 1e30, 0.5, max_steps=0, precision=msx.FP64)
+    rep = S.run(steps)
+    u, v, a = S.state()
+    wall = time.perf_counter() - t0
+    S.close()
+    h2d = X.nbytes + conn.nbytes + len(bcs) * 24
+    d2h = u.nbytes + v.nbytes + a.nbytes
+    return wall, rep, h2d, d2h
+
+
+def cpu_baseline(X, conn, bcs, target_s=10.0):
+    """The oracle's C restatement (OpenMP, all host cores) on a bounded number
+    of steps of the same mesh."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    mesh = O.Mesh(X, conn)
+    cores = os.cpu_count() or 1
+    mat = [O.Material(*MATERIAL)]
+    probe = O.run(mesh, mat, [O.Solver(0.0, 1e30, 0.5, bcs, max_steps=1)], nthreads=cores)
+    per_step = max(probe.loop_seconds, 1e-3)
+    nsteps = int(max(2, min(200, target_s / per_step)))
+    r = O.run(mesh, mat, [O.Solver(0.0, 1e30, 0.5, bcs, max_steps=nsteps)], nthreads=cores)
+    value = mesh.ne * r.steps / r.loop_seconds
+    return {"value": value, "unit": "element-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d steps of the 6M-tet FP64 workload, oracle C restatement (OpenMP, %d threads), "
+                      "set-up excluded; %.2f s" % (r.steps, cores, r.loop_seconds)}
+
+
+def reference_arm(args):
+    """The CPU implementation of the path (the oracle's C restatement of the
+    reference, OpenMP over all host cores) on the same workload: W warm-up
+    steps, then up to K timed steps bounded to about a minute."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    mesh = O.cube_mesh(N_CUBE, SEED, 0.1)
+    bcs = O.cube_bcs(N_CUBE, V_TOP, O.BC_VEL_RAMP, RAMP_STEPS)
+    cores = os.cpu_count() or 1
+    mat = [O.Material(*MATERIAL)]
+    w = O.run(mesh, mat, [O.Solver(0.0, 1e30, 0.5, bcs, max_steps=min(args.warmup, 3))], nthreads=cores)
+    per_step = max(w.loop_seconds / max(w.steps, 1), 1e-3)
+    k = int(max(1, min(args.steps, 60.0 / per_step)))
+    r = O.run(mesh, mat, [O.Solver(0.0, 1e30, 0.5, bcs, max_steps=k)], nthreads=cores)
+    value = mesh.ne * r.steps / r.loop_seconds
+    sample = ("%d of %d steps of the 6M-tet FP64 workload (bounded to ~60 s), oracle C restatement of the "
+              "reference path, OpenMP %d threads, set-up excluded" % (r.steps, args.steps, cores))
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "element-steps/s", "n_gpus": 0,
+            "steps": r.steps, "warmup": w.steps, "ms_per_step": 1e3 * r.loop_seconds / r.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "num_elems": mesh.ne, "num_nodes": mesh.nn,
+                                            "precision": "FP64"},
+            "cpu_baseline": {"value": value, "unit": "element-steps/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "element-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def reduce_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--cube", type=int, default=N_CUBE, help="hexes per cube edge (profiling runs only)")
+    ap.add_argument("--only", choices=["fp64", "mixed", "fp64_exact"], default=None,
+                    help="time a single variant (profiling runs only)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(reference_arm(args)))
+        return
+    import msx
+
+    msx.load()
+    msx.set_device(local)
+    X, conn, bcs = make_case(args.cube)
+    ne, nn = conn.shape[0], X.shape[1]
+
+    barrier(ws)
+    first = {"mixed": msx.MIXED, "fp64_exact": msx.FP64_EXACT}.get(args.only, msx.FP64)
+    rep, prof, clocks = run_variant(X, conn, bcs, first, args.steps, args.warmup, local)
+    secs = reduce_max(rep.device_ms / 1e3, ws)
+    value = ws * ne * args.steps / secs
+
+    variants = {}
+    if not args.no_variants and args.only is None:
+        for name, prec in (("mixed", msx.MIXED), ("fp64_exact", msx.FP64_EXACT)):
+            r2, p2, c2 = run_variant(X, conn, bcs, prec, args.steps, args.warmup, local)
+            s2 = reduce_max(r2.device_ms / 1e3, ws)
+            variants[name] = {"value": ws * ne * args.steps / s2, "ms_per_step": 1e3 * s2 / args.steps,
+                              "element_kernel_ms": p2.element_ms, "node_kernel_ms": p2.node_ms,
+                              "clocks": c2}
+    e2e = None
+    if not args.no_e2e and args.only is None:
+        wall, r3, h2d, d2h = run_e2e(X, conn, bcs, args.steps)
+        wall = reduce_max(wall, ws)
+        e2e = {"value": ws * ne * args.steps / wall, "unit": "element-steps/s",
+               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+               "h2d_bytes_total": h2d, "d2h_bytes_total": d2h, "wall_s": wall,
+               "note": "msx_create (mesh upload + set-up) + msx_run(K) + msx_get_state, host buffers"}
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    alg_elem = 128.0 * ne + 48.0 * nn     # element data + gathered X and u per node
+    achieved = alg_elem / (prof.element_ms * 1e-3) / 1e9
+    tr = profiled_traffic()
+    roofline = {"bound": "hbm", "kernel": "elem_kernel_fp64", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": tr * ne if tr else None,
+                "alg_bytes_per_launch": alg_elem, "element_kernel_ms": prof.element_ms,
+                "node_kernel_ms": prof.node_ms,
+                "note": "FP64-pipe bound on GB300 (~0.5 T DP-op/s); HBM fraction reported as asked"}
+    line = {"metric": METRIC, "value": value, "unit": "element-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "num_elems": ne, "num_nodes": nn, "precision": "FP64",
+                       "parallelism": "replicas" if ws > 1 else "single", "l2": "inputs larger than L2 "
+                       "(element arrays %.2f GB resident)" % (ne * 128 / 1e9)},
+            "roofline": roofline, "gpu_launches": rep.kernel_launches, "clocks": clocks, "e2e": e2e,
+            "variants": variants}
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(X, conn, bcs)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,160 @@
+/*
+ * msx.h -- C ABI of the GB300-native explicit solid-mechanics step.
+ *
+ * Drop-in for MuPhiSim v1.1's explicit solver path: C3D4 linear tets with one
+ * Gauss point, "Neo-Hookean", "3D-Compressible-Neo-Hookean" and
+ * "St-Venant-Kirchhoff" laws, lumped mass, central differences, Dirichlet
+ * ramp/instantaneous BCs and the CFL stable time step.
+ *
+ * Conventions (as in the reference):
+ *   - nodal fields are SoA float64, entry [dof] with dof = node + comp*num_nodes
+ *     (src/spatialDiscretisation/classGPs.cpp:37-67 getLocalDofs);
+ *   - connectivity is 0-based int32, 4 nodes per element;
+ *   - a solver block runs from t0 to tf with dt = scale_factor * CFL dt
+ *     recomputed every step (src/solvers/solverExplicit.cpp:217-276).
+ * All functions return an msx_status; none exits the process.  The library
+ * owns device memory; the caller owns host buffers.  A handle is used by one
+ * host thread at a time; the pool API is thread-safe.
+ */
+#ifndef MSX_H
+#define MSX_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MSX_OK = 0,
+    MSX_ERR_ARG = 1,           /* invalid argument (sizes, ids, pointers)            */
+    MSX_ERR_CUDA = 2,          /* CUDA runtime failure; see msx_last_error()          */
+    MSX_ERR_NEG_JACOBIAN = 3,  /* dt < 1e-20 ("Negative jacobian", solverExplicit.cpp:270-273) */
+    MSX_ERR_NAN = 4,           /* non-finite displacement (solverExplicit.cpp:306-308) */
+    MSX_ERR_OOM = 5,           /* device memory exhausted / admission refused         */
+    MSX_ERR_STATE = 6,         /* call not valid in the handle's current state        */
+    MSX_ERR_NO_DEVICE = 7,     /* no CUDA device or not an sm_103 device              */
+    MSX_ERR_TIMEOUT = 8,       /* a bounded device-side wait ran out                  */
+    MSX_ERR_BUSY = 9           /* pool full: try again after a poll                   */
+} msx_status;
+
+enum { MSX_LAW_NEO_HOOKEAN = 0,             /* *HyperElastic, Neo-Hookean                 */
+       MSX_LAW_COMPRESSIBLE_NEO_HOOKEAN = 1, /* *HyperElastic, 3D-Compressible-Neo-Hookean */
+       MSX_LAW_STVK = 2 };                   /* *HyperElastic, St-Venant-Kirchhoff          */
+
+enum { MSX_BC_RAMP = 0,      /* *BOUNDARY, TYPE=DISPLACEMENT RAMP: value reached at tf         */
+       MSX_BC_INST = 1,      /* *BOUNDARY, TYPE=DISPLACEMENT INST: value applied at first step */
+       MSX_BC_VEL_RAMP = 2 };/* extension: velocity ramped linearly to `value` over ramp_steps */
+
+enum { MSX_PREC_FP64 = 0,        /* plain FP64, FMA-contracted, algebraically simplified laws */
+       MSX_PREC_FP64_EXACT = 1,  /* FP64 in the reference's operation order, no contraction   */
+       MSX_PREC_MIXED = 2 };     /* FP32 element kinematics/stress/B^T P; FP64 nodes, J-1, dt  */
+
+typedef struct {
+    int64_t num_nodes, num_elems;
+    const double *X;              /* 3*num_nodes coordinates, X[c*num_nodes + node]        */
+    const int32_t *conn;          /* 4*num_elems node ids                                  */
+    const int32_t *elem_material; /* num_elems material ids, or NULL for material 0       */
+} msx_mesh;
+
+typedef struct {
+    int32_t law;
+    int32_t reserved;
+    double young, nu, rho;        /* *HyperElastic "E, nu" and *Density                   */
+} msx_material;
+
+typedef struct {
+    int64_t dof;                  /* node + comp*num_nodes (deck line "node, comp, value") */
+    int32_t mode;                 /* MSX_BC_*                                              */
+    int32_t ramp_steps;           /* MSX_BC_VEL_RAMP only                                  */
+    double value;
+} msx_bc;
+
+typedef struct {
+    double t0, tf, scale_factor;  /* *Time t0, tf and *Scale Factor                        */
+    int64_t max_steps;            /* 0: run to tf like the reference; >0: stop after N     */
+    int32_t precision;            /* MSX_PREC_*                                            */
+    int32_t steps_per_graph;      /* steps per captured CUDA graph; 0 = default (64)       */
+} msx_solver_opts;
+
+typedef struct {
+    int64_t steps;                /* steps executed by this call                           */
+    int64_t total_steps;          /* steps executed in this solver block so far            */
+    double t, dt, dt_init;        /* time reached, last dt, initial dt of the block        */
+    int32_t status;               /* msx_status of the run                                 */
+    int32_t reserved;
+    double device_ms;             /* device time of the call (CUDA events)                 */
+    int64_t kernel_launches;      /* step kernels launched by the call (incl. no-op tail)   */
+} msx_run_report;
+
+typedef struct {
+    double element_ms, node_ms;   /* mean duration of one element / node kernel launch     */
+    int64_t element_launches, node_launches;
+    double element_alg_bytes, node_alg_bytes; /* algorithmic bytes per launch              */
+} msx_profile_report;
+
+typedef struct msx_handle msx_handle;
+
+/* Mesh, materials, BCs and the first solver block: uploads the mesh, builds
+ * the per-element shape-function gradients, wJ, reference characteristic
+ * lengths, lumped mass and node->corner CSR on the device.
+ * Replaces the set-up of classSolverExplicit::calculate
+ * (src/solvers/solverExplicit.cpp:63-215) fed by the input deck readers
+ * (src/IO/inputFile.cpp:20-323, 838-1029, 2253-2831, 2960-3218). */
+msx_status msx_create(const msx_mesh *mesh, const msx_material *mats, int32_t num_mats,
+                      const msx_bc *bcs, int64_t num_bcs, const msx_solver_opts *opts,
+                      msx_handle **out);
+
+/* Advance the current solver block to tf (or opts.max_steps, or the extra
+ * cap max_steps > 0 of this call).  Replaces the time loop of
+ * classSolverExplicit::calculate (src/solvers/solverExplicit.cpp:217-338). */
+msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *report);
+
+/* Final nodal fields, host buffers of 3*num_nodes doubles each (any may be
+ * NULL).  Replaces solvers::getFinalValues (src/solvers/solvers.h:171-187). */
+msx_status msx_get_state(msx_handle *h, double *u, double *v, double *a);
+
+/* Initial nodal fields.  Replaces solvers::initValues (src/solvers/solvers.h:171-187). */
+msx_status msx_set_state(msx_handle *h, const double *u, const double *v, const double *a);
+
+/* Start the next *SOLVER, EXPLICIT block with the current state, as the
+ * reference's solver chain does (src/main.cpp:162-181). */
+msx_status msx_next_solver(msx_handle *h, const msx_bc *bcs, int64_t num_bcs,
+                           const msx_solver_opts *opts);
+
+msx_status msx_destroy(msx_handle *h);
+
+/* Message of the last failing call on this host thread. */
+const char *msx_last_error(void);
+
+/* Internal force f_int(u) for host u (3*num_nodes), host fint out: one element
+ * pass plus the CSR gather (classSolverExplicit::computeInternalForce,
+ * src/solvers/solverExplicit.cpp:363-379).  Leaves the solver state untouched. */
+msx_status msx_internal_force(msx_handle *h, const double *u, double *fint);
+
+/* Per-element set-up data and per-node lumped mass: G[9*num_elems] (rows of
+ * the inverse reference Jacobian = dphi of local nodes 1..3), wJ, Lref
+ * [num_elems], mass[num_nodes] (classLinearTetrahedra.cpp:129-268,
+ * solverExplicit.cpp:429-459).  Any pointer may be NULL. */
+msx_status msx_get_element_data(msx_handle *h, double *G, double *wJ, double *Lref, double *mass);
+
+/* Run `steps` steps launching each kernel separately with CUDA events around
+ * it on the library's stream, and report the mean kernel durations. */
+msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_report *report);
+
+/* Seeded unit-cube mesh: (n+1)^3 nodes, 6 n^3 tets (each hex split into six
+ * around its N1-N7 diagonal as applications/tools/Hex2Tet-Parallel/
+ * Hex2Tet-Partitioning.py:87-110 does), interior nodes jittered by
+ * jitter*h*(2r-1), r from splitmix64(seed) in node order. */
+msx_status msx_mesh_cube(int32_t n, uint64_t seed, double jitter, double *X, int32_t *conn);
+
+/* The library's CUDA stream (cudaStream_t) for callers that time it. */
+void *msx_stream(msx_handle *h);
+
+/* Select the CUDA device used by later msx_create calls on this host thread
+ * (one process per GPU: pass the local rank). */
+msx_status msx_set_device(int32_t device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

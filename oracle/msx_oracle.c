@@ -90,11 +90,15 @@ int orc_precompute(int64_t nn, int64_t ne, const double *X, const int32_t *conn,
     static const double natDev[12] = {-1.0, -1.0, -1.0, 1.0, 0.0, 0.0,
                                       0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
     const double w = 0.166666666667;
+    int bad = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(| : bad)
+#endif
     for (int64_t e = 0; e < ne; e++) {
         double xyz[12], pts[12], Jac[9], invJ[9];
         for (int k = 0; k < 4; k++) {
             int64_t nd = conn[e * 4 + k];
-            if (nd < 0 || nd >= nn) return ORC_ERR_ARG;
+            if (nd < 0 || nd >= nn) { bad = 1; nd = 0; }
             for (int i = 0; i < 3; i++) {
                 xyz[i * 4 + k] = X[i * nn + nd];
                 pts[k * 3 + i] = X[i * nn + nd];
@@ -117,7 +121,7 @@ int orc_precompute(int64_t nn, int64_t ne, const double *X, const int32_t *conn,
         wJ[e] = w * fabs(J);
         Lref[e] = orc_char_length(pts);
     }
-    return ORC_OK;
+    return bad ? ORC_ERR_ARG : ORC_OK;
 }
 
 /* constitutiveAlgorithms.cpp:135-206 getLumpedMassVector (generic branch),
@@ -351,6 +355,9 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
     if (t < 1E-12 && !p->first_step_zero_uK) memcpy(uK, u, sizeof(double) * (size_t)ndof);
     else memset(uK, 0, sizeof(double) * (size_t)ndof);
     int64_t step = 0;
+#ifdef _OPENMP
+    double wall0 = omp_get_wtime();
+#endif
     while (t < tf - 1E-12) {
         if (p->max_steps > 0 && step >= p->max_steps) break;
         if (t + dt > tf) { dt = tf - t; t = tf; } else { t += dt; }
@@ -359,6 +366,9 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
         if (dt < 1E-20) { rc = ORC_ERR_NEG_JACOBIAN; break; }
         step++;
         if (dt_hist && step <= max_hist) dt_hist[step - 1] = dt;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(p->nthreads > 0 ? p->nthreads : 1)
+#endif
         for (int64_t j = 0; j < ndof; j++)
             if (!cons[j]) u[j] += dt * v[j] + 0.5 * dt * dt * a[j];
         for (int64_t b = 0; b < p->nbc; b++) {
@@ -376,6 +386,9 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
             a[d] = 0.;
         }
         orc_internal_force(nn, ne, p->conn, dphi, wJ, p->elem_mat, p->mats, u, fint, 0, 0, p->nthreads);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(p->nthreads > 0 ? p->nthreads : 1)
+#endif
         for (int64_t j = 0; j < ndof; j++) {
             if (cons[j]) continue;
             double val = -fint[j] + 0.0;
@@ -388,7 +401,14 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
         if (!isfinite(uK[1])) { rc = ORC_ERR_NAN; break; }
         memcpy(aprev, a, sizeof(double) * (size_t)ndof);
     }
-    if (res) { res->steps = step; res->t = t; res->dt_last = dt; res->status = rc; }
+    if (res) {
+        res->steps = step; res->t = t; res->dt_last = dt; res->status = rc;
+#ifdef _OPENMP
+        res->loop_seconds = omp_get_wtime() - wall0;
+#else
+        res->loop_seconds = 0;
+#endif
+    }
 done:
     free(dphi); free(wJ); free(Lref); free(cel); free(mass); free(fint);
     free(uK); free(aprev); free(cons); free(flag); free(UU);

@@ -46,7 +46,7 @@ typedef struct {
     int32_t nthreads;
 } orc_problem;
 
-typedef struct { int64_t steps; double t, dt_last, dt_init; int32_t status; } orc_result;
+typedef struct { int64_t steps; double t, dt_last, dt_init; int32_t status; double loop_seconds; } orc_result;
 
 /* status codes */
 enum { ORC_OK = 0, ORC_ERR_NEG_JACOBIAN = 1, ORC_ERR_NAN = 2, ORC_ERR_ARG = 3 };

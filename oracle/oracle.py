@@ -47,7 +47,7 @@ class _Problem(C.Structure):
 
 class _Result(C.Structure):
     _fields_ = [("steps", C.c_int64), ("t", C.c_double), ("dt_last", C.c_double),
-                ("dt_init", C.c_double), ("status", C.c_int32)]
+                ("dt_init", C.c_double), ("status", C.c_int32), ("loop_seconds", C.c_double)]
 
 
 _lib = None
@@ -229,6 +229,7 @@ class RunResult:
     dt_last: float
     status: int
     dt_hist: np.ndarray
+    loop_seconds: float = 0.0
 
 
 def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int = 0) -> RunResult:
@@ -243,6 +244,7 @@ def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int 
     em = None if mesh.elem_mat is None else np.ascontiguousarray(mesh.elem_mat, np.int32)
     marr = _mats_array(mats)
     total = 0
+    loop_s = 0.0
     res = _Result()
     hist_all = []
     for k, s in enumerate(solvers):
@@ -255,11 +257,12 @@ def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int 
         hist = np.zeros(max(1, max_hist))
         rc = lib().orc_run(C.byref(prob), _p(u), _p(v), _p(a), _p(hist), max_hist, C.byref(res))
         total += res.steps
+        loop_s += res.loop_seconds
         hist_all.append(hist[: min(res.steps, max_hist)])
         if rc != 0:
             break
     return RunResult(u, v, a, total, res.t, res.dt_init, res.dt_last, res.status,
-                     np.concatenate(hist_all) if hist_all else np.zeros(0))
+                     np.concatenate(hist_all) if hist_all else np.zeros(0), loop_s)
 
 
 # ---------------------------------------------------------------- the reference

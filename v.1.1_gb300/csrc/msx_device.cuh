@@ -1,0 +1,830 @@
+// msx_device.cuh -- device code of the explicit C3D4 step.
+//
+// Included by one translation unit per numeric mode.  msx_exact.cu is built
+// with --fmad=false and instantiates the reference-order kernels; msx_fast.cu
+// is built with contraction on and instantiates the FP64 and mixed kernels.
+#pragma once
+#include <cfloat>
+#include <cmath>
+#include "msx_internal.h"
+
+namespace msx {
+
+#define MSX_INF_BITS 0x7FF0000000000000ULL
+
+// ---------------------------------------------------------------------------
+// Reference-order arithmetic (src/mathematics/maths.cpp, geometry.cpp and the
+// laws).  These compile to plain mul/add only when contraction is off.
+// ---------------------------------------------------------------------------
+// maths.cpp:1564-1577 determinantTensor
+__device__ __forceinline__ double det3_ref(const double *A)
+{
+    return A[0] * (A[4] * A[8] - A[7] * A[5]) - A[1] * (A[3] * A[8] - A[6] * A[5]) +
+           A[2] * (A[3] * A[7] - A[6] * A[4]);
+}
+
+// maths.cpp:2749-2785 inverse
+__device__ __forceinline__ void inv3_ref(const double *A, double *Ai)
+{
+    double idet = 1.0 / det3_ref(A);
+    Ai[0] = idet * (A[4] * A[8] - A[5] * A[7]);
+    Ai[3] = -idet * (A[3] * A[8] - A[5] * A[6]);
+    Ai[6] = idet * (A[3] * A[7] - A[4] * A[6]);
+    Ai[1] = -idet * (A[1] * A[8] - A[2] * A[7]);
+    Ai[4] = idet * (A[0] * A[8] - A[2] * A[6]);
+    Ai[7] = -idet * (A[0] * A[7] - A[1] * A[6]);
+    Ai[2] = idet * (A[1] * A[5] - A[2] * A[4]);
+    Ai[5] = -idet * (A[0] * A[5] - A[2] * A[3]);
+    Ai[8] = idet * (A[0] * A[4] - A[1] * A[3]);
+}
+
+// geometry.cpp:90-136 areaTriangle (3D) of triangle (p, q, r): 0.5*|(p-r)x(q-r)|
+__device__ __forceinline__ double area_tri_ref(const double *p, const double *q, const double *r)
+{
+    double A0 = p[0] - r[0], A1 = p[1] - r[1], A2 = p[2] - r[2];
+    double B0 = q[0] - r[0], B1 = q[1] - r[1], B2 = q[2] - r[2];
+    double C0 = A1 * B2 - A2 * B1;
+    double C1 = A2 * B0 - A0 * B2;
+    double C2 = A0 * B1 - A1 * B0;
+    return 0.5 * sqrt(C0 * C0 + C1 * C1 + C2 * C2);
+}
+
+// geometry.cpp:264-301 inscribedSphere x 2 (classLinearTetrahedra.cpp:146-163)
+__device__ __forceinline__ double char_length_ref(const double *x)
+{
+    const double *p0 = x, *p1 = x + 3, *p2 = x + 6, *p3 = x + 9;
+    double s1 = area_tri_ref(p0, p1, p2);
+    double s2 = area_tri_ref(p1, p2, p3);
+    double s3 = area_tri_ref(p0, p2, p3);
+    double s4 = area_tri_ref(p0, p1, p3);
+    double A = fabs(s1) + fabs(s2) + fabs(s3) + fabs(s4);
+    double M[9] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], p2[0] - p0[0], p2[1] - p0[1],
+                   p2[2] - p0[2], p3[0] - p0[0], p3[1] - p0[1], p3[2] - p0[2]};
+    double V = 1.0 / 6.0 * fabs(det3_ref(M));
+    double r = 3.0 * V / A;
+    return 2 * r;
+}
+
+// First Piola stress in the reference's operation order:
+// hyperElasticNeoHookean.cpp:84-127 (Neo-Hookean), :235-259 (compressible),
+// hyperElasticStVenantKirchhoff.cpp:64-101,219-222 (StVK).
+__device__ __forceinline__ void stress_ref(const MatParams &m, const double *F, double *P)
+{
+    if (m.law == 1) {
+        double J = det3_ref(F), C[9], iC[9], S[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) c += F[k * 3 + i] * F[k * 3 + j];
+                C[i * 3 + j] = c;
+            }
+        inv3_ref(C, iC);
+#pragma unroll
+        for (int i = 0; i < 9; i++) S[i] = 0;
+#pragma unroll
+        for (int i = 0; i < 3; i++) S[i * 3 + i] += m.mu;
+        double alpha = m.lambda * log(J) - m.mu;
+#pragma unroll
+        for (int i = 0; i < 9; i++) S[i] += alpha * iC[i];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) c += F[i * 3 + k] * S[k * 3 + j];
+                P[i * 3 + j] = c;
+            }
+    } else if (m.law == 0) {
+        double B[9], iF[9], Ca[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) c += F[i * 3 + k] * F[j * 3 + k];
+                B[i * 3 + j] = c;
+            }
+        double J = det3_ref(F);
+        inv3_ref(F, iF);
+        double trB = 0;
+#pragma unroll
+        for (int i = 0; i < 3; i++) trB += B[i * 3 + i];
+        double fact1 = pow(J, 5.0 / 3.0);
+        double fact2 = m.mu / fact1;
+#pragma unroll
+        for (int i = 0; i < 9; i++) Ca[i] = 0 + fact2 * B[i];
+        double fact3 = -(m.mu / 3.0) * trB / fact1 + m.K1 * (J - 1.0);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) Ca[i * 3 + j] += fact3 * (i == j ? 1.0 : 0.0);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) c += Ca[i * 3 + k] * iF[j * 3 + k] * J;
+                P[i * 3 + j] = c;
+            }
+    } else {
+        double C[9], S[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) c += F[k * 3 + i] * F[k * 3 + j];
+                C[i * 3 + j] = c;
+            }
+        double trE = 0;
+#pragma unroll
+        for (int i = 0; i < 9; i++) S[i] = 0.5 * (C[i] - ((i % 4) == 0 ? 1.0 : 0.0));
+#pragma unroll
+        for (int i = 0; i < 3; i++) trE += S[i * 3 + i];
+#pragma unroll
+        for (int i = 0; i < 9; i++) S[i] = S[i] * m.mu2;
+#pragma unroll
+        for (int i = 0; i < 3; i++) S[i * 3 + i] += m.lam_stvk * trE;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) c += F[i * 3 + k] * S[k * 3 + j];
+                P[i * 3 + j] = c;
+            }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Shared pieces
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ const MatParams &mat_of(const Problem &p, long long e)
+{
+    return p.mats[p.mat ? p.mat[e] : 0];
+}
+
+// Block-wide min of a positive double, then one integer atomicMin on its bit
+// pattern (monotone for non-negative doubles; exact and order independent).
+__device__ __forceinline__ void block_min_to(double v, unsigned long long *slot)
+{
+    __shared__ double wmin[32];
+    if (!(v >= 0.0)) v = INFINITY;    // NaN or negative: ignored
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) wmin[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int nw = (blockDim.x + 31) >> 5;
+        v = l < nw ? wmin[l] : INFINITY;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (l == 0 && v < INFINITY) atomicMin(slot, (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+// The control decision of the node kernel: derived identically in every
+// thread from the previous slot (solverExplicit.cpp:217-276).
+struct StepDecision {
+    Ctrl next;
+    bool run;
+};
+
+__device__ __forceinline__ StepDecision decide_step(const Problem &p, const Ctrl &cp, int parity)
+{
+    StepDecision d;
+    d.next = cp;
+    d.next.ran = 0;
+    d.run = false;
+    if (cp.stop) return d;
+    if (cp.ran && p.flags[parity]) {        // uK[1] not finite after the last step
+        d.next.status = 4;
+        d.next.stop = 1;
+        return d;
+    }
+    if (cp.t < p.tf - 1E-12 && cp.step < cp.limit) {
+        double t = cp.t, dt = cp.dt;
+        if (t + dt > p.tf) {
+            dt = p.tf - t;
+            t = p.tf;
+        } else {
+            t += dt;
+        }
+        double dtn = __longlong_as_double((long long)p.dtmin[parity]);
+        dtn = dtn * p.sf;
+        d.next.t = t;
+        if (dtn < 1E-20) {
+            d.next.status = 3;
+            d.next.stop = 1;
+            d.next.dt = dtn;
+        } else {
+            d.next.dt = dtn;
+            d.next.step = cp.step + 1;
+            d.next.ran = 1;
+            d.run = true;
+        }
+    } else {
+        d.next.stop = 1;
+    }
+    return d;
+}
+
+// Dirichlet increment of one entry at block step `step` (solverExplicit.cpp:545-575)
+__device__ __forceinline__ double bc_increment(const BCEntry &b, double dt, long long step)
+{
+    if (b.mode == 1) return step == 1 ? b.val : 0.0;
+    if (b.mode == 2) {
+        double r = (b.ramp_steps > 0 && step < b.ramp_steps) ? (double)step / (double)b.ramp_steps : 1.0;
+        return b.val * r * dt;
+    }
+    return b.val * dt;
+}
+
+// ---------------------------------------------------------------------------
+// Node kernel: post-update of step n-1 (a = -f_int/m, v += dt (a_prev+a)/2,
+// nonlinearSystem.cpp:1034-1117), control of step n, prediction
+// u += dt v + dt^2/2 a (nonlinearSystem.cpp:1186-1200) and Dirichlet values.
+// One thread per node, three components.
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(kNodeBlock) node_kernel(Problem p, int parity)
+{
+    const Ctrl cp = p.ctrl[parity ^ 1];
+    StepDecision d = decide_step(p, cp, parity);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        p.ctrl[parity] = d.next;
+        p.dtmin[parity ^ 1] = MSX_INF_BITS;
+        p.flags[parity ^ 1] = 0;
+    }
+    if (!cp.ran && !d.run) return;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.nn) return;
+    const long long nn = p.nn;
+    int rec = p.node_bc[i];
+    int2 br[3] = {make_int2(0, 0), make_int2(0, 0), make_int2(0, 0)};
+    if (rec >= 0) {
+        br[0] = p.bc_rec[rec * 3 + 0];
+        br[1] = p.bc_rec[rec * 3 + 1];
+        br[2] = p.bc_rec[rec * 3 + 2];
+    }
+    bool act[3] = {br[0].y == 0, br[1].y == 0, br[2].y == 0};
+    double s[3] = {0.0, 0.0, 0.0};
+    if (cp.ran && (act[0] || act[1] || act[2])) {
+        int k0 = p.node_ptr[i], k1 = p.node_ptr[i + 1];
+        if (MODE == MODE_MIXED) {
+            // Neumaier-compensated FP32 sums of the FP32 corner forces
+            float sh[3] = {0.f, 0.f, 0.f}, sc[3] = {0.f, 0.f, 0.f};
+            for (int k = k0; k < k1; k++) {
+                const float *f = p.fe32 + (long long)p.node_inc[k] * 3;
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    float x = f[c], t = sh[c] + x;
+                    sc[c] += fabsf(sh[c]) >= fabsf(x) ? (sh[c] - t) + x : (x - t) + sh[c];
+                    sh[c] = t;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) s[c] = (double)sh[c] + (double)sc[c];
+        } else {
+            for (int k = k0; k < k1; k++) {
+                const double *f = p.fe + (long long)p.node_inc[k] * 3;
+                s[0] += f[0];
+                s[1] += f[1];
+                s[2] += f[2];
+            }
+        }
+    }
+    const double dtp = cp.dt, dtn = d.next.dt;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        long long dof = i + c * nn;
+        double ui = p.u[dof], vi = p.v[dof], ai = p.a[dof];
+        bool changed = false;
+        if (cp.ran && act[c]) {
+            double an;
+            if (MODE == MODE_EXACT) {
+                double val = -s[c] + 0.0;
+                double rhs = 0;
+                rhs += val;
+                an = rhs / p.mass[i];
+                vi += dtp * ((1. - 0.5) * ai + 0.5 * an);
+            } else {
+                an = -s[c] * p.minv[i];
+                vi += dtp * (0.5 * ai + 0.5 * an);
+            }
+            ai = an;
+            changed = true;
+        }
+        if (d.run) {
+            if (act[c]) {
+                ui += dtn * vi + 0.5 * dtn * dtn * ai;
+            } else {
+                for (int k = br[c].x; k < br[c].x + br[c].y; k++) {
+                    double Ud = bc_increment(p.bcs[k], dtn, d.next.step);
+                    ui += Ud;
+                    vi = Ud;
+                    ai = 0.;
+                }
+            }
+            changed = true;
+        }
+        if (changed) {
+            p.u[dof] = ui;
+            p.v[dof] = vi;
+            p.a[dof] = ai;
+            if (MODE == MODE_MIXED) {
+                float hi = (float)ui;
+                p.uhl[dof] = make_float2(hi, (float)(ui - (double)hi));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Element kernels: F, P, wJ B^T P corner forces and the deformed CFL length.
+// ---------------------------------------------------------------------------
+
+// Reference operation order (used with contraction off).
+template <bool FORCE_ONLY>
+__global__ void __launch_bounds__(kElemBlock) elem_kernel_exact(Problem p, int parity)
+{
+    if (!FORCE_ONLY && !p.ctrl[parity].ran) return;
+    const long long ne = p.ne, nn = p.nn;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double vmin = INFINITY;
+    if (e < ne) {
+        int4 cn = p.conn[e];
+        int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+        double dphi[12];
+#pragma unroll
+        for (int k = 0; k < 9; k++) dphi[3 + k] = p.G[k * ne + e];
+#pragma unroll
+        for (int j = 0; j < 3; j++) dphi[j] = (-dphi[3 + j] - dphi[6 + j]) - dphi[9 + j];
+        double ue[12];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int i = 0; i < 3; i++) ue[a * 3 + i] = p.u[nd[a] + i * nn];
+        // constitutiveManager.cpp:151-164
+        double F[9], P[9];
+#pragma unroll
+        for (int i = 0; i < 9; i++) F[i] = 0.;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            F[i * 3 + i] += 1.;
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) F[i * 3 + j] += dphi[a * 3 + j] * ue[a * 3 + i];
+        }
+        const MatParams &m = mat_of(p, e);
+        stress_ref(m, F, P);
+        // constitutiveAlgorithms.cpp:46-56
+        double wJ = p.wJ[e];
+        double *fe = p.fe + e * 12;
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                double f = 0;
+#pragma unroll
+                for (int J = 0; J < 3; J++) f += wJ * P[i * 3 + J] * dphi[a * 3 + J];
+                fe[a * 3 + i] = 0 + f;
+            }
+        if (!FORCE_ONLY) {
+            // solvers.cpp:304-317: deformed inscribed sphere
+            double x[12];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    x[a * 3 + k] = p.X[k * nn + nd[a]];
+                    x[a * 3 + k] += ue[a * 3 + k];
+                }
+            double dist = char_length_ref(x);
+            double Lr = p.Lref[e];
+            double mlen = (dist < Lr) ? dist : Lr;
+            vmin = mlen / m.c;
+            if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
+        }
+    }
+    if (!FORCE_ONLY) block_min_to(vmin, p.dtmin + (parity ^ 1));
+}
+
+// Plain FP64 with contraction: H from node differences, laws written through
+// the cofactor of F (F C^-1 = F^-T = cof(F)/J), the 4th corner force as minus
+// the sum of the other three.  Same algebra as the reference, fewer FP64
+// operations.
+__device__ __forceinline__ void cofactor(const double *F, double *K)
+{
+    K[0] = F[4] * F[8] - F[5] * F[7];
+    K[1] = F[5] * F[6] - F[3] * F[8];
+    K[2] = F[3] * F[7] - F[4] * F[6];
+    K[3] = F[2] * F[7] - F[1] * F[8];
+    K[4] = F[0] * F[8] - F[2] * F[6];
+    K[5] = F[1] * F[6] - F[0] * F[7];
+    K[6] = F[1] * F[5] - F[2] * F[4];
+    K[7] = F[2] * F[3] - F[0] * F[5];
+    K[8] = F[0] * F[4] - F[1] * F[3];
+}
+
+__device__ __forceinline__ void stress_fast(const MatParams &m, const double *F, double *P)
+{
+    if (m.law == 2) {
+        // S = mu2 E + lam tr(E) I, E = (F^T F - I)/2; P = F S
+        double C00 = F[0] * F[0] + F[3] * F[3] + F[6] * F[6];
+        double C11 = F[1] * F[1] + F[4] * F[4] + F[7] * F[7];
+        double C22 = F[2] * F[2] + F[5] * F[5] + F[8] * F[8];
+        double C01 = F[0] * F[1] + F[3] * F[4] + F[6] * F[7];
+        double C02 = F[0] * F[2] + F[3] * F[5] + F[6] * F[8];
+        double C12 = F[1] * F[2] + F[4] * F[5] + F[7] * F[8];
+        double trE = 0.5 * ((C00 - 1.0) + (C11 - 1.0) + (C22 - 1.0));
+        double h = 0.5 * m.mu2, dg = m.lam_stvk * trE;
+        double S00 = h * (C00 - 1.0) + dg, S11 = h * (C11 - 1.0) + dg, S22 = h * (C22 - 1.0) + dg;
+        double S01 = h * C01, S02 = h * C02, S12 = h * C12;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            double f0 = F[i * 3], f1 = F[i * 3 + 1], f2 = F[i * 3 + 2];
+            P[i * 3 + 0] = f0 * S00 + f1 * S01 + f2 * S02;
+            P[i * 3 + 1] = f0 * S01 + f1 * S11 + f2 * S12;
+            P[i * 3 + 2] = f0 * S02 + f1 * S12 + f2 * S22;
+        }
+        return;
+    }
+    double K[9];
+    cofactor(F, K);
+    double J = F[0] * K[0] + F[1] * K[1] + F[2] * K[2];
+    double iJ = 1.0 / J;
+    if (m.law == 1) {
+        // P = mu F + (lambda ln J - mu) F^-T
+        double g = (m.lambda * log(J) - m.mu) * iJ;
+#pragma unroll
+        for (int k = 0; k < 9; k++) P[k] = m.mu * F[k] + g * K[k];
+    } else {
+        // P = mu J^-2/3 F + (-mu/3 trB J^-5/3 + K1 (J-1)) cof(F)
+        double r = rcbrt(J);
+        double j23 = r * r;
+        double trB = 0;
+#pragma unroll
+        for (int k = 0; k < 9; k++) trB += F[k] * F[k];
+        double a1 = m.mu * j23;
+        double g = -(m.mu / 3.0) * trB * j23 * iJ + m.K1 * (J - 1.0);
+#pragma unroll
+        for (int k = 0; k < 9; k++) P[k] = a1 * F[k] + g * K[k];
+    }
+}
+
+// Inscribed-sphere diameter from the three edge vectors at vertex 0:
+// 2 r = 2 |e1.(e2 x e3)| / (|e1xe2| + |e1xe3| + |e2xe3| + |(e2-e1)x(e3-e1)|).
+template <typename T>
+__device__ __forceinline__ T char_length_edges(const T *e1, const T *e2, const T *e3)
+{
+    T A0 = e1[1] * e2[2] - e1[2] * e2[1], A1 = e1[2] * e2[0] - e1[0] * e2[2], A2 = e1[0] * e2[1] - e1[1] * e2[0];
+    T B0 = e1[1] * e3[2] - e1[2] * e3[1], B1 = e1[2] * e3[0] - e1[0] * e3[2], B2 = e1[0] * e3[1] - e1[1] * e3[0];
+    T C0 = e2[1] * e3[2] - e2[2] * e3[1], C1 = e2[2] * e3[0] - e2[0] * e3[2], C2 = e2[0] * e3[1] - e2[1] * e3[0];
+    T D0 = C0 + A0 - B0, D1 = C1 + A1 - B1, D2 = C2 + A2 - B2;
+    T s = sqrt(A0 * A0 + A1 * A1 + A2 * A2) + sqrt(B0 * B0 + B1 * B1 + B2 * B2) +
+          sqrt(C0 * C0 + C1 * C1 + C2 * C2) + sqrt(D0 * D0 + D1 * D1 + D2 * D2);
+    T v6 = fabs(e1[0] * C0 + e1[1] * C1 + e1[2] * C2);
+    return T(2) * v6 / s;
+}
+
+template <bool FORCE_ONLY>
+__global__ void __launch_bounds__(kElemBlock) elem_kernel_fp64(Problem p, int parity)
+{
+    if (!FORCE_ONLY && !p.ctrl[parity].ran) return;
+    const long long ne = p.ne, nn = p.nn;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double vmin = INFINITY;
+    if (e < ne) {
+        int4 cn = p.conn[e];
+        int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+        double G[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) G[k] = __ldg(p.G + k * ne + e);
+        double u0[3], du[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++) u0[i] = p.u[nd[0] + i * nn];
+#pragma unroll
+        for (int a = 1; a < 4; a++)
+#pragma unroll
+            for (int i = 0; i < 3; i++) du[(a - 1) * 3 + i] = p.u[nd[a] + i * nn] - u0[i];
+        double F[9], P[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+                F[i * 3 + j] = (i == j ? 1.0 : 0.0) +
+                               (du[i] * G[j] + du[3 + i] * G[3 + j] + du[6 + i] * G[6 + j]);
+        const MatParams &m = mat_of(p, e);
+        stress_fast(m, F, P);
+        double wJ = __ldg(p.wJ + e);
+#pragma unroll
+        for (int k = 0; k < 9; k++) P[k] *= wJ;
+        double f[12];
+#pragma unroll
+        for (int a = 1; a < 4; a++)
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+                f[a * 3 + i] = P[i * 3] * G[(a - 1) * 3] + P[i * 3 + 1] * G[(a - 1) * 3 + 1] +
+                               P[i * 3 + 2] * G[(a - 1) * 3 + 2];
+#pragma unroll
+        for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
+        double2 *fe = reinterpret_cast<double2 *>(p.fe + e * 12);
+#pragma unroll
+        for (int k = 0; k < 6; k++) fe[k] = make_double2(f[2 * k], f[2 * k + 1]);
+        if (!FORCE_ONLY) {
+            double X0[3], e1[3], e2[3], e3[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) X0[k] = __ldg(p.X + k * nn + nd[0]);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                e1[k] = (__ldg(p.X + k * nn + nd[1]) - X0[k]) + du[k];
+                e2[k] = (__ldg(p.X + k * nn + nd[2]) - X0[k]) + du[3 + k];
+                e3[k] = (__ldg(p.X + k * nn + nd[3]) - X0[k]) + du[6 + k];
+            }
+            double dist = char_length_edges<double>(e1, e2, e3);
+            double Lr = __ldg(p.Lref + e);
+            vmin = ((dist < Lr) ? dist : Lr) / m.c;
+            if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
+        }
+    }
+    if (!FORCE_ONLY) block_min_to(vmin, p.dtmin + (parity ^ 1));
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision: FP32 kinematics, stress and B^T P written in terms of the
+// displacement gradient H = F - I (no 1 - 1 cancellation in FP32); J - 1 and
+// ln J in FP64; FP32 corner forces; FP32 CFL length with the dt min in FP64.
+// cof(I + H) = I + D with D = (tr H + I2) I - (1 + tr H) H^T + (H^2)^T.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H, double Jm1d, double lnJd,
+                                             float t, float I2, float *P)
+{
+    if (m.law == 2) {
+        // E = (H + H^T + H^T H)/2, S = mu2 E + lam tr(E) I, P = (I + H) S
+        float E[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+                E[i * 3 + j] = 0.5f * (H[i * 3 + j] + H[j * 3 + i] +
+                                       (H[i] * H[j] + H[3 + i] * H[3 + j] + H[6 + i] * H[6 + j]));
+        float trE = E[0] + E[4] + E[8];
+        float S[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) S[k] = m.mu2_f * E[k];
+        S[0] += m.lam_stvk_f * trE;
+        S[4] += m.lam_stvk_f * trE;
+        S[8] += m.lam_stvk_f * trE;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+                P[i * 3 + j] = S[i * 3 + j] + (H[i * 3] * S[j] + H[i * 3 + 1] * S[3 + j] + H[i * 3 + 2] * S[6 + j]);
+        return;
+    }
+    float D[9];
+    float a0 = t + I2, a1 = 1.0f + t;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            // (H^2)^T_ij = sum_k H_jk H_ki
+            float h2 = H[j * 3] * H[i] + H[j * 3 + 1] * H[3 + i] + H[j * 3 + 2] * H[6 + i];
+            D[i * 3 + j] = (i == j ? a0 : 0.0f) - a1 * H[j * 3 + i] + h2;
+        }
+    float Jm1 = (float)Jm1d, lnJ = (float)lnJd;
+    float iJ = 1.0f / (1.0f + Jm1);
+    if (m.law == 1) {
+        // P = [mu (Jm1 I + (1+Jm1) H - D) + lambda lnJ (I + D)] / J
+        float lj = m.lambda_f * lnJ;
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            float dg = (k % 4 == 0) ? 1.0f : 0.0f;
+            P[k] = (m.mu_f * (Jm1 * dg + (1.0f + Jm1) * H[k] - D[k]) + lj * (dg + D[k])) * iJ;
+        }
+    } else {
+        // P = mu J^-2/3 [(Jm1 - beta) I + (1+Jm1) H - (1+beta) D]/J + K Jm1 (I + D)
+        float hh = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 9; k++) hh += H[k] * H[k];
+        float beta = (2.0f * t + hh) * (1.0f / 3.0f);
+        float j23 = expf(-(2.0f / 3.0f) * lnJ) * m.mu_f * iJ;
+        float kj = m.K1_f * Jm1;
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            float dg = (k % 4 == 0) ? 1.0f : 0.0f;
+            P[k] = j23 * ((Jm1 - beta) * dg + (1.0f + Jm1) * H[k] - (1.0f + beta) * D[k]) + kj * (dg + D[k]);
+        }
+    }
+}
+
+template <bool FORCE_ONLY>
+__global__ void __launch_bounds__(kElemBlock) elem_kernel_mixed(Problem p, int parity)
+{
+    if (!FORCE_ONLY && !p.ctrl[parity].ran) return;
+    const long long ne = p.ne, nn = p.nn;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double vmin = INFINITY;
+    if (e < ne) {
+        int4 cn = p.conn[e];
+        int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+        float G[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) G[k] = __ldg(p.G32 + k * ne + e);
+        // du = u_a - u_0 from the (hi, lo) split: the hi difference is exact for
+        // nearby values, the lo difference restores the bits FP32 drops
+        float2 h0[3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) h0[i] = p.uhl[nd[0] + i * nn];
+        float du[9];
+#pragma unroll
+        for (int a = 1; a < 4; a++)
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                float2 ha = p.uhl[nd[a] + i * nn];
+                du[(a - 1) * 3 + i] = (ha.x - h0[i].x) + (ha.y - h0[i].y);
+            }
+        float H[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) H[i * 3 + j] = du[i] * G[j] + du[3 + i] * G[3 + j] + du[6 + i] * G[6 + j];
+        // J - 1 = tr H + I2(H) + det H and ln J = log1p(J - 1) in FP64
+        double Hd[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) Hd[k] = (double)H[k];
+        double td = Hd[0] + Hd[4] + Hd[8];
+        double I2d = Hd[0] * Hd[4] + Hd[4] * Hd[8] + Hd[0] * Hd[8] - Hd[1] * Hd[3] - Hd[5] * Hd[7] - Hd[2] * Hd[6];
+        double I3d = Hd[0] * (Hd[4] * Hd[8] - Hd[5] * Hd[7]) - Hd[1] * (Hd[3] * Hd[8] - Hd[5] * Hd[6]) +
+                     Hd[2] * (Hd[3] * Hd[7] - Hd[4] * Hd[6]);
+        double Jm1 = td + I2d + I3d;
+        double lnJ = log1p(Jm1);
+        const MatParams &m = mat_of(p, e);
+        float P[9];
+        stress_mixed(m, H, Jm1, lnJ, (float)td, (float)I2d, P);
+        float wJ = __ldg(p.wJ32 + e);
+#pragma unroll
+        for (int k = 0; k < 9; k++) P[k] *= wJ;
+        float f[12];
+#pragma unroll
+        for (int a = 1; a < 4; a++)
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+                f[a * 3 + i] = P[i * 3] * G[(a - 1) * 3] + P[i * 3 + 1] * G[(a - 1) * 3 + 1] +
+                               P[i * 3 + 2] * G[(a - 1) * 3 + 2];
+#pragma unroll
+        for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
+        float4 *fe = reinterpret_cast<float4 *>(p.fe32 + e * 12);
+        fe[0] = make_float4(f[0], f[1], f[2], f[3]);
+        fe[1] = make_float4(f[4], f[5], f[6], f[7]);
+        fe[2] = make_float4(f[8], f[9], f[10], f[11]);
+        if (!FORCE_ONLY) {
+            float e1[3], e2[3], e3[3];
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                e1[i] = __ldg(p.Eref32 + i * ne + e) + du[i];
+                e2[i] = __ldg(p.Eref32 + (3 + i) * ne + e) + du[3 + i];
+                e3[i] = __ldg(p.Eref32 + (6 + i) * ne + e) + du[6 + i];
+            }
+            float dist = char_length_edges<float>(e1, e2, e3);
+            float Lr = __ldg(p.Lref32 + e);
+            vmin = (double)(((dist < Lr) ? dist : Lr) * m.inv_c_f);
+            if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
+        }
+    }
+    if (!FORCE_ONLY) block_min_to(vmin, p.dtmin + (parity ^ 1));
+}
+
+#ifdef MSX_SETUP_KERNELS
+// ---------------------------------------------------------------------------
+// Set-up kernels (reference operation order), built in the exact unit only
+// ---------------------------------------------------------------------------
+// classLinearTetrahedra.cpp:171-268 (Jacobian, inverse, dphi), classGPs.cpp:27
+// (wJ = 0.166666666667 |J|), classLinearTetrahedra.cpp:129-140 (charLength).
+__global__ void setup_elements_kernel(Problem p, const double *X, double *G, double *wJ, double *Lref,
+                                      float *G32, float *wJ32, float *Lref32, float *Eref32)
+{
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.ne) return;
+    const long long nn = p.nn, ne = p.ne;
+    int4 cn = p.conn[e];
+    int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    double xyz[12], pts[12];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            xyz[i * 4 + k] = X[i * nn + nd[k]];
+            pts[k * 3 + i] = X[i * nn + nd[k]];
+        }
+    const double natDev[12] = {-1.0, -1.0, -1.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
+    double Jac[9], iJ[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            double c = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) c += xyz[i * 4 + k] * natDev[k * 3 + j];
+            Jac[i * 3 + j] = c;
+        }
+    double J = det3_ref(Jac);
+    inv3_ref(Jac, iJ);
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        double g = 0.0 + iJ[k];
+        G[k * ne + e] = g;
+        G32[k * ne + e] = (float)g;
+    }
+    double w = 0.166666666667 * fabs(J);
+    wJ[e] = w;
+    wJ32[e] = (float)w;
+    double L = char_length_ref(pts);
+    Lref[e] = L;
+    Lref32[e] = (float)L;
+#pragma unroll
+    for (int a = 1; a < 4; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) Eref32[((a - 1) * 3 + i) * ne + e] = (float)(pts[a * 3 + i] - pts[i]);
+}
+
+// constitutiveAlgorithms.cpp:191-205 (rho wJ phi_a phi_b summed over b) and
+// solverExplicit.cpp:429-459 (element-order sum per node).
+__global__ void setup_mass_kernel(Problem p, double *mass, double *minv)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.nn) return;
+    const double phi = -1.0 * 0.25 - 1.0 * 0.25 - 1.0 * 0.25 + 1.0;
+    double m = 0;
+    for (int k = p.node_ptr[i]; k < p.node_ptr[i + 1]; k++) {
+        long long e = p.node_inc[k] >> 2;
+        double rho = mat_of(p, e).rho;
+        double me = 0;
+#pragma unroll
+        for (int b = 0; b < 4; b++) me += p.wJ[e] * rho * phi * phi;
+        m += me;
+    }
+    mass[i] = m;
+    minv[i] = 1.0 / m;
+}
+
+// solvers.cpp:276-287 (uK == nullptr) and :296-320: element min into dtmin[slot]
+__global__ void __launch_bounds__(kElemBlock) initial_cfl_kernel(Problem p, const double *uK, int slot)
+{
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double v = INFINITY;
+    if (e < p.ne) {
+        const MatParams &m = mat_of(p, e);
+        if (!uK) {
+            v = p.Lref[e] / m.c;
+        } else {
+            int4 cn = p.conn[e];
+            int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+            double x[12];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    x[a * 3 + k] = p.X[k * p.nn + nd[a]];
+                    x[a * 3 + k] += uK[p.nn * k + nd[a]];
+                }
+            double dist = char_length_ref(x);
+            double Lr = p.Lref[e];
+            v = ((dist < Lr) ? dist : Lr) / m.c;
+        }
+    }
+    block_min_to(v, p.dtmin + slot);
+}
+
+#endif  // MSX_SETUP_KERNELS
+
+// f_int gather for the test hook: fint[node + c*nn] in element order
+template <int MODE>
+__global__ void gather_kernel(Problem p, double *fint)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.nn) return;
+    double s[3] = {0, 0, 0};
+    for (int k = p.node_ptr[i]; k < p.node_ptr[i + 1]; k++) {
+        long long inc = p.node_inc[k];
+#pragma unroll
+        for (int c = 0; c < 3; c++) s[c] += MODE == MODE_MIXED ? (double)p.fe32[inc * 3 + c] : p.fe[inc * 3 + c];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) fint[i + c * p.nn] = s[c];
+}
+
+inline unsigned grid_for(long long n, int block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace msx

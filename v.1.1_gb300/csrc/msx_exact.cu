@@ -1,0 +1,45 @@
+// msx_exact.cu -- kernels in the reference's operation order.
+// Built with --fmad=false: every product and sum rounds on its own, as in the
+// reference compiled without FMA contraction, so FP64_EXACT results can be
+// compared with the reference bit for bit.  Also holds the set-up kernels,
+// whose outputs (dphi, wJ, characteristic length, lumped mass) every mode uses.
+#define MSX_SETUP_KERNELS
+#include "msx_device.cuh"
+
+namespace msx {
+
+void launch_node_exact(const Problem &p, int parity, cudaStream_t s)
+{
+    node_kernel<MODE_EXACT><<<grid_for(p.nn, kNodeBlock), kNodeBlock, 0, s>>>(p, parity);
+}
+
+void launch_elem_exact(const Problem &p, int parity, cudaStream_t s)
+{
+    elem_kernel_exact<false><<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, parity);
+}
+
+void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s)
+{
+    setup_elements_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(
+        p, X, const_cast<double *>(p.G), const_cast<double *>(p.wJ), const_cast<double *>(p.Lref),
+        const_cast<float *>(p.G32), const_cast<float *>(p.wJ32), const_cast<float *>(p.Lref32),
+        const_cast<float *>(p.Eref32));
+}
+
+void launch_setup_mass(const Problem &p, double *mass, double *minv, cudaStream_t s)
+{
+    setup_mass_kernel<<<grid_for(p.nn, 256), 256, 0, s>>>(p, mass, minv);
+}
+
+void launch_initial_cfl(const Problem &p, const double *uK, int slot, cudaStream_t s)
+{
+    initial_cfl_kernel<<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, uK, slot);
+}
+
+void launch_internal_force_exact(const Problem &p, double *fint, cudaStream_t s)
+{
+    elem_kernel_exact<true><<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, 0);
+    gather_kernel<MODE_EXACT><<<grid_for(p.nn, 256), 256, 0, s>>>(p, fint);
+}
+
+}  // namespace msx

@@ -1,0 +1,102 @@
+// msx_internal.h -- device-side data layout shared by the kernels and the
+// host runtime of the explicit C3D4 step.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace msx {
+
+constexpr int kMaxMats = 16;
+constexpr int kElemBlock = 256;   // element-kernel CTA (one element per thread)
+constexpr int kNodeBlock = 256;   // node-kernel CTA (one node per thread)
+
+enum Mode { MODE_FP64 = 0, MODE_EXACT = 1, MODE_MIXED = 2 };
+
+// Material constants, derived on the host the way the reference's law
+// constructors do (hyperElasticNeoHookean.cpp:23-33,203-215,
+// hyperElasticStVenantKirchhoff.cpp:23-31,64-70).
+struct MatParams {
+    int law;
+    double young, nu, rho;
+    double lambda, mu, K1;        // NH / compressible NH
+    double mu2, lam_stvk;         // StVK: E/(1+nu), E nu/((1+nu)(1-2nu))
+    double c;                     // sound speed used by the CFL
+    float lambda_f, mu_f, K1_f, mu2_f, lam_stvk_f, inv_c_f;
+};
+
+// One Dirichlet entry; `val` is what classDirichlet stores
+// (classNodes.cpp:58-74): U/(tf-t0) for RAMP, U for INST, Vmax for VEL_RAMP.
+struct BCEntry {
+    int mode;
+    int ramp_steps;
+    double val;
+};
+
+// Step control, double-buffered by step parity.  The node kernel of step n
+// reads slot (n-1)&1 and writes slot n&1; every thread derives the same
+// values, so no thread waits for another.
+struct Ctrl {
+    double t;            // time after the last time advance
+    double dt;           // dt of the last executed step (dt_init before any)
+    long long step;      // steps executed in this solver block
+    long long limit;     // stop once step reaches this count
+    int ran;             // 1: the last node kernel started a step (its post is pending)
+    int stop;            // 1: block finished (tf reached, limit hit or error)
+    int status;          // msx_status
+    int pad;
+};
+
+struct Problem {
+    long long nn, ne;
+    // elements (SoA)
+    const int4 *conn;
+    const double *G;          // 9*ne: G[k*ne + e] = invJ[k/3][k%3] = dphi of node k/3+1
+    const double *wJ;
+    const double *Lref;
+    const float *G32, *wJ32, *Lref32;       // FP32 copies (mixed mode)
+    const float *Eref32;      // 9*ne reference edge vectors X_a - X_0 (mixed CFL)
+    const unsigned char *mat; // per-element material id, or nullptr
+    int nmat;
+    MatParams mats[kMaxMats];
+    // nodes (SoA, dof = node + c*nn)
+    const double *X;
+    double *u, *v, *a;
+    const double *mass;       // lumped mass per node
+    const double *minv;       // 1/mass per node
+    float2 *uhl;              // 3*nn (hi, lo) split of u for the mixed element kernel
+    // corner forces, fe[(e*4 + a)*3 + i]
+    double *fe;
+    float *fe32;
+    // node -> (element, corner) incidences sorted by element id
+    const int *node_ptr;
+    const int *node_inc;      // e*4 + a
+    // Dirichlet data
+    const int *node_bc;       // per node: -1 or record index
+    const int2 *bc_rec;       // per record, per comp: (first entry, count)
+    const BCEntry *bcs;
+    // control
+    Ctrl *ctrl;                       // [2]
+    unsigned long long *dtmin;        // [2] bit patterns of positive doubles
+    int *flags;                       // [2] NaN flag raised by the element kernel
+    double sf, tf;
+};
+
+// launchers (one translation unit per numeric mode)
+void launch_node_exact(const Problem &p, int parity, cudaStream_t s);
+void launch_elem_exact(const Problem &p, int parity, cudaStream_t s);
+void launch_node_fp64(const Problem &p, int parity, cudaStream_t s);
+void launch_elem_fp64(const Problem &p, int parity, cudaStream_t s);
+void launch_node_mixed(const Problem &p, int parity, cudaStream_t s);
+void launch_elem_mixed(const Problem &p, int parity, cudaStream_t s);
+
+// set-up (exact operation order)
+void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s);
+void launch_setup_mass(const Problem &p, double *mass, double *minv, cudaStream_t s);
+// min over elements of Lref/c (undeformed) or min(Lref, L(X+u))/c, into dtmin[slot]
+void launch_initial_cfl(const Problem &p, const double *uK, int slot, cudaStream_t s);
+// one element pass + gather for f_int(u) (test hook); writes fint[3*nn]
+void launch_internal_force_exact(const Problem &p, double *fint, cudaStream_t s);
+void launch_internal_force_fp64(const Problem &p, double *fint, cudaStream_t s);
+void launch_internal_force_mixed(const Problem &p, double *fint, cudaStream_t s);
+
+}  // namespace msx

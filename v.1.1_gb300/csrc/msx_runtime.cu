@@ -1,0 +1,708 @@
+// msx_runtime.cu -- host runtime and C ABI (include/msx.h) of the explicit
+// C3D4 step: validation, node->corner CSR, Dirichlet tables, device buffers,
+// step-chunk CUDA graphs, state transfer and the cube generator.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/msx.h"
+#include "msx_internal.h"
+
+using namespace msx;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_last_error;
+
+static msx_status fail(msx_status st, const std::string &msg)
+{
+    g_last_error = msg;
+    return st;
+}
+
+#define MSX_CUDA(call)                                                                          \
+    do {                                                                                        \
+        cudaError_t err_ = (call);                                                              \
+        if (err_ != cudaSuccess)                                                                \
+            return fail(err_ == cudaErrorMemoryAllocation ? MSX_ERR_OOM : MSX_ERR_CUDA,          \
+                        std::string(#call) + ": " + cudaGetErrorString(err_));                   \
+    } while (0)
+
+extern "C" const char *msx_last_error(void) { return g_last_error.c_str(); }
+
+// ------------------------------------------------------------------ small kernels
+namespace {
+
+__global__ void init_block_kernel(Problem p, double t0, long long limit)
+{
+    // solverExplicit.cpp:165-166: initial dt from the undeformed lengths
+    double dt0 = __longlong_as_double((long long)p.dtmin[0]);
+    dt0 = dt0 * p.sf;
+    Ctrl c;
+    c.t = t0;
+    c.dt = dt0;
+    c.step = 0;
+    c.limit = limit;
+    c.ran = 0;
+    c.stop = 0;
+    c.status = 0;
+    c.pad = 0;
+    p.ctrl[0] = c;
+    p.ctrl[1] = c;
+    p.flags[0] = 0;
+    p.flags[1] = 0;
+}
+
+__global__ void split_kernel(const double *u, float2 *uhl, long long n)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x = u[i];
+    float hi = (float)x;
+    uhl[i] = make_float2(hi, (float)(x - (double)hi));
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ device buffer helper
+template <typename T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count)
+    {
+        n = count;
+        return cudaMalloc((void **)&p, sizeof(T) * (count ? count : 1));
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+typedef void (*launch_fn)(const Problem &, int, cudaStream_t);
+
+struct msx_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    Problem P{};
+    // owned device storage
+    DBuf<int4> conn;
+    DBuf<double> G, wJ, Lref, X, u, v, a, mass, minv, fe;
+    DBuf<float> G32, wJ32, Lref32, Eref32, fe32;
+    DBuf<float2> uhl;
+    DBuf<unsigned char> mat;
+    DBuf<int> node_ptr, node_inc, node_bc;
+    DBuf<int2> bc_rec;
+    DBuf<BCEntry> bcs;
+    DBuf<Ctrl> ctrl;
+    DBuf<unsigned long long> dtmin;
+    DBuf<int> flags;
+    Ctrl *h_ctrl = nullptr;   // pinned [2]
+    // solver block
+    double t0 = 0, tf = 0, sf = 1;
+    long long max_steps = 0;
+    int precision = MSX_PREC_FP64;
+    int spg = 64;
+    bool block_ready = false;
+    long long block_steps = 0;
+    double dt_init = 0;
+    launch_fn node = nullptr, elem = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc[2] = {nullptr, nullptr};
+    std::vector<int> h_node_bc;   // host copies for next_solver rebuilds
+};
+
+// ------------------------------------------------------------------ host helpers
+static msx_status make_material(const msx_material &m, MatParams &o)
+{
+    if (m.law < 0 || m.law > 2) return fail(MSX_ERR_ARG, "unknown constitutive law");
+    if (!(m.young > 0) || !(m.rho > 0) || !(m.nu > -1.0) || !(m.nu < 0.5))
+        return fail(MSX_ERR_ARG, "material needs E > 0, rho > 0, -1 < nu < 0.5");
+    memset(&o, 0, sizeof(o));
+    const double E = m.young, nu = m.nu;
+    o.law = m.law;
+    o.young = E;
+    o.nu = nu;
+    o.rho = m.rho;
+    // hyperElasticNeoHookean.cpp:23-33 / :206-213
+    o.lambda = (E * nu) / ((1. + nu) * (1. - 2. * nu));
+    o.mu = 0.5 * E / (1. + nu);
+    o.K1 = E / (3 * (1 - 2 * nu));
+    // hyperElasticStVenantKirchhoff.cpp:68-69
+    o.mu2 = E / (1. + nu);
+    o.lam_stvk = E * nu / ((1. + nu) * (1. - (2 * nu)));
+    // soundSpeed: NH forms :51-54, StVK :50-55
+    o.c = m.law == 2 ? std::sqrt(E / m.rho) : std::sqrt((o.lambda + 2 * o.mu) / m.rho);
+    o.lambda_f = (float)o.lambda;
+    o.mu_f = (float)o.mu;
+    o.K1_f = (float)o.K1;
+    o.mu2_f = (float)o.mu2;
+    o.lam_stvk_f = (float)o.lam_stvk;
+    o.inv_c_f = (float)(1.0 / o.c);
+    return MSX_OK;
+}
+
+// Dirichlet tables: entries grouped by DOF in input order, one record per
+// constrained node with (first, count) per component.
+static msx_status build_bcs(long long nn, const msx_bc *bcs, long long nbc, double t0, double tf,
+                            std::vector<int> &node_bc, std::vector<int2> &rec, std::vector<BCEntry> &ent)
+{
+    if (nbc < 0 || (nbc > 0 && !bcs)) return fail(MSX_ERR_ARG, "bad boundary-condition array");
+    std::vector<long long> order(nbc);
+    std::iota(order.begin(), order.end(), 0);
+    for (long long k = 0; k < nbc; k++) {
+        if (bcs[k].dof < 0 || bcs[k].dof >= 3 * nn) return fail(MSX_ERR_ARG, "BC dof out of range");
+        if (bcs[k].mode < 0 || bcs[k].mode > 2) return fail(MSX_ERR_ARG, "unknown BC mode");
+        if (bcs[k].mode == MSX_BC_RAMP && !(tf - t0 != 0)) return fail(MSX_ERR_ARG, "ramp BC needs tf != t0");
+    }
+    std::stable_sort(order.begin(), order.end(), [&](long long x, long long y) { return bcs[x].dof < bcs[y].dof; });
+    node_bc.assign(nn, -1);
+    rec.clear();
+    ent.clear();
+    ent.reserve(nbc);
+    for (long long k = 0; k < nbc; k++) {
+        const msx_bc &b = bcs[order[k]];
+        BCEntry e;
+        e.mode = b.mode;
+        e.ramp_steps = b.ramp_steps;
+        // classNodes.cpp:58-74: a ramp stores U/duration, an instant BC stores U
+        e.val = b.mode == MSX_BC_RAMP ? b.value / (tf - t0) : b.value;
+        long long node = b.dof % nn;
+        int comp = (int)(b.dof / nn);
+        if (node_bc[node] < 0) {
+            node_bc[node] = (int)(rec.size() / 3);
+            rec.resize(rec.size() + 3, make_int2(0, 0));
+        }
+        int2 &r = rec[node_bc[node] * 3 + comp];
+        if (r.y == 0) r.x = (int)ent.size();
+        r.y++;
+        ent.push_back(e);
+    }
+    return MSX_OK;
+}
+
+static void bind_problem(msx_handle *h)
+{
+    Problem &P = h->P;
+    P.conn = h->conn.p;
+    P.G = h->G.p;
+    P.wJ = h->wJ.p;
+    P.Lref = h->Lref.p;
+    P.G32 = h->G32.p;
+    P.wJ32 = h->wJ32.p;
+    P.Lref32 = h->Lref32.p;
+    P.Eref32 = h->Eref32.p;
+    P.X = h->X.p;
+    P.u = h->u.p;
+    P.v = h->v.p;
+    P.a = h->a.p;
+    P.mass = h->mass.p;
+    P.minv = h->minv.p;
+    P.uhl = h->uhl.p;
+    P.fe = h->fe.p;
+    P.fe32 = h->fe32.p;
+    P.node_ptr = h->node_ptr.p;
+    P.node_inc = h->node_inc.p;
+    P.node_bc = h->node_bc.p;
+    P.bc_rec = h->bc_rec.p;
+    P.bcs = h->bcs.p;
+    P.ctrl = h->ctrl.p;
+    P.dtmin = h->dtmin.p;
+    P.flags = h->flags.p;
+    P.sf = h->sf;
+    P.tf = h->tf;
+}
+
+static msx_status set_mode(msx_handle *h, int precision)
+{
+    switch (precision) {
+    case MSX_PREC_FP64: h->node = launch_node_fp64; h->elem = launch_elem_fp64; break;
+    case MSX_PREC_FP64_EXACT: h->node = launch_node_exact; h->elem = launch_elem_exact; break;
+    case MSX_PREC_MIXED: h->node = launch_node_mixed; h->elem = launch_elem_mixed; break;
+    default: return fail(MSX_ERR_ARG, "unknown precision mode");
+    }
+    h->precision = precision;
+    return MSX_OK;
+}
+
+static msx_status upload_bcs(msx_handle *h, const msx_bc *bcs, long long nbc)
+{
+    std::vector<int> node_bc;
+    std::vector<int2> rec;
+    std::vector<BCEntry> ent;
+    msx_status st = build_bcs(h->P.nn, bcs, nbc, h->t0, h->tf, node_bc, rec, ent);
+    if (st != MSX_OK) return st;
+    h->bc_rec.release();
+    h->bcs.release();
+    if (!h->node_bc.p) MSX_CUDA(h->node_bc.alloc(h->P.nn));
+    MSX_CUDA(h->bc_rec.alloc(rec.size()));
+    MSX_CUDA(h->bcs.alloc(ent.size()));
+    MSX_CUDA(cudaMemcpyAsync(h->node_bc.p, node_bc.data(), sizeof(int) * node_bc.size(), cudaMemcpyHostToDevice, h->stream));
+    if (!rec.empty())
+        MSX_CUDA(cudaMemcpyAsync(h->bc_rec.p, rec.data(), sizeof(int2) * rec.size(), cudaMemcpyHostToDevice, h->stream));
+    if (!ent.empty())
+        MSX_CUDA(cudaMemcpyAsync(h->bcs.p, ent.data(), sizeof(BCEntry) * ent.size(), cudaMemcpyHostToDevice, h->stream));
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    h->h_node_bc.swap(node_bc);
+    return MSX_OK;
+}
+
+static msx_status set_opts(msx_handle *h, const msx_solver_opts *o)
+{
+    if (!o) return fail(MSX_ERR_ARG, "solver options required");
+    if (!(o->scale_factor > 0)) return fail(MSX_ERR_ARG, "scale factor must be > 0");
+    if (!(o->tf >= o->t0)) return fail(MSX_ERR_ARG, "need tf >= t0");
+    if (o->max_steps < 0) return fail(MSX_ERR_ARG, "max_steps must be >= 0");
+    msx_status st = set_mode(h, o->precision);
+    if (st != MSX_OK) return st;
+    h->t0 = o->t0;
+    h->tf = o->tf;
+    h->sf = o->scale_factor;
+    h->max_steps = o->max_steps;
+    int spg = o->steps_per_graph > 0 ? o->steps_per_graph : 64;
+    spg = (spg + 1) & ~1;   // even: every replay starts on the same parity
+    if (spg != h->spg && h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    h->spg = spg;
+    h->block_ready = false;
+    h->block_steps = 0;
+    return MSX_OK;
+}
+
+// Set-up of one solver block (solverExplicit.cpp:141-177): initial dt from
+// the undeformed lengths and the first step's CFL from uK (u when t0 < 1e-12,
+// zero otherwise, which is the undeformed value again).
+static msx_status init_block(msx_handle *h)
+{
+    bind_problem(h);
+    const Problem &P = h->P;
+    unsigned long long inf[2] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL};
+    MSX_CUDA(cudaMemcpyAsync(h->dtmin.p, inf, sizeof(inf), cudaMemcpyHostToDevice, h->stream));
+    launch_initial_cfl(P, nullptr, 0, h->stream);
+    launch_initial_cfl(P, h->t0 < 1E-12 ? h->u.p : nullptr, 1, h->stream);
+    long long limit = h->max_steps > 0 ? h->max_steps : (1LL << 62);
+    init_block_kernel<<<1, 1, 0, h->stream>>>(P, h->t0, limit);
+    MSX_CUDA(cudaGetLastError());
+    if (h->precision == MSX_PREC_MIXED) {
+        long long n = 3 * P.nn;
+        split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(h->u.p, h->uhl.p, n);
+        MSX_CUDA(cudaGetLastError());
+    }
+    MSX_CUDA(cudaMemcpyAsync(h->h_ctrl, h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    h->dt_init = h->h_ctrl[0].dt;
+    h->block_ready = true;
+    return MSX_OK;
+}
+
+static msx_status build_graph(msx_handle *h)
+{
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    bind_problem(h);
+    cudaGraph_t g;
+    MSX_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < h->spg; i++) {
+        int parity = (i & 1) ? 0 : 1;
+        h->node(h->P, parity, h->stream);
+        h->elem(h->P, parity, h->stream);
+    }
+    cudaError_t err = cudaStreamEndCapture(h->stream, &g);
+    if (err != cudaSuccess) return fail(MSX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(err));
+    err = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (err != cudaSuccess) return fail(MSX_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(err));
+    return MSX_OK;
+}
+
+// ------------------------------------------------------------------ C ABI
+extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats, int32_t num_mats,
+                                 const msx_bc *bcs, int64_t num_bcs, const msx_solver_opts *opts,
+                                 msx_handle **out)
+{
+    if (!out) return fail(MSX_ERR_ARG, "out handle pointer is NULL");
+    *out = nullptr;
+    if (!mesh || !mesh->X || !mesh->conn || mesh->num_nodes < 4 || mesh->num_elems < 1)
+        return fail(MSX_ERR_ARG, "mesh needs >= 4 nodes, >= 1 element, X and conn");
+    if (mesh->num_nodes >= (1LL << 31) || 4 * mesh->num_elems >= (1LL << 31))
+        return fail(MSX_ERR_ARG, "mesh too large for 32-bit node/incidence indices");
+    if (!mats || num_mats < 1 || num_mats > kMaxMats) return fail(MSX_ERR_ARG, "need 1..16 materials");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(MSX_ERR_NO_DEVICE, "no CUDA device");
+    const long long nn = mesh->num_nodes, ne = mesh->num_elems;
+    for (long long k = 0; k < 4 * ne; k++)
+        if (mesh->conn[k] < 0 || mesh->conn[k] >= nn) return fail(MSX_ERR_ARG, "connectivity index out of range");
+    if (mesh->elem_material)
+        for (long long e = 0; e < ne; e++)
+            if (mesh->elem_material[e] < 0 || mesh->elem_material[e] >= num_mats)
+                return fail(MSX_ERR_ARG, "element material id out of range");
+
+    msx_handle *h = new msx_handle();
+    auto bail = [&](msx_status st) {
+        msx_destroy(h);
+        return st;
+    };
+    msx_status st;
+    cudaGetDevice(&h->device);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess || prop.major * 10 + prop.minor != 103) {
+        delete h;
+        return fail(MSX_ERR_NO_DEVICE, "the library is built for sm_103 (GB300) only");
+    }
+    h->P.nn = nn;
+    h->P.ne = ne;
+    h->P.nmat = num_mats;
+    for (int k = 0; k < num_mats; k++)
+        if ((st = make_material(mats[k], h->P.mats[k])) != MSX_OK) return bail(st);
+    if ((st = set_opts(h, opts)) != MSX_OK) return bail(st);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(MSX_ERR_CUDA, "stream creation failed"));
+    cudaEventCreate(&h->ev0);
+    cudaEventCreate(&h->ev1);
+    cudaEventCreateWithFlags(&h->evc[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&h->evc[1], cudaEventDisableTiming);
+    if (cudaMallocHost((void **)&h->h_ctrl, 2 * sizeof(Ctrl)) != cudaSuccess)
+        return bail(fail(MSX_ERR_OOM, "pinned control buffer"));
+
+    // node -> (element, corner) CSR in element order: the per-node summation
+    // order of classSolverExplicit::computeInternalForce (solverExplicit.cpp:363-379)
+    std::vector<int> ptr(nn + 1, 0), inc(4 * ne);
+    for (long long k = 0; k < 4 * ne; k++) ptr[mesh->conn[k] + 1]++;
+    for (long long i = 0; i < nn; i++) ptr[i + 1] += ptr[i];
+    {
+        std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+        for (long long e = 0; e < ne; e++)
+            for (int q = 0; q < 4; q++) inc[fill[mesh->conn[e * 4 + q]]++] = (int)(e * 4 + q);
+    }
+
+#define ALLOC(buf, n) \
+    if (cudaError_t e_ = buf.alloc(n)) return bail(fail(MSX_ERR_OOM, std::string("device allocation: ") + cudaGetErrorString(e_)))
+    ALLOC(h->conn, ne);
+    ALLOC(h->G, 9 * ne);
+    ALLOC(h->wJ, ne);
+    ALLOC(h->Lref, ne);
+    ALLOC(h->G32, 9 * ne);
+    ALLOC(h->wJ32, ne);
+    ALLOC(h->Lref32, ne);
+    ALLOC(h->Eref32, 9 * ne);
+    ALLOC(h->X, 3 * nn);
+    ALLOC(h->u, 3 * nn);
+    ALLOC(h->v, 3 * nn);
+    ALLOC(h->a, 3 * nn);
+    ALLOC(h->mass, nn);
+    ALLOC(h->minv, nn);
+    ALLOC(h->uhl, 3 * nn);
+    ALLOC(h->fe, 12 * ne);
+    ALLOC(h->fe32, 12 * ne);
+    ALLOC(h->node_ptr, nn + 1);
+    ALLOC(h->node_inc, 4 * ne);
+    ALLOC(h->ctrl, 2);
+    ALLOC(h->dtmin, 2);
+    ALLOC(h->flags, 2);
+    if (mesh->elem_material && num_mats > 1) ALLOC(h->mat, ne);
+#undef ALLOC
+    cudaStream_t s = h->stream;
+    std::vector<unsigned char> mids;
+    if (h->mat.p) {
+        mids.resize(ne);
+        for (long long e = 0; e < ne; e++) mids[e] = (unsigned char)mesh->elem_material[e];
+    }
+#define UP(dst, src, bytes) \
+    if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return bail(fail(MSX_ERR_CUDA, "upload failed"))
+    UP(h->conn.p, mesh->conn, sizeof(int4) * ne);
+    UP(h->X.p, mesh->X, sizeof(double) * 3 * nn);
+    UP(h->node_ptr.p, ptr.data(), sizeof(int) * (nn + 1));
+    UP(h->node_inc.p, inc.data(), sizeof(int) * 4 * ne);
+    if (h->mat.p) UP(h->mat.p, mids.data(), ne);
+#undef UP
+    cudaMemsetAsync(h->u.p, 0, sizeof(double) * 3 * nn, s);
+    cudaMemsetAsync(h->v.p, 0, sizeof(double) * 3 * nn, s);
+    cudaMemsetAsync(h->a.p, 0, sizeof(double) * 3 * nn, s);
+    bind_problem(h);
+    h->P.mat = h->mat.p;
+    launch_setup_elements(h->P, h->X.p, s);
+    launch_setup_mass(h->P, h->mass.p, h->minv.p, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+        return bail(fail(MSX_ERR_CUDA, "set-up kernels failed"));
+    if ((st = upload_bcs(h, bcs, num_bcs)) != MSX_OK) return bail(st);
+    bind_problem(h);
+    *out = h;
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_destroy(msx_handle *h)
+{
+    if (!h) return MSX_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    DBuf<int4> *b4[] = {&h->conn};
+    for (auto *b : b4) b->release();
+    for (auto *b : {&h->G, &h->wJ, &h->Lref, &h->X, &h->u, &h->v, &h->a, &h->mass, &h->minv, &h->fe}) b->release();
+    for (auto *b : {&h->G32, &h->wJ32, &h->Lref32, &h->Eref32, &h->fe32}) b->release();
+    h->uhl.release();
+    h->mat.release();
+    for (auto *b : {&h->node_ptr, &h->node_inc, &h->node_bc, &h->flags}) b->release();
+    h->bc_rec.release();
+    h->bcs.release();
+    h->ctrl.release();
+    h->dtmin.release();
+    if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
+    for (cudaEvent_t e : {h->ev0, h->ev1, h->evc[0], h->evc[1]})
+        if (e) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *rep)
+{
+    if (!h) return fail(MSX_ERR_ARG, "NULL handle");
+    msx_status st;
+    if (!h->block_ready && (st = init_block(h)) != MSX_OK) return st;
+    if (!h->graph && (st = build_graph(h)) != MSX_OK) return st;
+    // per-call cap: the node kernel stops at ctrl.limit
+    const Ctrl &cur = h->h_ctrl[0];
+    MSX_CUDA(cudaMemcpyAsync(h->h_ctrl, h->ctrl.p, 2 * sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    Ctrl latest = h->h_ctrl[0];   // replays start on parity 1 and read slot 0
+    long long start_steps = latest.step;
+    long long limit = h->max_steps > 0 ? h->max_steps : (1LL << 62);
+    if (max_steps > 0) limit = std::min(limit, start_steps + (long long)max_steps);
+    // a block stopped only by an earlier per-call cap resumes; tf, errors stay final
+    bool resume = latest.stop && latest.status == 0 && latest.t < h->tf - 1E-12 && latest.step < limit;
+    if (latest.limit != limit || resume) {
+        latest.limit = limit;
+        if (resume) latest.stop = 0;
+        MSX_CUDA(cudaMemcpyAsync(h->ctrl.p, &latest, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream));
+        MSX_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    (void)cur;
+    MSX_CUDA(cudaEventRecord(h->ev0, h->stream));
+    // two replays in flight: check the older one's control slot
+    long long k = 0;
+    for (;; k++) {
+        MSX_CUDA(cudaGraphLaunch(h->graph, h->stream));
+        MSX_CUDA(cudaMemcpyAsync(h->h_ctrl + (k & 1), h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+        MSX_CUDA(cudaEventRecord(h->evc[k & 1], h->stream));
+        if (latest.stop) break;
+        if (k >= 1) {
+            MSX_CUDA(cudaEventSynchronize(h->evc[(k - 1) & 1]));
+            if (h->h_ctrl[(k - 1) & 1].stop) break;
+        }
+    }
+    MSX_CUDA(cudaEventRecord(h->ev1, h->stream));
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    Ctrl fin = h->h_ctrl[k & 1];
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    h->block_steps = fin.step;
+    if (rep) {
+        rep->steps = fin.step - start_steps;
+        rep->total_steps = fin.step;
+        rep->t = fin.t;
+        rep->dt = fin.dt;
+        rep->dt_init = h->dt_init;
+        rep->status = fin.status;
+        rep->device_ms = ms;
+        rep->kernel_launches = (k + 1) * 2LL * h->spg;
+    }
+    if (fin.status == MSX_ERR_NEG_JACOBIAN) return fail(MSX_ERR_NEG_JACOBIAN, "Negative jacobian: dt < 1e-20");
+    if (fin.status == MSX_ERR_NAN) return fail(MSX_ERR_NAN, "There are NANs in the displacements");
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_get_state(msx_handle *h, double *u, double *v, double *a)
+{
+    if (!h) return fail(MSX_ERR_ARG, "NULL handle");
+    size_t bytes = sizeof(double) * 3 * h->P.nn;
+    if (u) MSX_CUDA(cudaMemcpyAsync(u, h->u.p, bytes, cudaMemcpyDeviceToHost, h->stream));
+    if (v) MSX_CUDA(cudaMemcpyAsync(v, h->v.p, bytes, cudaMemcpyDeviceToHost, h->stream));
+    if (a) MSX_CUDA(cudaMemcpyAsync(a, h->a.p, bytes, cudaMemcpyDeviceToHost, h->stream));
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_set_state(msx_handle *h, const double *u, const double *v, const double *a)
+{
+    if (!h) return fail(MSX_ERR_ARG, "NULL handle");
+    if (h->block_steps > 0) return fail(MSX_ERR_STATE, "state can only be set before a block's first step");
+    size_t bytes = sizeof(double) * 3 * h->P.nn;
+    if (u) MSX_CUDA(cudaMemcpyAsync(h->u.p, u, bytes, cudaMemcpyHostToDevice, h->stream));
+    if (v) MSX_CUDA(cudaMemcpyAsync(h->v.p, v, bytes, cudaMemcpyHostToDevice, h->stream));
+    if (a) MSX_CUDA(cudaMemcpyAsync(h->a.p, a, bytes, cudaMemcpyHostToDevice, h->stream));
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    h->block_ready = false;
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_next_solver(msx_handle *h, const msx_bc *bcs, int64_t num_bcs, const msx_solver_opts *opts)
+{
+    if (!h) return fail(MSX_ERR_ARG, "NULL handle");
+    msx_status st;
+    if ((st = set_opts(h, opts)) != MSX_OK) return st;
+    if ((st = upload_bcs(h, bcs, num_bcs)) != MSX_OK) return st;
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_internal_force(msx_handle *h, const double *u, double *fint)
+{
+    if (!h || !u || !fint) return fail(MSX_ERR_ARG, "NULL argument");
+    size_t bytes = sizeof(double) * 3 * h->P.nn;
+    DBuf<double> du, df;
+    if (du.alloc(3 * h->P.nn) != cudaSuccess || df.alloc(3 * h->P.nn) != cudaSuccess) {
+        du.release();
+        df.release();
+        return fail(MSX_ERR_OOM, "scratch for internal force");
+    }
+    bind_problem(h);
+    Problem P = h->P;
+    P.u = du.p;
+    cudaMemcpyAsync(du.p, u, bytes, cudaMemcpyHostToDevice, h->stream);
+    if (h->precision == MSX_PREC_MIXED) {
+        long long n = 3 * P.nn;
+        split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(du.p, P.uhl, n);
+    }
+    if (h->precision == MSX_PREC_FP64_EXACT) launch_internal_force_exact(P, df.p, h->stream);
+    else if (h->precision == MSX_PREC_MIXED) launch_internal_force_mixed(P, df.p, h->stream);
+    else launch_internal_force_fp64(P, df.p, h->stream);
+    cudaMemcpyAsync(fint, df.p, bytes, cudaMemcpyDeviceToHost, h->stream);
+    cudaError_t err = cudaStreamSynchronize(h->stream);
+    du.release();
+    df.release();
+    if (err != cudaSuccess) return fail(MSX_ERR_CUDA, cudaGetErrorString(err));
+    if (h->precision == MSX_PREC_MIXED) {
+        // the split above overwrote the mixed kernel's copy of u: rebuild it
+        long long n = 3 * P.nn;
+        split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(h->u.p, h->uhl.p, n);
+        MSX_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_get_element_data(msx_handle *h, double *G, double *wJ, double *Lref, double *mass)
+{
+    if (!h) return fail(MSX_ERR_ARG, "NULL handle");
+    const long long ne = h->P.ne, nn = h->P.nn;
+    if (G) MSX_CUDA(cudaMemcpyAsync(G, h->G.p, sizeof(double) * 9 * ne, cudaMemcpyDeviceToHost, h->stream));
+    if (wJ) MSX_CUDA(cudaMemcpyAsync(wJ, h->wJ.p, sizeof(double) * ne, cudaMemcpyDeviceToHost, h->stream));
+    if (Lref) MSX_CUDA(cudaMemcpyAsync(Lref, h->Lref.p, sizeof(double) * ne, cudaMemcpyDeviceToHost, h->stream));
+    if (mass) MSX_CUDA(cudaMemcpyAsync(mass, h->mass.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, h->stream));
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_report *rep)
+{
+    if (!h || !rep || steps < 1) return fail(MSX_ERR_ARG, "bad profile arguments");
+    msx_status st;
+    if (!h->block_ready && (st = init_block(h)) != MSX_OK) return st;
+    bind_problem(h);
+    // replays start on parity 1: launch an even number of steps from parity 1
+    long long n = (steps + 1) & ~1LL;
+    std::vector<cudaEvent_t> ev(3 * n);
+    for (auto &e : ev) cudaEventCreate(&e);
+    for (long long i = 0; i < n; i++) {
+        int parity = (i & 1) ? 0 : 1;
+        cudaEventRecord(ev[3 * i], h->stream);
+        h->node(h->P, parity, h->stream);
+        cudaEventRecord(ev[3 * i + 1], h->stream);
+        h->elem(h->P, parity, h->stream);
+        cudaEventRecord(ev[3 * i + 2], h->stream);
+    }
+    cudaError_t err = cudaStreamSynchronize(h->stream);
+    double tn = 0, te = 0;
+    for (long long i = 0; i < n; i++) {
+        float a = 0, b = 0;
+        cudaEventElapsedTime(&a, ev[3 * i], ev[3 * i + 1]);
+        cudaEventElapsedTime(&b, ev[3 * i + 1], ev[3 * i + 2]);
+        tn += a;
+        te += b;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (err != cudaSuccess) return fail(MSX_ERR_CUDA, cudaGetErrorString(err));
+    MSX_CUDA(cudaMemcpy(h->h_ctrl, h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+    h->block_steps = h->h_ctrl[0].step;
+    const double ne = (double)h->P.ne, nn = (double)h->P.nn;
+    rep->element_ms = te / n;
+    rep->node_ms = tn / n;
+    rep->element_launches = n;
+    rep->node_launches = n;
+    bool mixed = h->precision == MSX_PREC_MIXED;
+    // algorithmic bytes: element data per element (conn 16 + dphi 96 + wJ 8 + Lref 8,
+    // or the FP32 set 16 + 48 + 4 + 4) and nodal state per node
+    // (read X, u, v, a 96 + m 8, write u, v, a 72)
+    rep->element_alg_bytes = ne * (mixed ? 72.0 : 128.0);
+    rep->node_alg_bytes = nn * 176.0;
+    return MSX_OK;
+}
+
+extern "C" void *msx_stream(msx_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+extern "C" msx_status msx_set_device(int32_t device)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return fail(MSX_ERR_NO_DEVICE, "no CUDA device");
+    if (device < 0 || device >= n) return fail(MSX_ERR_ARG, "device index out of range");
+    MSX_CUDA(cudaSetDevice(device));
+    return MSX_OK;
+}
+
+// Cube generator (same recipe as the test fixtures): see include/msx.h.
+static uint64_t splitmix64(uint64_t *s)
+{
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+extern "C" msx_status msx_mesh_cube(int32_t n, uint64_t seed, double jitter, double *X, int32_t *conn)
+{
+    if (n < 1 || n > 1000 || !X || !conn) return fail(MSX_ERR_ARG, "cube needs 1 <= n <= 1000 and buffers");
+    const long long m = n + 1, nn = m * m * m;
+    const double h = 1.0 / (double)n;
+    uint64_t s = seed;
+    for (long long k = 0; k < m; k++)
+        for (long long j = 0; j < m; j++)
+            for (long long i = 0; i < m; i++) {
+                long long id = i + m * j + m * m * k;
+                double c[3] = {(double)i / (double)n, (double)j / (double)n, (double)k / (double)n};
+                if (i > 0 && i < n && j > 0 && j < n && k > 0 && k < n)
+                    for (int d = 0; d < 3; d++) {
+                        double r = (double)(splitmix64(&s) >> 11) * 0x1.0p-53;
+                        c[d] += (2.0 * r - 1.0) * (jitter * h);
+                    }
+                for (int d = 0; d < 3; d++) X[d * nn + id] = c[d];
+            }
+    // C3D8 corners N1..N8 of hex (i,j,k); six tets per hex
+    static const int T[6][4] = {{1, 3, 4, 7}, {1, 2, 3, 7}, {4, 1, 7, 8}, {1, 5, 7, 8}, {1, 5, 6, 7}, {2, 1, 6, 7}};
+    long long e = 0;
+    for (long long k = 0; k < n; k++)
+        for (long long j = 0; j < n; j++)
+            for (long long i = 0; i < n; i++) {
+                int32_t N[9];
+                N[1] = (int32_t)(i + m * j + m * m * k);
+                N[2] = N[1] + 1;
+                N[3] = N[1] + 1 + (int32_t)m;
+                N[4] = N[1] + (int32_t)m;
+                for (int q = 5; q <= 8; q++) N[q] = N[q - 4] + (int32_t)(m * m);
+                for (int t = 0; t < 6; t++, e++)
+                    for (int q = 0; q < 4; q++) conn[e * 4 + q] = N[T[t][q]];
+            }
+    return MSX_OK;
+}

@@ -1,0 +1,239 @@
+"""ctypes binding of libmsx (include/msx.h) for Python callers, tests and bench.
+
+The product is the C ABI; this module only marshals arrays into it.  It loads
+the in-tree v.1.1_gb300/_build/libmsx.so and raises if that library is missing
+or if no GB300 is present: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmsx.so")
+
+OK = 0
+ERR = {0: "OK", 1: "ARG", 2: "CUDA", 3: "NEG_JACOBIAN", 4: "NAN", 5: "OOM", 6: "STATE",
+       7: "NO_DEVICE", 8: "TIMEOUT", 9: "BUSY"}
+NEO_HOOKEAN, COMPRESSIBLE_NH, STVK = 0, 1, 2
+BC_RAMP, BC_INST, BC_VEL_RAMP = 0, 1, 2
+FP64, FP64_EXACT, MIXED = 0, 1, 2
+
+
+class MsxError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("msx error %s (%d): %s" % (ERR.get(status, "?"), status, msg))
+        self.status = status
+
+
+class Mesh_(C.Structure):
+    _fields_ = [("num_nodes", C.c_int64), ("num_elems", C.c_int64), ("X", C.c_void_p),
+                ("conn", C.c_void_p), ("elem_material", C.c_void_p)]
+
+
+class Material_(C.Structure):
+    _fields_ = [("law", C.c_int32), ("reserved", C.c_int32), ("young", C.c_double),
+                ("nu", C.c_double), ("rho", C.c_double)]
+
+
+class BC_(C.Structure):
+    _fields_ = [("dof", C.c_int64), ("mode", C.c_int32), ("ramp_steps", C.c_int32), ("value", C.c_double)]
+
+
+class Opts_(C.Structure):
+    _fields_ = [("t0", C.c_double), ("tf", C.c_double), ("scale_factor", C.c_double),
+                ("max_steps", C.c_int64), ("precision", C.c_int32), ("steps_per_graph", C.c_int32)]
+
+
+class Report_(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("total_steps", C.c_int64), ("t", C.c_double), ("dt", C.c_double),
+                ("dt_init", C.c_double), ("status", C.c_int32), ("reserved", C.c_int32),
+                ("device_ms", C.c_double), ("kernel_launches", C.c_int64)]
+
+
+class Profile_(C.Structure):
+    _fields_ = [("element_ms", C.c_double), ("node_ms", C.c_double), ("element_launches", C.c_int64),
+                ("node_launches", C.c_int64), ("element_alg_bytes", C.c_double), ("node_alg_bytes", C.c_double)]
+
+
+class PoolOpts_(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_slots", C.c_int32), ("precision", C.c_int32),
+                ("elems_per_block", C.c_int32), ("steps_per_launch", C.c_int32), ("tune_cache", C.c_char_p)]
+
+
+class PoolResult_(C.Structure):
+    _fields_ = [("ticket", C.c_int64), ("status", C.c_int32), ("reserved", C.c_int32), ("steps", C.c_int64),
+                ("t", C.c_double), ("submit_to_done_ms", C.c_double)]
+
+
+# every entry point declared in include/msx.h
+SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_solver", "msx_destroy",
+           "msx_last_error", "msx_internal_force", "msx_get_element_data", "msx_profile", "msx_mesh_cube",
+           "msx_stream", "msx_set_device"]
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libmsx.so; raise if it is absent (no fallback path exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError("libmsx.so not built: run python v.1.1_gb300/build.py (%s)" % path)
+    L = C.CDLL(path)
+    vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int32
+    sig = {
+        "msx_create": [C.POINTER(Mesh_), vp, i32, vp, i64, C.POINTER(Opts_), C.POINTER(vp)],
+        "msx_run": [vp, i64, C.POINTER(Report_)],
+        "msx_get_state": [vp, vp, vp, vp],
+        "msx_set_state": [vp, vp, vp, vp],
+        "msx_next_solver": [vp, vp, i64, C.POINTER(Opts_)],
+        "msx_destroy": [vp],
+        "msx_internal_force": [vp, vp, vp],
+        "msx_get_element_data": [vp, vp, vp, vp, vp],
+        "msx_profile": [vp, i64, C.POINTER(Profile_)],
+        "msx_mesh_cube": [i32, C.c_uint64, C.c_double, vp, vp],
+        "msx_stream": [vp],
+        "msx_set_device": [i32],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.msx_last_error.restype = C.c_char_p
+    L.msx_stream.restype = vp
+    _lib = L
+    return L
+
+
+def set_device(device: int):
+    _check(load().msx_set_device(int(device)))
+
+
+def _check(st):
+    if st != OK:
+        raise MsxError(st, load().msx_last_error().decode())
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def mesh_cube(n: int, seed: int = 1234, jitter: float = 0.1):
+    """Seeded cube mesh from the library: X (3, nn), conn (ne, 4)."""
+    nn, ne = (n + 1) ** 3, 6 * n ** 3
+    X = np.zeros((3, nn))
+    conn = np.zeros((ne, 4), np.int32)
+    _check(load().msx_mesh_cube(n, seed, jitter, _p(X), _p(conn)))
+    return X, conn
+
+
+def cube_bcs(n: int, top_value: float, mode: int = BC_RAMP, ramp_steps: int = 0):
+    """Bottom face held at zero, top face z DOF driven (same recipe as the fixtures)."""
+    m = n + 1
+    nn = m ** 3
+    bottom = BC_INST if mode == BC_INST else BC_RAMP
+    ij = np.arange(m * m)
+    dof_b = np.concatenate([[(node + c * nn) for c in range(3)] for node in ij])
+    dof_t = ij + m * m * n + 2 * nn
+    rows = [(int(d), bottom, 0.0, 0) for d in dof_b] + [(int(d), mode, top_value, ramp_steps) for d in dof_t]
+    return rows
+
+
+def _bc_array(bcs):
+    arr = (BC_ * max(1, len(bcs)))()
+    for i, (dof, mode, value, ramp) in enumerate(bcs):
+        arr[i] = BC_(int(dof), int(mode), int(ramp), float(value))
+    return arr
+
+
+def _opts(t0, tf, sf, max_steps, precision, spg):
+    return Opts_(t0, tf, sf, max_steps, precision, spg)
+
+
+@dataclass
+class Report:
+    steps: int
+    total_steps: int
+    t: float
+    dt: float
+    dt_init: float
+    status: int
+    device_ms: float
+    kernel_launches: int
+
+
+class Solver:
+    """One device-resident explicit solve (mesh + materials + solver blocks)."""
+
+    def __init__(self, X, conn, materials, bcs, t0, tf, scale_factor, max_steps=0,
+                 precision=FP64, elem_material=None, steps_per_graph=0):
+        L = load()
+        self.X = np.ascontiguousarray(X, dtype=np.float64)
+        self.conn = np.ascontiguousarray(conn, dtype=np.int32)
+        self.nn, self.ne = self.X.shape[1], self.conn.shape[0]
+        em = None if elem_material is None else np.ascontiguousarray(elem_material, np.int32)
+        mesh = Mesh_(self.nn, self.ne, _p(self.X), _p(self.conn), _p(em))
+        mats = (Material_ * len(materials))()
+        for k, m in enumerate(materials):
+            law, E, nu, rho = m
+            mats[k] = Material_(int(law), 0, float(E), float(nu), float(rho))
+        barr = _bc_array(bcs)
+        opts = _opts(t0, tf, scale_factor, max_steps, precision, steps_per_graph)
+        h = C.c_void_p()
+        _check(L.msx_create(C.byref(mesh), C.cast(mats, C.c_void_p), len(materials),
+                            C.cast(barr, C.c_void_p), len(bcs), C.byref(opts), C.byref(h)))
+        self.h = h
+
+    def run(self, max_steps: int = 0) -> Report:
+        r = Report_()
+        st = load().msx_run(self.h, max_steps, C.byref(r))
+        rep = Report(r.steps, r.total_steps, r.t, r.dt, r.dt_init, r.status, r.device_ms, r.kernel_launches)
+        self.last_report = rep
+        _check(st)
+        return rep
+
+    def next_solver(self, bcs, t0, tf, scale_factor, max_steps=0, precision=FP64, steps_per_graph=0):
+        barr = _bc_array(bcs)
+        opts = _opts(t0, tf, scale_factor, max_steps, precision, steps_per_graph)
+        _check(load().msx_next_solver(self.h, C.cast(barr, C.c_void_p), len(bcs), C.byref(opts)))
+
+    def state(self):
+        u, v, a = (np.zeros(3 * self.nn) for _ in range(3))
+        _check(load().msx_get_state(self.h, _p(u), _p(v), _p(a)))
+        return u, v, a
+
+    def set_state(self, u=None, v=None, a=None):
+        conv = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (u, v, a)]
+        _check(load().msx_set_state(self.h, *[_p(x) for x in conv]))
+
+    def internal_force(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        f = np.zeros(3 * self.nn)
+        _check(load().msx_internal_force(self.h, _p(u), _p(f)))
+        return f
+
+    def element_data(self):
+        G, wJ, L, m = np.zeros(9 * self.ne), np.zeros(self.ne), np.zeros(self.ne), np.zeros(self.nn)
+        _check(load().msx_get_element_data(self.h, _p(G), _p(wJ), _p(L), _p(m)))
+        return G.reshape(9, self.ne), wJ, L, m
+
+    def profile(self, steps: int):
+        r = Profile_()
+        _check(load().msx_profile(self.h, steps, C.byref(r)))
+        return r
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().msx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
