@@ -101,7 +101,7 @@ class Clocks:
         sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
         mx = max(float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit())
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": reasons,
                 "samples": len(rows)}
 
@@ -188,6 +188,133 @@ def reference_arm(args):
             "e2e": {"value": value, "unit": "element-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def batched_variant(seed=7, count=256, steps=1000, warmup=3):
+    """256 independent solves (cube side n log-uniform in [8, 48], E log-uniform
+    in [1e5, 1e7], nu uniform in [0.25, 0.45], top velocity uniform in
+    [0.01, 0.2]) stepped together by the pool, FP32 elements / FP64 nodes,
+    1000 steps each.  The timed region starts after admission, autotuning and
+    warm-up and ends when the last solve finishes."""
+    import msx
+    rng = np.random.default_rng(seed)
+    ns = np.floor(np.exp(rng.uniform(np.log(8), np.log(49), count))).astype(int)
+    Es = np.exp(rng.uniform(np.log(1e5), np.log(1e7), count))
+    nus = rng.uniform(0.25, 0.45, count)
+    vs = rng.uniform(0.01, 0.2, count)
+    if os.path.exists(TUNE_CACHE):
+        os.remove(TUNE_CACHE)
+    P = msx.Pool(max_slots=count, precision=msx.MIXED, steps_per_launch=32, tune_cache=TUNE_CACHE)
+    total_elems = 0
+    t0 = time.perf_counter()
+    for k in range(count):
+        X, conn = msx.mesh_cube(int(ns[k]), SEED + k, 0.1)
+        t = P.submit(X, conn, (1, float(Es[k]), float(nus[k]), 1000.0),
+                     msx.cube_bcs(int(ns[k]), float(vs[k]), msx.BC_VEL_RAMP, RAMP_STEPS), steps)
+        assert t is not None, "batched workload does not fit"
+        total_elems += conn.shape[0]
+    admit_s = time.perf_counter() - t0
+    P.step(warmup)   # autotunes the schedule on the resident work, then warms up
+    before = P.stats()
+    t1 = time.perf_counter()
+    res = []
+    while len(res) < count:
+        P.step(steps)
+        res += P.poll()
+    wall = time.perf_counter() - t1
+    after = P.stats()
+    P.close()
+    timed = after["element_steps"] - before["element_steps"]
+    return {"value": timed / wall, "unit": "element-steps/s", "solves": count, "total_elems": int(total_elems),
+            "steps_per_solve": steps, "wall_s": wall, "admit_s": admit_s,
+            "all_ok": all(r["status"] == 0 and r["steps"] == steps for r in res),
+            "schedule": {"threads": before["threads"], "tile_elems": before["tile_elems"],
+                         "ctas_per_sm": before["ctas_per_sm"], "steps_per_graph": before["steps_per_launch"]}}
+
+
+TUNE_CACHE = os.path.join(os.environ.get("TMPDIR", "/tmp"), "msx_pool_schedule.txt")
+
+
+def serving_variant(lam, count=64, seed=11, max_slots=64):
+    """Request stream with Poisson arrivals at rate `lam` per second; each
+    request is a seeded cube of side n log-uniform in [8, 64], compressible
+    neo-Hookean with E log-uniform in [1e5, 1e7] and nu uniform in
+    [0.25, 0.45], and a step count uniform in [200, 2000].  Requests are
+    admitted into the pool as slots and HBM free up (continuous batching);
+    latency runs from a request's arrival to its result on the host."""
+    import msx
+    rng = np.random.default_rng(seed + int(lam))
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, count))
+    ns = np.floor(np.exp(rng.uniform(np.log(8), np.log(65), count))).astype(int)
+    steps = rng.integers(200, 2001, count)
+    Es = np.exp(rng.uniform(np.log(1e5), np.log(1e7), count))
+    nus = rng.uniform(0.25, 0.45, count)
+    vs = rng.uniform(0.01, 0.2, count)
+    work = sum(6 * int(n) ** 3 * int(st) for n, st in zip(ns, steps))
+
+    def request(k):
+        X, conn = msx.mesh_cube(int(ns[k]), SEED + 1000 + k, 0.1)
+        return X, conn, (1, float(Es[k]), float(nus[k]), 1000.0), \
+            msx.cube_bcs(int(ns[k]), float(vs[k]), msx.BC_VEL_RAMP, RAMP_STEPS), int(steps[k])
+
+    # continuous batching in the pool
+    P = msx.Pool(max_slots=max_slots, precision=msx.MIXED, steps_per_launch=16, tune_cache=TUNE_CACHE)
+    start = time.perf_counter()
+    queue, nxt, owner, lat = [], 0, {}, {}
+    while len(lat) < count:
+        now = time.perf_counter() - start
+        while nxt < count and arrivals[nxt] <= now:
+            queue.append(nxt)
+            nxt += 1
+        while queue:
+            t = P.submit(*request(queue[0]))
+            if t is None:
+                break
+            owner[t] = queue.pop(0)
+        if len(owner) > len(lat):
+            P.step(1)
+        elif nxt < count:
+            time.sleep(max(0.0, min(0.01, arrivals[nxt] - (time.perf_counter() - start))))
+        for r in P.poll():
+            k = owner[r["ticket"]]
+            lat[k] = (time.perf_counter() - start) - arrivals[k]
+            P.fetch(r["ticket"])
+    wall = time.perf_counter() - start
+    P.close()
+    L = np.array([lat[k] for k in range(count)]) * 1e3
+    return {"lambda_per_s": lam, "requests": count, "value": work / wall, "unit": "element-steps/s",
+            "p50_ms": float(np.percentile(L, 50)), "p99_ms": float(np.percentile(L, 99)), "wall_s": wall}
+
+
+def serving_sequential_fp64(lam, count=64, seed=11):
+    """The same request stream served one solve at a time by the plain FP64 path."""
+    import msx
+    rng = np.random.default_rng(seed + int(lam))
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, count))
+    ns = np.floor(np.exp(rng.uniform(np.log(8), np.log(65), count))).astype(int)
+    steps = rng.integers(200, 2001, count)
+    Es = np.exp(rng.uniform(np.log(1e5), np.log(1e7), count))
+    nus = rng.uniform(0.25, 0.45, count)
+    vs = rng.uniform(0.01, 0.2, count)
+    work = sum(6 * int(n) ** 3 * int(st) for n, st in zip(ns, steps))
+    start = time.perf_counter()
+    lat = []
+    for k in range(count):
+        now = time.perf_counter() - start
+        if arrivals[k] > now:
+            time.sleep(arrivals[k] - now)
+        X, conn = msx.mesh_cube(int(ns[k]), SEED + 1000 + k, 0.1)
+        S = msx.Solver(X, conn, [(1, float(Es[k]), float(nus[k]), 1000.0)],
+                       msx.cube_bcs(int(ns[k]), float(vs[k]), msx.BC_VEL_RAMP, RAMP_STEPS), 0.0, 1e30, 0.5,
+                       max_steps=int(steps[k]), precision=msx.FP64)
+        S.run()
+        S.state()
+        S.close()
+        lat.append((time.perf_counter() - start) - arrivals[k])
+    wall = time.perf_counter() - start
+    L = np.array(lat) * 1e3
+    return {"lambda_per_s": lam, "requests": count, "value": work / wall, "unit": "element-steps/s",
+            "p50_ms": float(np.percentile(L, 50)), "p99_ms": float(np.percentile(L, 99)), "wall_s": wall}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -220,6 +347,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-pool", action="store_true", help="skip the batched and serving variants")
     ap.add_argument("--cube", type=int, default=N_CUBE, help="hexes per cube edge (profiling runs only)")
     ap.add_argument("--only", choices=["fp64", "mixed", "fp64_exact"], default=None,
                     help="time a single variant (profiling runs only)")
@@ -256,6 +384,10 @@ def main():
             variants[name] = {"value": ws * ne * args.steps / s2, "ms_per_step": 1e3 * s2 / args.steps,
                               "element_kernel_ms": p2.element_ms, "node_kernel_ms": p2.node_ms,
                               "clocks": c2}
+    if not args.no_pool and args.only is None and args.cube == N_CUBE:
+        variants["batched"] = batched_variant()
+        variants["serving"] = [serving_variant(lam) for lam in (50, 200, 800)]
+        variants["serving_one_at_a_time_fp64"] = serving_sequential_fp64(200)
     e2e = None
     if not args.no_e2e and args.only is None:
         wall, r3, h2d, d2h = run_e2e(X, conn, bcs, args.steps)

@@ -154,6 +154,55 @@ void *msx_stream(msx_handle *h);
  * (one process per GPU: pass the local rank). */
 msx_status msx_set_device(int32_t device);
 
+/* ------------------------------------------------------------------------
+ * Batched / serving pool: many independent solves resident on the device,
+ * stepped together by one persistent, graph-captured step kernel pair.
+ * Each solve is one mesh + material + BCs + solver block (tf or max_steps).
+ * ------------------------------------------------------------------------ */
+typedef struct msx_pool msx_pool;
+
+typedef struct {
+    int64_t hbm_budget_bytes;     /* admission limit for resident solves (0 = 80% free) */
+    int32_t max_slots;            /* concurrent solves                                   */
+    int32_t precision;            /* MSX_PREC_FP64 or MSX_PREC_MIXED                    */
+    int32_t elems_per_block;      /* element-kernel CTA size; 0 = autotuned             */
+    int32_t steps_per_launch;     /* steps per graph replay; 0 = default                */
+    const char *tune_cache;       /* autotuner cache file, or NULL                       */
+} msx_pool_opts;
+
+typedef struct {
+    int64_t ticket;
+    int32_t status;               /* msx_status of the solve                            */
+    int32_t reserved;
+    int64_t steps;
+    double t;
+    double submit_to_done_ms;     /* wall latency from submit to completion            */
+} msx_pool_result;
+
+msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out);
+/* Admit a solve (copies host inputs); MSX_ERR_BUSY if slots/HBM are full. */
+msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const msx_material *mat,
+                           const msx_bc *bcs, int64_t num_bcs, const msx_solver_opts *opts,
+                           int64_t *ticket);
+/* Advance every resident solve by up to `steps` steps (one graph replay). */
+msx_status msx_pool_step(msx_pool *p, int64_t steps);
+/* Collect finished solves: fills up to max results, returns the count in *n.
+ * u (3*num_nodes of that solve) is copied out by msx_pool_fetch. */
+msx_status msx_pool_poll(msx_pool *p, msx_pool_result *results, int32_t max, int32_t *n);
+msx_status msx_pool_fetch(msx_pool *p, int64_t ticket, double *u, double *v, double *a);
+msx_status msx_pool_destroy(msx_pool *p);
+
+typedef struct {
+    int32_t active, finished_unfetched;   /* resident solves; results awaiting fetch      */
+    int32_t threads, tile_elems;          /* schedule in use (after autotuning)            */
+    int32_t ctas_per_sm, steps_per_launch;
+    int64_t element_steps;                /* sum over all solves of elements x steps done  */
+    int64_t used_bytes, budget_bytes;     /* HBM held by resident solves / admission limit */
+} msx_pool_stats;
+
+/* Counters of the pool (reads the device control table). */
+msx_status msx_pool_stats_get(msx_pool *p, msx_pool_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

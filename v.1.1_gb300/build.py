@@ -25,6 +25,7 @@ UNITS = {
     "msx_runtime.cu": [],
     "msx_pool.cu": [],
 }
+DECK = os.path.join(OUT, "msx_deck")
 
 
 def nvcc():
@@ -65,6 +66,12 @@ def build(force=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stderr)
     os.replace(tmp, LIB)
+    deck = os.path.join(OUT, "msx_deck")
+    cxx = shutil.which("g++") or "c++"
+    r = subprocess.run([cxx, "-O2", "-std=c++17", os.path.join(CSRC, "msx_deck.cpp"), "-o", deck, "-L" + OUT,
+                        "-lmsx", "-Wl,-rpath,$ORIGIN"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("msx_deck build failed:\n" + r.stderr)
     return LIB
 
 

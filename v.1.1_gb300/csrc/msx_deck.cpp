@@ -1,0 +1,301 @@
+// msx_deck.cpp -- input-deck front end: runs an explicit C3D4 deck through
+// the C ABI, as `MuPhiSim -input <deck>` runs it through the reference's
+// solver chain (src/main.cpp:37-217).
+//
+//   msx_deck -input deck.inp [-inputDir d] [-precision fp64|exact|mixed]
+//            [-dump final.bin] [-csv final.csv] [-parse-only]
+//
+// Keyword subset (src/IO/inputFile.cpp): *Node (:20-108), *Element, type=C3D4
+// (:118-323), *FEM Nodes / *FEM Elements, *MATERIAL with *Density,
+// *HyperElastic {Neo-Hookean | 3D-Compressible-Neo-Hookean |
+// St-Venant-Kirchhoff} and *List of Elements (:838-1029, 2010-2053),
+// *SOLVER, EXPLICIT ... *END SOLVER with *Scale Factor, *Outputs, *Time and
+// *BOUNDARY, TYPE=DISPLACEMENT RAMP|INST (:2253-2831, 2960-3218).  Other
+// keywords belong to paths this library does not implement and are refused.
+// As in the reference, a RAMP BC stores U/(tf - t0) with the *Time read so
+// far, and once an INST block has been read every later displacement block
+// is instantaneous (the flag is not reset between solvers).
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/msx.h"
+
+namespace {
+
+struct SolverBlock {
+    double sf = 1, t0 = 0, tf = 0;
+    int outputs = -1;
+    std::vector<msx_bc> bcs;
+};
+
+struct Deck {
+    std::vector<double> xyz;          // node-major while reading
+    std::vector<int32_t> conn;
+    std::vector<msx_material> mats;
+    std::vector<int32_t> elem_mat;    // -1 until assigned
+    std::vector<SolverBlock> solvers;
+};
+
+std::string trim(const std::string &s)
+{
+    size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+    return a == std::string::npos ? "" : s.substr(a, b - a + 1);
+}
+
+bool starts(const std::string &s, const char *p) { return s.compare(0, strlen(p), p) == 0; }
+
+std::vector<std::string> split(const std::string &s)
+{
+    std::vector<std::string> out;
+    std::stringstream ss(s);
+    std::string item;
+    while (std::getline(ss, item, ',')) out.push_back(trim(item));
+    return out;
+}
+
+[[noreturn]] void die(const std::string &msg, int line)
+{
+    fprintf(stderr, "msx_deck: %s (line %d)\n", msg.c_str(), line);
+    exit(2);
+}
+
+Deck parse(const std::string &path)
+{
+    std::ifstream in(path);
+    if (!in) die("cannot open " + path, 0);
+    std::vector<std::string> lines;
+    for (std::string l; std::getline(in, l);) lines.push_back(trim(l));
+    Deck d;
+    bool instantaneous = false;
+    const size_t n = lines.size();
+    size_t i = 0;
+    auto data_line = [&](size_t k) { return k < n && !lines[k].empty() && lines[k][0] != '*'; };
+    while (i < n) {
+        const std::string &L = lines[i];
+        int ln = (int)i + 1;
+        if (L.empty() || starts(L, "**")) {
+            i++;
+        } else if (starts(L, "*Node")) {
+            for (i++; data_line(i); i++) {
+                auto f = split(lines[i]);
+                if (f.size() != 4) die("a 3D node line has id, x, y, z", (int)i + 1);
+                if (atoi(f[0].c_str()) != (int)d.xyz.size() / 3 + 1) die("node ids must be 1..N in order", (int)i + 1);
+                for (int c = 1; c < 4; c++) d.xyz.push_back(atof(f[c].c_str()));
+            }
+        } else if (starts(L, "*Element")) {
+            if (L.find("C3D4") == std::string::npos) die("only *Element, type=C3D4 is supported", ln);
+            for (i++; data_line(i); i++) {
+                auto f = split(lines[i]);
+                if (f.size() != 5) die("a C3D4 line has id and 4 nodes", (int)i + 1);
+                for (int c = 1; c < 5; c++) d.conn.push_back(atoi(f[c].c_str()) - 1);
+            }
+        } else if (starts(L, "*FEM Nodes") || starts(L, "*FEM Elements")) {
+            if (i + 1 >= n || !starts(lines[i + 1], "All")) die("only 'All' FEM sets are supported", ln);
+            i += 2;
+        } else if (starts(L, "*MATERIAL")) {
+            msx_material m{};
+            m.law = -1;
+            bool have_rho = false;
+            int id = (int)d.mats.size();
+            for (i++; i < n && !starts(lines[i], "*MATERIAL") && !starts(lines[i], "*END") && !starts(lines[i], "*SOLVER");) {
+                const std::string &K = lines[i];
+                if (starts(K, "*Density")) {
+                    m.rho = atof(lines[i + 1].c_str());
+                    have_rho = true;
+                    i += 2;
+                } else if (starts(K, "*HyperElastic")) {
+                    std::string law = trim(K.substr(K.find(',') + 1));
+                    if (law == "Neo-Hookean") m.law = MSX_LAW_NEO_HOOKEAN;
+                    else if (law == "3D-Compressible-Neo-Hookean") m.law = MSX_LAW_COMPRESSIBLE_NEO_HOOKEAN;
+                    else if (law == "St-Venant-Kirchhoff") m.law = MSX_LAW_STVK;
+                    else die("unsupported law " + law, (int)i + 1);
+                    auto f = split(lines[i + 1]);
+                    if (f.size() < 2) die("*HyperElastic needs E, nu", (int)i + 2);
+                    m.young = atof(f[0].c_str());
+                    m.nu = atof(f[1].c_str());
+                    i += 2;
+                } else if (starts(K, "*List of Elements")) {
+                    if (d.elem_mat.size() != d.conn.size() / 4) d.elem_mat.assign(d.conn.size() / 4, -1);
+                    if (starts(lines[i + 1], "All")) {
+                        for (auto &e : d.elem_mat) e = id;
+                    } else {
+                        // the reference reads one element id per keyword
+                        int e = atoi(lines[i + 1].c_str()) - 1;
+                        if (e < 0 || e >= (int)d.elem_mat.size()) die("element id out of range", (int)i + 2);
+                        d.elem_mat[e] = id;
+                    }
+                    i += 2;
+                } else if (K.empty()) {
+                    i++;
+                } else {
+                    die("unsupported material keyword " + K, (int)i + 1);
+                }
+            }
+            if (m.law < 0 || !have_rho) die("material needs *Density and *HyperElastic", ln);
+            d.mats.push_back(m);
+        } else if (starts(L, "*SOLVER")) {
+            if (trim(L.substr(L.find(',') + 1)) != "EXPLICIT") die("only *SOLVER, EXPLICIT is supported", ln);
+            SolverBlock s;
+            bool have_time = false;
+            for (i++; i < n && !starts(lines[i], "*END SOLVER"); ) {
+                const std::string &K = lines[i];
+                if (starts(K, "*Scale Factor")) {
+                    s.sf = atof(lines[i + 1].c_str());
+                    i += 2;
+                } else if (starts(K, "*Outputs")) {
+                    s.outputs = atoi(lines[i + 1].c_str());
+                    i += 2;
+                    if (data_line(i)) i++;   // optional variable list
+                } else if (starts(K, "*Time")) {
+                    auto f = split(lines[i + 1]);
+                    if (f.size() != 2) die("*Time needs t0, tf", (int)i + 2);
+                    s.t0 = atof(f[0].c_str());
+                    s.tf = atof(f[1].c_str());
+                    have_time = true;
+                    i += 2;
+                } else if (starts(K, "*BOUNDARY, TYPE=DISPLACEMENT")) {
+                    // the reference divides a ramp by the *Time read before it
+                    if (!have_time) die("put *Time before *BOUNDARY in a solver block", (int)i + 1);
+                    if (K.find("INST") != std::string::npos) instantaneous = true;
+                    else if (K.find("RAMP") == std::string::npos) die("unknown displacement BC type", (int)i + 1);
+                    for (i++; data_line(i); i++) {
+                        auto f = split(lines[i]);
+                        if (f.size() != 3) die("a BC line has node, direction, value", (int)i + 1);
+                        msx_bc b{};
+                        long long node = atoll(f[0].c_str()) - 1, dir = atoll(f[1].c_str());
+                        long long nn = (long long)d.xyz.size() / 3;
+                        if (node < 0 || node >= nn || dir < 0 || dir > 2) die("BC node/direction out of range", (int)i + 1);
+                        b.dof = node + dir * nn;
+                        b.mode = instantaneous ? MSX_BC_INST : MSX_BC_RAMP;
+                        // a ramp is U/(tf - t0) with the *Time read so far: pass U and
+                        // make the library divide by this block's own duration
+                        b.value = atof(f[2].c_str());
+                        s.bcs.push_back(b);
+                    }
+                } else if (K.empty()) {
+                    i++;
+                } else {
+                    die("unsupported solver keyword " + K, (int)i + 1);
+                }
+            }
+            if (s.outputs < 0) die("*Outputs is required in an explicit solver block", ln);
+            d.solvers.push_back(s);
+            i++;
+        } else if (starts(L, "*END")) {
+            break;
+        } else {
+            die("unsupported keyword " + L, ln);
+        }
+    }
+    if (d.xyz.size() < 12 || d.conn.empty()) die("deck needs nodes and C3D4 elements", 0);
+    if (d.mats.empty() || d.solvers.empty()) die("deck needs a material and a solver block", 0);
+    if (!d.elem_mat.empty())
+        for (int32_t m : d.elem_mat)
+            if (m < 0) die("an element has no material", 0);
+    return d;
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+    std::string input, dir = ".", dump, csv;
+    int precision = MSX_PREC_FP64;
+    bool parse_only = false;
+    for (int k = 1; k < argc; k++) {
+        std::string a = argv[k];
+        auto next = [&]() { return k + 1 < argc ? std::string(argv[++k]) : std::string(); };
+        if (a == "-input") input = next();
+        else if (a == "-inputDir") dir = next();
+        else if (a == "-dump") dump = next();
+        else if (a == "-csv") csv = next();
+        else if (a == "-parse-only") parse_only = true;
+        else if (a == "-precision") {
+            std::string p = next();
+            precision = p == "exact" ? MSX_PREC_FP64_EXACT : (p == "mixed" ? MSX_PREC_MIXED : MSX_PREC_FP64);
+        }
+    }
+    if (input.empty()) {
+        fprintf(stderr, "usage: msx_deck -input deck.inp [-inputDir d] [-precision fp64|exact|mixed] "
+                        "[-dump f.bin] [-csv f.csv] [-parse-only]\n");
+        return 2;
+    }
+    Deck d = parse(dir + "/" + input);
+    const long long nn = (long long)d.xyz.size() / 3, ne = (long long)d.conn.size() / 4;
+    std::vector<double> X(3 * nn);
+    for (long long i = 0; i < nn; i++)
+        for (int c = 0; c < 3; c++) X[c * nn + i] = d.xyz[3 * i + c];
+    if (parse_only) {
+        size_t nbc = 0;
+        for (auto &s : d.solvers) nbc += s.bcs.size();
+        printf("{\"nodes\": %lld, \"elements\": %lld, \"materials\": %zu, \"solvers\": %zu, \"bcs\": %zu",
+               nn, ne, d.mats.size(), d.solvers.size(), nbc);
+        printf(", \"blocks\": [");
+        for (size_t k = 0; k < d.solvers.size(); k++)
+            printf("%s{\"t0\": %.17g, \"tf\": %.17g, \"sf\": %.17g, \"bcs\": %zu, \"inst\": %d}", k ? ", " : "",
+                   d.solvers[k].t0, d.solvers[k].tf, d.solvers[k].sf, d.solvers[k].bcs.size(),
+                   d.solvers[k].bcs.empty() ? 0 : d.solvers[k].bcs[0].mode == MSX_BC_INST);
+        printf("]}\n");
+        return 0;
+    }
+    msx_mesh mesh{nn, ne, X.data(), d.conn.data(), d.elem_mat.empty() ? nullptr : d.elem_mat.data()};
+    msx_handle *h = nullptr;
+    long long total = 0;
+    for (size_t k = 0; k < d.solvers.size(); k++) {
+        const SolverBlock &s = d.solvers[k];
+        msx_solver_opts o{s.t0, s.tf, s.sf, 0, precision, 0};
+        msx_status st;
+        if (k == 0) {
+            st = msx_create(&mesh, d.mats.data(), (int32_t)d.mats.size(), s.bcs.data(), (int64_t)s.bcs.size(), &o, &h);
+        } else {
+            // src/main.cpp:171-179: time continuity between solvers
+            if (s.t0 - d.solvers[k - 1].tf > 1E-12) {
+                fprintf(stderr, "msx_deck: This is not continuity in time between solvers\n");
+                return 1;
+            }
+            st = msx_next_solver(h, s.bcs.data(), (int64_t)s.bcs.size(), &o);
+        }
+        if (st != MSX_OK) {
+            fprintf(stderr, "msx_deck: %s\n", msx_last_error());
+            return 1;
+        }
+        msx_run_report r{};
+        st = msx_run(h, 0, &r);
+        total += r.steps;
+        printf("solver %zu: %lld steps, t = %.9g, dt = %.6g, device %.3f ms\n", k, (long long)r.steps, r.t, r.dt,
+               r.device_ms);
+        if (st != MSX_OK) {
+            fprintf(stderr, "msx_deck: %s\n", msx_last_error());
+            return 1;
+        }
+    }
+    std::vector<double> u(3 * nn), v(3 * nn), a(3 * nn);
+    msx_get_state(h, u.data(), v.data(), a.data());
+    if (!dump.empty()) {
+        FILE *f = fopen(dump.c_str(), "wb");
+        if (!f) return 3;
+        fwrite(u.data(), sizeof(double), u.size(), f);
+        fwrite(v.data(), sizeof(double), v.size(), f);
+        fwrite(a.data(), sizeof(double), a.size(), f);
+        fclose(f);
+    }
+    if (!csv.empty()) {
+        // full precision, as the reference's node extraction writes (dataExtraction.cpp:282-300)
+        FILE *f = fopen(csv.c_str(), "w");
+        if (!f) return 3;
+        fprintf(f, "node,ux,uy,uz,vx,vy,vz\n");
+        for (long long i = 0; i < nn; i++)
+            fprintf(f, "%lld,%.16g,%.16g,%.16g,%.16g,%.16g,%.16g\n", i + 1, u[i], u[nn + i], u[2 * nn + i], v[i],
+                    v[nn + i], v[2 * nn + i]);
+        fclose(f);
+    }
+    printf("total %lld steps\n", total);
+    msx_destroy(h);
+    return 0;
+}

@@ -190,6 +190,7 @@ __device__ __forceinline__ void block_min_to(double v, unsigned long long *slot)
         for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
         if (l == 0 && v < INFINITY) atomicMin(slot, (unsigned long long)__double_as_longlong(v));
     }
+    __syncthreads();   // wmin may be reused by the next call
 }
 
 // The control decision of the node kernel: derived identically in every
@@ -233,7 +234,10 @@ __device__ __forceinline__ StepDecision decide_step(const Problem &p, const Ctrl
             d.run = true;
         }
     } else {
+        // stopped at tf or at the step limit: keep the CFL min of the next step
+        // so that a later call can resume the block where it left off
         d.next.stop = 1;
+        d.next.pending = p.dtmin[parity];
     }
     return d;
 }
@@ -256,18 +260,8 @@ __device__ __forceinline__ double bc_increment(const BCEntry &b, double dt, long
 // One thread per node, three components.
 // ---------------------------------------------------------------------------
 template <int MODE>
-__global__ void __launch_bounds__(kNodeBlock) node_kernel(Problem p, int parity)
+__device__ __forceinline__ void node_body(const Problem &p, long long i, const Ctrl &cp, const StepDecision &d)
 {
-    const Ctrl cp = p.ctrl[parity ^ 1];
-    StepDecision d = decide_step(p, cp, parity);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        p.ctrl[parity] = d.next;
-        p.dtmin[parity ^ 1] = MSX_INF_BITS;
-        p.flags[parity ^ 1] = 0;
-    }
-    if (!cp.ran && !d.run) return;
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.nn) return;
     const long long nn = p.nn;
     int rec = p.node_bc[i];
     int2 br[3] = {make_int2(0, 0), make_int2(0, 0), make_int2(0, 0)};
@@ -349,19 +343,36 @@ __global__ void __launch_bounds__(kNodeBlock) node_kernel(Problem p, int parity)
     }
 }
 
+// Writes the new control slot and clears the slots the element kernel fills.
+__device__ __forceinline__ void publish_step(const Problem &p, const StepDecision &d, int parity)
+{
+    p.ctrl[parity] = d.next;
+    p.dtmin[parity ^ 1] = MSX_INF_BITS;
+    p.flags[parity ^ 1] = 0;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kNodeBlock) node_kernel(Problem p, int parity)
+{
+    const Ctrl cp = p.ctrl[parity ^ 1];
+    StepDecision d = decide_step(p, cp, parity);
+    if (blockIdx.x == 0 && threadIdx.x == 0) publish_step(p, d, parity);
+    if (!cp.ran && !d.run) return;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < p.nn) node_body<MODE>(p, i, cp, d);
+}
+
 // ---------------------------------------------------------------------------
 // Element kernels: F, P, wJ B^T P corner forces and the deformed CFL length.
 // ---------------------------------------------------------------------------
 
 // Reference operation order (used with contraction off).
 template <bool FORCE_ONLY>
-__global__ void __launch_bounds__(kElemBlock) elem_kernel_exact(Problem p, int parity)
+__device__ __forceinline__ double elem_body_exact(const Problem &p, long long e, int parity)
 {
-    if (!FORCE_ONLY && !p.ctrl[parity].ran) return;
     const long long ne = p.ne, nn = p.nn;
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double vmin = INFINITY;
-    if (e < ne) {
+    {
         int4 cn = p.conn[e];
         int nd[4] = {cn.x, cn.y, cn.z, cn.w};
         double dphi[12];
@@ -417,7 +428,16 @@ __global__ void __launch_bounds__(kElemBlock) elem_kernel_exact(Problem p, int p
             if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
         }
     }
-    if (!FORCE_ONLY) block_min_to(vmin, p.dtmin + (parity ^ 1));
+    return vmin;
+}
+
+template <bool FORCE_ONLY>
+__global__ void __launch_bounds__(kElemBlock) elem_kernel_exact(Problem p, int parity)
+{
+    if (!FORCE_ONLY && !p.ctrl[parity].ran) return;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double v = e < p.ne ? elem_body_exact<FORCE_ONLY>(p, e, parity) : INFINITY;
+    if (!FORCE_ONLY) block_min_to(v, p.dtmin + (parity ^ 1));
 }
 
 // Plain FP64 with contraction: H from node differences, laws written through
@@ -499,13 +519,11 @@ __device__ __forceinline__ T char_length_edges(const T *e1, const T *e2, const T
 }
 
 template <bool FORCE_ONLY>
-__global__ void __launch_bounds__(kElemBlock) elem_kernel_fp64(Problem p, int parity)
+__device__ __forceinline__ double elem_body_fp64(const Problem &p, long long e, int parity)
 {
-    if (!FORCE_ONLY && !p.ctrl[parity].ran) return;
     const long long ne = p.ne, nn = p.nn;
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double vmin = INFINITY;
-    if (e < ne) {
+    {
         int4 cn = p.conn[e];
         int nd[4] = {cn.x, cn.y, cn.z, cn.w};
         double G[9];
@@ -558,7 +576,16 @@ __global__ void __launch_bounds__(kElemBlock) elem_kernel_fp64(Problem p, int pa
             if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
         }
     }
-    if (!FORCE_ONLY) block_min_to(vmin, p.dtmin + (parity ^ 1));
+    return vmin;
+}
+
+template <bool FORCE_ONLY>
+__global__ void __launch_bounds__(kElemBlock) elem_kernel_fp64(Problem p, int parity)
+{
+    if (!FORCE_ONLY && !p.ctrl[parity].ran) return;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double v = e < p.ne ? elem_body_fp64<FORCE_ONLY>(p, e, parity) : INFINITY;
+    if (!FORCE_ONLY) block_min_to(v, p.dtmin + (parity ^ 1));
 }
 
 // ---------------------------------------------------------------------------
@@ -630,13 +657,11 @@ __device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H,
 }
 
 template <bool FORCE_ONLY>
-__global__ void __launch_bounds__(kElemBlock) elem_kernel_mixed(Problem p, int parity)
+__device__ __forceinline__ double elem_body_mixed(const Problem &p, long long e, int parity)
 {
-    if (!FORCE_ONLY && !p.ctrl[parity].ran) return;
     const long long ne = p.ne, nn = p.nn;
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double vmin = INFINITY;
-    if (e < ne) {
+    {
         int4 cn = p.conn[e];
         int nd[4] = {cn.x, cn.y, cn.z, cn.w};
         float G[9];
@@ -703,7 +728,63 @@ __global__ void __launch_bounds__(kElemBlock) elem_kernel_mixed(Problem p, int p
             if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
         }
     }
-    if (!FORCE_ONLY) block_min_to(vmin, p.dtmin + (parity ^ 1));
+    return vmin;
+}
+
+template <bool FORCE_ONLY>
+__global__ void __launch_bounds__(kElemBlock) elem_kernel_mixed(Problem p, int parity)
+{
+    if (!FORCE_ONLY && !p.ctrl[parity].ran) return;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double v = e < p.ne ? elem_body_mixed<FORCE_ONLY>(p, e, parity) : INFINITY;
+    if (!FORCE_ONLY) block_min_to(v, p.dtmin + (parity ^ 1));
+}
+
+
+// ---------------------------------------------------------------------------
+// Pooled kernels: many independent solves stepped by one persistent grid.
+// Each tile is a contiguous element (or node) range of one solve; CTAs stride
+// over the tile list, so the grid size is fixed (a multiple of the SM count)
+// and the same graph serves any admitted set.  Per-solve control, CFL slot
+// and NaN flag are those of the solve's Problem.
+// ---------------------------------------------------------------------------
+struct Tile {
+    int solve;
+    int begin, end;
+};
+
+template <int MODE>
+__global__ void pool_node_kernel(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
+                                 const int *__restrict__ ntiles, int parity)
+{
+    const int n = *ntiles;
+    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+        const Tile tl = tiles[t];
+        const Problem &p = descs[tl.solve];
+        const Ctrl cp = p.ctrl[parity ^ 1];
+        StepDecision d = decide_step(p, cp, parity);
+        if (tl.begin == 0 && threadIdx.x == 0) publish_step(p, d, parity);
+        if (!cp.ran && !d.run) continue;
+        for (long long i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x) node_body<MODE>(p, i, cp, d);
+    }
+}
+
+template <int MODE>
+__global__ void pool_elem_kernel(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
+                                 const int *__restrict__ ntiles, int parity)
+{
+    const int n = *ntiles;
+    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+        const Tile tl = tiles[t];
+        const Problem &p = descs[tl.solve];
+        if (!p.ctrl[parity].ran) continue;
+        double v = INFINITY;
+        for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
+            double w = MODE == MODE_MIXED ? elem_body_mixed<false>(p, e, parity) : elem_body_fp64<false>(p, e, parity);
+            v = fmin(v, w);
+        }
+        block_min_to(v, p.dtmin + (parity ^ 1));
+    }
 }
 
 #ifdef MSX_SETUP_KERNELS

@@ -44,6 +44,7 @@ struct Ctrl {
     int stop;            // 1: block finished (tf reached, limit hit or error)
     int status;          // msx_status
     int pad;
+    unsigned long long pending;  // CFL min for the next step, saved when a block stops
 };
 
 struct Problem {
@@ -80,6 +81,9 @@ struct Problem {
     int *flags;                       // [2] NaN flag raised by the element kernel
     double sf, tf;
 };
+
+// records the message returned by msx_last_error() on this host thread
+void msx_set_error(const char *msg);
 
 // launchers (one translation unit per numeric mode)
 void launch_node_exact(const Problem &p, int parity, cudaStream_t s);

@@ -1,0 +1,625 @@
+// msx_pool.cu -- batched / serving pool of independent explicit solves.
+//
+// Every admitted solve owns one device arena (mesh, set-up data, nodal state,
+// corner forces, CSR, Dirichlet tables) and one entry of the pool's control,
+// CFL and NaN-flag tables.  All resident solves advance together: one pooled
+// node kernel and one pooled element kernel per step, persistent grids that
+// stride over a tile list (tile = contiguous element or node range of one
+// solve), captured as a CUDA graph of `steps_per_launch` steps.  Admission is
+// by HBM footprint; finished solves are copied out, freed and replaced
+// between graph replays (continuous batching).  Tile size, CTA size and grid
+// size are picked by timing candidates on the resident work.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/msx.h"
+#include "msx_device.cuh"
+
+using namespace msx;
+
+namespace {
+
+msx_status pfail(msx_status st, const std::string &m)
+{
+    msx_set_error(m.c_str());
+    return st;
+}
+
+#define PCUDA(call)                                                                          \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return pfail(e_ == cudaErrorMemoryAllocation ? MSX_ERR_OOM : MSX_ERR_CUDA,        \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+    } while (0)
+
+__global__ void pool_init_ctrl(Problem p, double t0, long long limit)
+{
+    double dt0 = __longlong_as_double((long long)p.dtmin[0]) * p.sf;
+    Ctrl c;
+    c.t = t0;
+    c.dt = dt0;
+    c.step = 0;
+    c.limit = limit;
+    c.ran = 0;
+    c.stop = 0;
+    c.status = 0;
+    c.pad = 0;
+    c.pending = 0;
+    p.ctrl[0] = c;
+    p.ctrl[1] = c;
+    p.flags[0] = 0;
+    p.flags[1] = 0;
+}
+
+double now_ms()
+{
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Slot {
+    bool active = false;
+    long long ticket = -1;
+    long long nn = 0, ne = 0;
+    void *arena = nullptr;
+    size_t bytes = 0;
+    Problem P{};
+    double submit_ms = 0;
+};
+
+struct Finished {
+    msx_pool_result res;
+    std::vector<double> u, v, a;
+};
+
+struct Sched {
+    int threads = 256;
+    int tile_elems = 1024;
+    int ctas_per_sm = 4;
+};
+
+}  // namespace
+
+struct msx_pool {
+    std::mutex mu;
+    msx_pool_opts opts{};
+    int device = 0, sms = 152;
+    cudaStream_t stream = nullptr;
+    std::vector<Slot> slots;
+    Problem *d_descs = nullptr;
+    Ctrl *d_ctrl = nullptr, *h_ctrl = nullptr;
+    unsigned long long *d_dtmin = nullptr;
+    int *d_flags = nullptr;
+    Tile *d_etiles = nullptr, *d_ntiles = nullptr;
+    int *d_counts = nullptr;   // [0] element tiles, [1] node tiles
+    size_t tile_cap = 0;
+    std::vector<Tile> h_etiles, h_ntiles;
+    bool tiles_dirty = true;
+    cudaGraphExec_t graph = nullptr;
+    Sched sched;
+    bool tuned = false;
+    int spl = 32;
+    long long next_ticket = 1;
+    size_t used = 0, budget = 0;
+    std::map<long long, Finished> done;
+    std::deque<long long> done_order;
+    long long elem_steps_finished = 0;   // element-steps of solves already collected
+    long long elem_steps_active = 0;     // element-steps of resident solves at the last read
+};
+
+// ------------------------------------------------------------------ helpers
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+static size_t footprint(long long nn, long long ne, long long nbc, int precision)
+{
+    size_t b = 0;
+    b += align256(sizeof(int4) * ne) + align256(sizeof(double) * 9 * ne);           // conn, G
+    b += 2 * align256(sizeof(double) * ne);                                         // wJ, Lref
+    b += 2 * align256(sizeof(float) * 9 * ne) + 2 * align256(sizeof(float) * ne);    // G32, Eref32, wJ32, Lref32
+    b += 4 * align256(sizeof(double) * 3 * nn) + 2 * align256(sizeof(double) * nn);  // X, u, v, a, mass, minv
+    b += align256(sizeof(float2) * 3 * nn);                                          // uhl
+    b += precision == MSX_PREC_MIXED ? align256(sizeof(float) * 12 * ne) : align256(sizeof(double) * 12 * ne);
+    b += align256(sizeof(int) * (nn + 1)) + align256(sizeof(int) * 4 * ne) + align256(sizeof(int) * nn);
+    b += align256(sizeof(int2) * 3 * nn) + align256(sizeof(BCEntry) * (nbc > 0 ? nbc : 1));
+    return b;
+}
+
+static msx_status make_mat(const msx_material &m, MatParams &o)
+{
+    if (m.law < 0 || m.law > 2) return pfail(MSX_ERR_ARG, "unknown constitutive law");
+    if (!(m.young > 0) || !(m.rho > 0) || !(m.nu > -1.0) || !(m.nu < 0.5))
+        return pfail(MSX_ERR_ARG, "material needs E > 0, rho > 0, -1 < nu < 0.5");
+    memset(&o, 0, sizeof(o));
+    const double E = m.young, nu = m.nu;
+    o.law = m.law;
+    o.young = E;
+    o.nu = nu;
+    o.rho = m.rho;
+    o.lambda = (E * nu) / ((1. + nu) * (1. - 2. * nu));
+    o.mu = 0.5 * E / (1. + nu);
+    o.K1 = E / (3 * (1 - 2 * nu));
+    o.mu2 = E / (1. + nu);
+    o.lam_stvk = E * nu / ((1. + nu) * (1. - (2 * nu)));
+    o.c = m.law == 2 ? std::sqrt(E / m.rho) : std::sqrt((o.lambda + 2 * o.mu) / m.rho);
+    o.lambda_f = (float)o.lambda;
+    o.mu_f = (float)o.mu;
+    o.K1_f = (float)o.K1;
+    o.mu2_f = (float)o.mu2;
+    o.lam_stvk_f = (float)o.lam_stvk;
+    o.inv_c_f = (float)(1.0 / o.c);
+    return MSX_OK;
+}
+
+static void rebuild_tiles(msx_pool *p)
+{
+    p->h_etiles.clear();
+    p->h_ntiles.clear();
+    const int te = p->sched.tile_elems, tn = p->sched.threads * 4;
+    for (int s = 0; s < (int)p->slots.size(); s++) {
+        const Slot &sl = p->slots[s];
+        if (!sl.active) continue;
+        for (long long b = 0; b < sl.ne; b += te) p->h_etiles.push_back({s, (int)b, (int)std::min<long long>(sl.ne, b + te)});
+        for (long long b = 0; b < sl.nn; b += tn) p->h_ntiles.push_back({s, (int)b, (int)std::min<long long>(sl.nn, b + tn)});
+    }
+    p->tiles_dirty = true;
+}
+
+static msx_status upload_tiles(msx_pool *p)
+{
+    if (!p->tiles_dirty) return MSX_OK;
+    size_t need = std::max(p->h_etiles.size(), p->h_ntiles.size());
+    if (need > p->tile_cap) {
+        size_t cap = std::max<size_t>(need * 2, 4096);
+        if (p->d_etiles) cudaFree(p->d_etiles);
+        if (p->d_ntiles) cudaFree(p->d_ntiles);
+        PCUDA(cudaMalloc(&p->d_etiles, sizeof(Tile) * cap));
+        PCUDA(cudaMalloc(&p->d_ntiles, sizeof(Tile) * cap));
+        p->tile_cap = cap;
+        if (p->graph) {
+            cudaGraphExecDestroy(p->graph);   // kernel arguments changed
+            p->graph = nullptr;
+        }
+    }
+    int counts[2] = {(int)p->h_etiles.size(), (int)p->h_ntiles.size()};
+    if (counts[0]) PCUDA(cudaMemcpyAsync(p->d_etiles, p->h_etiles.data(), sizeof(Tile) * counts[0], cudaMemcpyHostToDevice, p->stream));
+    if (counts[1]) PCUDA(cudaMemcpyAsync(p->d_ntiles, p->h_ntiles.data(), sizeof(Tile) * counts[1], cudaMemcpyHostToDevice, p->stream));
+    PCUDA(cudaMemcpyAsync(p->d_counts, counts, sizeof(counts), cudaMemcpyHostToDevice, p->stream));
+    PCUDA(cudaStreamSynchronize(p->stream));
+    p->tiles_dirty = false;
+    return MSX_OK;
+}
+
+static msx_status build_pool_graph(msx_pool *p, int steps)
+{
+    if (p->graph) {
+        cudaGraphExecDestroy(p->graph);
+        p->graph = nullptr;
+    }
+    const int threads = p->sched.threads, grid = p->sms * p->sched.ctas_per_sm;
+    const bool mixed = p->opts.precision == MSX_PREC_MIXED;
+    cudaGraph_t g;
+    PCUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < steps; i++) {
+        int parity = (i & 1) ? 0 : 1;
+        if (mixed) {
+            pool_node_kernel<MODE_MIXED><<<grid, threads, 0, p->stream>>>(p->d_descs, p->d_ntiles, p->d_counts + 1, parity);
+            pool_elem_kernel<MODE_MIXED><<<grid, threads, 0, p->stream>>>(p->d_descs, p->d_etiles, p->d_counts, parity);
+        } else {
+            pool_node_kernel<MODE_FP64><<<grid, threads, 0, p->stream>>>(p->d_descs, p->d_ntiles, p->d_counts + 1, parity);
+            pool_elem_kernel<MODE_FP64><<<grid, threads, 0, p->stream>>>(p->d_descs, p->d_etiles, p->d_counts, parity);
+        }
+    }
+    cudaError_t err = cudaStreamEndCapture(p->stream, &g);
+    if (err != cudaSuccess) return pfail(MSX_ERR_CUDA, std::string("pool graph capture: ") + cudaGetErrorString(err));
+    err = cudaGraphInstantiate(&p->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (err != cudaSuccess) return pfail(MSX_ERR_CUDA, std::string("pool graph instantiate: ") + cudaGetErrorString(err));
+    return MSX_OK;
+}
+
+// Copies out and frees every solve whose control slot says it stopped.
+static msx_status collect(msx_pool *p)
+{
+    const size_t n = p->slots.size();
+    PCUDA(cudaMemcpyAsync(p->h_ctrl, p->d_ctrl, sizeof(Ctrl) * 2 * n, cudaMemcpyDeviceToHost, p->stream));
+    PCUDA(cudaStreamSynchronize(p->stream));
+    bool changed = false;
+    p->elem_steps_active = 0;
+    for (size_t s = 0; s < n; s++) {
+        Slot &sl = p->slots[s];
+        if (!sl.active) continue;
+        const Ctrl &c = p->h_ctrl[2 * s];   // replays end on parity 0
+        if (!c.stop) {
+            p->elem_steps_active += sl.ne * c.step;
+            continue;
+        }
+        p->elem_steps_finished += sl.ne * c.step;
+        Finished f;
+        f.res.ticket = sl.ticket;
+        f.res.status = c.status;
+        f.res.reserved = 0;
+        f.res.steps = c.step;
+        f.res.t = c.t;
+        size_t bytes = sizeof(double) * 3 * sl.nn;
+        f.u.resize(3 * sl.nn);
+        f.v.resize(3 * sl.nn);
+        f.a.resize(3 * sl.nn);
+        PCUDA(cudaMemcpyAsync(f.u.data(), sl.P.u, bytes, cudaMemcpyDeviceToHost, p->stream));
+        PCUDA(cudaMemcpyAsync(f.v.data(), sl.P.v, bytes, cudaMemcpyDeviceToHost, p->stream));
+        PCUDA(cudaMemcpyAsync(f.a.data(), sl.P.a, bytes, cudaMemcpyDeviceToHost, p->stream));
+        PCUDA(cudaStreamSynchronize(p->stream));
+        f.res.submit_to_done_ms = now_ms() - sl.submit_ms;
+        PCUDA(cudaFreeAsync(sl.arena, p->stream));
+        p->used -= sl.bytes;
+        sl = Slot();
+        const long long t = f.res.ticket;
+        p->done[t] = std::move(f);
+        p->done_order.push_back(t);
+        changed = true;
+    }
+    if (changed) rebuild_tiles(p);
+    return MSX_OK;
+}
+
+static bool any_active(const msx_pool *p)
+{
+    for (const Slot &s : p->slots)
+        if (s.active) return true;
+    return false;
+}
+
+// One graph replay (spl steps) with the current schedule; returns device ms.
+static msx_status replay(msx_pool *p, float *ms)
+{
+    msx_status st;
+    if ((st = upload_tiles(p)) != MSX_OK) return st;
+    if (!p->graph && (st = build_pool_graph(p, p->spl)) != MSX_OK) return st;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, p->stream);
+    cudaError_t err = cudaGraphLaunch(p->graph, p->stream);
+    cudaEventRecord(b, p->stream);
+    cudaError_t err2 = cudaEventSynchronize(b);
+    if (ms) cudaEventElapsedTime(ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (err != cudaSuccess || err2 != cudaSuccess)
+        return pfail(MSX_ERR_CUDA, std::string("pool replay: ") + cudaGetErrorString(err != cudaSuccess ? err : err2));
+    return MSX_OK;
+}
+
+// Autotuner: times one replay per candidate schedule on the resident work and
+// keeps the fastest.  Candidates differ only in scheduling, so the solves'
+// results are the same whichever one runs a step.
+static msx_status autotune(msx_pool *p)
+{
+    const Sched cands[] = {{128, 512, 8}, {256, 1024, 4}, {256, 2048, 4}, {256, 1024, 8},
+                           {512, 2048, 2}, {512, 4096, 2}, {128, 1024, 8}, {256, 512, 6}};
+    const int spl = p->spl;
+    p->spl = 2;
+    double best = 1e300;
+    Sched bs = p->sched;
+    msx_status st = MSX_OK;
+    for (const Sched &c : cands) {
+        if (!any_active(p)) break;
+        p->sched = c;
+        rebuild_tiles(p);
+        if (p->graph) {
+            cudaGraphExecDestroy(p->graph);
+            p->graph = nullptr;
+        }
+        float ms = 0, tot = 0;
+        for (int r = 0; r < 2 && st == MSX_OK; r++) {
+            st = replay(p, &ms);
+            tot += ms;
+        }
+        if (st != MSX_OK || (st = collect(p)) != MSX_OK) break;
+        if (tot < best) {
+            best = tot;
+            bs = c;
+        }
+    }
+    p->spl = spl;
+    p->sched = bs;
+    rebuild_tiles(p);
+    if (p->graph) {
+        cudaGraphExecDestroy(p->graph);
+        p->graph = nullptr;
+    }
+    if (st != MSX_OK) return st;
+    p->tuned = true;
+    if (p->opts.tune_cache) {
+        if (FILE *f = fopen(p->opts.tune_cache, "w")) {
+            fprintf(f, "%d %d %d\n", bs.threads, bs.tile_elems, bs.ctas_per_sm);
+            fclose(f);
+        }
+    }
+    return MSX_OK;
+}
+
+// ------------------------------------------------------------------ C ABI
+extern "C" msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out)
+{
+    if (!out || !opts) return pfail(MSX_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    if (opts->precision != MSX_PREC_FP64 && opts->precision != MSX_PREC_MIXED)
+        return pfail(MSX_ERR_ARG, "pool precision must be FP64 or MIXED");
+    if (opts->max_slots < 1 || opts->max_slots > 4096) return pfail(MSX_ERR_ARG, "max_slots must be 1..4096");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return pfail(MSX_ERR_NO_DEVICE, "no CUDA device");
+    msx_pool *p = new msx_pool();
+    p->opts = *opts;
+    cudaGetDevice(&p->device);
+    cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device);
+    p->spl = opts->steps_per_launch > 0 ? ((opts->steps_per_launch + 1) & ~1) : 32;
+    if (opts->elems_per_block > 0) {
+        p->sched.threads = opts->elems_per_block >= 512 ? 512 : (opts->elems_per_block >= 256 ? 256 : 128);
+        p->sched.tile_elems = opts->elems_per_block;
+        p->tuned = true;
+    } else if (opts->tune_cache) {
+        if (FILE *f = fopen(opts->tune_cache, "r")) {
+            Sched s;
+            if (fscanf(f, "%d %d %d", &s.threads, &s.tile_elems, &s.ctas_per_sm) == 3 && s.threads > 0 &&
+                s.threads <= 1024 && s.tile_elems > 0 && s.ctas_per_sm > 0) {
+                p->sched = s;
+                p->tuned = true;
+            }
+            fclose(f);
+        }
+    }
+    p->slots.resize(opts->max_slots);
+    auto bail = [&](msx_status st) {
+        msx_pool_destroy(p);
+        return st;
+    };
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(pfail(MSX_ERR_CUDA, "stream"));
+    size_t n = opts->max_slots;
+    if (cudaMalloc(&p->d_descs, sizeof(Problem) * n) != cudaSuccess || cudaMalloc(&p->d_ctrl, sizeof(Ctrl) * 2 * n) != cudaSuccess ||
+        cudaMalloc(&p->d_dtmin, sizeof(unsigned long long) * 2 * n) != cudaSuccess ||
+        cudaMalloc(&p->d_flags, sizeof(int) * 2 * n) != cudaSuccess || cudaMalloc(&p->d_counts, sizeof(int) * 2) != cudaSuccess ||
+        cudaMallocHost(&p->h_ctrl, sizeof(Ctrl) * 2 * n) != cudaSuccess)
+        return bail(pfail(MSX_ERR_OOM, "pool tables"));
+    cudaMemset(p->d_ctrl, 0, sizeof(Ctrl) * 2 * n);
+    cudaMemset(p->d_counts, 0, sizeof(int) * 2);
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    p->budget = opts->hbm_budget_bytes > 0 ? (size_t)opts->hbm_budget_bytes : (size_t)(0.8 * fr);
+    *out = p;
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_pool_destroy(msx_pool *p)
+{
+    if (!p) return MSX_OK;
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    for (Slot &s : p->slots)
+        if (s.arena) cudaFree(s.arena);
+    if (p->graph) cudaGraphExecDestroy(p->graph);
+    for (void *q : {(void *)p->d_descs, (void *)p->d_ctrl, (void *)p->d_dtmin, (void *)p->d_flags, (void *)p->d_counts,
+                    (void *)p->d_etiles, (void *)p->d_ntiles})
+        if (q) cudaFree(q);
+    if (p->h_ctrl) cudaFreeHost(p->h_ctrl);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const msx_material *mat, const msx_bc *bcs,
+                                      int64_t num_bcs, const msx_solver_opts *o, int64_t *ticket)
+{
+    if (!p || !mesh || !mat || !o || !ticket) return pfail(MSX_ERR_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(p->mu);
+    const long long nn = mesh->num_nodes, ne = mesh->num_elems;
+    if (!mesh->X || !mesh->conn || nn < 4 || ne < 1 || nn >= (1LL << 31) || 4 * ne >= (1LL << 31))
+        return pfail(MSX_ERR_ARG, "bad mesh");
+    if (num_bcs < 0 || (num_bcs > 0 && !bcs)) return pfail(MSX_ERR_ARG, "bad boundary conditions");
+    if (!(o->scale_factor > 0) || !(o->tf >= o->t0) || o->max_steps < 0) return pfail(MSX_ERR_ARG, "bad solver options");
+    if (o->max_steps == 0 && !std::isfinite(o->tf)) return pfail(MSX_ERR_ARG, "need max_steps or a finite tf");
+    for (long long k = 0; k < 4 * ne; k++)
+        if (mesh->conn[k] < 0 || mesh->conn[k] >= nn) return pfail(MSX_ERR_ARG, "connectivity index out of range");
+    MatParams mp;
+    msx_status st = make_mat(*mat, mp);
+    if (st != MSX_OK) return st;
+    int slot = -1;
+    for (size_t s = 0; s < p->slots.size(); s++)
+        if (!p->slots[s].active) {
+            slot = (int)s;
+            break;
+        }
+    const int prec = p->opts.precision;
+    size_t bytes = footprint(nn, ne, num_bcs, prec);
+    if (slot < 0 || p->used + bytes > p->budget) return pfail(MSX_ERR_BUSY, "pool full (slots or HBM budget)");
+
+    // host tables: CSR in element order and Dirichlet records (as the single-solve path)
+    std::vector<int> ptr(nn + 1, 0), inc(4 * ne), node_bc(nn, -1);
+    for (long long k = 0; k < 4 * ne; k++) ptr[mesh->conn[k] + 1]++;
+    for (long long i = 0; i < nn; i++) ptr[i + 1] += ptr[i];
+    {
+        std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+        for (long long e = 0; e < ne; e++)
+            for (int q = 0; q < 4; q++) inc[fill[mesh->conn[e * 4 + q]]++] = (int)(e * 4 + q);
+    }
+    std::vector<long long> order(num_bcs);
+    std::iota(order.begin(), order.end(), 0);
+    for (long long k = 0; k < num_bcs; k++) {
+        if (bcs[k].dof < 0 || bcs[k].dof >= 3 * nn || bcs[k].mode < 0 || bcs[k].mode > 2)
+            return pfail(MSX_ERR_ARG, "bad boundary condition entry");
+        if (bcs[k].mode == MSX_BC_RAMP && !(o->tf - o->t0 != 0)) return pfail(MSX_ERR_ARG, "ramp BC needs tf != t0");
+    }
+    std::stable_sort(order.begin(), order.end(), [&](long long x, long long y) { return bcs[x].dof < bcs[y].dof; });
+    std::vector<int2> rec;
+    std::vector<BCEntry> ent;
+    for (long long k = 0; k < num_bcs; k++) {
+        const msx_bc &b = bcs[order[k]];
+        BCEntry e{b.mode, b.ramp_steps, b.mode == MSX_BC_RAMP ? b.value / (o->tf - o->t0) : b.value};
+        long long node = b.dof % nn;
+        int comp = (int)(b.dof / nn);
+        if (node_bc[node] < 0) {
+            node_bc[node] = (int)(rec.size() / 3);
+            rec.resize(rec.size() + 3, make_int2(0, 0));
+        }
+        int2 &r = rec[node_bc[node] * 3 + comp];
+        if (r.y == 0) r.x = (int)ent.size();
+        r.y++;
+        ent.push_back(e);
+    }
+
+    Slot sl;
+    sl.nn = nn;
+    sl.ne = ne;
+    sl.bytes = bytes;
+    PCUDA(cudaMallocAsync(&sl.arena, bytes, p->stream));
+    char *q = (char *)sl.arena;
+    auto carve = [&](size_t b) {
+        char *r = q;
+        q += align256(b);
+        return (void *)r;
+    };
+    Problem &P = sl.P;
+    memset(&P, 0, sizeof(P));
+    P.nn = nn;
+    P.ne = ne;
+    P.nmat = 1;
+    P.mats[0] = mp;
+    P.mat = nullptr;
+    P.conn = (int4 *)carve(sizeof(int4) * ne);
+    P.G = (double *)carve(sizeof(double) * 9 * ne);
+    P.wJ = (double *)carve(sizeof(double) * ne);
+    P.Lref = (double *)carve(sizeof(double) * ne);
+    P.G32 = (float *)carve(sizeof(float) * 9 * ne);
+    P.Eref32 = (float *)carve(sizeof(float) * 9 * ne);
+    P.wJ32 = (float *)carve(sizeof(float) * ne);
+    P.Lref32 = (float *)carve(sizeof(float) * ne);
+    double *X = (double *)carve(sizeof(double) * 3 * nn);
+    P.X = X;
+    P.u = (double *)carve(sizeof(double) * 3 * nn);
+    P.v = (double *)carve(sizeof(double) * 3 * nn);
+    P.a = (double *)carve(sizeof(double) * 3 * nn);
+    double *mass = (double *)carve(sizeof(double) * nn), *minv = (double *)carve(sizeof(double) * nn);
+    P.mass = mass;
+    P.minv = minv;
+    P.uhl = (float2 *)carve(sizeof(float2) * 3 * nn);
+    if (prec == MSX_PREC_MIXED) P.fe32 = (float *)carve(sizeof(float) * 12 * ne);
+    else P.fe = (double *)carve(sizeof(double) * 12 * ne);
+    int *d_ptr = (int *)carve(sizeof(int) * (nn + 1)), *d_inc = (int *)carve(sizeof(int) * 4 * ne);
+    int *d_nbc = (int *)carve(sizeof(int) * nn);
+    int2 *d_rec = (int2 *)carve(sizeof(int2) * 3 * nn);
+    BCEntry *d_ent = (BCEntry *)carve(sizeof(BCEntry) * (num_bcs > 0 ? num_bcs : 1));
+    P.node_ptr = d_ptr;
+    P.node_inc = d_inc;
+    P.node_bc = d_nbc;
+    P.bc_rec = d_rec;
+    P.bcs = d_ent;
+    P.ctrl = p->d_ctrl + 2 * slot;
+    P.dtmin = p->d_dtmin + 2 * slot;
+    P.flags = p->d_flags + 2 * slot;
+    P.sf = o->scale_factor;
+    P.tf = o->tf;
+    cudaStream_t s = p->stream;
+    PCUDA(cudaMemcpyAsync((void *)P.conn, mesh->conn, sizeof(int4) * ne, cudaMemcpyHostToDevice, s));
+    PCUDA(cudaMemcpyAsync(X, mesh->X, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, s));
+    PCUDA(cudaMemcpyAsync(d_ptr, ptr.data(), sizeof(int) * (nn + 1), cudaMemcpyHostToDevice, s));
+    PCUDA(cudaMemcpyAsync(d_inc, inc.data(), sizeof(int) * 4 * ne, cudaMemcpyHostToDevice, s));
+    PCUDA(cudaMemcpyAsync(d_nbc, node_bc.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, s));
+    if (!rec.empty()) PCUDA(cudaMemcpyAsync(d_rec, rec.data(), sizeof(int2) * rec.size(), cudaMemcpyHostToDevice, s));
+    if (!ent.empty()) PCUDA(cudaMemcpyAsync(d_ent, ent.data(), sizeof(BCEntry) * ent.size(), cudaMemcpyHostToDevice, s));
+    PCUDA(cudaMemsetAsync(P.u, 0, sizeof(double) * 3 * nn, s));
+    PCUDA(cudaMemsetAsync(P.v, 0, sizeof(double) * 3 * nn, s));
+    PCUDA(cudaMemsetAsync(P.a, 0, sizeof(double) * 3 * nn, s));
+    PCUDA(cudaMemsetAsync(P.uhl, 0, sizeof(float2) * 3 * nn, s));
+    launch_setup_elements(P, X, s);
+    launch_setup_mass(P, mass, minv, s);
+    unsigned long long inf2[2] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL};
+    PCUDA(cudaMemcpyAsync(P.dtmin, inf2, sizeof(inf2), cudaMemcpyHostToDevice, s));
+    launch_initial_cfl(P, nullptr, 0, s);
+    launch_initial_cfl(P, nullptr, 1, s);   // u = 0: the deformed CFL equals the undeformed one
+    long long limit = o->max_steps > 0 ? o->max_steps : (1LL << 62);
+    pool_init_ctrl<<<1, 1, 0, s>>>(P, o->t0, limit);
+    PCUDA(cudaGetLastError());
+    PCUDA(cudaMemcpyAsync(p->d_descs + slot, &P, sizeof(Problem), cudaMemcpyHostToDevice, s));
+    PCUDA(cudaStreamSynchronize(s));
+    sl.active = true;
+    sl.ticket = p->next_ticket++;
+    sl.submit_ms = now_ms();
+    p->slots[slot] = sl;
+    p->used += bytes;
+    rebuild_tiles(p);
+    *ticket = sl.ticket;
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_pool_step(msx_pool *p, int64_t steps)
+{
+    if (!p) return pfail(MSX_ERR_ARG, "NULL pool");
+    std::lock_guard<std::mutex> lk(p->mu);
+    msx_status st;
+    if (!p->tuned && any_active(p) && (st = autotune(p)) != MSX_OK) return st;
+    long long reps = steps > 0 ? (steps + p->spl - 1) / p->spl : 1;
+    for (long long r = 0; r < reps && any_active(p); r++) {
+        if ((st = replay(p, nullptr)) != MSX_OK) return st;
+        if ((st = collect(p)) != MSX_OK) return st;
+    }
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_pool_stats_get(msx_pool *p, msx_pool_stats *st)
+{
+    if (!p || !st) return pfail(MSX_ERR_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(p->mu);
+    msx_status r = collect(p);
+    if (r != MSX_OK) return r;
+    int act = 0;
+    for (const Slot &s : p->slots) act += s.active;
+    st->active = act;
+    st->finished_unfetched = (int32_t)p->done.size();
+    st->threads = p->sched.threads;
+    st->tile_elems = p->sched.tile_elems;
+    st->ctas_per_sm = p->sched.ctas_per_sm;
+    st->steps_per_launch = p->spl;
+    st->element_steps = p->elem_steps_finished + p->elem_steps_active;
+    st->used_bytes = (int64_t)p->used;
+    st->budget_bytes = (int64_t)p->budget;
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_pool_poll(msx_pool *p, msx_pool_result *results, int32_t max, int32_t *n)
+{
+    if (!p || !n || (max > 0 && !results)) return pfail(MSX_ERR_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(p->mu);
+    int k = 0;
+    while (k < max && !p->done_order.empty()) {
+        long long t = p->done_order.front();
+        p->done_order.pop_front();
+        auto it = p->done.find(t);
+        if (it == p->done.end()) continue;
+        results[k++] = it->second.res;
+    }
+    *n = k;
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_pool_fetch(msx_pool *p, int64_t ticket, double *u, double *v, double *a)
+{
+    if (!p) return pfail(MSX_ERR_ARG, "NULL pool");
+    std::lock_guard<std::mutex> lk(p->mu);
+    auto it = p->done.find(ticket);
+    if (it == p->done.end()) return pfail(MSX_ERR_STATE, "ticket not finished or already fetched");
+    const Finished &f = it->second;
+    if (u) memcpy(u, f.u.data(), sizeof(double) * f.u.size());
+    if (v) memcpy(v, f.v.data(), sizeof(double) * f.v.size());
+    if (a) memcpy(a, f.a.data(), sizeof(double) * f.a.size());
+    p->done.erase(it);
+    return MSX_OK;
+}
+

@@ -34,6 +34,8 @@ static msx_status fail(msx_status st, const std::string &msg)
 
 extern "C" const char *msx_last_error(void) { return g_last_error.c_str(); }
 
+void msx::msx_set_error(const char *msg) { g_last_error = msg; }
+
 // ------------------------------------------------------------------ small kernels
 namespace {
 
@@ -51,6 +53,7 @@ __global__ void init_block_kernel(Problem p, double t0, long long limit)
     c.stop = 0;
     c.status = 0;
     c.pad = 0;
+    c.pending = 0;
     p.ctrl[0] = c;
     p.ctrl[1] = c;
     p.flags[0] = 0;
@@ -326,6 +329,34 @@ static msx_status build_graph(msx_handle *h)
     return MSX_OK;
 }
 
+// Reads the latest control slot, applies this call's step cap and resumes a
+// block that an earlier cap stopped (tf and errors stay final).
+static msx_status arm_block(msx_handle *h, long long max_steps, long long *start_steps)
+{
+    MSX_CUDA(cudaMemcpyAsync(h->h_ctrl, h->ctrl.p, 2 * sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    Ctrl latest = h->h_ctrl[0];   // replays start on parity 1 and read slot 0
+    *start_steps = latest.step;
+    long long limit = h->max_steps > 0 ? h->max_steps : (1LL << 62);
+    if (max_steps > 0) limit = std::min(limit, latest.step + max_steps);
+    bool resume = latest.stop && latest.status == 0 && latest.t < h->tf - 1E-12 && latest.step < limit;
+    if (latest.limit != limit || resume) {
+        latest.limit = limit;
+        if (resume) {
+            // the first resumed step reads the CFL min saved when the block stopped
+            latest.stop = 0;
+            unsigned long long slot1 = latest.pending;
+            int zero = 0;
+            MSX_CUDA(cudaMemcpyAsync(h->dtmin.p + 1, &slot1, sizeof(slot1), cudaMemcpyHostToDevice, h->stream));
+            MSX_CUDA(cudaMemcpyAsync(h->flags.p + 1, &zero, sizeof(zero), cudaMemcpyHostToDevice, h->stream));
+        }
+        MSX_CUDA(cudaMemcpyAsync(h->ctrl.p, &latest, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream));
+        MSX_CUDA(cudaStreamSynchronize(h->stream));
+        h->h_ctrl[0] = latest;
+    }
+    return MSX_OK;
+}
+
 // ------------------------------------------------------------------ C ABI
 extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats, int32_t num_mats,
                                  const msx_bc *bcs, int64_t num_bcs, const msx_solver_opts *opts,
@@ -471,23 +502,9 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
     msx_status st;
     if (!h->block_ready && (st = init_block(h)) != MSX_OK) return st;
     if (!h->graph && (st = build_graph(h)) != MSX_OK) return st;
-    // per-call cap: the node kernel stops at ctrl.limit
-    const Ctrl &cur = h->h_ctrl[0];
-    MSX_CUDA(cudaMemcpyAsync(h->h_ctrl, h->ctrl.p, 2 * sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
-    MSX_CUDA(cudaStreamSynchronize(h->stream));
-    Ctrl latest = h->h_ctrl[0];   // replays start on parity 1 and read slot 0
-    long long start_steps = latest.step;
-    long long limit = h->max_steps > 0 ? h->max_steps : (1LL << 62);
-    if (max_steps > 0) limit = std::min(limit, start_steps + (long long)max_steps);
-    // a block stopped only by an earlier per-call cap resumes; tf, errors stay final
-    bool resume = latest.stop && latest.status == 0 && latest.t < h->tf - 1E-12 && latest.step < limit;
-    if (latest.limit != limit || resume) {
-        latest.limit = limit;
-        if (resume) latest.stop = 0;
-        MSX_CUDA(cudaMemcpyAsync(h->ctrl.p, &latest, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream));
-        MSX_CUDA(cudaStreamSynchronize(h->stream));
-    }
-    (void)cur;
+    long long start_steps = 0;
+    if ((st = arm_block(h, max_steps, &start_steps)) != MSX_OK) return st;
+    Ctrl latest = h->h_ctrl[0];
     MSX_CUDA(cudaEventRecord(h->ev0, h->stream));
     // two replays in flight: check the older one's control slot
     long long k = 0;
@@ -611,9 +628,11 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
     if (!h || !rep || steps < 1) return fail(MSX_ERR_ARG, "bad profile arguments");
     msx_status st;
     if (!h->block_ready && (st = init_block(h)) != MSX_OK) return st;
-    bind_problem(h);
+    long long start_steps = 0;
     // replays start on parity 1: launch an even number of steps from parity 1
     long long n = (steps + 1) & ~1LL;
+    if ((st = arm_block(h, n, &start_steps)) != MSX_OK) return st;
+    bind_problem(h);
     std::vector<cudaEvent_t> ev(3 * n);
     for (auto &e : ev) cudaEventCreate(&e);
     for (long long i = 0; i < n; i++) {

@@ -64,6 +64,12 @@ class PoolOpts_(C.Structure):
                 ("elems_per_block", C.c_int32), ("steps_per_launch", C.c_int32), ("tune_cache", C.c_char_p)]
 
 
+class PoolStats_(C.Structure):
+    _fields_ = [("active", C.c_int32), ("finished_unfetched", C.c_int32), ("threads", C.c_int32),
+                ("tile_elems", C.c_int32), ("ctas_per_sm", C.c_int32), ("steps_per_launch", C.c_int32),
+                ("element_steps", C.c_int64), ("used_bytes", C.c_int64), ("budget_bytes", C.c_int64)]
+
+
 class PoolResult_(C.Structure):
     _fields_ = [("ticket", C.c_int64), ("status", C.c_int32), ("reserved", C.c_int32), ("steps", C.c_int64),
                 ("t", C.c_double), ("submit_to_done_ms", C.c_double)]
@@ -72,7 +78,8 @@ class PoolResult_(C.Structure):
 # every entry point declared in include/msx.h
 SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_solver", "msx_destroy",
            "msx_last_error", "msx_internal_force", "msx_get_element_data", "msx_profile", "msx_mesh_cube",
-           "msx_stream", "msx_set_device"]
+           "msx_stream", "msx_set_device", "msx_pool_create", "msx_pool_submit", "msx_pool_step",
+           "msx_pool_poll", "msx_pool_fetch", "msx_pool_destroy", "msx_pool_stats_get"]
 
 _lib = None
 
@@ -230,6 +237,83 @@ class Solver:
     def close(self):
         if getattr(self, "h", None):
             load().msx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Pool:
+    """Batched / serving pool: independent solves resident on the device and
+    stepped together (include/msx.h msx_pool_*)."""
+
+    def __init__(self, max_slots=256, precision=MIXED, hbm_budget_bytes=0, elems_per_block=0,
+                 steps_per_launch=0, tune_cache=None):
+        L = load()
+        for name, args in (("msx_pool_create", [C.POINTER(PoolOpts_), C.POINTER(C.c_void_p)]),
+                           ("msx_pool_submit", [C.c_void_p, C.POINTER(Mesh_), C.POINTER(Material_), C.c_void_p,
+                                                C.c_int64, C.POINTER(Opts_), C.POINTER(C.c_int64)]),
+                           ("msx_pool_step", [C.c_void_p, C.c_int64]),
+                           ("msx_pool_poll", [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+                           ("msx_pool_fetch", [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+                           ("msx_pool_destroy", [C.c_void_p]),
+                           ("msx_pool_stats_get", [C.c_void_p, C.POINTER(PoolStats_)])):
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        self._cache = tune_cache.encode() if tune_cache else None
+        o = PoolOpts_(hbm_budget_bytes, max_slots, precision, elems_per_block, steps_per_launch, self._cache)
+        h = C.c_void_p()
+        _check(L.msx_pool_create(C.byref(o), C.byref(h)))
+        self.h = h
+        self.sizes = {}
+        self._keep = {}
+
+    def submit(self, X, conn, material, bcs, max_steps, t0=0.0, tf=1e30, scale_factor=0.5):
+        """Admit one solve; returns its ticket or None when the pool is full."""
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        conn = np.ascontiguousarray(conn, dtype=np.int32)
+        mesh = Mesh_(X.shape[1], conn.shape[0], _p(X), _p(conn), None)
+        law, E, nu, rho = material
+        mat = Material_(int(law), 0, float(E), float(nu), float(rho))
+        barr = _bc_array(bcs)
+        opts = Opts_(t0, tf, scale_factor, max_steps, 0, 0)
+        t = C.c_int64()
+        st = load().msx_pool_submit(self.h, C.byref(mesh), C.byref(mat), C.cast(barr, C.c_void_p), len(bcs),
+                                    C.byref(opts), C.byref(t))
+        if st == 9:
+            return None
+        _check(st)
+        self.sizes[t.value] = X.shape[1]
+        return t.value
+
+    def step(self, steps=0):
+        _check(load().msx_pool_step(self.h, steps))
+
+    def poll(self, max_results=4096):
+        arr = (PoolResult_ * max_results)()
+        n = C.c_int32()
+        _check(load().msx_pool_poll(self.h, C.cast(arr, C.c_void_p), max_results, C.byref(n)))
+        return [dict(ticket=arr[i].ticket, status=arr[i].status, steps=arr[i].steps, t=arr[i].t,
+                     latency_ms=arr[i].submit_to_done_ms) for i in range(n.value)]
+
+    def fetch(self, ticket):
+        nn = self.sizes.pop(ticket)
+        u, v, a = (np.zeros(3 * nn) for _ in range(3))
+        _check(load().msx_pool_fetch(self.h, ticket, _p(u), _p(v), _p(a)))
+        return u, v, a
+
+    def stats(self):
+        st = PoolStats_()
+        _check(load().msx_pool_stats_get(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in PoolStats_._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().msx_pool_destroy(self.h)
             self.h = None
 
     def __del__(self):
