@@ -54,8 +54,12 @@ def test_pool_results_equal_single_solves(precision):
 
 def test_continuous_admission_and_budget():
     X, c, m, b = case(6, 1e6, 0.3, 0.1, 3)
-    # a budget that fits two solves of this size (about 0.45 MB each)
-    P = msx.Pool(max_slots=64, precision=msx.MIXED, hbm_budget_bytes=2 * 600_000, steps_per_launch=4)
+    probe = msx.Pool(max_slots=4, precision=msx.MIXED)
+    probe.submit(X, c, m, b, 2)
+    one = probe.stats()["used_bytes"]
+    probe.close()
+    # a budget that fits two solves of this size but not three
+    P = msx.Pool(max_slots=64, precision=msx.MIXED, hbm_budget_bytes=int(2.5 * one), steps_per_launch=4)
     admitted, waiting, done = [], list(range(6)), {}
     while waiting or admitted:
         while waiting:

@@ -457,10 +457,12 @@ __device__ __forceinline__ void cofactor(const double *F, double *K)
     K[8] = F[0] * F[4] - F[1] * F[3];
 }
 
-__device__ __forceinline__ void stress_fast(const MatParams &m, const double *F, double *P)
+// wJ * P written through the cofactor; the quadrature weight is folded into
+// the law's scalar coefficients instead of scaling the nine entries of P.
+__device__ __forceinline__ void stress_fast(const MatParams &m, const double *F, double wJ, double *P)
 {
     if (m.law == 2) {
-        // S = mu2 E + lam tr(E) I, E = (F^T F - I)/2; P = F S
+        // S = mu2 E + lam tr(E) I, E = (F^T F - I)/2; wJ P = F (wJ S)
         double C00 = F[0] * F[0] + F[3] * F[3] + F[6] * F[6];
         double C11 = F[1] * F[1] + F[4] * F[4] + F[7] * F[7];
         double C22 = F[2] * F[2] + F[5] * F[5] + F[8] * F[8];
@@ -468,7 +470,7 @@ __device__ __forceinline__ void stress_fast(const MatParams &m, const double *F,
         double C02 = F[0] * F[2] + F[3] * F[5] + F[6] * F[8];
         double C12 = F[1] * F[2] + F[4] * F[5] + F[7] * F[8];
         double trE = 0.5 * ((C00 - 1.0) + (C11 - 1.0) + (C22 - 1.0));
-        double h = 0.5 * m.mu2, dg = m.lam_stvk * trE;
+        double h = 0.5 * m.mu2 * wJ, dg = m.lam_stvk * trE * wJ;
         double S00 = h * (C00 - 1.0) + dg, S11 = h * (C11 - 1.0) + dg, S22 = h * (C22 - 1.0) + dg;
         double S01 = h * C01, S02 = h * C02, S12 = h * C12;
 #pragma unroll
@@ -484,11 +486,11 @@ __device__ __forceinline__ void stress_fast(const MatParams &m, const double *F,
     cofactor(F, K);
     double J = F[0] * K[0] + F[1] * K[1] + F[2] * K[2];
     double iJ = 1.0 / J;
+    double a1, g;
     if (m.law == 1) {
         // P = mu F + (lambda ln J - mu) F^-T
-        double g = (m.lambda * log(J) - m.mu) * iJ;
-#pragma unroll
-        for (int k = 0; k < 9; k++) P[k] = m.mu * F[k] + g * K[k];
+        a1 = m.mu * wJ;
+        g = (m.lambda * log(J) - m.mu) * iJ * wJ;
     } else {
         // P = mu J^-2/3 F + (-mu/3 trB J^-5/3 + K1 (J-1)) cof(F)
         double r = rcbrt(J);
@@ -496,11 +498,11 @@ __device__ __forceinline__ void stress_fast(const MatParams &m, const double *F,
         double trB = 0;
 #pragma unroll
         for (int k = 0; k < 9; k++) trB += F[k] * F[k];
-        double a1 = m.mu * j23;
-        double g = -(m.mu / 3.0) * trB * j23 * iJ + m.K1 * (J - 1.0);
-#pragma unroll
-        for (int k = 0; k < 9; k++) P[k] = a1 * F[k] + g * K[k];
+        a1 = m.mu * j23 * wJ;
+        g = (-(m.mu / 3.0) * trB * j23 * iJ + m.K1 * (J - 1.0)) * wJ;
     }
+#pragma unroll
+    for (int k = 0; k < 9; k++) P[k] = a1 * F[k] + g * K[k];
 }
 
 // Inscribed-sphere diameter from the three edge vectors at vertex 0:
@@ -518,74 +520,106 @@ __device__ __forceinline__ T char_length_edges(const T *e1, const T *e2, const T
     return T(2) * v6 / s;
 }
 
-template <bool FORCE_ONLY>
-__device__ __forceinline__ double elem_body_fp64(const Problem &p, long long e, int parity)
+// Exact FP64 CFL value of one element, min(L_ref, L(X+u)) / c, for the
+// elements the FP32 screen keeps (solvers.cpp:296-320).
+static __device__ __noinline__ double cfl_fp64(const Problem &p, long long e)
 {
-    const long long ne = p.ne, nn = p.nn;
-    double vmin = INFINITY;
-    {
-        int4 cn = p.conn[e];
-        int nd[4] = {cn.x, cn.y, cn.z, cn.w};
-        double G[9];
+    const long long nn = p.nn;
+    int4 cn = p.conn[e];
+    int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    double x0[3], e1[3], e2[3], e3[3];
 #pragma unroll
-        for (int k = 0; k < 9; k++) G[k] = __ldg(p.G + k * ne + e);
-        double u0[3], du[9];
+    for (int k = 0; k < 3; k++) x0[k] = p.X[k * nn + nd[0]] + p.u[k * nn + nd[0]];
 #pragma unroll
-        for (int i = 0; i < 3; i++) u0[i] = p.u[nd[0] + i * nn];
-#pragma unroll
-        for (int a = 1; a < 4; a++)
-#pragma unroll
-            for (int i = 0; i < 3; i++) du[(a - 1) * 3 + i] = p.u[nd[a] + i * nn] - u0[i];
-        double F[9], P[9];
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-            for (int j = 0; j < 3; j++)
-                F[i * 3 + j] = (i == j ? 1.0 : 0.0) +
-                               (du[i] * G[j] + du[3 + i] * G[3 + j] + du[6 + i] * G[6 + j]);
-        const MatParams &m = mat_of(p, e);
-        stress_fast(m, F, P);
-        double wJ = __ldg(p.wJ + e);
-#pragma unroll
-        for (int k = 0; k < 9; k++) P[k] *= wJ;
-        double f[12];
-#pragma unroll
-        for (int a = 1; a < 4; a++)
-#pragma unroll
-            for (int i = 0; i < 3; i++)
-                f[a * 3 + i] = P[i * 3] * G[(a - 1) * 3] + P[i * 3 + 1] * G[(a - 1) * 3 + 1] +
-                               P[i * 3 + 2] * G[(a - 1) * 3 + 2];
-#pragma unroll
-        for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
-        double2 *fe = reinterpret_cast<double2 *>(p.fe + e * 12);
-#pragma unroll
-        for (int k = 0; k < 6; k++) fe[k] = make_double2(f[2 * k], f[2 * k + 1]);
-        if (!FORCE_ONLY) {
-            double X0[3], e1[3], e2[3], e3[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) X0[k] = __ldg(p.X + k * nn + nd[0]);
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                e1[k] = (__ldg(p.X + k * nn + nd[1]) - X0[k]) + du[k];
-                e2[k] = (__ldg(p.X + k * nn + nd[2]) - X0[k]) + du[3 + k];
-                e3[k] = (__ldg(p.X + k * nn + nd[3]) - X0[k]) + du[6 + k];
-            }
-            double dist = char_length_edges<double>(e1, e2, e3);
-            double Lr = __ldg(p.Lref + e);
-            vmin = ((dist < Lr) ? dist : Lr) / m.c;
-            if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
-        }
+    for (int k = 0; k < 3; k++) {
+        e1[k] = (p.X[k * nn + nd[1]] + p.u[k * nn + nd[1]]) - x0[k];
+        e2[k] = (p.X[k * nn + nd[2]] + p.u[k * nn + nd[2]]) - x0[k];
+        e3[k] = (p.X[k * nn + nd[3]] + p.u[k * nn + nd[3]]) - x0[k];
     }
-    return vmin;
+    double dist = char_length_edges<double>(e1, e2, e3);
+    double Lr = p.Lref[e];
+    return ((dist < Lr) ? dist : Lr) / mat_of(p, e).c;
 }
 
-template <bool FORCE_ONLY>
-__global__ void __launch_bounds__(kElemBlock) elem_kernel_fp64(Problem p, int parity)
+// FP32 estimate of an element's CFL value from the FP32 reference edges plus
+// the displacement differences.  Its relative error stays below ~3e-4 unless
+// the tet is a sliver (6V < 4e-3 |e1||e2||e3|); slivers are returned negated
+// so that the caller always recomputes them in FP64.
+__device__ __forceinline__ float cfl_screen(const Problem &p, long long e, const float *du, const MatParams &m)
 {
-    if (!FORCE_ONLY && !p.ctrl[parity].ran) return;
+    const long long ne = p.ne;
+    float e1[3], e2[3], e3[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        e1[i] = __ldg(p.Eref32 + i * ne + e) + du[i];
+        e2[i] = __ldg(p.Eref32 + (3 + i) * ne + e) + du[3 + i];
+        e3[i] = __ldg(p.Eref32 + (6 + i) * ne + e) + du[6 + i];
+    }
+    float C0 = e2[1] * e3[2] - e2[2] * e3[1], C1 = e2[2] * e3[0] - e2[0] * e3[2], C2 = e2[0] * e3[1] - e2[1] * e3[0];
+    float v6 = fabsf(e1[0] * C0 + e1[1] * C1 + e1[2] * C2);
+    float l1 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+    float l2 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+    float l3 = e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2];
+    float dist = char_length_edges<float>(e1, e2, e3);
+    float Lr = __ldg(p.Lref32 + e);
+    float dt = ((dist < Lr) ? dist : Lr) * m.inv_c_f;
+    bool sliver = !(v6 * v6 >= 1.6e-5f * l1 * l2 * l3) || !(dt > 0.0f);
+    return sliver ? -1.0f : dt;
+}
+
+// Plain FP64 with contraction: H from node differences, laws through the
+// cofactor (F C^-1 = F^-T = cof(F)/J), wJ folded into the law's coefficients,
+// the 4th corner force as minus the sum of the other three.  Same algebra as
+// the reference, about half its FP64 operations.  Returns the FP32 CFL screen
+// value (see cfl_screen).
+template <bool FORCE_ONLY>
+__device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, int parity)
+{
+    const long long ne = p.ne, nn = p.nn;
+    int4 cn = p.conn[e];
+    int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    double G[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) G[k] = __ldg(p.G + k * ne + e);
+    double u0[3], du[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++) u0[i] = p.u[nd[0] + i * nn];
+#pragma unroll
+    for (int a = 1; a < 4; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) du[(a - 1) * 3 + i] = p.u[nd[a] + i * nn] - u0[i];
+    double F[9], P[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+            F[i * 3 + j] = (i == j ? 1.0 : 0.0) + (du[i] * G[j] + du[3 + i] * G[3 + j] + du[6 + i] * G[6 + j]);
+    const MatParams &m = mat_of(p, e);
+    stress_fast(m, F, __ldg(p.wJ + e), P);
+    double f[12];
+#pragma unroll
+    for (int a = 1; a < 4; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            f[a * 3 + i] = P[i * 3] * G[(a - 1) * 3] + P[i * 3 + 1] * G[(a - 1) * 3 + 1] + P[i * 3 + 2] * G[(a - 1) * 3 + 2];
+#pragma unroll
+    for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
+    double2 *fe = reinterpret_cast<double2 *>(p.fe + e * 12);
+#pragma unroll
+    for (int k = 0; k < 6; k++) fe[k] = make_double2(f[2 * k], f[2 * k + 1]);
+    if (FORCE_ONLY) return 0.0f;
+    if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
+    float du32[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) du32[k] = (float)du[k];
+    return cfl_screen(p, e, du32, m);
+}
+
+// corner forces only (internal-force hook)
+static __global__ void __launch_bounds__(kElemBlock) elem_force_kernel_fp64(Problem p, int parity)
+{
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double v = e < p.ne ? elem_body_fp64<FORCE_ONLY>(p, e, parity) : INFINITY;
-    if (!FORCE_ONLY) block_min_to(v, p.dtmin + (parity ^ 1));
+    if (e < p.ne) elem_body_fp64<true>(p, e, parity);
 }
 
 // ---------------------------------------------------------------------------
@@ -657,10 +691,10 @@ __device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H,
 }
 
 template <bool FORCE_ONLY>
-__device__ __forceinline__ double elem_body_mixed(const Problem &p, long long e, int parity)
+__device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, int parity)
 {
     const long long ne = p.ne, nn = p.nn;
-    double vmin = INFINITY;
+    float vmin = INFINITY;
     {
         int4 cn = p.conn[e];
         int nd[4] = {cn.x, cn.y, cn.z, cn.w};
@@ -724,22 +758,36 @@ __device__ __forceinline__ double elem_body_mixed(const Problem &p, long long e,
             }
             float dist = char_length_edges<float>(e1, e2, e3);
             float Lr = __ldg(p.Lref32 + e);
-            vmin = (double)(((dist < Lr) ? dist : Lr) * m.inv_c_f);
+            vmin = ((dist < Lr) ? dist : Lr) * m.inv_c_f;
             if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
         }
     }
     return vmin;
 }
 
-template <bool FORCE_ONLY>
-__global__ void __launch_bounds__(kElemBlock) elem_kernel_mixed(Problem p, int parity)
+// corner forces only (internal-force hook)
+static __global__ void __launch_bounds__(kElemBlock) elem_force_kernel_mixed(Problem p, int parity)
 {
-    if (!FORCE_ONLY && !p.ctrl[parity].ran) return;
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double v = e < p.ne ? elem_body_mixed<FORCE_ONLY>(p, e, parity) : INFINITY;
-    if (!FORCE_ONLY) block_min_to(v, p.dtmin + (parity ^ 1));
+    if (e < p.ne) elem_body_mixed<true>(p, e, parity);
 }
 
+
+// Block-wide min of a float, returned to every thread of the block.
+__device__ __forceinline__ float block_min_bcast(float v)
+{
+    __shared__ float wm[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) wm[w] = v;
+    __syncthreads();
+    int nw = (blockDim.x + 31) >> 5;
+    float r = INFINITY;
+    for (int k = 0; k < nw; k++) r = fminf(r, wm[k]);
+    __syncthreads();
+    return r;
+}
 
 // ---------------------------------------------------------------------------
 // Pooled kernels: many independent solves stepped by one persistent grid.
@@ -748,13 +796,8 @@ __global__ void __launch_bounds__(kElemBlock) elem_kernel_mixed(Problem p, int p
 // and the same graph serves any admitted set.  Per-solve control, CFL slot
 // and NaN flag are those of the solve's Problem.
 // ---------------------------------------------------------------------------
-struct Tile {
-    int solve;
-    int begin, end;
-};
-
 template <int MODE>
-__global__ void pool_node_kernel(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
+__global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
                                  const int *__restrict__ ntiles, int parity)
 {
     const int n = *ntiles;
@@ -769,19 +812,38 @@ __global__ void pool_node_kernel(const Problem *__restrict__ descs, const Tile *
     }
 }
 
+// Element kernel over tiles.  FP64: every element's FP32 CFL screen value is
+// kept in shared memory; after the tile's FP32 minimum is known, elements
+// within 2^-8 of it (and slivers) recompute the exact FP64 value, whose
+// minimum goes to the solve's CFL slot.  Mixed: the FP32 minimum itself.
 template <int MODE>
-__global__ void pool_elem_kernel(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
-                                 const int *__restrict__ ntiles, int parity)
+__global__ void __launch_bounds__(kStepThreads) pool_elem_kernel(const Problem *__restrict__ descs,
+                                                                 const Tile *__restrict__ tiles,
+                                                                 const int *__restrict__ ntiles, int parity)
 {
+    __shared__ float sdt[MODE == MODE_MIXED ? 1 : kMaxTileElems];
     const int n = *ntiles;
     for (int t = blockIdx.x; t < n; t += gridDim.x) {
         const Tile tl = tiles[t];
         const Problem &p = descs[tl.solve];
         if (!p.ctrl[parity].ran) continue;
+        float v32 = INFINITY;
+        for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
+            float d = MODE == MODE_MIXED ? elem_body_mixed<false>(p, e, parity) : elem_body_fp64<false>(p, e, parity);
+            if (MODE != MODE_MIXED) sdt[e - tl.begin] = d;
+            if (d >= 0.0f) v32 = fminf(v32, d);
+        }
+        float bmin = block_min_bcast(v32);   // also orders the sdt writes before the reads below
+        if (MODE == MODE_MIXED) {
+            if (threadIdx.x == 0 && bmin < INFINITY)
+                atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong((double)bmin));
+            continue;
+        }
+        const float thr = bmin * (1.0f + 1.0f / 256.0f);
         double v = INFINITY;
         for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
-            double w = MODE == MODE_MIXED ? elem_body_mixed<false>(p, e, parity) : elem_body_fp64<false>(p, e, parity);
-            v = fmin(v, w);
+            float d = sdt[e - tl.begin];
+            if (d < 0.0f || d <= thr) v = fmin(v, cfl_fp64(p, e));
         }
         block_min_to(v, p.dtmin + (parity ^ 1));
     }

@@ -1,38 +1,52 @@
-// msx_fast.cu -- FP64 (contracted, simplified algebra) and mixed-precision kernels.
+// msx_fast.cu -- FP64 (contracted, simplified algebra) and mixed-precision
+// kernels.  The tiled step kernels are instantiated here only, so a single
+// solve (msx_run) and the pool execute the same machine code.
 #include "msx_device.cuh"
 
 namespace msx {
 
-void launch_node_fp64(const Problem &p, int parity, cudaStream_t s)
-{
-    node_kernel<MODE_FP64><<<grid_for(p.nn, kNodeBlock), kNodeBlock, 0, s>>>(p, parity);
-}
-
-void launch_elem_fp64(const Problem &p, int parity, cudaStream_t s)
-{
-    elem_kernel_fp64<false><<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, parity);
-}
-
 void launch_internal_force_fp64(const Problem &p, double *fint, cudaStream_t s)
 {
-    elem_kernel_fp64<true><<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, 0);
+    elem_force_kernel_fp64<<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, 0);
     gather_kernel<MODE_FP64><<<grid_for(p.nn, 256), 256, 0, s>>>(p, fint);
-}
-
-void launch_node_mixed(const Problem &p, int parity, cudaStream_t s)
-{
-    node_kernel<MODE_MIXED><<<grid_for(p.nn, kNodeBlock), kNodeBlock, 0, s>>>(p, parity);
-}
-
-void launch_elem_mixed(const Problem &p, int parity, cudaStream_t s)
-{
-    elem_kernel_mixed<false><<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, parity);
 }
 
 void launch_internal_force_mixed(const Problem &p, double *fint, cudaStream_t s)
 {
-    elem_kernel_mixed<true><<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, 0);
+    elem_force_kernel_mixed<<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, 0);
     gather_kernel<MODE_MIXED><<<grid_for(p.nn, 256), 256, 0, s>>>(p, fint);
+}
+
+void launch_tiled_node(const Problem *descs, const Tile *ntiles, const int *counts, int mode, int parity, int grid,
+                       int threads, cudaStream_t s)
+{
+    if (mode == MODE_MIXED)
+        pool_node_kernel<MODE_MIXED><<<grid, threads, 0, s>>>(descs, ntiles, counts + 1, parity);
+    else
+        pool_node_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, ntiles, counts + 1, parity);
+}
+
+void launch_tiled_elem(const Problem *descs, const Tile *etiles, const int *counts, int mode, int parity, int grid,
+                       int threads, cudaStream_t s)
+{
+    if (mode == MODE_MIXED)
+        pool_elem_kernel<MODE_MIXED><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
+    else
+        pool_elem_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
+}
+
+int tiled_ctas_per_sm(int mode, int threads)
+{
+    int a = 0, b = 0;
+    if (mode == MODE_MIXED) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, pool_node_kernel<MODE_MIXED>, threads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pool_elem_kernel<MODE_MIXED>, threads, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, pool_node_kernel<MODE_FP64>, threads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pool_elem_kernel<MODE_FP64>, threads, 0);
+    }
+    int c = a < b ? a : b;
+    return c > 0 ? c : 1;
 }
 
 }  // namespace msx

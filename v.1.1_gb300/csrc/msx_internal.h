@@ -82,16 +82,33 @@ struct Problem {
     double sf, tf;
 };
 
+// A contiguous element (or node) range [begin, end) of one solve.  The step
+// kernels of the FP64 and mixed modes stride over a list of tiles, so one
+// solve and many pooled solves run the same kernels.
+struct Tile {
+    int solve;
+    int begin, end;
+};
+
+constexpr int kStepThreads = 256;   // upper bound on the CTA size of the tiled step kernels
+constexpr int kMaxTileElems = 4096; // upper bound on the elements of one tile
+
+// Tiled step kernels (one instantiation in msx_fast.cu, used by msx_run and
+// the pool).  `counts` points to the element-tile count, counts + 1 to the
+// node-tile count, both in device memory.
+void launch_tiled_node(const Problem *descs, const Tile *ntiles, const int *counts, int mode, int parity, int grid,
+                       int threads, cudaStream_t s);
+void launch_tiled_elem(const Problem *descs, const Tile *etiles, const int *counts, int mode, int parity, int grid,
+                       int threads, cudaStream_t s);
+// CTAs of the tiled kernels that fit on one SM at this CTA size (min of node and element kernel)
+int tiled_ctas_per_sm(int mode, int threads);
+
 // records the message returned by msx_last_error() on this host thread
 void msx_set_error(const char *msg);
 
 // launchers (one translation unit per numeric mode)
 void launch_node_exact(const Problem &p, int parity, cudaStream_t s);
 void launch_elem_exact(const Problem &p, int parity, cudaStream_t s);
-void launch_node_fp64(const Problem &p, int parity, cudaStream_t s);
-void launch_elem_fp64(const Problem &p, int parity, cudaStream_t s);
-void launch_node_mixed(const Problem &p, int parity, cudaStream_t s);
-void launch_elem_mixed(const Problem &p, int parity, cudaStream_t s);
 
 // set-up (exact operation order)
 void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s);

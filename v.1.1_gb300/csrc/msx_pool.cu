@@ -22,7 +22,7 @@
 #include <vector>
 
 #include "../../include/msx.h"
-#include "msx_device.cuh"
+#include "msx_internal.h"
 
 using namespace msx;
 
@@ -205,18 +205,13 @@ static msx_status build_pool_graph(msx_pool *p, int steps)
         p->graph = nullptr;
     }
     const int threads = p->sched.threads, grid = p->sms * p->sched.ctas_per_sm;
-    const bool mixed = p->opts.precision == MSX_PREC_MIXED;
+    const int mode = p->opts.precision == MSX_PREC_MIXED ? MODE_MIXED : MODE_FP64;
     cudaGraph_t g;
     PCUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
     for (int i = 0; i < steps; i++) {
         int parity = (i & 1) ? 0 : 1;
-        if (mixed) {
-            pool_node_kernel<MODE_MIXED><<<grid, threads, 0, p->stream>>>(p->d_descs, p->d_ntiles, p->d_counts + 1, parity);
-            pool_elem_kernel<MODE_MIXED><<<grid, threads, 0, p->stream>>>(p->d_descs, p->d_etiles, p->d_counts, parity);
-        } else {
-            pool_node_kernel<MODE_FP64><<<grid, threads, 0, p->stream>>>(p->d_descs, p->d_ntiles, p->d_counts + 1, parity);
-            pool_elem_kernel<MODE_FP64><<<grid, threads, 0, p->stream>>>(p->d_descs, p->d_etiles, p->d_counts, parity);
-        }
+        launch_tiled_node(p->d_descs, p->d_ntiles, p->d_counts, mode, parity, grid, threads, p->stream);
+        launch_tiled_elem(p->d_descs, p->d_etiles, p->d_counts, mode, parity, grid, threads, p->stream);
     }
     cudaError_t err = cudaStreamEndCapture(p->stream, &g);
     if (err != cudaSuccess) return pfail(MSX_ERR_CUDA, std::string("pool graph capture: ") + cudaGetErrorString(err));
@@ -303,8 +298,11 @@ static msx_status replay(msx_pool *p, float *ms)
 // results are the same whichever one runs a step.
 static msx_status autotune(msx_pool *p)
 {
-    const Sched cands[] = {{128, 512, 8}, {256, 1024, 4}, {256, 2048, 4}, {256, 1024, 8},
-                           {512, 2048, 2}, {512, 4096, 2}, {128, 1024, 8}, {256, 512, 6}};
+    const int mode = p->opts.precision == MSX_PREC_MIXED ? MODE_MIXED : MODE_FP64;
+    const int occ128 = tiled_ctas_per_sm(mode, 128), occ256 = tiled_ctas_per_sm(mode, 256);
+    const Sched cands[] = {{128, 512, occ128}, {128, 1024, occ128}, {256, 512, occ256}, {256, 1024, occ256},
+                           {256, 2048, occ256}, {256, 4096, occ256}, {256, 1024, std::max(1, occ256 / 2)},
+                           {128, 2048, occ128}};
     const int spl = p->spl;
     p->spl = 2;
     double best = 1e300;
@@ -362,15 +360,20 @@ extern "C" msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out)
     cudaGetDevice(&p->device);
     cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device);
     p->spl = opts->steps_per_launch > 0 ? ((opts->steps_per_launch + 1) & ~1) : 32;
+    const int pmode = opts->precision == MSX_PREC_MIXED ? MODE_MIXED : MODE_FP64;
+    p->sched.threads = kStepThreads;
+    p->sched.ctas_per_sm = tiled_ctas_per_sm(pmode, kStepThreads);
     if (opts->elems_per_block > 0) {
-        p->sched.threads = opts->elems_per_block >= 512 ? 512 : (opts->elems_per_block >= 256 ? 256 : 128);
+        p->sched.threads = opts->elems_per_block >= 256 ? 256 : 128;
         p->sched.tile_elems = opts->elems_per_block;
+        p->sched.ctas_per_sm = tiled_ctas_per_sm(pmode, p->sched.threads);
         p->tuned = true;
     } else if (opts->tune_cache) {
         if (FILE *f = fopen(opts->tune_cache, "r")) {
             Sched s;
             if (fscanf(f, "%d %d %d", &s.threads, &s.tile_elems, &s.ctas_per_sm) == 3 && s.threads > 0 &&
-                s.threads <= 1024 && s.tile_elems > 0 && s.ctas_per_sm > 0) {
+                s.threads <= kStepThreads && s.tile_elems > 0 && s.ctas_per_sm > 0 &&
+                s.ctas_per_sm <= tiled_ctas_per_sm(pmode, s.threads)) {
                 p->sched = s;
                 p->tuned = true;
             }

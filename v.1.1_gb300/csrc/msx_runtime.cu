@@ -116,7 +116,12 @@ struct msx_handle {
     bool block_ready = false;
     long long block_steps = 0;
     double dt_init = 0;
-    launch_fn node = nullptr, elem = nullptr;
+    launch_fn node = nullptr, elem = nullptr;   // reference-order kernels (exact mode)
+    bool tiled = false;                          // FP64 / mixed: the shared tiled step kernels
+    DBuf<Problem> d_desc;
+    DBuf<Tile> d_etiles, d_ntiles;
+    DBuf<int> d_counts;
+    int tgrid = 0, tthreads = kStepThreads;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc[2] = {nullptr, nullptr};
     std::vector<int> h_node_bc;   // host copies for next_solver rebuilds
@@ -226,12 +231,55 @@ static void bind_problem(msx_handle *h)
 static msx_status set_mode(msx_handle *h, int precision)
 {
     switch (precision) {
-    case MSX_PREC_FP64: h->node = launch_node_fp64; h->elem = launch_elem_fp64; break;
-    case MSX_PREC_FP64_EXACT: h->node = launch_node_exact; h->elem = launch_elem_exact; break;
-    case MSX_PREC_MIXED: h->node = launch_node_mixed; h->elem = launch_elem_mixed; break;
+    case MSX_PREC_FP64: h->tiled = true; break;
+    case MSX_PREC_FP64_EXACT: h->tiled = false; h->node = launch_node_exact; h->elem = launch_elem_exact; break;
+    case MSX_PREC_MIXED: h->tiled = true; break;
     default: return fail(MSX_ERR_ARG, "unknown precision mode");
     }
     h->precision = precision;
+    return MSX_OK;
+}
+
+static int tiled_mode(const msx_handle *h) { return h->precision == MSX_PREC_MIXED ? MODE_MIXED : MODE_FP64; }
+
+// One step's kernels: the shared tiled pair for FP64 / mixed (the same
+// machine code the pool runs), the reference-order pair for exact mode.
+static void launch_step(msx_handle *h, int parity)
+{
+    if (h->tiled) {
+        launch_tiled_node(h->d_desc.p, h->d_ntiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
+                          h->stream);
+        launch_tiled_elem(h->d_desc.p, h->d_etiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
+                          h->stream);
+    } else {
+        h->node(h->P, parity, h->stream);
+        h->elem(h->P, parity, h->stream);
+    }
+}
+
+// Descriptor and one-solve tile list of the tiled kernels.
+static msx_status upload_tiled(msx_handle *h)
+{
+    if (!h->tiled) return MSX_OK;
+    const int te = 1024, tn = 1024;
+    if (!h->d_desc.p) {
+        std::vector<Tile> et, nt;
+        for (long long b = 0; b < h->P.ne; b += te) et.push_back({0, (int)b, (int)std::min<long long>(h->P.ne, b + te)});
+        for (long long b = 0; b < h->P.nn; b += tn) nt.push_back({0, (int)b, (int)std::min<long long>(h->P.nn, b + tn)});
+        int counts[2] = {(int)et.size(), (int)nt.size()};
+        MSX_CUDA(h->d_desc.alloc(1));
+        MSX_CUDA(h->d_etiles.alloc(et.size()));
+        MSX_CUDA(h->d_ntiles.alloc(nt.size()));
+        MSX_CUDA(h->d_counts.alloc(2));
+        MSX_CUDA(cudaMemcpyAsync(h->d_etiles.p, et.data(), sizeof(Tile) * et.size(), cudaMemcpyHostToDevice, h->stream));
+        MSX_CUDA(cudaMemcpyAsync(h->d_ntiles.p, nt.data(), sizeof(Tile) * nt.size(), cudaMemcpyHostToDevice, h->stream));
+        MSX_CUDA(cudaMemcpyAsync(h->d_counts.p, counts, sizeof(counts), cudaMemcpyHostToDevice, h->stream));
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    h->tgrid = sms * tiled_ctas_per_sm(tiled_mode(h), h->tthreads);
+    MSX_CUDA(cudaMemcpyAsync(h->d_desc.p, &h->P, sizeof(Problem), cudaMemcpyHostToDevice, h->stream));
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
     return MSX_OK;
 }
 
@@ -287,6 +335,8 @@ static msx_status set_opts(msx_handle *h, const msx_solver_opts *o)
 static msx_status init_block(msx_handle *h)
 {
     bind_problem(h);
+    msx_status tst = upload_tiled(h);
+    if (tst != MSX_OK) return tst;
     const Problem &P = h->P;
     unsigned long long inf[2] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL};
     MSX_CUDA(cudaMemcpyAsync(h->dtmin.p, inf, sizeof(inf), cudaMemcpyHostToDevice, h->stream));
@@ -316,11 +366,7 @@ static msx_status build_graph(msx_handle *h)
     bind_problem(h);
     cudaGraph_t g;
     MSX_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < h->spg; i++) {
-        int parity = (i & 1) ? 0 : 1;
-        h->node(h->P, parity, h->stream);
-        h->elem(h->P, parity, h->stream);
-    }
+    for (int i = 0; i < h->spg; i++) launch_step(h, (i & 1) ? 0 : 1);
     cudaError_t err = cudaStreamEndCapture(h->stream, &g);
     if (err != cudaSuccess) return fail(MSX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(err));
     err = cudaGraphInstantiate(&h->graph, g, 0);
@@ -486,6 +532,10 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     for (auto *b : {&h->node_ptr, &h->node_inc, &h->node_bc, &h->flags}) b->release();
     h->bc_rec.release();
     h->bcs.release();
+    h->d_desc.release();
+    h->d_etiles.release();
+    h->d_ntiles.release();
+    h->d_counts.release();
     h->ctrl.release();
     h->dtmin.release();
     if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
@@ -638,9 +688,17 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
     for (long long i = 0; i < n; i++) {
         int parity = (i & 1) ? 0 : 1;
         cudaEventRecord(ev[3 * i], h->stream);
-        h->node(h->P, parity, h->stream);
+        if (h->tiled)
+            launch_tiled_node(h->d_desc.p, h->d_ntiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
+                              h->stream);
+        else
+            h->node(h->P, parity, h->stream);
         cudaEventRecord(ev[3 * i + 1], h->stream);
-        h->elem(h->P, parity, h->stream);
+        if (h->tiled)
+            launch_tiled_elem(h->d_desc.p, h->d_etiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
+                              h->stream);
+        else
+            h->elem(h->P, parity, h->stream);
         cudaEventRecord(ev[3 * i + 2], h->stream);
     }
     cudaError_t err = cudaStreamSynchronize(h->stream);
