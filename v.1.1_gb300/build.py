@@ -24,6 +24,7 @@ UNITS = {
     "msx_fast.cu": [],
     "msx_runtime.cu": [],
     "msx_pool.cu": [],
+    "msx_noalloc.cu": ["--fmad=false"],
 }
 DECK = os.path.join(OUT, "msx_deck")
 

@@ -79,7 +79,8 @@ class PoolResult_(C.Structure):
 SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_solver", "msx_destroy",
            "msx_last_error", "msx_internal_force", "msx_get_element_data", "msx_profile", "msx_mesh_cube",
            "msx_stream", "msx_set_device", "msx_pool_create", "msx_pool_submit", "msx_pool_step",
-           "msx_pool_poll", "msx_pool_fetch", "msx_pool_destroy", "msx_pool_stats_get"]
+           "msx_pool_poll", "msx_pool_fetch", "msx_pool_destroy", "msx_pool_stats_get",
+           "msx_internal_force_noalloc"]
 
 _lib = None
 
