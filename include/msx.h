@@ -121,6 +121,23 @@ msx_status msx_set_state(msx_handle *h, const double *u, const double *v, const 
 msx_status msx_next_solver(msx_handle *h, const msx_bc *bcs, int64_t num_bcs,
                            const msx_solver_opts *opts);
 
+/* One nodal-force DOF of *BOUNDARY, TYPE=FORCE (deck block "t0, tf, Ff" then
+ * "node, Fx, Fy, Fz" lines): value = F_comp * Ff; the force at time t is
+ * value/(tf - t0) * t for t0 <= t <= tf and 0 outside, as
+ * classNeumann::getTracAmount computes it (spatialDiscretisation/classNodes.h:101-109). */
+typedef struct {
+    int64_t dof;
+    double t0, tf, value;
+} msx_nodal_force;
+
+/* Neumann loads of the explicit path (solvers/boundaryConditions.cpp:75-138):
+ * nodal forces in deck order and *GRAVITY g (force -w rho |J| g phi on the z
+ * DOFs, :1146-1171; 0 for none).  gravity_first = 1 when *GRAVITY comes before
+ * the force blocks in the deck (the summation order of the reference).
+ * Replaces any loads set before; takes effect from the next step. */
+msx_status msx_set_loads(msx_handle *h, const msx_nodal_force *forces, int64_t num_forces, double gravity,
+                         int32_t gravity_first);
+
 msx_status msx_destroy(msx_handle *h);
 
 /* Message of the last failing call on this host thread. */
@@ -136,6 +153,19 @@ msx_status msx_internal_force(msx_handle *h, const double *u, double *fint);
  * [num_elems], mass[num_nodes] (classLinearTetrahedra.cpp:129-268,
  * solverExplicit.cpp:429-459).  Any pointer may be NULL. */
 msx_status msx_get_element_data(msx_handle *h, double *G, double *wJ, double *Lref, double *mass);
+
+/* Initial dt of the current solver block (the undeformed CFL times the scale
+ * factor, solverExplicit.cpp:165-166); sets the block up without stepping.
+ * The reference derives its output cadence from it (solverExplicit.cpp:171-174). */
+msx_status msx_initial_dt(msx_handle *h, double *dt_init);
+
+/* Element output fields of the current state, host buffers: Cauchy stress and
+ * Green-Lagrange strain (9 doubles per element, row-major) and von Mises
+ * stress (1 per element), in the reference's operation order
+ * (maths.cpp:1227-1271; the Neo-Hookean law's own sigma; zero strain for the
+ * compressible neo-Hookean law, which never updates it).  Any may be NULL.
+ * Computed on the device only when called, i.e. at output steps. */
+msx_status msx_element_fields(msx_handle *h, double *cauchy, double *green_lagrange, double *von_mises);
 
 /* Run `steps` steps launching each kernel separately with CUDA events around
  * it on the library's stream, and report the mean kernel durations. */

@@ -255,6 +255,69 @@ static void element_force(const double *dphi, double wJ, const orc_material *m,
     if (Po) memcpy(Po, P, sizeof P);
 }
 
+/* Output fields: F (constitutiveManager.cpp:151-164); Cauchy = the
+ * Neo-Hookean law's sigma (hyperElasticNeoHookean.cpp:113-124) or P F^T / J
+ * (maths.cpp:1250-1254 computeCauchy) for the other two laws; Green-Lagrange
+ * (maths.cpp:1227-1243); von Mises (maths.cpp:1261-1271). */
+int orc_element_fields(int64_t nn, int64_t ne, const int32_t *conn, const double *dphi, const int32_t *elem_mat,
+                       const orc_material *mats, const double *u, double *cauchy, double *gl, double *vms)
+{
+    for (int64_t e = 0; e < ne; e++) {
+        const double *dp = dphi + 12 * e;
+        const orc_material *m = &mats[elem_mat ? elem_mat[e] : 0];
+        double F[9], P[9], S[9], C[9];
+        for (int i = 0; i < 9; i++) F[i] = 0.;
+        for (int i = 0; i < 3; i++) {
+            F[i * 3 + i] += 1.;
+            for (int a = 0; a < 4; a++)
+                for (int j = 0; j < 3; j++) F[i * 3 + j] += dp[a * 3 + j] * u[conn[e * 4 + a] + i * nn];
+        }
+        if (m->law == ORC_NEO_HOOKEAN) {
+            double E = m->young, nu = m->nu, mu = 0.5 * E / (1. + nu), K1 = E / (3 * (1 - 2 * nu)), B[9];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) {
+                    double c = 0;
+                    for (int k = 0; k < 3; k++) c += F[i * 3 + k] * F[j * 3 + k];
+                    B[i * 3 + j] = c;
+                }
+            double J = det3(F), trB = 0;
+            for (int i = 0; i < 3; i++) trB += B[i * 3 + i];
+            double fact1 = pow(J, 5.0 / 3.0), fact2 = mu / fact1;
+            for (int i = 0; i < 9; i++) S[i] = 0 + fact2 * B[i];
+            double fact3 = -(mu / 3.0) * trB / fact1 + K1 * (J - 1.0);
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) S[i * 3 + j] += fact3 * (i == j ? 1.0 : 0.0);
+        } else {
+            orc_stress(m, F, P);
+            double detJinv = 1. / det3(F);
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) {
+                    double c = 0;
+                    for (int k = 0; k < 3; k++) c += P[i * 3 + k] * F[j * 3 + k];
+                    S[i * 3 + j] = c;
+                }
+            for (int i = 0; i < 9; i++) S[i] = S[i] * detJinv;
+        }
+        /* the compressible neo-Hookean law never updates its Green-Lagrange
+         * strain (hyperElasticNeoHookean.cpp:221-289 has no computeGL), so the
+         * reference reports it as zero */
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+                for (int k = 0; k < 3; k++) c += F[k * 3 + i] * F[k * 3 + j];
+                C[i * 3 + j] = m->law == ORC_COMPRESSIBLE_NH ? 0.0 : 0.5 * (c - (i == j ? 1.0 : 0.0));
+            }
+        for (int k = 0; k < 9; k++) {
+            if (cauchy) cauchy[e * 9 + k] = S[k];
+            if (gl) gl[e * 9 + k] = C[k];
+        }
+        if (vms)
+            vms[e] = sqrt(0.5 * ((S[0] - S[4]) * (S[0] - S[4]) + (S[4] - S[8]) * (S[4] - S[8]) +
+                                 (S[8] - S[0]) * (S[8] - S[0]) + 6 * (S[1] * S[1] + S[2] * S[2] + S[5] * S[5])));
+    }
+    return ORC_OK;
+}
+
 /* solverExplicit.cpp:363-379 computeInternalForce: scatter in element order. */
 int orc_internal_force(int64_t nn, int64_t ne, const int32_t *conn, const double *dphi,
                        const double *wJ, const int32_t *elem_mat, const orc_material *mats,
@@ -312,6 +375,35 @@ static double critical_dt(int64_t nn, int64_t ne, const double *X, const int32_t
     return best;
 }
 
+/* External force at time t, src/solvers/boundaryConditions.cpp:75-138
+ * (NeumannBCManagement): nodal forces (:17-34 BCsNodalForces with
+ * classNeumann::getTracAmount, classNodes.h:101-109, slope value/(tf-t0)
+ * times the absolute time inside [t0, tf]) and gravity (:1146-1171 BCsGravity,
+ * -w rho |J| g phi_a on the z DOF, element order), in the order of the deck. */
+static void external_force(const orc_problem *p, const double *absJ, double t, double *fext)
+{
+    const int64_t nn = p->nn;
+    for (int64_t i = 0; i < 3 * nn; i++) fext[i] = 0;
+    for (int pass = 0; pass < 2; pass++) {
+        int gravity_now = (pass == 0) == (p->gravity_first != 0);
+        if (gravity_now) {
+            if (p->gravity == 0) continue;
+            const double w = 0.166666666667, phi = -1.0 * 0.25 - 1.0 * 0.25 - 1.0 * 0.25 + 1.0;
+            for (int64_t e = 0; e < p->ne; e++) {
+                double rho = p->mats[p->elem_mat ? p->elem_mat[e] : 0].rho;
+                for (int a = 0; a < 4; a++) fext[p->conn[e * 4 + a] + 2 * nn] += -w * rho * absJ[e] * p->gravity * phi;
+            }
+        } else {
+            for (int64_t k = 0; k < p->nforces; k++) {
+                const orc_force *f = &p->forces[k];
+                double m = f->value / (f->tf - f->t0);
+                double F = (t >= f->t0 && t <= f->tf) ? m * t : 0;
+                fext[f->dof] += F;
+            }
+        }
+    }
+}
+
 /* The explicit solve, src/solvers/solverExplicit.cpp:63-338 (sequential build):
  * time advance with the previous dt (:227-232), dt from the deformed CFL
  * (:267-276), prediction (nonlinearSystem.cpp:1186-1200), Dirichlet
@@ -326,14 +418,22 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
     double *Lref = malloc(sizeof(double) * (size_t)ne), *cel = malloc(sizeof(double) * (size_t)ne);
     double *mass = malloc(sizeof(double) * (size_t)nn), *fint = malloc(sizeof(double) * (size_t)ndof);
     double *uK = malloc(sizeof(double) * (size_t)ndof), *aprev = malloc(sizeof(double) * (size_t)ndof);
+    double *fext = malloc(sizeof(double) * (size_t)ndof), *absJ = malloc(sizeof(double) * (size_t)ne);
     char *cons = calloc((size_t)ndof, 1);
     int32_t *flag = malloc(sizeof(int32_t) * (size_t)(p->nbc > 0 ? p->nbc : 1));
     double *UU = malloc(sizeof(double) * (size_t)(p->nbc > 0 ? p->nbc : 1));
-    if (!dphi || !wJ || !Lref || !cel || !mass || !fint || !uK || !aprev || !cons || !flag || !UU) {
+    if (!dphi || !wJ || !Lref || !cel || !mass || !fint || !uK || !aprev || !cons || !flag || !UU || !fext || !absJ) {
         rc = ORC_ERR_ARG;
         goto done;
     }
     if ((rc = orc_precompute(nn, ne, p->X, p->conn, dphi, wJ, Lref)) != ORC_OK) goto done;
+    /* |det J| of each element, as classGPs::getJ returns it (classGPs.cpp:24-31) */
+    for (int64_t e = 0; e < ne; e++) {
+        double M[9];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) M[i * 3 + j] = p->X[i * nn + p->conn[e * 4 + j + 1]] - p->X[i * nn + p->conn[e * 4]];
+        absJ[e] = fabs(det3(M));
+    }
     orc_lumped_mass(nn, ne, p->conn, wJ, p->elem_mat, p->mats, mass);
     for (int64_t e = 0; e < ne; e++) cel[e] = orc_sound_speed(&p->mats[p->elem_mat ? p->elem_mat[e] : 0]);
     /* classNodes.cpp:58-74: ramp stores U/duration (flag -1), inst stores U (flag 1) */
@@ -386,12 +486,13 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
             a[d] = 0.;
         }
         orc_internal_force(nn, ne, p->conn, dphi, wJ, p->elem_mat, p->mats, u, fint, 0, 0, p->nthreads);
+        external_force(p, absJ, t, fext);
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static) num_threads(p->nthreads > 0 ? p->nthreads : 1)
 #endif
         for (int64_t j = 0; j < ndof; j++) {
             if (cons[j]) continue;
-            double val = -fint[j] + 0.0;
+            double val = -fint[j] + fext[j];
             double rhs = 0;
             rhs += val;
             a[j] = rhs / mass[j % nn];
@@ -411,7 +512,7 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
     }
 done:
     free(dphi); free(wJ); free(Lref); free(cel); free(mass); free(fint);
-    free(uK); free(aprev); free(cons); free(flag); free(UU);
+    free(uK); free(aprev); free(cons); free(flag); free(UU); free(fext); free(absJ);
     return rc;
 }
 

@@ -31,6 +31,8 @@ enum { ORC_NEO_HOOKEAN = 0,          /* "Neo-Hookean" (Belytschko form)      */
 enum { ORC_BC_RAMP = 0, ORC_BC_INST = 1, ORC_BC_VEL_RAMP = 2 };
 
 typedef struct { int32_t law; double young, nu, rho; } orc_material;
+/* one nodal force DOF of *BOUNDARY, TYPE=FORCE: value = F_k * Ff over [t0, tf] */
+typedef struct { int64_t dof; double t0, tf, value; } orc_force;
 typedef struct { int64_t dof; int32_t mode; int32_t ramp_steps; double value; } orc_bc;
 
 typedef struct {
@@ -44,6 +46,9 @@ typedef struct {
     int64_t max_steps;        /* 0: run to tf as the reference does          */
     int32_t first_step_zero_uK; /* 1: the reference's chained-solver quirk   */
     int32_t nthreads;
+    const orc_force *forces; int64_t nforces;  /* nodal forces, input order   */
+    double gravity;           /* *GRAVITY g (0: none), applied on the z DOFs  */
+    int32_t gravity_first;    /* 1: *GRAVITY precedes *BOUNDARY, TYPE=FORCE   */
 } orc_problem;
 
 typedef struct { int64_t steps; double t, dt_last, dt_init; int32_t status; double loop_seconds; } orc_result;
@@ -67,6 +72,10 @@ double orc_char_length(const double *x);
 int orc_internal_force(int64_t nn, int64_t ne, const int32_t *conn, const double *dphi,
                        const double *wJ, const int32_t *elem_mat, const orc_material *mats,
                        const double *u, double *fint, double *F_out, double *P_out, int nthreads);
+/* Element output fields of displacement u: Cauchy and Green-Lagrange (9 per
+ * element) and von Mises (1 per element), as the reference's laws store them. */
+int orc_element_fields(int64_t nn, int64_t ne, const int32_t *conn, const double *dphi, const int32_t *elem_mat,
+                       const orc_material *mats, const double *u, double *cauchy, double *gl, double *vms);
 /* Full explicit solve; u,v,a (3*nn each) in = initial, out = final.
  * dt_hist (optional) receives one dt per executed step (max_hist entries). */
 int orc_run(const orc_problem *p, double *u, double *v, double *a,

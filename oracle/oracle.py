@@ -33,6 +33,10 @@ class _Mat(C.Structure):
     _fields_ = [("law", C.c_int32), ("young", C.c_double), ("nu", C.c_double), ("rho", C.c_double)]
 
 
+class _Force(C.Structure):
+    _fields_ = [("dof", C.c_int64), ("t0", C.c_double), ("tf", C.c_double), ("value", C.c_double)]
+
+
 class _BC(C.Structure):
     _fields_ = [("dof", C.c_int64), ("mode", C.c_int32), ("ramp_steps", C.c_int32), ("value", C.c_double)]
 
@@ -42,7 +46,9 @@ class _Problem(C.Structure):
                 ("elem_mat", C.c_void_p), ("mats", C.c_void_p), ("nmat", C.c_int32),
                 ("bcs", C.c_void_p), ("nbc", C.c_int64), ("t0", C.c_double), ("tf", C.c_double),
                 ("scale_factor", C.c_double), ("max_steps", C.c_int64),
-                ("first_step_zero_uK", C.c_int32), ("nthreads", C.c_int32)]
+                ("first_step_zero_uK", C.c_int32), ("nthreads", C.c_int32),
+                ("forces", C.c_void_p), ("nforces", C.c_int64), ("gravity", C.c_double),
+                ("gravity_first", C.c_int32)]
 
 
 class _Result(C.Structure):
@@ -86,6 +92,8 @@ def lib():
         _lib.orc_sound_speed.restype = C.c_double
         _lib.orc_char_length.argtypes = [C.c_void_p]
         _lib.orc_char_length.restype = C.c_double
+        _lib.orc_element_fields.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_internal_force.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.c_int]
@@ -102,6 +110,31 @@ class Material:
     young: float = 1e6
     nu: float = 0.3
     rho: float = 1000.0
+
+
+@dataclass
+class Loads:
+    """Neumann loads of a deck, in deck order: ("force", t0, tf, Ff, [(node, Fx, Fy, Fz), ...])
+    for *BOUNDARY, TYPE=FORCE and ("gravity", g) for *GRAVITY."""
+    items: list = field(default_factory=list)
+
+    def force_entries(self, nn):
+        out = []
+        for it in self.items:
+            if it[0] == "force":
+                _, t0, tf, Ff, rows = it
+                for node, *F in rows:
+                    for k in range(3):
+                        out.append((node + k * nn, t0, tf, F[k] * Ff))
+        return out
+
+    def gravity(self):
+        g = [it[1] for it in self.items if it[0] == "gravity"]
+        return g[-1] if g else 0.0
+
+    def gravity_first(self):
+        kinds = [it[0] for it in self.items]
+        return 1 if kinds and kinds[0] == "gravity" else 0
 
 
 @dataclass
@@ -218,6 +251,40 @@ def internal_force(mesh: Mesh, mats, u: np.ndarray, nthreads: int = 1):
     return f, F, P
 
 
+def element_fields(mesh: Mesh, mats, u: np.ndarray):
+    """Cauchy (ne,3,3), Green-Lagrange (ne,3,3), von Mises (ne,) of displacement u."""
+    dphi, _, _ = precompute(mesh)
+    ne = mesh.ne
+    c, g, v = np.zeros(9 * ne), np.zeros(9 * ne), np.zeros(ne)
+    arr = _mats_array(mats)
+    em = None if mesh.elem_mat is None else np.ascontiguousarray(mesh.elem_mat, np.int32)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    lib().orc_element_fields(mesh.nn, ne, _p(np.ascontiguousarray(mesh.conn)), _p(dphi), _p(em),
+                             C.cast(arr, C.c_void_p), _p(u), _p(c), _p(g), _p(v))
+    return c.reshape(-1, 3, 3), g.reshape(-1, 3, 3), v
+
+
+def read_vtk_outputs(outdir: str):
+    """The reference's VTK outputs: list of (time, Cauchy (ne,9), E (ne,9), VMS (ne,))
+    read from allOutputs_0.vtk.series and MuPhiSimOutputs_0_.<k>.vtk (6 digits)."""
+    import json
+    series = json.load(open(os.path.join(outdir, "allOutputs_0.vtk.series")))
+    out = []
+    for item in series["files"]:
+        toks = open(os.path.join(outdir, item["name"])).read().split()
+        ne = int(toks[toks.index("CELL_DATA") + 1])
+
+        def block(kind, tag, width, skip):
+            i = next(k for k in range(len(toks) - 1) if toks[k] == kind and toks[k + 1] == tag)
+            start = i + skip
+            return np.array(toks[start:start + ne * width], dtype=np.float64).reshape(ne, width)
+        cau = block("TENSORS", "Cauchy", 9, 3)
+        E = block("TENSORS", "E", 9, 3)
+        vms = block("SCALARS", "VMS", 1, 5)[:, 0]
+        out.append((float(item["time"]), cau, E, vms))
+    return out
+
+
 @dataclass
 class RunResult:
     u: np.ndarray
@@ -232,7 +299,7 @@ class RunResult:
     loop_seconds: float = 0.0
 
 
-def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int = 0) -> RunResult:
+def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int = 0, loads: Loads = None) -> RunResult:
     """Run a chain of explicit solver blocks as the reference's main does."""
     nn = mesh.nn
     if state is None:
@@ -247,13 +314,18 @@ def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int 
     loop_s = 0.0
     res = _Result()
     hist_all = []
+    fl = loads.force_entries(nn) if loads else []
+    farr = (_Force * max(1, len(fl)))()
+    for i, f in enumerate(fl):
+        farr[i] = _Force(*f)
     for k, s in enumerate(solvers):
         barr = (_BC * max(1, len(s.bcs)))()
         for i, (dof, mode, value, ramp) in enumerate(s.bcs):
             barr[i] = _BC(dof, mode, ramp, value)
         prob = _Problem(nn, mesh.ne, _p(X), _p(conn), _p(em), C.cast(marr, C.c_void_p), len(mats),
                         C.cast(barr, C.c_void_p), len(s.bcs), s.t0, s.tf, s.scale_factor, s.max_steps,
-                        0, nthreads)
+                        0, nthreads, C.cast(farr, C.c_void_p), len(fl),
+                        loads.gravity() if loads else 0.0, loads.gravity_first() if loads else 0)
         hist = np.zeros(max(1, max_hist))
         rc = lib().orc_run(C.byref(prob), _p(u), _p(v), _p(a), _p(hist), max_hist, C.byref(res))
         total += res.steps
@@ -266,7 +338,7 @@ def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int 
 
 
 # ---------------------------------------------------------------- the reference
-def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None):
+def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Loads = None):
     """Abaqus-style deck in the keyword subset the reference parses
     (src/IO/inputFile.cpp: nodes :20-108, C3D4 elements :118-323, materials
     :838-1029, solver blocks :2253-2831, displacement BCs :2960-3218)."""
@@ -280,6 +352,14 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None):
         lines.append("%d, %d, %d, %d, %d" % (e + 1, c[0], c[1], c[2], c[3]))
     lines += ["*FEM Nodes", "All", "*FEM Elements", "All"]
     nn = mesh.nn
+    # Neumann loads (src/IO/inputFile.cpp:4705-4735 and 2841-2945), in deck order
+    for it in (loads.items if loads else []):
+        if it[0] == "force":
+            _, t0, tf, Ff, rows = it
+            lines += ["*BOUNDARY, TYPE=FORCE", "%.17g, %.17g, %.17g" % (t0, tf, Ff)]
+            lines += ["%d, %.17g, %.17g, %.17g" % (node + 1, F0, F1, F2) for node, F0, F1, F2 in rows]
+        else:
+            lines += ["*GRAVITY", "%.17g" % it[1]]
     for s in solvers:
         if any(b[1] == BC_VEL_RAMP for b in s.bcs):
             raise ValueError("the reference has no velocity-ramp boundary condition")
@@ -310,7 +390,8 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None):
         f.write("\n".join(lines) + "\n")
 
 
-def run_reference(mesh: Mesh, mats, solvers, workdir: str | None = None, timeout: float = 3600):
+def run_reference(mesh: Mesh, mats, solvers, workdir: str | None = None, timeout: float = 3600,
+                  loads: Loads = None):
     """Run the shim-built reference on a deck; returns (u, v, a, solve_wall_s)."""
     if not os.path.exists(REF_BIN):
         raise FileNotFoundError("reference binary not built: make -C oracle ref")
@@ -320,7 +401,7 @@ def run_reference(mesh: Mesh, mats, solvers, workdir: str | None = None, timeout
     mat_elems = None
     if mesh.elem_mat is not None:
         mat_elems = [np.nonzero(mesh.elem_mat == k)[0] for k in range(len(mats))]
-    write_deck(os.path.join(wd, "deck.inp"), mesh, mats, solvers, mat_elems)
+    write_deck(os.path.join(wd, "deck.inp"), mesh, mats, solvers, mat_elems, loads)
     dump, timing = os.path.join(wd, "final.bin"), os.path.join(wd, "timing.txt")
     r = subprocess.run([REF_BIN, "-input", "deck.inp", "-inputDir", ".", "-outputDir", "out",
                         "-dump", dump, "-timing", timing], cwd=wd, capture_output=True, text=True,
@@ -330,4 +411,4 @@ def run_reference(mesh: Mesh, mats, solvers, workdir: str | None = None, timeout
     data = np.fromfile(dump, dtype=np.float64)
     n = 3 * mesh.nn
     wall = float(open(timing).read())
-    return data[:n], data[n:2 * n], data[2 * n:3 * n], wall, r.stdout
+    return data[:n], data[n:2 * n], data[2 * n:3 * n], wall, r.stdout, os.path.join(wd, "out")

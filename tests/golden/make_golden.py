@@ -57,20 +57,33 @@ def cases(ref_src):
     bcs = [(node + c * nn, O.BC_RAMP, (-0.5 if (node, c) == (3, 1) else 0.0), 0)
            for node in (0, 3, 6, 7) for c in range(3)]
     out["tet12_stvk"] = (t12, [O.Material(stvk, 1e9, 0.3, 1000.0)], [O.Solver(0.0, 0.05, 0.1, bcs)])
+    top = [i + 4 * j + 16 * 3 for j in range(4) for i in range(4)]
+    forces = ("force", 0.0, 0.015, 2.5, [(nd, 0.1 * k, -0.2, 0.3) for k, nd in enumerate(top[:6])])
+    out["cube3_cnh_force_gravity"] = (m3, [O.Material(cnh)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.0))],
+                                      O.Loads([forces, ("gravity", 9.81)]))
+    out["cube3_nh_gravity_force"] = (m3, [O.Material(nh)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.0))],
+                                     O.Loads([("gravity", 9.81), forces]))
     m10 = O.cube_mesh(10)
     for name, law in (("cnh", cnh), ("nh", nh), ("stvk", stvk)):
         out["cube10_%s_S" % name] = (m10, [O.Material(law)], [O.Solver(0.0, 0.5, 0.5, O.cube_bcs(10, 0.05))])
     return out
 
 
-def pack(mesh, mats, solvers, ref, orc):
+def pack(mesh, mats, solvers, ref, orc, loads=None):
+    outs = O.read_vtk_outputs(ref[5])
+    t_last, cau, E, vms = outs[-1]
     d = {"X": mesh.X, "conn": mesh.conn,
+         # the reference's own VTK output of the final state (6 significant digits)
+         "vtk_times": np.array([o[0] for o in outs]), "vtk_cauchy": cau, "vtk_E": E, "vtk_vms": vms,
          "mats": np.array([[m.law, m.young, m.nu, m.rho] for m in mats]),
          "solvers": np.array([[s.t0, s.tf, s.scale_factor, len(s.bcs)] for s in solvers]),
          "bcs": np.array([[b[0], b[1], b[2], b[3]] for s in solvers for b in s.bcs], dtype=np.float64),
          "u": ref[0], "v": ref[1], "a": ref[2], "steps": np.array(orc.steps)}
     if mesh.elem_mat is not None:
         d["elem_mat"] = mesh.elem_mat
+    if loads is not None:
+        import json
+        d["loads_json"] = np.array(json.dumps(loads.items))
     return d
 
 
@@ -79,12 +92,14 @@ def main():
     O.build()
     if O.build_reference() is None:
         raise SystemExit("reference sources not found at " + ref_src)
-    for name, (mesh, mats, solvers) in cases(ref_src).items():
-        ref = O.run_reference(mesh, mats, solvers)
-        orc = O.run(mesh, mats, solvers)
+    for name, case in cases(ref_src).items():
+        mesh, mats, solvers = case[:3]
+        loads = case[3] if len(case) > 3 else None
+        ref = O.run_reference(mesh, mats, solvers, loads=loads)
+        orc = O.run(mesh, mats, solvers, loads=loads)
         same = all(np.array_equal(x, y) for x, y in zip((orc.u, orc.v, orc.a), ref[:3]))
         print("%-22s steps %5d  oracle==reference bitwise: %s  ref solve %.2fs" % (name, orc.steps, same, ref[3]))
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), **pack(mesh, mats, solvers, ref, orc))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **pack(mesh, mats, solvers, ref, orc, loads))
 
 
 if __name__ == "__main__":

@@ -25,3 +25,13 @@ def load(name):
         k += nb
         solvers.append(O.Solver(float(t0), float(tf), float(sf), bcs))
     return mesh, mats, solvers, (d["u"], d["v"], d["a"]), int(d["steps"])
+
+
+def load_loads(name):
+    """The Neumann loads of a case (oracle.Loads) or None."""
+    import json
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    if "loads_json" not in d:
+        return None
+    return O.Loads([tuple(it) if it[0] == "gravity" else (it[0], it[1], it[2], it[3], [tuple(r) for r in it[4]])
+                    for it in json.loads(str(d["loads_json"]))])

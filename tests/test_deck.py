@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from golden_cases import load, names
+from golden_cases import load, load_loads, names
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DECK = os.path.join(ROOT, "v.1.1_gb300", "_build", "msx_deck")
@@ -26,11 +26,12 @@ def write(tmp_path, name):
     mat_elems = None
     if mesh.elem_mat is not None:
         mat_elems = [np.nonzero(mesh.elem_mat == k)[0] for k in range(len(mats))]
-    O.write_deck(str(tmp_path / "deck.inp"), mesh, mats, solvers, mat_elems)
+    O.write_deck(str(tmp_path / "deck.inp"), mesh, mats, solvers, mat_elems, load_loads(name))
     return mesh, mats, solvers, ref, steps
 
 
-@pytest.mark.parametrize("name", ["cube3_cnh_chain", "cube2_two_materials", "cube3_cnh_inst", "tet12_stvk"])
+@pytest.mark.parametrize("name", ["cube3_cnh_chain", "cube2_two_materials", "cube3_cnh_inst", "tet12_stvk",
+                                  "cube3_cnh_force_gravity", "cube3_nh_gravity_force"])
 def test_parse_summary(tmp_path, name):
     mesh, mats, solvers, _, _ = write(tmp_path, name)
     r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-parse-only"],
@@ -38,6 +39,10 @@ def test_parse_summary(tmp_path, name):
     d = json.loads(r.stdout)
     assert d["nodes"] == mesh.nn and d["elements"] == mesh.ne
     assert d["materials"] == len(mats) and d["solvers"] == len(solvers)
+    L = load_loads(name)
+    assert d["forces"] == (len(L.force_entries(mesh.nn)) if L else 0)
+    assert d["gravity"] == (L.gravity() if L else 0.0)
+    assert d["gravity_first"] == (L.gravity_first() if L else 0)
     for blk, s in zip(d["blocks"], solvers):
         assert (blk["t0"], blk["tf"], blk["sf"], blk["bcs"]) == (s.t0, s.tf, s.scale_factor, len(s.bcs))
 
@@ -62,3 +67,25 @@ def test_deck_run_matches_reference(tmp_path, name):
     assert ("total %d steps" % steps) in r.stdout
     d = np.fromfile(out, dtype=np.float64).reshape(3, -1)
     assert np.linalg.norm(d[0] - u) <= 1e-12 * np.linalg.norm(u)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["cube3_cnh_ramp", "cube3_cnh_chain", "cube10_stvk_S"])
+def test_deck_outputs_follow_reference_cadence(tmp_path, name):
+    """VTK outputs at the reference's *Outputs cadence, final fields as the
+    reference's own VTK file (6 digits there)."""
+    mesh, mats, solvers, ref, steps = write(tmp_path, name)
+    d = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+    outdir = tmp_path / "out"
+    outdir.mkdir()
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-outputDir", str(outdir),
+                        "-precision", "exact"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    outs = O.read_vtk_outputs(str(outdir))
+    times = np.array([o[0] for o in outs])
+    assert len(times) == len(d["vtk_times"])
+    assert np.allclose(times, d["vtk_times"], rtol=1e-5, atol=1e-12)
+    _, cau, E, vms = outs[-1]
+    for mine, refv in ((cau, d["vtk_cauchy"]), (E, d["vtk_E"]), (vms, d["vtk_vms"])):
+        scale = max(np.abs(refv).max(), 1e-300)
+        assert np.all(np.abs(mine - refv) <= 6e-6 * np.abs(refv) + 1e-6 * scale)

@@ -7,7 +7,7 @@ import pytest
 
 import msx
 import oracle as O
-from golden_cases import load, names
+from golden_cases import load, load_loads, names
 
 pytestmark = pytest.mark.gpu
 
@@ -29,6 +29,9 @@ def run_case(name, precision, spg=0):
     s0 = solvers[0]
     S = msx.Solver(mesh.X, mesh.conn, m, s0.bcs, s0.t0, s0.tf, s0.scale_factor, precision=precision,
                    elem_material=mesh.elem_mat, steps_per_graph=spg)
+    L = load_loads(name)
+    if L is not None:
+        S.set_loads(L.force_entries(mesh.nn), L.gravity(), L.gravity_first())
     total = S.run().steps
     for s in solvers[1:]:
         S.next_solver(s.bcs, s.t0, s.tf, s.scale_factor, precision=precision, steps_per_graph=spg)
@@ -155,3 +158,16 @@ def test_degenerate_element_gives_negative_jacobian_error():
     with pytest.raises(msx.MsxError) as ei:
         S.run()
     assert ei.value.status == 3
+
+
+@pytest.mark.parametrize("name", ["cube4_nh_ramp", "cube4_stvk_ramp", "cube10_cnh_S", "cube2_two_materials"])
+def test_element_fields_match_oracle(name):
+    mesh, mats, solvers, (u, v, a), _ = load(name)
+    m = [(x.law, x.young, x.nu, x.rho) for x in mats]
+    S = msx.Solver(mesh.X, mesh.conn, m, solvers[0].bcs, 0.0, 1.0, 0.5, elem_material=mesh.elem_mat)
+    S.set_state(u=u)
+    cau, E, vms = S.element_fields()
+    S.close()
+    oc, oE, ov = O.element_fields(mesh, mats, u)
+    for x, y in ((cau, oc), (E, oE), (vms, ov)):
+        assert rel(x, y) <= 1e-12, rel(x, y)

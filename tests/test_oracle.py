@@ -4,13 +4,13 @@ import numpy as np
 import pytest
 
 import oracle as O
-from golden_cases import load, names
+from golden_cases import load, load_loads, names
 
 
 @pytest.mark.parametrize("name", names())
 def test_oracle_matches_reference_bitwise(name):
     mesh, mats, solvers, (u, v, a), steps = load(name)
-    r = O.run(mesh, mats, solvers, nthreads=2)
+    r = O.run(mesh, mats, solvers, nthreads=2, loads=load_loads(name))
     assert r.status == 0 and r.steps == steps
     # the oracle keeps the reference's operation order: identical bits
     assert np.array_equal(r.u, u)
@@ -73,3 +73,17 @@ def test_rigid_translation_gives_zero_force():
     u[2 * m.nn:] = -0.1
     f, F, P = O.internal_force(m, [O.Material(O.COMPRESSIBLE_NH)], u)
     assert np.abs(f).max() < 1e-9
+
+
+@pytest.mark.parametrize("name", names())
+def test_oracle_output_fields_match_reference_vtk(name):
+    """Cauchy, Green-Lagrange and von Mises of the final state against the
+    reference's own VTK output (written with 6 significant digits)."""
+    import numpy as np
+    from golden_cases import GOLDEN
+    mesh, mats, solvers, (u, v, a), steps = load(name)
+    d = np.load(GOLDEN + "/" + name + ".npz")
+    cau, E, vms = O.element_fields(mesh, mats, u)
+    for mine, ref in ((cau.reshape(-1, 9), d["vtk_cauchy"]), (E.reshape(-1, 9), d["vtk_E"]), (vms, d["vtk_vms"])):
+        scale = max(np.abs(ref).max(), 1e-300)
+        assert np.all(np.abs(mine - ref) <= 6e-6 * np.abs(ref) + 1e-6 * scale)

@@ -2,8 +2,15 @@
 // the C ABI, as `MuPhiSim -input <deck>` runs it through the reference's
 // solver chain (src/main.cpp:37-217).
 //
-//   msx_deck -input deck.inp [-inputDir d] [-precision fp64|exact|mixed]
+//   msx_deck -input deck.inp [-inputDir d] [-outputDir o] [-precision fp64|exact|mixed]
 //            [-dump final.bin] [-csv final.csv] [-parse-only]
+//
+// With -outputDir, VTK files MuPhiSimOutputs_0_.<k>.vtk and the series index
+// allOutputs_0.vtk.series are written at the reference's *Outputs cadence
+// (solverExplicit.cpp:171-174, 310-321): at t0 when t0 < 1e-12, then every
+// long(long((tf - t0)/dt0)/outputs) steps and when the block ends at tf; the
+// element fields (Cauchy, Green-Lagrange, von Mises) are computed on the
+// device only at those steps.  Values are written at full precision.
 //
 // Keyword subset (src/IO/inputFile.cpp): *Node (:20-108), *Element, type=C3D4
 // (:118-323), *FEM Nodes / *FEM Elements, *MATERIAL with *Density,
@@ -36,6 +43,10 @@ struct SolverBlock {
 
 struct Deck {
     std::vector<double> xyz;          // node-major while reading
+    struct Force { long long node; int comp; double t0, tf, value; };
+    std::vector<Force> forces;        // *BOUNDARY, TYPE=FORCE entries in deck order
+    double gravity = 0;
+    int gravity_first = 0;
     std::vector<int32_t> conn;
     std::vector<msx_material> mats;
     std::vector<int32_t> elem_mat;    // -1 until assigned
@@ -95,6 +106,23 @@ Deck parse(const std::string &path)
                 if (f.size() != 5) die("a C3D4 line has id and 4 nodes", (int)i + 1);
                 for (int c = 1; c < 5; c++) d.conn.push_back(atoi(f[c].c_str()) - 1);
             }
+        } else if (starts(L, "*BOUNDARY, TYPE=FORCE")) {
+            // src/IO/inputFile.cpp:2841-2945: "t0, tf, Ff" then "node, Fx, Fy, Fz"
+            auto h = split(lines[i + 1]);
+            if (h.size() != 3) die("a force block starts with t0, tf, Ff", (int)i + 2);
+            double t0 = atof(h[0].c_str()), tf = atof(h[1].c_str()), Ff = atof(h[2].c_str());
+            for (i += 2; data_line(i); i++) {
+                auto f = split(lines[i]);
+                if (f.size() != 4) die("a force line has node, Fx, Fy, Fz", (int)i + 1);
+                long long node = atoll(f[0].c_str()) - 1;
+                if (node < 0 || node >= (long long)d.xyz.size() / 3) die("force node out of range", (int)i + 1);
+                for (int c = 0; c < 3; c++) d.forces.push_back({node, c, t0, tf, atof(f[c + 1].c_str()) * Ff});
+            }
+        } else if (starts(L, "*GRAVITY")) {
+            // src/IO/inputFile.cpp:4723-4735
+            d.gravity = atof(lines[i + 1].c_str());
+            if (d.forces.empty()) d.gravity_first = 1;
+            i += 2;
         } else if (starts(L, "*FEM Nodes") || starts(L, "*FEM Elements")) {
             if (i + 1 >= n || !starts(lines[i + 1], "All")) die("only 'All' FEM sets are supported", ln);
             i += 2;
@@ -201,11 +229,72 @@ Deck parse(const std::string &path)
     return d;
 }
 
+// One output file in the reference's VTK layout (src/IO/output.cpp:296-700):
+// undeformed points, C3D4 cells, nodal displacement / velocity /
+// acceleration, element Cauchy, Green-Lagrange and von Mises.
+bool write_vtk(const std::string &dir, int index, double t, const std::vector<double> &X, const std::vector<int32_t> &conn,
+               msx_handle *h)
+{
+    const long long nn = (long long)X.size() / 3, ne = (long long)conn.size() / 4;
+    std::vector<double> u(3 * nn), v(3 * nn), a(3 * nn), cau(9 * ne), gl(9 * ne), vms(ne);
+    if (msx_get_state(h, u.data(), v.data(), a.data()) != MSX_OK ||
+        msx_element_fields(h, cau.data(), gl.data(), vms.data()) != MSX_OK)
+        return false;
+    std::string name = "MuPhiSimOutputs_0_." + std::to_string(index) + ".vtk";
+    FILE *f = fopen((dir + "/" + name).c_str(), "w");
+    if (!f) return false;
+    fprintf(f, "# vtk DataFile Version 1.0\n3D Unstructured Grid of C3D4 elements\nASCII\n\n");
+    fprintf(f, "DATASET UNSTRUCTURED_GRID\nPOINTS %lld float\n", nn);
+    for (long long i = 0; i < nn; i++) fprintf(f, "%.17g %.17g %.17g\n", X[i], X[nn + i], X[2 * nn + i]);
+    fprintf(f, "\nCELLS %lld %lld\n", ne, 5 * ne);
+    for (long long e = 0; e < ne; e++)
+        fprintf(f, "4 %d %d %d %d\n", conn[4 * e], conn[4 * e + 1], conn[4 * e + 2], conn[4 * e + 3]);
+    fprintf(f, "\nCELL_TYPES %lld\n", ne);
+    for (long long e = 0; e < ne; e++) fprintf(f, "10\n");
+    fprintf(f, "\nPOINT_DATA %lld\n", nn);
+    const char *names[3] = {"Displacement", "Velocity", "Acceleration"};
+    const std::vector<double> *fields[3] = {&u, &v, &a};
+    for (int k = 0; k < 3; k++) {
+        fprintf(f, "VECTORS %s float\n", names[k]);
+        const std::vector<double> &w = *fields[k];
+        for (long long i = 0; i < nn; i++) fprintf(f, "%.17g %.17g %.17g\n", w[i], w[nn + i], w[2 * nn + i]);
+        fprintf(f, "\n");
+    }
+    fprintf(f, "CELL_DATA %lld\n", ne);
+    const char *tnames[2] = {"Cauchy", "E"};
+    const std::vector<double> *tens[2] = {&cau, &gl};
+    for (int k = 0; k < 2; k++) {
+        fprintf(f, "TENSORS %s float\n", tnames[k]);
+        const std::vector<double> &w = *tens[k];
+        for (long long e = 0; e < ne; e++)
+            for (int r = 0; r < 3; r++)
+                fprintf(f, "%.17g %.17g %.17g\n", w[9 * e + 3 * r], w[9 * e + 3 * r + 1], w[9 * e + 3 * r + 2]);
+        fprintf(f, "\n");
+    }
+    fprintf(f, "SCALARS VMS float\nLOOKUP_TABLE default\n");
+    for (long long e = 0; e < ne; e++) fprintf(f, "%.17g\n", vms[e]);
+    fclose(f);
+    return true;
+}
+
+// allOutputs_0.vtk.series (ParaView file-series JSON), rewritten after each output
+void write_series(const std::string &dir, const std::vector<std::pair<std::string, double>> &files)
+{
+    FILE *f = fopen((dir + "/allOutputs_0.vtk.series").c_str(), "w");
+    if (!f) return;
+    fprintf(f, "{\n\"file-series-version\" : \"1.0\",\n\"files\" : [\n");
+    for (size_t k = 0; k < files.size(); k++)
+        fprintf(f, "{ \"name\" : \"%s\", \"time\" :%.17g}%s\n", files[k].first.c_str(), files[k].second,
+                k + 1 < files.size() ? "," : "");
+    fprintf(f, "]\n}\n");
+    fclose(f);
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
 {
-    std::string input, dir = ".", dump, csv;
+    std::string input, dir = ".", dump, csv, outdir;
     int precision = MSX_PREC_FP64;
     bool parse_only = false;
     for (int k = 1; k < argc; k++) {
@@ -214,6 +303,7 @@ int main(int argc, char **argv)
         if (a == "-input") input = next();
         else if (a == "-inputDir") dir = next();
         else if (a == "-dump") dump = next();
+        else if (a == "-outputDir") outdir = next();
         else if (a == "-csv") csv = next();
         else if (a == "-parse-only") parse_only = true;
         else if (a == "-precision") {
@@ -236,6 +326,8 @@ int main(int argc, char **argv)
         for (auto &s : d.solvers) nbc += s.bcs.size();
         printf("{\"nodes\": %lld, \"elements\": %lld, \"materials\": %zu, \"solvers\": %zu, \"bcs\": %zu",
                nn, ne, d.mats.size(), d.solvers.size(), nbc);
+        printf(", \"forces\": %zu, \"gravity\": %.17g, \"gravity_first\": %d", d.forces.size(), d.gravity,
+               d.gravity_first);
         printf(", \"blocks\": [");
         for (size_t k = 0; k < d.solvers.size(); k++)
             printf("%s{\"t0\": %.17g, \"tf\": %.17g, \"sf\": %.17g, \"bcs\": %zu, \"inst\": %d}", k ? ", " : "",
@@ -247,12 +339,18 @@ int main(int argc, char **argv)
     msx_mesh mesh{nn, ne, X.data(), d.conn.data(), d.elem_mat.empty() ? nullptr : d.elem_mat.data()};
     msx_handle *h = nullptr;
     long long total = 0;
+    std::vector<std::pair<std::string, double>> outputs;
     for (size_t k = 0; k < d.solvers.size(); k++) {
         const SolverBlock &s = d.solvers[k];
         msx_solver_opts o{s.t0, s.tf, s.sf, 0, precision, 0};
         msx_status st;
         if (k == 0) {
             st = msx_create(&mesh, d.mats.data(), (int32_t)d.mats.size(), s.bcs.data(), (int64_t)s.bcs.size(), &o, &h);
+            if (st == MSX_OK && (!d.forces.empty() || d.gravity != 0)) {
+                std::vector<msx_nodal_force> nf;
+                for (const auto &f : d.forces) nf.push_back({f.node + f.comp * nn, f.t0, f.tf, f.value});
+                st = msx_set_loads(h, nf.data(), (int64_t)nf.size(), d.gravity, d.gravity_first);
+            }
         } else {
             // src/main.cpp:171-179: time continuity between solvers
             if (s.t0 - d.solvers[k - 1].tf > 1E-12) {
@@ -266,10 +364,47 @@ int main(int argc, char **argv)
             return 1;
         }
         msx_run_report r{};
-        st = msx_run(h, 0, &r);
-        total += r.steps;
-        printf("solver %zu: %lld steps, t = %.9g, dt = %.6g, device %.3f ms\n", k, (long long)r.steps, r.t, r.dt,
-               r.device_ms);
+        if (outdir.empty()) {
+            st = msx_run(h, 0, &r);
+            total += r.steps;
+            printf("solver %zu: %lld steps, t = %.9g, dt = %.6g, device %.3f ms\n", k, (long long)r.steps, r.t, r.dt,
+                   r.device_ms);
+        } else {
+            // the reference's output cadence (solverExplicit.cpp:171-174, 176-187, 310-321)
+            double dt0 = 0;
+            if ((st = msx_initial_dt(h, &dt0)) != MSX_OK) {
+                fprintf(stderr, "msx_deck: %s\n", msx_last_error());
+                return 1;
+            }
+            long long numStepsT = (long long)((s.tf - s.t0) / dt0);
+            long long sampler = s.outputs > 0 ? numStepsT / s.outputs : numStepsT;
+            auto emit = [&](double t) {
+                if (!write_vtk(outdir, (int)outputs.size(), t, X, d.conn, h)) return false;
+                outputs.push_back({"MuPhiSimOutputs_0_." + std::to_string(outputs.size()) + ".vtk", t});
+                write_series(outdir, outputs);
+                return true;
+            };
+            if (s.t0 < 1E-12 && !emit(s.t0)) {
+                fprintf(stderr, "msx_deck: cannot write output\n");
+                return 1;
+            }
+            long long steps = 0;
+            for (;;) {
+                long long chunk = sampler > 0 ? sampler : 1;
+                st = msx_run(h, chunk, &r);
+                if (st != MSX_OK) break;
+                steps += r.steps;
+                if (r.steps == 0) break;
+                if ((r.steps == chunk || r.t == s.tf) && !emit(r.t)) {
+                    fprintf(stderr, "msx_deck: cannot write output\n");
+                    return 1;
+                }
+                if (r.steps < chunk || r.t >= s.tf - 1E-12) break;
+            }
+            total += steps;
+            printf("solver %zu: %lld steps, t = %.9g, dt = %.6g, %zu outputs so far\n", k, steps, r.t, r.dt,
+                   outputs.size());
+        }
         if (st != MSX_OK) {
             fprintf(stderr, "msx_deck: %s\n", msx_last_error());
             return 1;

@@ -259,88 +259,182 @@ __device__ __forceinline__ double bc_increment(const BCEntry &b, double dt, long
 // u += dt v + dt^2/2 a (nonlinearSystem.cpp:1186-1200) and Dirichlet values.
 // One thread per node, three components.
 // ---------------------------------------------------------------------------
-template <int MODE>
-__device__ __forceinline__ void node_body(const Problem &p, long long i, const Ctrl &cp, const StepDecision &d)
+// Dirichlet records of node i: per component (first entry, count); count 0 = active.
+__device__ __forceinline__ void node_bc_records(const Problem &p, long long i, int2 *br)
 {
-    const long long nn = p.nn;
+    br[0] = br[1] = br[2] = make_int2(0, 0);
     int rec = p.node_bc[i];
-    int2 br[3] = {make_int2(0, 0), make_int2(0, 0), make_int2(0, 0)};
     if (rec >= 0) {
         br[0] = p.bc_rec[rec * 3 + 0];
         br[1] = p.bc_rec[rec * 3 + 1];
         br[2] = p.bc_rec[rec * 3 + 2];
     }
-    bool act[3] = {br[0].y == 0, br[1].y == 0, br[2].y == 0};
-    double s[3] = {0.0, 0.0, 0.0};
-    if (cp.ran && (act[0] || act[1] || act[2])) {
-        int k0 = p.node_ptr[i], k1 = p.node_ptr[i + 1];
-        if (MODE == MODE_MIXED) {
-            // Neumaier-compensated FP32 sums of the FP32 corner forces
-            float sh[3] = {0.f, 0.f, 0.f}, sc[3] = {0.f, 0.f, 0.f};
-            for (int k = k0; k < k1; k++) {
-                const float *f = p.fe32 + (long long)p.node_inc[k] * 3;
+}
+
+// External force of node i for the step being completed, in the deck's order
+// of the Neumann blocks (boundaryConditions.cpp:75-138): gravity sums start
+// from zero, nodal forces add m t inside their window.
+__device__ __forceinline__ void external_force(const Problem &p, long long i, double t, double *fx)
+{
+    fx[0] = fx[1] = fx[2] = 0.0;
+    if (!p.grav_n && !p.node_nf) return;
+    const int rf = p.node_nf ? p.node_nf[i] : -1;
+    if (p.grav_n && (p.gravity_first || rf < 0)) fx[2] = p.grav_n[i];
+    if (rf >= 0) {
 #pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    float x = f[c], t = sh[c] + x;
-                    sc[c] += fabsf(sh[c]) >= fabsf(x) ? (sh[c] - t) + x : (x - t) + sh[c];
-                    sh[c] = t;
-                }
+        for (int c = 0; c < 3; c++) {
+            int2 r = p.nf_rec[rf * 3 + c];
+            for (int k = r.x; k < r.x + r.y; k++) {
+                const ForceEntry f = p.nfs[k];
+                double F = (t >= f.t0 && t <= f.tf) ? f.m * t : 0;
+                fx[c] += F;
             }
-#pragma unroll
-            for (int c = 0; c < 3; c++) s[c] = (double)sh[c] + (double)sc[c];
+        }
+        if (p.grav_n && !p.gravity_first)
+            for (int k = p.node_ptr[i]; k < p.node_ptr[i + 1]; k++) fx[2] += p.grav_e[p.node_inc[k] >> 2];
+    }
+}
+
+// One DOF: post-update of step n-1 with the gathered internal force s and
+// external force fx (a = (fx - s)/m, v += dt (a_prev + a)/2), then the
+// prediction (active) or the Dirichlet values (constrained) of step n.
+template <int MODE>
+__device__ __forceinline__ void dof_update(const Problem &p, long long i, int c, double s, double fx, int2 br,
+                                           const Ctrl &cp, const StepDecision &d)
+{
+    const bool act = br.y == 0;
+    const long long dof = i + c * p.nn;
+    double ui = p.u[dof], vi = p.v[dof], ai = p.a[dof];
+    bool changed = false;
+    if (cp.ran && act) {
+        double an;
+        if (MODE == MODE_EXACT) {
+            double val = -s + fx;
+            double rhs = 0;
+            rhs += val;
+            an = rhs / p.mass[i];
+            vi += cp.dt * ((1. - 0.5) * ai + 0.5 * an);
         } else {
-            for (int k = k0; k < k1; k++) {
-                const double *f = p.fe + (long long)p.node_inc[k] * 3;
-                s[0] += f[0];
-                s[1] += f[1];
-                s[2] += f[2];
+            an = (fx - s) * p.minv[i];
+            vi += cp.dt * (0.5 * ai + 0.5 * an);
+        }
+        ai = an;
+        changed = true;
+    }
+    if (d.run) {
+        const double dtn = d.next.dt;
+        if (act) {
+            ui += dtn * vi + 0.5 * dtn * dtn * ai;
+        } else {
+            for (int k = br.x; k < br.x + br.y; k++) {
+                double Ud = bc_increment(p.bcs[k], dtn, d.next.step);
+                ui += Ud;
+                vi = Ud;
+                ai = 0.;
             }
+        }
+        changed = true;
+    }
+    if (changed) {
+        p.u[dof] = ui;
+        p.v[dof] = vi;
+        p.a[dof] = ai;
+        if (MODE == MODE_MIXED) {
+            float hi = (float)ui;
+            p.uhl[dof] = make_float2(hi, (float)(ui - (double)hi));
         }
     }
-    const double dtp = cp.dt, dtn = d.next.dt;
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        long long dof = i + c * nn;
-        double ui = p.u[dof], vi = p.v[dof], ai = p.a[dof];
-        bool changed = false;
-        if (cp.ran && act[c]) {
-            double an;
-            if (MODE == MODE_EXACT) {
-                double val = -s[c] + 0.0;
-                double rhs = 0;
-                rhs += val;
-                an = rhs / p.mass[i];
-                vi += dtp * ((1. - 0.5) * ai + 0.5 * an);
-            } else {
-                an = -s[c] * p.minv[i];
-                vi += dtp * (0.5 * ai + 0.5 * an);
-            }
-            ai = an;
-            changed = true;
+}
+
+// Node kernel body, one thread per node (reference-order mode): corner forces
+// of the incident elements summed in element order, then the three DOFs.
+template <int MODE>
+__device__ __forceinline__ void node_body(const Problem &p, long long i, const Ctrl &cp, const StepDecision &d)
+{
+    int2 br[3];
+    node_bc_records(p, i, br);
+    double s[3] = {0.0, 0.0, 0.0};
+    if (cp.ran && (br[0].y == 0 || br[1].y == 0 || br[2].y == 0)) {
+        for (int k = p.node_ptr[i]; k < p.node_ptr[i + 1]; k++) {
+            const double *f = p.fe + (long long)p.node_inc[k] * 3;
+            s[0] += f[0];
+            s[1] += f[1];
+            s[2] += f[2];
         }
-        if (d.run) {
-            if (act[c]) {
-                ui += dtn * vi + 0.5 * dtn * dtn * ai;
-            } else {
-                for (int k = br[c].x; k < br[c].x + br[c].y; k++) {
-                    double Ud = bc_increment(p.bcs[k], dtn, d.next.step);
-                    ui += Ud;
-                    vi = Ud;
-                    ai = 0.;
+    }
+    double fx[3] = {0.0, 0.0, 0.0};
+    if (cp.ran) external_force(p, i, cp.t, fx);
+#pragma unroll
+    for (int c = 0; c < 3; c++) dof_update<MODE>(p, i, c, s[c], fx[c], br[c], cp, d);
+}
+
+// Neumaier merge of two compensated FP32 partial sums (lo first).
+__device__ __forceinline__ void neumaier_merge(float &sh, float &sc, float oh, float oc)
+{
+    float t = sh + oh;
+    float e = fabsf(sh) >= fabsf(oh) ? (sh - t) + oh : (oh - t) + sh;
+    sh = t;
+    sc = (sc + oc) + e;
+}
+
+// Node kernel body for the tiled FP64 and mixed kernels: four lanes per node.
+// Lane q sums incidences k0+q, k0+q+4, ... of node i; the four partial sums
+// are combined by shuffles in a fixed (lane-ordered) way; lane c < 3 then
+// updates DOF c.  All 32 lanes of a warp must call this together (valid =
+// false for lanes past the tile's end).
+template <int MODE>
+__device__ __forceinline__ void node_body_quad(const Problem &p, long long i, bool valid, const Ctrl &cp,
+                                               const StepDecision &d)
+{
+    const int q = threadIdx.x & 3;
+    int2 br[3] = {make_int2(0, 1), make_int2(0, 1), make_int2(0, 1)};
+    if (valid) node_bc_records(p, i, br);
+    const bool need = valid && cp.ran && (br[0].y == 0 || br[1].y == 0 || br[2].y == 0);
+    const int k0 = need ? p.node_ptr[i] : 0, k1 = need ? p.node_ptr[i + 1] : 0;
+    double s[3];
+    if (MODE == MODE_MIXED) {
+        float sh[3] = {0.f, 0.f, 0.f}, sc[3] = {0.f, 0.f, 0.f};
+        for (int k = k0 + q; k < k1; k += 4) {
+            const float *f = p.fe32 + (long long)p.node_inc[k] * 3;
+#pragma unroll
+            for (int c = 0; c < 3; c++) neumaier_merge(sh[c], sc[c], f[c], 0.0f);
+        }
+#pragma unroll
+        for (int m = 1; m <= 2; m <<= 1)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                float oh = __shfl_xor_sync(0xffffffffu, sh[c], m), oc = __shfl_xor_sync(0xffffffffu, sc[c], m);
+                if (q & m) {   // partner is the lower lane: it goes first
+                    float th = oh, tc = oc;
+                    neumaier_merge(th, tc, sh[c], sc[c]);
+                    sh[c] = th;
+                    sc[c] = tc;
+                } else {
+                    neumaier_merge(sh[c], sc[c], oh, oc);
                 }
             }
-            changed = true;
+#pragma unroll
+        for (int c = 0; c < 3; c++) s[c] = (double)sh[c] + (double)sc[c];
+    } else {
+        s[0] = s[1] = s[2] = 0.0;
+        for (int k = k0 + q; k < k1; k += 4) {
+            const double *f = p.fe + (long long)p.node_inc[k] * 3;
+            s[0] += f[0];
+            s[1] += f[1];
+            s[2] += f[2];
         }
-        if (changed) {
-            p.u[dof] = ui;
-            p.v[dof] = vi;
-            p.a[dof] = ai;
-            if (MODE == MODE_MIXED) {
-                float hi = (float)ui;
-                p.uhl[dof] = make_float2(hi, (float)(ui - (double)hi));
+#pragma unroll
+        for (int m = 1; m <= 2; m <<= 1)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                double o = __shfl_xor_sync(0xffffffffu, s[c], m);
+                s[c] = (q & m) ? o + s[c] : s[c] + o;
             }
-        }
     }
+    if (!valid || q == 3) return;
+    double fx[3] = {0.0, 0.0, 0.0};
+    if (cp.ran) external_force(p, i, cp.t, fx);
+    dof_update<MODE>(p, i, q, s[q], fx[q], br[q], cp, d);
 }
 
 // Writes the new control slot and clears the slots the element kernel fills.
@@ -628,6 +722,24 @@ static __global__ void __launch_bounds__(kElemBlock) elem_force_kernel_fp64(Prob
 // ln J in FP64; FP32 corner forces; FP32 CFL length with the dt min in FP64.
 // cof(I + H) = I + D with D = (tr H + I2) I - (1 + tr H) H^T + (H^2)^T.
 // ---------------------------------------------------------------------------
+// ln(1 + x) in FP64.  For |x| < 2^-7, the usual size of J - 1, the Taylor
+// series to x^9 by Horner's rule (truncation below |x|^10/10 < 1e-21 |x|);
+// otherwise the library log1p.
+__device__ __forceinline__ double log1p_fp64(double x)
+{
+    if (fabs(x) >= 0.0078125) return log1p(x);
+    double p = 1.0 / 9.0;
+    p = fma(p, -x, 1.0 / 8.0);
+    p = fma(p, -x, 1.0 / 7.0);
+    p = fma(p, -x, 1.0 / 6.0);
+    p = fma(p, -x, 1.0 / 5.0);
+    p = fma(p, -x, 1.0 / 4.0);
+    p = fma(p, -x, 1.0 / 3.0);
+    p = fma(p, -x, 1.0 / 2.0);
+    p = fma(p, -x, 1.0);
+    return p * x;
+}
+
 __device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H, double Jm1d, double lnJd,
                                              float t, float I2, float *P)
 {
@@ -719,19 +831,20 @@ __device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, 
         for (int i = 0; i < 3; i++)
 #pragma unroll
             for (int j = 0; j < 3; j++) H[i * 3 + j] = du[i] * G[j] + du[3 + i] * G[3 + j] + du[6 + i] * G[6 + j];
-        // J - 1 = tr H + I2(H) + det H and ln J = log1p(J - 1) in FP64
-        double Hd[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) Hd[k] = (double)H[k];
-        double td = Hd[0] + Hd[4] + Hd[8];
-        double I2d = Hd[0] * Hd[4] + Hd[4] * Hd[8] + Hd[0] * Hd[8] - Hd[1] * Hd[3] - Hd[5] * Hd[7] - Hd[2] * Hd[6];
-        double I3d = Hd[0] * (Hd[4] * Hd[8] - Hd[5] * Hd[7]) - Hd[1] * (Hd[3] * Hd[8] - Hd[5] * Hd[6]) +
-                     Hd[2] * (Hd[3] * Hd[7] - Hd[4] * Hd[6]);
-        double Jm1 = td + I2d + I3d;
-        double lnJ = log1p(Jm1);
+        // J - 1 = tr H + (I2(H) + det H) in FP64 and ln J = log1p(J - 1) in
+        // FP64: the trace, the term that carries J - 1, is summed exactly in
+        // FP64; I2 and det H are O(|H|^2) and their FP32 rounding lies far
+        // below the FP32 precision of J - 1, so forming them in FP32 loses
+        // nothing while F = I + H never has to be formed or reduced.
+        float tf = H[0] + H[4] + H[8];
+        float I2f = (H[0] * H[4] - H[1] * H[3]) + (H[4] * H[8] - H[5] * H[7]) + (H[0] * H[8] - H[2] * H[6]);
+        float I3f = H[0] * (H[4] * H[8] - H[5] * H[7]) - H[1] * (H[3] * H[8] - H[5] * H[6]) +
+                    H[2] * (H[3] * H[7] - H[4] * H[6]);
+        double Jm1 = (((double)H[0] + (double)H[4]) + (double)H[8]) + (double)(I2f + I3f);
+        double lnJ = log1p_fp64(Jm1);
         const MatParams &m = mat_of(p, e);
         float P[9];
-        stress_mixed(m, H, Jm1, lnJ, (float)td, (float)I2d, P);
+        stress_mixed(m, H, Jm1, lnJ, tf, I2f, P);
         float wJ = __ldg(p.wJ32 + e);
 #pragma unroll
         for (int k = 0; k < 9; k++) P[k] *= wJ;
@@ -808,7 +921,12 @@ __global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *
         StepDecision d = decide_step(p, cp, parity);
         if (tl.begin == 0 && threadIdx.x == 0) publish_step(p, d, parity);
         if (!cp.ran && !d.run) continue;
-        for (long long i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x) node_body<MODE>(p, i, cp, d);
+        // four lanes per node; every lane runs the same number of iterations
+        const int per = blockDim.x >> 2;
+        for (long long b = tl.begin; b < tl.end; b += per) {
+            long long i = b + (threadIdx.x >> 2);
+            node_body_quad<MODE>(p, i, i < tl.end, cp, d);
+        }
     }
 }
 
@@ -922,6 +1040,33 @@ __global__ void setup_mass_kernel(Problem p, double *mass, double *minv)
     minv[i] = 1.0 / m;
 }
 
+// boundaryConditions.cpp:1146-1171 BCsGravity: -w rho |J| g phi_a on the z DOF
+// of each corner (|J| as classGPs::getJ keeps it), summed per node in element order.
+__global__ void setup_gravity_elem_kernel(Problem p, double g, double *grav_e)
+{
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.ne) return;
+    const long long nn = p.nn;
+    int4 cn = p.conn[e];
+    int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    double M[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) M[i * 3 + j] = p.X[i * nn + nd[j + 1]] - p.X[i * nn + nd[0]];
+    const double w = 0.166666666667, phi = -1.0 * 0.25 - 1.0 * 0.25 - 1.0 * 0.25 + 1.0;
+    grav_e[e] = -w * mat_of(p, e).rho * fabs(det3_ref(M)) * g * phi;
+}
+
+__global__ void setup_gravity_node_kernel(Problem p, const double *grav_e, double *grav_n)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.nn) return;
+    double s = 0;
+    for (int k = p.node_ptr[i]; k < p.node_ptr[i + 1]; k++) s += grav_e[p.node_inc[k] >> 2];
+    grav_n[i] = s;
+}
+
 // solvers.cpp:276-287 (uK == nullptr) and :296-320: element min into dtmin[slot]
 __global__ void __launch_bounds__(kElemBlock) initial_cfl_kernel(Problem p, const double *uK, int slot)
 {
@@ -948,6 +1093,95 @@ __global__ void __launch_bounds__(kElemBlock) initial_cfl_kernel(Problem p, cons
         }
     }
     block_min_to(v, p.dtmin + slot);
+}
+
+// Output fields of one element from the current u, in the reference's order:
+// Cauchy (NH: the law's sigma, hyperElasticNeoHookean.cpp:113-124; other laws
+// P F^T / J, maths.cpp:1250-1254), Green-Lagrange E (maths.cpp:1227-1243) and
+// von Mises (maths.cpp:1261-1271).
+__global__ void element_fields_kernel(Problem p, double *cauchy, double *gl, double *vms)
+{
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.ne) return;
+    const long long ne = p.ne, nn = p.nn;
+    int4 cn = p.conn[e];
+    int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    double dphi[12];
+#pragma unroll
+    for (int k = 0; k < 9; k++) dphi[3 + k] = p.G[k * ne + e];
+#pragma unroll
+    for (int j = 0; j < 3; j++) dphi[j] = (-dphi[3 + j] - dphi[6 + j]) - dphi[9 + j];
+    double F[9], P[9], S[9], E[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) F[i] = 0.;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        F[i * 3 + i] += 1.;
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) F[i * 3 + j] += dphi[a * 3 + j] * p.u[nd[a] + i * nn];
+    }
+    const MatParams &m = mat_of(p, e);
+    if (m.law == 0) {
+        double B[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) c += F[i * 3 + k] * F[j * 3 + k];
+                B[i * 3 + j] = c;
+            }
+        double J = det3_ref(F);
+        double trB = 0;
+#pragma unroll
+        for (int i = 0; i < 3; i++) trB += B[i * 3 + i];
+        double fact1 = pow(J, 5.0 / 3.0);
+        double fact2 = m.mu / fact1;
+#pragma unroll
+        for (int i = 0; i < 9; i++) S[i] = 0 + fact2 * B[i];
+        double fact3 = -(m.mu / 3.0) * trB / fact1 + m.K1 * (J - 1.0);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) S[i * 3 + j] += fact3 * (i == j ? 1.0 : 0.0);
+    } else {
+        stress_ref(m, F, P);
+        double detJinv = 1. / det3_ref(F);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) c += P[i * 3 + k] * F[j * 3 + k];
+                S[i * 3 + j] = c;
+            }
+#pragma unroll
+        for (int i = 0; i < 9; i++) S[i] = S[i] * detJinv;
+    }
+    // the compressible neo-Hookean law never updates its Green-Lagrange strain
+    // (hyperElasticNeoHookean.cpp:221-289), so the reference reports zero
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            double c = 0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) c += F[k * 3 + i] * F[k * 3 + j];
+            E[i * 3 + j] = m.law == 1 ? 0.0 : 0.5 * (c - (i == j ? 1.0 : 0.0));
+        }
+    if (cauchy)
+#pragma unroll
+        for (int k = 0; k < 9; k++) cauchy[e * 9 + k] = S[k];
+    if (gl)
+#pragma unroll
+        for (int k = 0; k < 9; k++) gl[e * 9 + k] = E[k];
+    if (vms)
+        vms[e] = sqrt(0.5 * ((S[0] - S[4]) * (S[0] - S[4]) + (S[4] - S[8]) * (S[4] - S[8]) +
+                             (S[8] - S[0]) * (S[8] - S[0]) + 6 * (S[1] * S[1] + S[2] * S[2] + S[5] * S[5])));
 }
 
 #endif  // MSX_SETUP_KERNELS

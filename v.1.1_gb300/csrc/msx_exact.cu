@@ -42,4 +42,15 @@ void launch_internal_force_exact(const Problem &p, double *fint, cudaStream_t s)
     gather_kernel<MODE_EXACT><<<grid_for(p.nn, 256), 256, 0, s>>>(p, fint);
 }
 
+void launch_setup_gravity(const Problem &p, double g, double *grav_e, double *grav_n, cudaStream_t s)
+{
+    setup_gravity_elem_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, g, grav_e);
+    setup_gravity_node_kernel<<<grid_for(p.nn, 256), 256, 0, s>>>(p, grav_e, grav_n);
+}
+
+void launch_element_fields(const Problem &p, double *cauchy, double *gl, double *vms, cudaStream_t s)
+{
+    element_fields_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, cauchy, gl, vms);
+}
+
 }  // namespace msx

@@ -35,18 +35,16 @@ void launch_tiled_elem(const Problem *descs, const Tile *etiles, const int *coun
         pool_elem_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
 }
 
-int tiled_ctas_per_sm(int mode, int threads)
+int tiled_ctas_per_sm(int mode, int threads, bool node)
 {
-    int a = 0, b = 0;
-    if (mode == MODE_MIXED) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, pool_node_kernel<MODE_MIXED>, threads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pool_elem_kernel<MODE_MIXED>, threads, 0);
-    } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, pool_node_kernel<MODE_FP64>, threads, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pool_elem_kernel<MODE_FP64>, threads, 0);
-    }
-    int c = a < b ? a : b;
-    return c > 0 ? c : 1;
+    int a = 0;
+    if (mode == MODE_MIXED)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, node ? (const void *)pool_node_kernel<MODE_MIXED>
+                                                               : (const void *)pool_elem_kernel<MODE_MIXED>, threads, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, node ? (const void *)pool_node_kernel<MODE_FP64>
+                                                               : (const void *)pool_elem_kernel<MODE_FP64>, threads, 0);
+    return a > 0 ? a : 1;
 }
 
 }  // namespace msx

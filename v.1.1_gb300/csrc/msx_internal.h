@@ -32,6 +32,12 @@ struct BCEntry {
     double val;
 };
 
+// One nodal-force DOF of *BOUNDARY, TYPE=FORCE: f(t) = m t for t0 <= t <= tf
+// (classNeumann::getTracAmount, classNodes.h:101-109), m = value / (tf - t0).
+struct ForceEntry {
+    double m, t0, tf;
+};
+
 // Step control, double-buffered by step parity.  The node kernel of step n
 // reads slot (n-1)&1 and writes slot n&1; every thread derives the same
 // values, so no thread waits for another.
@@ -75,6 +81,13 @@ struct Problem {
     const int *node_bc;       // per node: -1 or record index
     const int2 *bc_rec;       // per record, per comp: (first entry, count)
     const BCEntry *bcs;
+    // Neumann loads (all nullptr without loads)
+    const double *grav_e;     // per element gravity term -w rho |J| g phi (z DOFs)
+    const double *grav_n;     // per node sum of grav_e over its elements, element order
+    const int *node_nf;       // per node: -1 or nodal-force record index
+    const int2 *nf_rec;       // per record, per comp: (first entry, count)
+    const ForceEntry *nfs;
+    int gravity_first;        // 1: *GRAVITY precedes the *BOUNDARY, TYPE=FORCE blocks
     // control
     Ctrl *ctrl;                       // [2]
     unsigned long long *dtmin;        // [2] bit patterns of positive doubles
@@ -100,8 +113,8 @@ void launch_tiled_node(const Problem *descs, const Tile *ntiles, const int *coun
                        int threads, cudaStream_t s);
 void launch_tiled_elem(const Problem *descs, const Tile *etiles, const int *counts, int mode, int parity, int grid,
                        int threads, cudaStream_t s);
-// CTAs of the tiled kernels that fit on one SM at this CTA size (min of node and element kernel)
-int tiled_ctas_per_sm(int mode, int threads);
+// CTAs of the tiled element kernel (node kernel when `node` is true) that fit on one SM
+int tiled_ctas_per_sm(int mode, int threads, bool node = false);
 
 // records the message returned by msx_last_error() on this host thread
 void msx_set_error(const char *msg);
@@ -115,6 +128,10 @@ void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s);
 void launch_setup_mass(const Problem &p, double *mass, double *minv, cudaStream_t s);
 // min over elements of Lref/c (undeformed) or min(Lref, L(X+u))/c, into dtmin[slot]
 void launch_initial_cfl(const Problem &p, const double *uK, int slot, cudaStream_t s);
+// gravity terms per element and their per-node sums (reference order)
+void launch_setup_gravity(const Problem &p, double g, double *grav_e, double *grav_n, cudaStream_t s);
+// Cauchy, Green-Lagrange (9 per element, row-major) and von Mises of the current u
+void launch_element_fields(const Problem &p, double *cauchy, double *gl, double *vms, cudaStream_t s);
 // one element pass + gather for f_int(u) (test hook); writes fint[3*nn]
 void launch_internal_force_exact(const Problem &p, double *fint, cudaStream_t s);
 void launch_internal_force_fp64(const Problem &p, double *fint, cudaStream_t s);

@@ -204,13 +204,14 @@ static msx_status build_pool_graph(msx_pool *p, int steps)
         cudaGraphExecDestroy(p->graph);
         p->graph = nullptr;
     }
-    const int threads = p->sched.threads, grid = p->sms * p->sched.ctas_per_sm;
     const int mode = p->opts.precision == MSX_PREC_MIXED ? MODE_MIXED : MODE_FP64;
+    const int threads = p->sched.threads, grid = p->sms * p->sched.ctas_per_sm;
+    const int node_grid = p->sms * tiled_ctas_per_sm(mode, threads, true);
     cudaGraph_t g;
     PCUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
     for (int i = 0; i < steps; i++) {
         int parity = (i & 1) ? 0 : 1;
-        launch_tiled_node(p->d_descs, p->d_ntiles, p->d_counts, mode, parity, grid, threads, p->stream);
+        launch_tiled_node(p->d_descs, p->d_ntiles, p->d_counts, mode, parity, node_grid, threads, p->stream);
         launch_tiled_elem(p->d_descs, p->d_etiles, p->d_counts, mode, parity, grid, threads, p->stream);
     }
     cudaError_t err = cudaStreamEndCapture(p->stream, &g);

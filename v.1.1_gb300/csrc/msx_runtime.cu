@@ -104,6 +104,12 @@ struct msx_handle {
     DBuf<int> node_ptr, node_inc, node_bc;
     DBuf<int2> bc_rec;
     DBuf<BCEntry> bcs;
+    DBuf<double> grav_e, grav_n;
+    DBuf<int> node_nf;
+    DBuf<int2> nf_rec;
+    DBuf<ForceEntry> nfs;
+    double gravity = 0;
+    int gravity_first = 0;
     DBuf<Ctrl> ctrl;
     DBuf<unsigned long long> dtmin;
     DBuf<int> flags;
@@ -121,7 +127,7 @@ struct msx_handle {
     DBuf<Problem> d_desc;
     DBuf<Tile> d_etiles, d_ntiles;
     DBuf<int> d_counts;
-    int tgrid = 0, tthreads = kStepThreads;
+    int tgrid = 0, tgrid_node = 0, tthreads = kStepThreads;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc[2] = {nullptr, nullptr};
     std::vector<int> h_node_bc;   // host copies for next_solver rebuilds
@@ -221,6 +227,12 @@ static void bind_problem(msx_handle *h)
     P.node_bc = h->node_bc.p;
     P.bc_rec = h->bc_rec.p;
     P.bcs = h->bcs.p;
+    P.grav_e = h->gravity != 0 ? h->grav_e.p : nullptr;
+    P.grav_n = h->gravity != 0 ? h->grav_n.p : nullptr;
+    P.node_nf = h->nfs.p ? h->node_nf.p : nullptr;
+    P.nf_rec = h->nf_rec.p;
+    P.nfs = h->nfs.p;
+    P.gravity_first = h->gravity_first;
     P.ctrl = h->ctrl.p;
     P.dtmin = h->dtmin.p;
     P.flags = h->flags.p;
@@ -247,8 +259,8 @@ static int tiled_mode(const msx_handle *h) { return h->precision == MSX_PREC_MIX
 static void launch_step(msx_handle *h, int parity)
 {
     if (h->tiled) {
-        launch_tiled_node(h->d_desc.p, h->d_ntiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
-                          h->stream);
+        launch_tiled_node(h->d_desc.p, h->d_ntiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid_node,
+                          h->tthreads, h->stream);
         launch_tiled_elem(h->d_desc.p, h->d_etiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
                           h->stream);
     } else {
@@ -278,6 +290,7 @@ static msx_status upload_tiled(msx_handle *h)
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
     h->tgrid = sms * tiled_ctas_per_sm(tiled_mode(h), h->tthreads);
+    h->tgrid_node = sms * tiled_ctas_per_sm(tiled_mode(h), h->tthreads, true);
     MSX_CUDA(cudaMemcpyAsync(h->d_desc.p, &h->P, sizeof(Problem), cudaMemcpyHostToDevice, h->stream));
     MSX_CUDA(cudaStreamSynchronize(h->stream));
     return MSX_OK;
@@ -532,6 +545,11 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     for (auto *b : {&h->node_ptr, &h->node_inc, &h->node_bc, &h->flags}) b->release();
     h->bc_rec.release();
     h->bcs.release();
+    h->grav_e.release();
+    h->grav_n.release();
+    h->node_nf.release();
+    h->nf_rec.release();
+    h->nfs.release();
     h->d_desc.release();
     h->d_etiles.release();
     h->d_ntiles.release();
@@ -543,6 +561,69 @@ extern "C" msx_status msx_destroy(msx_handle *h)
         if (e) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_set_loads(msx_handle *h, const msx_nodal_force *forces, int64_t num_forces, double gravity,
+                                    int32_t gravity_first)
+{
+    if (!h) return fail(MSX_ERR_ARG, "NULL handle");
+    if (num_forces < 0 || (num_forces > 0 && !forces)) return fail(MSX_ERR_ARG, "bad nodal force array");
+    const long long nn = h->P.nn;
+    for (long long k = 0; k < num_forces; k++) {
+        if (forces[k].dof < 0 || forces[k].dof >= 3 * nn) return fail(MSX_ERR_ARG, "nodal force dof out of range");
+        if (!(forces[k].tf - forces[k].t0 != 0)) return fail(MSX_ERR_ARG, "nodal force needs tf != t0");
+    }
+    if (!std::isfinite(gravity)) return fail(MSX_ERR_ARG, "gravity must be finite");
+    // records per node and component, entries kept in input order
+    std::vector<long long> order(num_forces);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](long long x, long long y) { return forces[x].dof < forces[y].dof; });
+    std::vector<int> node_nf(nn, -1);
+    std::vector<int2> rec;
+    std::vector<ForceEntry> ent;
+    for (long long k = 0; k < num_forces; k++) {
+        const msx_nodal_force &f = forces[order[k]];
+        long long node = f.dof % nn;
+        int comp = (int)(f.dof / nn);
+        if (node_nf[node] < 0) {
+            node_nf[node] = (int)(rec.size() / 3);
+            rec.resize(rec.size() + 3, make_int2(0, 0));
+        }
+        int2 &r = rec[node_nf[node] * 3 + comp];
+        if (r.y == 0) r.x = (int)ent.size();
+        r.y++;
+        ent.push_back({f.value / (f.tf - f.t0), f.t0, f.tf});
+    }
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    h->node_nf.release();
+    h->nf_rec.release();
+    h->nfs.release();
+    if (num_forces > 0) {
+        MSX_CUDA(h->node_nf.alloc(nn));
+        MSX_CUDA(h->nf_rec.alloc(rec.size()));
+        MSX_CUDA(h->nfs.alloc(ent.size()));
+        MSX_CUDA(cudaMemcpyAsync(h->node_nf.p, node_nf.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, h->stream));
+        MSX_CUDA(cudaMemcpyAsync(h->nf_rec.p, rec.data(), sizeof(int2) * rec.size(), cudaMemcpyHostToDevice, h->stream));
+        MSX_CUDA(cudaMemcpyAsync(h->nfs.p, ent.data(), sizeof(ForceEntry) * ent.size(), cudaMemcpyHostToDevice, h->stream));
+    }
+    h->gravity = gravity;
+    h->gravity_first = gravity_first ? 1 : 0;
+    if (gravity != 0) {
+        if (!h->grav_e.p) MSX_CUDA(h->grav_e.alloc(h->P.ne));
+        if (!h->grav_n.p) MSX_CUDA(h->grav_n.alloc(nn));
+        bind_problem(h);
+        launch_setup_gravity(h->P, gravity, h->grav_e.p, h->grav_n.p, h->stream);
+    }
+    bind_problem(h);
+    msx_status st = upload_tiled(h);
+    if (st != MSX_OK) return st;
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->graph) {   // exact-mode graphs hold the Problem by value
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
     return MSX_OK;
 }
 
@@ -689,8 +770,8 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
         int parity = (i & 1) ? 0 : 1;
         cudaEventRecord(ev[3 * i], h->stream);
         if (h->tiled)
-            launch_tiled_node(h->d_desc.p, h->d_ntiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
-                              h->stream);
+            launch_tiled_node(h->d_desc.p, h->d_ntiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid_node,
+                              h->tthreads, h->stream);
         else
             h->node(h->P, parity, h->stream);
         cudaEventRecord(ev[3 * i + 1], h->stream);
@@ -725,6 +806,40 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
     // (read X, u, v, a 96 + m 8, write u, v, a 72)
     rep->element_alg_bytes = ne * (mixed ? 72.0 : 128.0);
     rep->node_alg_bytes = nn * 176.0;
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_initial_dt(msx_handle *h, double *dt_init)
+{
+    if (!h || !dt_init) return fail(MSX_ERR_ARG, "NULL argument");
+    msx_status st;
+    if (!h->block_ready && (st = init_block(h)) != MSX_OK) return st;
+    *dt_init = h->dt_init;
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_element_fields(msx_handle *h, double *cauchy, double *green_lagrange, double *von_mises)
+{
+    if (!h) return fail(MSX_ERR_ARG, "NULL handle");
+    const long long ne = h->P.ne;
+    DBuf<double> dc, dg, dv;
+    if ((cauchy && dc.alloc(9 * ne) != cudaSuccess) || (green_lagrange && dg.alloc(9 * ne) != cudaSuccess) ||
+        (von_mises && dv.alloc(ne) != cudaSuccess)) {
+        dc.release();
+        dg.release();
+        dv.release();
+        return fail(MSX_ERR_OOM, "element field buffers");
+    }
+    bind_problem(h);
+    launch_element_fields(h->P, dc.p, dg.p, dv.p, h->stream);
+    if (cauchy) cudaMemcpyAsync(cauchy, dc.p, sizeof(double) * 9 * ne, cudaMemcpyDeviceToHost, h->stream);
+    if (green_lagrange) cudaMemcpyAsync(green_lagrange, dg.p, sizeof(double) * 9 * ne, cudaMemcpyDeviceToHost, h->stream);
+    if (von_mises) cudaMemcpyAsync(von_mises, dv.p, sizeof(double) * ne, cudaMemcpyDeviceToHost, h->stream);
+    cudaError_t err = cudaStreamSynchronize(h->stream);
+    dc.release();
+    dg.release();
+    dv.release();
+    if (err != cudaSuccess) return fail(MSX_ERR_CUDA, cudaGetErrorString(err));
     return MSX_OK;
 }
 

@@ -43,6 +43,10 @@ class BC_(C.Structure):
     _fields_ = [("dof", C.c_int64), ("mode", C.c_int32), ("ramp_steps", C.c_int32), ("value", C.c_double)]
 
 
+class Force_(C.Structure):
+    _fields_ = [("dof", C.c_int64), ("t0", C.c_double), ("tf", C.c_double), ("value", C.c_double)]
+
+
 class Opts_(C.Structure):
     _fields_ = [("t0", C.c_double), ("tf", C.c_double), ("scale_factor", C.c_double),
                 ("max_steps", C.c_int64), ("precision", C.c_int32), ("steps_per_graph", C.c_int32)]
@@ -80,7 +84,7 @@ SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_
            "msx_last_error", "msx_internal_force", "msx_get_element_data", "msx_profile", "msx_mesh_cube",
            "msx_stream", "msx_set_device", "msx_pool_create", "msx_pool_submit", "msx_pool_step",
            "msx_pool_poll", "msx_pool_fetch", "msx_pool_destroy", "msx_pool_stats_get",
-           "msx_internal_force_noalloc"]
+           "msx_internal_force_noalloc", "msx_initial_dt", "msx_element_fields", "msx_set_loads"]
 
 _lib = None
 
@@ -107,6 +111,9 @@ def load(path: str = LIB_PATH):
         "msx_mesh_cube": [i32, C.c_uint64, C.c_double, vp, vp],
         "msx_stream": [vp],
         "msx_set_device": [i32],
+        "msx_initial_dt": [vp, C.POINTER(C.c_double)],
+        "msx_element_fields": [vp, vp, vp, vp],
+        "msx_set_loads": [vp, vp, i64, C.c_double, i32],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -224,6 +231,25 @@ class Solver:
         f = np.zeros(3 * self.nn)
         _check(load().msx_internal_force(self.h, _p(u), _p(f)))
         return f
+
+    def set_loads(self, forces=(), gravity=0.0, gravity_first=False):
+        """forces: (dof, t0, tf, value) per nodal-force DOF in deck order."""
+        arr = (Force_ * max(1, len(forces)))()
+        for i, f in enumerate(forces):
+            arr[i] = Force_(*f)
+        _check(load().msx_set_loads(self.h, C.cast(arr, C.c_void_p), len(forces), float(gravity),
+                                    1 if gravity_first else 0))
+
+    def initial_dt(self):
+        d = C.c_double()
+        _check(load().msx_initial_dt(self.h, C.byref(d)))
+        return d.value
+
+    def element_fields(self):
+        """Cauchy (ne, 3, 3), Green-Lagrange (ne, 3, 3), von Mises (ne,) of the current state."""
+        c, g, v = np.zeros(9 * self.ne), np.zeros(9 * self.ne), np.zeros(self.ne)
+        _check(load().msx_element_fields(self.h, _p(c), _p(g), _p(v)))
+        return c.reshape(-1, 3, 3), g.reshape(-1, 3, 3), v
 
     def element_data(self):
         G, wJ, L, m = np.zeros(9 * self.ne), np.zeros(self.ne), np.zeros(self.ne), np.zeros(self.nn)
