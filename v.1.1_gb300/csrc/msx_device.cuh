@@ -297,14 +297,15 @@ __device__ __forceinline__ void external_force(const Problem &p, long long i, do
 
 // One DOF: post-update of step n-1 with the gathered internal force s and
 // external force fx (a = (fx - s)/m, v += dt (a_prev + a)/2), then the
-// prediction (active) or the Dirichlet values (constrained) of step n.
+// prediction (active) or the Dirichlet values (constrained) of step n.  The
+// reference-order mode keeps the reference's operations; the others use
+// v += (dt/2)(a_prev + a) and u += dt (v + (dt/2) a) with 1/m.
 template <int MODE>
-__device__ __forceinline__ void dof_update(const Problem &p, long long i, int c, double s, double fx, int2 br,
-                                           const Ctrl &cp, const StepDecision &d)
+__device__ __forceinline__ void dof_update(const Problem &p, long long dof, double ui, double vi, double ai, double s,
+                                           double fx, bool loads, int2 br, const Ctrl &cp, const StepDecision &d,
+                                           double mass, double minv)
 {
     const bool act = br.y == 0;
-    const long long dof = i + c * p.nn;
-    double ui = p.u[dof], vi = p.v[dof], ai = p.a[dof];
     bool changed = false;
     if (cp.ran && act) {
         double an;
@@ -312,11 +313,11 @@ __device__ __forceinline__ void dof_update(const Problem &p, long long i, int c,
             double val = -s + fx;
             double rhs = 0;
             rhs += val;
-            an = rhs / p.mass[i];
+            an = rhs / mass;
             vi += cp.dt * ((1. - 0.5) * ai + 0.5 * an);
         } else {
-            an = (fx - s) * p.minv[i];
-            vi += cp.dt * (0.5 * ai + 0.5 * an);
+            an = (loads ? fx - s : -s) * minv;
+            vi = fma(0.5 * cp.dt, ai + an, vi);
         }
         ai = an;
         changed = true;
@@ -324,7 +325,8 @@ __device__ __forceinline__ void dof_update(const Problem &p, long long i, int c,
     if (d.run) {
         const double dtn = d.next.dt;
         if (act) {
-            ui += dtn * vi + 0.5 * dtn * dtn * ai;
+            if (MODE == MODE_EXACT) ui += dtn * vi + 0.5 * dtn * dtn * ai;
+            else ui = fma(dtn, fma(0.5 * dtn, ai, vi), ui);
         } else {
             for (int k = br.x; k < br.x + br.y; k++) {
                 double Ud = bc_increment(p.bcs[k], dtn, d.next.step);
@@ -364,8 +366,19 @@ __device__ __forceinline__ void node_body(const Problem &p, long long i, const C
     }
     double fx[3] = {0.0, 0.0, 0.0};
     if (cp.ran) external_force(p, i, cp.t, fx);
+    const double mass = MODE == MODE_EXACT ? p.mass[i] : 0.0, minv = MODE == MODE_EXACT ? 0.0 : p.minv[i];
 #pragma unroll
-    for (int c = 0; c < 3; c++) dof_update<MODE>(p, i, c, s[c], fx[c], br[c], cp, d);
+    for (int c = 0; c < 3; c++) {
+        const long long dof = i + c * p.nn;
+        dof_update<MODE>(p, dof, p.u[dof], p.v[dof], p.a[dof], s[c], fx[c], true, br[c], cp, d, mass, minv);
+    }
+}
+
+// Rounding error of s = fl(a + b): a + b = s + err exactly (Knuth's TwoSum).
+__device__ __forceinline__ float two_sum_err(float a, float b, float s)
+{
+    float bp = s - a;
+    return (a - (s - bp)) + (b - bp);
 }
 
 // Neumaier merge of two compensated FP32 partial sums (lo first).
@@ -377,64 +390,259 @@ __device__ __forceinline__ void neumaier_merge(float &sh, float &sc, float oh, f
     sc = (sc + oc) + e;
 }
 
-// Node kernel body for the tiled FP64 and mixed kernels: four lanes per node.
-// Lane q sums incidences k0+q, k0+q+4, ... of node i; the four partial sums
-// are combined by shuffles in a fixed (lane-ordered) way; lane c < 3 then
-// updates DOF c.  All 32 lanes of a warp must call this together (valid =
-// false for lanes past the tile's end).
+// ---------------------------------------------------------------------------
+// Double-word ("double-float") arithmetic: a value is a pair (hi, lo) of FP32
+// numbers with value hi + lo and |lo| <= ulp(hi)/2, about 48 significant
+// bits.  The mixed mode keeps the nodal state u, v, a in this form while a
+// block runs, so its node update runs on the FP32 pipe (on this GPU the FP64
+// pipe issues about 1/64 of the FP32 rate).  Algorithms: TwoSum (Knuth),
+// Fast2Sum (Dekker), and the accurate double-word sum and double-word product
+// of Joldes, Muller and Popescu, "Tight and rigorous error bounds for basic
+// building blocks of double-word arithmetic", ACM TOMS 44 (2017), Algs. 6, 12.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 df_fast2sum(float a, float b)   // needs |a| >= |b| (or a = 0)
+{
+    float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+
+__device__ __forceinline__ float2 df_two_sum(float a, float b)
+{
+    float s = a + b;
+    return make_float2(s, two_sum_err(a, b, s));
+}
+
+__device__ __forceinline__ float2 df_add(float2 x, float2 y)
+{
+    float2 s = df_two_sum(x.x, y.x), t = df_two_sum(x.y, y.y);
+    float2 v = df_fast2sum(s.x, s.y + t.x);
+    return df_fast2sum(v.x, t.y + v.y);
+}
+
+__device__ __forceinline__ float2 df_mul(float2 x, float2 y)
+{
+    float ch = x.x * y.x;
+    float cl1 = fmaf(x.x, y.x, -ch);
+    float cl2 = fmaf(x.y, y.x, fmaf(x.x, y.y, x.y * y.y));
+    return df_fast2sum(ch, cl1 + cl2);
+}
+
+__device__ __forceinline__ float2 df_neg(float2 x) { return make_float2(-x.x, -x.y); }
+
+// nearest double-word to an FP64 value (FP64 pipe: control values and loads only)
+__device__ __forceinline__ float2 df_from(double x)
+{
+    float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+
+// Per-solve quantities of the node kernel, derived once per block and solve
+// from the solve's control slot (not once per tile).
+struct NodeStep {
+    bool ran, run, loads;       // step n-1 ran / step n runs / external loads present
+    long long step;             // block step number of step n
+    double t;                   // time of step n-1 (external forces)
+    double hdt, dtn, hdtn;      // dt/2 of the step being completed; dt, dt/2 of the next
+    float2 hdt2, dtn2, hdtn2;   // the same as double-words (mixed)
+};
+
 template <int MODE>
-__device__ __forceinline__ void node_body_quad(const Problem &p, long long i, bool valid, const Ctrl &cp,
-                                               const StepDecision &d)
+__device__ __forceinline__ void node_step(const Problem &p, int parity, NodeStep &ns)
+{
+    const Ctrl cp = p.ctrl[parity ^ 1];
+    const StepDecision d = decide_step(p, cp, parity);
+    ns.ran = cp.ran;
+    ns.run = d.run;
+    ns.step = d.next.step;
+    ns.t = cp.t;
+    ns.hdt = 0.5 * cp.dt;
+    ns.dtn = d.next.dt;
+    ns.hdtn = 0.5 * ns.dtn;
+    if (MODE == MODE_MIXED) {
+        ns.hdt2 = df_from(ns.hdt);
+        ns.dtn2 = df_from(ns.dtn);
+        ns.hdtn2 = df_from(ns.hdtn);
+    }
+    ns.loads = p.grav_n || p.node_nf;
+}
+
+// Node kernel bodies of the tiled FP64 and mixed kernels: four lanes per node.
+// The node's corner forces sit in its CSR slots [node_ptr[i], node_ptr[i+1]),
+// in element order; lane q sums slots k0+q, k0+q+4, ...  The lane sums l_q
+// are combined as (l0 + l1) + (l2 + l3) for every component (addition and
+// the compensated merge are commutative, so the result does not depend on
+// which lane adds): each lane receives only what it or the lane it serves
+// next needs.  Lane c < 3 then updates DOF c: a = (f_ext - f_int)/m,
+// v += (dt/2)(a_prev + a), u += dt (v + (dt/2) a), or the Dirichlet values.
+// The DOF state, mass and Dirichlet record are loaded before the gather so
+// their latency overlaps it.  All 32 lanes of a warp call these together
+// (valid = false past the tile's end).
+template <typename T>
+__device__ __forceinline__ T pick3(int c, T a, T b, T d) { return c == 0 ? a : (c == 1 ? b : d); }
+
+__device__ __forceinline__ double node_fext(const Problem &p, long long i, int q, const NodeStep &ns)
+{
+    double f3[3];
+    external_force(p, i, ns.t, f3);
+    return pick3(q, f3[0], f3[1], f3[2]);
+}
+
+__device__ __forceinline__ void node_quad_fp64(const Problem &p, long long i, bool valid, const NodeStep &ns)
 {
     const int q = threadIdx.x & 3;
-    int2 br[3] = {make_int2(0, 1), make_int2(0, 1), make_int2(0, 1)};
-    if (valid) node_bc_records(p, i, br);
-    const bool need = valid && cp.ran && (br[0].y == 0 || br[1].y == 0 || br[2].y == 0);
-    const int k0 = need ? p.node_ptr[i] : 0, k1 = need ? p.node_ptr[i + 1] : 0;
-    double s[3];
-    if (MODE == MODE_MIXED) {
-        float sh[3] = {0.f, 0.f, 0.f}, sc[3] = {0.f, 0.f, 0.f};
-        for (int k = k0 + q; k < k1; k += 4) {
-            const float *f = p.fe32 + (long long)p.node_inc[k] * 3;
-#pragma unroll
-            for (int c = 0; c < 3; c++) neumaier_merge(sh[c], sc[c], f[c], 0.0f);
-        }
-#pragma unroll
-        for (int m = 1; m <= 2; m <<= 1)
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                float oh = __shfl_xor_sync(0xffffffffu, sh[c], m), oc = __shfl_xor_sync(0xffffffffu, sc[c], m);
-                if (q & m) {   // partner is the lower lane: it goes first
-                    float th = oh, tc = oc;
-                    neumaier_merge(th, tc, sh[c], sc[c]);
-                    sh[c] = th;
-                    sc[c] = tc;
-                } else {
-                    neumaier_merge(sh[c], sc[c], oh, oc);
-                }
-            }
-#pragma unroll
-        for (int c = 0; c < 3; c++) s[c] = (double)sh[c] + (double)sc[c];
-    } else {
-        s[0] = s[1] = s[2] = 0.0;
-        for (int k = k0 + q; k < k1; k += 4) {
-            const double *f = p.fe + (long long)p.node_inc[k] * 3;
-            s[0] += f[0];
-            s[1] += f[1];
-            s[2] += f[2];
-        }
-#pragma unroll
-        for (int m = 1; m <= 2; m <<= 1)
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                double o = __shfl_xor_sync(0xffffffffu, s[c], m);
-                s[c] = (q & m) ? o + s[c] : s[c] + o;
-            }
+    const bool odd = q & 1;
+    const bool own = valid && q < 3;   // this lane updates DOF q of node i
+    const long long dof = i + (long long)q * p.nn;
+    double ui = 0, vi = 0, ai = 0, minv = 0;
+    int rec = -1;
+    if (own) {
+        ui = p.u[dof];
+        vi = p.v[dof];
+        ai = p.a[dof];
+        minv = p.minv[i];
+        rec = p.node_bc[i];
     }
-    if (!valid || q == 3) return;
-    double fx[3] = {0.0, 0.0, 0.0};
-    if (cp.ran) external_force(p, i, cp.t, fx);
-    dof_update<MODE>(p, i, q, s[q], fx[q], br[q], cp, d);
+    int k0 = 0, k1 = 0;
+    if (valid && ns.ran) {
+        k0 = p.node_ptr[i];
+        k1 = p.node_ptr[i + 1];
+    }
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    int k = k0 + q;
+    if (k < k1) {
+        const double *f = p.fe + (long long)k * 3;
+        s0 = f[0];
+        s1 = f[1];
+        s2 = f[2];
+        k += 4;
+    }
+    for (; k < k1; k += 4) {
+        const double *f = p.fe + (long long)k * 3;
+        s0 += f[0];
+        s1 += f[1];
+        s2 += f[2];
+    }
+    // pairs (0,1), (2,3): even lanes need components 0 and 2, odd lanes 1
+    double x = __shfl_xor_sync(0xffffffffu, odd ? s0 : s1, 1), y = __shfl_xor_sync(0xffffffffu, s2, 1);
+    if (odd) {
+        s1 += x;
+    } else {
+        s0 += x;
+        s2 += y;
+    }
+    // across pairs: lanes 0 <-> 2 exchange components 2 / 0, lane 1 <- 3 component 1
+    double z = __shfl_xor_sync(0xffffffffu, odd ? s1 : (q == 0 ? s2 : s0), 2);
+    if (!own) return;
+    const double s = pick3(q, s0, s1, s2) + z;
+    const int2 br = rec >= 0 ? p.bc_rec[rec * 3 + q] : make_int2(0, 0);
+    const bool act = br.y == 0;
+    bool changed = false;
+    if (ns.ran && act) {
+        const double an = (ns.loads ? node_fext(p, i, q, ns) - s : -s) * minv;
+        vi = fma(ns.hdt, ai + an, vi);
+        ai = an;
+        changed = true;
+    }
+    if (ns.run) {
+        if (act) {
+            ui = fma(ns.dtn, fma(ns.hdtn, ai, vi), ui);
+        } else {
+            for (int k = br.x; k < br.x + br.y; k++) {
+                double Ud = bc_increment(p.bcs[k], ns.dtn, ns.step);
+                ui += Ud;
+                vi = Ud;
+                ai = 0.;
+            }
+        }
+        changed = true;
+    }
+    if (changed) {
+        p.u[dof] = ui;
+        p.v[dof] = vi;
+        p.a[dof] = ai;
+    }
+}
+
+__device__ __forceinline__ void node_quad_mixed(const Problem &p, long long i, bool valid, const NodeStep &ns)
+{
+    const int q = threadIdx.x & 3;
+    const bool odd = q & 1;
+    const bool own = valid && q < 3;
+    const long long dof = i + (long long)q * p.nn;
+    float2 uq = make_float2(0.f, 0.f), vq = uq, aq = uq, minv = uq;
+    int rec = -1;
+    if (own) {
+        uq = p.uhl[dof];
+        vq = p.vhl[dof];
+        aq = p.ahl[dof];
+        minv = p.minv2[i];
+        rec = p.node_bc[i];
+    }
+    int k0 = 0, k1 = 0;
+    if (valid && ns.ran) {
+        k0 = p.node_ptr[i];
+        k1 = p.node_ptr[i + 1];
+    }
+    // compensated FP32 sums (Neumaier) of the FP32 corner forces
+    const float4 *fe = reinterpret_cast<const float4 *>(p.fe32);
+    float h0 = 0.f, h1 = 0.f, h2 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
+    int k = k0 + q;
+    if (k < k1) {
+        const float4 f = fe[k];
+        h0 = f.x;
+        h1 = f.y;
+        h2 = f.z;
+        k += 4;
+    }
+    for (; k < k1; k += 4) {
+        const float4 f = fe[k];
+        neumaier_merge(h0, c0, f.x, 0.0f);
+        neumaier_merge(h1, c1, f.y, 0.0f);
+        neumaier_merge(h2, c2, f.z, 0.0f);
+    }
+    float ah = odd ? h0 : h1, ac = odd ? c0 : c1;
+    float xh = __shfl_xor_sync(0xffffffffu, ah, 1), xc = __shfl_xor_sync(0xffffffffu, ac, 1);
+    float yh = __shfl_xor_sync(0xffffffffu, h2, 1), yc = __shfl_xor_sync(0xffffffffu, c2, 1);
+    if (odd) {
+        neumaier_merge(h1, c1, xh, xc);
+    } else {
+        neumaier_merge(h0, c0, xh, xc);
+        neumaier_merge(h2, c2, yh, yc);
+    }
+    float sh = odd ? h1 : (q == 0 ? h2 : h0), sc = odd ? c1 : (q == 0 ? c2 : c0);
+    float zh = __shfl_xor_sync(0xffffffffu, sh, 2), zc = __shfl_xor_sync(0xffffffffu, sc, 2);
+    float mh = pick3(q, h0, h1, h2), mc = pick3(q, c0, c1, c2);
+    neumaier_merge(mh, mc, zh, zc);
+    if (!own) return;
+    const float2 s = df_two_sum(mh, mc);
+    const int2 br = rec >= 0 ? p.bc_rec[rec * 3 + q] : make_int2(0, 0);
+    const bool act = br.y == 0;
+    bool changed = false;
+    if (ns.ran && act) {
+        const float2 f = ns.loads ? df_add(df_from(node_fext(p, i, q, ns)), df_neg(s)) : df_neg(s);
+        const float2 an = df_mul(f, minv);
+        vq = df_add(vq, df_mul(ns.hdt2, df_add(aq, an)));
+        aq = an;
+        changed = true;
+    }
+    if (ns.run) {
+        if (act) {
+            uq = df_add(uq, df_mul(ns.dtn2, df_add(vq, df_mul(ns.hdtn2, aq))));
+        } else {
+            for (int k = br.x; k < br.x + br.y; k++) {
+                const float2 Ud = df_from(bc_increment(p.bcs[k], ns.dtn, ns.step));
+                uq = df_add(uq, Ud);
+                vq = Ud;
+                aq = make_float2(0.f, 0.f);
+            }
+        }
+        changed = true;
+    }
+    if (changed) {
+        p.uhl[dof] = uq;
+        p.vhl[dof] = vq;
+        p.ahl[dof] = aq;
+    }
 }
 
 // Writes the new control slot and clears the slots the element kernel fills.
@@ -635,6 +843,19 @@ static __device__ __noinline__ double cfl_fp64(const Problem &p, long long e)
     return ((dist < Lr) ? dist : Lr) / mat_of(p, e).c;
 }
 
+// x rounded toward zero to FP32 with integer operations only (the FP64->FP32
+// conversion instruction would take the FP64 pipe): relative error below
+// 2^-23 in FP32's normal range, signed zero below it, signed infinity above.
+__device__ __forceinline__ float f32_trunc(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned sign = hi & 0x80000000u;
+    const int ex = (int)((hi >> 20) & 0x7FFu) - (1023 - 127);
+    const unsigned mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned r = ex <= 0 ? sign : (ex >= 255 ? (sign | 0x7F800000u) : (sign | ((unsigned)ex << 23) | mant));
+    return __uint_as_float(r);
+}
+
 // FP32 estimate of an element's CFL value from the FP32 reference edges plus
 // the displacement differences.  Its relative error stays below ~3e-4 unless
 // the tet is a sliver (6V < 4e-3 |e1||e2||e3|); slivers are returned negated
@@ -698,14 +919,20 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
             f[a * 3 + i] = P[i * 3] * G[(a - 1) * 3] + P[i * 3 + 1] * G[(a - 1) * 3 + 1] + P[i * 3 + 2] * G[(a - 1) * 3 + 2];
 #pragma unroll
     for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
-    double2 *fe = reinterpret_cast<double2 *>(p.fe + e * 12);
+    const int4 sl = __ldg(p.slot + e);
+    const int ks[4] = {sl.x, sl.y, sl.z, sl.w};
 #pragma unroll
-    for (int k = 0; k < 6; k++) fe[k] = make_double2(f[2 * k], f[2 * k + 1]);
+    for (int a = 0; a < 4; a++) {
+        double *fk = p.fe + (long long)ks[a] * 3;
+        fk[0] = f[a * 3];
+        fk[1] = f[a * 3 + 1];
+        fk[2] = f[a * 3 + 2];
+    }
     if (FORCE_ONLY) return 0.0f;
     if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
     float du32[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) du32[k] = (float)du[k];
+    for (int k = 0; k < 9; k++) du32[k] = f32_trunc(du[k]);
     return cfl_screen(p, e, du32, m);
 }
 
@@ -722,25 +949,7 @@ static __global__ void __launch_bounds__(kElemBlock) elem_force_kernel_fp64(Prob
 // ln J in FP64; FP32 corner forces; FP32 CFL length with the dt min in FP64.
 // cof(I + H) = I + D with D = (tr H + I2) I - (1 + tr H) H^T + (H^2)^T.
 // ---------------------------------------------------------------------------
-// ln(1 + x) in FP64.  For |x| < 2^-7, the usual size of J - 1, the Taylor
-// series to x^9 by Horner's rule (truncation below |x|^10/10 < 1e-21 |x|);
-// otherwise the library log1p.
-__device__ __forceinline__ double log1p_fp64(double x)
-{
-    if (fabs(x) >= 0.0078125) return log1p(x);
-    double p = 1.0 / 9.0;
-    p = fma(p, -x, 1.0 / 8.0);
-    p = fma(p, -x, 1.0 / 7.0);
-    p = fma(p, -x, 1.0 / 6.0);
-    p = fma(p, -x, 1.0 / 5.0);
-    p = fma(p, -x, 1.0 / 4.0);
-    p = fma(p, -x, 1.0 / 3.0);
-    p = fma(p, -x, 1.0 / 2.0);
-    p = fma(p, -x, 1.0);
-    return p * x;
-}
-
-__device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H, double Jm1d, double lnJd,
+__device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H, float Jm1, float lnJ,
                                              float t, float I2, float *P)
 {
     if (m.law == 2) {
@@ -776,7 +985,6 @@ __device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H,
             float h2 = H[j * 3] * H[i] + H[j * 3 + 1] * H[3 + i] + H[j * 3 + 2] * H[6 + i];
             D[i * 3 + j] = (i == j ? a0 : 0.0f) - a1 * H[j * 3 + i] + h2;
         }
-    float Jm1 = (float)Jm1d, lnJ = (float)lnJd;
     float iJ = 1.0f / (1.0f + Jm1);
     if (m.law == 1) {
         // P = [mu (Jm1 I + (1+Jm1) H - D) + lambda lnJ (I + D)] / J
@@ -831,17 +1039,20 @@ __device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, 
         for (int i = 0; i < 3; i++)
 #pragma unroll
             for (int j = 0; j < 3; j++) H[i * 3 + j] = du[i] * G[j] + du[3 + i] * G[3 + j] + du[6 + i] * G[6 + j];
-        // J - 1 = tr H + (I2(H) + det H) in FP64 and ln J = log1p(J - 1) in
-        // FP64: the trace, the term that carries J - 1, is summed exactly in
-        // FP64; I2 and det H are O(|H|^2) and their FP32 rounding lies far
-        // below the FP32 precision of J - 1, so forming them in FP32 loses
-        // nothing while F = I + H never has to be formed or reduced.
+        // J - 1 = tr H + (I2(H) + det H).  The trace carries J - 1 and may
+        // cancel (nearly isochoric motion), so it is summed without rounding,
+        // as s + err by TwoSum; I2 and det H are O(|H|^2) and their FP32
+        // rounding lies far below the FP32 precision of J - 1.  So J - 1 is
+        // good to FP32 relative precision, and so is ln J = log1p(J - 1);
+        // F = I + H is never formed or reduced.
         float tf = H[0] + H[4] + H[8];
         float I2f = (H[0] * H[4] - H[1] * H[3]) + (H[4] * H[8] - H[5] * H[7]) + (H[0] * H[8] - H[2] * H[6]);
         float I3f = H[0] * (H[4] * H[8] - H[5] * H[7]) - H[1] * (H[3] * H[8] - H[5] * H[6]) +
                     H[2] * (H[3] * H[7] - H[4] * H[6]);
-        double Jm1 = (((double)H[0] + (double)H[4]) + (double)H[8]) + (double)(I2f + I3f);
-        double lnJ = log1p_fp64(Jm1);
+        const float s1 = H[0] + H[4], s2 = s1 + H[8];
+        const float terr = two_sum_err(H[0], H[4], s1) + two_sum_err(s1, H[8], s2);
+        const float Jm1 = s2 + (terr + (I2f + I3f));
+        const float lnJ = log1pf(Jm1);
         const MatParams &m = mat_of(p, e);
         float P[9];
         stress_mixed(m, H, Jm1, lnJ, tf, I2f, P);
@@ -857,10 +1068,12 @@ __device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, 
                                P[i * 3 + 2] * G[(a - 1) * 3 + 2];
 #pragma unroll
         for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
-        float4 *fe = reinterpret_cast<float4 *>(p.fe32 + e * 12);
-        fe[0] = make_float4(f[0], f[1], f[2], f[3]);
-        fe[1] = make_float4(f[4], f[5], f[6], f[7]);
-        fe[2] = make_float4(f[8], f[9], f[10], f[11]);
+        const int4 sl = __ldg(p.slot + e);
+        float4 *fe = reinterpret_cast<float4 *>(p.fe32);
+        fe[sl.x] = make_float4(f[0], f[1], f[2], 0.f);
+        fe[sl.y] = make_float4(f[3], f[4], f[5], 0.f);
+        fe[sl.z] = make_float4(f[6], f[7], f[8], 0.f);
+        fe[sl.w] = make_float4(f[9], f[10], f[11], 0.f);
         if (!FORCE_ONLY) {
             float e1[3], e2[3], e3[3];
 #pragma unroll
@@ -872,7 +1085,7 @@ __device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, 
             float dist = char_length_edges<float>(e1, e2, e3);
             float Lr = __ldg(p.Lref32 + e);
             vmin = ((dist < Lr) ? dist : Lr) * m.inv_c_f;
-            if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
+            if (e == 0 && !isfinite(p.uhl[1].x)) atomicOr(p.flags + (parity ^ 1), 1);
         }
     }
     return vmin;
@@ -909,25 +1122,59 @@ __device__ __forceinline__ float block_min_bcast(float v)
 // and the same graph serves any admitted set.  Per-solve control, CFL slot
 // and NaN flag are those of the solve's Problem.
 // ---------------------------------------------------------------------------
-template <int MODE>
-__global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
-                                 const int *__restrict__ ntiles, int parity)
-{
-    const int n = *ntiles;
-    for (int t = blockIdx.x; t < n; t += gridDim.x) {
-        const Tile tl = tiles[t];
-        const Problem &p = descs[tl.solve];
-        const Ctrl cp = p.ctrl[parity ^ 1];
-        StepDecision d = decide_step(p, cp, parity);
-        if (tl.begin == 0 && threadIdx.x == 0) publish_step(p, d, parity);
-        if (!cp.ran && !d.run) continue;
-        // four lanes per node; every lane runs the same number of iterations
-        const int per = blockDim.x >> 2;
-        for (long long b = tl.begin; b < tl.end; b += per) {
-            long long i = b + (threadIdx.x >> 2);
-            node_body_quad<MODE>(p, i, i < tl.end, cp, d);
+// Dynamic tile assignment.  sched = {tile count, claim counter, blocks done}.
+// Thread 0 claims the block's next tile while the block works on the current
+// one; every block makes exactly one claim past the end, and the last block to
+// run out puts both counters back to zero for the next launch.  Which block
+// runs a tile changes no result.
+struct TileQueue {
+    int *sched;
+    int n;
+    __device__ __forceinline__ int claim() { return atomicAdd(sched + 1, 1); }
+    __device__ __forceinline__ void finish()
+    {
+        if (threadIdx.x == 0 && atomicAdd(sched + 2, 1) == (int)gridDim.x - 1) {
+            atomicExch(sched + 1, 0);
+            atomicExch(sched + 2, 0);
         }
     }
+};
+
+// Node kernel over tiles (node ranges of one solve), four lanes per node.
+template <int MODE>
+__global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
+                                 int *__restrict__ sched, int parity)
+{
+    __shared__ int s_tile;
+    TileQueue q{sched, sched[0]};
+    if (threadIdx.x == 0) s_tile = q.claim();
+    __syncthreads();
+    int t = s_tile, cur = -1;
+    NodeStep ns;
+    while (t < q.n) {
+        int next = 0;
+        if (threadIdx.x == 0) next = q.claim();
+        const Tile tl = tiles[t];
+        const Problem &p = descs[tl.solve];
+        if (tl.solve != cur) {
+            node_step<MODE>(p, parity, ns);
+            cur = tl.solve;
+        }
+        if (tl.begin == 0 && threadIdx.x == 0) publish_step(p, decide_step(p, p.ctrl[parity ^ 1], parity), parity);
+        if (ns.ran || ns.run) {
+            const int per = blockDim.x >> 2;   // every lane runs the same number of passes
+            for (long long b = tl.begin; b < tl.end; b += per) {
+                long long i = b + (threadIdx.x >> 2);
+                if (MODE == MODE_MIXED) node_quad_mixed(p, i, i < tl.end, ns);
+                else node_quad_fp64(p, i, i < tl.end, ns);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_tile = next;
+        __syncthreads();
+        t = s_tile;
+    }
+    q.finish();
 }
 
 // Element kernel over tiles.  FP64: every element's FP32 CFL screen value is
@@ -937,34 +1184,46 @@ __global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *
 template <int MODE>
 __global__ void __launch_bounds__(kStepThreads) pool_elem_kernel(const Problem *__restrict__ descs,
                                                                  const Tile *__restrict__ tiles,
-                                                                 const int *__restrict__ ntiles, int parity)
+                                                                 int *__restrict__ sched, int parity)
 {
     __shared__ float sdt[MODE == MODE_MIXED ? 1 : kMaxTileElems];
-    const int n = *ntiles;
-    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+    __shared__ int s_tile;
+    TileQueue q{sched, sched[0]};
+    if (threadIdx.x == 0) s_tile = q.claim();
+    __syncthreads();
+    int t = s_tile;
+    while (t < q.n) {
+        int next = 0;
+        if (threadIdx.x == 0) next = q.claim();
         const Tile tl = tiles[t];
         const Problem &p = descs[tl.solve];
-        if (!p.ctrl[parity].ran) continue;
-        float v32 = INFINITY;
-        for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
-            float d = MODE == MODE_MIXED ? elem_body_mixed<false>(p, e, parity) : elem_body_fp64<false>(p, e, parity);
-            if (MODE != MODE_MIXED) sdt[e - tl.begin] = d;
-            if (d >= 0.0f) v32 = fminf(v32, d);
+        if (p.ctrl[parity].ran) {
+            float v32 = INFINITY;
+            for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
+                float d = MODE == MODE_MIXED ? elem_body_mixed<false>(p, e, parity) : elem_body_fp64<false>(p, e, parity);
+                if (MODE != MODE_MIXED) sdt[e - tl.begin] = d;
+                if (d >= 0.0f) v32 = fminf(v32, d);
+            }
+            float bmin = block_min_bcast(v32);   // also orders the sdt writes before the reads below
+            if (MODE == MODE_MIXED) {
+                if (threadIdx.x == 0 && bmin < INFINITY)
+                    atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong((double)bmin));
+            } else {
+                const float thr = bmin * (1.0f + 1.0f / 256.0f);
+                double v = INFINITY;
+                for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
+                    float d = sdt[e - tl.begin];
+                    if (d < 0.0f || d <= thr) v = fmin(v, cfl_fp64(p, e));
+                }
+                block_min_to(v, p.dtmin + (parity ^ 1));
+            }
         }
-        float bmin = block_min_bcast(v32);   // also orders the sdt writes before the reads below
-        if (MODE == MODE_MIXED) {
-            if (threadIdx.x == 0 && bmin < INFINITY)
-                atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong((double)bmin));
-            continue;
-        }
-        const float thr = bmin * (1.0f + 1.0f / 256.0f);
-        double v = INFINITY;
-        for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
-            float d = sdt[e - tl.begin];
-            if (d < 0.0f || d <= thr) v = fmin(v, cfl_fp64(p, e));
-        }
-        block_min_to(v, p.dtmin + (parity ^ 1));
+        __syncthreads();
+        if (threadIdx.x == 0) s_tile = next;
+        __syncthreads();
+        t = s_tile;
     }
+    q.finish();
 }
 
 #ifdef MSX_SETUP_KERNELS
@@ -1194,9 +1453,10 @@ __global__ void gather_kernel(Problem p, double *fint)
     if (i >= p.nn) return;
     double s[3] = {0, 0, 0};
     for (int k = p.node_ptr[i]; k < p.node_ptr[i + 1]; k++) {
-        long long inc = p.node_inc[k];
+        // reference-order corner forces are in element order, the others in CSR slots
+        long long inc = MODE == MODE_EXACT ? p.node_inc[k] : k;
 #pragma unroll
-        for (int c = 0; c < 3; c++) s[c] += MODE == MODE_MIXED ? (double)p.fe32[inc * 3 + c] : p.fe[inc * 3 + c];
+        for (int c = 0; c < 3; c++) s[c] += MODE == MODE_MIXED ? (double)p.fe32[inc * 4 + c] : p.fe[inc * 3 + c];
     }
 #pragma unroll
     for (int c = 0; c < 3; c++) fint[i + c * p.nn] = s[c];

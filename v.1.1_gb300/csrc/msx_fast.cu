@@ -17,22 +17,62 @@ void launch_internal_force_mixed(const Problem &p, double *fint, cudaStream_t s)
     gather_kernel<MODE_MIXED><<<grid_for(p.nn, 256), 256, 0, s>>>(p, fint);
 }
 
-void launch_tiled_node(const Problem *descs, const Tile *ntiles, const int *counts, int mode, int parity, int grid,
+void launch_tiled_node(const Problem *descs, const Tile *ntiles, int *counts, int mode, int parity, int grid,
                        int threads, cudaStream_t s)
 {
     if (mode == MODE_MIXED)
-        pool_node_kernel<MODE_MIXED><<<grid, threads, 0, s>>>(descs, ntiles, counts + 1, parity);
+        pool_node_kernel<MODE_MIXED><<<grid, threads, 0, s>>>(descs, ntiles, counts + 3, parity);
     else
-        pool_node_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, ntiles, counts + 1, parity);
+        pool_node_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, ntiles, counts + 3, parity);
 }
 
-void launch_tiled_elem(const Problem *descs, const Tile *etiles, const int *counts, int mode, int parity, int grid,
+void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, int mode, int parity, int grid,
                        int threads, cudaStream_t s)
 {
     if (mode == MODE_MIXED)
         pool_elem_kernel<MODE_MIXED><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
     else
         pool_elem_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
+}
+
+__global__ void state_split_kernel(Problem p)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * p.nn) return;
+    p.uhl[i] = df_from(p.u[i]);
+    p.vhl[i] = df_from(p.v[i]);
+    p.ahl[i] = df_from(p.a[i]);
+}
+
+__global__ void state_merge_kernel(Problem p)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * p.nn) return;
+    float2 u = p.uhl[i], v = p.vhl[i], a = p.ahl[i];
+    p.u[i] = (double)u.x + (double)u.y;
+    p.v[i] = (double)v.x + (double)v.y;
+    p.a[i] = (double)a.x + (double)a.y;
+}
+
+__global__ void minv_split_kernel(const double *minv, float2 *minv2, long long nn)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nn) minv2[i] = df_from(minv[i]);
+}
+
+void launch_state_split(const Problem &p, cudaStream_t s)
+{
+    state_split_kernel<<<grid_for(3 * p.nn, 256), 256, 0, s>>>(p);
+}
+
+void launch_state_merge(const Problem &p, cudaStream_t s)
+{
+    state_merge_kernel<<<grid_for(3 * p.nn, 256), 256, 0, s>>>(p);
+}
+
+void launch_minv_split(const double *minv, float2 *minv2, long long nn, cudaStream_t s)
+{
+    minv_split_kernel<<<grid_for(nn, 256), 256, 0, s>>>(minv, minv2, nn);
 }
 
 int tiled_ctas_per_sm(int mode, int threads, bool node)

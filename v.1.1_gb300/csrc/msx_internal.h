@@ -70,13 +70,19 @@ struct Problem {
     double *u, *v, *a;
     const double *mass;       // lumped mass per node
     const double *minv;       // 1/mass per node
-    float2 *uhl;              // 3*nn (hi, lo) split of u for the mixed element kernel
-    // corner forces, fe[(e*4 + a)*3 + i]
+    // mixed mode: u, v, a as FP32 (hi, lo) pairs (value hi + lo) while a block
+    // runs; u, v, a above hold the state between calls (state_merge)
+    float2 *uhl, *vhl, *ahl;  // 3*nn each
+    const float2 *minv2;      // 1/mass as an (hi, lo) pair
+    // corner forces.  Reference-order mode: fe[(e*4 + a)*3 + i] (element
+    // order).  FP64 and mixed modes: in the node's CSR slot k = slot[e].a,
+    // fe[k*3 + i] and fe32[k*4 + i], so a node's corner forces are contiguous.
     double *fe;
     float *fe32;
     // node -> (element, corner) incidences sorted by element id
     const int *node_ptr;
     const int *node_inc;      // e*4 + a
+    const int4 *slot;         // per element: CSR positions k of its four corners
     // Dirichlet data
     const int *node_bc;       // per node: -1 or record index
     const int2 *bc_rec;       // per record, per comp: (first entry, count)
@@ -96,8 +102,8 @@ struct Problem {
 };
 
 // A contiguous element (or node) range [begin, end) of one solve.  The step
-// kernels of the FP64 and mixed modes stride over a list of tiles, so one
-// solve and many pooled solves run the same kernels.
+// kernels of the FP64 and mixed modes take tiles from a list, so one solve and
+// many pooled solves run the same kernels.
 struct Tile {
     int solve;
     int begin, end;
@@ -107,14 +113,21 @@ constexpr int kStepThreads = 256;   // upper bound on the CTA size of the tiled 
 constexpr int kMaxTileElems = 4096; // upper bound on the elements of one tile
 
 // Tiled step kernels (one instantiation in msx_fast.cu, used by msx_run and
-// the pool).  `counts` points to the element-tile count, counts + 1 to the
-// node-tile count, both in device memory.
-void launch_tiled_node(const Problem *descs, const Tile *ntiles, const int *counts, int mode, int parity, int grid,
+// the pool).  `counts` is kTileSched ints of device memory: element-tile
+// count, claim counter, blocks done, then the same three for the node tiles;
+// the counters start at zero and every launch leaves them at zero.
+constexpr int kTileSched = 6;
+void launch_tiled_node(const Problem *descs, const Tile *ntiles, int *counts, int mode, int parity, int grid,
                        int threads, cudaStream_t s);
-void launch_tiled_elem(const Problem *descs, const Tile *etiles, const int *counts, int mode, int parity, int grid,
+void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, int mode, int parity, int grid,
                        int threads, cudaStream_t s);
 // CTAs of the tiled element kernel (node kernel when `node` is true) that fit on one SM
 int tiled_ctas_per_sm(int mode, int threads, bool node = false);
+// Mixed-mode state conversions: u, v, a (FP64) -> uhl, vhl, ahl, and back
+// (hi + lo, exact unless the pair spans more than 53 bits); minv -> minv2.
+void launch_state_split(const Problem &p, cudaStream_t s);
+void launch_state_merge(const Problem &p, cudaStream_t s);
+void launch_minv_split(const double *minv, float2 *minv2, long long nn, cudaStream_t s);
 
 // records the message returned by msx_last_error() on this host thread
 void msx_set_error(const char *msg);

@@ -100,7 +100,7 @@ struct msx_pool {
     unsigned long long *d_dtmin = nullptr;
     int *d_flags = nullptr;
     Tile *d_etiles = nullptr, *d_ntiles = nullptr;
-    int *d_counts = nullptr;   // [0] element tiles, [1] node tiles
+    int *d_counts = nullptr;   // element tiles, claim, done, node tiles, claim, done
     size_t tile_cap = 0;
     std::vector<Tile> h_etiles, h_ntiles;
     bool tiles_dirty = true;
@@ -127,8 +127,11 @@ static size_t footprint(long long nn, long long ne, long long nbc, int precision
     b += 2 * align256(sizeof(float) * 9 * ne) + 2 * align256(sizeof(float) * ne);    // G32, Eref32, wJ32, Lref32
     b += 4 * align256(sizeof(double) * 3 * nn) + 2 * align256(sizeof(double) * nn);  // X, u, v, a, mass, minv
     b += align256(sizeof(float2) * 3 * nn);                                          // uhl
-    b += precision == MSX_PREC_MIXED ? align256(sizeof(float) * 12 * ne) : align256(sizeof(double) * 12 * ne);
+    if (precision == MSX_PREC_MIXED)                                                 // vhl, ahl, minv2
+        b += 2 * align256(sizeof(float2) * 3 * nn) + align256(sizeof(float2) * nn);
+    b += precision == MSX_PREC_MIXED ? align256(sizeof(float) * 16 * ne) : align256(sizeof(double) * 12 * ne);
     b += align256(sizeof(int) * (nn + 1)) + align256(sizeof(int) * 4 * ne) + align256(sizeof(int) * nn);
+    b += align256(sizeof(int4) * ne);                                                // corner slots
     b += align256(sizeof(int2) * 3 * nn) + align256(sizeof(BCEntry) * (nbc > 0 ? nbc : 1));
     return b;
 }
@@ -163,7 +166,7 @@ static void rebuild_tiles(msx_pool *p)
 {
     p->h_etiles.clear();
     p->h_ntiles.clear();
-    const int te = p->sched.tile_elems, tn = p->sched.threads * 4;
+    const int te = p->sched.tile_elems, tn = p->sched.threads / 2;   // node tiles: two passes of four lanes per node
     for (int s = 0; s < (int)p->slots.size(); s++) {
         const Slot &sl = p->slots[s];
         if (!sl.active) continue;
@@ -189,9 +192,9 @@ static msx_status upload_tiles(msx_pool *p)
             p->graph = nullptr;
         }
     }
-    int counts[2] = {(int)p->h_etiles.size(), (int)p->h_ntiles.size()};
+    int counts[kTileSched] = {(int)p->h_etiles.size(), 0, 0, (int)p->h_ntiles.size(), 0, 0};
     if (counts[0]) PCUDA(cudaMemcpyAsync(p->d_etiles, p->h_etiles.data(), sizeof(Tile) * counts[0], cudaMemcpyHostToDevice, p->stream));
-    if (counts[1]) PCUDA(cudaMemcpyAsync(p->d_ntiles, p->h_ntiles.data(), sizeof(Tile) * counts[1], cudaMemcpyHostToDevice, p->stream));
+    if (counts[3]) PCUDA(cudaMemcpyAsync(p->d_ntiles, p->h_ntiles.data(), sizeof(Tile) * counts[3], cudaMemcpyHostToDevice, p->stream));
     PCUDA(cudaMemcpyAsync(p->d_counts, counts, sizeof(counts), cudaMemcpyHostToDevice, p->stream));
     PCUDA(cudaStreamSynchronize(p->stream));
     p->tiles_dirty = false;
@@ -246,6 +249,7 @@ static msx_status collect(msx_pool *p)
         f.res.steps = c.step;
         f.res.t = c.t;
         size_t bytes = sizeof(double) * 3 * sl.nn;
+        if (p->opts.precision == MSX_PREC_MIXED) launch_state_merge(sl.P, p->stream);
         f.u.resize(3 * sl.nn);
         f.v.resize(3 * sl.nn);
         f.a.resize(3 * sl.nn);
@@ -391,11 +395,11 @@ extern "C" msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out)
     size_t n = opts->max_slots;
     if (cudaMalloc(&p->d_descs, sizeof(Problem) * n) != cudaSuccess || cudaMalloc(&p->d_ctrl, sizeof(Ctrl) * 2 * n) != cudaSuccess ||
         cudaMalloc(&p->d_dtmin, sizeof(unsigned long long) * 2 * n) != cudaSuccess ||
-        cudaMalloc(&p->d_flags, sizeof(int) * 2 * n) != cudaSuccess || cudaMalloc(&p->d_counts, sizeof(int) * 2) != cudaSuccess ||
+        cudaMalloc(&p->d_flags, sizeof(int) * 2 * n) != cudaSuccess || cudaMalloc(&p->d_counts, sizeof(int) * kTileSched) != cudaSuccess ||
         cudaMallocHost(&p->h_ctrl, sizeof(Ctrl) * 2 * n) != cudaSuccess)
         return bail(pfail(MSX_ERR_OOM, "pool tables"));
     cudaMemset(p->d_ctrl, 0, sizeof(Ctrl) * 2 * n);
-    cudaMemset(p->d_counts, 0, sizeof(int) * 2);
+    cudaMemset(p->d_counts, 0, sizeof(int) * kTileSched);
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     p->budget = opts->hbm_budget_bytes > 0 ? (size_t)opts->hbm_budget_bytes : (size_t)(0.8 * fr);
@@ -446,13 +450,17 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     if (slot < 0 || p->used + bytes > p->budget) return pfail(MSX_ERR_BUSY, "pool full (slots or HBM budget)");
 
     // host tables: CSR in element order and Dirichlet records (as the single-solve path)
-    std::vector<int> ptr(nn + 1, 0), inc(4 * ne), node_bc(nn, -1);
+    std::vector<int> ptr(nn + 1, 0), inc(4 * ne), slots(4 * ne), node_bc(nn, -1);
     for (long long k = 0; k < 4 * ne; k++) ptr[mesh->conn[k] + 1]++;
     for (long long i = 0; i < nn; i++) ptr[i + 1] += ptr[i];
     {
         std::vector<int> fill(ptr.begin(), ptr.end() - 1);
         for (long long e = 0; e < ne; e++)
-            for (int q = 0; q < 4; q++) inc[fill[mesh->conn[e * 4 + q]]++] = (int)(e * 4 + q);
+            for (int q = 0; q < 4; q++) {
+                int k = fill[mesh->conn[e * 4 + q]]++;
+                inc[k] = (int)(e * 4 + q);
+                slots[e * 4 + q] = k;
+            }
     }
     std::vector<long long> order(num_bcs);
     std::iota(order.begin(), order.end(), 0);
@@ -514,14 +522,27 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     P.mass = mass;
     P.minv = minv;
     P.uhl = (float2 *)carve(sizeof(float2) * 3 * nn);
-    if (prec == MSX_PREC_MIXED) P.fe32 = (float *)carve(sizeof(float) * 12 * ne);
+    float2 *minv2 = nullptr;
+    if (prec == MSX_PREC_MIXED) {
+        P.vhl = (float2 *)carve(sizeof(float2) * 3 * nn);
+        P.ahl = (float2 *)carve(sizeof(float2) * 3 * nn);
+        minv2 = (float2 *)carve(sizeof(float2) * nn);
+        P.minv2 = minv2;
+    }
+    if (prec == MSX_PREC_MIXED) P.fe32 = (float *)carve(sizeof(float) * 16 * ne);
     else P.fe = (double *)carve(sizeof(double) * 12 * ne);
     int *d_ptr = (int *)carve(sizeof(int) * (nn + 1)), *d_inc = (int *)carve(sizeof(int) * 4 * ne);
     int *d_nbc = (int *)carve(sizeof(int) * nn);
+    int4 *d_slot = (int4 *)carve(sizeof(int4) * ne);
     int2 *d_rec = (int2 *)carve(sizeof(int2) * 3 * nn);
     BCEntry *d_ent = (BCEntry *)carve(sizeof(BCEntry) * (num_bcs > 0 ? num_bcs : 1));
+    if ((size_t)(q - (char *)sl.arena) > bytes) {   // the footprint must cover every array carved above
+        cudaFreeAsync(sl.arena, p->stream);
+        return pfail(MSX_ERR_CUDA, "internal: solve arena smaller than its arrays");
+    }
     P.node_ptr = d_ptr;
     P.node_inc = d_inc;
+    P.slot = d_slot;
     P.node_bc = d_nbc;
     P.bc_rec = d_rec;
     P.bcs = d_ent;
@@ -535,6 +556,7 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     PCUDA(cudaMemcpyAsync(X, mesh->X, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, s));
     PCUDA(cudaMemcpyAsync(d_ptr, ptr.data(), sizeof(int) * (nn + 1), cudaMemcpyHostToDevice, s));
     PCUDA(cudaMemcpyAsync(d_inc, inc.data(), sizeof(int) * 4 * ne, cudaMemcpyHostToDevice, s));
+    PCUDA(cudaMemcpyAsync(d_slot, slots.data(), sizeof(int4) * ne, cudaMemcpyHostToDevice, s));
     PCUDA(cudaMemcpyAsync(d_nbc, node_bc.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, s));
     if (!rec.empty()) PCUDA(cudaMemcpyAsync(d_rec, rec.data(), sizeof(int2) * rec.size(), cudaMemcpyHostToDevice, s));
     if (!ent.empty()) PCUDA(cudaMemcpyAsync(d_ent, ent.data(), sizeof(BCEntry) * ent.size(), cudaMemcpyHostToDevice, s));
@@ -542,8 +564,13 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     PCUDA(cudaMemsetAsync(P.v, 0, sizeof(double) * 3 * nn, s));
     PCUDA(cudaMemsetAsync(P.a, 0, sizeof(double) * 3 * nn, s));
     PCUDA(cudaMemsetAsync(P.uhl, 0, sizeof(float2) * 3 * nn, s));
+    if (prec == MSX_PREC_MIXED) {
+        PCUDA(cudaMemsetAsync(P.vhl, 0, sizeof(float2) * 3 * nn, s));
+        PCUDA(cudaMemsetAsync(P.ahl, 0, sizeof(float2) * 3 * nn, s));
+    }
     launch_setup_elements(P, X, s);
     launch_setup_mass(P, mass, minv, s);
+    if (prec == MSX_PREC_MIXED) launch_minv_split(minv, minv2, nn, s);
     unsigned long long inf2[2] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL};
     PCUDA(cudaMemcpyAsync(P.dtmin, inf2, sizeof(inf2), cudaMemcpyHostToDevice, s));
     launch_initial_cfl(P, nullptr, 0, s);

@@ -96,10 +96,10 @@ struct msx_handle {
     cudaStream_t stream = nullptr;
     Problem P{};
     // owned device storage
-    DBuf<int4> conn;
+    DBuf<int4> conn, slot;
     DBuf<double> G, wJ, Lref, X, u, v, a, mass, minv, fe;
     DBuf<float> G32, wJ32, Lref32, Eref32, fe32;
-    DBuf<float2> uhl;
+    DBuf<float2> uhl, vhl, ahl, minv2;
     DBuf<unsigned char> mat;
     DBuf<int> node_ptr, node_inc, node_bc;
     DBuf<int2> bc_rec;
@@ -220,10 +220,14 @@ static void bind_problem(msx_handle *h)
     P.mass = h->mass.p;
     P.minv = h->minv.p;
     P.uhl = h->uhl.p;
+    P.vhl = h->vhl.p;
+    P.ahl = h->ahl.p;
+    P.minv2 = h->minv2.p;
     P.fe = h->fe.p;
     P.fe32 = h->fe32.p;
     P.node_ptr = h->node_ptr.p;
     P.node_inc = h->node_inc.p;
+    P.slot = h->slot.p;
     P.node_bc = h->node_bc.p;
     P.bc_rec = h->bc_rec.p;
     P.bcs = h->bcs.p;
@@ -273,16 +277,16 @@ static void launch_step(msx_handle *h, int parity)
 static msx_status upload_tiled(msx_handle *h)
 {
     if (!h->tiled) return MSX_OK;
-    const int te = 1024, tn = 1024;
+    const int te = 1024, tn = 128;
     if (!h->d_desc.p) {
         std::vector<Tile> et, nt;
         for (long long b = 0; b < h->P.ne; b += te) et.push_back({0, (int)b, (int)std::min<long long>(h->P.ne, b + te)});
         for (long long b = 0; b < h->P.nn; b += tn) nt.push_back({0, (int)b, (int)std::min<long long>(h->P.nn, b + tn)});
-        int counts[2] = {(int)et.size(), (int)nt.size()};
+        int counts[kTileSched] = {(int)et.size(), 0, 0, (int)nt.size(), 0, 0};
         MSX_CUDA(h->d_desc.alloc(1));
         MSX_CUDA(h->d_etiles.alloc(et.size()));
         MSX_CUDA(h->d_ntiles.alloc(nt.size()));
-        MSX_CUDA(h->d_counts.alloc(2));
+        MSX_CUDA(h->d_counts.alloc(kTileSched));
         MSX_CUDA(cudaMemcpyAsync(h->d_etiles.p, et.data(), sizeof(Tile) * et.size(), cudaMemcpyHostToDevice, h->stream));
         MSX_CUDA(cudaMemcpyAsync(h->d_ntiles.p, nt.data(), sizeof(Tile) * nt.size(), cudaMemcpyHostToDevice, h->stream));
         MSX_CUDA(cudaMemcpyAsync(h->d_counts.p, counts, sizeof(counts), cudaMemcpyHostToDevice, h->stream));
@@ -359,8 +363,7 @@ static msx_status init_block(msx_handle *h)
     init_block_kernel<<<1, 1, 0, h->stream>>>(P, h->t0, limit);
     MSX_CUDA(cudaGetLastError());
     if (h->precision == MSX_PREC_MIXED) {
-        long long n = 3 * P.nn;
-        split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(h->u.p, h->uhl.p, n);
+        launch_state_split(P, h->stream);   // the running state of a mixed block
         MSX_CUDA(cudaGetLastError());
     }
     MSX_CUDA(cudaMemcpyAsync(h->h_ctrl, h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
@@ -467,13 +470,19 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
 
     // node -> (element, corner) CSR in element order: the per-node summation
     // order of classSolverExplicit::computeInternalForce (solverExplicit.cpp:363-379)
-    std::vector<int> ptr(nn + 1, 0), inc(4 * ne);
+    // (slots: where each corner sits in that list; the FP64 and mixed element
+    // kernels write corner forces there, so the node kernel reads them in a run)
+    std::vector<int> ptr(nn + 1, 0), inc(4 * ne), slots(4 * ne);
     for (long long k = 0; k < 4 * ne; k++) ptr[mesh->conn[k] + 1]++;
     for (long long i = 0; i < nn; i++) ptr[i + 1] += ptr[i];
     {
         std::vector<int> fill(ptr.begin(), ptr.end() - 1);
         for (long long e = 0; e < ne; e++)
-            for (int q = 0; q < 4; q++) inc[fill[mesh->conn[e * 4 + q]]++] = (int)(e * 4 + q);
+            for (int q = 0; q < 4; q++) {
+                int k = fill[mesh->conn[e * 4 + q]]++;
+                inc[k] = (int)(e * 4 + q);
+                slots[e * 4 + q] = k;
+            }
     }
 
 #define ALLOC(buf, n) \
@@ -493,8 +502,12 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     ALLOC(h->mass, nn);
     ALLOC(h->minv, nn);
     ALLOC(h->uhl, 3 * nn);
+    ALLOC(h->vhl, 3 * nn);
+    ALLOC(h->ahl, 3 * nn);
+    ALLOC(h->minv2, nn);
     ALLOC(h->fe, 12 * ne);
-    ALLOC(h->fe32, 12 * ne);
+    ALLOC(h->fe32, 16 * ne);
+    ALLOC(h->slot, ne);
     ALLOC(h->node_ptr, nn + 1);
     ALLOC(h->node_inc, 4 * ne);
     ALLOC(h->ctrl, 2);
@@ -514,6 +527,7 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     UP(h->X.p, mesh->X, sizeof(double) * 3 * nn);
     UP(h->node_ptr.p, ptr.data(), sizeof(int) * (nn + 1));
     UP(h->node_inc.p, inc.data(), sizeof(int) * 4 * ne);
+    UP(h->slot.p, slots.data(), sizeof(int4) * ne);
     if (h->mat.p) UP(h->mat.p, mids.data(), ne);
 #undef UP
     cudaMemsetAsync(h->u.p, 0, sizeof(double) * 3 * nn, s);
@@ -523,6 +537,7 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     h->P.mat = h->mat.p;
     launch_setup_elements(h->P, h->X.p, s);
     launch_setup_mass(h->P, h->mass.p, h->minv.p, s);
+    launch_minv_split(h->minv.p, h->minv2.p, nn, s);
     if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
         return bail(fail(MSX_ERR_CUDA, "set-up kernels failed"));
     if ((st = upload_bcs(h, bcs, num_bcs)) != MSX_OK) return bail(st);
@@ -536,11 +551,11 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     if (!h) return MSX_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->graph) cudaGraphExecDestroy(h->graph);
-    DBuf<int4> *b4[] = {&h->conn};
+    DBuf<int4> *b4[] = {&h->conn, &h->slot};
     for (auto *b : b4) b->release();
     for (auto *b : {&h->G, &h->wJ, &h->Lref, &h->X, &h->u, &h->v, &h->a, &h->mass, &h->minv, &h->fe}) b->release();
     for (auto *b : {&h->G32, &h->wJ32, &h->Lref32, &h->Eref32, &h->fe32}) b->release();
-    h->uhl.release();
+    for (auto *b : {&h->uhl, &h->vhl, &h->ahl, &h->minv2}) b->release();
     h->mat.release();
     for (auto *b : {&h->node_ptr, &h->node_inc, &h->node_bc, &h->flags}) b->release();
     h->bc_rec.release();
@@ -649,6 +664,7 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
             if (h->h_ctrl[(k - 1) & 1].stop) break;
         }
     }
+    if (h->precision == MSX_PREC_MIXED) launch_state_merge(h->P, h->stream);   // u, v, a for the caller
     MSX_CUDA(cudaEventRecord(h->ev1, h->stream));
     MSX_CUDA(cudaStreamSynchronize(h->stream));
     Ctrl fin = h->h_ctrl[k & 1];
@@ -721,8 +737,15 @@ extern "C" msx_status msx_internal_force(msx_handle *h, const double *u, double 
     Problem P = h->P;
     P.u = du.p;
     cudaMemcpyAsync(du.p, u, bytes, cudaMemcpyHostToDevice, h->stream);
+    DBuf<float2> uh;   // the mixed kernel reads u as (hi, lo) pairs; the block's own stay untouched
     if (h->precision == MSX_PREC_MIXED) {
+        if (uh.alloc(3 * h->P.nn) != cudaSuccess) {
+            du.release();
+            df.release();
+            return fail(MSX_ERR_OOM, "scratch for internal force");
+        }
         long long n = 3 * P.nn;
+        P.uhl = uh.p;
         split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(du.p, P.uhl, n);
     }
     if (h->precision == MSX_PREC_FP64_EXACT) launch_internal_force_exact(P, df.p, h->stream);
@@ -732,13 +755,8 @@ extern "C" msx_status msx_internal_force(msx_handle *h, const double *u, double 
     cudaError_t err = cudaStreamSynchronize(h->stream);
     du.release();
     df.release();
+    uh.release();
     if (err != cudaSuccess) return fail(MSX_ERR_CUDA, cudaGetErrorString(err));
-    if (h->precision == MSX_PREC_MIXED) {
-        // the split above overwrote the mixed kernel's copy of u: rebuild it
-        long long n = 3 * P.nn;
-        split_kernel<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(h->u.p, h->uhl.p, n);
-        MSX_CUDA(cudaStreamSynchronize(h->stream));
-    }
     return MSX_OK;
 }
 
@@ -782,6 +800,7 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
             h->elem(h->P, parity, h->stream);
         cudaEventRecord(ev[3 * i + 2], h->stream);
     }
+    if (h->precision == MSX_PREC_MIXED) launch_state_merge(h->P, h->stream);
     cudaError_t err = cudaStreamSynchronize(h->stream);
     double tn = 0, te = 0;
     for (long long i = 0; i < n; i++) {
