@@ -53,9 +53,9 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profiled(key):
-    """A per-element figure of the FP64 element kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "element_kernel_fp64_cube.md")
+def profiled(key, name="element_kernel_fp64_cube.md"):
+    """A per-element figure of an element kernel from its committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(path):
             if line.startswith(key + ":"):
@@ -124,6 +124,20 @@ def run_variant(X, conn, bcs, precision, steps, warmup, device):
     prof = S.profile(6)
     S.close()
     return rep, prof, ck.summary()
+
+
+def mixed_roofline(ne, nn, prof, ms_per_step):
+    """HBM roofline of the mixed step: per element conn 16 + FP32 dphi/dX 48 + wJ 4 + length 4
+    = 72 B, per node 176 B as in the FP64 step."""
+    peak, peak_kind = peaks()
+    alg_elem, alg_step = 72.0 * ne, 72.0 * ne + 176.0 * nn
+    ach = alg_elem / (prof.element_ms * 1e-3) / 1e9
+    step = alg_step / (ms_per_step * 1e-3) / 1e9
+    tr = profiled("dram_bytes_per_element", "element_kernel_mixed_cube.md")
+    return {"bound": "hbm", "kernel": "pool_elem_kernel<MIXED>", "achieved": ach, "peak": peak, "unit": "GB/s",
+            "frac": ach / peak, "peak_kind": peak_kind, "traffic": tr * ne if tr else None,
+            "alg_bytes_per_launch": alg_elem,
+            "step": {"alg_bytes": alg_step, "achieved": step, "frac": step / peak}}
 
 
 def run_e2e(X, conn, bcs, steps):
@@ -384,6 +398,8 @@ def main():
             variants[name] = {"value": ws * ne * args.steps / s2, "ms_per_step": 1e3 * s2 / args.steps,
                               "element_kernel_ms": p2.element_ms, "node_kernel_ms": p2.node_ms,
                               "clocks": c2}
+            if name == "mixed":
+                variants[name]["roofline"] = mixed_roofline(ne, nn, p2, 1e3 * s2 / args.steps)
     if not args.no_pool and args.only is None and args.cube == N_CUBE:
         variants["batched"] = batched_variant()
         variants["serving"] = [serving_variant(lam) for lam in (50, 200, 800)]
@@ -399,15 +415,21 @@ def main():
     if rank != 0:
         return
     peak, peak_kind = peaks()
-    alg_elem = 128.0 * ne + 48.0 * nn     # element data + gathered X and u per node
+    # algorithmic bytes: per element conn 16 + dphi/dX 96 + wJ 8 + reference length 8 = 128 B;
+    # per node X, u, v, a, m read and u, v, a written = 176 B
+    alg_elem = 128.0 * ne
+    alg_step = 128.0 * ne + 176.0 * nn
     achieved = alg_elem / (prof.element_ms * 1e-3) / 1e9
     tr = profiled("dram_bytes_per_element")
     ops, opk = profiled("fp64_ops_per_element"), profiled("fp64_peak_gops")
+    step_gbs = alg_step / (secs / args.steps) / 1e9
     roofline = {"bound": "hbm", "kernel": "pool_elem_kernel<FP64>", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                 "traffic": tr * ne if tr else None,
                 "alg_bytes_per_launch": alg_elem, "element_kernel_ms": prof.element_ms,
                 "node_kernel_ms": prof.node_ms,
+                "step": {"alg_bytes": alg_step, "achieved": step_gbs, "frac": step_gbs / peak,
+                         "note": "whole step (element + node kernel): 128 B per element + 176 B per node"},
                 "fp64_pipe": None if not ops else {
                     "achieved_gops": ops * ne / (prof.element_ms * 1e-3) / 1e9, "peak_gops": opk,
                     "frac": ops * ne / (prof.element_ms * 1e-3) / 1e9 / opk, "ops_per_element": ops,

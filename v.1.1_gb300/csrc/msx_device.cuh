@@ -759,6 +759,27 @@ __device__ __forceinline__ void cofactor(const double *F, double *K)
     K[8] = F[0] * F[4] - F[1] * F[3];
 }
 
+// ln J for J = det F in FP64.  For |J - 1| < 2^-7 (the usual case) the
+// series of log1p(x), x = J - 1, to x^9 by Horner's rule: truncation below
+// |x|^10/10 < 1e-22 |x|, so its error is that of the rounded coefficients,
+// about 1 ulp of ln J; x itself carries J's rounding, as log(J) does.
+// Otherwise the library log.
+__device__ __forceinline__ double log_near1(double J)
+{
+    const double x = J - 1.0;
+    if (!(fabs(x) < 0.0078125)) return log(J);
+    double q = 1.0 / 9.0;
+    q = fma(q, -x, 1.0 / 8.0);
+    q = fma(q, -x, 1.0 / 7.0);
+    q = fma(q, -x, 1.0 / 6.0);
+    q = fma(q, -x, 1.0 / 5.0);
+    q = fma(q, -x, 1.0 / 4.0);
+    q = fma(q, -x, 1.0 / 3.0);
+    q = fma(q, -x, 1.0 / 2.0);
+    q = fma(q, -x, 1.0);
+    return q * x;
+}
+
 // wJ * P written through the cofactor; the quadrature weight is folded into
 // the law's scalar coefficients instead of scaling the nine entries of P.
 __device__ __forceinline__ void stress_fast(const MatParams &m, const double *F, double wJ, double *P)
@@ -792,7 +813,7 @@ __device__ __forceinline__ void stress_fast(const MatParams &m, const double *F,
     if (m.law == 1) {
         // P = mu F + (lambda ln J - mu) F^-T
         a1 = m.mu * wJ;
-        g = (m.lambda * log(J) - m.mu) * iJ * wJ;
+        g = (m.lambda * log_near1(J) - m.mu) * iJ * wJ;
     } else {
         // P = mu J^-2/3 F + (-mu/3 trB J^-5/3 + K1 (J-1)) cof(F)
         double r = rcbrt(J);
@@ -908,7 +929,9 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
     for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = 0; j < 3; j++)
-            F[i * 3 + j] = (i == j ? 1.0 : 0.0) + (du[i] * G[j] + du[3 + i] * G[3 + j] + du[6 + i] * G[6 + j]);
+            // the identity enters the FMA chain (no separate 0 + x or 1 + x)
+            F[i * 3 + j] = fma(du[i], G[j], fma(du[3 + i], G[3 + j], i == j ? fma(du[6 + i], G[6 + j], 1.0)
+                                                                             : du[6 + i] * G[6 + j]));
     const MatParams &m = mat_of(p, e);
     stress_fast(m, F, __ldg(p.wJ + e), P);
     double f[12];
@@ -1182,7 +1205,7 @@ __global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *
 // within 2^-8 of it (and slivers) recompute the exact FP64 value, whose
 // minimum goes to the solve's CFL slot.  Mixed: the FP32 minimum itself.
 template <int MODE>
-__global__ void __launch_bounds__(kStepThreads) pool_elem_kernel(const Problem *__restrict__ descs,
+__global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : 2) pool_elem_kernel(const Problem *__restrict__ descs,
                                                                  const Tile *__restrict__ tiles,
                                                                  int *__restrict__ sched, int parity)
 {
