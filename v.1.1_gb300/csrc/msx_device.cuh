@@ -1091,6 +1091,7 @@ __device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, 
                                P[i * 3 + 2] * G[(a - 1) * 3 + 2];
 #pragma unroll
         for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
+        // one 16-byte store per corner (a padded slot) rather than three scalar ones
         const int4 sl = __ldg(p.slot + e);
         float4 *fe = reinterpret_cast<float4 *>(p.fe32);
         fe[sl.x] = make_float4(f[0], f[1], f[2], 0.f);
@@ -1098,12 +1099,26 @@ __device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, 
         fe[sl.z] = make_float4(f[6], f[7], f[8], 0.f);
         fe[sl.w] = make_float4(f[9], f[10], f[11], 0.f);
         if (!FORCE_ONLY) {
+            // reference edges X_b - X_0 = columns of G^-1 (G's rows are the
+            // gradients of shape functions 1-3): cof(G)^T / det G in FP32,
+            // instead of streaming them; only the CFL value uses them
+            float C[9];
+            C[0] = G[4] * G[8] - G[5] * G[7];
+            C[1] = G[5] * G[6] - G[3] * G[8];
+            C[2] = G[3] * G[7] - G[4] * G[6];
+            C[3] = G[2] * G[7] - G[1] * G[8];
+            C[4] = G[0] * G[8] - G[2] * G[6];
+            C[5] = G[1] * G[6] - G[0] * G[7];
+            C[6] = G[1] * G[5] - G[2] * G[4];
+            C[7] = G[2] * G[3] - G[0] * G[5];
+            C[8] = G[0] * G[4] - G[1] * G[3];
+            const float idet = 1.0f / (G[0] * C[0] + G[1] * C[1] + G[2] * C[2]);
             float e1[3], e2[3], e3[3];
 #pragma unroll
             for (int i = 0; i < 3; i++) {
-                e1[i] = __ldg(p.Eref32 + i * ne + e) + du[i];
-                e2[i] = __ldg(p.Eref32 + (3 + i) * ne + e) + du[3 + i];
-                e3[i] = __ldg(p.Eref32 + (6 + i) * ne + e) + du[6 + i];
+                e1[i] = C[i] * idet + du[i];
+                e2[i] = C[3 + i] * idet + du[3 + i];
+                e3[i] = C[6 + i] * idet + du[6 + i];
             }
             float dist = char_length_edges<float>(e1, e2, e3);
             float Lr = __ldg(p.Lref32 + e);

@@ -61,7 +61,7 @@ struct Problem {
     const double *wJ;
     const double *Lref;
     const float *G32, *wJ32, *Lref32;       // FP32 copies (mixed mode)
-    const float *Eref32;      // 9*ne reference edge vectors X_a - X_0 (mixed CFL)
+    const float *Eref32;      // 9*ne reference edge vectors X_a - X_0 (FP32 CFL screen of the FP64 mode)
     const unsigned char *mat; // per-element material id, or nullptr
     int nmat;
     MatParams mats[kMaxMats];
@@ -76,7 +76,7 @@ struct Problem {
     const float2 *minv2;      // 1/mass as an (hi, lo) pair
     // corner forces.  Reference-order mode: fe[(e*4 + a)*3 + i] (element
     // order).  FP64 and mixed modes: in the node's CSR slot k = slot[e].a,
-    // fe[k*3 + i] and fe32[k*4 + i], so a node's corner forces are contiguous.
+    // fe[k*3 + i] and fe32[k*4 + i] (16-byte slots), so a node's corner forces are contiguous.
     double *fe;
     float *fe32;
     // node -> (element, corner) incidences sorted by element id
