@@ -651,6 +651,11 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
     long long start_steps = 0;
     if ((st = arm_block(h, max_steps, &start_steps)) != MSX_OK) return st;
     Ctrl latest = h->h_ctrl[0];
+    // replays needed to reach the step limit (time may end the block sooner): the
+    // limit's last step is post-updated, and the stop raised, by one more node
+    // kernel, so room + 1 node kernels in all
+    const long long room = latest.limit - latest.step;
+    const long long needed = room >= (1LL << 61) ? (1LL << 62) : (room + 1 + h->spg - 1) / h->spg;
     MSX_CUDA(cudaEventRecord(h->ev0, h->stream));
     // two replays in flight: check the older one's control slot
     long long k = 0;
@@ -658,7 +663,7 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
         MSX_CUDA(cudaGraphLaunch(h->graph, h->stream));
         MSX_CUDA(cudaMemcpyAsync(h->h_ctrl + (k & 1), h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
         MSX_CUDA(cudaEventRecord(h->evc[k & 1], h->stream));
-        if (latest.stop) break;
+        if (latest.stop || k + 1 >= needed) break;
         if (k >= 1) {
             MSX_CUDA(cudaEventSynchronize(h->evc[(k - 1) & 1]));
             if (h->h_ctrl[(k - 1) & 1].stop) break;
