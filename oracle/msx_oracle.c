@@ -375,31 +375,193 @@ static double critical_dt(int64_t nn, int64_t ne, const double *X, const int32_t
     return best;
 }
 
-/* External force at time t, src/solvers/boundaryConditions.cpp:75-138
- * (NeumannBCManagement): nodal forces (:17-34 BCsNodalForces with
- * classNeumann::getTracAmount, classNodes.h:101-109, slope value/(tf-t0)
- * times the absolute time inside [t0, tf]) and gravity (:1146-1171 BCsGravity,
- * -w rho |J| g phi_a on the z DOF, element order), in the order of the deck. */
-static void external_force(const orc_problem *p, const double *absJ, double t, double *fext)
+/* src/mathematics/maths.cpp:1550-1557 norm2 */
+static double norm2_3(const double *a)
+{
+    double temp = 0;
+    for (int i = 0; i < 3; i++) temp += a[i] * a[i];
+    return sqrt(temp);
+}
+
+/* src/mathematics/geometry.cpp:180-190 crossProduct */
+static void cross3(const double *A, const double *B, double *C)
+{
+    C[0] = A[1] * B[2] - A[2] * B[1];
+    C[1] = A[2] * B[0] - A[0] * B[2];
+    C[2] = A[0] * B[1] - A[1] * B[0];
+}
+
+/* Face S of a tet: classLinearTetrahedra::getSubElement, classLinearTetrahedra.cpp:30-62. */
+static void tet_face(const int32_t *c, int S, int32_t *t)
+{
+    if (S == 1) { t[0] = c[0]; t[1] = c[1]; t[2] = c[2]; }
+    else if (S == 2 || S == 3) { t[0] = c[S - 2]; t[1] = c[3]; t[2] = c[S - 1]; }
+    else { t[0] = c[0]; t[1] = c[2]; t[2] = c[S - 1]; }
+}
+
+/* The face triangle's one Gauss point: weight * |J| and phi.
+ * classLinearTriangles::defineGPs (classLinearTriangles.cpp:194-290) with
+ * GPsTriangle2DValues order 1 (GPsDistribution.cpp:149-155), the local basis of
+ * createOrthogonalBasisOnPlane (geometry.cpp:363-390), vectorArithmetic
+ * (maths.cpp:3107-3117), multGeneralMatrices (maths.cpp:1679-1693) and the
+ * triangle's shape functions (classLinearTriangles.cpp:302-317).  xyz = the three
+ * face nodes, node-major. */
+static void face_rule(const double *xyz, double *wabsJ, double *phi)
+{
+    const double *p1 = xyz;
+    double a[3], b[3], normal[3], xhat[3], yhat[3];
+    for (int i = 0; i < 3; i++) {
+        a[i] = xyz[3 + i] + (-1.0) * p1[i];
+        b[i] = xyz[6 + i] + (-1.0) * p1[i];
+    }
+    cross3(b, a, normal);
+    cross3(a, normal, xhat);
+    double magA = norm2_3(a), magX = norm2_3(xhat);
+    for (int i = 0; i < 3; i++) {
+        yhat[i] = a[i] / magA;
+        xhat[i] = xhat[i] / magX;
+    }
+    double map[6] = {xhat[0], xhat[1], xhat[2], yhat[0], yhat[1], yhat[2]};
+    double T[9];   /* T[r*3 + k]: coordinate r of node k, offset by p1 */
+    for (int k = 0; k < 3; k++)
+        for (int r = 0; r < 3; r++) T[r * 3 + k] = xyz[k * 3 + r] + (-1.0) * p1[r];
+    double L[6];
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 3; j++) {
+            L[i * 3 + j] = 0;
+            for (int k = 0; k < 3; k++) L[i * 3 + j] += map[i * 3 + k] * T[k * 3 + j];
+        }
+    const double natDev[6] = {-1.0 - 0.0 + 0.0, -0.0 - 1.0 + 0.0, 1.0, 0.0, 0.0, 1.0};
+    double Jm[4];
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++) {
+            Jm[i * 2 + j] = 0;
+            for (int k = 0; k < 3; k++) Jm[i * 2 + j] += L[i * 3 + k] * natDev[k * 2 + j];
+        }
+    double J = Jm[0] * Jm[3] - Jm[2] * Jm[1];   /* determinantTensor, size 2 */
+    double weight = 0.5 * 1.;
+    *wabsJ = weight * fabs(J);
+    const double x = 0.33333333333333, y = 0.33333333333333;
+    phi[0] = -1.0 * x - 1.0 * y + 1.0;
+    phi[1] = 1.0 * x;
+    phi[2] = 1.0 * y;
+}
+
+/* Unit normal of the face triangle: classLinearTriangles::getn0, classLinearTriangles.cpp:19-45. */
+static void face_normal(const double *xyz, double *n0)
+{
+    const double *x1 = xyz, *x2 = xyz + 3, *x3 = xyz + 6;
+    for (int i = 0; i < 3; i++) {
+        int c1 = i == 0 ? 1 : (i == 1 ? 2 : 0), c2 = i == 0 ? 2 : (i == 1 ? 0 : 1);
+        n0[i] = (x2[c1] - x1[c1]) * (x3[c2] - x1[c2]) - (x3[c1] - x1[c1]) * (x2[c2] - x1[c2]);
+    }
+    double no = norm2_3(n0);
+    for (int i = 0; i < 3; i++) n0[i] = n0[i] / no;
+}
+
+/* Traction and pressure of one block (boundaryConditions.cpp:218-275 BCsTractionInst/Ramp,
+ * :370-505 BCsPressureRamp/Inst, classNeumannBCs.h:57-181 for the amounts).  Pressure
+ * follows the face: n = F^-T n0 with F of the bulk tet (classSpatialPoint::getF,
+ * classSpatialPoint.cpp:41-66, with the tet's dphi), force w|J| phi_a det(F) P n_i.
+ * The ramp variant takes phi and the node list of the bulk tet evaluated at natural
+ * coordinates 0 (classLinearTetrahedra::defineShapeOnAPoint, :66-121, :270-292), so
+ * phi = (1, 0, 0, 0): the face's force goes to the tet's first node. */
+static void surface_block(const orc_problem *p, const orc_load *L, const double *dphi, const double *u,
+                          double t, double *fext)
+{
+    const int64_t nn = p->nn;
+    const int ramp = L->kind == ORC_LOAD_TRACTION_RAMP || L->kind == ORC_LOAD_PRESSURE_RAMP;
+    const int pressure = L->kind == ORC_LOAD_PRESSURE_INST || L->kind == ORC_LOAD_PRESSURE_RAMP;
+    double amount[3] = {0, 0, 0};
+    if (t >= L->t0 && t <= L->tf)
+        for (int i = 0; i < (pressure ? 1 : 3); i++)
+            amount[i] = ramp ? L->value[i] / (L->tf - L->t0) * (t - L->t0) : L->value[i];
+    for (int64_t k = 0; k < L->nelems; k++) {
+        const int64_t e = L->elems[k];
+        const int32_t *c = p->conn + 4 * e;
+        int32_t tri[3];
+        tet_face(c, L->face, tri);
+        double xyz[9], wabsJ, phi[3];
+        for (int a = 0; a < 3; a++)
+            for (int i = 0; i < 3; i++) xyz[a * 3 + i] = p->X[i * nn + tri[a]];
+        face_rule(xyz, &wabsJ, phi);
+        if (!pressure) {
+            for (int a = 0; a < 3; a++)
+                for (int i = 0; i < 3; i++) fext[tri[a] + i * nn] += wabsJ * phi[a] * amount[i];
+            continue;
+        }
+        double n0[3];
+        face_normal(xyz, n0);
+        double F[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int a = 0; a < 4; a++) {
+            const double *ds = dphi + 12 * e + 3 * a;
+            double disp[3];
+            for (int i = 0; i < 3; i++) disp[i] = u[c[a] + i * nn];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) F[i * 3 + j] += ds[j] * disp[i];
+        }
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) F[i * 3 + j] += (i == j ? 1 : 0);
+        double Jac = det3(F), Fi[9], n[3] = {0, 0, 0};
+        inverse3(F, Fi);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) n[i] += Fi[j * 3 + i] * n0[j];   /* (F^-1)^T n0 */
+        if (ramp) {
+            const double phit[4] = {-1.0 * 0 - 1.0 * 0 - 1.0 * 0 + 1.0, 1.0 * 0, 1.0 * 0, 1.0 * 0};
+            for (int a = 0; a < 4; a++)
+                for (int i = 0; i < 3; i++) fext[c[a] + i * nn] += wabsJ * phit[a] * Jac * amount[0] * n[i];
+        } else {
+            for (int a = 0; a < 3; a++)
+                for (int i = 0; i < 3; i++) fext[tri[a] + i * nn] += wabsJ * phi[a] * Jac * amount[0] * n[i];
+        }
+    }
+}
+
+/* External force at displacement u and time t, src/solvers/boundaryConditions.cpp:75-138
+ * (NeumannBCManagement), block by block in the order of the deck: nodal forces
+ * (:17-34 BCsNodalForces with classNeumann::getTracAmount, classNodes.h:101-109,
+ * slope value/(tf-t0) times the absolute time inside [t0, tf]), gravity
+ * (:1146-1171 BCsGravity, -w rho |J| g phi_a on the z DOF, element order),
+ * traction and pressure (surface_block). */
+static void gravity_block(const orc_problem *p, const double *absJ, double g, double *fext)
+{
+    const double w = 0.166666666667, phi = -1.0 * 0.25 - 1.0 * 0.25 - 1.0 * 0.25 + 1.0;
+    for (int64_t e = 0; e < p->ne; e++) {
+        double rho = p->mats[p->elem_mat ? p->elem_mat[e] : 0].rho;
+        for (int a = 0; a < 4; a++) fext[p->conn[e * 4 + a] + 2 * p->nn] += -w * rho * absJ[e] * g * phi;
+    }
+}
+
+static void force_block(const orc_force *fs, int64_t n, double t, double *fext)
+{
+    for (int64_t k = 0; k < n; k++) {
+        const orc_force *f = &fs[k];
+        double m = f->value / (f->tf - f->t0);
+        double F = (t >= f->t0 && t <= f->tf) ? m * t : 0;
+        fext[f->dof] += F;
+    }
+}
+
+static void external_force(const orc_problem *p, const double *absJ, const double *dphi, const double *u,
+                           double t, double *fext)
 {
     const int64_t nn = p->nn;
     for (int64_t i = 0; i < 3 * nn; i++) fext[i] = 0;
+    if (p->nloads > 0) {
+        for (int64_t b = 0; b < p->nloads; b++) {
+            const orc_load *L = &p->loads[b];
+            if (L->kind == ORC_LOAD_FORCE) force_block(L->forces, L->nforces, t, fext);
+            else if (L->kind == ORC_LOAD_GRAVITY) { if (L->value[0] != 0) gravity_block(p, absJ, L->value[0], fext); }
+            else surface_block(p, L, dphi, u, t, fext);
+        }
+        return;
+    }
     for (int pass = 0; pass < 2; pass++) {
         int gravity_now = (pass == 0) == (p->gravity_first != 0);
         if (gravity_now) {
-            if (p->gravity == 0) continue;
-            const double w = 0.166666666667, phi = -1.0 * 0.25 - 1.0 * 0.25 - 1.0 * 0.25 + 1.0;
-            for (int64_t e = 0; e < p->ne; e++) {
-                double rho = p->mats[p->elem_mat ? p->elem_mat[e] : 0].rho;
-                for (int a = 0; a < 4; a++) fext[p->conn[e * 4 + a] + 2 * nn] += -w * rho * absJ[e] * p->gravity * phi;
-            }
+            if (p->gravity != 0) gravity_block(p, absJ, p->gravity, fext);
         } else {
-            for (int64_t k = 0; k < p->nforces; k++) {
-                const orc_force *f = &p->forces[k];
-                double m = f->value / (f->tf - f->t0);
-                double F = (t >= f->t0 && t <= f->tf) ? m * t : 0;
-                fext[f->dof] += F;
-            }
+            force_block(p->forces, p->nforces, t, fext);
         }
     }
 }
@@ -486,7 +648,7 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
             a[d] = 0.;
         }
         orc_internal_force(nn, ne, p->conn, dphi, wJ, p->elem_mat, p->mats, u, fint, 0, 0, p->nthreads);
-        external_force(p, absJ, t, fext);
+        external_force(p, absJ, dphi, u, t, fext);
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static) num_threads(p->nthreads > 0 ? p->nthreads : 1)
 #endif
@@ -513,6 +675,27 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
 done:
     free(dphi); free(wJ); free(Lref); free(cel); free(mass); free(fint);
     free(uK); free(aprev); free(cons); free(flag); free(UU); free(fext); free(absJ);
+    return rc;
+}
+
+/* External force of all Neumann blocks at displacement u and time t (test hook). */
+int orc_external_force(const orc_problem *p, const double *u, double t, double *fext)
+{
+    const int64_t nn = p->nn, ne = p->ne;
+    double *dphi = malloc(sizeof(double) * 12 * (size_t)ne), *wJ = malloc(sizeof(double) * (size_t)ne);
+    double *Lref = malloc(sizeof(double) * (size_t)ne), *absJ = malloc(sizeof(double) * (size_t)ne);
+    int rc = ORC_OK;
+    if (!dphi || !wJ || !Lref || !absJ) { rc = ORC_ERR_ARG; goto done; }
+    if ((rc = orc_precompute(nn, ne, p->X, p->conn, dphi, wJ, Lref)) != ORC_OK) goto done;
+    for (int64_t e = 0; e < ne; e++) {
+        double M[9];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) M[i * 3 + j] = p->X[i * nn + p->conn[e * 4 + j + 1]] - p->X[i * nn + p->conn[e * 4]];
+        absJ[e] = fabs(det3(M));
+    }
+    external_force(p, absJ, dphi, u, t, fext);
+done:
+    free(dphi); free(wJ); free(Lref); free(absJ);
     return rc;
 }
 

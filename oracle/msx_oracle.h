@@ -35,6 +35,18 @@ typedef struct { int32_t law; double young, nu, rho; } orc_material;
 typedef struct { int64_t dof; double t0, tf, value; } orc_force;
 typedef struct { int64_t dof; int32_t mode; int32_t ramp_steps; double value; } orc_bc;
 
+/* One Neumann block of the deck (src/solvers/boundaryConditions.cpp:75-138). */
+enum { ORC_LOAD_FORCE = 0, ORC_LOAD_GRAVITY = 1, ORC_LOAD_TRACTION_INST = 2, ORC_LOAD_TRACTION_RAMP = 3,
+       ORC_LOAD_PRESSURE_INST = 4, ORC_LOAD_PRESSURE_RAMP = 5 };
+typedef struct {
+    int32_t kind;
+    int32_t face;                 /* surface loads: face S (1..4) of every listed tet        */
+    double t0, tf;                /* surface loads: active for t0 <= t <= tf                  */
+    double value[3];              /* traction (Tx, Ty, Tz); pressure P or gravity g: value[0] */
+    const int32_t *elems; int64_t nelems;      /* surface loads: bulk tets, 0-based, deck order */
+    const orc_force *forces; int64_t nforces;  /* FORCE block: its entries, deck order          */
+} orc_load;
+
 typedef struct {
     int64_t nn, ne;
     const double *X;          /* 3*nn, X[c*nn + node]                        */
@@ -49,6 +61,8 @@ typedef struct {
     const orc_force *forces; int64_t nforces;  /* nodal forces, input order   */
     double gravity;           /* *GRAVITY g (0: none), applied on the z DOFs  */
     int32_t gravity_first;    /* 1: *GRAVITY precedes *BOUNDARY, TYPE=FORCE   */
+    const orc_load *loads; int64_t nloads;     /* when nloads > 0: all Neumann blocks in deck
+                                                  order; forces/gravity above are then unused */
 } orc_problem;
 
 typedef struct { int64_t steps; double t, dt_last, dt_init; int32_t status; double loop_seconds; } orc_result;
@@ -81,6 +95,8 @@ int orc_element_fields(int64_t nn, int64_t ne, const int32_t *conn, const double
 int orc_run(const orc_problem *p, double *u, double *v, double *a,
             double *dt_hist, int64_t max_hist, orc_result *res);
 /* Seeded cube generator: (n+1)^3 nodes, 6 n^3 tets (hex -> 6 tets). */
+/* External force of all Neumann blocks at displacement u and time t (3*nn). */
+int orc_external_force(const orc_problem *p, const double *u, double t, double *fext);
 int orc_cube_mesh(int32_t n, uint64_t seed, double jitter, double *X, int32_t *conn);
 
 #ifdef __cplusplus

@@ -37,6 +37,17 @@ class _Force(C.Structure):
     _fields_ = [("dof", C.c_int64), ("t0", C.c_double), ("tf", C.c_double), ("value", C.c_double)]
 
 
+class _Load(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("face", C.c_int32), ("t0", C.c_double), ("tf", C.c_double),
+                ("value", C.c_double * 3), ("elems", C.c_void_p), ("nelems", C.c_int64),
+                ("forces", C.c_void_p), ("nforces", C.c_int64)]
+
+
+LOAD_FORCE, LOAD_GRAVITY, LOAD_TRACTION_INST, LOAD_TRACTION_RAMP, LOAD_PRESSURE_INST, LOAD_PRESSURE_RAMP = range(6)
+_SURFACE_KINDS = {"traction_inst": LOAD_TRACTION_INST, "traction_ramp": LOAD_TRACTION_RAMP,
+                  "pressure_inst": LOAD_PRESSURE_INST, "pressure_ramp": LOAD_PRESSURE_RAMP}
+
+
 class _BC(C.Structure):
     _fields_ = [("dof", C.c_int64), ("mode", C.c_int32), ("ramp_steps", C.c_int32), ("value", C.c_double)]
 
@@ -48,7 +59,7 @@ class _Problem(C.Structure):
                 ("scale_factor", C.c_double), ("max_steps", C.c_int64),
                 ("first_step_zero_uK", C.c_int32), ("nthreads", C.c_int32),
                 ("forces", C.c_void_p), ("nforces", C.c_int64), ("gravity", C.c_double),
-                ("gravity_first", C.c_int32)]
+                ("gravity_first", C.c_int32), ("loads", C.c_void_p), ("nloads", C.c_int64)]
 
 
 class _Result(C.Structure):
@@ -82,6 +93,7 @@ def lib():
         _lib = C.CDLL(LIB_PATH)
         _lib.orc_run.argtypes = [C.POINTER(_Problem), C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p, C.c_int64, C.POINTER(_Result)]
+        _lib.orc_external_force.argtypes = [C.POINTER(_Problem), C.c_void_p, C.c_double, C.c_void_p]
         _lib.orc_cube_mesh.argtypes = [C.c_int32, C.c_uint64, C.c_double, C.c_void_p, C.c_void_p]
         _lib.orc_precompute.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_void_p]
@@ -115,8 +127,39 @@ class Material:
 @dataclass
 class Loads:
     """Neumann loads of a deck, in deck order: ("force", t0, tf, Ff, [(node, Fx, Fy, Fz), ...])
-    for *BOUNDARY, TYPE=FORCE and ("gravity", g) for *GRAVITY."""
+    for *BOUNDARY, TYPE=FORCE, ("gravity", g) for *GRAVITY,
+    ("traction_inst" | "traction_ramp", t0, tf, (Tx, Ty, Tz), S, [elem, ...]) and
+    ("pressure_inst" | "pressure_ramp", t0, tf, P, S, [elem, ...]) for *BOUNDARY,
+    TYPE=TRACTION/PRESSURE INST/RAMP on face S (1..4) of the listed tets (0-based)."""
     items: list = field(default_factory=list)
+
+    def blocks(self, nn):
+        """ctypes blocks in deck order, plus the arrays they point into (keep alive)."""
+        keep, out = [], []
+        for it in self.items:
+            L = _Load()
+            if it[0] == "force":
+                _, t0, tf, Ff, rows = it
+                ents = [(node + k * nn, t0, tf, F[k] * Ff) for node, *F in rows for k in range(3)]
+                arr = (_Force * max(1, len(ents)))(*[_Force(*e) for e in ents])
+                keep.append(arr)
+                L.kind, L.forces, L.nforces = LOAD_FORCE, C.cast(arr, C.c_void_p), len(ents)
+            elif it[0] == "gravity":
+                L.kind = LOAD_GRAVITY
+                L.value[0] = it[1]
+            else:
+                kind, t0, tf, val, S, elems = it
+                L.kind, L.t0, L.tf, L.face = _SURFACE_KINDS[kind], t0, tf, S
+                vals = (val,) if kind.startswith("pressure") else tuple(val)
+                for i, x in enumerate(vals):
+                    L.value[i] = x
+                e = np.ascontiguousarray(elems, dtype=np.int32)
+                keep.append(e)
+                L.elems, L.nelems = e.ctypes.data, len(e)
+            out.append(L)
+        arr = (_Load * max(1, len(out)))(*out)
+        keep.append(arr)
+        return arr, len(out), keep
 
     def force_entries(self, nn):
         out = []
@@ -237,6 +280,22 @@ def char_length(x: np.ndarray) -> float:
     return lib().orc_char_length(_p(x))
 
 
+def external_force(mesh: Mesh, mats, loads: Loads, u: np.ndarray, t: float) -> np.ndarray:
+    """All Neumann blocks at displacement u and time t (3*nn)."""
+    nn = mesh.nn
+    larr, nl, _keep = loads.blocks(nn)
+    X = np.ascontiguousarray(mesh.X)
+    conn = np.ascontiguousarray(mesh.conn)
+    em = None if mesh.elem_mat is None else np.ascontiguousarray(mesh.elem_mat, np.int32)
+    marr = _mats_array(mats)
+    prob = _Problem(nn, mesh.ne, _p(X), _p(conn), _p(em), C.cast(marr, C.c_void_p), len(mats),
+                    None, 0, 0.0, 1.0, 0.5, 0, 0, 1, None, 0, 0.0, 0, C.cast(larr, C.c_void_p), nl)
+    f = np.zeros(3 * nn)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    lib().orc_external_force(C.byref(prob), _p(u), C.c_double(t), _p(f))
+    return f
+
+
 def internal_force(mesh: Mesh, mats, u: np.ndarray, nthreads: int = 1):
     dphi, wJ, _ = precompute(mesh)
     nn, ne = mesh.nn, mesh.ne
@@ -318,6 +377,7 @@ def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int 
     farr = (_Force * max(1, len(fl)))()
     for i, f in enumerate(fl):
         farr[i] = _Force(*f)
+    larr, nl, _keep = loads.blocks(nn) if loads else (None, 0, None)
     for k, s in enumerate(solvers):
         barr = (_BC * max(1, len(s.bcs)))()
         for i, (dof, mode, value, ramp) in enumerate(s.bcs):
@@ -325,7 +385,8 @@ def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int 
         prob = _Problem(nn, mesh.ne, _p(X), _p(conn), _p(em), C.cast(marr, C.c_void_p), len(mats),
                         C.cast(barr, C.c_void_p), len(s.bcs), s.t0, s.tf, s.scale_factor, s.max_steps,
                         0, nthreads, C.cast(farr, C.c_void_p), len(fl),
-                        loads.gravity() if loads else 0.0, loads.gravity_first() if loads else 0)
+                        loads.gravity() if loads else 0.0, loads.gravity_first() if loads else 0,
+                        C.cast(larr, C.c_void_p) if nl else None, nl)
         hist = np.zeros(max(1, max_hist))
         rc = lib().orc_run(C.byref(prob), _p(u), _p(v), _p(a), _p(hist), max_hist, C.byref(res))
         total += res.steps
@@ -358,8 +419,15 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Load
             _, t0, tf, Ff, rows = it
             lines += ["*BOUNDARY, TYPE=FORCE", "%.17g, %.17g, %.17g" % (t0, tf, Ff)]
             lines += ["%d, %.17g, %.17g, %.17g" % (node + 1, F0, F1, F2) for node, F0, F1, F2 in rows]
-        else:
+        elif it[0] == "gravity":
             lines += ["*GRAVITY", "%.17g" % it[1]]
+        else:
+            kind, t0, tf, val, S, elems = it
+            name = kind.split("_")[0].upper() + " " + kind.split("_")[1].upper()
+            vals = (val,) if kind.startswith("pressure") else tuple(val)
+            lines += ["*BOUNDARY, TYPE=" + name,
+                      ", ".join("%.17g" % x for x in (t0, tf) + vals) + ", %d" % S]
+            lines += ["%d" % (int(e) + 1) for e in elems]
     for s in solvers:
         if any(b[1] == BC_VEL_RAMP for b in s.bcs):
             raise ValueError("the reference has no velocity-ramp boundary condition")

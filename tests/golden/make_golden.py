@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder from the reference MuPhiSim.
 
 Run in a container where the reference sources are mounted:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 It compiles the reference in place behind our PETSc/MPI shim (oracle/Makefile),
 runs each case below through the reference's own input-deck reader and
 explicit solver, and stores the inputs and the reference's final u, v, a
@@ -35,6 +35,25 @@ def tet12_mesh(ref_src):
     return O.Mesh(X, np.array(elems, np.int32))
 
 
+def tet_face(c, S):
+    """Nodes of face S (1..4) of a tet, as classLinearTetrahedra::getSubElement orders them."""
+    if S == 1:
+        return (c[0], c[1], c[2])
+    if S in (2, 3):
+        return (c[S - 2], c[3], c[S - 1])
+    return (c[0], c[2], c[S - 1])
+
+
+def plane_faces(mesh, coord, value):
+    """[(S, [elems])] of the tet faces lying on the plane X[coord] == value, by face index."""
+    out = {}
+    for e in range(mesh.ne):
+        for S in range(1, 5):
+            if all(abs(mesh.X[coord, n] - value) < 1e-12 for n in tet_face(mesh.conn[e], S)):
+                out.setdefault(S, []).append(e)
+    return sorted(out.items())
+
+
 def cases(ref_src):
     cnh, nh, stvk = O.COMPRESSIBLE_NH, O.NEO_HOOKEAN, O.STVK
     out = {}
@@ -63,6 +82,20 @@ def cases(ref_src):
                                       O.Loads([forces, ("gravity", 9.81)]))
     out["cube3_nh_gravity_force"] = (m3, [O.Material(nh)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.0))],
                                      O.Loads([("gravity", 9.81), forces]))
+    # surface loads: traction on the top face, pressure on the x = 1 face
+    top3, side3 = plane_faces(m3, 2, 1.0), plane_faces(m3, 0, 1.0)
+    out["cube3_cnh_traction_pressure"] = (
+        m3, [O.Material(cnh)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.0))],
+        O.Loads([("traction_ramp", 0.0, 0.015, (1e3, -2e3, 4e3), S, el) for S, el in top3] +
+                [("pressure_inst", 0.0, 0.02, 5e3, S, el) for S, el in side3]))
+    out["cube3_nh_loads_mixed"] = (
+        m3, [O.Material(nh)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.0))],
+        O.Loads([("gravity", 9.81)] + [("pressure_ramp", 0.0, 0.02, 5e3, S, el) for S, el in side3] +
+                [forces] + [("traction_inst", 0.002, 0.012, (0.0, 0.0, -2e3), S, el) for S, el in top3]))
+    side4 = plane_faces(m4, 0, 1.0)
+    out["cube4_stvk_pressure_ramp"] = (
+        m4, [O.Material(stvk)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(4, 0.001))],
+        O.Loads([("pressure_ramp", 0.0, 0.02, 8e3, S, el) for S, el in side4]))
     m10 = O.cube_mesh(10)
     for name, law in (("cnh", cnh), ("nh", nh), ("stvk", stvk)):
         out["cube10_%s_S" % name] = (m10, [O.Material(law)], [O.Solver(0.0, 0.5, 0.5, O.cube_bcs(10, 0.05))])
@@ -92,7 +125,10 @@ def main():
     O.build()
     if O.build_reference() is None:
         raise SystemExit("reference sources not found at " + ref_src)
+    only = set(sys.argv[1:])   # optional case names: regenerate just those
     for name, case in cases(ref_src).items():
+        if only and name not in only:
+            continue
         mesh, mats, solvers = case[:3]
         loads = case[3] if len(case) > 3 else None
         ref = O.run_reference(mesh, mats, solvers, loads=loads)

@@ -33,5 +33,13 @@ def load_loads(name):
     d = np.load(os.path.join(GOLDEN, name + ".npz"))
     if "loads_json" not in d:
         return None
-    return O.Loads([tuple(it) if it[0] == "gravity" else (it[0], it[1], it[2], it[3], [tuple(r) for r in it[4]])
-                    for it in json.loads(str(d["loads_json"]))])
+    return O.Loads([_item(it) for it in json.loads(str(d["loads_json"]))])
+
+
+def _item(it):
+    if it[0] == "gravity":
+        return tuple(it)
+    if it[0] == "force":
+        return (it[0], it[1], it[2], it[3], [tuple(r) for r in it[4]])
+    kind, t0, tf, val, S, elems = it
+    return (kind, t0, tf, val if kind.startswith("pressure") else tuple(val), int(S), [int(e) for e in elems])

@@ -87,3 +87,53 @@ def test_oracle_output_fields_match_reference_vtk(name):
     for mine, ref in ((cau.reshape(-1, 9), d["vtk_cauchy"]), (E.reshape(-1, 9), d["vtk_E"]), (vms, d["vtk_vms"])):
         scale = max(np.abs(ref).max(), 1e-300)
         assert np.all(np.abs(mine - ref) <= 6e-6 * np.abs(ref) + 1e-6 * scale)
+
+
+def _plane_faces(mesh, coord, value):
+    import golden.make_golden as G   # noqa: E402  (face numbering helper of the fixture generator)
+    return G.plane_faces(mesh, coord, value)
+
+
+def test_surface_traction_totals_traction_times_area():
+    m = O.cube_mesh(4)
+    T = (1.5e3, -2e3, 3e3)
+    loads = O.Loads([("traction_inst", 0.0, 1.0, T, S, el) for S, el in _plane_faces(m, 2, 1.0)])
+    f = O.external_force(m, [O.Material()], loads, np.zeros(3 * m.nn), 0.5).reshape(3, -1)
+    # one-point rule: each face node gets area/3 of the traction; the top face has area 1
+    assert np.allclose(f.sum(axis=1), T, rtol=1e-12)
+    # outside the window nothing is applied
+    f2 = O.external_force(m, [O.Material()], loads, np.zeros(3 * m.nn), 1.5)
+    assert not f2.any()
+
+
+def test_surface_pressure_at_rest_is_p_area_normal():
+    m = O.cube_mesh(3)
+    P = 4e3
+    faces = _plane_faces(m, 0, 1.0)
+    inst = O.Loads([("pressure_inst", 0.0, 1.0, P, S, el) for S, el in faces])
+    f = O.external_force(m, [O.Material()], inst, np.zeros(3 * m.nn), 0.25).reshape(3, -1)
+    # F = I: the force is P A n0 with n0 the face's unit normal (+-x on the x = 1 face)
+    total = f.sum(axis=1)
+    assert abs(abs(total[0]) - P) < 1e-9 * P and np.abs(total[1:]).max() < 1e-9 * P
+    # a follower load: a rigid rotation of the body rotates the force with it
+    th = 0.2
+    R = np.array([[np.cos(th), -np.sin(th), 0], [np.sin(th), np.cos(th), 0], [0, 0, 1]])
+    u = (R @ m.X - m.X).reshape(-1)
+    fr = O.external_force(m, [O.Material()], inst, u, 0.25).reshape(3, -1)
+    assert np.allclose(fr.sum(axis=1), R @ total, rtol=1e-10, atol=1e-9 * P)
+
+
+def test_surface_pressure_ramp_loads_first_tet_node():
+    # the reference's ramp variant evaluates the bulk tet's shape functions at natural
+    # coordinates 0: phi = (1, 0, 0, 0), the face force goes to the tet's first node
+    m = O.cube_mesh(3)
+    faces = _plane_faces(m, 0, 1.0)
+    ramp = O.Loads([("pressure_ramp", 0.0, 1.0, 4e3, S, el) for S, el in faces])
+    f = O.external_force(m, [O.Material()], ramp, np.zeros(3 * m.nn), 1.0).reshape(3, -1)
+    loaded = set(np.nonzero(np.abs(f).sum(axis=0))[0])
+    firsts = {int(m.conn[e][0]) for _, el in faces for e in el}
+    assert loaded and loaded <= firsts
+    # at t = tf the ramp has reached P: same total as the instantaneous load
+    inst = O.Loads([("pressure_inst", 0.0, 1.0, 4e3, S, el) for S, el in faces])
+    fi = O.external_force(m, [O.Material()], inst, np.zeros(3 * m.nn), 1.0).reshape(3, -1)
+    assert np.allclose(f.sum(axis=1), fi.sum(axis=1), rtol=1e-12, atol=1e-9)
