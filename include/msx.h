@@ -138,6 +138,38 @@ typedef struct {
 msx_status msx_set_loads(msx_handle *h, const msx_nodal_force *forces, int64_t num_forces, double gravity,
                          int32_t gravity_first);
 
+/* One Neumann block of the deck, for msx_set_load_blocks.  Replaces the
+ * reference's classNeumannBCs list (solvers/classNeumannBCs.h:32-181) as built
+ * by NeumannCommonManagement (IO/inputFile.cpp:4705-4760) and applied by
+ * NeumannBCManagement (solvers/boundaryConditions.cpp:75-138). */
+typedef enum {
+    MSX_LOAD_FORCE = 0,          /* *BOUNDARY, TYPE=FORCE: `forces` (value = F_k * Ff)        */
+    MSX_LOAD_GRAVITY = 1,        /* *GRAVITY g = value[0]                                      */
+    MSX_LOAD_TRACTION_INST = 2,  /* *BOUNDARY, TYPE=TRACTION INST: t0, tf, Tx, Ty, Tz, S       */
+    MSX_LOAD_TRACTION_RAMP = 3,  /* *BOUNDARY, TYPE=TRACTION RAMP: T (t - t0)/(tf - t0)        */
+    MSX_LOAD_PRESSURE_INST = 4,  /* *BOUNDARY, TYPE=PRESSURE INST: t0, tf, P, S; follower load */
+    MSX_LOAD_PRESSURE_RAMP = 5   /* *BOUNDARY, TYPE=PRESSURE RAMP: P (t - t0)/(tf - t0)        */
+} msx_load_kind;
+
+typedef struct {
+    int32_t kind;                       /* msx_load_kind */
+    int32_t face;                       /* traction/pressure: face S (1..4) of every listed tet */
+    double t0, tf;                      /* traction/pressure: active for t0 <= t <= tf          */
+    double value[3];                    /* traction (Tx, Ty, Tz); pressure P, gravity g: [0]    */
+    const int32_t *elems;               /* traction/pressure: bulk tets, 0-based, deck order    */
+    int64_t num_elems;
+    const msx_nodal_force *forces;      /* FORCE: entries, deck order                           */
+    int64_t num_forces;
+} msx_load_block;
+
+/* All Neumann loads as blocks in deck order: each DOF's external force is
+ * summed block by block in that order, as the reference sums it.  Pressure
+ * follows the deformation (J F^-T n0 of the face's tet at the step's u);
+ * a ramped pressure loads the tet's first node, as the reference does
+ * (boundaryConditions.cpp:370-452).  Replaces any loads set before (by either
+ * call); takes effect from the next step. */
+msx_status msx_set_load_blocks(msx_handle *h, const msx_load_block *blocks, int64_t num_blocks);
+
 msx_status msx_destroy(msx_handle *h);
 
 /* Message of the last failing call on this host thread. */

@@ -47,6 +47,21 @@ def test_parse_summary(tmp_path, name):
         assert (blk["t0"], blk["tf"], blk["sf"], blk["bcs"]) == (s.t0, s.tf, s.scale_factor, len(s.bcs))
 
 
+@pytest.mark.parametrize("name", ["cube3_cnh_traction_pressure", "cube3_nh_loads_mixed", "cube4_stvk_pressure_ramp"])
+def test_parse_surface_load_blocks(tmp_path, name):
+    mesh, _, _, _, _ = write(tmp_path, name)
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-parse-only"],
+                       capture_output=True, text=True, check=True)
+    d = json.loads(r.stdout)
+    items = load_loads(name).items
+    assert [b["kind"] for b in d["loads"]] == [it[0].replace("_", " ").upper() for it in items]
+    for b, it in zip(d["loads"], items):
+        if it[0] in ("traction_inst", "traction_ramp", "pressure_inst", "pressure_ramp"):
+            assert b["face"] == it[4] and b["elements"] == len(it[5])
+        elif it[0] == "force":
+            assert b["entries"] == 3 * len(it[4])
+
+
 def test_rejects_out_of_scope_keywords(tmp_path):
     mesh, mats, solvers, _, _ = write(tmp_path, "cube3_cnh_ramp")
     p = tmp_path / "deck.inp"

@@ -31,7 +31,7 @@ def run_case(name, precision, spg=0):
                    elem_material=mesh.elem_mat, steps_per_graph=spg)
     L = load_loads(name)
     if L is not None:
-        S.set_loads(L.force_entries(mesh.nn), L.gravity(), L.gravity_first())
+        S.set_load_blocks(L.items)
     total = S.run().steps
     for s in solvers[1:]:
         S.next_solver(s.bcs, s.t0, s.tf, s.scale_factor, precision=precision, steps_per_graph=spg)
@@ -171,3 +171,35 @@ def test_element_fields_match_oracle(name):
     oc, oE, ov = O.element_fields(mesh, mats, u)
     for x, y in ((cau, oc), (E, oE), (vms, ov)):
         assert rel(x, y) <= 1e-12, rel(x, y)
+
+
+@pytest.mark.parametrize("name", ["cube3_cnh_force_gravity", "cube3_nh_gravity_force"])
+def test_force_gravity_wrapper_equals_blocks(name):
+    """msx_set_loads (forces + gravity) is the two-block case of msx_set_load_blocks."""
+    mesh, mats, solvers, ref, steps = load(name)
+    L = load_loads(name)
+    m = [(x.law, x.young, x.nu, x.rho) for x in mats]
+    s0 = solvers[0]
+    out = []
+    for use_blocks in (False, True):
+        S = msx.Solver(mesh.X, mesh.conn, m, s0.bcs, s0.t0, s0.tf, s0.scale_factor, precision=msx.FP64_EXACT)
+        if use_blocks:
+            S.set_load_blocks(L.items)
+        else:
+            S.set_loads(L.force_entries(mesh.nn), L.gravity(), L.gravity_first())
+        S.run()
+        out.append(S.state())
+        S.close()
+    assert all(np.array_equal(x, y) for x, y in zip(*out))
+
+
+def test_surface_load_errors():
+    X, conn = msx.mesh_cube(2)
+    S = msx.Solver(X, conn, [(msx.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0)], msx.cube_bcs(2, 0.0), 0.0, 0.01, 0.5)
+    with pytest.raises(msx.MsxError):
+        S.set_load_blocks([("pressure_inst", 0.0, 1.0, 1e3, 5, [0])])        # face 1..4 only
+    with pytest.raises(msx.MsxError):
+        S.set_load_blocks([("traction_inst", 0.0, 1.0, (1, 2, 3), 1, [len(conn)])])   # element range
+    with pytest.raises(msx.MsxError):
+        S.set_load_blocks([("pressure_ramp", 0.5, 0.5, 1e3, 1, [0])])        # ramp needs tf != t0
+    S.close()

@@ -44,9 +44,15 @@ struct SolverBlock {
 struct Deck {
     std::vector<double> xyz;          // node-major while reading
     struct Force { long long node; int comp; double t0, tf, value; };
-    std::vector<Force> forces;        // *BOUNDARY, TYPE=FORCE entries in deck order
-    double gravity = 0;
-    int gravity_first = 0;
+    // Neumann blocks in deck order (the reference's NeumannBCs list)
+    struct Load {
+        int kind;                     // MSX_LOAD_*
+        int face = 0;
+        double t0 = 0, tf = 0, value[3] = {0, 0, 0};
+        std::vector<Force> forces;    // FORCE entries
+        std::vector<int32_t> elems;   // traction / pressure: bulk tets, 0-based
+    };
+    std::vector<Load> loads;
     std::vector<int32_t> conn;
     std::vector<msx_material> mats;
     std::vector<int32_t> elem_mat;    // -1 until assigned
@@ -111,17 +117,41 @@ Deck parse(const std::string &path)
             auto h = split(lines[i + 1]);
             if (h.size() != 3) die("a force block starts with t0, tf, Ff", (int)i + 2);
             double t0 = atof(h[0].c_str()), tf = atof(h[1].c_str()), Ff = atof(h[2].c_str());
+            Deck::Load B;
+            B.kind = MSX_LOAD_FORCE;
             for (i += 2; data_line(i); i++) {
                 auto f = split(lines[i]);
                 if (f.size() != 4) die("a force line has node, Fx, Fy, Fz", (int)i + 1);
                 long long node = atoll(f[0].c_str()) - 1;
                 if (node < 0 || node >= (long long)d.xyz.size() / 3) die("force node out of range", (int)i + 1);
-                for (int c = 0; c < 3; c++) d.forces.push_back({node, c, t0, tf, atof(f[c + 1].c_str()) * Ff});
+                for (int c = 0; c < 3; c++) B.forces.push_back({node, c, t0, tf, atof(f[c + 1].c_str()) * Ff});
             }
+            d.loads.push_back(B);
+        } else if (starts(L, "*BOUNDARY, TYPE=TRACTION RAMP") || starts(L, "*BOUNDARY, TYPE=TRACTION INST") ||
+                   starts(L, "*BOUNDARY, TYPE=PRESSURE RAMP") || starts(L, "*BOUNDARY, TYPE=PRESSURE INST")) {
+            // src/IO/inputFile.cpp:3229-3700: "t0, tf, Tx, Ty, Tz, S" (traction) or
+            // "t0, tf, P, S" (pressure), then one bulk element per line; face S of each
+            const bool pressure = L.find("PRESSURE") != std::string::npos, ramp = L.find("RAMP") != std::string::npos;
+            Deck::Load B;
+            B.kind = pressure ? (ramp ? MSX_LOAD_PRESSURE_RAMP : MSX_LOAD_PRESSURE_INST)
+                              : (ramp ? MSX_LOAD_TRACTION_RAMP : MSX_LOAD_TRACTION_INST);
+            auto h = split(lines[i + 1]);
+            const size_t nv = pressure ? 1 : 3;
+            if (h.size() != nv + 3) die(pressure ? "a pressure block starts with t0, tf, P, S"
+                                                 : "a traction block starts with t0, tf, Tx, Ty, Tz, S", (int)i + 2);
+            B.t0 = atof(h[0].c_str());
+            B.tf = atof(h[1].c_str());
+            for (size_t k = 0; k < nv; k++) B.value[k] = atof(h[2 + k].c_str());
+            B.face = (int)atof(h[2 + nv].c_str());
+            if (B.face < 1 || B.face > 4) die("the face of a C3D4 surface load is 1..4", (int)i + 2);
+            for (i += 2; data_line(i); i++) B.elems.push_back(atoi(lines[i].c_str()) - 1);
+            d.loads.push_back(B);
         } else if (starts(L, "*GRAVITY")) {
             // src/IO/inputFile.cpp:4723-4735
-            d.gravity = atof(lines[i + 1].c_str());
-            if (d.forces.empty()) d.gravity_first = 1;
+            Deck::Load B;
+            B.kind = MSX_LOAD_GRAVITY;
+            B.value[0] = atof(lines[i + 1].c_str());
+            d.loads.push_back(B);
             i += 2;
         } else if (starts(L, "*FEM Nodes") || starts(L, "*FEM Elements")) {
             if (i + 1 >= n || !starts(lines[i + 1], "All")) die("only 'All' FEM sets are supported", ln);
@@ -326,8 +356,24 @@ int main(int argc, char **argv)
         for (auto &s : d.solvers) nbc += s.bcs.size();
         printf("{\"nodes\": %lld, \"elements\": %lld, \"materials\": %zu, \"solvers\": %zu, \"bcs\": %zu",
                nn, ne, d.mats.size(), d.solvers.size(), nbc);
-        printf(", \"forces\": %zu, \"gravity\": %.17g, \"gravity_first\": %d", d.forces.size(), d.gravity,
-               d.gravity_first);
+        size_t nforces = 0;
+        double gravity = 0;
+        int gravity_first = 0;
+        for (const auto &B : d.loads) {
+            if (B.kind == MSX_LOAD_FORCE) nforces += B.forces.size();
+            if (B.kind == MSX_LOAD_GRAVITY) {
+                if (nforces == 0 && gravity == 0) gravity_first = 1;
+                gravity = B.value[0];
+            }
+        }
+        printf(", \"forces\": %zu, \"gravity\": %.17g, \"gravity_first\": %d", nforces, gravity, gravity_first);
+        static const char *names[] = {"FORCE", "GRAVITY", "TRACTION INST", "TRACTION RAMP", "PRESSURE INST",
+                                      "PRESSURE RAMP"};
+        printf(", \"loads\": [");
+        for (size_t k = 0; k < d.loads.size(); k++)
+            printf("%s{\"kind\": \"%s\", \"face\": %d, \"elements\": %zu, \"entries\": %zu}", k ? ", " : "",
+                   names[d.loads[k].kind], d.loads[k].face, d.loads[k].elems.size(), d.loads[k].forces.size());
+        printf("]");
         printf(", \"blocks\": [");
         for (size_t k = 0; k < d.solvers.size(); k++)
             printf("%s{\"t0\": %.17g, \"tf\": %.17g, \"sf\": %.17g, \"bcs\": %zu, \"inst\": %d}", k ? ", " : "",
@@ -346,10 +392,17 @@ int main(int argc, char **argv)
         msx_status st;
         if (k == 0) {
             st = msx_create(&mesh, d.mats.data(), (int32_t)d.mats.size(), s.bcs.data(), (int64_t)s.bcs.size(), &o, &h);
-            if (st == MSX_OK && (!d.forces.empty() || d.gravity != 0)) {
-                std::vector<msx_nodal_force> nf;
-                for (const auto &f : d.forces) nf.push_back({f.node + f.comp * nn, f.t0, f.tf, f.value});
-                st = msx_set_loads(h, nf.data(), (int64_t)nf.size(), d.gravity, d.gravity_first);
+            if (st == MSX_OK && !d.loads.empty()) {
+                std::vector<std::vector<msx_nodal_force>> nf(d.loads.size());
+                std::vector<msx_load_block> blocks(d.loads.size());
+                for (size_t k = 0; k < d.loads.size(); k++) {
+                    const Deck::Load &B = d.loads[k];
+                    for (const auto &f : B.forces) nf[k].push_back({f.node + f.comp * nn, f.t0, f.tf, f.value});
+                    blocks[k] = msx_load_block{B.kind, B.face, B.t0, B.tf, {B.value[0], B.value[1], B.value[2]},
+                                               B.elems.data(), (int64_t)B.elems.size(), nf[k].data(),
+                                               (int64_t)nf[k].size()};
+                }
+                st = msx_set_load_blocks(h, blocks.data(), (int64_t)blocks.size());
             }
         } else {
             // src/main.cpp:171-179: time continuity between solvers

@@ -271,28 +271,29 @@ __device__ __forceinline__ void node_bc_records(const Problem &p, long long i, i
     }
 }
 
-// External force of node i for the step being completed, in the deck's order
-// of the Neumann blocks (boundaryConditions.cpp:75-138): gravity sums start
-// from zero, nodal forces add m t inside their window.
-__device__ __forceinline__ void external_force(const Problem &p, long long i, double t, double *fx)
+// External force of DOF d at time t (the step being completed): its terms in
+// deck order, summed from 0 as NeumannBCManagement fills the force vector
+// (boundaryConditions.cpp:75-138; nodal forces m t inside [t0, tf],
+// classNodes.h:101-109).
+__device__ __forceinline__ double ext_force_dof(const Problem &p, long long d, double t)
 {
-    fx[0] = fx[1] = fx[2] = 0.0;
-    if (!p.grav_n && !p.node_nf) return;
-    const int rf = p.node_nf ? p.node_nf[i] : -1;
-    if (p.grav_n && (p.gravity_first || rf < 0)) fx[2] = p.grav_n[i];
-    if (rf >= 0) {
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            int2 r = p.nf_rec[rf * 3 + c];
-            for (int k = r.x; k < r.x + r.y; k++) {
-                const ForceEntry f = p.nfs[k];
-                double F = (t >= f.t0 && t <= f.tf) ? f.m * t : 0;
-                fx[c] += F;
-            }
+    double fx = 0.0;
+    for (int k = p.ext_ptr[d]; k < p.ext_ptr[d + 1]; k++) {
+        const unsigned term = p.ext_term[k], idx = term & ((1u << kExtIndexBits) - 1u);
+        double v;
+        switch (term >> kExtIndexBits) {
+        case EXT_FORCE: {
+            const ForceEntry f = p.nfs[idx];
+            v = (t >= f.t0 && t <= f.tf) ? f.m * t : 0;
+            break;
         }
-        if (p.grav_n && !p.gravity_first)
-            for (int k = p.node_ptr[i]; k < p.node_ptr[i + 1]; k++) fx[2] += p.grav_e[p.node_inc[k] >> 2];
+        case EXT_GRAV_ELEM: v = p.grav_e[idx]; break;
+        case EXT_GRAV_NODE: v = p.grav_n[idx]; break;
+        default: v = p.fcon[idx]; break;
+        }
+        fx += v;
     }
+    return fx;
 }
 
 // One DOF: post-update of step n-1 with the gathered internal force s and
@@ -365,7 +366,8 @@ __device__ __forceinline__ void node_body(const Problem &p, long long i, const C
         }
     }
     double fx[3] = {0.0, 0.0, 0.0};
-    if (cp.ran) external_force(p, i, cp.t, fx);
+    if (cp.ran && p.ext_ptr)
+        for (int c = 0; c < 3; c++) fx[c] = ext_force_dof(p, i + c * p.nn, cp.t);
     const double mass = MODE == MODE_EXACT ? p.mass[i] : 0.0, minv = MODE == MODE_EXACT ? 0.0 : p.minv[i];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
@@ -463,7 +465,7 @@ __device__ __forceinline__ void node_step(const Problem &p, int parity, NodeStep
         ns.dtn2 = df_from(ns.dtn);
         ns.hdtn2 = df_from(ns.hdtn);
     }
-    ns.loads = p.grav_n || p.node_nf;
+    ns.loads = p.ext_ptr != nullptr;
 }
 
 // Node kernel bodies of the tiled FP64 and mixed kernels: four lanes per node.
@@ -482,9 +484,7 @@ __device__ __forceinline__ T pick3(int c, T a, T b, T d) { return c == 0 ? a : (
 
 __device__ __forceinline__ double node_fext(const Problem &p, long long i, int q, const NodeStep &ns)
 {
-    double f3[3];
-    external_force(p, i, ns.t, f3);
-    return pick3(q, f3[0], f3[1], f3[2]);
+    return ext_force_dof(p, i + (long long)q * p.nn, ns.t);
 }
 
 __device__ __forceinline__ void node_quad_fp64(const Problem &p, long long i, bool valid, const NodeStep &ns)
@@ -1362,6 +1362,67 @@ __global__ void setup_gravity_node_kernel(Problem p, const double *grav_e, doubl
     double s = 0;
     for (int k = p.node_ptr[i]; k < p.node_ptr[i + 1]; k++) s += grav_e[p.node_inc[k] >> 2];
     grav_n[i] = s;
+}
+
+// Contributions of the traction and pressure faces for the step whose control
+// slot `parity` the node kernel just wrote, at that step's time and
+// displacement, in the reference's operation order (boundaryConditions.cpp:
+// 218-275 BCsTractionInst/Ramp, :370-505 BCsPressureRamp/Inst; amounts from
+// classNeumannBCs.h:57-181).  Pressure follows the face: n = F^-T n0 with F of
+// the bulk tet by classSpatialPoint::getF (classSpatialPoint.cpp:41-66):
+// F_ij = 0 + sum_a dphi_aj u_ai (corner order) + delta_ij.
+__global__ void face_load_kernel(Problem p, int parity, bool mixed)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= p.nfaces) return;
+    const Ctrl c = p.ctrl[parity];
+    if (!c.ran) return;
+    const double t = c.t;
+    const FaceLoad L = p.faces[f];
+    const bool ramp = L.kind == MSX_LOAD_TRACTION_RAMP || L.kind == MSX_LOAD_PRESSURE_RAMP;
+    const bool pressure = L.kind == MSX_LOAD_PRESSURE_INST || L.kind == MSX_LOAD_PRESSURE_RAMP;
+    double amount[3] = {0.0, 0.0, 0.0};
+    if (t >= L.t0 && t <= L.tf)
+        for (int i = 0; i < (pressure ? 1 : 3); i++) amount[i] = ramp ? L.value[i] / (L.tf - L.t0) * (t - L.t0) : L.value[i];
+    double *out = p.fcon + (long long)L.con * 3;
+    if (!pressure) {
+        for (int a = 0; a < 3; a++)
+            for (int i = 0; i < 3; i++) out[a * 3 + i] = L.wabsJ * L.phi[a] * amount[i];
+        return;
+    }
+    const long long nn = p.nn, ne = p.ne, e = L.tet;
+    const int4 cn = p.conn[e];
+    const int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    double dphi[12];
+    for (int a = 1; a < 4; a++)
+        for (int j = 0; j < 3; j++) dphi[a * 3 + j] = p.G[((a - 1) * 3 + j) * ne + e];
+    for (int j = 0; j < 3; j++) dphi[j] = ((-dphi[3 + j]) - dphi[6 + j]) - dphi[9 + j];
+    double F[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int a = 0; a < 4; a++) {
+        double disp[3];
+        for (int i = 0; i < 3; i++) {
+            const long long dof = nd[a] + i * nn;
+            disp[i] = mixed ? (double)p.uhl[dof].x + (double)p.uhl[dof].y : p.u[dof];
+        }
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) F[i * 3 + j] += dphi[a * 3 + j] * disp[i];
+    }
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) F[i * 3 + j] += (i == j ? 1.0 : 0.0);
+    double Fi[9], n[3];
+    const double Jac = det3_ref(F);
+    inv3_ref(F, Fi);
+    for (int i = 0; i < 3; i++) {
+        n[i] = 0;
+        for (int j = 0; j < 3; j++) n[i] += Fi[j * 3 + i] * L.n0[j];
+    }
+    if (L.kind == MSX_LOAD_PRESSURE_RAMP) {
+        // the bulk tet's shape function of its first node at natural coordinates 0 is 1
+        for (int i = 0; i < 3; i++) out[i] = L.wabsJ * 1.0 * Jac * amount[0] * n[i];
+    } else {
+        for (int a = 0; a < 3; a++)
+            for (int i = 0; i < 3; i++) out[a * 3 + i] = L.wabsJ * L.phi[a] * Jac * amount[0] * n[i];
+    }
 }
 
 // solvers.cpp:276-287 (uK == nullptr) and :296-320: element min into dtmin[slot]

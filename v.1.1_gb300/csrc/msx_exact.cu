@@ -42,6 +42,11 @@ void launch_internal_force_exact(const Problem &p, double *fint, cudaStream_t s)
     gather_kernel<MODE_EXACT><<<grid_for(p.nn, 256), 256, 0, s>>>(p, fint);
 }
 
+void launch_face_loads(const Problem &p, int parity, bool mixed, cudaStream_t s)
+{
+    if (p.nfaces > 0) face_load_kernel<<<grid_for(p.nfaces, 128), 128, 0, s>>>(p, parity, mixed);
+}
+
 void launch_setup_gravity(const Problem &p, double g, double *grav_e, double *grav_n, cudaStream_t s)
 {
     setup_gravity_elem_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, g, grav_e);

@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/msx.h"
+
 namespace msx {
 
 constexpr int kMaxMats = 16;
@@ -37,6 +39,25 @@ struct BCEntry {
 struct ForceEntry {
     double m, t0, tf;
 };
+
+// One face of a traction or pressure block (boundaryConditions.cpp:218-505):
+// face S of bulk tet `tet`, its one-point rule (w |J|, phi) and unit normal n0
+// from the reference geometry, and the block's amount.  Its contributions
+// fcon[(con + a)*3 + i] go to node[a]: the three face nodes, or for a ramped
+// pressure only the tet's first node (phi = 1, the reference's evaluation of
+// the bulk shape functions at natural coordinates 0).
+struct FaceLoad {
+    int kind;                 // MSX_LOAD_TRACTION_INST .. MSX_LOAD_PRESSURE_RAMP
+    int tet;
+    int node[3];
+    int con;
+    double wabsJ, phi[3], n0[3];
+    double t0, tf, value[3];
+};
+
+// Terms of the external-force lists: kind in the top 4 bits, index below.
+enum : unsigned { EXT_FORCE = 0u, EXT_GRAV_ELEM = 1u, EXT_GRAV_NODE = 2u, EXT_FACE = 3u };
+constexpr unsigned kExtIndexBits = 28;
 
 // Step control, double-buffered by step parity.  The node kernel of step n
 // reads slot (n-1)&1 and writes slot n&1; every thread derives the same
@@ -87,13 +108,21 @@ struct Problem {
     const int *node_bc;       // per node: -1 or record index
     const int2 *bc_rec;       // per record, per comp: (first entry, count)
     const BCEntry *bcs;
-    // Neumann loads (all nullptr without loads)
-    const double *grav_e;     // per element gravity term -w rho |J| g phi (z DOFs)
-    const double *grav_n;     // per node sum of grav_e over its elements, element order
-    const int *node_nf;       // per node: -1 or nodal-force record index
-    const int2 *nf_rec;       // per record, per comp: (first entry, count)
+    // Neumann loads (ext_ptr == nullptr without loads).  The external force of
+    // DOF d is the sum, in deck order starting from 0, of its terms
+    // ext_term[ext_ptr[d] .. ext_ptr[d+1]): EXT_FORCE i = nodal-force entry
+    // nfs[i]; EXT_GRAV_ELEM i = grav_e[i] (gravity block b, element e:
+    // i = b ne + e); EXT_GRAV_NODE i = grav_n[i] (block b, node: b nn + node;
+    // the block's element terms of the node summed in element order, used only
+    // as a DOF's first term); EXT_FACE i = fcon[i] (filled each step by the
+    // face kernel from that step's u and t).
+    const int *ext_ptr;
+    const unsigned *ext_term;
     const ForceEntry *nfs;
-    int gravity_first;        // 1: *GRAVITY precedes the *BOUNDARY, TYPE=FORCE blocks
+    const double *grav_e, *grav_n;
+    double *fcon;
+    const FaceLoad *faces;
+    int nfaces;
     // control
     Ctrl *ctrl;                       // [2]
     unsigned long long *dtmin;        // [2] bit patterns of positive doubles
@@ -143,6 +172,9 @@ void launch_setup_mass(const Problem &p, double *mass, double *minv, cudaStream_
 void launch_initial_cfl(const Problem &p, const double *uK, int slot, cudaStream_t s);
 // gravity terms per element and their per-node sums (reference order)
 void launch_setup_gravity(const Problem &p, double g, double *grav_e, double *grav_n, cudaStream_t s);
+// Face contributions of the step whose control slot `parity` the node kernel
+// just wrote (its time and displacement); mixed mode reads u as (hi, lo) pairs.
+void launch_face_loads(const Problem &p, int parity, bool mixed, cudaStream_t s);
 // Cauchy, Green-Lagrange (9 per element, row-major) and von Mises of the current u
 void launch_element_fields(const Problem &p, double *cauchy, double *gl, double *vms, cudaStream_t s);
 // one element pass + gather for f_int(u) (test hook); writes fint[3*nn]

@@ -104,12 +104,15 @@ struct msx_handle {
     DBuf<int> node_ptr, node_inc, node_bc;
     DBuf<int2> bc_rec;
     DBuf<BCEntry> bcs;
-    DBuf<double> grav_e, grav_n;
-    DBuf<int> node_nf;
-    DBuf<int2> nf_rec;
+    // Neumann loads: term lists per DOF, nodal-force entries, gravity terms per
+    // gravity block, surface faces and their per-step contributions
+    DBuf<double> grav_e, grav_n, fcon;
+    DBuf<int> ext_ptr;
+    DBuf<unsigned> ext_term;
     DBuf<ForceEntry> nfs;
-    double gravity = 0;
-    int gravity_first = 0;
+    DBuf<FaceLoad> faces;
+    int nfaces = 0;
+    bool loads = false;
     DBuf<Ctrl> ctrl;
     DBuf<unsigned long long> dtmin;
     DBuf<int> flags;
@@ -231,12 +234,14 @@ static void bind_problem(msx_handle *h)
     P.node_bc = h->node_bc.p;
     P.bc_rec = h->bc_rec.p;
     P.bcs = h->bcs.p;
-    P.grav_e = h->gravity != 0 ? h->grav_e.p : nullptr;
-    P.grav_n = h->gravity != 0 ? h->grav_n.p : nullptr;
-    P.node_nf = h->nfs.p ? h->node_nf.p : nullptr;
-    P.nf_rec = h->nf_rec.p;
+    P.ext_ptr = h->loads ? h->ext_ptr.p : nullptr;
+    P.ext_term = h->ext_term.p;
     P.nfs = h->nfs.p;
-    P.gravity_first = h->gravity_first;
+    P.grav_e = h->grav_e.p;
+    P.grav_n = h->grav_n.p;
+    P.fcon = h->fcon.p;
+    P.faces = h->faces.p;
+    P.nfaces = h->nfaces;
     P.ctrl = h->ctrl.p;
     P.dtmin = h->dtmin.p;
     P.flags = h->flags.p;
@@ -262,15 +267,17 @@ static int tiled_mode(const msx_handle *h) { return h->precision == MSX_PREC_MIX
 // machine code the pool runs), the reference-order pair for exact mode.
 static void launch_step(msx_handle *h, int parity)
 {
-    if (h->tiled) {
+    if (h->tiled)
         launch_tiled_node(h->d_desc.p, h->d_ntiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid_node,
                           h->tthreads, h->stream);
+    else
+        h->node(h->P, parity, h->stream);
+    if (h->nfaces) launch_face_loads(h->P, parity, h->precision == MSX_PREC_MIXED, h->stream);
+    if (h->tiled)
         launch_tiled_elem(h->d_desc.p, h->d_etiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
                           h->stream);
-    } else {
-        h->node(h->P, parity, h->stream);
+    else
         h->elem(h->P, parity, h->stream);
-    }
 }
 
 // Descriptor and one-solve tile list of the tiled kernels.
@@ -562,9 +569,11 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     h->bcs.release();
     h->grav_e.release();
     h->grav_n.release();
-    h->node_nf.release();
-    h->nf_rec.release();
+    h->fcon.release();
+    h->ext_ptr.release();
+    h->ext_term.release();
     h->nfs.release();
+    h->faces.release();
     h->d_desc.release();
     h->d_etiles.release();
     h->d_ntiles.release();
@@ -579,67 +588,268 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     return MSX_OK;
 }
 
-extern "C" msx_status msx_set_loads(msx_handle *h, const msx_nodal_force *forces, int64_t num_forces, double gravity,
-                                    int32_t gravity_first)
+// Geometry of a face triangle from its three nodes (node-major xyz), in the
+// reference's operation order: the one-point rule's weight * |J| and phi
+// (classLinearTriangles::defineGPs, spatialDiscretisation/classLinearTriangles.cpp:194-290,
+// order 1 of GPsTriangle2DValues, GPsDistribution.cpp:149-155, with the local
+// basis of createOrthogonalBasisOnPlane, mathematics/geometry.cpp:363-390) and
+// the unit normal (classLinearTriangles::getn0, :19-45).  Host code built
+// without FMA contraction, so both hosts produce the reference's bits.
+static double norm3(const double *a)
+{
+    double s = 0;
+    for (int i = 0; i < 3; i++) s += a[i] * a[i];
+    return std::sqrt(s);
+}
+
+static void cross(const double *A, const double *B, double *C)
+{
+    C[0] = A[1] * B[2] - A[2] * B[1];
+    C[1] = A[2] * B[0] - A[0] * B[2];
+    C[2] = A[0] * B[1] - A[1] * B[0];
+}
+
+static void face_geometry(const double *xyz, double *wabsJ, double *phi, double *n0)
+{
+    const double *p1 = xyz;
+    double a[3], b[3], nrm[3], xh[3], yh[3];
+    for (int i = 0; i < 3; i++) {
+        a[i] = xyz[3 + i] + (-1.0) * p1[i];
+        b[i] = xyz[6 + i] + (-1.0) * p1[i];
+    }
+    cross(b, a, nrm);
+    cross(a, nrm, xh);
+    const double magA = norm3(a), magX = norm3(xh);
+    for (int i = 0; i < 3; i++) {
+        yh[i] = a[i] / magA;
+        xh[i] = xh[i] / magX;
+    }
+    const double map[6] = {xh[0], xh[1], xh[2], yh[0], yh[1], yh[2]};
+    double T[9];   // T[r*3 + k]: coordinate r of face node k relative to the first
+    for (int k = 0; k < 3; k++)
+        for (int r = 0; r < 3; r++) T[r * 3 + k] = xyz[k * 3 + r] + (-1.0) * p1[r];
+    double L[6], Jm[4];
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 3; j++) {
+            L[i * 3 + j] = 0;
+            for (int k = 0; k < 3; k++) L[i * 3 + j] += map[i * 3 + k] * T[k * 3 + j];
+        }
+    const double dN[6] = {-1.0, -1.0, 1.0, 0.0, 0.0, 1.0};   // d phi_k / d xi_j at [k*2 + j]
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 2; j++) {
+            Jm[i * 2 + j] = 0;
+            for (int k = 0; k < 3; k++) Jm[i * 2 + j] += L[i * 3 + k] * dN[k * 2 + j];
+        }
+    const double J = Jm[0] * Jm[3] - Jm[2] * Jm[1];
+    *wabsJ = (0.5 * 1.) * std::fabs(J);
+    const double x = 0.33333333333333, y = 0.33333333333333;
+    phi[0] = -1.0 * x - 1.0 * y + 1.0;
+    phi[1] = 1.0 * x;
+    phi[2] = 1.0 * y;
+    const double *x1 = xyz, *x2 = xyz + 3, *x3 = xyz + 6;
+    for (int i = 0; i < 3; i++) {
+        const int c1 = i == 0 ? 1 : (i == 1 ? 2 : 0), c2 = i == 0 ? 2 : (i == 1 ? 0 : 1);
+        n0[i] = (x2[c1] - x1[c1]) * (x3[c2] - x1[c2]) - (x3[c1] - x1[c1]) * (x2[c2] - x1[c2]);
+    }
+    const double no = norm3(n0);
+    for (int i = 0; i < 3; i++) n0[i] = n0[i] / no;
+}
+
+// Face S (1..4) of a tet: classLinearTetrahedra::getSubElement
+// (spatialDiscretisation/classLinearTetrahedra.cpp:30-62).
+static void tet_face(const int *c, int S, int *t)
+{
+    if (S == 1) {
+        t[0] = c[0]; t[1] = c[1]; t[2] = c[2];
+    } else if (S == 2 || S == 3) {
+        t[0] = c[S - 2]; t[1] = c[3]; t[2] = c[S - 1];
+    } else {
+        t[0] = c[0]; t[1] = c[2]; t[2] = c[S - 1];
+    }
+}
+
+extern "C" msx_status msx_set_load_blocks(msx_handle *h, const msx_load_block *blocks, int64_t num_blocks)
 {
     if (!h) return fail(MSX_ERR_ARG, "NULL handle");
-    if (num_forces < 0 || (num_forces > 0 && !forces)) return fail(MSX_ERR_ARG, "bad nodal force array");
-    const long long nn = h->P.nn;
-    for (long long k = 0; k < num_forces; k++) {
-        if (forces[k].dof < 0 || forces[k].dof >= 3 * nn) return fail(MSX_ERR_ARG, "nodal force dof out of range");
-        if (!(forces[k].tf - forces[k].t0 != 0)) return fail(MSX_ERR_ARG, "nodal force needs tf != t0");
-    }
-    if (!std::isfinite(gravity)) return fail(MSX_ERR_ARG, "gravity must be finite");
-    // records per node and component, entries kept in input order
-    std::vector<long long> order(num_forces);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(),
-                     [&](long long x, long long y) { return forces[x].dof < forces[y].dof; });
-    std::vector<int> node_nf(nn, -1);
-    std::vector<int2> rec;
-    std::vector<ForceEntry> ent;
-    for (long long k = 0; k < num_forces; k++) {
-        const msx_nodal_force &f = forces[order[k]];
-        long long node = f.dof % nn;
-        int comp = (int)(f.dof / nn);
-        if (node_nf[node] < 0) {
-            node_nf[node] = (int)(rec.size() / 3);
-            rec.resize(rec.size() + 3, make_int2(0, 0));
+    if (num_blocks < 0 || (num_blocks > 0 && !blocks)) return fail(MSX_ERR_ARG, "bad load block array");
+    const long long nn = h->P.nn, ne = h->P.ne;
+    const unsigned kMaxIndex = (1u << kExtIndexBits) - 1;
+    long long nforce = 0, ngrav = 0, nface = 0, ncon = 0;
+    for (long long b = 0; b < num_blocks; b++) {
+        const msx_load_block &B = blocks[b];
+        if (B.kind == MSX_LOAD_FORCE) {
+            if (B.num_forces < 0 || (B.num_forces > 0 && !B.forces)) return fail(MSX_ERR_ARG, "bad nodal force array");
+            for (long long k = 0; k < B.num_forces; k++) {
+                if (B.forces[k].dof < 0 || B.forces[k].dof >= 3 * nn)
+                    return fail(MSX_ERR_ARG, "nodal force dof out of range");
+                if (!(B.forces[k].tf - B.forces[k].t0 != 0)) return fail(MSX_ERR_ARG, "nodal force needs tf != t0");
+            }
+            nforce += B.num_forces;
+        } else if (B.kind == MSX_LOAD_GRAVITY) {
+            if (!std::isfinite(B.value[0])) return fail(MSX_ERR_ARG, "gravity must be finite");
+            ngrav++;
+        } else if (B.kind >= MSX_LOAD_TRACTION_INST && B.kind <= MSX_LOAD_PRESSURE_RAMP) {
+            if (B.face < 1 || B.face > 4) return fail(MSX_ERR_ARG, "surface load face must be 1..4");
+            if (B.num_elems < 0 || (B.num_elems > 0 && !B.elems)) return fail(MSX_ERR_ARG, "bad surface element list");
+            if ((B.kind == MSX_LOAD_TRACTION_RAMP || B.kind == MSX_LOAD_PRESSURE_RAMP) && !(B.tf - B.t0 != 0))
+                return fail(MSX_ERR_ARG, "ramped surface load needs tf != t0");
+            for (long long k = 0; k < B.num_elems; k++)
+                if (B.elems[k] < 0 || B.elems[k] >= ne) return fail(MSX_ERR_ARG, "surface load element out of range");
+            nface += B.num_elems;
+            ncon += B.num_elems * (B.kind == MSX_LOAD_PRESSURE_RAMP ? 1 : 3);
+        } else {
+            return fail(MSX_ERR_ARG, "unknown load block kind");
         }
-        int2 &r = rec[node_nf[node] * 3 + comp];
-        if (r.y == 0) r.x = (int)ent.size();
-        r.y++;
-        ent.push_back({f.value / (f.tf - f.t0), f.t0, f.tf});
     }
+    if (nforce > kMaxIndex || ngrav * std::max(nn, ne) > kMaxIndex || 3 * ncon > kMaxIndex)
+        return fail(MSX_ERR_ARG, "too many load terms");
+
+    // host copies of the mesh and the node -> (element, corner) incidences
     MSX_CUDA(cudaStreamSynchronize(h->stream));
-    h->node_nf.release();
-    h->nf_rec.release();
-    h->nfs.release();
-    if (num_forces > 0) {
-        MSX_CUDA(h->node_nf.alloc(nn));
-        MSX_CUDA(h->nf_rec.alloc(rec.size()));
-        MSX_CUDA(h->nfs.alloc(ent.size()));
-        MSX_CUDA(cudaMemcpyAsync(h->node_nf.p, node_nf.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, h->stream));
-        MSX_CUDA(cudaMemcpyAsync(h->nf_rec.p, rec.data(), sizeof(int2) * rec.size(), cudaMemcpyHostToDevice, h->stream));
-        MSX_CUDA(cudaMemcpyAsync(h->nfs.p, ent.data(), sizeof(ForceEntry) * ent.size(), cudaMemcpyHostToDevice, h->stream));
+    std::vector<double> X(3 * nn);
+    std::vector<int4> conn(ne);
+    std::vector<int> ptr(nn + 1), inc(4 * ne);
+    MSX_CUDA(cudaMemcpy(X.data(), h->X.p, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost));
+    MSX_CUDA(cudaMemcpy(conn.data(), h->conn.p, sizeof(int4) * ne, cudaMemcpyDeviceToHost));
+    MSX_CUDA(cudaMemcpy(ptr.data(), h->node_ptr.p, sizeof(int) * (nn + 1), cudaMemcpyDeviceToHost));
+    MSX_CUDA(cudaMemcpy(inc.data(), h->node_inc.p, sizeof(int) * 4 * ne, cudaMemcpyDeviceToHost));
+
+    // nodal-force entries, faces, and each DOF's terms in deck order (two passes:
+    // count, then fill).  A gravity block contributes its per-node sum when it is
+    // the first term of the z DOF, else its element terms in element order.
+    std::vector<ForceEntry> ents;
+    std::vector<FaceLoad> faces;
+    std::vector<int> cnt(3 * nn + 1, 0), pos;
+    std::vector<unsigned> terms;
+    for (int pass = 0; pass < 2; pass++) {
+        std::vector<char> touched(3 * nn, 0);
+        long long fk = 0, gb = 0, con = 0;
+        auto emit = [&](long long dof, unsigned kind, unsigned idx) {
+            if (pass == 0) cnt[dof]++;
+            else terms[pos[dof]++] = (kind << kExtIndexBits) | idx;
+            touched[dof] = 1;
+        };
+        for (long long b = 0; b < num_blocks; b++) {
+            const msx_load_block &B = blocks[b];
+            if (B.kind == MSX_LOAD_FORCE) {
+                for (long long k = 0; k < B.num_forces; k++, fk++) {
+                    const msx_nodal_force &f = B.forces[k];
+                    if (pass == 0) ents.push_back({f.value / (f.tf - f.t0), f.t0, f.tf});
+                    emit(f.dof, EXT_FORCE, (unsigned)fk);
+                }
+            } else if (B.kind == MSX_LOAD_GRAVITY) {
+                for (long long i = 0; i < nn; i++) {
+                    const long long dof = i + 2 * nn;
+                    if (!touched[dof]) {
+                        emit(dof, EXT_GRAV_NODE, (unsigned)(gb * nn + i));
+                    } else {
+                        for (int k = ptr[i]; k < ptr[i + 1]; k++)
+                            emit(dof, EXT_GRAV_ELEM, (unsigned)(gb * ne + (inc[k] >> 2)));
+                    }
+                }
+                gb++;
+            } else {
+                const bool pramp = B.kind == MSX_LOAD_PRESSURE_RAMP;
+                for (long long k = 0; k < B.num_elems; k++) {
+                    const int e = B.elems[k];
+                    const int c[4] = {conn[e].x, conn[e].y, conn[e].z, conn[e].w};
+                    FaceLoad F{};
+                    F.kind = B.kind;
+                    F.tet = e;
+                    F.con = (int)con;
+                    F.t0 = B.t0;
+                    F.tf = B.tf;
+                    for (int i = 0; i < 3; i++) F.value[i] = B.value[i];
+                    int tri[3];
+                    tet_face(c, B.face, tri);
+                    if (pass == 0) {
+                        double xyz[9];
+                        for (int a = 0; a < 3; a++)
+                            for (int i = 0; i < 3; i++) xyz[a * 3 + i] = X[i * nn + tri[a]];
+                        face_geometry(xyz, &F.wabsJ, F.phi, F.n0);
+                    }
+                    const int nc = pramp ? 1 : 3;
+                    for (int a = 0; a < 3; a++) F.node[a] = pramp ? c[0] : tri[a];
+                    for (int a = 0; a < nc; a++)
+                        for (int i = 0; i < 3; i++) emit(F.node[a] + i * nn, EXT_FACE, (unsigned)((con + a) * 3 + i));
+                    if (pass == 0) faces.push_back(F);
+                    con += nc;
+                }
+            }
+        }
+        if (pass == 0) {
+            pos.assign(3 * nn + 1, 0);
+            for (long long d = 0; d < 3 * nn; d++) pos[d + 1] = pos[d] + cnt[d];
+            cnt.assign(pos.begin(), pos.end());   // cnt now holds the row starts
+            terms.resize(pos[3 * nn]);
+        }
     }
-    h->gravity = gravity;
-    h->gravity_first = gravity_first ? 1 : 0;
-    if (gravity != 0) {
-        if (!h->grav_e.p) MSX_CUDA(h->grav_e.alloc(h->P.ne));
-        if (!h->grav_n.p) MSX_CUDA(h->grav_n.alloc(nn));
+
+    for (auto *b : {&h->grav_e, &h->grav_n, &h->fcon}) b->release();
+    h->ext_ptr.release();
+    h->ext_term.release();
+    h->nfs.release();
+    h->faces.release();
+    h->nfaces = 0;
+    h->loads = !terms.empty();
+    if (h->loads) {
+        MSX_CUDA(h->ext_ptr.alloc(3 * nn + 1));
+        MSX_CUDA(h->ext_term.alloc(terms.size()));
+        MSX_CUDA(cudaMemcpyAsync(h->ext_ptr.p, cnt.data(), sizeof(int) * (3 * nn + 1), cudaMemcpyHostToDevice, h->stream));
+        MSX_CUDA(cudaMemcpyAsync(h->ext_term.p, terms.data(), sizeof(unsigned) * terms.size(), cudaMemcpyHostToDevice,
+                                 h->stream));
+    }
+    if (!ents.empty()) {
+        MSX_CUDA(h->nfs.alloc(ents.size()));
+        MSX_CUDA(cudaMemcpyAsync(h->nfs.p, ents.data(), sizeof(ForceEntry) * ents.size(), cudaMemcpyHostToDevice,
+                                 h->stream));
+    }
+    if (ngrav > 0) {
+        MSX_CUDA(h->grav_e.alloc(ngrav * ne));
+        MSX_CUDA(h->grav_n.alloc(ngrav * nn));
         bind_problem(h);
-        launch_setup_gravity(h->P, gravity, h->grav_e.p, h->grav_n.p, h->stream);
+        long long gb = 0;
+        for (long long b = 0; b < num_blocks; b++)
+            if (blocks[b].kind == MSX_LOAD_GRAVITY) {
+                launch_setup_gravity(h->P, blocks[b].value[0], h->grav_e.p + gb * ne, h->grav_n.p + gb * nn, h->stream);
+                gb++;
+            }
+    }
+    if (!faces.empty()) {
+        MSX_CUDA(h->faces.alloc(faces.size()));
+        MSX_CUDA(h->fcon.alloc(3 * ncon));
+        MSX_CUDA(cudaMemcpyAsync(h->faces.p, faces.data(), sizeof(FaceLoad) * faces.size(), cudaMemcpyHostToDevice,
+                                 h->stream));
+        MSX_CUDA(cudaMemsetAsync(h->fcon.p, 0, sizeof(double) * 3 * ncon, h->stream));
+        h->nfaces = (int)faces.size();
     }
     bind_problem(h);
     msx_status st = upload_tiled(h);
     if (st != MSX_OK) return st;
     MSX_CUDA(cudaStreamSynchronize(h->stream));
-    if (h->graph) {   // exact-mode graphs hold the Problem by value
+    if (h->graph) {   // the step's kernel list (face kernel) and the exact mode's Problem changed
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
     }
     return MSX_OK;
+}
+
+extern "C" msx_status msx_set_loads(msx_handle *h, const msx_nodal_force *forces, int64_t num_forces, double gravity,
+                                    int32_t gravity_first)
+{
+    msx_load_block B[2] = {};
+    msx_load_block f{}, g{};
+    f.kind = MSX_LOAD_FORCE;
+    f.forces = forces;
+    f.num_forces = num_forces;
+    g.kind = MSX_LOAD_GRAVITY;
+    g.value[0] = gravity;
+    int n = 0;
+    if (gravity_first && gravity != 0) B[n++] = g;
+    if (num_forces != 0) B[n++] = f;
+    if (!gravity_first && gravity != 0) B[n++] = g;
+    if (!std::isfinite(gravity)) return fail(MSX_ERR_ARG, "gravity must be finite");
+    return msx_set_load_blocks(h, B, n);
 }
 
 extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *rep)
@@ -797,6 +1007,7 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
                               h->tthreads, h->stream);
         else
             h->node(h->P, parity, h->stream);
+        if (h->nfaces) launch_face_loads(h->P, parity, h->precision == MSX_PREC_MIXED, h->stream);
         cudaEventRecord(ev[3 * i + 1], h->stream);
         if (h->tiled)
             launch_tiled_elem(h->d_desc.p, h->d_etiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,

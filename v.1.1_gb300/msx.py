@@ -43,6 +43,15 @@ class BC_(C.Structure):
     _fields_ = [("dof", C.c_int64), ("mode", C.c_int32), ("ramp_steps", C.c_int32), ("value", C.c_double)]
 
 
+LOAD_FORCE, LOAD_GRAVITY, LOAD_TRACTION_INST, LOAD_TRACTION_RAMP, LOAD_PRESSURE_INST, LOAD_PRESSURE_RAMP = range(6)
+
+
+class LoadBlock_(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("face", C.c_int32), ("t0", C.c_double), ("tf", C.c_double),
+                ("value", C.c_double * 3), ("elems", C.c_void_p), ("num_elems", C.c_int64),
+                ("forces", C.c_void_p), ("num_forces", C.c_int64)]
+
+
 class Force_(C.Structure):
     _fields_ = [("dof", C.c_int64), ("t0", C.c_double), ("tf", C.c_double), ("value", C.c_double)]
 
@@ -84,7 +93,8 @@ SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_
            "msx_last_error", "msx_internal_force", "msx_get_element_data", "msx_profile", "msx_mesh_cube",
            "msx_stream", "msx_set_device", "msx_pool_create", "msx_pool_submit", "msx_pool_step",
            "msx_pool_poll", "msx_pool_fetch", "msx_pool_destroy", "msx_pool_stats_get",
-           "msx_internal_force_noalloc", "msx_initial_dt", "msx_element_fields", "msx_set_loads"]
+           "msx_internal_force_noalloc", "msx_initial_dt", "msx_element_fields", "msx_set_loads",
+           "msx_set_load_blocks"]
 
 _lib = None
 
@@ -114,6 +124,7 @@ def load(path: str = LIB_PATH):
         "msx_initial_dt": [vp, C.POINTER(C.c_double)],
         "msx_element_fields": [vp, vp, vp, vp],
         "msx_set_loads": [vp, vp, i64, C.c_double, i32],
+        "msx_set_load_blocks": [vp, vp, i64],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -239,6 +250,39 @@ class Solver:
             arr[i] = Force_(*f)
         _check(load().msx_set_loads(self.h, C.cast(arr, C.c_void_p), len(forces), float(gravity),
                                     1 if gravity_first else 0))
+
+    def set_load_blocks(self, items):
+        """All Neumann loads in deck order, items as
+        ("force", t0, tf, Ff, [(node, Fx, Fy, Fz), ...]), ("gravity", g),
+        ("traction_inst" | "traction_ramp", t0, tf, (Tx, Ty, Tz), S, [tet, ...]),
+        ("pressure_inst" | "pressure_ramp", t0, tf, P, S, [tet, ...]) (S = face 1..4)."""
+        kinds = {"force": LOAD_FORCE, "gravity": LOAD_GRAVITY, "traction_inst": LOAD_TRACTION_INST,
+                 "traction_ramp": LOAD_TRACTION_RAMP, "pressure_inst": LOAD_PRESSURE_INST,
+                 "pressure_ramp": LOAD_PRESSURE_RAMP}
+        keep, blocks = [], []
+        for it in items:
+            B = LoadBlock_()
+            B.kind = kinds[it[0]]
+            if it[0] == "force":
+                _, t0, tf, Ff, rows = it
+                ents = [(int(node) + k * self.nn, t0, tf, F[k] * Ff) for node, *F in rows for k in range(3)]
+                arr = (Force_ * max(1, len(ents)))(*[Force_(*e) for e in ents])
+                keep.append(arr)
+                B.forces, B.num_forces = C.cast(arr, C.c_void_p), len(ents)
+            elif it[0] == "gravity":
+                B.value[0] = it[1]
+            else:
+                _, t0, tf, val, S, elems = it
+                B.t0, B.tf, B.face = t0, tf, S
+                vals = (val,) if it[0].startswith("pressure") else tuple(val)
+                for i, x in enumerate(vals):
+                    B.value[i] = x
+                e = np.ascontiguousarray(elems, dtype=np.int32)
+                keep.append(e)
+                B.elems, B.num_elems = e.ctypes.data, len(e)
+            blocks.append(B)
+        arr = (LoadBlock_ * max(1, len(blocks)))(*blocks)
+        _check(load().msx_set_load_blocks(self.h, C.cast(arr, C.c_void_p), len(blocks)))
 
     def initial_dt(self):
         d = C.c_double()
