@@ -68,6 +68,7 @@ double now_ms()
 
 struct Slot {
     bool active = false;
+    bool launched = false;   // a replay ordered after the solve's admission has run on it
     long long ticket = -1;
     long long nn = 0, ne = 0;
     void *arena = nullptr;
@@ -93,7 +94,11 @@ struct msx_pool {
     std::mutex mu;
     msx_pool_opts opts{};
     int device = 0, sms = 152;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;   // graph replays and result copies
+    cudaStream_t upload = nullptr;   // admissions: uploads and set-up kernels, overlapping a replay
+    cudaEvent_t ev_upload = nullptr, ev_step = nullptr;
+    bool uploads_pending = false;    // admissions since the last replay launch
+    bool inflight = false;           // a replay launched by msx_pool_step not yet collected
     std::vector<Slot> slots;
     Problem *d_descs = nullptr;
     Ctrl *d_ctrl = nullptr, *h_ctrl = nullptr;
@@ -235,7 +240,7 @@ static msx_status collect(msx_pool *p)
     p->elem_steps_active = 0;
     for (size_t s = 0; s < n; s++) {
         Slot &sl = p->slots[s];
-        if (!sl.active) continue;
+        if (!sl.active || !sl.launched) continue;   // admitted since the last launch: nothing to read yet
         const Ctrl &c = p->h_ctrl[2 * s];   // replays end on parity 0
         if (!c.stop) {
             p->elem_steps_active += sl.ne * c.step;
@@ -278,9 +283,47 @@ static bool any_active(const msx_pool *p)
 }
 
 // One graph replay (spl steps) with the current schedule; returns device ms.
+// Replays wait for the admissions enqueued on the upload stream.
+static msx_status order_after_uploads(msx_pool *p)
+{
+    if (p->uploads_pending) {
+        PCUDA(cudaStreamWaitEvent(p->stream, p->ev_upload, 0));
+        p->uploads_pending = false;
+    }
+    // from here on every resident solve's control slot is initialised in stream
+    // order: collect may read it
+    for (Slot &s : p->slots)
+        if (s.active) s.launched = true;
+    return MSX_OK;
+}
+
+// One graph replay, launched without waiting (msx_pool_step): collected by the
+// next step, poll or stats call.
+static msx_status launch_replay(msx_pool *p)
+{
+    msx_status st;
+    if ((st = order_after_uploads(p)) != MSX_OK) return st;
+    if ((st = upload_tiles(p)) != MSX_OK) return st;
+    if (!p->graph && (st = build_pool_graph(p, p->spl)) != MSX_OK) return st;
+    PCUDA(cudaGraphLaunch(p->graph, p->stream));
+    PCUDA(cudaEventRecord(p->ev_step, p->stream));
+    p->inflight = true;
+    return MSX_OK;
+}
+
+// Waits for the replay in flight, if any, and collects it.
+static msx_status finish_inflight(msx_pool *p)
+{
+    if (!p->inflight) return MSX_OK;
+    p->inflight = false;
+    PCUDA(cudaEventSynchronize(p->ev_step));
+    return collect(p);
+}
+
 static msx_status replay(msx_pool *p, float *ms)
 {
     msx_status st;
+    if ((st = order_after_uploads(p)) != MSX_OK) return st;
     if ((st = upload_tiles(p)) != MSX_OK) return st;
     if (!p->graph && (st = build_pool_graph(p, p->spl)) != MSX_OK) return st;
     cudaEvent_t a, b;
@@ -390,8 +433,11 @@ extern "C" msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out)
         msx_pool_destroy(p);
         return st;
     };
-    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
-        return bail(pfail(MSX_ERR_CUDA, "stream"));
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&p->upload, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->ev_upload, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->ev_step, cudaEventDisableTiming) != cudaSuccess)
+        return bail(pfail(MSX_ERR_CUDA, "streams"));
     size_t n = opts->max_slots;
     if (cudaMalloc(&p->d_descs, sizeof(Problem) * n) != cudaSuccess || cudaMalloc(&p->d_ctrl, sizeof(Ctrl) * 2 * n) != cudaSuccess ||
         cudaMalloc(&p->d_dtmin, sizeof(unsigned long long) * 2 * n) != cudaSuccess ||
@@ -410,6 +456,7 @@ extern "C" msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out)
 extern "C" msx_status msx_pool_destroy(msx_pool *p)
 {
     if (!p) return MSX_OK;
+    if (p->upload) cudaStreamSynchronize(p->upload);
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (Slot &s : p->slots)
         if (s.arena) cudaFree(s.arena);
@@ -419,6 +466,9 @@ extern "C" msx_status msx_pool_destroy(msx_pool *p)
         if (q) cudaFree(q);
     if (p->h_ctrl) cudaFreeHost(p->h_ctrl);
     if (p->stream) cudaStreamDestroy(p->stream);
+    if (p->upload) cudaStreamDestroy(p->upload);
+    for (cudaEvent_t e : {p->ev_upload, p->ev_step})
+        if (e) cudaEventDestroy(e);
     delete p;
     return MSX_OK;
 }
@@ -491,7 +541,7 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     sl.nn = nn;
     sl.ne = ne;
     sl.bytes = bytes;
-    PCUDA(cudaMallocAsync(&sl.arena, bytes, p->stream));
+    PCUDA(cudaMallocAsync(&sl.arena, bytes, p->upload));
     char *q = (char *)sl.arena;
     auto carve = [&](size_t b) {
         char *r = q;
@@ -537,7 +587,7 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     int2 *d_rec = (int2 *)carve(sizeof(int2) * 3 * nn);
     BCEntry *d_ent = (BCEntry *)carve(sizeof(BCEntry) * (num_bcs > 0 ? num_bcs : 1));
     if ((size_t)(q - (char *)sl.arena) > bytes) {   // the footprint must cover every array carved above
-        cudaFreeAsync(sl.arena, p->stream);
+        cudaFreeAsync(sl.arena, p->upload);
         return pfail(MSX_ERR_CUDA, "internal: solve arena smaller than its arrays");
     }
     P.node_ptr = d_ptr;
@@ -551,7 +601,9 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     P.flags = p->d_flags + 2 * slot;
     P.sf = o->scale_factor;
     P.tf = o->tf;
-    cudaStream_t s = p->stream;
+    // everything on the upload stream: a replay in flight on the main stream
+    // keeps running; the next replay waits for ev_upload
+    cudaStream_t s = p->upload;
     PCUDA(cudaMemcpyAsync((void *)P.conn, mesh->conn, sizeof(int4) * ne, cudaMemcpyHostToDevice, s));
     PCUDA(cudaMemcpyAsync(X, mesh->X, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, s));
     PCUDA(cudaMemcpyAsync(d_ptr, ptr.data(), sizeof(int) * (nn + 1), cudaMemcpyHostToDevice, s));
@@ -579,7 +631,8 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     pool_init_ctrl<<<1, 1, 0, s>>>(P, o->t0, limit);
     PCUDA(cudaGetLastError());
     PCUDA(cudaMemcpyAsync(p->d_descs + slot, &P, sizeof(Problem), cudaMemcpyHostToDevice, s));
-    PCUDA(cudaStreamSynchronize(s));
+    PCUDA(cudaEventRecord(p->ev_upload, s));
+    p->uploads_pending = true;
     sl.active = true;
     sl.ticket = p->next_ticket++;
     sl.submit_ms = now_ms();
@@ -595,20 +648,23 @@ extern "C" msx_status msx_pool_step(msx_pool *p, int64_t steps)
     if (!p) return pfail(MSX_ERR_ARG, "NULL pool");
     std::lock_guard<std::mutex> lk(p->mu);
     msx_status st;
+    if ((st = finish_inflight(p)) != MSX_OK) return st;
     if (!p->tuned && any_active(p) && (st = autotune(p)) != MSX_OK) return st;
     long long reps = steps > 0 ? (steps + p->spl - 1) / p->spl : 1;
-    for (long long r = 0; r < reps && any_active(p); r++) {
-        if ((st = replay(p, nullptr)) != MSX_OK) return st;
-        if ((st = collect(p)) != MSX_OK) return st;
+    for (long long r = 0; r < reps; r++) {
+        if (r > 0 && (st = finish_inflight(p)) != MSX_OK) return st;
+        if (!any_active(p)) break;
+        if ((st = launch_replay(p)) != MSX_OK) return st;
     }
-    return MSX_OK;
+    return MSX_OK;   // the last replay may still run: collected by the next step, poll or stats
 }
 
 extern "C" msx_status msx_pool_stats_get(msx_pool *p, msx_pool_stats *st)
 {
     if (!p || !st) return pfail(MSX_ERR_ARG, "NULL argument");
     std::lock_guard<std::mutex> lk(p->mu);
-    msx_status r = collect(p);
+    msx_status r = finish_inflight(p);
+    if (r == MSX_OK) r = collect(p);
     if (r != MSX_OK) return r;
     int act = 0;
     for (const Slot &s : p->slots) act += s.active;
@@ -628,6 +684,17 @@ extern "C" msx_status msx_pool_poll(msx_pool *p, msx_pool_result *results, int32
 {
     if (!p || !n || (max > 0 && !results)) return pfail(MSX_ERR_ARG, "NULL argument");
     std::lock_guard<std::mutex> lk(p->mu);
+    if (p->inflight) {   // never waits: collect only a replay that has finished
+        const cudaError_t q = cudaEventQuery(p->ev_step);
+        if (q == cudaSuccess) {
+            msx_status st = finish_inflight(p);
+            if (st != MSX_OK) return st;
+        } else if (q == cudaErrorNotReady) {
+            cudaGetLastError();   // "not ready" is no error: keep it out of later launch checks
+        } else {
+            return pfail(MSX_ERR_CUDA, std::string("pool replay: ") + cudaGetErrorString(q));
+        }
+    }
     int k = 0;
     while (k < max && !p->done_order.empty()) {
         long long t = p->done_order.front();
