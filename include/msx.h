@@ -274,10 +274,14 @@ msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out);
 msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const msx_material *mat,
                            const msx_bc *bcs, int64_t num_bcs, const msx_solver_opts *opts,
                            int64_t *ticket);
-/* Advance every resident solve by up to `steps` steps (one graph replay). */
+/* Advance every resident solve by up to `steps` steps (graph replays of
+ * steps_per_launch steps).  Keeps one replay in flight: waits for the previous
+ * one, collects its finished solves, launches the next and returns without
+ * waiting for it, so the caller's next admissions overlap it. */
 msx_status msx_pool_step(msx_pool *p, int64_t steps);
-/* Collect finished solves: fills up to max results, returns the count in *n.
- * u (3*num_nodes of that solve) is copied out by msx_pool_fetch. */
+/* Finished solves collected so far (never waits; takes in the replay in flight
+ * if it has completed): fills up to max results, returns the count in *n.
+ * u, v, a of a solve are copied out by msx_pool_fetch. */
 msx_status msx_pool_poll(msx_pool *p, msx_pool_result *results, int32_t max, int32_t *n);
 msx_status msx_pool_fetch(msx_pool *p, int64_t ticket, double *u, double *v, double *a);
 msx_status msx_pool_destroy(msx_pool *p);
