@@ -192,11 +192,11 @@ def reference_arm(args):
     value = mesh.ne * r.steps / r.loop_seconds
     sample = ("%d of %d steps of the 6M-tet FP64 workload (bounded to ~60 s), oracle C restatement of the "
               "reference path, OpenMP %d threads, set-up excluded" % (r.steps, args.steps, cores))
-    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "element-steps/s", "n_gpus": 0,
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "element-steps/s", "n_gpus": args.gpus,
             "steps": r.steps, "warmup": w.steps, "ms_per_step": 1e3 * r.loop_seconds / r.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": WORKLOAD, "num_elems": mesh.ne, "num_nodes": mesh.nn,
-                                            "precision": "FP64"},
+                                            "precision": "FP64", "parallelism": "host cores (OpenMP)"},
             "cpu_baseline": {"value": value, "unit": "element-steps/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "element-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
