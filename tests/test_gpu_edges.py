@@ -1,0 +1,95 @@
+"""Edge cases of the explicit step on the GPU, against the oracle: a single
+tet, a mesh whose every DOF is prescribed, a solver chain that changes
+precision between blocks, a block of zero length, malformed meshes."""
+import numpy as np
+import pytest
+
+import msx
+import oracle as O
+
+MODES = [(msx.FP64_EXACT, 1e-12), (msx.FP64, 1e-10), (msx.MIXED, 1e-5)]
+
+
+def rel(x, y):
+    return float(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))
+
+
+def run_gpu(mesh, law, solvers, precision):
+    s0 = solvers[0]
+    S = msx.Solver(mesh.X, mesh.conn, [(law, 1e6, 0.3, 1000.0)], s0.bcs, s0.t0, s0.tf, s0.scale_factor,
+                   precision=precision[0] if isinstance(precision, tuple) else precision)
+    steps = S.run().steps
+    for k, s in enumerate(solvers[1:], 1):
+        S.next_solver(s.bcs, s.t0, s.tf, s.scale_factor,
+                      precision=precision[k] if isinstance(precision, tuple) else precision)
+        steps += S.run().steps
+    out = S.state()
+    S.close()
+    return out, steps
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", MODES)
+def test_single_tet(precision, tol):
+    X = np.array([[0.0, 1.0, 0.0, 0.0], [0.0, 0.0, 1.0, 0.0], [0.0, 0.0, 0.0, 1.0]])
+    mesh = O.Mesh(X, np.array([[0, 1, 2, 3]], np.int32))
+    bcs = [(0 + c * 4, O.BC_RAMP, 0.0, 0) for c in range(3)] + [(3 + 2 * 4, O.BC_RAMP, 0.01, 0)]
+    solvers = [O.Solver(0.0, 0.01, 0.5, bcs)]
+    ref = O.run(mesh, [O.Material(O.COMPRESSIBLE_NH)], solvers)
+    (u, v, a), steps = run_gpu(mesh, msx.COMPRESSIBLE_NH, solvers, precision)
+    assert steps == ref.steps > 0
+    assert rel(u, ref.u) <= tol and rel(v, ref.v) <= 10 * tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", MODES)
+def test_every_dof_prescribed(precision, tol):
+    mesh = O.cube_mesh(3)
+    rng = np.random.default_rng(5)
+    bcs = [(d, O.BC_RAMP, float(x), 0) for d, x in enumerate(rng.uniform(-1e-3, 1e-3, 3 * mesh.nn))]
+    solvers = [O.Solver(0.0, 0.02, 0.5, bcs)]
+    ref = O.run(mesh, [O.Material(O.STVK)], solvers)
+    (u, v, a), steps = run_gpu(mesh, msx.STVK, solvers, precision)
+    assert steps == ref.steps > 0
+    # no DOF is free: u is the sum of the ramp increments, a stays zero
+    assert rel(u, ref.u) <= tol and not a.any()
+
+
+@pytest.mark.gpu
+def test_chain_changes_precision():
+    mesh = O.cube_mesh(4)
+    solvers = [O.Solver(0.0, 0.01, 0.5, O.cube_bcs(4, 0.001)), O.Solver(0.01, 0.02, 0.5, O.cube_bcs(4, 0.002)),
+               O.Solver(0.02, 0.03, 0.5, O.cube_bcs(4, 0.003))]
+    ref = O.run(mesh, [O.Material(O.COMPRESSIBLE_NH)], solvers)
+    (u, v, a), steps = run_gpu(mesh, msx.COMPRESSIBLE_NH, solvers, (msx.FP64, msx.MIXED, msx.FP64))
+    assert steps == ref.steps
+    assert rel(u, ref.u) <= 1e-5
+
+
+@pytest.mark.gpu
+def test_zero_length_block_takes_no_step():
+    mesh = O.cube_mesh(2)
+    bcs = [(d, O.BC_INST, 1e-4, 0) for d in range(3)]
+    S = msx.Solver(mesh.X, mesh.conn, [(msx.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0)], bcs, 0.01, 0.01, 0.5)
+    rep = S.run()
+    u, v, a = S.state()
+    S.close()
+    assert rep.steps == 0 and not u.any() and not v.any()
+
+
+@pytest.mark.gpu
+def test_malformed_meshes_are_refused():
+    X, conn = msx.mesh_cube(2)
+    mat = [(msx.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0)]
+    bad = conn.copy()
+    bad[3, 2] = X.shape[1]                      # node index past the end
+    with pytest.raises(msx.MsxError):
+        msx.Solver(X, bad, mat, [], 0.0, 0.01, 0.5)
+    bad = conn.copy()
+    bad[0, 0] = -1
+    with pytest.raises(msx.MsxError):
+        msx.Solver(X, bad, mat, [], 0.0, 0.01, 0.5)
+    with pytest.raises(msx.MsxError):
+        msx.Solver(X, conn, mat, [(3 * X.shape[1], msx.BC_RAMP, 0.0, 0)], 0.0, 0.01, 0.5)   # DOF out of range
+    with pytest.raises(msx.MsxError):
+        msx.Solver(X, conn, [(msx.COMPRESSIBLE_NH, 1e6, 0.3, -1.0)], [], 0.0, 0.01, 0.5)  # negative density
