@@ -170,6 +170,15 @@ typedef struct {
  * call); takes effect from the next step. */
 msx_status msx_set_load_blocks(msx_handle *h, const msx_load_block *blocks, int64_t num_blocks);
 
+/* Nodal values of the current state for the reference's node data extraction
+ * (*EXTRACTION, NODE: solvers/dataExtraction.cpp:778-840, written every step by
+ * classSolverExplicit::calculate, solverExplicit.cpp:325).  field: displacement
+ * ("Unknown"), external force or internal force of the last step; component
+ * comp (0..2) of the n listed nodes (0-based) into out[n].  The internal force
+ * is summed from zero in element order, as computeInternalForce scatters it. */
+typedef enum { MSX_FIELD_DISPLACEMENT = 0, MSX_FIELD_EXTERNAL_FORCE = 1, MSX_FIELD_INTERNAL_FORCE = 2 } msx_node_field;
+msx_status msx_node_values(msx_handle *h, int32_t field, int32_t comp, const int32_t *nodes, int64_t n, double *out);
+
 msx_status msx_destroy(msx_handle *h);
 
 /* Message of the last failing call on this host thread. */

@@ -399,7 +399,7 @@ def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int 
 
 
 # ---------------------------------------------------------------- the reference
-def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Loads = None):
+def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Loads = None, extractions=()):
     """Abaqus-style deck in the keyword subset the reference parses
     (src/IO/inputFile.cpp: nodes :20-108, C3D4 elements :118-323, materials
     :838-1029, solver blocks :2253-2831, displacement BCs :2960-3218)."""
@@ -428,6 +428,11 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Load
             lines += ["*BOUNDARY, TYPE=" + name,
                       ", ".join("%.17g" % x for x in (t0, tf) + vals) + ", %d" % S]
             lines += ["%d" % (int(e) + 1) for e in elems]
+    # node data extraction (src/IO/inputFile.cpp:4950-5026): the header is sliced at the
+    # commas without trimming, so it is written without spaces
+    for name, dtype, op, comp, nodes in extractions:
+        lines += ["*EXTRACTION, NODE", "%s,%s,%s,%d" % (name, dtype, op, comp)]
+        lines += ["%d" % (int(nd) + 1) for nd in nodes]
     for s in solvers:
         if any(b[1] == BC_VEL_RAMP for b in s.bcs):
             raise ValueError("the reference has no velocity-ramp boundary condition")
@@ -459,7 +464,7 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Load
 
 
 def run_reference(mesh: Mesh, mats, solvers, workdir: str | None = None, timeout: float = 3600,
-                  loads: Loads = None):
+                  loads: Loads = None, extractions=()):
     """Run the shim-built reference on a deck; returns (u, v, a, solve_wall_s)."""
     if not os.path.exists(REF_BIN):
         raise FileNotFoundError("reference binary not built: make -C oracle ref")
@@ -469,7 +474,7 @@ def run_reference(mesh: Mesh, mats, solvers, workdir: str | None = None, timeout
     mat_elems = None
     if mesh.elem_mat is not None:
         mat_elems = [np.nonzero(mesh.elem_mat == k)[0] for k in range(len(mats))]
-    write_deck(os.path.join(wd, "deck.inp"), mesh, mats, solvers, mat_elems, loads)
+    write_deck(os.path.join(wd, "deck.inp"), mesh, mats, solvers, mat_elems, loads, extractions)
     dump, timing = os.path.join(wd, "final.bin"), os.path.join(wd, "timing.txt")
     r = subprocess.run([REF_BIN, "-input", "deck.inp", "-inputDir", ".", "-outputDir", "out",
                         "-dump", dump, "-timing", timing], cwd=wd, capture_output=True, text=True,

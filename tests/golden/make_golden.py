@@ -92,6 +92,17 @@ def cases(ref_src):
         m3, [O.Material(nh)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.0))],
         O.Loads([("gravity", 9.81)] + [("pressure_ramp", 0.0, 0.02, 5e3, S, el) for S, el in side3] +
                 [forces] + [("traction_inst", 0.002, 0.012, (0.0, 0.0, -2e3), S, el) for S, el in top3]))
+    # node data extraction (*EXTRACTION, NODE): every node datatype and operation
+    node_on = lambda mesh, c, v: [i for i in range(mesh.nn) if abs(mesh.X[c, i] - v) < 1e-12]
+    topn, siden, botn = node_on(m3, 2, 1.0), node_on(m3, 0, 1.0), node_on(m3, 2, 0.0)
+    out["cube3_cnh_extraction"] = (
+        m3, [O.Material(cnh)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.0))],
+        O.Loads([("traction_ramp", 0.0, 0.015, (1e3, -2e3, 4e3), S, el) for S, el in top3] +
+                [("pressure_inst", 0.0, 0.02, 5e3, S, el) for S, el in side3] + [("gravity", 9.81)]),
+        [("top", "Unknown", "Mean", 2, topn), ("top", "Unknown", "Rough", 2, topn[:5]),
+         ("side", "ExternalForce", "Sum", 0, siden), ("side", "ExternalForce", "Rough", 2, siden[:4]),
+         ("bottom", "InternalForce", "Max", 2, botn), ("mid", "InternalForce", "Min", 1, list(range(20, 40))),
+         ("mid", "Unknown", "Max", 0, list(range(20, 40)))])
     side4 = plane_faces(m4, 0, 1.0)
     out["cube4_stvk_pressure_ramp"] = (
         m4, [O.Material(stvk)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(4, 0.001))],
@@ -102,7 +113,7 @@ def cases(ref_src):
     return out
 
 
-def pack(mesh, mats, solvers, ref, orc, loads=None):
+def pack(mesh, mats, solvers, ref, orc, loads=None, extractions=()):
     outs = O.read_vtk_outputs(ref[5])
     t_last, cau, E, vms = outs[-1]
     d = {"X": mesh.X, "conn": mesh.conn,
@@ -117,6 +128,12 @@ def pack(mesh, mats, solvers, ref, orc, loads=None):
     if loads is not None:
         import json
         d["loads_json"] = np.array(json.dumps(loads.items))
+    if extractions:
+        import json
+        # the extraction blocks and the reference's own CSV files they produced
+        d["extractions_json"] = np.array(json.dumps([list(x) for x in extractions]))
+        files = sorted(f for f in os.listdir(ref[5]) if f.endswith(".csv"))
+        d["extract_files_json"] = np.array(json.dumps({f: open(os.path.join(ref[5], f)).read() for f in files}))
     return d
 
 
@@ -131,11 +148,13 @@ def main():
             continue
         mesh, mats, solvers = case[:3]
         loads = case[3] if len(case) > 3 else None
-        ref = O.run_reference(mesh, mats, solvers, loads=loads)
+        extractions = case[4] if len(case) > 4 else ()
+        ref = O.run_reference(mesh, mats, solvers, loads=loads, extractions=extractions)
         orc = O.run(mesh, mats, solvers, loads=loads)
         same = all(np.array_equal(x, y) for x, y in zip((orc.u, orc.v, orc.a), ref[:3]))
         print("%-22s steps %5d  oracle==reference bitwise: %s  ref solve %.2fs" % (name, orc.steps, same, ref[3]))
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), **pack(mesh, mats, solvers, ref, orc, loads))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                            **pack(mesh, mats, solvers, ref, orc, loads, extractions))
 
 
 if __name__ == "__main__":

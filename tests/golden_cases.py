@@ -43,3 +43,13 @@ def _item(it):
         return (it[0], it[1], it[2], it[3], [tuple(r) for r in it[4]])
     kind, t0, tf, val, S, elems = it
     return (kind, t0, tf, val if kind.startswith("pressure") else tuple(val), int(S), [int(e) for e in elems])
+
+
+def load_extractions(name):
+    """(extraction blocks, {file name: the reference's CSV text}) of a case, or ((), {})."""
+    import json
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    if "extractions_json" not in d:
+        return (), {}
+    ex = [tuple(x) for x in json.loads(str(d["extractions_json"]))]
+    return ex, json.loads(str(d["extract_files_json"]))

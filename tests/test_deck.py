@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from golden_cases import load, load_loads, names
+from golden_cases import load, load_extractions, load_loads, names
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DECK = os.path.join(ROOT, "v.1.1_gb300", "_build", "msx_deck")
@@ -26,7 +26,8 @@ def write(tmp_path, name):
     mat_elems = None
     if mesh.elem_mat is not None:
         mat_elems = [np.nonzero(mesh.elem_mat == k)[0] for k in range(len(mats))]
-    O.write_deck(str(tmp_path / "deck.inp"), mesh, mats, solvers, mat_elems, load_loads(name))
+    O.write_deck(str(tmp_path / "deck.inp"), mesh, mats, solvers, mat_elems, load_loads(name),
+                 load_extractions(name)[0])
     return mesh, mats, solvers, ref, steps
 
 
@@ -104,3 +105,49 @@ def test_deck_outputs_follow_reference_cadence(tmp_path, name):
     for mine, refv in ((cau, d["vtk_cauchy"]), (E, d["vtk_E"]), (vms, d["vtk_vms"])):
         scale = max(np.abs(refv).max(), 1e-300)
         assert np.all(np.abs(mine - refv) <= 6e-6 * np.abs(refv) + 1e-6 * scale)
+
+
+def test_parse_node_extractions(tmp_path):
+    write(tmp_path, "cube3_cnh_extraction")
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-parse-only"],
+                       capture_output=True, text=True, check=True)
+    d = json.loads(r.stdout)
+    ex, files = load_extractions("cube3_cnh_extraction")
+    assert sorted(e["name"] + ".csv" for e in d["extractions"]) == sorted(files)
+    assert [e["nodes"] for e in d["extractions"]] == [len(x[4]) for x in ex]
+
+
+def test_element_extraction_is_refused(tmp_path):
+    write(tmp_path, "cube3_cnh_ramp")
+    p = tmp_path / "deck.inp"
+    p.write_text(p.read_text().replace("*END\n", "*EXTRACTION, ELEMENT\nall,SVM,Max\n*END\n"))
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-parse-only"],
+                       capture_output=True, text=True)
+    assert r.returncode == 2 and "ELEMENT" in r.stderr
+
+
+def _csv(text):
+    lines = text.strip().splitlines()
+    return lines[0], np.array([[float(x) for x in ln.split(",")] for ln in lines[1:]])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [("exact", 1e-12), ("fp64", 1e-9)])
+def test_node_extraction_matches_reference_files(tmp_path, precision, tol):
+    """*EXTRACTION, NODE: the files the reference writes every step, same names,
+    headers, rows (times and values at %.16g)."""
+    write(tmp_path, "cube3_cnh_extraction")
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-precision", precision,
+                        "-outputDir", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    _, files = load_extractions("cube3_cnh_extraction")
+    for fname, ref_text in files.items():
+        got = (out / fname).read_text()
+        h_ref, v_ref = _csv(ref_text)
+        h_got, v_got = _csv(got)
+        assert h_got == h_ref and v_got.shape == v_ref.shape, fname
+        scale = max(np.abs(v_ref[:, 1:]).max(), 1e-300)
+        assert np.allclose(v_got[:, 0], v_ref[:, 0], rtol=tol, atol=0), fname
+        assert np.abs(v_got[:, 1:] - v_ref[:, 1:]).max() <= tol * scale, fname

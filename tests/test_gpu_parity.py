@@ -203,3 +203,29 @@ def test_surface_load_errors():
     with pytest.raises(msx.MsxError):
         S.set_load_blocks([("pressure_ramp", 0.5, 0.5, 1e3, 1, [0])])        # ramp needs tf != t0
     S.close()
+
+
+@pytest.mark.parametrize("precision,tol", [(msx.FP64_EXACT, 1e-12), (msx.FP64, 1e-10), (msx.MIXED, 2e-5)])
+def test_node_values_match_oracle(precision, tol):
+    """msx_node_values: displacement, internal force (element-order sum) and
+    external force of the last step, against the oracle at that state."""
+    mesh, mats, solvers, _, _ = load("cube3_cnh_extraction")
+    L = load_loads("cube3_cnh_extraction")
+    s0 = solvers[0]
+    m = [(x.law, x.young, x.nu, x.rho) for x in mats]
+    S = msx.Solver(mesh.X, mesh.conn, m, s0.bcs, s0.t0, s0.tf, s0.scale_factor, precision=precision)
+    S.set_load_blocks(L.items)
+    rep = S.run(7)
+    u = S.state()[0]
+    nodes = np.arange(mesh.nn, dtype=np.int32)
+    fint = O.internal_force(mesh, mats, u)[0]
+    fext = O.external_force(mesh, mats, L, u, rep.t)
+    for c in range(3):
+        got_u = S.node_values(msx.FIELD_DISPLACEMENT, c, nodes)
+        got_i = S.node_values(msx.FIELD_INTERNAL_FORCE, c, nodes)
+        got_e = S.node_values(msx.FIELD_EXTERNAL_FORCE, c, nodes)
+        assert np.array_equal(got_u, u[c * mesh.nn:(c + 1) * mesh.nn])
+        ref_i, ref_e = fint[c * mesh.nn:(c + 1) * mesh.nn], fext[c * mesh.nn:(c + 1) * mesh.nn]
+        assert np.abs(got_i - ref_i).max() <= tol * max(np.abs(fint).max(), 1e-300)
+        assert np.abs(got_e - ref_e).max() <= 1e-12 * max(np.abs(fext).max(), 1e-300)
+    S.close()

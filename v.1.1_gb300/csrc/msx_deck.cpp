@@ -22,6 +22,9 @@
 // As in the reference, a RAMP BC stores U/(tf - t0) with the *Time read so
 // far, and once an INST block has been read every later displacement block
 // is instantaneous (the flag is not reset between solvers).
+#include <sys/stat.h>
+
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -53,6 +56,16 @@ struct Deck {
         std::vector<int32_t> elems;   // traction / pressure: bulk tets, 0-based
     };
     std::vector<Load> loads;
+    // *EXTRACTION, NODE blocks (IO/inputFile.cpp:4950-5026): "name, type, operation, comp"
+    struct Extraction {
+        std::string name;             // <name>_<Type><comp>_<Operation>, the output file's stem
+        int field = 0, comp = 0;      // msx_node_field
+        std::string op;               // Mean, Min, Max, Sum, Rough
+        std::vector<int32_t> nodes;   // 0-based
+        double last_time = 0;
+        FILE *file = nullptr;
+    };
+    std::vector<Extraction> extractions;
     std::vector<int32_t> conn;
     std::vector<msx_material> mats;
     std::vector<int32_t> elem_mat;    // -1 until assigned
@@ -153,6 +166,30 @@ Deck parse(const std::string &path)
             B.value[0] = atof(lines[i + 1].c_str());
             d.loads.push_back(B);
             i += 2;
+        } else if (starts(L, "*EXTRACTION, NODE")) {
+            // data extraction of nodal values written every step (solvers/dataExtraction.cpp)
+            auto h = split(lines[i + 1]);
+            if (h.size() != 4) die("a node extraction starts with name, type, operation, comp", (int)i + 2);
+            Deck::Extraction E;
+            static const char *types[] = {"Unknown", "ExternalForce", "InternalForce"};
+            E.field = -1;
+            for (int t = 0; t < 3; t++)
+                if (h[1] == types[t]) E.field = t;
+            if (E.field < 0) die("node datatype " + h[1] + " has not defined", (int)i + 2);
+            E.op = h[2];
+            if (E.op != "Mean" && E.op != "Min" && E.op != "Max" && E.op != "Sum" && E.op != "Rough")
+                die("operation " + E.op + " has not defined", (int)i + 2);
+            E.comp = (int)atof(h[3].c_str());
+            if (E.comp < 0 || E.comp > 2) die("node extraction component must be 0..2", (int)i + 2);
+            E.name = h[0] + "_" + types[E.field] + std::to_string(E.comp) + "_" + E.op;
+            for (i += 2; data_line(i); i++) {
+                long long node = atoll(lines[i].c_str()) - 1;
+                if (node < 0 || node >= (long long)d.xyz.size() / 3) die("extraction node out of range", (int)i + 1);
+                E.nodes.push_back((int32_t)node);
+            }
+            if (!E.nodes.empty()) d.extractions.push_back(E);
+        } else if (starts(L, "*EXTRACTION, ELEMENT")) {
+            die("*EXTRACTION, ELEMENT (per-element data extraction) is not supported", ln);
         } else if (starts(L, "*FEM Nodes") || starts(L, "*FEM Elements")) {
             if (i + 1 >= n || !starts(lines[i + 1], "All")) die("only 'All' FEM sets are supported", ln);
             i += 2;
@@ -322,6 +359,48 @@ void write_series(const std::string &dir, const std::vector<std::pair<std::strin
 
 }  // namespace
 
+// One row of a node extraction (solvers/dataExtraction.cpp:190-300): written
+// only when the time has advanced; the file <dir>/<name>.csv is opened at the
+// first row with the reference's header; the time and either every value
+// (Rough) or the operation over them (Mean, Sum: sums from 0 in node order;
+// Max, Min: first extreme), at %.16g.
+static bool write_extraction(Deck::Extraction &E, const std::string &dir, msx_handle *h, double t)
+{
+    if (!(t > E.last_time)) return true;
+    E.last_time = t;
+    std::vector<double> v(E.nodes.size());
+    if (msx_node_values(h, E.field, E.comp, E.nodes.data(), (int64_t)v.size(), v.data()) != MSX_OK) return false;
+    if (!E.file) {
+        E.file = fopen((dir + "/" + E.name + ".csv").c_str(), "w");
+        if (!E.file) return false;
+        if (E.op == "Rough") {
+            fprintf(E.file, "Time");
+            for (int32_t nd : E.nodes) fprintf(E.file, ",Node%dComp%d", nd + 1, E.comp);
+            fprintf(E.file, "\n");
+        } else {
+            fprintf(E.file, "Time,Value\n");
+        }
+    }
+    if (E.op == "Rough") {
+        fprintf(E.file, "%.16g", t);
+        for (double x : v) fprintf(E.file, ",%.16g", x);
+        fprintf(E.file, "\n");
+    } else {
+        double val = 0;
+        if (E.op == "Mean" || E.op == "Sum") {
+            for (double x : v) val += x;
+            if (E.op == "Mean") val /= (double)v.size();
+        } else if (E.op == "Max") {
+            val = *std::max_element(v.begin(), v.end());
+        } else {
+            val = *std::min_element(v.begin(), v.end());
+        }
+        fprintf(E.file, "%.16g,%.16g\n", t, val);
+    }
+    fflush(E.file);
+    return true;
+}
+
 int main(int argc, char **argv)
 {
     std::string input, dir = ".", dump, csv, outdir;
@@ -369,6 +448,11 @@ int main(int argc, char **argv)
         printf(", \"forces\": %zu, \"gravity\": %.17g, \"gravity_first\": %d", nforces, gravity, gravity_first);
         static const char *names[] = {"FORCE", "GRAVITY", "TRACTION INST", "TRACTION RAMP", "PRESSURE INST",
                                       "PRESSURE RAMP"};
+        printf(", \"extractions\": [");
+        for (size_t k = 0; k < d.extractions.size(); k++)
+            printf("%s{\"name\": \"%s\", \"nodes\": %zu}", k ? ", " : "", d.extractions[k].name.c_str(),
+                   d.extractions[k].nodes.size());
+        printf("]");
         printf(", \"loads\": [");
         for (size_t k = 0; k < d.loads.size(); k++)
             printf("%s{\"kind\": \"%s\", \"face\": %d, \"elements\": %zu, \"entries\": %zu}", k ? ", " : "",
@@ -383,12 +467,16 @@ int main(int argc, char **argv)
         return 0;
     }
     msx_mesh mesh{nn, ne, X.data(), d.conn.data(), d.elem_mat.empty() ? nullptr : d.elem_mat.data()};
+    // extraction files go to the output directory, by default ./output (IO/commandLine.cpp:20, 165-170)
+    const std::string xdir = outdir.empty() ? "output" : outdir;
+    if (!d.extractions.empty()) mkdir(xdir.c_str(), 0755);
     msx_handle *h = nullptr;
     long long total = 0;
     std::vector<std::pair<std::string, double>> outputs;
     for (size_t k = 0; k < d.solvers.size(); k++) {
         const SolverBlock &s = d.solvers[k];
-        msx_solver_opts o{s.t0, s.tf, s.sf, 0, precision, 0};
+        // with node extraction the block advances one step per call: two-step graphs
+        msx_solver_opts o{s.t0, s.tf, s.sf, 0, precision, d.extractions.empty() ? 0 : 2};
         msx_status st;
         if (k == 0) {
             st = msx_create(&mesh, d.mats.data(), (int32_t)d.mats.size(), s.bcs.data(), (int64_t)s.bcs.size(), &o, &h);
@@ -417,13 +505,15 @@ int main(int argc, char **argv)
             return 1;
         }
         msx_run_report r{};
-        if (outdir.empty()) {
+        const bool stepwise = !d.extractions.empty();
+        if (outdir.empty() && !stepwise) {
             st = msx_run(h, 0, &r);
             total += r.steps;
             printf("solver %zu: %lld steps, t = %.9g, dt = %.6g, device %.3f ms\n", k, (long long)r.steps, r.t, r.dt,
                    r.device_ms);
         } else {
             // the reference's output cadence (solverExplicit.cpp:171-174, 176-187, 310-321)
+            // and, with node extraction, a row per step (:325)
             double dt0 = 0;
             if ((st = msx_initial_dt(h, &dt0)) != MSX_OK) {
                 fprintf(stderr, "msx_deck: %s\n", msx_last_error());
@@ -431,26 +521,36 @@ int main(int argc, char **argv)
             }
             long long numStepsT = (long long)((s.tf - s.t0) / dt0);
             long long sampler = s.outputs > 0 ? numStepsT / s.outputs : numStepsT;
+            const long long every = sampler > 0 ? sampler : 1;
             auto emit = [&](double t) {
                 if (!write_vtk(outdir, (int)outputs.size(), t, X, d.conn, h)) return false;
                 outputs.push_back({"MuPhiSimOutputs_0_." + std::to_string(outputs.size()) + ".vtk", t});
                 write_series(outdir, outputs);
                 return true;
             };
-            if (s.t0 < 1E-12 && !emit(s.t0)) {
+            if (!outdir.empty() && s.t0 < 1E-12 && !emit(s.t0)) {
                 fprintf(stderr, "msx_deck: cannot write output\n");
                 return 1;
             }
-            long long steps = 0;
+            long long steps = 0, since = 0;
             for (;;) {
-                long long chunk = sampler > 0 ? sampler : 1;
+                const long long chunk = stepwise ? 1 : every;
                 st = msx_run(h, chunk, &r);
                 if (st != MSX_OK) break;
                 steps += r.steps;
+                since += r.steps;
                 if (r.steps == 0) break;
-                if ((r.steps == chunk || r.t == s.tf) && !emit(r.t)) {
-                    fprintf(stderr, "msx_deck: cannot write output\n");
-                    return 1;
+                for (auto &E : d.extractions)
+                    if (!write_extraction(E, xdir, h, r.t)) {
+                        fprintf(stderr, "msx_deck: cannot write %s/%s.csv\n", xdir.c_str(), E.name.c_str());
+                        return 1;
+                    }
+                if (!outdir.empty() && (since >= every || r.t == s.tf)) {
+                    if (!emit(r.t)) {
+                        fprintf(stderr, "msx_deck: cannot write output\n");
+                        return 1;
+                    }
+                    since = 0;
                 }
                 if (r.steps < chunk || r.t >= s.tf - 1E-12) break;
             }
@@ -484,6 +584,8 @@ int main(int argc, char **argv)
         fclose(f);
     }
     printf("total %lld steps\n", total);
+    for (auto &E : d.extractions)
+        if (E.file) fclose(E.file);
     msx_destroy(h);
     return 0;
 }

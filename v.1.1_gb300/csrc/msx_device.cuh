@@ -1425,6 +1425,32 @@ __global__ void face_load_kernel(Problem p, int parity, bool mixed)
     }
 }
 
+// Node data extraction (dataExtraction.cpp:778-840): the displacement, the
+// external force of the last step at its time t, or the internal force summed
+// from zero in element order (computeInternalForce, solverExplicit.cpp:363-379)
+// from the corner forces the last element kernel left: element order in the
+// reference-order mode, the node's CSR slots (also element order) otherwise.
+__global__ void node_values_kernel(Problem p, int mode, int field, int comp, const int *nodes, long long n, double t,
+                                   double *out)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const long long i = nodes[j], dof = i + comp * p.nn;
+    double v = 0.0;
+    if (field == MSX_FIELD_DISPLACEMENT) {
+        v = p.u[dof];
+    } else if (field == MSX_FIELD_EXTERNAL_FORCE) {
+        if (p.ext_ptr) v = ext_force_dof(p, dof, t);
+    } else {
+        for (int k = p.node_ptr[i]; k < p.node_ptr[i + 1]; k++) {
+            if (mode == MODE_EXACT) v += p.fe[(long long)p.node_inc[k] * 3 + comp];
+            else if (mode == MODE_MIXED) v += (double)p.fe32[(long long)k * 4 + comp];
+            else v += p.fe[(long long)k * 3 + comp];
+        }
+    }
+    out[j] = v;
+}
+
 // solvers.cpp:276-287 (uK == nullptr) and :296-320: element min into dtmin[slot]
 __global__ void __launch_bounds__(kElemBlock) initial_cfl_kernel(Problem p, const double *uK, int slot)
 {

@@ -42,6 +42,12 @@ void launch_internal_force_exact(const Problem &p, double *fint, cudaStream_t s)
     gather_kernel<MODE_EXACT><<<grid_for(p.nn, 256), 256, 0, s>>>(p, fint);
 }
 
+void launch_node_values(const Problem &p, int mode, int field, int comp, const int *nodes, long long n, double t,
+                        double *out, cudaStream_t s)
+{
+    if (n > 0) node_values_kernel<<<grid_for(n, 128), 128, 0, s>>>(p, mode, field, comp, nodes, n, t, out);
+}
+
 void launch_face_loads(const Problem &p, int parity, bool mixed, cudaStream_t s)
 {
     if (p.nfaces > 0) face_load_kernel<<<grid_for(p.nfaces, 128), 128, 0, s>>>(p, parity, mixed);

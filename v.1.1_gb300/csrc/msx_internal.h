@@ -175,6 +175,11 @@ void launch_setup_gravity(const Problem &p, double g, double *grav_e, double *gr
 // Face contributions of the step whose control slot `parity` the node kernel
 // just wrote (its time and displacement); mixed mode reads u as (hi, lo) pairs.
 void launch_face_loads(const Problem &p, int parity, bool mixed, cudaStream_t s);
+// Values of one field component at n nodes for the current state (node data
+// extraction): field as msx_node_field, t = time of the last step, mode = the
+// corner-force layout in use (MODE_*).
+void launch_node_values(const Problem &p, int mode, int field, int comp, const int *nodes, long long n, double t,
+                        double *out, cudaStream_t s);
 // Cauchy, Green-Lagrange (9 per element, row-major) and von Mises of the current u
 void launch_element_fields(const Problem &p, double *cauchy, double *gl, double *vms, cudaStream_t s);
 // one element pass + gather for f_int(u) (test hook); writes fint[3*nn]

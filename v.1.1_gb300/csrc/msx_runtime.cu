@@ -123,6 +123,7 @@ struct msx_handle {
     int precision = MSX_PREC_FP64;
     int spg = 64;
     bool block_ready = false;
+    double last_t = 0;   // time of the last step run (external force of node extraction)
     long long block_steps = 0;
     double dt_init = 0;
     launch_fn node = nullptr, elem = nullptr;   // reference-order kernels (exact mode)
@@ -537,6 +538,8 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     UP(h->slot.p, slots.data(), sizeof(int4) * ne);
     if (h->mat.p) UP(h->mat.p, mids.data(), ne);
 #undef UP
+    cudaMemsetAsync(h->fe.p, 0, sizeof(double) * 12 * ne, s);
+    cudaMemsetAsync(h->fe32.p, 0, sizeof(float) * 16 * ne, s);
     cudaMemsetAsync(h->u.p, 0, sizeof(double) * 3 * nn, s);
     cudaMemsetAsync(h->v.p, 0, sizeof(double) * 3 * nn, s);
     cudaMemsetAsync(h->a.p, 0, sizeof(double) * 3 * nn, s);
@@ -886,6 +889,7 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
     float ms = 0;
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     h->block_steps = fin.step;
+    h->last_t = fin.t;
     if (rep) {
         rep->steps = fin.step - start_steps;
         rep->total_steps = fin.step;
@@ -898,6 +902,35 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
     }
     if (fin.status == MSX_ERR_NEG_JACOBIAN) return fail(MSX_ERR_NEG_JACOBIAN, "Negative jacobian: dt < 1e-20");
     if (fin.status == MSX_ERR_NAN) return fail(MSX_ERR_NAN, "There are NANs in the displacements");
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_node_values(msx_handle *h, int32_t field, int32_t comp, const int32_t *nodes, int64_t n,
+                                      double *out)
+{
+    if (!h || n < 0 || (n > 0 && (!nodes || !out))) return fail(MSX_ERR_ARG, "bad node value arguments");
+    if (field < MSX_FIELD_DISPLACEMENT || field > MSX_FIELD_INTERNAL_FORCE || comp < 0 || comp > 2)
+        return fail(MSX_ERR_ARG, "field must be a msx_node_field, comp 0..2");
+    for (int64_t k = 0; k < n; k++)
+        if (nodes[k] < 0 || nodes[k] >= h->P.nn) return fail(MSX_ERR_ARG, "node index out of range");
+    if (n == 0) return MSX_OK;
+    DBuf<int> dn;
+    DBuf<double> dv;
+    if (dn.alloc(n) != cudaSuccess || dv.alloc(n) != cudaSuccess) {
+        dn.release();
+        dv.release();
+        return fail(MSX_ERR_OOM, "node value scratch");
+    }
+    bind_problem(h);
+    const int mode = h->precision == MSX_PREC_FP64_EXACT ? MODE_EXACT
+                                                         : (h->precision == MSX_PREC_MIXED ? MODE_MIXED : MODE_FP64);
+    cudaMemcpyAsync(dn.p, nodes, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream);
+    launch_node_values(h->P, mode, field, comp, dn.p, n, h->last_t, dv.p, h->stream);
+    cudaMemcpyAsync(out, dv.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream);
+    const cudaError_t err = cudaStreamSynchronize(h->stream);
+    dn.release();
+    dv.release();
+    if (err != cudaSuccess) return fail(MSX_ERR_CUDA, cudaGetErrorString(err));
     return MSX_OK;
 }
 

@@ -43,6 +43,7 @@ class BC_(C.Structure):
     _fields_ = [("dof", C.c_int64), ("mode", C.c_int32), ("ramp_steps", C.c_int32), ("value", C.c_double)]
 
 
+FIELD_DISPLACEMENT, FIELD_EXTERNAL_FORCE, FIELD_INTERNAL_FORCE = 0, 1, 2
 LOAD_FORCE, LOAD_GRAVITY, LOAD_TRACTION_INST, LOAD_TRACTION_RAMP, LOAD_PRESSURE_INST, LOAD_PRESSURE_RAMP = range(6)
 
 
@@ -94,7 +95,7 @@ SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_
            "msx_stream", "msx_set_device", "msx_pool_create", "msx_pool_submit", "msx_pool_step",
            "msx_pool_poll", "msx_pool_fetch", "msx_pool_destroy", "msx_pool_stats_get",
            "msx_internal_force_noalloc", "msx_initial_dt", "msx_element_fields", "msx_set_loads",
-           "msx_set_load_blocks"]
+           "msx_set_load_blocks", "msx_node_values"]
 
 _lib = None
 
@@ -125,6 +126,7 @@ def load(path: str = LIB_PATH):
         "msx_element_fields": [vp, vp, vp, vp],
         "msx_set_loads": [vp, vp, i64, C.c_double, i32],
         "msx_set_load_blocks": [vp, vp, i64],
+        "msx_node_values": [vp, i32, i32, vp, i64, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -283,6 +285,14 @@ class Solver:
             blocks.append(B)
         arr = (LoadBlock_ * max(1, len(blocks)))(*blocks)
         _check(load().msx_set_load_blocks(self.h, C.cast(arr, C.c_void_p), len(blocks)))
+
+    def node_values(self, field, comp, nodes):
+        """Component comp of FIELD_DISPLACEMENT / FIELD_EXTERNAL_FORCE /
+        FIELD_INTERNAL_FORCE at the listed nodes for the current state."""
+        n = np.ascontiguousarray(nodes, dtype=np.int32)
+        out = np.zeros(len(n))
+        _check(load().msx_node_values(self.h, int(field), int(comp), _p(n), len(n), _p(out)))
+        return out
 
     def initial_dt(self):
         d = C.c_double()
