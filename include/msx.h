@@ -293,6 +293,10 @@ msx_status msx_pool_step(msx_pool *p, int64_t steps);
  * u, v, a of a solve are copied out by msx_pool_fetch. */
 msx_status msx_pool_poll(msx_pool *p, msx_pool_result *results, int32_t max, int32_t *n);
 msx_status msx_pool_fetch(msx_pool *p, int64_t ticket, double *u, double *v, double *a);
+/* Step the pool until solve `ticket` has finished and fill its result (the
+ * other resident solves advance too; their results are kept for poll/fetch).
+ * MSX_ERR_ARG if the ticket is unknown or already fetched. */
+msx_status msx_pool_wait(msx_pool *p, int64_t ticket, msx_pool_result *result);
 msx_status msx_pool_destroy(msx_pool *p);
 
 typedef struct {

@@ -77,3 +77,29 @@ def test_continuous_admission_and_budget():
     for t, r in done.items():
         assert np.array_equal(P.fetch(t)[0], ref[r["steps"]])
     P.close()
+
+
+def test_wait_for_one_ticket():
+    """msx_pool_wait steps the pool until one solve is done; the others keep
+    their results for poll/fetch, and every result equals the solve alone."""
+    cases = [case(n, 1e6, 0.3, 0.05, s) for s, n in enumerate((4, 6, 5))]
+    steps = [40, 90, 60]
+    P = msx.Pool(max_slots=4, precision=msx.MIXED, steps_per_launch=8)
+    tickets = [P.submit(X, c, m, b, st) for (X, c, m, b), st in zip(cases, steps)]
+    r = P.wait(tickets[1])
+    assert r["ticket"] == tickets[1] and r["status"] == 0 and r["steps"] == 90
+    u1 = P.fetch(tickets[1])[0]
+    done = {}
+    for _ in range(50):
+        for q in P.poll():
+            done[q["ticket"]] = q
+        if tickets[0] in done and tickets[2] in done:
+            break
+        P.step()
+    assert tickets[0] in done and tickets[2] in done
+    for t, (X, c, m, b), st in zip(tickets, cases, steps):
+        u = u1 if t == tickets[1] else P.fetch(t)[0]
+        assert np.array_equal(u, alone(X, c, m, b, st, msx.MIXED)[0])
+    with pytest.raises(msx.MsxError):
+        P.wait(tickets[1])   # already fetched
+    P.close()

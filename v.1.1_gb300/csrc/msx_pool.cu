@@ -707,6 +707,29 @@ extern "C" msx_status msx_pool_poll(msx_pool *p, msx_pool_result *results, int32
     return MSX_OK;
 }
 
+extern "C" msx_status msx_pool_wait(msx_pool *p, int64_t ticket, msx_pool_result *result)
+{
+    if (!p || !result) return pfail(MSX_ERR_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(p->mu);
+    auto resident = [&] {
+        for (const Slot &s : p->slots)
+            if (s.active && s.ticket == ticket) return true;
+        return false;
+    };
+    msx_status st;
+    for (;;) {
+        if ((st = finish_inflight(p)) != MSX_OK) return st;
+        auto it = p->done.find(ticket);
+        if (it != p->done.end()) {
+            *result = it->second.res;
+            return MSX_OK;
+        }
+        if (!resident()) return pfail(MSX_ERR_ARG, "unknown or already fetched ticket");
+        if (!p->tuned && (st = autotune(p)) != MSX_OK) return st;
+        if ((st = launch_replay(p)) != MSX_OK) return st;
+    }
+}
+
 extern "C" msx_status msx_pool_fetch(msx_pool *p, int64_t ticket, double *u, double *v, double *a)
 {
     if (!p) return pfail(MSX_ERR_ARG, "NULL pool");

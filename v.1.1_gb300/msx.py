@@ -93,7 +93,7 @@ class PoolResult_(C.Structure):
 SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_solver", "msx_destroy",
            "msx_last_error", "msx_internal_force", "msx_get_element_data", "msx_profile", "msx_mesh_cube",
            "msx_stream", "msx_set_device", "msx_pool_create", "msx_pool_submit", "msx_pool_step",
-           "msx_pool_poll", "msx_pool_fetch", "msx_pool_destroy", "msx_pool_stats_get",
+           "msx_pool_poll", "msx_pool_fetch", "msx_pool_wait", "msx_pool_destroy", "msx_pool_stats_get",
            "msx_internal_force_noalloc", "msx_initial_dt", "msx_element_fields", "msx_set_loads",
            "msx_set_load_blocks", "msx_node_values"]
 
@@ -340,6 +340,7 @@ class Pool:
                            ("msx_pool_step", [C.c_void_p, C.c_int64]),
                            ("msx_pool_poll", [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
                            ("msx_pool_fetch", [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+                           ("msx_pool_wait", [C.c_void_p, C.c_int64, C.c_void_p]),
                            ("msx_pool_destroy", [C.c_void_p]),
                            ("msx_pool_stats_get", [C.c_void_p, C.POINTER(PoolStats_)])):
             f = getattr(L, name)
@@ -380,6 +381,12 @@ class Pool:
         _check(load().msx_pool_poll(self.h, C.cast(arr, C.c_void_p), max_results, C.byref(n)))
         return [dict(ticket=arr[i].ticket, status=arr[i].status, steps=arr[i].steps, t=arr[i].t,
                      latency_ms=arr[i].submit_to_done_ms) for i in range(n.value)]
+
+    def wait(self, ticket):
+        """Step the pool until `ticket` has finished; its result (fetch it next)."""
+        r = PoolResult_()
+        _check(load().msx_pool_wait(self.h, ticket, C.byref(r)))
+        return dict(ticket=r.ticket, status=r.status, steps=r.steps, t=r.t, latency_ms=r.submit_to_done_ms)
 
     def fetch(self, ticket):
         nn = self.sizes.pop(ticket)
