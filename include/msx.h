@@ -179,6 +179,51 @@ msx_status msx_set_load_blocks(msx_handle *h, const msx_load_block *blocks, int6
 typedef enum { MSX_FIELD_DISPLACEMENT = 0, MSX_FIELD_EXTERNAL_FORCE = 1, MSX_FIELD_INTERNAL_FORCE = 2 } msx_node_field;
 msx_status msx_node_values(msx_handle *h, int32_t field, int32_t comp, const int32_t *nodes, int64_t n, double *out);
 
+/* Element data extraction (*EXTRACTION, ELEMENT: classElementData and
+ * classExtractData, solvers/dataExtraction.cpp:304-470 and 508-890, written
+ * every step by solverExplicit.cpp:325).  The quantities carry the numbers of
+ * the reference's ExtractData::ElementDataType and the operations those of
+ * ExtractData::Operation (solvers/dataExtraction.h:23-29), so a caller casts
+ * them across.  Values are taken at the state of the last step: F = I + grad u,
+ * the law's first Piola-Kirchhoff P, von Mises of P F^T / det F (SVM), SVM det F
+ * (KVM), the internal variables (none of the three laws has more than one, so
+ * INVAR1..6 read zero, dataExtraction.cpp:552-557), the law's strain energy
+ * density (DEFO_ENERGY; zero for the Neo-Hookean law, which keeps the default),
+ * the kinetic energy density 0.5 rho |v(centroid)|^2 (KIN_ENERGY) and the
+ * current volume wJ det F (VOLUME). */
+typedef enum {
+    MSX_ELEM_FXX = 1, MSX_ELEM_FXY, MSX_ELEM_FXZ, MSX_ELEM_FYX, MSX_ELEM_FYY, MSX_ELEM_FYZ, MSX_ELEM_FZX,
+    MSX_ELEM_FZY, MSX_ELEM_FZZ,
+    MSX_ELEM_PXX = 10, MSX_ELEM_PXY, MSX_ELEM_PXZ, MSX_ELEM_PYX, MSX_ELEM_PYY, MSX_ELEM_PYZ, MSX_ELEM_PZX,
+    MSX_ELEM_PZY, MSX_ELEM_PZZ,
+    MSX_ELEM_SVM = 19, MSX_ELEM_KVM = 20,
+    MSX_ELEM_INVAR1 = 21, MSX_ELEM_INVAR2, MSX_ELEM_INVAR3, MSX_ELEM_INVAR4, MSX_ELEM_INVAR5, MSX_ELEM_INVAR6,
+    MSX_ELEM_DEFO_ENERGY = 27, MSX_ELEM_EXTERNAL_ENERGY = 28, MSX_ELEM_KIN_ENERGY = 29, MSX_ELEM_VOLUME = 30
+} msx_element_quantity;
+typedef enum { MSX_OP_MEAN = 1, MSX_OP_MIN = 2, MSX_OP_MAX = 3, MSX_OP_SUM = 4 } msx_element_op;
+
+/* Per-element value of `quantity` for the n listed elements (0-based; elems
+ * NULL means all, n then ignored) into out[n] (all: out[num_elems]), in list
+ * order.  EXTERNAL_ENERGY is not per element and is refused. */
+msx_status msx_element_values(msx_handle *h, int32_t quantity, const int32_t *elems, int64_t n, double *out);
+
+/* The number the reference writes in one row of an element extraction over
+ * the listed elements (elems NULL: all), reduced on the device.  Each listed
+ * element counts once, whatever its order or repeats, as the reference selects
+ * the Gauss points of the listed elements (classElementData::initialise, :441-464).
+ *   F..INVAR6  Mean sum(v dV)/V, Sum sum(v dV), Max, Min of v, with dV = wJ
+ *              and V = sum(dV) (classElementData::getValue, :338-378);
+ *   DEFO_ENERGY, KIN_ENERGY  Mean sum(w dV)/V, Sum sum(w dV), Max, Min of the
+ *              density w (defoEnergy, kineticEnergy :569-688);
+ *   VOLUME     Sum, Max, Min of wJ det F (volume :690-748; its Mean returns no
+ *              value in the reference and is refused here);
+ *   EXTERNAL_ENERGY  u . f_ext over every DOF whatever op and list (:853-861).
+ * Sums run in a fixed tree order, so a result differs from the reference's
+ * element-order sum by rounding only and repeats bit for bit from run to run.
+ * An empty list is refused (the reference builds no extraction for it). */
+msx_status msx_element_reduce(msx_handle *h, int32_t quantity, int32_t op, const int32_t *elems, int64_t n,
+                              double *value);
+
 msx_status msx_destroy(msx_handle *h);
 
 /* Message of the last failing call on this host thread. */

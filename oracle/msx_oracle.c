@@ -678,6 +678,164 @@ done:
     return rc;
 }
 
+/* One Gauss point's element-extraction value at u, v (q numbered as
+ * ExtractData::ElementDataType, solvers/dataExtraction.h:24-27):
+ * getValueAtGP (dataExtraction.cpp:508-563) with Cauchy = P F^T / det F
+ * (classStates.cpp:309-316; maths.cpp:2257-2290), the laws' defoEnergy
+ * (hyperElasticNeoHookean.cpp:291-304, hyperElasticStVenantKirchhoff.cpp:251-274,
+ * zero default constitutiveModels.h:91-94), kineticEnergy's density (phi = 0.25
+ * at the one-point rule's centroid, dataExtraction.cpp:626-688) and volume's
+ * w J det F (:690-748).  The three laws keep at most one internal variable,
+ * and getValueAtGP reads INVAR k only past k of them, so INVAR1..6 are 0. */
+enum { ORC_Q_FXX = 1, ORC_Q_PXX = 10, ORC_Q_SVM = 19, ORC_Q_KVM = 20, ORC_Q_INVAR1 = 21, ORC_Q_INVAR6 = 26,
+       ORC_Q_DEFO = 27, ORC_Q_EXTERNAL = 28, ORC_Q_KIN = 29, ORC_Q_VOLUME = 30 };
+enum { ORC_OP_MEAN = 1, ORC_OP_MIN = 2, ORC_OP_MAX = 3, ORC_OP_SUM = 4 };
+
+static double gp_value(const orc_problem *p, const double *dphi, const double *wJ, const double *u, const double *v,
+                       int q, int64_t e)
+{
+    const int64_t nn = p->nn;
+    const int32_t *c = p->conn + 4 * e;
+    const orc_material *m = &p->mats[p->elem_mat ? p->elem_mat[e] : 0];
+    if (q >= ORC_Q_INVAR1 && q <= ORC_Q_INVAR6) return 0.;
+    if (q == ORC_Q_KIN) {
+        double vel[3] = {0., 0., 0.}, val = 0;
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 3; j++) vel[j] += 0.25 * v[c[i] + j * nn];
+        for (int j = 0; j < 3; j++) val += 0.5 * m->rho * vel[j] * vel[j];
+        return val;
+    }
+    if (q == ORC_Q_DEFO && m->law == ORC_NEO_HOOKEAN) return 0.;
+    const double *dp = dphi + 12 * e;
+    double F[9], P[9], C[9];
+    for (int i = 0; i < 9; i++) F[i] = 0.;
+    for (int i = 0; i < 3; i++) {
+        F[i * 3 + i] += 1.;
+        for (int a = 0; a < 4; a++)
+            for (int j = 0; j < 3; j++) F[i * 3 + j] += dp[a * 3 + j] * u[c[a] + i * nn];
+    }
+    if (q >= ORC_Q_FXX && q < ORC_Q_FXX + 9) return F[q - ORC_Q_FXX];
+    if (q == ORC_Q_VOLUME) return wJ[e] * det3(F);
+    if (q == ORC_Q_DEFO) {
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double s = 0;
+                for (int k = 0; k < 3; k++) s += F[k * 3 + i] * F[k * 3 + j];
+                C[i * 3 + j] = s;
+            }
+        if (m->law == ORC_COMPRESSIBLE_NH) {
+            double lambda = (m->young * m->nu) / ((1. + m->nu) * (1. - 2. * m->nu));
+            double mu = 0.5 * m->young / (1. + m->nu);
+            double J = det3(F), tr = 0;
+            for (int i = 0; i < 3; i++) tr += C[i * 3 + i];
+            return 0.5 * lambda * log(J) * log(J) - mu * log(J) + 0.5 * mu * tr;
+        }
+        double E[9], S[9], mu2 = m->young / (1. + m->nu);
+        double lam = m->young * m->nu / ((1. + m->nu) * (1. - (2 * m->nu))), trE = 0, w = 0;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) E[i * 3 + j] = 0.5 * (C[i * 3 + j] - (i == j ? 1. : 0.));
+        for (int i = 0; i < 3; i++) trE += E[i * 3 + i];
+        for (int i = 0; i < 9; i++) S[i] = E[i] * mu2;
+        for (int i = 0; i < 3; i++) S[i * 3 + i] += lam * trE;
+        for (int i = 0; i < 9; i++) w += S[i] * E[i];
+        return 0.5 * w;
+    }
+    orc_stress(m, F, P);
+    if (q >= ORC_Q_PXX && q < ORC_Q_PXX + 9) return P[q - ORC_Q_PXX];
+    double detJinv = 1. / det3(F), S[9];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double s = 0;
+            for (int k = 0; k < 3; k++) s += P[i * 3 + k] * F[j * 3 + k];
+            S[i * 3 + j] = s;
+        }
+    for (int i = 0; i < 9; i++) S[i] = S[i] * detJinv;
+    double svm = sqrt(0.5 * ((S[0] - S[4]) * (S[0] - S[4]) + (S[4] - S[8]) * (S[4] - S[8]) +
+                             (S[8] - S[0]) * (S[8] - S[0]) + 6 * (S[1] * S[1] + S[2] * S[2] + S[5] * S[5])));
+    return q == ORC_Q_KVM ? svm * det3(F) : svm;
+}
+
+static int element_setup(const orc_problem *p, double **dphi, double **wJ)
+{
+    double *Lref = malloc(sizeof(double) * (size_t)(p->ne > 0 ? p->ne : 1));
+    *dphi = malloc(sizeof(double) * 12 * (size_t)(p->ne > 0 ? p->ne : 1));
+    *wJ = malloc(sizeof(double) * (size_t)(p->ne > 0 ? p->ne : 1));
+    int rc = (!Lref || !*dphi || !*wJ) ? ORC_ERR_ARG : orc_precompute(p->nn, p->ne, p->X, p->conn, *dphi, *wJ, Lref);
+    free(Lref);
+    return rc;
+}
+
+int orc_element_values(const orc_problem *p, const double *u, const double *v, int32_t q, const int32_t *elems,
+                       int64_t n, double *out)
+{
+    double *dphi, *wJ;
+    int rc = element_setup(p, &dphi, &wJ);
+    if (rc == ORC_OK)
+        for (int64_t k = 0; k < (elems ? n : p->ne); k++) out[k] = gp_value(p, dphi, wJ, u, v, q, elems ? elems[k] : k);
+    free(dphi); free(wJ);
+    return rc;
+}
+
+/* The value one *EXTRACTION, ELEMENT row holds (dataExtraction.cpp:841-889):
+ * the selected Gauss points are those of the listed elements in element order,
+ * each once (classElementData::initialise, :441-464); then
+ * classElementData::getValue (:338-378) on weights dV/V for F..INVAR,
+ * defoEnergy / kineticEnergy / volume (:569-748) for the energies and volume,
+ * and u . f_ext over every DOF for the external energy (:853-861). */
+int orc_element_reduce(const orc_problem *p, const double *u, const double *v, const double *fext, int32_t q,
+                       int32_t op, const int32_t *elems, int64_t n, double *value)
+{
+    if (q == ORC_Q_EXTERNAL) {
+        double energ = 0;
+        for (int64_t i = 0; i < 3 * p->nn; i++) energ += u[i] * fext[i];
+        *value = energ;
+        return ORC_OK;
+    }
+    double *dphi, *wJ;
+    int rc = element_setup(p, &dphi, &wJ);
+    unsigned char *sel = calloc((size_t)(p->ne > 0 ? p->ne : 1), 1);
+    if (!sel) rc = ORC_ERR_ARG;
+    if (rc != ORC_OK) { free(dphi); free(wJ); free(sel); return rc; }
+    for (int64_t k = 0; k < (elems ? n : p->ne); k++) sel[elems ? elems[k] : k] = 1;
+    double val = 0;
+    if (q == ORC_Q_DEFO || q == ORC_Q_KIN || q == ORC_Q_VOLUME) {
+        double ener = 0, volume = 0;
+        int init = 0;
+        for (int64_t e = 0; e < p->ne; e++) {
+            if (!sel[e]) continue;
+            /* defoEnergy and kineticEnergy weigh the density by dV = wJ;
+             * volume's own value is its dV = wJ det F */
+            double x = gp_value(p, dphi, wJ, u, v, q, e), dV = q == ORC_Q_VOLUME ? x : wJ[e];
+            if (q != ORC_Q_VOLUME) volume += dV;
+            if (op == ORC_OP_SUM || op == ORC_OP_MEAN) {
+                ener += q == ORC_Q_VOLUME ? dV : x * dV;
+            } else if (op == ORC_OP_MAX) {
+                if (!init) { init = 1; ener = x; } else if (x > ener) ener = x;
+            } else if (op == ORC_OP_MIN) {
+                if (!init) { init = 1; ener = x; } else if (x < ener) ener = x;
+            }
+        }
+        val = (op == ORC_OP_MEAN) ? ener / volume : ener;
+    } else {
+        double V = 0, acc = 0;
+        for (int64_t e = 0; e < p->ne; e++)
+            if (sel[e]) V += wJ[e];
+        int first = 1;
+        for (int64_t e = 0; e < p->ne; e++) {
+            if (!sel[e]) continue;
+            double x = gp_value(p, dphi, wJ, u, v, q, e);
+            if (op == ORC_OP_MEAN || op == ORC_OP_SUM) acc += x * (wJ[e] / V);
+            else if (first) acc = x;
+            else if (op == ORC_OP_MAX ? acc < x : x < acc) acc = x;
+            first = 0;
+        }
+        val = op == ORC_OP_SUM ? V * acc : acc;
+    }
+    *value = val;
+    free(dphi); free(wJ); free(sel);
+    return ORC_OK;
+}
+
 /* External force of all Neumann blocks at displacement u and time t (test hook). */
 int orc_external_force(const orc_problem *p, const double *u, double t, double *fext)
 {

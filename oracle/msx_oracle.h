@@ -90,6 +90,16 @@ int orc_internal_force(int64_t nn, int64_t ne, const int32_t *conn, const double
  * element) and von Mises (1 per element), as the reference's laws store them. */
 int orc_element_fields(int64_t nn, int64_t ne, const int32_t *conn, const double *dphi, const int32_t *elem_mat,
                        const orc_material *mats, const double *u, double *cauchy, double *gl, double *vms);
+/* Element data extraction (*EXTRACTION, ELEMENT) at the state u, v: the
+ * per-element value of quantity q (numbered as the reference's
+ * ExtractData::ElementDataType, 1..30) for the listed elements (elems NULL:
+ * all), and the value one extraction row holds for operation op (1 Mean,
+ * 2 Min, 3 Max, 4 Sum) over them; fext (3*nn) serves q = 28, the external
+ * energy, only.  The problem's X, conn, elem_mat and mats are used. */
+int orc_element_values(const orc_problem *p, const double *u, const double *v, int32_t q, const int32_t *elems,
+                       int64_t n, double *out);
+int orc_element_reduce(const orc_problem *p, const double *u, const double *v, const double *fext, int32_t q,
+                       int32_t op, const int32_t *elems, int64_t n, double *value);
 /* Full explicit solve; u,v,a (3*nn each) in = initial, out = final.
  * dt_hist (optional) receives one dt per executed step (max_hist entries). */
 int orc_run(const orc_problem *p, double *u, double *v, double *a,

@@ -106,6 +106,10 @@ def lib():
         _lib.orc_char_length.restype = C.c_double
         _lib.orc_element_fields.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_element_values.argtypes = [C.POINTER(_Problem), C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                            C.c_int64, C.c_void_p]
+        _lib.orc_element_reduce.argtypes = [C.POINTER(_Problem), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                            C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_double)]
         _lib.orc_internal_force.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.c_int]
@@ -296,6 +300,54 @@ def external_force(mesh: Mesh, mats, loads: Loads, u: np.ndarray, t: float) -> n
     return f
 
 
+# Element data extraction (*EXTRACTION, ELEMENT): quantity names and numbers as
+# the reference's ExtractData::ElementDataType, operations as ExtractData::Operation
+# (src/solvers/dataExtraction.h:23-29).
+ELEMENT_QUANTITIES = (["F" + a + b for a in "XYZ" for b in "XYZ"] + ["P" + a + b for a in "XYZ" for b in "XYZ"] +
+                      ["SVM", "KVM"] + ["INVAR%d" % k for k in range(1, 7)] +
+                      ["DEFO_ENERGY", "EXTERNAL_ENERGY", "KIN_ENERGY", "VOLUME"])
+ELEMENT_QUANTITY = {name: k + 1 for k, name in enumerate(ELEMENT_QUANTITIES)}
+ELEMENT_OPS = {"Mean": 1, "Min": 2, "Max": 3, "Sum": 4}
+
+
+def _plain_problem(mesh: Mesh, mats, keep: list):
+    X = np.ascontiguousarray(mesh.X)
+    conn = np.ascontiguousarray(mesh.conn)
+    em = None if mesh.elem_mat is None else np.ascontiguousarray(mesh.elem_mat, np.int32)
+    marr = _mats_array(mats)
+    keep += [X, conn, em, marr]
+    return _Problem(mesh.nn, mesh.ne, _p(X), _p(conn), _p(em), C.cast(marr, C.c_void_p), len(mats),
+                    None, 0, 0.0, 1.0, 0.5, 0, 0, 1, None, 0, 0.0, 0, None, 0)
+
+
+def element_values(mesh: Mesh, mats, quantity: str, u, v, elems=None) -> np.ndarray:
+    """Per-element value of an element-extraction quantity at the state u, v."""
+    keep = []
+    prob = _plain_problem(mesh, mats, keep)
+    el = None if elems is None else np.ascontiguousarray(elems, np.int32)
+    out = np.zeros(mesh.ne if el is None else len(el))
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    lib().orc_element_values(C.byref(prob), _p(u), _p(v), ELEMENT_QUANTITY[quantity], _p(el),
+                             0 if el is None else len(el), _p(out))
+    return out
+
+
+def element_reduce(mesh: Mesh, mats, quantity: str, op: str, u, v, elems=None, fext=None) -> float:
+    """The value one *EXTRACTION, ELEMENT row holds at the state u, v (fext: the
+    external force of that step, for EXTERNAL_ENERGY)."""
+    keep = []
+    prob = _plain_problem(mesh, mats, keep)
+    el = None if elems is None else np.ascontiguousarray(elems, np.int32)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    f = np.zeros(3 * mesh.nn) if fext is None else np.ascontiguousarray(fext, dtype=np.float64)
+    out = C.c_double(0.0)
+    lib().orc_element_reduce(C.byref(prob), _p(u), _p(v), _p(f), ELEMENT_QUANTITY[quantity], ELEMENT_OPS[op],
+                             _p(el), 0 if el is None else len(el), C.byref(out))
+    return out.value
+
+
 def internal_force(mesh: Mesh, mats, u: np.ndarray, nthreads: int = 1):
     dphi, wJ, _ = precompute(mesh)
     nn, ne = mesh.nn, mesh.ne
@@ -430,7 +482,15 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Load
             lines += ["%d" % (int(e) + 1) for e in elems]
     # node data extraction (src/IO/inputFile.cpp:4950-5026): the header is sliced at the
     # commas without trimming, so it is written without spaces
-    for name, dtype, op, comp, nodes in extractions:
+    # element data extraction (:5028-5111): "name,type,operation", then "All" or
+    # one element per line
+    for ex in extractions:
+        if ex[0] == "element":
+            _, name, dtype, op, elems = ex
+            lines += ["*EXTRACTION, ELEMENT", "%s,%s,%s" % (name, dtype, op)]
+            lines += ["All"] if elems is None else ["%d" % (int(e) + 1) for e in elems]
+            continue
+        name, dtype, op, comp, nodes = ex
         lines += ["*EXTRACTION, NODE", "%s,%s,%s,%d" % (name, dtype, op, comp)]
         lines += ["%d" % (int(nd) + 1) for nd in nodes]
     for s in solvers:

@@ -103,6 +103,32 @@ def cases(ref_src):
          ("side", "ExternalForce", "Sum", 0, siden), ("side", "ExternalForce", "Rough", 2, siden[:4]),
          ("bottom", "InternalForce", "Max", 2, botn), ("mid", "InternalForce", "Min", 1, list(range(20, 40))),
          ("mid", "Unknown", "Max", 0, list(range(20, 40)))])
+    # element data extraction (*EXTRACTION, ELEMENT): every quantity kind and
+    # operation over All and over element lists (one given in reverse order, one
+    # with repeats, and a second block of an existing name, which the reference drops)
+    every = lambda t, op: ("element", "all", t, op, None)
+    mid = list(range(40, 80))
+    out["cube3_cnh_element_extraction"] = (
+        m3, [O.Material(cnh)], [O.Solver(0.0, 0.04, 0.5, O.cube_bcs(3, 0.002))],
+        O.Loads([("traction_ramp", 0.0, 0.015, (1e3, -2e3, 4e3), S, el) for S, el in top3] +
+                [("pressure_inst", 0.0, 0.02, 5e3, S, el) for S, el in side3] + [("gravity", 9.81), forces]),
+        [every(t, op) for t in ("DEFO_ENERGY", "KIN_ENERGY") for op in ("Sum", "Mean", "Max", "Min")] +
+        [every("EXTERNAL_ENERGY", "Sum"), every("VOLUME", "Sum"), every("VOLUME", "Max"), every("VOLUME", "Min"),
+         every("FXX", "Mean"), every("FYZ", "Sum"), every("FZZ", "Max"), every("FZX", "Min"),
+         every("PXX", "Mean"), every("PZZ", "Sum"), every("PXY", "Max"), every("PYZ", "Min"),
+         every("SVM", "Max"), every("SVM", "Mean"), every("KVM", "Sum"), every("INVAR1", "Mean"),
+         ("element", "mid", "FZZ", "Mean", mid), ("element", "mid", "PZZ", "Sum", mid[::-1]),
+         ("element", "mid", "SVM", "Max", mid), ("element", "mid", "SVM", "Max", [0, 1, 2]),
+         ("element", "mid", "DEFO_ENERGY", "Sum", mid), ("element", "mid", "KIN_ENERGY", "Mean", mid),
+         ("element", "mid", "VOLUME", "Min", mid), ("element", "dup", "PZZ", "Sum", mid + mid[:5])])
+    out["cube2_two_materials_element_extraction"] = (
+        m2, [O.Material(nh, 1e6, 0.3, 1000.0), O.Material(stvk, 3e6, 0.25, 2000.0)],
+        [O.Solver(0.0, 0.04, 0.5, O.cube_bcs(2, 0.002))], None,
+        [every("DEFO_ENERGY", "Sum"), every("DEFO_ENERGY", "Max"), every("KIN_ENERGY", "Sum"),
+         every("SVM", "Mean"), every("SVM", "Max"), every("KVM", "Max"), every("PXX", "Mean"),
+         every("FXX", "Min"), every("VOLUME", "Sum"), every("EXTERNAL_ENERGY", "Sum"),
+         ("element", "nh", "DEFO_ENERGY", "Mean", list(range(0, m2.ne, 2))),
+         ("element", "stvk", "DEFO_ENERGY", "Mean", list(range(1, m2.ne, 2)))])
     side4 = plane_faces(m4, 0, 1.0)
     out["cube4_stvk_pressure_ramp"] = (
         m4, [O.Material(stvk)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(4, 0.001))],

@@ -117,13 +117,42 @@ def test_parse_node_extractions(tmp_path):
     assert [e["nodes"] for e in d["extractions"]] == [len(x[4]) for x in ex]
 
 
-def test_element_extraction_is_refused(tmp_path):
+ELEMENT_CASES = ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction"]
+
+
+@pytest.mark.parametrize("name", ELEMENT_CASES)
+def test_parse_element_extractions(tmp_path, name):
+    """One extraction per file the reference wrote: All_<TYPE>_<op> or
+    <name>_<TYPE>_<op>, the first block of a name kept."""
+    write(tmp_path, name)
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-parse-only"],
+                       capture_output=True, text=True, check=True)
+    d = json.loads(r.stdout)
+    _, files = load_extractions(name)
+    assert sorted(e["name"] + ".csv" for e in d["extractions"]) == sorted(files)
+    mid = [e for e in d["extractions"] if e["name"] == "mid_SVM_Max"]
+    assert not mid or mid[0]["elements"] == 40
+
+
+@pytest.mark.parametrize("block,message", [("all,SVM,Rough\nAll", "Rough"), ("v,VOLUME,Mean\nAll", "VOLUME"),
+                                           ("x,STRAIN,Max\nAll", "STRAIN"), ("x,SVM,Max\n999", "out of range")])
+def test_element_extraction_refusals(tmp_path, block, message):
     write(tmp_path, "cube3_cnh_ramp")
     p = tmp_path / "deck.inp"
-    p.write_text(p.read_text().replace("*END\n", "*EXTRACTION, ELEMENT\nall,SVM,Max\n*END\n"))
+    p.write_text(p.read_text().replace("*END\n", "*EXTRACTION, ELEMENT\n" + block + "\n*END\n"))
     r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-parse-only"],
                        capture_output=True, text=True)
-    assert r.returncode == 2 and "ELEMENT" in r.stderr
+    assert r.returncode == 2 and message in r.stderr
+
+
+def test_element_extraction_all_and_list_in_one_block(tmp_path):
+    write(tmp_path, "cube3_cnh_ramp")
+    p = tmp_path / "deck.inp"
+    p.write_text(p.read_text().replace("*END\n", "*EXTRACTION, ELEMENT\nsome,KVM,Max\nAll\n3\n5\n*END\n"))
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-parse-only"],
+                       capture_output=True, text=True, check=True)
+    ex = json.loads(r.stdout)["extractions"]
+    assert ex == [{"name": "All_KVM_Max", "elements": "All"}, {"name": "some_KVM_Max", "elements": 2}]
 
 
 def _csv(text):
@@ -151,3 +180,26 @@ def test_node_extraction_matches_reference_files(tmp_path, precision, tol):
         scale = max(np.abs(v_ref[:, 1:]).max(), 1e-300)
         assert np.allclose(v_got[:, 0], v_ref[:, 0], rtol=tol, atol=0), fname
         assert np.abs(v_got[:, 1:] - v_ref[:, 1:]).max() <= tol * scale, fname
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ELEMENT_CASES)
+@pytest.mark.parametrize("precision,tol", [("exact", 1e-12), ("fp64", 1e-9), ("mixed", 1e-4)])
+def test_element_extraction_matches_reference_files(tmp_path, name, precision, tol):
+    """*EXTRACTION, ELEMENT: the files the reference writes every step, same
+    names, headers and rows; values within tol of the file's largest value."""
+    write(tmp_path, name)
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-precision", precision,
+                        "-outputDir", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    _, files = load_extractions(name)
+    assert sorted(f.name for f in out.glob("*.csv")) == sorted(files)
+    for fname, ref_text in files.items():
+        h_ref, v_ref = _csv(ref_text)
+        h_got, v_got = _csv((out / fname).read_text())
+        assert h_got == h_ref and v_got.shape == v_ref.shape, fname
+        assert np.allclose(v_got[:, 0], v_ref[:, 0], rtol=1e-12 if precision != "mixed" else 1e-6, atol=0), fname
+        scale = max(np.abs(v_ref[:, 1]).max(), 1e-300)
+        assert np.abs(v_got[:, 1] - v_ref[:, 1]).max() <= tol * scale, (fname, np.abs(v_got[:, 1] - v_ref[:, 1]).max())

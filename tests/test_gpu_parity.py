@@ -229,3 +229,73 @@ def test_node_values_match_oracle(precision, tol):
         assert np.abs(got_i - ref_i).max() <= tol * max(np.abs(fint).max(), 1e-300)
         assert np.abs(got_e - ref_e).max() <= 1e-12 * max(np.abs(fext).max(), 1e-300)
     S.close()
+
+
+ELEMENT_QS = [q for q in msx.ELEMENT_QUANTITIES if q != "EXTERNAL_ENERGY"]
+
+
+@pytest.mark.parametrize("name", ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction"])
+def test_element_values_match_oracle(name):
+    """msx_element_values against the oracle at the same state (the reference's
+    final u, v put in with msx_set_state): both follow the reference's operation
+    order in FP64, so they agree to rounding (log and sqrt are the library's)."""
+    mesh, mats, solvers, (u, v, a), _ = load(name)
+    s0 = solvers[0]
+    m = [(x.law, x.young, x.nu, x.rho) for x in mats]
+    S = msx.Solver(mesh.X, mesh.conn, m, s0.bcs, s0.t0, s0.tf, s0.scale_factor, precision=msx.FP64_EXACT,
+                   elem_material=mesh.elem_mat)
+    S.set_state(u, v, a)
+    some = np.array([7, 3, 3, 0, mesh.ne - 1], np.int32)
+    for q in ELEMENT_QS:
+        ref = O.element_values(mesh, mats, q, u, v)
+        got = S.element_values(q)
+        scale = max(np.abs(ref).max(), 1e-300)
+        assert np.abs(got - ref).max() <= 1e-13 * scale, q
+        assert np.array_equal(S.element_values(q, some), got[some]), q
+    S.close()
+
+
+@pytest.mark.parametrize("precision", [msx.FP64_EXACT, msx.FP64, msx.MIXED])
+def test_element_reduce_matches_oracle(precision):
+    """msx_element_reduce for every quantity and operation, over all elements
+    and over a list with repeats in no order, against the oracle's reference-
+    order reduction of the GPU's own state after 9 steps with loads (so the
+    comparison isolates the extraction: tree sums against element-order sums)."""
+    name = "cube3_cnh_element_extraction"
+    mesh, mats, solvers, _, _ = load(name)
+    L = load_loads(name)
+    s0 = solvers[0]
+    m = [(x.law, x.young, x.nu, x.rho) for x in mats]
+    S = msx.Solver(mesh.X, mesh.conn, m, s0.bcs, s0.t0, s0.tf, s0.scale_factor, precision=precision)
+    S.set_load_blocks(L.items)
+    rep = S.run(9)
+    u, v, _ = S.state()
+    fext = O.external_force(mesh, mats, L, u, rep.t)
+    lst = [90, 5, 17, 5, 60, 61, 62, 90, 1]
+    _, wJ, _ = O.precompute(mesh)
+    for q in msx.ELEMENT_QUANTITIES:
+        vals = None if q == "EXTERNAL_ENERGY" else np.abs(O.element_values(mesh, mats, q, u, v))
+        for op in ("Mean", "Min", "Max", "Sum"):
+            if q == "VOLUME" and op == "Mean":
+                with pytest.raises(msx.MsxError):
+                    S.element_reduce(q, op)
+                continue
+            for el in (None, lst):
+                ref = O.element_reduce(mesh, mats, q, op, u, v, el, fext)
+                got = S.element_reduce(q, op, el)
+                if q == "EXTERNAL_ENERGY":
+                    scale = np.abs(u * fext).sum()
+                elif op in ("Min", "Max"):
+                    scale = abs(ref)
+                else:   # the sum of the magnitudes a sum's rounding scales with
+                    idx = np.arange(mesh.ne) if el is None else np.unique(el)
+                    scale = (vals[idx] * (1.0 if q == "VOLUME" else wJ[idx])).sum()
+                    scale /= wJ[idx].sum() if op == "Mean" else 1.0
+                assert abs(got - ref) <= 1e-13 * max(scale, 1e-300), (q, op, el is None, got, ref)
+    with pytest.raises(msx.MsxError):
+        S.element_reduce("SVM", "Max", [])
+    with pytest.raises(msx.MsxError):
+        S.element_reduce("SVM", "Max", [mesh.ne])
+    with pytest.raises(msx.MsxError):
+        S.element_values("EXTERNAL_ENERGY")
+    S.close()

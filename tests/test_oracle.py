@@ -137,3 +137,70 @@ def test_surface_pressure_ramp_loads_first_tet_node():
     inst = O.Loads([("pressure_inst", 0.0, 1.0, 4e3, S, el) for S, el in faces])
     fi = O.external_force(m, [O.Material()], inst, np.zeros(3 * m.nn), 1.0).reshape(3, -1)
     assert np.allclose(f.sum(axis=1), fi.sum(axis=1), rtol=1e-12, atol=1e-9)
+
+
+def element_extraction_rows(name):
+    """[(file name, quantity, op, elems or None, [(t, value), ...])] of a case's
+    *EXTRACTION, ELEMENT blocks, as the reference wrote them; a block whose file
+    name repeats an earlier one is dropped, as the reference keeps the first."""
+    from golden_cases import load_extractions
+    ex, files = load_extractions(name)
+    out, seen = [], set()
+    for e in ex:
+        if e[0] != "element":
+            continue
+        _, label, q, op, elems = e
+        fname = ("All" if elems is None else label) + "_%s_%s.csv" % (q, op)
+        if fname in seen:
+            continue
+        seen.add(fname)
+        rows = [tuple(float(x) for x in r.split(",")) for r in files[fname].strip().split("\n")[1:]]
+        out.append((fname, q, op, elems, rows))
+    return out
+
+
+ELEMENT_CASES = ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction"]
+
+
+@pytest.mark.parametrize("name", ELEMENT_CASES)
+def test_element_extraction_pinned_to_reference(name):
+    """Every row of every element-extraction file the reference wrote, from the
+    oracle's state after that many steps, to the digit (%.16g)."""
+    mesh, mats, solvers, _, steps = load(name)
+    loads = load_loads(name)
+    blocks = element_extraction_rows(name)
+    assert blocks and all(len(b[4]) == steps for b in blocks)
+    s0 = solvers[0]
+    for k in range(1, steps + 1):
+        r = O.run(mesh, mats, [O.Solver(s0.t0, s0.tf, s0.scale_factor, s0.bcs, max_steps=k)], loads=loads)
+        fext = O.external_force(mesh, mats, loads, r.u, r.t) if loads else np.zeros(3 * mesh.nn)
+        for fname, q, op, elems, rows in blocks:
+            t, val = rows[k - 1]
+            assert t == float("%.16g" % r.t), fname
+            got = O.element_reduce(mesh, mats, q, op, r.u, r.v, elems, fext)
+            assert float("%.16g" % got) == val, (fname, k, got, val)
+
+
+def test_element_extraction_files_dedupe_names():
+    blocks = element_extraction_rows("cube3_cnh_element_extraction")
+    assert [b[0] for b in blocks].count("mid_SVM_Max.csv") == 1
+    # the kept block is the first one, over the 40 'mid' elements
+    assert len([b for b in blocks if b[0] == "mid_SVM_Max.csv"][0][3]) == 40
+
+
+def test_element_values_agree_with_reductions():
+    """Per-element values against the reductions built from them, and the
+    identities the quantities obey (KVM = SVM det F, VOLUME = wJ det F)."""
+    mesh, mats, solvers, (u, v, _), _ = load("cube3_cnh_element_extraction")
+    _, wJ, _ = O.precompute(mesh)
+    val = {q: O.element_values(mesh, mats, q, u, v) for q in ("FXX", "FYY", "FZZ", "FXY", "FYZ", "FZX", "FYX", "FZY",
+                                                             "FXZ", "SVM", "KVM", "VOLUME", "DEFO_ENERGY", "KIN_ENERGY")}
+    F = np.stack([val[k] for k in ("FXX", "FXY", "FXZ", "FYX", "FYY", "FYZ", "FZX", "FZY", "FZZ")], 1).reshape(-1, 3, 3)
+    detF = np.linalg.det(F)
+    assert np.allclose(val["KVM"], val["SVM"] * detF, rtol=1e-12)
+    assert np.allclose(val["VOLUME"], wJ * detF, rtol=1e-12)
+    assert abs(O.element_reduce(mesh, mats, "DEFO_ENERGY", "Sum", u, v) - (val["DEFO_ENERGY"] * wJ).sum()) <= \
+        1e-12 * abs(val["DEFO_ENERGY"] * wJ).sum()
+    assert O.element_reduce(mesh, mats, "SVM", "Max", u, v) == val["SVM"].max()
+    mean = O.element_reduce(mesh, mats, "KIN_ENERGY", "Mean", u, v)
+    assert abs(mean - (val["KIN_ENERGY"] * wJ).sum() / wJ.sum()) <= 1e-12 * abs(mean)

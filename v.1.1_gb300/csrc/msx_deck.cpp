@@ -56,12 +56,17 @@ struct Deck {
         std::vector<int32_t> elems;   // traction / pressure: bulk tets, 0-based
     };
     std::vector<Load> loads;
-    // *EXTRACTION, NODE blocks (IO/inputFile.cpp:4950-5026): "name, type, operation, comp"
+    // *EXTRACTION, NODE blocks (IO/inputFile.cpp:4950-5026): "name, type, operation, comp";
+    // *EXTRACTION, ELEMENT blocks (:5028-5111): "name,type,operation", then All or elements
     struct Extraction {
-        std::string name;             // <name>_<Type><comp>_<Operation>, the output file's stem
-        int field = 0, comp = 0;      // msx_node_field
+        std::string name;             // the output file's stem: <name>_<Type><comp>_<Operation> (node),
+                                      // <name>_<TYPE>_<Operation> or All_<TYPE>_<Operation> (element)
+        bool element = false;
+        int field = 0, comp = 0;      // node: msx_node_field
+        int quantity = 0;             // element: msx_element_quantity
         std::string op;               // Mean, Min, Max, Sum, Rough
-        std::vector<int32_t> nodes;   // 0-based
+        bool all = false;             // element: every element
+        std::vector<int32_t> nodes;   // node: the nodes; element: the listed elements (0-based)
         double last_time = 0;
         FILE *file = nullptr;
     };
@@ -93,6 +98,16 @@ std::vector<std::string> split(const std::string &s)
 {
     fprintf(stderr, "msx_deck: %s (line %d)\n", msg.c_str(), line);
     exit(2);
+}
+
+// The reference keeps the first extraction of a file name and drops later
+// ones (classExtractData::addClassNodeDataToSave / addClassElementDataToSave,
+// solvers/dataExtraction.cpp:469-488).
+void add_extraction(Deck &d, const Deck::Extraction &E)
+{
+    for (const auto &x : d.extractions)
+        if (x.name == E.name) return;
+    d.extractions.push_back(E);
 }
 
 Deck parse(const std::string &path)
@@ -187,9 +202,46 @@ Deck parse(const std::string &path)
                 if (node < 0 || node >= (long long)d.xyz.size() / 3) die("extraction node out of range", (int)i + 1);
                 E.nodes.push_back((int32_t)node);
             }
-            if (!E.nodes.empty()) d.extractions.push_back(E);
+            if (!E.nodes.empty()) add_extraction(d, E);
         } else if (starts(L, "*EXTRACTION, ELEMENT")) {
-            die("*EXTRACTION, ELEMENT (per-element data extraction) is not supported", ln);
+            // element data written every step (solvers/dataExtraction.cpp:304-470, 841-889)
+            auto h = split(lines[i + 1]);
+            if (h.size() != 3) die("an element extraction starts with name, type, operation", (int)i + 2);
+            Deck::Extraction E;
+            E.element = true;
+            static const char *qn[] = {"FXX", "FXY", "FXZ", "FYX", "FYY", "FYZ", "FZX", "FZY", "FZZ",
+                                       "PXX", "PXY", "PXZ", "PYX", "PYY", "PYZ", "PZX", "PZY", "PZZ",
+                                       "SVM", "KVM", "INVAR1", "INVAR2", "INVAR3", "INVAR4", "INVAR5", "INVAR6",
+                                       "DEFO_ENERGY", "EXTERNAL_ENERGY", "KIN_ENERGY", "VOLUME"};
+            for (int q = 0; q < 30; q++)
+                if (h[1] == qn[q]) E.quantity = MSX_ELEM_FXX + q;
+            if (E.quantity == 0) die("element datatype " + h[1] + " has not defined", (int)i + 2);
+            E.op = h[2];
+            if (E.op == "Rough") die("Rough data is not implemented for element extraction", (int)i + 2);
+            if (E.op != "Mean" && E.op != "Min" && E.op != "Max" && E.op != "Sum")
+                die("operation " + E.op + " has not defined", (int)i + 2);
+            if (E.quantity == MSX_ELEM_VOLUME && E.op == "Mean")
+                die("VOLUME has no Mean (the reference's volume() returns no value for it)", (int)i + 2);
+            bool all = false;
+            for (i += 2; data_line(i); i++) {
+                if (starts(lines[i], "All")) {
+                    all = true;
+                    continue;
+                }
+                long long e = atoll(lines[i].c_str()) - 1;
+                if (e < 0 || e >= (long long)d.conn.size() / 4) die("extraction element out of range", (int)i + 1);
+                E.nodes.push_back((int32_t)e);
+            }
+            // "All" and a list make two extractions, the All one first (:5100-5111)
+            if (all) {
+                Deck::Extraction A = E;
+                A.all = true;
+                A.nodes.clear();
+                A.name = std::string("All_") + h[1] + "_" + E.op;
+                add_extraction(d, A);
+            }
+            E.name = h[0] + "_" + h[1] + "_" + E.op;
+            if (!E.nodes.empty()) add_extraction(d, E);
         } else if (starts(L, "*FEM Nodes") || starts(L, "*FEM Elements")) {
             if (i + 1 >= n || !starts(lines[i + 1], "All")) die("only 'All' FEM sets are supported", ln);
             i += 2;
@@ -198,7 +250,9 @@ Deck parse(const std::string &path)
             m.law = -1;
             bool have_rho = false;
             int id = (int)d.mats.size();
-            for (i++; i < n && !starts(lines[i], "*MATERIAL") && !starts(lines[i], "*END") && !starts(lines[i], "*SOLVER");) {
+            // the reference reads extraction blocks wherever they stand in the file
+            for (i++; i < n && !starts(lines[i], "*MATERIAL") && !starts(lines[i], "*END") && !starts(lines[i], "*SOLVER") &&
+                      !starts(lines[i], "*EXTRACTION");) {
                 const std::string &K = lines[i];
                 if (starts(K, "*Density")) {
                     m.rho = atof(lines[i + 1].c_str());
@@ -359,15 +413,31 @@ void write_series(const std::string &dir, const std::vector<std::pair<std::strin
 
 }  // namespace
 
-// One row of a node extraction (solvers/dataExtraction.cpp:190-300): written
-// only when the time has advanced; the file <dir>/<name>.csv is opened at the
-// first row with the reference's header; the time and either every value
-// (Rough) or the operation over them (Mean, Sum: sums from 0 in node order;
-// Max, Min: first extreme), at %.16g.
+// One row of an extraction (solvers/dataExtraction.cpp:190-300 node data,
+// :386-400 element data): written only when the time has advanced; the file
+// <dir>/<name>.csv is opened at the first row with the reference's header; the
+// time and either every value (Rough) or the operation over them (node data:
+// Mean, Sum sum from 0 in node order, Max, Min the first extreme; element data:
+// msx_element_reduce), at %.16g.
 static bool write_extraction(Deck::Extraction &E, const std::string &dir, msx_handle *h, double t)
 {
     if (!(t > E.last_time)) return true;
     E.last_time = t;
+    if (E.element) {
+        const int op = E.op == "Mean" ? MSX_OP_MEAN : E.op == "Min" ? MSX_OP_MIN : E.op == "Max" ? MSX_OP_MAX : MSX_OP_SUM;
+        double val = 0;
+        if (msx_element_reduce(h, E.quantity, op, E.all ? nullptr : E.nodes.data(), (int64_t)E.nodes.size(), &val) !=
+            MSX_OK)
+            return false;
+        if (!E.file) {
+            E.file = fopen((dir + "/" + E.name + ".csv").c_str(), "w");
+            if (!E.file) return false;
+            fprintf(E.file, "Time,Value\n");
+        }
+        fprintf(E.file, "%.16g,%.16g\n", t, val);
+        fflush(E.file);
+        return true;
+    }
     std::vector<double> v(E.nodes.size());
     if (msx_node_values(h, E.field, E.comp, E.nodes.data(), (int64_t)v.size(), v.data()) != MSX_OK) return false;
     if (!E.file) {
@@ -449,9 +519,14 @@ int main(int argc, char **argv)
         static const char *names[] = {"FORCE", "GRAVITY", "TRACTION INST", "TRACTION RAMP", "PRESSURE INST",
                                       "PRESSURE RAMP"};
         printf(", \"extractions\": [");
-        for (size_t k = 0; k < d.extractions.size(); k++)
-            printf("%s{\"name\": \"%s\", \"nodes\": %zu}", k ? ", " : "", d.extractions[k].name.c_str(),
-                   d.extractions[k].nodes.size());
+        for (size_t k = 0; k < d.extractions.size(); k++) {
+            const auto &E = d.extractions[k];
+            if (E.element && E.all)
+                printf("%s{\"name\": \"%s\", \"elements\": \"All\"}", k ? ", " : "", E.name.c_str());
+            else
+                printf("%s{\"name\": \"%s\", \"%s\": %zu}", k ? ", " : "", E.name.c_str(),
+                       E.element ? "elements" : "nodes", E.nodes.size());
+        }
         printf("]");
         printf(", \"loads\": [");
         for (size_t k = 0; k < d.loads.size(); k++)

@@ -1568,6 +1568,156 @@ __global__ void element_fields_kernel(Problem p, double *cauchy, double *gl, dou
                              (S[8] - S[0]) * (S[8] - S[0]) + 6 * (S[1] * S[1] + S[2] * S[2] + S[5] * S[5])));
 }
 
+// One Gauss point's element-extraction value (msx_element_quantity) at the
+// current u, v, in the reference's operation order: getValueAtGP
+// (dataExtraction.cpp:508-563; Cauchy = P F^T / det F, classStates.cpp:309-316),
+// the laws' defoEnergy (hyperElasticNeoHookean.cpp:291-304,
+// hyperElasticStVenantKirchhoff.cpp:251-274; the Neo-Hookean law keeps the
+// zero default, constitutiveModels.h:91-94), kineticEnergy's density at the
+// centroid, where every shape function is 0.25 (dataExtraction.cpp:626-688),
+// and volume's wJ det F (:690-748).  The internal variables read zero: no law
+// here has more than one (getValueAtGP wants more than k for INVAR k).
+__device__ double element_quantity_ref(const Problem &p, int q, long long e)
+{
+    if (q >= MSX_ELEM_INVAR1 && q <= MSX_ELEM_INVAR6) return 0.0;
+    const long long ne = p.ne, nn = p.nn;
+    const int4 cn = p.conn[e];
+    const int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    const MatParams &m = mat_of(p, e);
+    if (q == MSX_ELEM_KIN_ENERGY) {
+        double vel[3] = {0., 0., 0.}, val = 0;
+        for (int a = 0; a < 4; a++)
+            for (int j = 0; j < 3; j++) vel[j] += 0.25 * p.v[nd[a] + j * nn];
+        for (int j = 0; j < 3; j++) val += 0.5 * m.rho * vel[j] * vel[j];
+        return val;
+    }
+    if (q == MSX_ELEM_DEFO_ENERGY && m.law == 0) return 0.0;
+    double dphi[12];
+    for (int k = 0; k < 9; k++) dphi[3 + k] = p.G[k * ne + e];
+    for (int j = 0; j < 3; j++) dphi[j] = (-dphi[3 + j] - dphi[6 + j]) - dphi[9 + j];
+    double F[9];
+    for (int i = 0; i < 9; i++) F[i] = 0.;
+    for (int i = 0; i < 3; i++) {
+        F[i * 3 + i] += 1.;
+        for (int a = 0; a < 4; a++)
+            for (int j = 0; j < 3; j++) F[i * 3 + j] += dphi[a * 3 + j] * p.u[nd[a] + i * nn];
+    }
+    if (q >= MSX_ELEM_FXX && q <= MSX_ELEM_FZZ) return F[q - MSX_ELEM_FXX];
+    if (q == MSX_ELEM_VOLUME) return p.wJ[e] * det3_ref(F);
+    if (q == MSX_ELEM_DEFO_ENERGY) {
+        double C[9];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+                for (int k = 0; k < 3; k++) c += F[k * 3 + i] * F[k * 3 + j];
+                C[i * 3 + j] = c;
+            }
+        if (m.law == 1) {
+            const double J = det3_ref(F);
+            double tr = 0;
+            for (int i = 0; i < 3; i++) tr += C[i * 3 + i];
+            return 0.5 * m.lambda * log(J) * log(J) - m.mu * log(J) + 0.5 * m.mu * tr;
+        }
+        double E[9], S[9], trE = 0, w = 0;
+        for (int i = 0; i < 9; i++) E[i] = 0.5 * (C[i] - ((i % 4) == 0 ? 1.0 : 0.0));
+        for (int i = 0; i < 3; i++) trE += E[i * 3 + i];
+        for (int i = 0; i < 9; i++) S[i] = E[i] * m.mu2;
+        for (int i = 0; i < 3; i++) S[i * 3 + i] += m.lam_stvk * trE;
+        for (int i = 0; i < 9; i++) w += S[i] * E[i];
+        return 0.5 * w;
+    }
+    double P[9];
+    stress_ref(m, F, P);
+    if (q >= MSX_ELEM_PXX && q <= MSX_ELEM_PZZ) return P[q - MSX_ELEM_PXX];
+    // SVM, KVM
+    const double detF = det3_ref(F), detJinv = 1. / detF;
+    double S[9];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double c = 0;
+            for (int k = 0; k < 3; k++) c += P[i * 3 + k] * F[j * 3 + k];
+            S[i * 3 + j] = c;
+        }
+    for (int i = 0; i < 9; i++) S[i] = S[i] * detJinv;
+    const double svm = sqrt(0.5 * ((S[0] - S[4]) * (S[0] - S[4]) + (S[4] - S[8]) * (S[4] - S[8]) +
+                                   (S[8] - S[0]) * (S[8] - S[0]) + 6 * (S[1] * S[1] + S[2] * S[2] + S[5] * S[5])));
+    return q == MSX_ELEM_KVM ? svm * detF : svm;
+}
+
+__global__ void element_values_kernel(Problem p, int q, const int *elems, long long n, double *out)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) out[j] = element_quantity_ref(p, q, elems ? elems[j] : j);
+}
+
+// The element-extraction reduction in two fixed-shape passes, so the result
+// does not depend on the GPU or the run: kReduceBlocks blocks each take a
+// grid-stride share in index order and fold it in a shared-memory tree into
+// part[2b] (the weighted sum, or the extreme) and part[2b+1] (the sum of dV);
+// one block then folds the partials the same way.
+constexpr int kReduceBlocks = 512, kReduceThreads = 256;
+
+__device__ __forceinline__ void fold_pair(int op, double &s, double &w, double s2, double w2)
+{
+    if (op == MSX_OP_MAX) s = s2 > s ? s2 : s;
+    else if (op == MSX_OP_MIN) s = s2 < s ? s2 : s;
+    else s += s2;
+    w += w2;
+}
+
+__device__ __forceinline__ void block_fold(int op, double &s, double &w)
+{
+    __shared__ double ss[kReduceThreads], ws[kReduceThreads];
+    ss[threadIdx.x] = s;
+    ws[threadIdx.x] = w;
+    __syncthreads();
+    for (int h = kReduceThreads / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            double a = ss[threadIdx.x], b = ws[threadIdx.x];
+            fold_pair(op, a, b, ss[threadIdx.x + h], ws[threadIdx.x + h]);
+            ss[threadIdx.x] = a;
+            ws[threadIdx.x] = b;
+        }
+        __syncthreads();
+    }
+    s = ss[0];
+    w = ws[0];
+}
+
+__device__ __forceinline__ double reduce_identity(int op)
+{
+    return op == MSX_OP_MAX ? -INFINITY : (op == MSX_OP_MIN ? INFINITY : 0.0);
+}
+
+__global__ void __launch_bounds__(kReduceThreads) element_reduce_kernel(Problem p, int q, int op, const int *elems,
+                                                                        long long n, double t, double *part)
+{
+    double s = reduce_identity(op), w = 0.0;
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+        if (q == MSX_ELEM_EXTERNAL_ENERGY) {
+            s += p.u[j] * (p.ext_ptr ? ext_force_dof(p, j, t) : 0.0);
+            continue;
+        }
+        const long long e = elems ? elems[j] : j;
+        const double v = element_quantity_ref(p, q, e), dV = p.wJ[e];
+        fold_pair(op, s, w, q == MSX_ELEM_VOLUME || op == MSX_OP_MAX || op == MSX_OP_MIN ? v : v * dV, dV);
+    }
+    block_fold(op, s, w);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = s;
+        part[2 * blockIdx.x + 1] = w;
+    }
+}
+
+__global__ void __launch_bounds__(kReduceThreads) element_reduce_finish_kernel(int q, int op, const double *part,
+                                                                               double *out)
+{
+    double s = reduce_identity(op), w = 0.0;
+    for (int b = threadIdx.x; b < kReduceBlocks; b += blockDim.x) fold_pair(op, s, w, part[2 * b], part[2 * b + 1]);
+    block_fold(op, s, w);
+    if (threadIdx.x == 0) *out = op == MSX_OP_MEAN ? s / w : s;
+}
+
 #endif  // MSX_SETUP_KERNELS
 
 // f_int gather for the test hook: fint[node + c*nn] in element order

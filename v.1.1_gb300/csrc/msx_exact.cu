@@ -64,4 +64,18 @@ void launch_element_fields(const Problem &p, double *cauchy, double *gl, double 
     element_fields_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, cauchy, gl, vms);
 }
 
+void launch_element_values(const Problem &p, int quantity, const int *elems, long long n, double *out, cudaStream_t s)
+{
+    if (n > 0) element_values_kernel<<<grid_for(n, 128), 128, 0, s>>>(p, quantity, elems, n, out);
+}
+
+void launch_element_reduce(const Problem &p, int quantity, int op, const int *elems, long long n, double t,
+                           double *part, double *out, cudaStream_t s)
+{
+    element_reduce_kernel<<<kReduceBlocks, kReduceThreads, 0, s>>>(p, quantity, op, elems, n, t, part);
+    element_reduce_finish_kernel<<<1, kReduceThreads, 0, s>>>(quantity, op, part, out);
+}
+
+long long element_reduce_scratch() { return 2LL * kReduceBlocks + 1; }
+
 }  // namespace msx

@@ -182,6 +182,14 @@ void launch_node_values(const Problem &p, int mode, int field, int comp, const i
                         double *out, cudaStream_t s);
 // Cauchy, Green-Lagrange (9 per element, row-major) and von Mises of the current u
 void launch_element_fields(const Problem &p, double *cauchy, double *gl, double *vms, cudaStream_t s);
+// Element data extraction: per-element values of a msx_element_quantity, and
+// the reduction one extraction row writes (quantity, op as in msx.h), from the
+// current u, v and, for the external energy, the loads at time t.  part holds
+// element_reduce_scratch() - 1 doubles of partials, out one.
+void launch_element_values(const Problem &p, int quantity, const int *elems, long long n, double *out, cudaStream_t s);
+void launch_element_reduce(const Problem &p, int quantity, int op, const int *elems, long long n, double t,
+                           double *part, double *out, cudaStream_t s);
+long long element_reduce_scratch();
 // one element pass + gather for f_int(u) (test hook); writes fint[3*nn]
 void launch_internal_force_exact(const Problem &p, double *fint, cudaStream_t s);
 void launch_internal_force_fp64(const Problem &p, double *fint, cudaStream_t s);

@@ -934,6 +934,92 @@ extern "C" msx_status msx_node_values(msx_handle *h, int32_t field, int32_t comp
     return MSX_OK;
 }
 
+// Shared checks of the element-extraction calls: the quantity, and the element
+// list (NULL = all) copied to the device; n becomes the number of entries.
+static msx_status element_list(msx_handle *h, int32_t quantity, const int32_t *elems, int64_t &n, DBuf<int> &de)
+{
+    if (quantity < MSX_ELEM_FXX || quantity > MSX_ELEM_VOLUME)
+        return fail(MSX_ERR_ARG, "quantity must be a msx_element_quantity");
+    if (!elems) {
+        n = h->P.ne;
+        return MSX_OK;
+    }
+    if (n < 0) return fail(MSX_ERR_ARG, "negative element count");
+    for (int64_t k = 0; k < n; k++)
+        if (elems[k] < 0 || elems[k] >= h->P.ne) return fail(MSX_ERR_ARG, "element index out of range");
+    if (n == 0) return MSX_OK;
+    if (de.alloc(n) != cudaSuccess) return fail(MSX_ERR_OOM, "element list scratch");
+    cudaMemcpyAsync(de.p, elems, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream);
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_element_values(msx_handle *h, int32_t quantity, const int32_t *elems, int64_t n, double *out)
+{
+    if (!h || !out) return fail(MSX_ERR_ARG, "bad element value arguments");
+    if (quantity == MSX_ELEM_EXTERNAL_ENERGY) return fail(MSX_ERR_ARG, "EXTERNAL_ENERGY has no per-element value");
+    DBuf<int> de;
+    DBuf<double> dv;
+    msx_status st = element_list(h, quantity, elems, n, de);
+    if (st != MSX_OK || n == 0) {
+        de.release();
+        return st;
+    }
+    if (dv.alloc(n) != cudaSuccess) {
+        de.release();
+        return fail(MSX_ERR_OOM, "element value scratch");
+    }
+    bind_problem(h);
+    launch_element_values(h->P, quantity, elems ? de.p : nullptr, n, dv.p, h->stream);
+    cudaMemcpyAsync(out, dv.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream);
+    const cudaError_t err = cudaStreamSynchronize(h->stream);
+    de.release();
+    dv.release();
+    if (err != cudaSuccess) return fail(MSX_ERR_CUDA, cudaGetErrorString(err));
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_element_reduce(msx_handle *h, int32_t quantity, int32_t op, const int32_t *elems, int64_t n,
+                                         double *value)
+{
+    if (!h || !value) return fail(MSX_ERR_ARG, "bad element reduce arguments");
+    if (op < MSX_OP_MEAN || op > MSX_OP_SUM) return fail(MSX_ERR_ARG, "op must be a msx_element_op");
+    if (quantity == MSX_ELEM_VOLUME && op == MSX_OP_MEAN)
+        return fail(MSX_ERR_ARG, "VOLUME has no Mean (the reference's volume() returns no value for it)");
+    if (elems && n == 0) return fail(MSX_ERR_ARG, "empty element list");
+    // each listed element once, in element order: the reference's selection
+    std::vector<int32_t> set;
+    if (elems && n > 0) {
+        set.assign(elems, elems + n);
+        std::sort(set.begin(), set.end());
+        set.erase(std::unique(set.begin(), set.end()), set.end());
+        n = (int64_t)set.size();
+    }
+    DBuf<int> de;
+    DBuf<double> scratch;
+    msx_status st = element_list(h, quantity, elems ? set.data() : nullptr, n, de);
+    if (st != MSX_OK) {
+        de.release();
+        return st;
+    }
+    if (quantity == MSX_ELEM_EXTERNAL_ENERGY) {   // u . f_ext over every DOF, whatever the operation
+        n = 3 * h->P.nn;
+        op = MSX_OP_SUM;
+    }
+    if (scratch.alloc(element_reduce_scratch()) != cudaSuccess) {
+        de.release();
+        return fail(MSX_ERR_OOM, "element reduce scratch");
+    }
+    bind_problem(h);
+    double *out = scratch.p + element_reduce_scratch() - 1;
+    launch_element_reduce(h->P, quantity, op, elems ? de.p : nullptr, n, h->last_t, scratch.p, out, h->stream);
+    cudaMemcpyAsync(value, out, sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    const cudaError_t err = cudaStreamSynchronize(h->stream);
+    de.release();
+    scratch.release();
+    if (err != cudaSuccess) return fail(MSX_ERR_CUDA, cudaGetErrorString(err));
+    return MSX_OK;
+}
+
 extern "C" msx_status msx_get_state(msx_handle *h, double *u, double *v, double *a)
 {
     if (!h) return fail(MSX_ERR_ARG, "NULL handle");

@@ -44,6 +44,14 @@ class BC_(C.Structure):
 
 
 FIELD_DISPLACEMENT, FIELD_EXTERNAL_FORCE, FIELD_INTERNAL_FORCE = 0, 1, 2
+# element data extraction: quantity names numbered as the reference's
+# ExtractData::ElementDataType, operations as ExtractData::Operation
+ELEMENT_QUANTITIES = (["F" + a + b for a in "XYZ" for b in "XYZ"] + ["P" + a + b for a in "XYZ" for b in "XYZ"] +
+                      ["SVM", "KVM"] + ["INVAR%d" % k for k in range(1, 7)] +
+                      ["DEFO_ENERGY", "EXTERNAL_ENERGY", "KIN_ENERGY", "VOLUME"])
+ELEM = {name: k + 1 for k, name in enumerate(ELEMENT_QUANTITIES)}
+OP_MEAN, OP_MIN, OP_MAX, OP_SUM = 1, 2, 3, 4
+OPS = {"Mean": OP_MEAN, "Min": OP_MIN, "Max": OP_MAX, "Sum": OP_SUM}
 LOAD_FORCE, LOAD_GRAVITY, LOAD_TRACTION_INST, LOAD_TRACTION_RAMP, LOAD_PRESSURE_INST, LOAD_PRESSURE_RAMP = range(6)
 
 
@@ -95,7 +103,7 @@ SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_
            "msx_stream", "msx_set_device", "msx_pool_create", "msx_pool_submit", "msx_pool_step",
            "msx_pool_poll", "msx_pool_fetch", "msx_pool_wait", "msx_pool_destroy", "msx_pool_stats_get",
            "msx_internal_force_noalloc", "msx_initial_dt", "msx_element_fields", "msx_set_loads",
-           "msx_set_load_blocks", "msx_node_values"]
+           "msx_set_load_blocks", "msx_node_values", "msx_element_values", "msx_element_reduce"]
 
 _lib = None
 
@@ -127,6 +135,8 @@ def load(path: str = LIB_PATH):
         "msx_set_loads": [vp, vp, i64, C.c_double, i32],
         "msx_set_load_blocks": [vp, vp, i64],
         "msx_node_values": [vp, i32, i32, vp, i64, vp],
+        "msx_element_values": [vp, i32, vp, i64, vp],
+        "msx_element_reduce": [vp, i32, i32, vp, i64, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -293,6 +303,25 @@ class Solver:
         out = np.zeros(len(n))
         _check(load().msx_node_values(self.h, int(field), int(comp), _p(n), len(n), _p(out)))
         return out
+
+    def element_values(self, quantity, elems=None):
+        """Per-element value of an element-extraction quantity (a name of
+        ELEMENT_QUANTITIES or its number) for the listed elements (None: all)."""
+        q = ELEM[quantity] if isinstance(quantity, str) else int(quantity)
+        e = None if elems is None else np.ascontiguousarray(elems, dtype=np.int32)
+        out = np.zeros(self.ne if e is None else len(e))
+        _check(load().msx_element_values(self.h, q, _p(e), 0 if e is None else len(e), _p(out)))
+        return out
+
+    def element_reduce(self, quantity, op, elems=None):
+        """The value one *EXTRACTION, ELEMENT row holds: quantity as for
+        element_values, op "Mean", "Min", "Max", "Sum" or OP_*."""
+        q = ELEM[quantity] if isinstance(quantity, str) else int(quantity)
+        o = OPS[op] if isinstance(op, str) else int(op)
+        e = None if elems is None else np.ascontiguousarray(elems, dtype=np.int32)
+        out = np.zeros(1)
+        _check(load().msx_element_reduce(self.h, q, o, _p(e), 0 if e is None else len(e), _p(out)))
+        return float(out[0])
 
     def initial_dt(self):
         d = C.c_double()
