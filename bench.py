@@ -140,6 +140,22 @@ def mixed_roofline(ne, nn, prof, ms_per_step):
             "step": {"alg_bytes": alg_step, "achieved": step, "frac": step / peak}}
 
 
+def dword_roofline(ne, nn, prof, ms_per_step):
+    """HBM roofline of the double-word step: per element conn 16 + dphi/dX as (hi, lo) 72 +
+    wJ 8 + FP32 length 4 = 100 B, per node 176 B (the FP64 step's nodal data)."""
+    peak, peak_kind = peaks()
+    alg_elem, alg_step = 100.0 * ne, 100.0 * ne + 176.0 * nn
+    ach = alg_elem / (prof.element_ms * 1e-3) / 1e9
+    step = alg_step / (ms_per_step * 1e-3) / 1e9
+    tr = profiled("dram_bytes_per_element", "element_kernel_dword_cube.md")
+    return {"bound": "hbm", "kernel": "pool_elem_kernel<DW>", "achieved": ach, "peak": peak, "unit": "GB/s",
+            "frac": ach / peak, "peak_kind": peak_kind, "traffic": tr * ne if tr else None,
+            "alg_bytes_per_launch": alg_elem,
+            "step": {"alg_bytes": alg_step, "achieved": step, "frac": step / peak},
+            "note": "FP64's algebra in double-word FP32 arithmetic; rel. L2 of u vs the reference <= 6e-13 "
+                    "on the golden decks (tests/test_gpu_parity.py)"}
+
+
 def run_e2e(X, conn, bcs, steps):
     """Whole job through the C ABI from host buffers: upload, set-up, K steps,
     read back u, v, a.  Inputs come from pinned host memory."""
@@ -363,7 +379,7 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-pool", action="store_true", help="skip the batched and serving variants")
     ap.add_argument("--cube", type=int, default=N_CUBE, help="hexes per cube edge (profiling runs only)")
-    ap.add_argument("--only", choices=["fp64", "mixed", "fp64_exact"], default=None,
+    ap.add_argument("--only", choices=["fp64", "mixed", "fp64_exact", "dword"], default=None,
                     help="time a single variant (profiling runs only)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -385,14 +401,14 @@ def main():
     ne, nn = conn.shape[0], X.shape[1]
 
     barrier(ws)
-    first = {"mixed": msx.MIXED, "fp64_exact": msx.FP64_EXACT}.get(args.only, msx.FP64)
+    first = {"mixed": msx.MIXED, "fp64_exact": msx.FP64_EXACT, "dword": msx.DOUBLE_WORD}.get(args.only, msx.FP64)
     rep, prof, clocks = run_variant(X, conn, bcs, first, args.steps, args.warmup, local)
     secs = reduce_max(rep.device_ms / 1e3, ws)
     value = ws * ne * args.steps / secs
 
     variants = {}
     if not args.no_variants and args.only is None:
-        for name, prec in (("mixed", msx.MIXED), ("fp64_exact", msx.FP64_EXACT)):
+        for name, prec in (("mixed", msx.MIXED), ("double_word", msx.DOUBLE_WORD), ("fp64_exact", msx.FP64_EXACT)):
             r2, p2, c2 = run_variant(X, conn, bcs, prec, args.steps, args.warmup, local)
             s2 = reduce_max(r2.device_ms / 1e3, ws)
             variants[name] = {"value": ws * ne * args.steps / s2, "ms_per_step": 1e3 * s2 / args.steps,
@@ -400,6 +416,8 @@ def main():
                               "clocks": c2}
             if name == "mixed":
                 variants[name]["roofline"] = mixed_roofline(ne, nn, p2, 1e3 * s2 / args.steps)
+            if name == "double_word":
+                variants[name]["roofline"] = dword_roofline(ne, nn, p2, 1e3 * s2 / args.steps)
     if not args.no_pool and args.only is None and args.cube == N_CUBE:
         variants["batched"] = batched_variant()
         variants["serving"] = [serving_variant(lam) for lam in (50, 200, 800)]
@@ -439,7 +457,9 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "element-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "num_elems": ne, "num_nodes": nn, "precision": "FP64",
+            "config": {"workload": WORKLOAD, "num_elems": ne, "num_nodes": nn,
+                       "precision": {"mixed": "MIXED", "fp64_exact": "FP64_EXACT", "dword": "DOUBLE_WORD"}.get(
+                           args.only, "FP64"),
                        "parallelism": "replicas" if ws > 1 else "single", "l2": "inputs larger than L2 "
                        "(element arrays %.2f GB resident)" % (ne * 128 / 1e9)},
             "roofline": roofline, "gpu_launches": rep.kernel_launches, "clocks": clocks, "e2e": e2e,

@@ -47,7 +47,12 @@ enum { MSX_BC_RAMP = 0,      /* *BOUNDARY, TYPE=DISPLACEMENT RAMP: value reached
 
 enum { MSX_PREC_FP64 = 0,        /* plain FP64, FMA-contracted, algebraically simplified laws */
        MSX_PREC_FP64_EXACT = 1,  /* FP64 in the reference's operation order, no contraction   */
-       MSX_PREC_MIXED = 2 };     /* FP32 element kinematics/stress/B^T P; FP64 nodes, J-1, dt  */
+       MSX_PREC_MIXED = 2,       /* FP32 element kinematics/stress/B^T P; FP64 nodes, J-1, dt  */
+       MSX_PREC_DOUBLE_WORD = 3  /* MSX_PREC_FP64's algebra in double-word (FP32 pair, ~48-bit)
+                                    arithmetic on the FP32 pipe, state and corner forces too;
+                                    FP64 CFL check.  Values must stay inside FP32's exponent
+                                    range (|x| < 3e38, and near 1e-38 only as zeros).  Single
+                                    solves only (not msx_pool_*). */ };
 
 typedef struct {
     int64_t num_nodes, num_elems;

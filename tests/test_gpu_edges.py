@@ -7,7 +7,7 @@ import pytest
 import msx
 import oracle as O
 
-MODES = [(msx.FP64_EXACT, 1e-12), (msx.FP64, 1e-10), (msx.MIXED, 1e-5)]
+MODES = [(msx.FP64_EXACT, 1e-12), (msx.FP64, 1e-10), (msx.MIXED, 1e-5), (msx.DOUBLE_WORD, 1e-10)]
 
 
 def rel(x, y):
@@ -64,6 +64,9 @@ def test_chain_changes_precision():
     (u, v, a), steps = run_gpu(mesh, msx.COMPRESSIBLE_NH, solvers, (msx.FP64, msx.MIXED, msx.FP64))
     assert steps == ref.steps
     assert rel(u, ref.u) <= 1e-5
+    (u, v, a), steps = run_gpu(mesh, msx.COMPRESSIBLE_NH, solvers, (msx.DOUBLE_WORD, msx.FP64, msx.DOUBLE_WORD))
+    assert steps == ref.steps
+    assert rel(u, ref.u) <= 1e-10
 
 
 @pytest.mark.gpu

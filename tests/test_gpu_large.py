@@ -33,7 +33,8 @@ def large_reference():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision,tol", [(msx.FP64, 1e-10), (msx.FP64_EXACT, 1e-12), (msx.MIXED, 1e-5)])
+@pytest.mark.parametrize("precision,tol", [(msx.FP64, 1e-10), (msx.FP64_EXACT, 1e-12), (msx.MIXED, 1e-5),
+                                           (msx.DOUBLE_WORD, 1e-10)])
 def test_large_cube_against_oracle(large_reference, precision, tol):
     mesh, bcs, ref = large_reference
     S = msx.Solver(mesh.X, mesh.conn, [(msx.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0)], bcs, 0.0, 1e30, 0.5,

@@ -58,6 +58,16 @@ def test_fp64_mode_matches_reference(name):
     assert rel(v, vr) <= 1e-10
 
 
+@pytest.mark.parametrize("name", names())
+def test_double_word_mode_matches_reference(name):
+    """FP64's algebra in double-word arithmetic: within the FP64 bar of the reference."""
+    (u, v, a), (ur, vr, ar), steps, ref_steps = run_case(name, msx.DOUBLE_WORD)
+    assert steps == ref_steps
+    print("%s: double-word rel L2 u %.2e v %.2e" % (name, rel(u, ur), rel(v, vr)))
+    assert rel(u, ur) <= 1e-10, rel(u, ur)
+    assert rel(v, vr) <= 1e-10
+
+
 @pytest.mark.parametrize("name", [n for n in names() if n.startswith("cube10")])
 def test_mixed_mode_error_bound(name):
     (u, v, a), (ur, vr, ar), steps, ref_steps = run_case(name, msx.MIXED)
@@ -83,7 +93,8 @@ def test_setup_data_bitwise_equal_to_oracle():
 
 
 @pytest.mark.parametrize("law", [msx.NEO_HOOKEAN, msx.COMPRESSIBLE_NH, msx.STVK])
-@pytest.mark.parametrize("precision,tol", [(msx.FP64_EXACT, 0.0), (msx.FP64, 1e-12), (msx.MIXED, 2e-5)])
+@pytest.mark.parametrize("precision,tol", [(msx.FP64_EXACT, 0.0), (msx.FP64, 1e-12), (msx.MIXED, 2e-5),
+                                           (msx.DOUBLE_WORD, 1e-11)])
 def test_internal_force_matches_oracle(law, precision, tol):
     X, conn = msx.mesh_cube(5, seed=7)
     mesh = O.Mesh(X, conn)
@@ -110,7 +121,7 @@ def test_runs_are_deterministic():
     assert all(np.array_equal(x, y) for x, y in zip(*outs))
 
 
-@pytest.mark.parametrize("precision,tol", [(msx.FP64, 1e-10), (msx.MIXED, 1e-5)])
+@pytest.mark.parametrize("precision,tol", [(msx.FP64, 1e-10), (msx.MIXED, 1e-5), (msx.DOUBLE_WORD, 1e-10)])
 def test_velocity_ramp_extension_matches_oracle(precision, tol):
     n = 8
     X, conn = msx.mesh_cube(n)
@@ -205,7 +216,8 @@ def test_surface_load_errors():
     S.close()
 
 
-@pytest.mark.parametrize("precision,tol", [(msx.FP64_EXACT, 1e-12), (msx.FP64, 1e-10), (msx.MIXED, 2e-5)])
+@pytest.mark.parametrize("precision,tol", [(msx.FP64_EXACT, 1e-12), (msx.FP64, 1e-10), (msx.MIXED, 2e-5),
+                                           (msx.DOUBLE_WORD, 1e-10)])
 def test_node_values_match_oracle(precision, tol):
     """msx_node_values: displacement, internal force (element-order sum) and
     external force of the last step, against the oracle at that state."""
@@ -255,7 +267,7 @@ def test_element_values_match_oracle(name):
     S.close()
 
 
-@pytest.mark.parametrize("precision", [msx.FP64_EXACT, msx.FP64, msx.MIXED])
+@pytest.mark.parametrize("precision", [msx.FP64_EXACT, msx.FP64, msx.MIXED, msx.DOUBLE_WORD])
 def test_element_reduce_matches_oracle(precision):
     """msx_element_reduce for every quantity and operation, over all elements
     and over a list with repeats in no order, against the oracle's reference-

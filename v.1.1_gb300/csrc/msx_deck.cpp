@@ -487,7 +487,9 @@ int main(int argc, char **argv)
         else if (a == "-parse-only") parse_only = true;
         else if (a == "-precision") {
             std::string p = next();
-            precision = p == "exact" ? MSX_PREC_FP64_EXACT : (p == "mixed" ? MSX_PREC_MIXED : MSX_PREC_FP64);
+            precision = p == "exact" ? MSX_PREC_FP64_EXACT
+                        : p == "mixed" ? MSX_PREC_MIXED
+                        : p == "dword" ? MSX_PREC_DOUBLE_WORD : MSX_PREC_FP64;
         }
     }
     if (input.empty()) {

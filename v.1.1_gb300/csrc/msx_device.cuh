@@ -460,7 +460,7 @@ __device__ __forceinline__ void node_step(const Problem &p, int parity, NodeStep
     ns.hdt = 0.5 * cp.dt;
     ns.dtn = d.next.dt;
     ns.hdtn = 0.5 * ns.dtn;
-    if (MODE == MODE_MIXED) {
+    if (MODE == MODE_MIXED || MODE == MODE_DW) {
         ns.hdt2 = df_from(ns.hdt);
         ns.dtn2 = df_from(ns.dtn);
         ns.hdtn2 = df_from(ns.hdtn);
@@ -1137,6 +1137,382 @@ static __global__ void __launch_bounds__(kElemBlock) elem_force_kernel_mixed(Pro
 }
 
 
+// ---------------------------------------------------------------------------
+// Double-word mode: the algebra of elem_body_fp64 (F from node differences,
+// the laws through cof(F), B^T P with wJ folded in) evaluated in double-word
+// arithmetic on the FP32 pipe, with the nodal state and the corner forces as
+// double-words too.  A double-word operation costs 4-20 FP32 operations and
+// carries about 2^-47 relative error against FP64's 2^-53; on this GPU the
+// FP64 pipe issues 1/64 of the FP32 rate, so the element work runs several
+// times faster than in FP64 while results stay within a few 1e-13 of it.
+// The error-free pieces (TwoSum, Fast2Sum, the FMA product split) use the
+// _rn intrinsics, which the compiler never fuses into an FMA.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float dw_err(float a, float b, float s)   // a + b - s for s = fl(a + b)
+{
+    const float bb = __fsub_rn(s, a);
+    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ float2 dw_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    return make_float2(s, dw_err(a, b, s));
+}
+
+__device__ __forceinline__ float2 dw_fast(float a, float b)   // |a| >= |b| or a = 0
+{
+    const float s = __fadd_rn(a, b);
+    return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+
+__device__ __forceinline__ float2 dw_neg(float2 x) { return make_float2(-x.x, -x.y); }
+__device__ __forceinline__ float2 dw_scale2(float2 x, float p2) { return make_float2(x.x * p2, x.y * p2); }  // p2 = 2^k
+
+// Joldes, Muller, Popescu (2017) Alg. 6 (accurate sum), Alg. 12 (product),
+// Alg. 4 (double-word + FP32), Alg. 9 (double-word * FP32).
+__device__ __forceinline__ float2 dw_add(float2 x, float2 y)
+{
+    const float2 s = dw_two_sum(x.x, y.x), t = dw_two_sum(x.y, y.y);
+    const float2 v = dw_fast(s.x, __fadd_rn(s.y, t.x));
+    return dw_fast(v.x, __fadd_rn(t.y, v.y));
+}
+
+// x + y with absolute error a few 2^-48 (|x| + |y|) (the "sloppy" sum, JMP
+// Alg. 5): enough where the inputs' own rounding is of that size, as for node
+// differences and sums of corner forces; no bound relative to |x + y|.
+__device__ __forceinline__ float2 dw_add_sloppy(float2 x, float2 y)
+{
+    const float2 s = dw_two_sum(x.x, y.x);
+    return dw_fast(s.x, __fadd_rn(s.y, __fadd_rn(x.y, y.y)));
+}
+
+__device__ __forceinline__ float2 dw_mul(float2 x, float2 y)
+{
+    const float ch = __fmul_rn(x.x, y.x);
+    const float cl1 = fmaf(x.x, y.x, -ch);
+    const float cl2 = fmaf(x.y, y.x, fmaf(x.x, y.y, __fmul_rn(x.y, y.y)));
+    return dw_fast(ch, __fadd_rn(cl1, cl2));
+}
+
+__device__ __forceinline__ float2 dw_add_f(float2 x, float y)
+{
+    const float2 s = dw_two_sum(x.x, y);
+    return dw_fast(s.x, __fadd_rn(x.y, s.y));
+}
+
+__device__ __forceinline__ float2 dw_mul_f(float2 x, float y)
+{
+    const float ch = __fmul_rn(x.x, y);
+    return dw_fast(ch, fmaf(x.y, y, fmaf(x.x, y, -ch)));
+}
+
+__device__ __forceinline__ float2 dw_from(double x)
+{
+    const float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+
+// Compensated dot products of double-words (Ogita, Rump, Oishi, "Accurate sum
+// and dot product", SIAM J. Sci. Comput. 26 (2005), Dot2, with the low words'
+// cross terms): each hi*hi product is split exactly by an FMA and summed with
+// TwoSum; the product and sum errors and the hi*lo terms gather in one FP32
+// correction c.  Result s + c by Fast2Sum (exact unless the sum cancels below
+// |c|, where its error is still of the order 2^-48 sum |a_k b_k|); error a few
+// 2^-48 sum |a_k b_k|, the size of FP64's 2^-53 sum |a_k b_k| times ~30.
+__device__ __forceinline__ void dw_acc(float &s, float &c, float2 x, float2 y)
+{
+    const float p = __fmul_rn(x.x, y.x);
+    c = fmaf(x.y, y.x, fmaf(x.x, y.y, c + fmaf(x.x, y.x, -p)));
+    const float t = __fadd_rn(s, p);
+    c += dw_err(s, p, t);
+    s = t;
+}
+
+__device__ __forceinline__ float2 dw_dot2(float2 a0, float2 b0, float2 a1, float2 b1)
+{
+    float s = __fmul_rn(a0.x, b0.x);
+    float c = fmaf(a0.y, b0.x, fmaf(a0.x, b0.y, fmaf(a0.x, b0.x, -s)));
+    dw_acc(s, c, a1, b1);
+    return dw_fast(s, c);
+}
+
+// init + a0 b0 + a1 b1 + a2 b2 (init an FP32 constant, e.g. the identity's 1)
+__device__ __forceinline__ float2 dw_dot3(float2 a0, float2 b0, float2 a1, float2 b1, float2 a2, float2 b2,
+                                          float init)
+{
+    float s, c;
+    if (init == 0.0f) {   // a constant at every call: resolved at compile time
+        s = __fmul_rn(a0.x, b0.x);
+        c = fmaf(a0.y, b0.x, fmaf(a0.x, b0.y, fmaf(a0.x, b0.x, -s)));
+    } else {
+        s = init;
+        c = 0.0f;
+        dw_acc(s, c, a0, b0);
+    }
+    dw_acc(s, c, a1, b1);
+    dw_acc(s, c, a2, b2);
+    return dw_fast(s, c);
+}
+
+// ln(1 + x) for a double-word x.  For |x| < 2^-7: x - x^2/2 + x^3/3 in
+// double-words plus the tail x^4 (-1/4 + x/5 - x^2/6 + x^3/7 - x^4/8) in FP32
+// (|tail| < 2^-21 |x|, so its FP32 rounding stays below 2^-45 |x|; the next
+// term is below 2^-56 |x|).  Otherwise the FP64 library log.
+__device__ __forceinline__ float2 dw_log1p(float2 x)
+{
+    if (!(fabsf(x.x) < 0.0078125f)) return dw_from(log(1.0 + ((double)x.x + (double)x.y)));
+    const float2 third = make_float2(0x1.555556p-2f, -0x1.555556p-27f);
+    const float2 x2 = dw_mul(x, x), x3 = dw_mul(x2, x);
+    const float2 lead = dw_add(dw_add(x, dw_scale2(x2, -0.5f)), dw_mul(x3, third));
+    const float xf = x.x;
+    const float tail = (x2.x * x2.x) * fmaf(xf, fmaf(xf, fmaf(xf, fmaf(xf, -0.125f, 1.0f / 7.0f), -1.0f / 6.0f), 0.2f), -0.25f);
+    return dw_add_f(lead, tail);
+}
+
+// 1 / y: one Newton step from the FP32 reciprocal.
+__device__ __forceinline__ float2 dw_rcp(float2 y)
+{
+    const float r0 = __frcp_rn(y.x);
+    const float2 p = dw_mul_f(y, r0);                       // y r0 = 1 - e
+    const float e = __fsub_rn(__fsub_rn(1.0f, p.x), p.y);
+    return dw_fast(r0, __fmul_rn(r0, e));
+}
+
+// wJ * P through the cofactor, as stress_fast does in FP64.
+__device__ __forceinline__ void stress_dw(const MatParams &m, const float2 *F, float2 wJ, float2 *P)
+{
+    if (m.law == 2) {
+        // S = mu2 E + lam tr(E) I with E = (F^T F - I)/2; C_ii - 1 from the dot's initial -1
+        const float2 C00 = dw_dot3(F[0], F[0], F[3], F[3], F[6], F[6], -1.0f);
+        const float2 C11 = dw_dot3(F[1], F[1], F[4], F[4], F[7], F[7], -1.0f);
+        const float2 C22 = dw_dot3(F[2], F[2], F[5], F[5], F[8], F[8], -1.0f);
+        const float2 C01 = dw_dot3(F[0], F[1], F[3], F[4], F[6], F[7], 0.0f);
+        const float2 C02 = dw_dot3(F[0], F[2], F[3], F[5], F[6], F[8], 0.0f);
+        const float2 C12 = dw_dot3(F[1], F[2], F[4], F[5], F[7], F[8], 0.0f);
+        const float2 trE = dw_scale2(dw_add(dw_add(C00, C11), C22), 0.5f);
+        const float2 h = dw_scale2(dw_mul(m.mu2_w, wJ), 0.5f), dg = dw_mul(dw_mul(m.lam_stvk_w, trE), wJ);
+        const float2 S00 = dw_add(dw_mul(h, C00), dg), S11 = dw_add(dw_mul(h, C11), dg),
+                     S22 = dw_add(dw_mul(h, C22), dg);
+        const float2 S01 = dw_mul(h, C01), S02 = dw_mul(h, C02), S12 = dw_mul(h, C12);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float2 f0 = F[i * 3], f1 = F[i * 3 + 1], f2 = F[i * 3 + 2];
+            P[i * 3 + 0] = dw_dot3(f0, S00, f1, S01, f2, S02, 0.0f);
+            P[i * 3 + 1] = dw_dot3(f0, S01, f1, S11, f2, S12, 0.0f);
+            P[i * 3 + 2] = dw_dot3(f0, S02, f1, S12, f2, S22, 0.0f);
+        }
+        return;
+    }
+    float2 K[9];
+    K[0] = dw_dot2(F[4], F[8], dw_neg(F[5]), F[7]);
+    K[1] = dw_dot2(F[5], F[6], dw_neg(F[3]), F[8]);
+    K[2] = dw_dot2(F[3], F[7], dw_neg(F[4]), F[6]);
+    K[3] = dw_dot2(F[2], F[7], dw_neg(F[1]), F[8]);
+    K[4] = dw_dot2(F[0], F[8], dw_neg(F[2]), F[6]);
+    K[5] = dw_dot2(F[1], F[6], dw_neg(F[0]), F[7]);
+    K[6] = dw_dot2(F[1], F[5], dw_neg(F[2]), F[4]);
+    K[7] = dw_dot2(F[2], F[3], dw_neg(F[0]), F[5]);
+    K[8] = dw_dot2(F[0], F[4], dw_neg(F[1]), F[3]);
+    const float2 J = dw_dot3(F[0], K[0], F[1], K[1], F[2], K[2], 0.0f);
+    const float2 x = dw_add_f(J, -1.0f);   // J - 1
+    const float2 iJ = dw_rcp(J);
+    float2 a1, g;
+    if (m.law == 1) {
+        // P = mu F + (lambda ln J - mu) cof(F) / J
+        a1 = dw_mul(m.mu_w, wJ);
+        g = dw_mul(dw_mul(dw_add(dw_mul(m.lambda_w, dw_log1p(x)), dw_neg(m.mu_w)), iJ), wJ);
+    } else {
+        // P = mu J^-2/3 F + (-mu/3 trB J^-5/3 + K1 (J-1)) cof(F); J^-2/3 from the FP64 library
+        const double r = rcbrt((double)J.x + (double)J.y);
+        const float2 j23 = dw_from(r * r);
+        const float2 trB = dw_add(dw_add(dw_dot3(F[0], F[0], F[1], F[1], F[2], F[2], 0.0f),
+                                         dw_dot3(F[3], F[3], F[4], F[4], F[5], F[5], 0.0f)),
+                                  dw_dot3(F[6], F[6], F[7], F[7], F[8], F[8], 0.0f));
+        a1 = dw_mul(dw_mul(m.mu_w, j23), wJ);
+        g = dw_mul(dw_add(dw_neg(dw_mul(dw_mul(dw_mul(m.mu3_w, trB), j23), iJ)), dw_mul(m.K1_w, x)), wJ);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) P[k] = dw_dot2(a1, F[k], g, K[k]);
+}
+
+// Exact FP64 CFL value of one element from the double-word displacement.
+static __device__ __noinline__ double cfl_dw(const Problem &p, long long e)
+{
+    const long long nn = p.nn;
+    int4 cn = p.conn[e];
+    int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    double x[4][3];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float2 w = p.uhl[k * nn + nd[a]];
+            x[a][k] = p.X[k * nn + nd[a]] + ((double)w.x + (double)w.y);
+        }
+    double e1[3], e2[3], e3[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        e1[k] = x[1][k] - x[0][k];
+        e2[k] = x[2][k] - x[0][k];
+        e3[k] = x[3][k] - x[0][k];
+    }
+    double dist = char_length_edges<double>(e1, e2, e3);
+    double Lr = p.Lref[e];
+    return ((dist < Lr) ? dist : Lr) / mat_of(p, e).c;
+}
+
+template <bool FORCE_ONLY>
+__device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int parity)
+{
+    const long long ne = p.ne, nn = p.nn;
+    int4 cn = p.conn[e];
+    int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    float2 G[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) G[k] = make_float2(__ldg(p.G32 + k * ne + e), __ldg(p.G32lo + k * ne + e));
+    float2 u0[3], du[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++) u0[i] = p.uhl[nd[0] + i * nn];
+#pragma unroll
+    for (int a = 1; a < 4; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) du[(a - 1) * 3 + i] = dw_add_sloppy(p.uhl[nd[a] + i * nn], dw_neg(u0[i]));
+    float2 F[9], P[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+            F[i * 3 + j] = dw_dot3(du[i], G[j], du[3 + i], G[3 + j], du[6 + i], G[6 + j], i == j ? 1.0f : 0.0f);
+    const MatParams &m = mat_of(p, e);
+    stress_dw(m, F, make_float2(__ldg(p.wJ32 + e), __ldg(p.wJ32lo + e)), P);
+    float2 f[12];
+#pragma unroll
+    for (int a = 1; a < 4; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            f[a * 3 + i] = dw_dot3(P[i * 3], G[(a - 1) * 3], P[i * 3 + 1], G[(a - 1) * 3 + 1], P[i * 3 + 2],
+                                   G[(a - 1) * 3 + 2], 0.0f);
+#pragma unroll
+    for (int i = 0; i < 3; i++) f[i] = dw_neg(dw_add_sloppy(dw_add_sloppy(f[3 + i], f[6 + i]), f[9 + i]));
+    const int4 sl = __ldg(p.slot + e);
+    const int ks[4] = {sl.x, sl.y, sl.z, sl.w};
+    float2 *fe = reinterpret_cast<float2 *>(p.fe);
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        float2 *fk = fe + (long long)ks[a] * 3;
+        fk[0] = f[a * 3];
+        fk[1] = f[a * 3 + 1];
+        fk[2] = f[a * 3 + 2];
+    }
+    if (FORCE_ONLY) return 0.0f;
+    if (e == 0 && !isfinite(p.uhl[1].x)) atomicOr(p.flags + (parity ^ 1), 1);
+    float du32[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) du32[k] = du[k].x;
+    return cfl_screen(p, e, du32, m);
+}
+
+// corner forces only (internal-force hook)
+static __global__ void __launch_bounds__(kElemBlock) elem_force_kernel_dw(Problem p, int parity)
+{
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < p.ne) elem_body_dw<true>(p, e, parity);
+}
+
+// Node body of the double-word mode: the mixed mode's four-lane gather and
+// update, with double-word corner forces summed as (s, c): s the FP32 sum of
+// the high words by TwoSum, c the rounding errors plus the low words.
+__device__ __forceinline__ void dw_sum_merge(float &s, float &c, float s2, float c2)
+{
+    const float t = __fadd_rn(s, s2);
+    c = c + c2 + dw_err(s, s2, t);
+    s = t;
+}
+
+__device__ __forceinline__ void node_quad_dw(const Problem &p, long long i, bool valid, const NodeStep &ns)
+{
+    const int q = threadIdx.x & 3;
+    const bool odd = q & 1;
+    const bool own = valid && q < 3;
+    const long long dof = i + (long long)q * p.nn;
+    float2 uq = make_float2(0.f, 0.f), vq = uq, aq = uq, minv = uq;
+    int rec = -1;
+    if (own) {
+        uq = p.uhl[dof];
+        vq = p.vhl[dof];
+        aq = p.ahl[dof];
+        minv = p.minv2[i];
+        rec = p.node_bc[i];
+    }
+    int k0 = 0, k1 = 0;
+    if (valid && ns.ran) {
+        k0 = p.node_ptr[i];
+        k1 = p.node_ptr[i + 1];
+    }
+    const float2 *fe = reinterpret_cast<const float2 *>(p.fe);
+    float h0 = 0.f, h1 = 0.f, h2 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
+    int k = k0 + q;
+    if (k < k1) {
+        const float2 *f = fe + (long long)k * 3;
+        const float2 f0 = f[0], f1 = f[1], f2 = f[2];
+        h0 = f0.x, c0 = f0.y;
+        h1 = f1.x, c1 = f1.y;
+        h2 = f2.x, c2 = f2.y;
+        k += 4;
+    }
+    for (; k < k1; k += 4) {
+        const float2 *f = fe + (long long)k * 3;
+        const float2 f0 = f[0], f1 = f[1], f2 = f[2];
+        dw_sum_merge(h0, c0, f0.x, f0.y);
+        dw_sum_merge(h1, c1, f1.x, f1.y);
+        dw_sum_merge(h2, c2, f2.x, f2.y);
+    }
+    float ah = odd ? h0 : h1, ac = odd ? c0 : c1;
+    float xh = __shfl_xor_sync(0xffffffffu, ah, 1), xc = __shfl_xor_sync(0xffffffffu, ac, 1);
+    float yh = __shfl_xor_sync(0xffffffffu, h2, 1), yc = __shfl_xor_sync(0xffffffffu, c2, 1);
+    if (odd) {
+        dw_sum_merge(h1, c1, xh, xc);
+    } else {
+        dw_sum_merge(h0, c0, xh, xc);
+        dw_sum_merge(h2, c2, yh, yc);
+    }
+    float sh = odd ? h1 : (q == 0 ? h2 : h0), sc = odd ? c1 : (q == 0 ? c2 : c0);
+    float zh = __shfl_xor_sync(0xffffffffu, sh, 2), zc = __shfl_xor_sync(0xffffffffu, sc, 2);
+    float mh = pick3(q, h0, h1, h2), mc = pick3(q, c0, c1, c2);
+    dw_sum_merge(mh, mc, zh, zc);
+    if (!own) return;
+    const float2 s = dw_two_sum(mh, mc);
+    const int2 br = rec >= 0 ? p.bc_rec[rec * 3 + q] : make_int2(0, 0);
+    const bool act = br.y == 0;
+    bool changed = false;
+    if (ns.ran && act) {
+        const float2 f = ns.loads ? dw_add(dw_from(node_fext(p, i, q, ns)), dw_neg(s)) : dw_neg(s);
+        const float2 an = dw_mul(f, minv);
+        vq = dw_add(vq, dw_mul(ns.hdt2, dw_add(aq, an)));
+        aq = an;
+        changed = true;
+    }
+    if (ns.run) {
+        if (act) {
+            uq = dw_add(uq, dw_mul(ns.dtn2, dw_add(vq, dw_mul(ns.hdtn2, aq))));
+        } else {
+            for (int k = br.x; k < br.x + br.y; k++) {
+                const float2 Ud = dw_from(bc_increment(p.bcs[k], ns.dtn, ns.step));
+                uq = dw_add(uq, Ud);
+                vq = Ud;
+                aq = make_float2(0.f, 0.f);
+            }
+        }
+        changed = true;
+    }
+    if (changed) {
+        p.uhl[dof] = uq;
+        p.vhl[dof] = vq;
+        p.ahl[dof] = aq;
+    }
+}
+
 // Block-wide min of a float, returned to every thread of the block.
 __device__ __forceinline__ float block_min_bcast(float v)
 {
@@ -1204,6 +1580,7 @@ __global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *
             for (long long b = tl.begin; b < tl.end; b += per) {
                 long long i = b + (threadIdx.x >> 2);
                 if (MODE == MODE_MIXED) node_quad_mixed(p, i, i < tl.end, ns);
+                else if (MODE == MODE_DW) node_quad_dw(p, i, i < tl.end, ns);
                 else node_quad_fp64(p, i, i < tl.end, ns);
             }
         }
@@ -1215,17 +1592,19 @@ __global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *
     q.finish();
 }
 
-// Element kernel over tiles.  FP64: every element's FP32 CFL screen value is
-// kept in shared memory; after the tile's FP32 minimum is known, elements
-// within 2^-8 of it (and slivers) recompute the exact FP64 value, whose
-// minimum goes to the solve's CFL slot.  Mixed: the FP32 minimum itself.
+// Element kernel over tiles.  FP64 and double-word: every element's FP32 CFL
+// screen value is kept in shared memory; after the tile's FP32 minimum is
+// known, elements within 2^-8 of it (and slivers) recompute the exact FP64
+// value, whose minimum goes to the solve's CFL slot.  Mixed: the FP32 minimum
+// itself.
 template <int MODE>
-__global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : 2) pool_elem_kernel(const Problem *__restrict__ descs,
+__global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE == MODE_DW ? 3 : 2)) pool_elem_kernel(const Problem *__restrict__ descs,
                                                                  const Tile *__restrict__ tiles,
                                                                  int *__restrict__ sched, int parity)
 {
     __shared__ float sdt[MODE == MODE_MIXED ? 1 : kMaxTileElems];
-    __shared__ int s_tile;
+    __shared__ unsigned short scand[MODE == MODE_MIXED ? 1 : kMaxTileElems];
+    __shared__ int s_tile, s_ncand;
     TileQueue q{sched, sched[0]};
     if (threadIdx.x == 0) s_tile = q.claim();
     __syncthreads();
@@ -1236,9 +1615,12 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : 2) pool
         const Tile tl = tiles[t];
         const Problem &p = descs[tl.solve];
         if (p.ctrl[parity].ran) {
+            if (MODE != MODE_MIXED && threadIdx.x == 0) s_ncand = 0;
             float v32 = INFINITY;
             for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
-                float d = MODE == MODE_MIXED ? elem_body_mixed<false>(p, e, parity) : elem_body_fp64<false>(p, e, parity);
+                float d = MODE == MODE_MIXED ? elem_body_mixed<false>(p, e, parity)
+                                             : (MODE == MODE_DW ? elem_body_dw<false>(p, e, parity)
+                                                                : elem_body_fp64<false>(p, e, parity));
                 if (MODE != MODE_MIXED) sdt[e - tl.begin] = d;
                 if (d >= 0.0f) v32 = fminf(v32, d);
             }
@@ -1247,11 +1629,19 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : 2) pool
                 if (threadIdx.x == 0 && bmin < INFINITY)
                     atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong((double)bmin));
             } else {
+                // the tile's candidates are listed first and then recomputed by
+                // consecutive threads, so a few candidates take one warp, not several
                 const float thr = bmin * (1.0f + 1.0f / 256.0f);
-                double v = INFINITY;
                 for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
                     float d = sdt[e - tl.begin];
-                    if (d < 0.0f || d <= thr) v = fmin(v, cfl_fp64(p, e));
+                    if (d < 0.0f || d <= thr) scand[atomicAdd(&s_ncand, 1)] = (unsigned short)(e - tl.begin);
+                }
+                __syncthreads();
+                const int nc = s_ncand;
+                double v = INFINITY;
+                for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+                    const long long e = tl.begin + scand[c];
+                    v = fmin(v, MODE == MODE_DW ? cfl_dw(p, e) : cfl_fp64(p, e));
                 }
                 block_min_to(v, p.dtmin + (parity ^ 1));
             }
@@ -1304,10 +1694,12 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
         double g = 0.0 + iJ[k];
         G[k * ne + e] = g;
         G32[k * ne + e] = (float)g;
+        if (p.G32lo) const_cast<float *>(p.G32lo)[k * ne + e] = (float)(g - (double)(float)g);
     }
     double w = 0.166666666667 * fabs(J);
     wJ[e] = w;
     wJ32[e] = (float)w;
+    if (p.wJ32lo) const_cast<float *>(p.wJ32lo)[e] = (float)(w - (double)(float)w);
     double L = char_length_ref(pts);
     Lref[e] = L;
     Lref32[e] = (float)L;
@@ -1445,7 +1837,10 @@ __global__ void node_values_kernel(Problem p, int mode, int field, int comp, con
         for (int k = p.node_ptr[i]; k < p.node_ptr[i + 1]; k++) {
             if (mode == MODE_EXACT) v += p.fe[(long long)p.node_inc[k] * 3 + comp];
             else if (mode == MODE_MIXED) v += (double)p.fe32[(long long)k * 4 + comp];
-            else v += p.fe[(long long)k * 3 + comp];
+            else if (mode == MODE_DW) {
+                const float2 w = reinterpret_cast<const float2 *>(p.fe)[(long long)k * 3 + comp];
+                v += (double)w.x + (double)w.y;
+            } else v += p.fe[(long long)k * 3 + comp];
         }
     }
     out[j] = v;
@@ -1731,7 +2126,16 @@ __global__ void gather_kernel(Problem p, double *fint)
         // reference-order corner forces are in element order, the others in CSR slots
         long long inc = MODE == MODE_EXACT ? p.node_inc[k] : k;
 #pragma unroll
-        for (int c = 0; c < 3; c++) s[c] += MODE == MODE_MIXED ? (double)p.fe32[inc * 4 + c] : p.fe[inc * 3 + c];
+        for (int c = 0; c < 3; c++) {
+            if (MODE == MODE_MIXED) {
+                s[c] += (double)p.fe32[inc * 4 + c];
+            } else if (MODE == MODE_DW) {
+                const float2 w = reinterpret_cast<const float2 *>(p.fe)[inc * 3 + c];
+                s[c] += (double)w.x + (double)w.y;
+            } else {
+                s[c] += p.fe[inc * 3 + c];
+            }
+        }
     }
 #pragma unroll
     for (int c = 0; c < 3; c++) fint[i + c * p.nn] = s[c];

@@ -1,5 +1,5 @@
-// msx_fast.cu -- FP64 (contracted, simplified algebra) and mixed-precision
-// kernels.  The tiled step kernels are instantiated here only, so a single
+// msx_fast.cu -- FP64 (contracted, simplified algebra), double-word and
+// mixed-precision kernels.  The tiled step kernels are instantiated here only, so a single
 // solve (msx_run) and the pool execute the same machine code.
 #include "msx_device.cuh"
 
@@ -17,11 +17,19 @@ void launch_internal_force_mixed(const Problem &p, double *fint, cudaStream_t s)
     gather_kernel<MODE_MIXED><<<grid_for(p.nn, 256), 256, 0, s>>>(p, fint);
 }
 
+void launch_internal_force_dw(const Problem &p, double *fint, cudaStream_t s)
+{
+    elem_force_kernel_dw<<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, 0);
+    gather_kernel<MODE_DW><<<grid_for(p.nn, 256), 256, 0, s>>>(p, fint);
+}
+
 void launch_tiled_node(const Problem *descs, const Tile *ntiles, int *counts, int mode, int parity, int grid,
                        int threads, cudaStream_t s)
 {
     if (mode == MODE_MIXED)
         pool_node_kernel<MODE_MIXED><<<grid, threads, 0, s>>>(descs, ntiles, counts + 3, parity);
+    else if (mode == MODE_DW)
+        pool_node_kernel<MODE_DW><<<grid, threads, 0, s>>>(descs, ntiles, counts + 3, parity);
     else
         pool_node_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, ntiles, counts + 3, parity);
 }
@@ -31,6 +39,8 @@ void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, in
 {
     if (mode == MODE_MIXED)
         pool_elem_kernel<MODE_MIXED><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
+    else if (mode == MODE_DW)
+        pool_elem_kernel<MODE_DW><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
     else
         pool_elem_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
 }
@@ -81,6 +91,9 @@ int tiled_ctas_per_sm(int mode, int threads, bool node)
     if (mode == MODE_MIXED)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, node ? (const void *)pool_node_kernel<MODE_MIXED>
                                                                : (const void *)pool_elem_kernel<MODE_MIXED>, threads, 0);
+    else if (mode == MODE_DW)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, node ? (const void *)pool_node_kernel<MODE_DW>
+                                                               : (const void *)pool_elem_kernel<MODE_DW>, threads, 0);
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, node ? (const void *)pool_node_kernel<MODE_FP64>
                                                                : (const void *)pool_elem_kernel<MODE_FP64>, threads, 0);

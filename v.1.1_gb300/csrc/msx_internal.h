@@ -12,7 +12,7 @@ constexpr int kMaxMats = 16;
 constexpr int kElemBlock = 256;   // element-kernel CTA (one element per thread)
 constexpr int kNodeBlock = 256;   // node-kernel CTA (one node per thread)
 
-enum Mode { MODE_FP64 = 0, MODE_EXACT = 1, MODE_MIXED = 2 };
+enum Mode { MODE_FP64 = 0, MODE_EXACT = 1, MODE_MIXED = 2, MODE_DW = 3 };
 
 // Material constants, derived on the host the way the reference's law
 // constructors do (hyperElasticNeoHookean.cpp:23-33,203-215,
@@ -24,6 +24,7 @@ struct MatParams {
     double mu2, lam_stvk;         // StVK: E/(1+nu), E nu/((1+nu)(1-2nu))
     double c;                     // sound speed used by the CFL
     float lambda_f, mu_f, K1_f, mu2_f, lam_stvk_f, inv_c_f;
+    float2 lambda_w, mu_w, K1_w, mu2_w, lam_stvk_w, mu3_w;   // double-word copies (mu3 = mu/3)
 };
 
 // One Dirichlet entry; `val` is what classDirichlet stores
@@ -83,6 +84,7 @@ struct Problem {
     const double *Lref;
     const float *G32, *wJ32, *Lref32;       // FP32 copies (mixed mode)
     const float *Eref32;      // 9*ne reference edge vectors X_a - X_0 (FP32 CFL screen of the FP64 mode)
+    const float *G32lo, *wJ32lo;  // low words: G32 + G32lo and wJ32 + wJ32lo as double-words (double-word mode)
     const unsigned char *mat; // per-element material id, or nullptr
     int nmat;
     MatParams mats[kMaxMats];
@@ -97,7 +99,9 @@ struct Problem {
     const float2 *minv2;      // 1/mass as an (hi, lo) pair
     // corner forces.  Reference-order mode: fe[(e*4 + a)*3 + i] (element
     // order).  FP64 and mixed modes: in the node's CSR slot k = slot[e].a,
-    // fe[k*3 + i] and fe32[k*4 + i] (16-byte slots), so a node's corner forces are contiguous.
+    // fe[k*3 + i] and fe32[k*4 + i] (16-byte slots), so a node's corner forces
+    // are contiguous.  Double-word mode: fe's bytes hold float2 (hi, lo) pairs,
+    // ((float2 *)fe)[k*3 + i].
     double *fe;
     float *fe32;
     // node -> (element, corner) incidences sorted by element id
@@ -194,5 +198,6 @@ long long element_reduce_scratch();
 void launch_internal_force_exact(const Problem &p, double *fint, cudaStream_t s);
 void launch_internal_force_fp64(const Problem &p, double *fint, cudaStream_t s);
 void launch_internal_force_mixed(const Problem &p, double *fint, cudaStream_t s);
+void launch_internal_force_dw(const Problem &p, double *fint, cudaStream_t s);
 
 }  // namespace msx

@@ -98,7 +98,7 @@ struct msx_handle {
     // owned device storage
     DBuf<int4> conn, slot;
     DBuf<double> G, wJ, Lref, X, u, v, a, mass, minv, fe;
-    DBuf<float> G32, wJ32, Lref32, Eref32, fe32;
+    DBuf<float> G32, wJ32, Lref32, Eref32, fe32, G32lo, wJ32lo;
     DBuf<float2> uhl, vhl, ahl, minv2;
     DBuf<unsigned char> mat;
     DBuf<int> node_ptr, node_inc, node_bc;
@@ -164,6 +164,13 @@ static msx_status make_material(const msx_material &m, MatParams &o)
     o.mu2_f = (float)o.mu2;
     o.lam_stvk_f = (float)o.lam_stvk;
     o.inv_c_f = (float)(1.0 / o.c);
+    auto dw = [](double x) { const float hi = (float)x; return make_float2(hi, (float)(x - (double)hi)); };
+    o.lambda_w = dw(o.lambda);
+    o.mu_w = dw(o.mu);
+    o.K1_w = dw(o.K1);
+    o.mu2_w = dw(o.mu2);
+    o.lam_stvk_w = dw(o.lam_stvk);
+    o.mu3_w = dw(o.mu / 3.0);
     return MSX_OK;
 }
 
@@ -217,6 +224,8 @@ static void bind_problem(msx_handle *h)
     P.wJ32 = h->wJ32.p;
     P.Lref32 = h->Lref32.p;
     P.Eref32 = h->Eref32.p;
+    P.G32lo = h->G32lo.p;
+    P.wJ32lo = h->wJ32lo.p;
     P.X = h->X.p;
     P.u = h->u.p;
     P.v = h->v.p;
@@ -256,13 +265,23 @@ static msx_status set_mode(msx_handle *h, int precision)
     case MSX_PREC_FP64: h->tiled = true; break;
     case MSX_PREC_FP64_EXACT: h->tiled = false; h->node = launch_node_exact; h->elem = launch_elem_exact; break;
     case MSX_PREC_MIXED: h->tiled = true; break;
+    case MSX_PREC_DOUBLE_WORD: h->tiled = true; break;
     default: return fail(MSX_ERR_ARG, "unknown precision mode");
     }
     h->precision = precision;
     return MSX_OK;
 }
 
-static int tiled_mode(const msx_handle *h) { return h->precision == MSX_PREC_MIXED ? MODE_MIXED : MODE_FP64; }
+static int tiled_mode(const msx_handle *h)
+{
+    return h->precision == MSX_PREC_MIXED ? MODE_MIXED : (h->precision == MSX_PREC_DOUBLE_WORD ? MODE_DW : MODE_FP64);
+}
+
+// Modes whose running state is the (hi, lo) FP32 pairs uhl, vhl, ahl.
+static bool pair_state(const msx_handle *h)
+{
+    return h->precision == MSX_PREC_MIXED || h->precision == MSX_PREC_DOUBLE_WORD;
+}
 
 // One step's kernels: the shared tiled pair for FP64 / mixed (the same
 // machine code the pool runs), the reference-order pair for exact mode.
@@ -273,7 +292,7 @@ static void launch_step(msx_handle *h, int parity)
                           h->tthreads, h->stream);
     else
         h->node(h->P, parity, h->stream);
-    if (h->nfaces) launch_face_loads(h->P, parity, h->precision == MSX_PREC_MIXED, h->stream);
+    if (h->nfaces) launch_face_loads(h->P, parity, pair_state(h), h->stream);
     if (h->tiled)
         launch_tiled_elem(h->d_desc.p, h->d_etiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
                           h->stream);
@@ -285,7 +304,7 @@ static void launch_step(msx_handle *h, int parity)
 static msx_status upload_tiled(msx_handle *h)
 {
     if (!h->tiled) return MSX_OK;
-    const int te = 1024, tn = 128;
+    const int te = kMaxTileElems, tn = 128;   // large element tiles: fewer block-wide CFL reductions
     if (!h->d_desc.p) {
         std::vector<Tile> et, nt;
         for (long long b = 0; b < h->P.ne; b += te) et.push_back({0, (int)b, (int)std::min<long long>(h->P.ne, b + te)});
@@ -370,8 +389,8 @@ static msx_status init_block(msx_handle *h)
     long long limit = h->max_steps > 0 ? h->max_steps : (1LL << 62);
     init_block_kernel<<<1, 1, 0, h->stream>>>(P, h->t0, limit);
     MSX_CUDA(cudaGetLastError());
-    if (h->precision == MSX_PREC_MIXED) {
-        launch_state_split(P, h->stream);   // the running state of a mixed block
+    if (pair_state(h)) {
+        launch_state_split(P, h->stream);   // the running state of a mixed or double-word block
         MSX_CUDA(cudaGetLastError());
     }
     MSX_CUDA(cudaMemcpyAsync(h->h_ctrl, h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
@@ -503,6 +522,8 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     ALLOC(h->wJ32, ne);
     ALLOC(h->Lref32, ne);
     ALLOC(h->Eref32, 9 * ne);
+    ALLOC(h->G32lo, 9 * ne);
+    ALLOC(h->wJ32lo, ne);
     ALLOC(h->X, 3 * nn);
     ALLOC(h->u, 3 * nn);
     ALLOC(h->v, 3 * nn);
@@ -564,7 +585,7 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     DBuf<int4> *b4[] = {&h->conn, &h->slot};
     for (auto *b : b4) b->release();
     for (auto *b : {&h->G, &h->wJ, &h->Lref, &h->X, &h->u, &h->v, &h->a, &h->mass, &h->minv, &h->fe}) b->release();
-    for (auto *b : {&h->G32, &h->wJ32, &h->Lref32, &h->Eref32, &h->fe32}) b->release();
+    for (auto *b : {&h->G32, &h->wJ32, &h->Lref32, &h->Eref32, &h->fe32, &h->G32lo, &h->wJ32lo}) b->release();
     for (auto *b : {&h->uhl, &h->vhl, &h->ahl, &h->minv2}) b->release();
     h->mat.release();
     for (auto *b : {&h->node_ptr, &h->node_inc, &h->node_bc, &h->flags}) b->release();
@@ -882,7 +903,7 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
             if (h->h_ctrl[(k - 1) & 1].stop) break;
         }
     }
-    if (h->precision == MSX_PREC_MIXED) launch_state_merge(h->P, h->stream);   // u, v, a for the caller
+    if (pair_state(h)) launch_state_merge(h->P, h->stream);   // u, v, a for the caller
     MSX_CUDA(cudaEventRecord(h->ev1, h->stream));
     MSX_CUDA(cudaStreamSynchronize(h->stream));
     Ctrl fin = h->h_ctrl[k & 1];
@@ -922,8 +943,7 @@ extern "C" msx_status msx_node_values(msx_handle *h, int32_t field, int32_t comp
         return fail(MSX_ERR_OOM, "node value scratch");
     }
     bind_problem(h);
-    const int mode = h->precision == MSX_PREC_FP64_EXACT ? MODE_EXACT
-                                                         : (h->precision == MSX_PREC_MIXED ? MODE_MIXED : MODE_FP64);
+    const int mode = h->precision == MSX_PREC_FP64_EXACT ? MODE_EXACT : tiled_mode(h);
     cudaMemcpyAsync(dn.p, nodes, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream);
     launch_node_values(h->P, mode, field, comp, dn.p, n, h->last_t, dv.p, h->stream);
     cudaMemcpyAsync(out, dv.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream);
@@ -1071,8 +1091,8 @@ extern "C" msx_status msx_internal_force(msx_handle *h, const double *u, double 
     Problem P = h->P;
     P.u = du.p;
     cudaMemcpyAsync(du.p, u, bytes, cudaMemcpyHostToDevice, h->stream);
-    DBuf<float2> uh;   // the mixed kernel reads u as (hi, lo) pairs; the block's own stay untouched
-    if (h->precision == MSX_PREC_MIXED) {
+    DBuf<float2> uh;   // the mixed and double-word kernels read u as (hi, lo) pairs; the block's own stay untouched
+    if (pair_state(h)) {
         if (uh.alloc(3 * h->P.nn) != cudaSuccess) {
             du.release();
             df.release();
@@ -1084,6 +1104,7 @@ extern "C" msx_status msx_internal_force(msx_handle *h, const double *u, double 
     }
     if (h->precision == MSX_PREC_FP64_EXACT) launch_internal_force_exact(P, df.p, h->stream);
     else if (h->precision == MSX_PREC_MIXED) launch_internal_force_mixed(P, df.p, h->stream);
+    else if (h->precision == MSX_PREC_DOUBLE_WORD) launch_internal_force_dw(P, df.p, h->stream);
     else launch_internal_force_fp64(P, df.p, h->stream);
     cudaMemcpyAsync(fint, df.p, bytes, cudaMemcpyDeviceToHost, h->stream);
     cudaError_t err = cudaStreamSynchronize(h->stream);
@@ -1126,7 +1147,7 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
                               h->tthreads, h->stream);
         else
             h->node(h->P, parity, h->stream);
-        if (h->nfaces) launch_face_loads(h->P, parity, h->precision == MSX_PREC_MIXED, h->stream);
+        if (h->nfaces) launch_face_loads(h->P, parity, pair_state(h), h->stream);
         cudaEventRecord(ev[3 * i + 1], h->stream);
         if (h->tiled)
             launch_tiled_elem(h->d_desc.p, h->d_etiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
@@ -1135,7 +1156,7 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
             h->elem(h->P, parity, h->stream);
         cudaEventRecord(ev[3 * i + 2], h->stream);
     }
-    if (h->precision == MSX_PREC_MIXED) launch_state_merge(h->P, h->stream);
+    if (pair_state(h)) launch_state_merge(h->P, h->stream);
     cudaError_t err = cudaStreamSynchronize(h->stream);
     double tn = 0, te = 0;
     for (long long i = 0; i < n; i++) {
@@ -1154,11 +1175,11 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
     rep->node_ms = tn / n;
     rep->element_launches = n;
     rep->node_launches = n;
-    bool mixed = h->precision == MSX_PREC_MIXED;
-    // algorithmic bytes: element data per element (conn 16 + dphi 96 + wJ 8 + Lref 8,
-    // or the FP32 set 16 + 48 + 4 + 4) and nodal state per node
-    // (read X, u, v, a 96 + m 8, write u, v, a 72)
-    rep->element_alg_bytes = ne * (mixed ? 72.0 : 128.0);
+    // algorithmic bytes: element data per element (conn 16 + dphi 96 + wJ 8 + Lref 8;
+    // the FP32 set 16 + 48 + 4 + 4; the double-word set 16 + 72 + 8 + 4) and
+    // nodal state per node (read X, u, v, a 96 + m 8, write u, v, a 72)
+    rep->element_alg_bytes =
+        ne * (h->precision == MSX_PREC_MIXED ? 72.0 : (h->precision == MSX_PREC_DOUBLE_WORD ? 100.0 : 128.0));
     rep->node_alg_bytes = nn * 176.0;
     return MSX_OK;
 }
