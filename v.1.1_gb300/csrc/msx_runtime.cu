@@ -130,6 +130,7 @@ struct msx_handle {
     bool tiled = false;                          // FP64 / mixed: the shared tiled step kernels
     DBuf<Problem> d_desc;
     DBuf<Tile> d_etiles, d_ntiles;
+    int tile_elems = 0;                 // element-tile size of d_etiles
     DBuf<int> d_counts;
     int tgrid = 0, tgrid_node = 0, tthreads = kStepThreads;
     cudaGraphExec_t graph = nullptr;
@@ -304,24 +305,37 @@ static void launch_step(msx_handle *h, int parity)
 static msx_status upload_tiled(msx_handle *h)
 {
     if (!h->tiled) return MSX_OK;
-    const int te = kMaxTileElems, tn = 128;   // large element tiles: fewer block-wide CFL reductions
-    if (!h->d_desc.p) {
-        std::vector<Tile> et, nt;
-        for (long long b = 0; b < h->P.ne; b += te) et.push_back({0, (int)b, (int)std::min<long long>(h->P.ne, b + te)});
-        for (long long b = 0; b < h->P.nn; b += tn) nt.push_back({0, (int)b, (int)std::min<long long>(h->P.nn, b + tn)});
-        int counts[kTileSched] = {(int)et.size(), 0, 0, (int)nt.size(), 0, 0};
-        MSX_CUDA(h->d_desc.alloc(1));
-        MSX_CUDA(h->d_etiles.alloc(et.size()));
-        MSX_CUDA(h->d_ntiles.alloc(nt.size()));
-        MSX_CUDA(h->d_counts.alloc(kTileSched));
-        MSX_CUDA(cudaMemcpyAsync(h->d_etiles.p, et.data(), sizeof(Tile) * et.size(), cudaMemcpyHostToDevice, h->stream));
-        MSX_CUDA(cudaMemcpyAsync(h->d_ntiles.p, nt.data(), sizeof(Tile) * nt.size(), cudaMemcpyHostToDevice, h->stream));
-        MSX_CUDA(cudaMemcpyAsync(h->d_counts.p, counts, sizeof(counts), cudaMemcpyHostToDevice, h->stream));
-    }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
     h->tgrid = sms * tiled_ctas_per_sm(tiled_mode(h), h->tthreads);
     h->tgrid_node = sms * tiled_ctas_per_sm(tiled_mode(h), h->tthreads, true);
+    // Element tiles: the FP64 and double-word kernels close each tile with
+    // block-wide CFL reductions, so they take large tiles, halved while the
+    // grid would get fewer than two tiles per CTA; the mixed kernel's tiles
+    // are cheap to close and 1024 balances best.
+    int te = h->precision == MSX_PREC_MIXED ? 1024 : kMaxTileElems;
+    while (te > 256 && h->P.ne / te < 2LL * h->tgrid) te /= 2;
+    const int tn = 128;
+    if (!h->d_desc.p || te != h->tile_elems) {
+        std::vector<Tile> et, nt;
+        for (long long b = 0; b < h->P.ne; b += te) et.push_back({0, (int)b, (int)std::min<long long>(h->P.ne, b + te)});
+        for (long long b = 0; b < h->P.nn; b += tn) nt.push_back({0, (int)b, (int)std::min<long long>(h->P.nn, b + tn)});
+        int counts[kTileSched] = {(int)et.size(), 0, 0, (int)nt.size(), 0, 0};
+        h->d_etiles.release();
+        h->d_ntiles.release();
+        if (!h->d_desc.p) MSX_CUDA(h->d_desc.alloc(1));
+        MSX_CUDA(h->d_etiles.alloc(et.size()));
+        MSX_CUDA(h->d_ntiles.alloc(nt.size()));
+        if (!h->d_counts.p) MSX_CUDA(h->d_counts.alloc(kTileSched));
+        MSX_CUDA(cudaMemcpyAsync(h->d_etiles.p, et.data(), sizeof(Tile) * et.size(), cudaMemcpyHostToDevice, h->stream));
+        MSX_CUDA(cudaMemcpyAsync(h->d_ntiles.p, nt.data(), sizeof(Tile) * nt.size(), cudaMemcpyHostToDevice, h->stream));
+        MSX_CUDA(cudaMemcpyAsync(h->d_counts.p, counts, sizeof(counts), cudaMemcpyHostToDevice, h->stream));
+        h->tile_elems = te;
+        if (h->graph) {   // the captured launches name the old tile lists
+            cudaGraphExecDestroy(h->graph);
+            h->graph = nullptr;
+        }
+    }
     MSX_CUDA(cudaMemcpyAsync(h->d_desc.p, &h->P, sizeof(Problem), cudaMemcpyHostToDevice, h->stream));
     MSX_CUDA(cudaStreamSynchronize(h->stream));
     return MSX_OK;
