@@ -218,21 +218,24 @@ def reference_arm(args):
             "e2e": {"value": value, "unit": "element-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def batched_variant(seed=7, count=256, steps=1000, warmup=3):
+def batched_variant(seed=7, count=256, steps=1000, warmup=3, precision=None, cache=None):
     """256 independent solves (cube side n log-uniform in [8, 48], E log-uniform
     in [1e5, 1e7], nu uniform in [0.25, 0.45], top velocity uniform in
-    [0.01, 0.2]) stepped together by the pool, FP32 elements / FP64 nodes,
-    1000 steps each.  The timed region starts after admission, autotuning and
-    warm-up and ends when the last solve finishes."""
+    [0.01, 0.2]) stepped together by the pool, 1000 steps each: mixed (FP32
+    elements, double-word nodes) by default, or another pool precision.  The
+    timed region starts after admission, autotuning and warm-up and ends when
+    the last solve finishes."""
     import msx
     rng = np.random.default_rng(seed)
     ns = np.floor(np.exp(rng.uniform(np.log(8), np.log(49), count))).astype(int)
     Es = np.exp(rng.uniform(np.log(1e5), np.log(1e7), count))
     nus = rng.uniform(0.25, 0.45, count)
     vs = rng.uniform(0.01, 0.2, count)
-    if os.path.exists(TUNE_CACHE):
-        os.remove(TUNE_CACHE)
-    P = msx.Pool(max_slots=count, precision=msx.MIXED, steps_per_launch=32, tune_cache=TUNE_CACHE)
+    cache = cache or TUNE_CACHE
+    if os.path.exists(cache):
+        os.remove(cache)
+    P = msx.Pool(max_slots=count, precision=msx.MIXED if precision is None else precision, steps_per_launch=32,
+                 tune_cache=cache)
     total_elems = 0
     t0 = time.perf_counter()
     for k in range(count):
@@ -420,6 +423,7 @@ def main():
                 variants[name]["roofline"] = dword_roofline(ne, nn, p2, 1e3 * s2 / args.steps)
     if not args.no_pool and args.only is None and args.cube == N_CUBE:
         variants["batched"] = batched_variant()
+        variants["batched_double_word"] = batched_variant(precision=msx.DOUBLE_WORD, cache=TUNE_CACHE + ".dw")
         variants["serving"] = [serving_variant(lam) for lam in (50, 200, 800)]
         variants["serving_one_at_a_time_fp64"] = serving_sequential_fp64(200)
     e2e = None

@@ -51,8 +51,7 @@ enum { MSX_PREC_FP64 = 0,        /* plain FP64, FMA-contracted, algebraically si
        MSX_PREC_DOUBLE_WORD = 3  /* MSX_PREC_FP64's algebra in double-word (FP32 pair, ~48-bit)
                                     arithmetic on the FP32 pipe, state and corner forces too;
                                     FP64 CFL check.  Values must stay inside FP32's exponent
-                                    range (|x| < 3e38, and near 1e-38 only as zeros).  Single
-                                    solves only (not msx_pool_*). */ };
+                                    range (|x| < 3e38, and near 1e-38 only as zeros). */ };
 
 typedef struct {
     int64_t num_nodes, num_elems;
@@ -313,7 +312,7 @@ typedef struct msx_pool msx_pool;
 typedef struct {
     int64_t hbm_budget_bytes;     /* admission limit for resident solves (0 = 80% free) */
     int32_t max_slots;            /* concurrent solves                                   */
-    int32_t precision;            /* MSX_PREC_FP64 or MSX_PREC_MIXED                    */
+    int32_t precision;            /* MSX_PREC_FP64, MSX_PREC_MIXED or MSX_PREC_DOUBLE_WORD */
     int32_t elems_per_block;      /* element-kernel CTA size; 0 = autotuned             */
     int32_t steps_per_launch;     /* steps per graph replay; 0 = default                */
     const char *tune_cache;       /* autotuner cache file, or NULL                       */

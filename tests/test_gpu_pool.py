@@ -30,7 +30,7 @@ def alone(X, conn, mat, bcs, steps, precision):
     return out
 
 
-@pytest.mark.parametrize("precision", [msx.MIXED, msx.FP64])
+@pytest.mark.parametrize("precision", [msx.MIXED, msx.FP64, msx.DOUBLE_WORD])
 def test_pool_results_equal_single_solves(precision):
     rng = np.random.default_rng(11)
     cases = [case(int(n), float(E), float(nu), float(v), s)

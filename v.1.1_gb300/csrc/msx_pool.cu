@@ -124,6 +124,14 @@ struct msx_pool {
 // ------------------------------------------------------------------ helpers
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+static int pool_mode(int precision)
+{
+    return precision == MSX_PREC_MIXED ? MODE_MIXED : (precision == MSX_PREC_DOUBLE_WORD ? MODE_DW : MODE_FP64);
+}
+
+// modes whose running state is the (hi, lo) FP32 pairs uhl, vhl, ahl
+static bool pair_state(int precision) { return precision == MSX_PREC_MIXED || precision == MSX_PREC_DOUBLE_WORD; }
+
 static size_t footprint(long long nn, long long ne, long long nbc, int precision)
 {
     size_t b = 0;
@@ -132,8 +140,10 @@ static size_t footprint(long long nn, long long ne, long long nbc, int precision
     b += 2 * align256(sizeof(float) * 9 * ne) + 2 * align256(sizeof(float) * ne);    // G32, Eref32, wJ32, Lref32
     b += 4 * align256(sizeof(double) * 3 * nn) + 2 * align256(sizeof(double) * nn);  // X, u, v, a, mass, minv
     b += align256(sizeof(float2) * 3 * nn);                                          // uhl
-    if (precision == MSX_PREC_MIXED)                                                 // vhl, ahl, minv2
+    if (pair_state(precision))                                                       // vhl, ahl, minv2
         b += 2 * align256(sizeof(float2) * 3 * nn) + align256(sizeof(float2) * nn);
+    if (precision == MSX_PREC_DOUBLE_WORD)                                           // G32lo, wJ32lo
+        b += align256(sizeof(float) * 9 * ne) + align256(sizeof(float) * ne);
     b += precision == MSX_PREC_MIXED ? align256(sizeof(float) * 16 * ne) : align256(sizeof(double) * 12 * ne);
     b += align256(sizeof(int) * (nn + 1)) + align256(sizeof(int) * 4 * ne) + align256(sizeof(int) * nn);
     b += align256(sizeof(int4) * ne);                                                // corner slots
@@ -212,7 +222,7 @@ static msx_status build_pool_graph(msx_pool *p, int steps)
         cudaGraphExecDestroy(p->graph);
         p->graph = nullptr;
     }
-    const int mode = p->opts.precision == MSX_PREC_MIXED ? MODE_MIXED : MODE_FP64;
+    const int mode = pool_mode(p->opts.precision);
     const int threads = p->sched.threads, grid = p->sms * p->sched.ctas_per_sm;
     const int node_grid = p->sms * tiled_ctas_per_sm(mode, threads, true);
     cudaGraph_t g;
@@ -254,7 +264,7 @@ static msx_status collect(msx_pool *p)
         f.res.steps = c.step;
         f.res.t = c.t;
         size_t bytes = sizeof(double) * 3 * sl.nn;
-        if (p->opts.precision == MSX_PREC_MIXED) launch_state_merge(sl.P, p->stream);
+        if (pair_state(p->opts.precision)) launch_state_merge(sl.P, p->stream);
         f.u.resize(3 * sl.nn);
         f.v.resize(3 * sl.nn);
         f.a.resize(3 * sl.nn);
@@ -346,7 +356,7 @@ static msx_status replay(msx_pool *p, float *ms)
 // results are the same whichever one runs a step.
 static msx_status autotune(msx_pool *p)
 {
-    const int mode = p->opts.precision == MSX_PREC_MIXED ? MODE_MIXED : MODE_FP64;
+    const int mode = pool_mode(p->opts.precision);
     const int occ128 = tiled_ctas_per_sm(mode, 128), occ256 = tiled_ctas_per_sm(mode, 256);
     const Sched cands[] = {{128, 512, occ128}, {128, 1024, occ128}, {256, 512, occ256}, {256, 1024, occ256},
                            {256, 2048, occ256}, {256, 4096, occ256}, {256, 1024, std::max(1, occ256 / 2)},
@@ -398,8 +408,9 @@ extern "C" msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out)
 {
     if (!out || !opts) return pfail(MSX_ERR_ARG, "NULL argument");
     *out = nullptr;
-    if (opts->precision != MSX_PREC_FP64 && opts->precision != MSX_PREC_MIXED)
-        return pfail(MSX_ERR_ARG, "pool precision must be FP64 or MIXED");
+    if (opts->precision != MSX_PREC_FP64 && opts->precision != MSX_PREC_MIXED &&
+        opts->precision != MSX_PREC_DOUBLE_WORD)
+        return pfail(MSX_ERR_ARG, "pool precision must be FP64, MIXED or DOUBLE_WORD");
     if (opts->max_slots < 1 || opts->max_slots > 4096) return pfail(MSX_ERR_ARG, "max_slots must be 1..4096");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return pfail(MSX_ERR_NO_DEVICE, "no CUDA device");
@@ -408,7 +419,7 @@ extern "C" msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out)
     cudaGetDevice(&p->device);
     cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device);
     p->spl = opts->steps_per_launch > 0 ? ((opts->steps_per_launch + 1) & ~1) : 32;
-    const int pmode = opts->precision == MSX_PREC_MIXED ? MODE_MIXED : MODE_FP64;
+    const int pmode = pool_mode(opts->precision);
     p->sched.threads = kStepThreads;
     p->sched.ctas_per_sm = tiled_ctas_per_sm(pmode, kStepThreads);
     if (opts->elems_per_block > 0) {
@@ -563,6 +574,10 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     P.Eref32 = (float *)carve(sizeof(float) * 9 * ne);
     P.wJ32 = (float *)carve(sizeof(float) * ne);
     P.Lref32 = (float *)carve(sizeof(float) * ne);
+    if (prec == MSX_PREC_DOUBLE_WORD) {
+        P.G32lo = (float *)carve(sizeof(float) * 9 * ne);
+        P.wJ32lo = (float *)carve(sizeof(float) * ne);
+    }
     double *X = (double *)carve(sizeof(double) * 3 * nn);
     P.X = X;
     P.u = (double *)carve(sizeof(double) * 3 * nn);
@@ -573,7 +588,7 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     P.minv = minv;
     P.uhl = (float2 *)carve(sizeof(float2) * 3 * nn);
     float2 *minv2 = nullptr;
-    if (prec == MSX_PREC_MIXED) {
+    if (pair_state(prec)) {
         P.vhl = (float2 *)carve(sizeof(float2) * 3 * nn);
         P.ahl = (float2 *)carve(sizeof(float2) * 3 * nn);
         minv2 = (float2 *)carve(sizeof(float2) * nn);
@@ -616,13 +631,13 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     PCUDA(cudaMemsetAsync(P.v, 0, sizeof(double) * 3 * nn, s));
     PCUDA(cudaMemsetAsync(P.a, 0, sizeof(double) * 3 * nn, s));
     PCUDA(cudaMemsetAsync(P.uhl, 0, sizeof(float2) * 3 * nn, s));
-    if (prec == MSX_PREC_MIXED) {
+    if (pair_state(prec)) {
         PCUDA(cudaMemsetAsync(P.vhl, 0, sizeof(float2) * 3 * nn, s));
         PCUDA(cudaMemsetAsync(P.ahl, 0, sizeof(float2) * 3 * nn, s));
     }
     launch_setup_elements(P, X, s);
     launch_setup_mass(P, mass, minv, s);
-    if (prec == MSX_PREC_MIXED) launch_minv_split(minv, minv2, nn, s);
+    if (pair_state(prec)) launch_minv_split(minv, minv2, nn, s);
     unsigned long long inf2[2] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL};
     PCUDA(cudaMemcpyAsync(P.dtmin, inf2, sizeof(inf2), cudaMemcpyHostToDevice, s));
     launch_initial_cfl(P, nullptr, 0, s);
