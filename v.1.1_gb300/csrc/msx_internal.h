@@ -199,5 +199,7 @@ void launch_internal_force_exact(const Problem &p, double *fint, cudaStream_t s)
 void launch_internal_force_fp64(const Problem &p, double *fint, cudaStream_t s);
 void launch_internal_force_mixed(const Problem &p, double *fint, cudaStream_t s);
 void launch_internal_force_dw(const Problem &p, double *fint, cudaStream_t s);
+// Law parameters of one material, FP64 and the FP32 / double-word copies; false if invalid.
+bool material_params(const msx_material &m, MatParams &o);
 
 }  // namespace msx

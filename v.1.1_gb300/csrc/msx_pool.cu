@@ -154,26 +154,7 @@ static size_t footprint(long long nn, long long ne, long long nbc, int precision
 static msx_status make_mat(const msx_material &m, MatParams &o)
 {
     if (m.law < 0 || m.law > 2) return pfail(MSX_ERR_ARG, "unknown constitutive law");
-    if (!(m.young > 0) || !(m.rho > 0) || !(m.nu > -1.0) || !(m.nu < 0.5))
-        return pfail(MSX_ERR_ARG, "material needs E > 0, rho > 0, -1 < nu < 0.5");
-    memset(&o, 0, sizeof(o));
-    const double E = m.young, nu = m.nu;
-    o.law = m.law;
-    o.young = E;
-    o.nu = nu;
-    o.rho = m.rho;
-    o.lambda = (E * nu) / ((1. + nu) * (1. - 2. * nu));
-    o.mu = 0.5 * E / (1. + nu);
-    o.K1 = E / (3 * (1 - 2 * nu));
-    o.mu2 = E / (1. + nu);
-    o.lam_stvk = E * nu / ((1. + nu) * (1. - (2 * nu)));
-    o.c = m.law == 2 ? std::sqrt(E / m.rho) : std::sqrt((o.lambda + 2 * o.mu) / m.rho);
-    o.lambda_f = (float)o.lambda;
-    o.mu_f = (float)o.mu;
-    o.K1_f = (float)o.K1;
-    o.mu2_f = (float)o.mu2;
-    o.lam_stvk_f = (float)o.lam_stvk;
-    o.inv_c_f = (float)(1.0 / o.c);
+    if (!material_params(m, o)) return pfail(MSX_ERR_ARG, "material needs E > 0, rho > 0, -1 < nu < 0.5");
     return MSX_OK;
 }
 

@@ -139,11 +139,12 @@ struct msx_handle {
 };
 
 // ------------------------------------------------------------------ host helpers
-static msx_status make_material(const msx_material &m, MatParams &o)
+// Law parameters of one material (shared by single solves and the pool);
+// false for an invalid material.
+bool msx::material_params(const msx_material &m, MatParams &o)
 {
-    if (m.law < 0 || m.law > 2) return fail(MSX_ERR_ARG, "unknown constitutive law");
-    if (!(m.young > 0) || !(m.rho > 0) || !(m.nu > -1.0) || !(m.nu < 0.5))
-        return fail(MSX_ERR_ARG, "material needs E > 0, rho > 0, -1 < nu < 0.5");
+    if (m.law < 0 || m.law > 2) return false;
+    if (!(m.young > 0) || !(m.rho > 0) || !(m.nu > -1.0) || !(m.nu < 0.5)) return false;
     memset(&o, 0, sizeof(o));
     const double E = m.young, nu = m.nu;
     o.law = m.law;
@@ -172,6 +173,13 @@ static msx_status make_material(const msx_material &m, MatParams &o)
     o.mu2_w = dw(o.mu2);
     o.lam_stvk_w = dw(o.lam_stvk);
     o.mu3_w = dw(o.mu / 3.0);
+    return true;
+}
+
+static msx_status make_material(const msx_material &m, MatParams &o)
+{
+    if (m.law < 0 || m.law > 2) return fail(MSX_ERR_ARG, "unknown constitutive law");
+    if (!material_params(m, o)) return fail(MSX_ERR_ARG, "material needs E > 0, rho > 0, -1 < nu < 0.5");
     return MSX_OK;
 }
 
