@@ -207,6 +207,7 @@ class Solver:
     scale_factor: float
     bcs: list = field(default_factory=list)   # (dof, mode, value, ramp_steps)
     max_steps: int = 0
+    forces_out: tuple = None                  # *Forces: (frequency, [(node, direction), ...])
 
 
 def cube_mesh(n: int, seed: int = 1234, jitter: float = 0.1) -> Mesh:
@@ -505,6 +506,11 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Load
                   "*BOUNDARY, TYPE=DISPLACEMENT " + ("INST" if mode == BC_INST else "RAMP")]
         for dof, _, value, _ in s.bcs:
             lines.append("%d,%d,%.17g" % (dof % nn + 1, dof // nn, value))
+        if s.forces_out:
+            # *Forces (src/IO/inputFile.cpp:4830-4886): the reader slices each line
+            # between its first two commas, so the direction is followed by one
+            freq, pairs = s.forces_out
+            lines += ["*Forces", "%.17g" % freq] + ["%d,%d," % (int(nd) + 1, int(c)) for nd, c in pairs]
         lines.append("*END SOLVER")
     if mat_elems is None:
         mat_elems = [None] * len(mats)

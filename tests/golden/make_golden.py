@@ -129,6 +129,14 @@ def cases(ref_src):
          every("FXX", "Min"), every("VOLUME", "Sum"), every("EXTERNAL_ENERGY", "Sum"),
          ("element", "nh", "DEFO_ENERGY", "Mean", list(range(0, m2.ne, 2))),
          ("element", "stvk", "DEFO_ENERGY", "Mean", list(range(1, m2.ne, 2)))])
+    # *Forces output (internal force of listed node DOFs at a frequency): two
+    # chained blocks, one slower than the step (period 1/500 s), one faster (every step)
+    botn3 = node_on(m3, 2, 0.0)
+    out["cube3_cnh_print_forces"] = (
+        m3, [O.Material(cnh)],
+        [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.002),
+                  forces_out=(500.0, [(nd, 2) for nd in botn3[:6]] + [(21, 0), (22, 1), (42, 2)])),
+         O.Solver(0.02, 0.03, 0.4, O.cube_bcs(3, 0.003), forces_out=(1e5, [(botn3[0], 2), (30, 1)]))])
     side4 = plane_faces(m4, 0, 1.0)
     out["cube4_stvk_pressure_ramp"] = (
         m4, [O.Material(stvk)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(4, 0.001))],
@@ -151,6 +159,11 @@ def pack(mesh, mats, solvers, ref, orc, loads=None, extractions=()):
          "u": ref[0], "v": ref[1], "a": ref[2], "steps": np.array(orc.steps)}
     if mesh.elem_mat is not None:
         d["elem_mat"] = mesh.elem_mat
+    if any(s.forces_out for s in solvers):
+        import json
+        d["forces_out_json"] = np.array(json.dumps([s.forces_out for s in solvers]))
+        files = sorted(f for f in os.listdir(ref[5]) if f.startswith("externalForces"))
+        d["force_files_json"] = np.array(json.dumps({f: open(os.path.join(ref[5], f)).read() for f in files}))
     if loads is not None:
         import json
         d["loads_json"] = np.array(json.dumps(loads.items))

@@ -24,7 +24,18 @@ def load(name):
         bcs = [(int(b[0]), int(b[1]), float(b[2]), int(b[3])) for b in d["bcs"][k:k + nb]]
         k += nb
         solvers.append(O.Solver(float(t0), float(tf), float(sf), bcs))
+    if "forces_out_json" in d:
+        import json
+        for s, fo in zip(solvers, json.loads(str(d["forces_out_json"]))):
+            s.forces_out = None if fo is None else (fo[0], [tuple(x) for x in fo[1]])
     return mesh, mats, solvers, (d["u"], d["v"], d["a"]), int(d["steps"])
+
+
+def load_force_files(name):
+    """{file name: the reference's *Forces CSV text} of a case, or {}."""
+    import json
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return json.loads(str(d["force_files_json"])) if "force_files_json" in d else {}
 
 
 def load_loads(name):

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from golden_cases import load, load_extractions, load_loads, names
+from golden_cases import load, load_extractions, load_force_files, load_loads, names
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DECK = os.path.join(ROOT, "v.1.1_gb300", "_build", "msx_deck")
@@ -203,3 +203,35 @@ def test_element_extraction_matches_reference_files(tmp_path, name, precision, t
         assert np.allclose(v_got[:, 0], v_ref[:, 0], rtol=1e-12 if precision != "mixed" else 1e-6, atol=0), fname
         scale = max(np.abs(v_ref[:, 1]).max(), 1e-300)
         assert np.abs(v_got[:, 1] - v_ref[:, 1]).max() <= tol * scale, (fname, np.abs(v_got[:, 1] - v_ref[:, 1]).max())
+
+
+def test_parse_print_forces(tmp_path):
+    mesh, _, solvers, _, _ = write(tmp_path, "cube3_cnh_print_forces")
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-parse-only"],
+                       capture_output=True, text=True, check=True)
+    blocks = json.loads(r.stdout)["blocks"]
+    assert [(b["force_freq"], b["force_out"]) for b in blocks] == [(s.forces_out[0], len(s.forces_out[1]))
+                                                                   for s in solvers]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [("exact", 0.0), ("fp64", 1e-9), ("dword", 1e-9), ("mixed", 1e-4)])
+def test_print_forces_match_reference_files(tmp_path, precision, tol):
+    """*Forces: the reference's externalForces<t0>-<tf>.csv files, same rows; the
+    forces within the printed 6 decimals (one unit of the last digit, or tol of
+    the file's largest force)."""
+    write(tmp_path, "cube3_cnh_print_forces")
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-precision", precision,
+                        "-outputDir", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for fname, ref_text in load_force_files("cube3_cnh_print_forces").items():
+        got = (out / fname).read_text().strip().split("\n")
+        ref = ref_text.strip().split("\n")
+        assert got[0] == ref[0] and len(got) == len(ref), fname
+        g = np.array([[float(x) for x in ln.split(",")[:4]] for ln in got[1:]])
+        e = np.array([[float(x) for x in ln.split(",")[:4]] for ln in ref[1:]])
+        assert np.array_equal(g[:, :2], e[:, :2]) and np.abs(g[:, 3] - e[:, 3]).max() <= 1.01e-6, fname
+        scale = np.abs(e[:, 2]).max()
+        assert np.abs(g[:, 2] - e[:, 2]).max() <= 1.01e-6 + tol * scale, fname

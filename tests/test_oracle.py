@@ -204,3 +204,30 @@ def test_element_values_agree_with_reductions():
     assert O.element_reduce(mesh, mats, "SVM", "Max", u, v) == val["SVM"].max()
     mean = O.element_reduce(mesh, mats, "KIN_ENERGY", "Mean", u, v)
     assert abs(mean - (val["KIN_ENERGY"] * wJ).sum() / wJ.sum()) <= 1e-12 * abs(mean)
+
+
+def test_print_forces_pinned_to_reference():
+    """*Forces: every row the reference wrote (which steps, the internal force of
+    each listed node DOF, the time), from the oracle's state after that step,
+    formatted as the reference formats it (std::to_string, i.e. %f)."""
+    from golden_cases import load_force_files
+    mesh, mats, solvers, _, _ = load("cube3_cnh_print_forces")
+    files = load_force_files("cube3_cnh_print_forces")
+    nn = mesh.nn
+    for b, s in enumerate(solvers):
+        freq, pairs = s.forces_out
+        name = "externalForces%f-%f.csv" % (s.t0, s.tf)
+        rows = files[name].strip().split("\n")
+        assert rows[0] == "Node,Direction,Force,Time,"
+        expect, done, k = [], 0, 0
+        while k < 10000:
+            k += 1
+            r = O.run(mesh, mats, solvers[:b] + [O.Solver(s.t0, s.tf, s.scale_factor, s.bcs, max_steps=k)])
+            period = max(1.0 / freq, r.dt_last)
+            if r.t >= done * period + s.t0:
+                fint = O.internal_force(mesh, mats, r.u)[0]
+                expect += ["%d,%d,%f,%f," % (nd + 1, c, fint[nd + c * nn], r.t) for nd, c in pairs]
+                done += 1
+            if r.t >= s.tf - 1e-12:
+                break
+        assert rows[1:] == expect, name

@@ -42,6 +42,10 @@ struct SolverBlock {
     double sf = 1, t0 = 0, tf = 0;
     int outputs = -1;
     std::vector<msx_bc> bcs;
+    // *Forces (IO/inputFile.cpp:2537-2541, 4830-4886): output frequency and
+    // the (node, direction) pairs whose internal force is written
+    double force_freq = 0;
+    std::vector<std::pair<int32_t, int>> force_out;
 };
 
 struct Deck {
@@ -327,6 +331,19 @@ Deck parse(const std::string &path)
                         b.value = atof(f[2].c_str());
                         s.bcs.push_back(b);
                     }
+                } else if (starts(K, "*Forces")) {
+                    if (i + 1 >= n) die("*Forces needs a frequency", (int)i + 1);
+                    s.force_freq = atof(lines[i + 1].c_str());
+                    if (!(s.force_freq > 0)) die("*Forces frequency must be > 0", (int)i + 2);
+                    for (i += 2; data_line(i); i++) {
+                        auto f = split(lines[i]);
+                        if (f.size() < 2) die("a *Forces line has node, direction", (int)i + 1);
+                        long long node = atoll(f[0].c_str()) - 1, dir = atoll(f[1].c_str());
+                        if (node < 0 || node >= (long long)d.xyz.size() / 3) die("*Forces node out of range", (int)i + 1);
+                        // directions are 0..2 (output.cpp:121-124 refuses dir >= ndim)
+                        if (dir < 0 || dir > 2) die("*Forces direction must be 0, 1 or 2", (int)i + 1);
+                        s.force_out.push_back({(int32_t)node, (int)dir});
+                    }
                 } else if (K.empty()) {
                     i++;
                 } else {
@@ -471,6 +488,42 @@ static bool write_extraction(Deck::Extraction &E, const std::string &dir, msx_ha
     return true;
 }
 
+// *Forces output of one solver block (IO/output.cpp:107-133 writeExternalForces,
+// :153-279 printForcesOut, called every step at solverExplicit.cpp:304): when
+// t >= k * max(1/frequency, dt) + t0 (k = rows written so far), one line per
+// listed (node, direction) with the internal force of the step (the inertia
+// term the reference adds is zero: computeInertialForce is not called,
+// solverExplicit.cpp:611), in <dir>/externalForces<t0>-<tf>.csv, numbers
+// formatted as std::to_string does.
+struct ForcePrinter {
+    const SolverBlock &s;
+    std::string path;
+    long long done = 0;
+    ForcePrinter(const SolverBlock &b, const std::string &dir)
+        : s(b), path(dir + "/externalForces" + std::to_string(b.t0) + "-" + std::to_string(b.tf) + ".csv") {}
+    bool step(msx_handle *h, double t, double dt)
+    {
+        double period = 1.0 / s.force_freq;
+        if (period < dt) period = dt;
+        if (!(t >= done * period + s.t0)) return true;
+        FILE *f = fopen(path.c_str(), done == 0 ? "w" : "a");
+        if (!f) return false;
+        if (done == 0) fprintf(f, "Node,Direction,Force,Time,\n");
+        for (const auto &nd : s.force_out) {
+            double v = 0;
+            if (msx_node_values(h, MSX_FIELD_INTERNAL_FORCE, nd.second, &nd.first, 1, &v) != MSX_OK) {
+                fclose(f);
+                return false;
+            }
+            fprintf(f, "%s,%s,%s,%s,\n", std::to_string(nd.first + 1).c_str(), std::to_string(nd.second).c_str(),
+                    std::to_string(v).c_str(), std::to_string(t).c_str());
+        }
+        fclose(f);
+        done++;
+        return true;
+    }
+};
+
 int main(int argc, char **argv)
 {
     std::string input, dir = ".", dump, csv, outdir;
@@ -537,23 +590,28 @@ int main(int argc, char **argv)
         printf("]");
         printf(", \"blocks\": [");
         for (size_t k = 0; k < d.solvers.size(); k++)
-            printf("%s{\"t0\": %.17g, \"tf\": %.17g, \"sf\": %.17g, \"bcs\": %zu, \"inst\": %d}", k ? ", " : "",
+            printf("%s{\"t0\": %.17g, \"tf\": %.17g, \"sf\": %.17g, \"bcs\": %zu, \"inst\": %d, "
+                   "\"force_freq\": %.17g, \"force_out\": %zu}", k ? ", " : "",
                    d.solvers[k].t0, d.solvers[k].tf, d.solvers[k].sf, d.solvers[k].bcs.size(),
-                   d.solvers[k].bcs.empty() ? 0 : d.solvers[k].bcs[0].mode == MSX_BC_INST);
+                   d.solvers[k].bcs.empty() ? 0 : d.solvers[k].bcs[0].mode == MSX_BC_INST, d.solvers[k].force_freq,
+                   d.solvers[k].force_out.size());
         printf("]}\n");
         return 0;
     }
     msx_mesh mesh{nn, ne, X.data(), d.conn.data(), d.elem_mat.empty() ? nullptr : d.elem_mat.data()};
     // extraction files go to the output directory, by default ./output (IO/commandLine.cpp:20, 165-170)
     const std::string xdir = outdir.empty() ? "output" : outdir;
-    if (!d.extractions.empty()) mkdir(xdir.c_str(), 0755);
+    bool any_forces = false;
+    for (const auto &s : d.solvers) any_forces |= s.force_freq > 0;
+    if (!d.extractions.empty() || any_forces) mkdir(xdir.c_str(), 0755);
     msx_handle *h = nullptr;
     long long total = 0;
     std::vector<std::pair<std::string, double>> outputs;
     for (size_t k = 0; k < d.solvers.size(); k++) {
         const SolverBlock &s = d.solvers[k];
-        // with node extraction the block advances one step per call: two-step graphs
-        msx_solver_opts o{s.t0, s.tf, s.sf, 0, precision, d.extractions.empty() ? 0 : 2};
+        // with extraction or *Forces the block advances one step per call: two-step graphs
+        const bool stepwise = !d.extractions.empty() || s.force_freq > 0;
+        msx_solver_opts o{s.t0, s.tf, s.sf, 0, precision, stepwise ? 2 : 0};
         msx_status st;
         if (k == 0) {
             st = msx_create(&mesh, d.mats.data(), (int32_t)d.mats.size(), s.bcs.data(), (int64_t)s.bcs.size(), &o, &h);
@@ -582,7 +640,7 @@ int main(int argc, char **argv)
             return 1;
         }
         msx_run_report r{};
-        const bool stepwise = !d.extractions.empty();
+        ForcePrinter fp{s, xdir};
         if (outdir.empty() && !stepwise) {
             st = msx_run(h, 0, &r);
             total += r.steps;
@@ -617,6 +675,10 @@ int main(int argc, char **argv)
                 steps += r.steps;
                 since += r.steps;
                 if (r.steps == 0) break;
+                if (s.force_freq > 0 && !fp.step(h, r.t, r.dt)) {
+                    fprintf(stderr, "msx_deck: cannot write %s\n", fp.path.c_str());
+                    return 1;
+                }
                 for (auto &E : d.extractions)
                     if (!write_extraction(E, xdir, h, r.t)) {
                         fprintf(stderr, "msx_deck: cannot write %s/%s.csv\n", xdir.c_str(), E.name.c_str());
