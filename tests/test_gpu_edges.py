@@ -96,3 +96,18 @@ def test_malformed_meshes_are_refused():
         msx.Solver(X, conn, mat, [(3 * X.shape[1], msx.BC_RAMP, 0.0, 0)], 0.0, 0.01, 0.5)   # DOF out of range
     with pytest.raises(msx.MsxError):
         msx.Solver(X, conn, [(msx.COMPRESSIBLE_NH, 1e6, 0.3, -1.0)], [], 0.0, 0.01, 0.5)  # negative density
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("law", [O.COMPRESSIBLE_NH, O.NEO_HOOKEAN, O.STVK])
+@pytest.mark.parametrize("precision", [msx.FP64, msx.DOUBLE_WORD])
+def test_large_compression(law, precision):
+    """A 4^3 cube squeezed by 30 % in z: J far from 1, so the log series gives way
+    to the library log, 1/J is far from 1, and the strains are finite."""
+    mesh = O.cube_mesh(4)
+    solvers = [O.Solver(0.0, 0.05, 0.5, O.cube_bcs(4, -0.3))]
+    ref = O.run(mesh, [O.Material(law)], solvers)
+    (u, v, a), steps = run_gpu(mesh, law, solvers, precision)
+    assert steps == ref.steps
+    assert np.abs(u).max() > 0.2          # the top really moved
+    assert rel(u, ref.u) <= 1e-10, rel(u, ref.u)
