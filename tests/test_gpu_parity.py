@@ -1,6 +1,6 @@
 """CUDA path against the reference's own outputs (golden fixtures) and the
 oracle.  Tolerances: FP64_EXACT relative L2 <= 1e-12 (bit-identical where no
-transcendental is involved), FP64 relative L2 <= 1e-10 (the spec bar),
+transcendental is involved), FP64 relative L2 <= 1e-10 (the bar of the plain FP64 path),
 MIXED relative L2 <= 1e-5."""
 import numpy as np
 import pytest
