@@ -39,7 +39,8 @@ typedef enum {
 
 enum { MSX_LAW_NEO_HOOKEAN = 0,             /* *HyperElastic, Neo-Hookean                 */
        MSX_LAW_COMPRESSIBLE_NEO_HOOKEAN = 1, /* *HyperElastic, 3D-Compressible-Neo-Hookean */
-       MSX_LAW_STVK = 2 };                   /* *HyperElastic, St-Venant-Kirchhoff          */
+       MSX_LAW_STVK = 2,                     /* *HyperElastic, St-Venant-Kirchhoff          */
+       MSX_LAW_LINEAR_ELASTIC = 3 };         /* *Linear-Elastic (small strain; 3D isotropic) */
 
 enum { MSX_BC_RAMP = 0,      /* *BOUNDARY, TYPE=DISPLACEMENT RAMP: value reached at tf         */
        MSX_BC_INST = 1,      /* *BOUNDARY, TYPE=DISPLACEMENT INST: value applied at first step */

@@ -140,11 +140,12 @@ int orc_lumped_mass(int64_t nn, int64_t ne, const int32_t *conn, const double *w
     return ORC_OK;
 }
 
-/* hyperElasticNeoHookean.cpp:51-54 and hyperElasticStVenantKirchhoff.cpp:50-55. */
+/* hyperElasticNeoHookean.cpp:51-54, hyperElasticStVenantKirchhoff.cpp:50-55,
+ * linearElastic.cpp:43-48. */
 double orc_sound_speed(const orc_material *m)
 {
     double E = m->young, nu = m->nu;
-    if (m->law == ORC_STVK) return sqrt(E / m->rho);
+    if (m->law == ORC_STVK || m->law == ORC_LINEAR_ELASTIC) return sqrt(E / m->rho);
     double lambda = (E * nu) / ((1. + nu) * (1. - 2. * nu));
     double mu = 0.5 * E / (1. + nu);
     return sqrt((lambda + 2 * mu) / m->rho);
@@ -176,6 +177,15 @@ void orc_stress(const orc_material *m, const double *F, double *P)
                 for (int k = 0; k < 3; k++) c += F[i * 3 + k] * PK2[k * 3 + j] * 1.;
                 P[i * 3 + j] = c;
             }
+    } else if (m->law == ORC_LINEAR_ELASTIC) {
+        /* linearElastic.cpp:58-82 (E = (F + F^T)/2 - I), :114-145 stress (3D branch):
+         * P = E mu2, then P_ii += lam tr(E) */
+        double Eg[9], mu2 = E / (1. + nu), lam = E * nu / ((1. + nu) * (1. - (2 * nu))), trE = 0;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) Eg[i * 3 + j] = 0.5 * (F[i * 3 + j] + F[j * 3 + i] - 2. * (i == j ? 1. : 0.));
+        for (int i = 0; i < 3; i++) trE += Eg[i * 3 + i];
+        for (int i = 0; i < 9; i++) P[i] = Eg[i] * mu2;
+        for (int i = 0; i < 3; i++) P[i * 3 + i] += lam * trE;
     } else if (m->law == ORC_NEO_HOOKEAN) {
         /* hyperElasticNeoHookean.cpp:23-33 (constants), :70-127 (stress);
          * TensorOperations.h:517-551 leftCauchy, :577-592 dotSecondTranspose */
@@ -300,12 +310,15 @@ int orc_element_fields(int64_t nn, int64_t ne, const int32_t *conn, const double
         }
         /* the compressible neo-Hookean law never updates its Green-Lagrange
          * strain (hyperElasticNeoHookean.cpp:221-289 has no computeGL), so the
-         * reference reports it as zero */
+         * reference reports it as zero; the linear-elastic law stores its
+         * small strain there (linearElastic.cpp:71-76) */
         for (int i = 0; i < 3; i++)
             for (int j = 0; j < 3; j++) {
                 double c = 0;
                 for (int k = 0; k < 3; k++) c += F[k * 3 + i] * F[k * 3 + j];
-                C[i * 3 + j] = m->law == ORC_COMPRESSIBLE_NH ? 0.0 : 0.5 * (c - (i == j ? 1.0 : 0.0));
+                C[i * 3 + j] = m->law == ORC_COMPRESSIBLE_NH ? 0.0
+                             : m->law == ORC_LINEAR_ELASTIC ? 0.5 * (F[i * 3 + j] + F[j * 3 + i] - 2. * (i == j ? 1. : 0.))
+                                                            : 0.5 * (c - (i == j ? 1.0 : 0.0));
             }
         for (int k = 0; k < 9; k++) {
             if (cauchy) cauchy[e * 9 + k] = S[k];
@@ -706,6 +719,21 @@ static double gp_value(const orc_problem *p, const double *dphi, const double *w
         return val;
     }
     if (q == ORC_Q_DEFO && m->law == ORC_NEO_HOOKEAN) return 0.;
+    if (q == ORC_Q_DEFO && m->law == ORC_LINEAR_ELASTIC) {
+        /* linearElastic.cpp:88-101: 0.5 (P:F - P:I), contractions summed from 0 */
+        const double *dp = dphi + 12 * e;
+        double F[9], P[9], a = 0, b = 0;
+        for (int i = 0; i < 9; i++) F[i] = 0.;
+        for (int i = 0; i < 3; i++) {
+            F[i * 3 + i] += 1.;
+            for (int k = 0; k < 4; k++)
+                for (int j = 0; j < 3; j++) F[i * 3 + j] += dp[k * 3 + j] * u[c[k] + i * nn];
+        }
+        orc_stress(m, F, P);
+        for (int i = 0; i < 9; i++) a += P[i] * F[i];
+        for (int i = 0; i < 9; i++) b += P[i] * ((i % 4) == 0 ? 1. : 0.);
+        return 0.5 * (a - b);
+    }
     const double *dp = dphi + 12 * e;
     double F[9], P[9], C[9];
     for (int i = 0; i < 9; i++) F[i] = 0.;

@@ -24,7 +24,8 @@ extern "C" {
 /* Constitutive laws, named as in the reference's *HyperElastic keyword. */
 enum { ORC_NEO_HOOKEAN = 0,          /* "Neo-Hookean" (Belytschko form)      */
        ORC_COMPRESSIBLE_NH = 1,      /* "3D-Compressible-Neo-Hookean"        */
-       ORC_STVK = 2 };               /* "St-Venant-Kirchhoff" (3D isotropic)  */
+       ORC_STVK = 2,                 /* "St-Venant-Kirchhoff" (3D isotropic)  */
+       ORC_LINEAR_ELASTIC = 3 };     /* *Linear-Elastic (small strain, 3D)     */
 
 /* Dirichlet modes: reference *BOUNDARY, TYPE=DISPLACEMENT RAMP / INST, plus
  * the step-ramped velocity extension (no reference counterpart). */

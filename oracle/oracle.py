@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "muphisim_ref")
 
-NEO_HOOKEAN, COMPRESSIBLE_NH, STVK = 0, 1, 2
+NEO_HOOKEAN, COMPRESSIBLE_NH, STVK, LINEAR_ELASTIC = 0, 1, 2, 3
 LAW_NAMES = {NEO_HOOKEAN: "Neo-Hookean", COMPRESSIBLE_NH: "3D-Compressible-Neo-Hookean",
              STVK: "St-Venant-Kirchhoff"}
 BC_RAMP, BC_INST, BC_VEL_RAMP = 0, 1, 2
@@ -516,7 +516,8 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Load
         mat_elems = [None] * len(mats)
     for k, m in enumerate(mats):
         lines += ["*MATERIAL, name=Region%d" % (k + 1), "*Density", "%.17g" % m.rho,
-                  "*HyperElastic, " + LAW_NAMES[m.law], "%.17g, %.17g" % (m.young, m.nu)]
+                  ("*Linear-Elastic" if m.law == LINEAR_ELASTIC else "*HyperElastic, " + LAW_NAMES[m.law]),
+                  "%.17g, %.17g" % (m.young, m.nu)]
         if mat_elems[k] is None:
             lines += ["*List of Elements", "All"]
         else:

@@ -137,6 +137,17 @@ def cases(ref_src):
         [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.002),
                   forces_out=(500.0, [(nd, 2) for nd in botn3[:6]] + [(21, 0), (22, 1), (42, 2)])),
          O.Solver(0.02, 0.03, 0.4, O.cube_bcs(3, 0.003), forces_out=(1e5, [(botn3[0], 2), (30, 1)]))])
+    # the linear-elastic law (*Linear-Elastic): alone with element extraction, and
+    # beside the compressible neo-Hookean law on a two-material mesh
+    le = O.LINEAR_ELASTIC
+    out["cube4_le_ramp"] = (
+        m4, [O.Material(le)], [O.Solver(0.0, 0.03, 0.5, O.cube_bcs(4, 0.002))], None,
+        [every("DEFO_ENERGY", "Sum"), every("DEFO_ENERGY", "Max"), every("SVM", "Max"), every("PZZ", "Mean"),
+         every("KVM", "Min"), every("VOLUME", "Sum")])
+    m2b = O.cube_mesh(2)
+    m2b.elem_mat = (np.arange(m2b.ne) % 2).astype(np.int32)
+    out["cube2_le_cnh"] = (m2b, [O.Material(le, 2e6, 0.28, 1200.0), O.Material(cnh, 1e6, 0.3, 1000.0)],
+                           [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(2, 0.002))])
     side4 = plane_faces(m4, 0, 1.0)
     out["cube4_stvk_pressure_ramp"] = (
         m4, [O.Material(stvk)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(4, 0.001))],

@@ -117,7 +117,7 @@ def test_parse_node_extractions(tmp_path):
     assert [e["nodes"] for e in d["extractions"]] == [len(x[4]) for x in ex]
 
 
-ELEMENT_CASES = ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction"]
+ELEMENT_CASES = ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction", "cube4_le_ramp"]
 
 
 @pytest.mark.parametrize("name", ELEMENT_CASES)

@@ -46,7 +46,8 @@ def test_exact_mode_matches_reference(name):
     (u, v, a), (ur, vr, ar), steps, ref_steps = run_case(name, msx.FP64_EXACT)
     assert steps == ref_steps
     assert rel(u, ur) <= 1e-12 and rel(v, vr) <= 1e-12 and rel(a, ar) <= 1e-11
-    if "stvk" in name:   # no log/pow on this path: bit-identical to the reference
+    if all(m.law in (O.STVK, O.LINEAR_ELASTIC) for m in load(name)[1]):
+        # no log/pow on these laws' path: bit-identical to the reference
         assert np.array_equal(u, ur) and np.array_equal(v, vr) and np.array_equal(a, ar)
 
 
@@ -68,7 +69,7 @@ def test_double_word_mode_matches_reference(name):
     assert rel(v, vr) <= 1e-10
 
 
-@pytest.mark.parametrize("name", [n for n in names() if n.startswith("cube10")])
+@pytest.mark.parametrize("name", [n for n in names() if n.startswith("cube10")] + ["cube4_le_ramp"])
 def test_mixed_mode_error_bound(name):
     (u, v, a), (ur, vr, ar), steps, ref_steps = run_case(name, msx.MIXED)
     assert abs(steps - ref_steps) <= 1
@@ -92,7 +93,7 @@ def test_setup_data_bitwise_equal_to_oracle():
     assert np.array_equal(mass, O.lumped_mass(mesh, mats, wJo))
 
 
-@pytest.mark.parametrize("law", [msx.NEO_HOOKEAN, msx.COMPRESSIBLE_NH, msx.STVK])
+@pytest.mark.parametrize("law", [msx.NEO_HOOKEAN, msx.COMPRESSIBLE_NH, msx.STVK, msx.LINEAR_ELASTIC])
 @pytest.mark.parametrize("precision,tol", [(msx.FP64_EXACT, 0.0), (msx.FP64, 1e-12), (msx.MIXED, 2e-5),
                                            (msx.DOUBLE_WORD, 1e-11)])
 def test_internal_force_matches_oracle(law, precision, tol):
@@ -104,7 +105,7 @@ def test_internal_force_matches_oracle(law, precision, tol):
     S = msx.Solver(X, conn, [(law, 1e6, 0.3, 1000.0)], [], 0.0, 1.0, 0.5, precision=precision)
     f = S.internal_force(u)
     fo, _, _ = O.internal_force(mesh, [mat], u)
-    if tol == 0.0 and law == msx.STVK:
+    if tol == 0.0 and law in (msx.STVK, msx.LINEAR_ELASTIC):
         assert np.array_equal(f, fo)
     else:
         assert rel(f, fo) <= max(tol, 1e-14), rel(f, fo)
@@ -171,7 +172,8 @@ def test_degenerate_element_gives_negative_jacobian_error():
     assert ei.value.status == 3
 
 
-@pytest.mark.parametrize("name", ["cube4_nh_ramp", "cube4_stvk_ramp", "cube10_cnh_S", "cube2_two_materials"])
+@pytest.mark.parametrize("name", ["cube4_nh_ramp", "cube4_stvk_ramp", "cube10_cnh_S", "cube2_two_materials",
+                                  "cube4_le_ramp", "cube2_le_cnh"])
 def test_element_fields_match_oracle(name):
     mesh, mats, solvers, (u, v, a), _ = load(name)
     m = [(x.law, x.young, x.nu, x.rho) for x in mats]
@@ -246,7 +248,8 @@ def test_node_values_match_oracle(precision, tol):
 ELEMENT_QS = [q for q in msx.ELEMENT_QUANTITIES if q != "EXTERNAL_ENERGY"]
 
 
-@pytest.mark.parametrize("name", ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction"])
+@pytest.mark.parametrize("name", ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction",
+                                  "cube4_le_ramp"])
 def test_element_values_match_oracle(name):
     """msx_element_values against the oracle at the same state (the reference's
     final u, v put in with msx_set_state): both follow the reference's operation

@@ -159,7 +159,7 @@ def element_extraction_rows(name):
     return out
 
 
-ELEMENT_CASES = ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction"]
+ELEMENT_CASES = ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction", "cube4_le_ramp"]
 
 
 @pytest.mark.parametrize("name", ELEMENT_CASES)

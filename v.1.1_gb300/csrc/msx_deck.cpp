@@ -273,6 +273,15 @@ Deck parse(const std::string &path)
                     m.young = atof(f[0].c_str());
                     m.nu = atof(f[1].c_str());
                     i += 2;
+                } else if (starts(K, "*Linear-Elastic")) {
+                    // IO/inputFile.cpp:886-925: "E, nu[, PlaneStress|PlaneStrain]"; the
+                    // stress state only matters in 2D
+                    auto f = split(lines[i + 1]);
+                    if (f.size() < 2) die("*Linear-Elastic needs E, nu", (int)i + 2);
+                    m.law = MSX_LAW_LINEAR_ELASTIC;
+                    m.young = atof(f[0].c_str());
+                    m.nu = atof(f[1].c_str());
+                    i += 2;
                 } else if (starts(K, "*List of Elements")) {
                     if (d.elem_mat.size() != d.conn.size() / 4) d.elem_mat.assign(d.conn.size() / 4, -1);
                     if (starts(lines[i + 1], "All")) {
@@ -290,7 +299,7 @@ Deck parse(const std::string &path)
                     die("unsupported material keyword " + K, (int)i + 1);
                 }
             }
-            if (m.law < 0 || !have_rho) die("material needs *Density and *HyperElastic", ln);
+            if (m.law < 0 || !have_rho) die("material needs *Density and *HyperElastic or *Linear-Elastic", ln);
             d.mats.push_back(m);
         } else if (starts(L, "*SOLVER")) {
             if (trim(L.substr(L.find(',') + 1)) != "EXPLICIT") die("only *SOLVER, EXPLICIT is supported", ln);

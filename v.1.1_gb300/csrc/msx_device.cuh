@@ -67,7 +67,8 @@ __device__ __forceinline__ double char_length_ref(const double *x)
 
 // First Piola stress in the reference's operation order:
 // hyperElasticNeoHookean.cpp:84-127 (Neo-Hookean), :235-259 (compressible),
-// hyperElasticStVenantKirchhoff.cpp:64-101,219-222 (StVK).
+// hyperElasticStVenantKirchhoff.cpp:64-101,219-222 (StVK), linearElastic.cpp
+// :58-82,114-145 (linear elastic: the small-strain stress is returned as P).
 __device__ __forceinline__ void stress_ref(const MatParams &m, const double *F, double *P)
 {
     if (m.law == 1) {
@@ -132,6 +133,19 @@ __device__ __forceinline__ void stress_ref(const MatParams &m, const double *F, 
                 for (int k = 0; k < 3; k++) c += Ca[i * 3 + k] * iF[j * 3 + k] * J;
                 P[i * 3 + j] = c;
             }
+    } else if (m.law == 3) {
+        // linearElastic.cpp:71-76 E = (F + F^T)/2 - I, :114-145 P = mu2 E + lam tr(E) I
+        double E[9], trE = 0;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) E[i * 3 + j] = 0.5 * (F[i * 3 + j] + F[j * 3 + i] - 2. * (i == j ? 1. : 0.));
+#pragma unroll
+        for (int i = 0; i < 3; i++) trE += E[i * 3 + i];
+#pragma unroll
+        for (int i = 0; i < 9; i++) P[i] = E[i] * m.mu2;
+#pragma unroll
+        for (int i = 0; i < 3; i++) P[i * 3 + i] += m.lam_stvk * trE;
     } else {
         double C[9], S[9];
 #pragma unroll
@@ -784,6 +798,19 @@ __device__ __forceinline__ double log_near1(double J)
 // the law's scalar coefficients instead of scaling the nine entries of P.
 __device__ __forceinline__ void stress_fast(const MatParams &m, const double *F, double wJ, double *P)
 {
+    if (m.law == 3) {
+        // linear elastic: wJ P = wJ (mu2 E + lam tr(E) I), E = (F + F^T)/2 - I
+        const double h = m.mu2 * wJ;
+        const double E00 = F[0] - 1.0, E11 = F[4] - 1.0, E22 = F[8] - 1.0;
+        const double dg = m.lam_stvk * ((E00 + E11) + E22) * wJ;
+        P[0] = h * E00 + dg;
+        P[4] = h * E11 + dg;
+        P[8] = h * E22 + dg;
+        P[1] = P[3] = 0.5 * h * (F[1] + F[3]);
+        P[2] = P[6] = 0.5 * h * (F[2] + F[6]);
+        P[5] = P[7] = 0.5 * h * (F[5] + F[7]);
+        return;
+    }
     if (m.law == 2) {
         // S = mu2 E + lam tr(E) I, E = (F^T F - I)/2; wJ P = F (wJ S)
         double C00 = F[0] * F[0] + F[3] * F[3] + F[6] * F[6];
@@ -975,6 +1002,16 @@ static __global__ void __launch_bounds__(kElemBlock) elem_force_kernel_fp64(Prob
 __device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H, float Jm1, float lnJ,
                                              float t, float I2, float *P)
 {
+    if (m.law == 3) {
+        // linear elastic: P = mu2 E + lam tr(E) I with E = (H + H^T)/2
+        const float dg = m.lam_stvk_f * t;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+                P[i * 3 + j] = m.mu2_f * (0.5f * (H[i * 3 + j] + H[j * 3 + i])) + (i == j ? dg : 0.0f);
+        return;
+    }
     if (m.law == 2) {
         // E = (H + H^T + H^T H)/2, S = mu2 E + lam tr(E) I, P = (I + H) S
         float E[9];
@@ -1282,6 +1319,19 @@ __device__ __forceinline__ float2 dw_rcp(float2 y)
 // wJ * P through the cofactor, as stress_fast does in FP64.
 __device__ __forceinline__ void stress_dw(const MatParams &m, const float2 *F, float2 wJ, float2 *P)
 {
+    if (m.law == 3) {
+        // linear elastic: wJ P = wJ (mu2 E + lam tr(E) I), E = (F + F^T)/2 - I
+        const float2 h = dw_mul(m.mu2_w, wJ);
+        const float2 E00 = dw_add_f(F[0], -1.0f), E11 = dw_add_f(F[4], -1.0f), E22 = dw_add_f(F[8], -1.0f);
+        const float2 dg = dw_mul(dw_mul(m.lam_stvk_w, dw_add(dw_add(E00, E11), E22)), wJ);
+        P[0] = dw_add(dw_mul(h, E00), dg);
+        P[4] = dw_add(dw_mul(h, E11), dg);
+        P[8] = dw_add(dw_mul(h, E22), dg);
+        P[1] = P[3] = dw_mul(h, dw_scale2(dw_add(F[1], F[3]), 0.5f));
+        P[2] = P[6] = dw_mul(h, dw_scale2(dw_add(F[2], F[6]), 0.5f));
+        P[5] = P[7] = dw_mul(h, dw_scale2(dw_add(F[5], F[7]), 0.5f));
+        return;
+    }
     if (m.law == 2) {
         // S = mu2 E + lam tr(E) I with E = (F^T F - I)/2; C_ii - 1 from the dot's initial -1
         const float2 C00 = dw_dot3(F[0], F[0], F[3], F[3], F[6], F[6], -1.0f);
@@ -1942,7 +1992,8 @@ __global__ void element_fields_kernel(Problem p, double *cauchy, double *gl, dou
         for (int i = 0; i < 9; i++) S[i] = S[i] * detJinv;
     }
     // the compressible neo-Hookean law never updates its Green-Lagrange strain
-    // (hyperElasticNeoHookean.cpp:221-289), so the reference reports zero
+    // (hyperElasticNeoHookean.cpp:221-289), so the reference reports zero; the
+    // linear-elastic law stores its small strain there (linearElastic.cpp:71-76)
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -1950,7 +2001,9 @@ __global__ void element_fields_kernel(Problem p, double *cauchy, double *gl, dou
             double c = 0;
 #pragma unroll
             for (int k = 0; k < 3; k++) c += F[k * 3 + i] * F[k * 3 + j];
-            E[i * 3 + j] = m.law == 1 ? 0.0 : 0.5 * (c - (i == j ? 1.0 : 0.0));
+            E[i * 3 + j] = m.law == 1 ? 0.0
+                         : m.law == 3 ? 0.5 * (F[i * 3 + j] + F[j * 3 + i] - 2. * (i == j ? 1. : 0.))
+                                      : 0.5 * (c - (i == j ? 1.0 : 0.0));
         }
     if (cauchy)
 #pragma unroll
@@ -1999,6 +2052,14 @@ __device__ double element_quantity_ref(const Problem &p, int q, long long e)
     }
     if (q >= MSX_ELEM_FXX && q <= MSX_ELEM_FZZ) return F[q - MSX_ELEM_FXX];
     if (q == MSX_ELEM_VOLUME) return p.wJ[e] * det3_ref(F);
+    if (q == MSX_ELEM_DEFO_ENERGY && m.law == 3) {
+        // linearElastic.cpp:88-101: 0.5 (P:F - P:I), contractions summed from 0
+        double P[9], a = 0, b = 0;
+        stress_ref(m, F, P);
+        for (int i = 0; i < 9; i++) a += P[i] * F[i];
+        for (int i = 0; i < 9; i++) b += P[i] * ((i % 4) == 0 ? 1. : 0.);
+        return 0.5 * (a - b);
+    }
     if (q == MSX_ELEM_DEFO_ENERGY) {
         double C[9];
         for (int i = 0; i < 3; i++)

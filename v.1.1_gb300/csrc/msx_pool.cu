@@ -153,7 +153,7 @@ static size_t footprint(long long nn, long long ne, long long nbc, int precision
 
 static msx_status make_mat(const msx_material &m, MatParams &o)
 {
-    if (m.law < 0 || m.law > 2) return pfail(MSX_ERR_ARG, "unknown constitutive law");
+    if (m.law < 0 || m.law > 3) return pfail(MSX_ERR_ARG, "unknown constitutive law");
     if (!material_params(m, o)) return pfail(MSX_ERR_ARG, "material needs E > 0, rho > 0, -1 < nu < 0.5");
     return MSX_OK;
 }

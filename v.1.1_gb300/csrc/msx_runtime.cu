@@ -143,7 +143,7 @@ struct msx_handle {
 // false for an invalid material.
 bool msx::material_params(const msx_material &m, MatParams &o)
 {
-    if (m.law < 0 || m.law > 2) return false;
+    if (m.law < 0 || m.law > 3) return false;
     if (!(m.young > 0) || !(m.rho > 0) || !(m.nu > -1.0) || !(m.nu < 0.5)) return false;
     memset(&o, 0, sizeof(o));
     const double E = m.young, nu = m.nu;
@@ -158,8 +158,8 @@ bool msx::material_params(const msx_material &m, MatParams &o)
     // hyperElasticStVenantKirchhoff.cpp:68-69
     o.mu2 = E / (1. + nu);
     o.lam_stvk = E * nu / ((1. + nu) * (1. - (2 * nu)));
-    // soundSpeed: NH forms :51-54, StVK :50-55
-    o.c = m.law == 2 ? std::sqrt(E / m.rho) : std::sqrt((o.lambda + 2 * o.mu) / m.rho);
+    // soundSpeed: NH forms :51-54, StVK :50-55, linear elastic linearElastic.cpp:43-48
+    o.c = m.law >= 2 ? std::sqrt(E / m.rho) : std::sqrt((o.lambda + 2 * o.mu) / m.rho);
     o.lambda_f = (float)o.lambda;
     o.mu_f = (float)o.mu;
     o.K1_f = (float)o.K1;
@@ -178,7 +178,7 @@ bool msx::material_params(const msx_material &m, MatParams &o)
 
 static msx_status make_material(const msx_material &m, MatParams &o)
 {
-    if (m.law < 0 || m.law > 2) return fail(MSX_ERR_ARG, "unknown constitutive law");
+    if (m.law < 0 || m.law > 3) return fail(MSX_ERR_ARG, "unknown constitutive law");
     if (!material_params(m, o)) return fail(MSX_ERR_ARG, "material needs E > 0, rho > 0, -1 < nu < 0.5");
     return MSX_OK;
 }
