@@ -113,8 +113,10 @@ def make_case(n):
     return X, conn, bcs
 
 
-def run_variant(X, conn, bcs, precision, steps, warmup, device):
-    """Create, warm up, then time exactly `steps` steps with the mesh resident."""
+def run_variant(X, conn, bcs, precision, steps, warmup, device, keep_u=False):
+    """Create, warm up, then time exactly `steps` steps with the mesh resident.
+    With keep_u, also return u after the run (warm-up + steps + the 6 profiled
+    steps), to compare the precision modes at the same step."""
     import msx
     S = msx.Solver(X, conn, [MATERIAL], bcs, 0.0, 1e30, 0.5, max_steps=0, precision=precision)
     S.run(warmup)
@@ -122,8 +124,9 @@ def run_variant(X, conn, bcs, precision, steps, warmup, device):
         rep = S.run(steps)
     assert rep.steps == steps, rep
     prof = S.profile(6)
+    u = S.state()[0] if keep_u else None
     S.close()
-    return rep, prof, ck.summary()
+    return (rep, prof, ck.summary(), u) if keep_u else (rep, prof, ck.summary())
 
 
 def mixed_roofline(ne, nn, prof, ms_per_step):
@@ -405,18 +408,22 @@ def main():
 
     barrier(ws)
     first = {"mixed": msx.MIXED, "fp64_exact": msx.FP64_EXACT, "dword": msx.DOUBLE_WORD}.get(args.only, msx.FP64)
-    rep, prof, clocks = run_variant(X, conn, bcs, first, args.steps, args.warmup, local)
+    rep, prof, clocks, u_first = run_variant(X, conn, bcs, first, args.steps, args.warmup, local, keep_u=True)
     secs = reduce_max(rep.device_ms / 1e3, ws)
     value = ws * ne * args.steps / secs
 
     variants = {}
     if not args.no_variants and args.only is None:
         for name, prec in (("mixed", msx.MIXED), ("double_word", msx.DOUBLE_WORD), ("fp64_exact", msx.FP64_EXACT)):
-            r2, p2, c2 = run_variant(X, conn, bcs, prec, args.steps, args.warmup, local)
+            r2, p2, c2, u2 = run_variant(X, conn, bcs, prec, args.steps, args.warmup, local, keep_u=True)
             s2 = reduce_max(r2.device_ms / 1e3, ws)
             variants[name] = {"value": ws * ne * args.steps / s2, "ms_per_step": 1e3 * s2 / args.steps,
                               "element_kernel_ms": p2.element_ms, "node_kernel_ms": p2.node_ms,
-                              "clocks": c2}
+                              "clocks": c2,
+                              # error against the plain FP64 run at the same step (FP64 equals the
+                              # oracle to ~1e-15 on this mesh: tests/test_gpu_large.py)
+                              "rel_l2_u_vs_fp64": float(np.linalg.norm(u2 - u_first) /
+                                                        max(np.linalg.norm(u_first), 1e-300))}
             if name == "mixed":
                 variants[name]["roofline"] = mixed_roofline(ne, nn, p2, 1e3 * s2 / args.steps)
             if name == "double_word":
