@@ -1071,12 +1071,11 @@ __device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H,
 }
 
 template <bool FORCE_ONLY>
-__device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, int parity)
+__device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, int parity, int4 cn)
 {
     const long long ne = p.ne, nn = p.nn;
     float vmin = INFINITY;
     {
-        int4 cn = p.conn[e];
         int nd[4] = {cn.x, cn.y, cn.z, cn.w};
         float G[9];
 #pragma unroll
@@ -1170,7 +1169,7 @@ __device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, 
 static __global__ void __launch_bounds__(kElemBlock) elem_force_kernel_mixed(Problem p, int parity)
 {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < p.ne) elem_body_mixed<true>(p, e, parity);
+    if (e < p.ne) elem_body_mixed<true>(p, e, parity, p.conn[e]);
 }
 
 
@@ -1413,10 +1412,9 @@ static __device__ __noinline__ double cfl_dw(const Problem &p, long long e)
 }
 
 template <bool FORCE_ONLY>
-__device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int parity)
+__device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int parity, int4 cn)
 {
     const long long ne = p.ne, nn = p.nn;
-    int4 cn = p.conn[e];
     int nd[4] = {cn.x, cn.y, cn.z, cn.w};
     float2 G[9];
 #pragma unroll
@@ -1467,7 +1465,7 @@ __device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int
 static __global__ void __launch_bounds__(kElemBlock) elem_force_kernel_dw(Problem p, int parity)
 {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < p.ne) elem_body_dw<true>(p, e, parity);
+    if (e < p.ne) elem_body_dw<true>(p, e, parity, p.conn[e]);
 }
 
 // Node body of the double-word mode: the mixed mode's four-lane gather and
@@ -1667,9 +1665,19 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
         if (p.ctrl[parity].ran) {
             if (MODE != MODE_MIXED && threadIdx.x == 0) s_ncand = 0;
             float v32 = INFINITY;
-            for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
-                float d = MODE == MODE_MIXED ? elem_body_mixed<false>(p, e, parity)
-                                             : (MODE == MODE_DW ? elem_body_dw<false>(p, e, parity)
+            // the mixed and double-word bodies take the element's connectivity
+            // loaded one element ahead, so their node gathers wait for one memory
+            // latency instead of two (connectivity, then the nodes)
+            long long e = tl.begin + threadIdx.x;
+            int4 cn_next = make_int4(0, 0, 0, 0);
+            if (MODE == MODE_MIXED || MODE == MODE_DW) {
+                if (e < tl.end) cn_next = p.conn[e];
+            }
+            for (; e < tl.end; e += blockDim.x) {
+                const int4 cn = cn_next;
+                if ((MODE == MODE_MIXED || MODE == MODE_DW) && e + blockDim.x < tl.end) cn_next = p.conn[e + blockDim.x];
+                float d = MODE == MODE_MIXED ? elem_body_mixed<false>(p, e, parity, cn)
+                                             : (MODE == MODE_DW ? elem_body_dw<false>(p, e, parity, cn)
                                                                 : elem_body_fp64<false>(p, e, parity));
                 if (MODE != MODE_MIXED) sdt[e - tl.begin] = d;
                 if (d >= 0.0f) v32 = fminf(v32, d);
