@@ -208,6 +208,7 @@ class Solver:
     bcs: list = field(default_factory=list)   # (dof, mode, value, ramp_steps)
     max_steps: int = 0
     forces_out: tuple = None                  # *Forces: (frequency, [(node, direction), ...])
+    outputs: int = 1                          # *Outputs: number of VTK outputs of the block
 
 
 def cube_mesh(n: int, seed: int = 1234, jitter: float = 0.1) -> Mesh:
@@ -502,7 +503,7 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Load
             raise ValueError("one *BOUNDARY block per solver: a single mode only")
         mode = modes.pop() if modes else BC_RAMP
         lines += ["*SOLVER, EXPLICIT", "*Scale Factor", "%.17g" % s.scale_factor,
-                  "*Outputs", "1", "*Time", "%.17g, %.17g" % (s.t0, s.tf),
+                  "*Outputs", "%d" % s.outputs, "*Time", "%.17g, %.17g" % (s.t0, s.tf),
                   "*BOUNDARY, TYPE=DISPLACEMENT " + ("INST" if mode == BC_INST else "RAMP")]
         for dof, _, value, _ in s.bcs:
             lines.append("%d,%d,%.17g" % (dof % nn + 1, dof // nn, value))

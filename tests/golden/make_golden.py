@@ -148,6 +148,17 @@ def cases(ref_src):
     m2b.elem_mat = (np.arange(m2b.ne) % 2).astype(np.int32)
     out["cube2_le_cnh"] = (m2b, [O.Material(le, 2e6, 0.28, 1200.0), O.Material(cnh, 1e6, 0.3, 1000.0)],
                            [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(2, 0.002))])
+    # every output of the explicit solver at once in a two-block chain: VTK at the
+    # *Outputs cadence, node and element extraction, *Forces, with surface loads
+    out["cube3_cnh_all_outputs"] = (
+        m3, [O.Material(cnh)],
+        [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.002), forces_out=(300.0, [(nd, 2) for nd in botn3[:4]]),
+                  outputs=4),
+         O.Solver(0.02, 0.035, 0.45, O.cube_bcs(3, 0.003), forces_out=(1e4, [(21, 0), (42, 2)]), outputs=3)],
+        O.Loads([("traction_ramp", 0.0, 0.015, (1e3, -2e3, 4e3), S, el) for S, el in top3] + [("gravity", 9.81)]),
+        [("top", "Unknown", "Mean", 2, topn), ("bottom", "InternalForce", "Sum", 2, botn),
+         every("DEFO_ENERGY", "Sum"), every("KIN_ENERGY", "Max"), every("EXTERNAL_ENERGY", "Sum"),
+         ("element", "mid", "SVM", "Mean", mid)])
     side4 = plane_faces(m4, 0, 1.0)
     out["cube4_stvk_pressure_ramp"] = (
         m4, [O.Material(stvk)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(4, 0.001))],
@@ -170,6 +181,8 @@ def pack(mesh, mats, solvers, ref, orc, loads=None, extractions=()):
          "u": ref[0], "v": ref[1], "a": ref[2], "steps": np.array(orc.steps)}
     if mesh.elem_mat is not None:
         d["elem_mat"] = mesh.elem_mat
+    if any(s.outputs != 1 for s in solvers):
+        d["outputs"] = np.array([s.outputs for s in solvers])
     if any(s.forces_out for s in solvers):
         import json
         d["forces_out_json"] = np.array(json.dumps([s.forces_out for s in solvers]))

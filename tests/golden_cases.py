@@ -24,6 +24,9 @@ def load(name):
         bcs = [(int(b[0]), int(b[1]), float(b[2]), int(b[3])) for b in d["bcs"][k:k + nb]]
         k += nb
         solvers.append(O.Solver(float(t0), float(tf), float(sf), bcs))
+    if "outputs" in d:
+        for s, k in zip(solvers, d["outputs"]):
+            s.outputs = int(k)
     if "forces_out_json" in d:
         import json
         for s, fo in zip(solvers, json.loads(str(d["forces_out_json"]))):

@@ -235,3 +235,35 @@ def test_print_forces_match_reference_files(tmp_path, precision, tol):
         assert np.array_equal(g[:, :2], e[:, :2]) and np.abs(g[:, 3] - e[:, 3]).max() <= 1.01e-6, fname
         scale = np.abs(e[:, 2]).max()
         assert np.abs(g[:, 2] - e[:, 2]).max() <= 1.01e-6 + tol * scale, fname
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [("exact", 1e-12), ("fp64", 1e-9), ("dword", 1e-9)])
+def test_all_outputs_in_one_chain(tmp_path, precision, tol):
+    """A two-block chain with VTK outputs, node and element extraction, *Forces
+    and surface loads: the same files as the reference (names, headers, rows),
+    the VTK outputs at its times."""
+    name = "cube3_cnh_all_outputs"
+    write(tmp_path, name)
+    d = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-outputDir", str(out),
+                        "-precision", precision], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    times = np.array([o[0] for o in O.read_vtk_outputs(str(out))])
+    assert len(times) == len(d["vtk_times"]) and np.allclose(times, d["vtk_times"], rtol=1e-5, atol=1e-12)
+    _, files = load_extractions(name)
+    assert sorted(f.name for f in out.glob("*.csv")) == sorted(files)
+    for fname, ref_text in files.items():
+        ref = ref_text.strip().split("\n")
+        got = (out / fname).read_text().strip().split("\n")
+        assert got[0] == ref[0] and len(got) == len(ref), fname
+        g = np.array([[float(x) for x in ln.rstrip(",").split(",")] for ln in got[1:]])
+        e = np.array([[float(x) for x in ln.rstrip(",").split(",")] for ln in ref[1:]])
+        if fname.startswith("externalForces"):   # %f: six decimals
+            assert np.array_equal(g[:, :2], e[:, :2]) and np.abs(g[:, 3] - e[:, 3]).max() <= 1.01e-6, fname
+            assert np.abs(g[:, 2] - e[:, 2]).max() <= 1.01e-6 + tol * np.abs(e[:, 2]).max(), fname
+        else:                                     # %.16g
+            assert np.allclose(g[:, 0], e[:, 0], rtol=1e-12, atol=0), fname
+            assert np.abs(g[:, 1:] - e[:, 1:]).max() <= tol * max(np.abs(e[:, 1:]).max(), 1e-300), fname
