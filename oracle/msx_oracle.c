@@ -242,6 +242,19 @@ void orc_stress(const orc_material *m, const double *F, double *P)
     }
 }
 
+/* solvers.cpp:403-433 updateActivation with the laws' checkActivation
+ * (hyperElasticStVenantKirchhoff.cpp:185-194, linearElastic.cpp:230-239): with
+ * the *ACTIVATION option a St-Venant-Kirchhoff or linear-elastic Gauss point is
+ * active once its first internal variable (the activation time) is <= t; the
+ * neo-Hookean laws have no such variable and stay active. */
+static int gp_active(const orc_problem *p, int64_t e, double t)
+{
+    if (!p->activation || !p->act_time) return 1;
+    int law = p->mats[p->elem_mat ? p->elem_mat[e] : 0].law;
+    if (law != ORC_STVK && law != ORC_LINEAR_ELASTIC) return 1;
+    return p->act_time[e] <= t;
+}
+
 /* constitutiveManager.cpp:137-164 computeKinematicVariables (F), then the law,
  * then constitutiveAlgorithms.cpp:33-57 getForceVector; fe[a + 4*i]. */
 static void element_force(const double *dphi, double wJ, const orc_material *m,
@@ -332,9 +345,10 @@ int orc_element_fields(int64_t nn, int64_t ne, const int32_t *conn, const double
 }
 
 /* solverExplicit.cpp:363-379 computeInternalForce: scatter in element order. */
-int orc_internal_force(int64_t nn, int64_t ne, const int32_t *conn, const double *dphi,
-                       const double *wJ, const int32_t *elem_mat, const orc_material *mats,
-                       const double *u, double *fint, double *F_out, double *P_out, int nthreads)
+static int internal_force(int64_t nn, int64_t ne, const int32_t *conn, const double *dphi,
+                          const double *wJ, const int32_t *elem_mat, const orc_material *mats,
+                          const double *u, double *fint, double *F_out, double *P_out, int nthreads,
+                          const orc_problem *act, double t)
 {
     double *fe = (double *)malloc(sizeof(double) * 12 * (size_t)(ne > 0 ? ne : 1));
     if (!fe) return ORC_ERR_ARG;
@@ -342,6 +356,7 @@ int orc_internal_force(int64_t nn, int64_t ne, const int32_t *conn, const double
 #pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
 #endif
     for (int64_t e = 0; e < ne; e++) {
+        if (act && !gp_active(act, e, t)) continue;   /* solverExplicit.cpp:370-371 */
         double ue[12];
         for (int a = 0; a < 4; a++)
             for (int i = 0; i < 3; i++) ue[a * 3 + i] = u[conn[e * 4 + a] + i * nn];
@@ -350,11 +365,20 @@ int orc_internal_force(int64_t nn, int64_t ne, const int32_t *conn, const double
     }
     (void)nthreads;
     for (int64_t i = 0; i < 3 * nn; i++) fint[i] = 0;
-    for (int64_t e = 0; e < ne; e++)
+    for (int64_t e = 0; e < ne; e++) {
+        if (act && !gp_active(act, e, t)) continue;
         for (int i = 0; i < 3; i++)
             for (int a = 0; a < 4; a++) fint[conn[e * 4 + a] + nn * i] += fe[12 * e + a + 4 * i];
+    }
     free(fe);
     return ORC_OK;
+}
+
+int orc_internal_force(int64_t nn, int64_t ne, const int32_t *conn, const double *dphi,
+                       const double *wJ, const int32_t *elem_mat, const orc_material *mats,
+                       const double *u, double *fint, double *F_out, double *P_out, int nthreads)
+{
+    return internal_force(nn, ne, conn, dphi, wJ, elem_mat, mats, u, fint, F_out, P_out, nthreads, 0, 0.0);
 }
 
 /* solvers.cpp:296-320 calculateCriticalTimeStep(nod, elem, uK) without the
@@ -660,7 +684,7 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
             v[d] = Ud;
             a[d] = 0.;
         }
-        orc_internal_force(nn, ne, p->conn, dphi, wJ, p->elem_mat, p->mats, u, fint, 0, 0, p->nthreads);
+        internal_force(nn, ne, p->conn, dphi, wJ, p->elem_mat, p->mats, u, fint, 0, 0, p->nthreads, p, t);
         external_force(p, absJ, dphi, u, t, fext);
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static) num_threads(p->nthreads > 0 ? p->nthreads : 1)
@@ -710,6 +734,7 @@ static double gp_value(const orc_problem *p, const double *dphi, const double *w
     const int64_t nn = p->nn;
     const int32_t *c = p->conn + 4 * e;
     const orc_material *m = &p->mats[p->elem_mat ? p->elem_mat[e] : 0];
+    if (!gp_active(p, e, p->time)) return 0.;   /* dataExtraction.cpp:510 (and the energies skip it) */
     if (q >= ORC_Q_INVAR1 && q <= ORC_Q_INVAR6) return 0.;
     if (q == ORC_Q_KIN) {
         double vel[3] = {0., 0., 0.}, val = 0;
@@ -830,7 +855,7 @@ int orc_element_reduce(const orc_problem *p, const double *u, const double *v, c
         double ener = 0, volume = 0;
         int init = 0;
         for (int64_t e = 0; e < p->ne; e++) {
-            if (!sel[e]) continue;
+            if (!sel[e] || !gp_active(p, e, p->time)) continue;
             /* defoEnergy and kineticEnergy weigh the density by dV = wJ;
              * volume's own value is its dV = wJ det F */
             double x = gp_value(p, dphi, wJ, u, v, q, e), dV = q == ORC_Q_VOLUME ? x : wJ[e];

@@ -64,6 +64,9 @@ typedef struct {
     int32_t gravity_first;    /* 1: *GRAVITY precedes *BOUNDARY, TYPE=FORCE   */
     const orc_load *loads; int64_t nloads;     /* when nloads > 0: all Neumann blocks in deck
                                                   order; forces/gravity above are then unused */
+    const double *act_time;   /* ne activation times (first internal variable), or NULL  */
+    int32_t activation;       /* 1: the block's *ACTIVATION option (element birth)       */
+    double time;              /* element extraction: the time the element states are at */
 } orc_problem;
 
 typedef struct { int64_t steps; double t, dt_last, dt_init; int32_t status; double loop_seconds; } orc_result;

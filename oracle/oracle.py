@@ -59,7 +59,8 @@ class _Problem(C.Structure):
                 ("scale_factor", C.c_double), ("max_steps", C.c_int64),
                 ("first_step_zero_uK", C.c_int32), ("nthreads", C.c_int32),
                 ("forces", C.c_void_p), ("nforces", C.c_int64), ("gravity", C.c_double),
-                ("gravity_first", C.c_int32), ("loads", C.c_void_p), ("nloads", C.c_int64)]
+                ("gravity_first", C.c_int32), ("loads", C.c_void_p), ("nloads", C.c_int64),
+                ("act_time", C.c_void_p), ("activation", C.c_int32), ("time", C.c_double)]
 
 
 class _Result(C.Structure):
@@ -189,6 +190,7 @@ class Mesh:
     X: np.ndarray          # (3, nn) float64
     conn: np.ndarray       # (ne, 4) int32, 0-based
     elem_mat: np.ndarray | None = None
+    act_time: np.ndarray | None = None   # (ne,) activation times (*INITINTVARS position 1), or None (0)
 
     @property
     def nn(self):
@@ -209,6 +211,7 @@ class Solver:
     max_steps: int = 0
     forces_out: tuple = None                  # *Forces: (frequency, [(node, direction), ...])
     outputs: int = 1                          # *Outputs: number of VTK outputs of the block
+    activation: bool = False                  # *ACTIVATION: element birth at the activation times
 
 
 def cube_mesh(n: int, seed: int = 1234, jitter: float = 0.1) -> Mesh:
@@ -295,7 +298,7 @@ def external_force(mesh: Mesh, mats, loads: Loads, u: np.ndarray, t: float) -> n
     em = None if mesh.elem_mat is None else np.ascontiguousarray(mesh.elem_mat, np.int32)
     marr = _mats_array(mats)
     prob = _Problem(nn, mesh.ne, _p(X), _p(conn), _p(em), C.cast(marr, C.c_void_p), len(mats),
-                    None, 0, 0.0, 1.0, 0.5, 0, 0, 1, None, 0, 0.0, 0, C.cast(larr, C.c_void_p), nl)
+                    None, 0, 0.0, 1.0, 0.5, 0, 0, 1, None, 0, 0.0, 0, C.cast(larr, C.c_void_p), nl, None, 0, 0.0)
     f = np.zeros(3 * nn)
     u = np.ascontiguousarray(u, dtype=np.float64)
     lib().orc_external_force(C.byref(prob), _p(u), C.c_double(t), _p(f))
@@ -312,20 +315,32 @@ ELEMENT_QUANTITY = {name: k + 1 for k, name in enumerate(ELEMENT_QUANTITIES)}
 ELEMENT_OPS = {"Mean": 1, "Min": 2, "Max": 3, "Sum": 4}
 
 
-def _plain_problem(mesh: Mesh, mats, keep: list):
+def _plain_problem(mesh: Mesh, mats, keep: list, activation=False, t=0.0):
     X = np.ascontiguousarray(mesh.X)
     conn = np.ascontiguousarray(mesh.conn)
     em = None if mesh.elem_mat is None else np.ascontiguousarray(mesh.elem_mat, np.int32)
     marr = _mats_array(mats)
     keep += [X, conn, em, marr]
+    act = None if mesh.act_time is None else np.ascontiguousarray(mesh.act_time, np.float64)
+    keep.append(act)
     return _Problem(mesh.nn, mesh.ne, _p(X), _p(conn), _p(em), C.cast(marr, C.c_void_p), len(mats),
-                    None, 0, 0.0, 1.0, 0.5, 0, 0, 1, None, 0, 0.0, 0, None, 0)
+                    None, 0, 0.0, 1.0, 0.5, 0, 0, 1, None, 0, 0.0, 0, None, 0,
+                    _p(act), 1 if activation else 0, float(t))
 
 
-def element_values(mesh: Mesh, mats, quantity: str, u, v, elems=None) -> np.ndarray:
+def active_elements(mesh: Mesh, mats, activation: bool, t: float) -> np.ndarray:
+    """Elements active at time t under the *ACTIVATION option (the laws with an
+    activation time: St-Venant-Kirchhoff and linear elastic)."""
+    if not activation or mesh.act_time is None:
+        return np.ones(mesh.ne, bool)
+    laws = np.array([mats[k].law for k in (mesh.elem_mat if mesh.elem_mat is not None else np.zeros(mesh.ne, int))])
+    return ~np.isin(laws, [STVK, LINEAR_ELASTIC]) | (np.asarray(mesh.act_time) <= t)
+
+
+def element_values(mesh: Mesh, mats, quantity: str, u, v, elems=None, activation=False, t=0.0) -> np.ndarray:
     """Per-element value of an element-extraction quantity at the state u, v."""
     keep = []
-    prob = _plain_problem(mesh, mats, keep)
+    prob = _plain_problem(mesh, mats, keep, activation, t)
     el = None if elems is None else np.ascontiguousarray(elems, np.int32)
     out = np.zeros(mesh.ne if el is None else len(el))
     u = np.ascontiguousarray(u, dtype=np.float64)
@@ -335,11 +350,12 @@ def element_values(mesh: Mesh, mats, quantity: str, u, v, elems=None) -> np.ndar
     return out
 
 
-def element_reduce(mesh: Mesh, mats, quantity: str, op: str, u, v, elems=None, fext=None) -> float:
+def element_reduce(mesh: Mesh, mats, quantity: str, op: str, u, v, elems=None, fext=None, activation=False,
+                   t=0.0) -> float:
     """The value one *EXTRACTION, ELEMENT row holds at the state u, v (fext: the
     external force of that step, for EXTERNAL_ENERGY)."""
     keep = []
-    prob = _plain_problem(mesh, mats, keep)
+    prob = _plain_problem(mesh, mats, keep, activation, t)
     el = None if elems is None else np.ascontiguousarray(elems, np.int32)
     u = np.ascontiguousarray(u, dtype=np.float64)
     v = np.ascontiguousarray(v, dtype=np.float64)
@@ -432,6 +448,7 @@ def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int 
     for i, f in enumerate(fl):
         farr[i] = _Force(*f)
     larr, nl, _keep = loads.blocks(nn) if loads else (None, 0, None)
+    act = None if mesh.act_time is None else np.ascontiguousarray(mesh.act_time, np.float64)
     for k, s in enumerate(solvers):
         barr = (_BC * max(1, len(s.bcs)))()
         for i, (dof, mode, value, ramp) in enumerate(s.bcs):
@@ -440,7 +457,8 @@ def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int 
                         C.cast(barr, C.c_void_p), len(s.bcs), s.t0, s.tf, s.scale_factor, s.max_steps,
                         0, nthreads, C.cast(farr, C.c_void_p), len(fl),
                         loads.gravity() if loads else 0.0, loads.gravity_first() if loads else 0,
-                        C.cast(larr, C.c_void_p) if nl else None, nl)
+                        C.cast(larr, C.c_void_p) if nl else None, nl,
+                        _p(act), 1 if s.activation else 0, 0.0)
         hist = np.zeros(max(1, max_hist))
         rc = lib().orc_run(C.byref(prob), _p(u), _p(v), _p(a), _p(hist), max_hist, C.byref(res))
         total += res.steps
@@ -502,7 +520,8 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Load
         if len(modes) > 1:
             raise ValueError("one *BOUNDARY block per solver: a single mode only")
         mode = modes.pop() if modes else BC_RAMP
-        lines += ["*SOLVER, EXPLICIT", "*Scale Factor", "%.17g" % s.scale_factor,
+        lines += ["*SOLVER, EXPLICIT"] + (["*ACTIVATION"] if s.activation else [])
+        lines += ["*Scale Factor", "%.17g" % s.scale_factor,
                   "*Outputs", "%d" % s.outputs, "*Time", "%.17g, %.17g" % (s.t0, s.tf),
                   "*BOUNDARY, TYPE=DISPLACEMENT " + ("INST" if mode == BC_INST else "RAMP")]
         for dof, _, value, _ in s.bcs:
@@ -526,6 +545,13 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Load
             # (src/IO/inputFile.cpp:2010-2053)
             for e in mat_elems[k]:
                 lines += ["*List of Elements", str(int(e) + 1)]
+        # activation times as the first internal variable (src/IO/inputFile.cpp:2055-2111),
+        # after the element list the reader checks them against
+        if mesh.act_time is not None:
+            own = range(mesh.ne) if mat_elems[k] is None else mat_elems[k]
+            rows = ["%d, 1, %.17g" % (int(e) + 1, mesh.act_time[int(e)]) for e in own if mesh.act_time[int(e)] != 0.0]
+            if rows:
+                lines += ["*INITINTVARS"] + rows
     lines.append("*END")
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")

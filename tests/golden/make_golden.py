@@ -159,6 +159,23 @@ def cases(ref_src):
         [("top", "Unknown", "Mean", 2, topn), ("bottom", "InternalForce", "Sum", 2, botn),
          every("DEFO_ENERGY", "Sum"), every("KIN_ENERGY", "Max"), every("EXTERNAL_ENERGY", "Sum"),
          ("element", "mid", "SVM", "Mean", mid)])
+    # element birth (*ACTIVATION with activation times from *INITINTVARS): the upper
+    # elements of a St-Venant-Kirchhoff cube come alive at two later times; a
+    # linear-elastic chain whose second block runs with every element alive
+    m3a = O.cube_mesh(3)
+    zc = np.array([m3a.X[2, m3a.conn[e]].mean() for e in range(m3a.ne)])
+    m3a.act_time = np.where(zc > 0.7, 0.009, np.where(zc > 0.4, 0.004, 0.0))
+    out["cube3_stvk_activation"] = (
+        m3a, [O.Material(stvk)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.002), activation=True, outputs=2)],
+        O.Loads([("gravity", 9.81)]),
+        [every("DEFO_ENERGY", "Sum"), every("KIN_ENERGY", "Sum"), every("VOLUME", "Sum"), every("FZZ", "Mean"),
+         every("SVM", "Max"), every("DEFO_ENERGY", "Min"), ("element", "upper", "PZZ", "Mean", [int(e) for e in np.nonzero(zc > 0.7)[0]])])
+    m3b = O.cube_mesh(3)
+    m3b.act_time = np.where(zc > 0.5, 0.006, 0.0)
+    out["cube3_le_activation_chain"] = (
+        m3b, [O.Material(le)],
+        [O.Solver(0.0, 0.01, 0.5, O.cube_bcs(3, 0.001), activation=True),
+         O.Solver(0.01, 0.02, 0.5, O.cube_bcs(3, 0.002), activation=True)])
     side4 = plane_faces(m4, 0, 1.0)
     out["cube4_stvk_pressure_ramp"] = (
         m4, [O.Material(stvk)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(4, 0.001))],
@@ -181,6 +198,10 @@ def pack(mesh, mats, solvers, ref, orc, loads=None, extractions=()):
          "u": ref[0], "v": ref[1], "a": ref[2], "steps": np.array(orc.steps)}
     if mesh.elem_mat is not None:
         d["elem_mat"] = mesh.elem_mat
+    if mesh.act_time is not None:
+        d["act_time"] = np.asarray(mesh.act_time, np.float64)
+    if any(s.activation for s in solvers):
+        d["activation"] = np.array([int(s.activation) for s in solvers])
     if any(s.outputs != 1 for s in solvers):
         d["outputs"] = np.array([s.outputs for s in solvers])
     if any(s.forces_out for s in solvers):

@@ -24,6 +24,11 @@ def load(name):
         bcs = [(int(b[0]), int(b[1]), float(b[2]), int(b[3])) for b in d["bcs"][k:k + nb]]
         k += nb
         solvers.append(O.Solver(float(t0), float(tf), float(sf), bcs))
+    if "act_time" in d:
+        mesh.act_time = d["act_time"]
+    if "activation" in d:
+        for s, k in zip(solvers, d["activation"]):
+            s.activation = bool(k)
     if "outputs" in d:
         for s, k in zip(solvers, d["outputs"]):
             s.outputs = int(k)

@@ -159,7 +159,8 @@ def element_extraction_rows(name):
     return out
 
 
-ELEMENT_CASES = ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction", "cube4_le_ramp"]
+ELEMENT_CASES = ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction", "cube4_le_ramp",
+                 "cube3_stvk_activation"]
 
 
 @pytest.mark.parametrize("name", ELEMENT_CASES)
@@ -172,12 +173,13 @@ def test_element_extraction_pinned_to_reference(name):
     assert blocks and all(len(b[4]) == steps for b in blocks)
     s0 = solvers[0]
     for k in range(1, steps + 1):
-        r = O.run(mesh, mats, [O.Solver(s0.t0, s0.tf, s0.scale_factor, s0.bcs, max_steps=k)], loads=loads)
+        r = O.run(mesh, mats, [O.Solver(s0.t0, s0.tf, s0.scale_factor, s0.bcs, max_steps=k,
+                                        activation=s0.activation)], loads=loads)
         fext = O.external_force(mesh, mats, loads, r.u, r.t) if loads else np.zeros(3 * mesh.nn)
         for fname, q, op, elems, rows in blocks:
             t, val = rows[k - 1]
             assert t == float("%.16g" % r.t), fname
-            got = O.element_reduce(mesh, mats, q, op, r.u, r.v, elems, fext)
+            got = O.element_reduce(mesh, mats, q, op, r.u, r.v, elems, fext, s0.activation, r.t)
             assert float("%.16g" % got) == val, (fname, k, got, val)
 
 
