@@ -175,6 +175,21 @@ typedef struct {
  * call); takes effect from the next step. */
 msx_status msx_set_load_blocks(msx_handle *h, const msx_load_block *blocks, int64_t num_blocks);
 
+/* Element birth: the reference's *ACTIVATION option of a solver block
+ * (solvers.cpp:403-433, called each step at solverExplicit.cpp:259-264) with the
+ * activation times *INITINTVARS sets as the first internal variable of
+ * St-Venant-Kirchhoff and linear-elastic elements (IO/inputFile.cpp:2055-2111;
+ * elements without one have 0).  activation_time: num_elems values, or NULL to
+ * keep the current ones; enabled: 1 for blocks with *ACTIVATION (applies from
+ * the next step of the current block on, and to later blocks until changed).
+ * While enabled, such an element whose activation time is above the step's time
+ * is dead: it adds no internal force (solverExplicit.cpp:370-371), its output
+ * fields are zero and element extraction skips or zeroes it as the reference
+ * does; the neo-Hookean laws have no activation time and are always alive.  The
+ * lumped mass and the stable time step include every element, as there.  Not
+ * available in msx_pool_*. */
+msx_status msx_set_activation(msx_handle *h, const double *activation_time, int32_t enabled);
+
 /* Nodal values of the current state for the reference's node data extraction
  * (*EXTRACTION, NODE: solvers/dataExtraction.cpp:778-840, written every step by
  * classSolverExplicit::calculate, solverExplicit.cpp:325).  field: displacement

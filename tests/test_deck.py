@@ -86,7 +86,7 @@ def test_deck_run_matches_reference(tmp_path, name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["cube3_cnh_ramp", "cube3_cnh_chain", "cube10_stvk_S"])
+@pytest.mark.parametrize("name", ["cube3_cnh_ramp", "cube3_cnh_chain", "cube10_stvk_S", "cube3_stvk_activation"])
 def test_deck_outputs_follow_reference_cadence(tmp_path, name):
     """VTK outputs at the reference's *Outputs cadence, final fields as the
     reference's own VTK file (6 digits there)."""
@@ -117,7 +117,8 @@ def test_parse_node_extractions(tmp_path):
     assert [e["nodes"] for e in d["extractions"]] == [len(x[4]) for x in ex]
 
 
-ELEMENT_CASES = ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction", "cube4_le_ramp"]
+ELEMENT_CASES = ["cube3_cnh_element_extraction", "cube2_two_materials_element_extraction", "cube4_le_ramp",
+                 "cube3_stvk_activation"]
 
 
 @pytest.mark.parametrize("name", ELEMENT_CASES)

@@ -32,9 +32,13 @@ def run_case(name, precision, spg=0):
     L = load_loads(name)
     if L is not None:
         S.set_load_blocks(L.items)
+    if mesh.act_time is not None:
+        S.set_activation(mesh.act_time, s0.activation)
     total = S.run().steps
     for s in solvers[1:]:
         S.next_solver(s.bcs, s.t0, s.tf, s.scale_factor, precision=precision, steps_per_graph=spg)
+        if mesh.act_time is not None:
+            S.set_activation(None, s.activation)
         total += S.run().steps
     out = S.state()
     S.close()

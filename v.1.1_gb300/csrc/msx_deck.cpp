@@ -46,6 +46,7 @@ struct SolverBlock {
     // the (node, direction) pairs whose internal force is written
     double force_freq = 0;
     std::vector<std::pair<int32_t, int>> force_out;
+    bool activation = false;          // *ACTIVATION (element birth)
 };
 
 struct Deck {
@@ -77,6 +78,7 @@ struct Deck {
     std::vector<Extraction> extractions;
     std::vector<int32_t> conn;
     std::vector<msx_material> mats;
+    std::vector<double> act_time;     // *INITINTVARS position 1 per element (0 without), if any
     std::vector<int32_t> elem_mat;    // -1 until assigned
     std::vector<SolverBlock> solvers;
 };
@@ -282,6 +284,22 @@ Deck parse(const std::string &path)
                     m.young = atof(f[0].c_str());
                     m.nu = atof(f[1].c_str());
                     i += 2;
+                } else if (starts(K, "*INITINTVARS")) {
+                    // IO/inputFile.cpp:2055-2111 and init.cpp:54-80: "element, position, value";
+                    // the St-Venant-Kirchhoff and linear-elastic laws have one internal
+                    // variable, the activation time; the neo-Hookean laws have none
+                    if (m.law != MSX_LAW_STVK && m.law != MSX_LAW_LINEAR_ELASTIC)
+                        die("*INITINTVARS needs a St-Venant-Kirchhoff or linear-elastic law before it", (int)i + 1);
+                    if (d.act_time.empty()) d.act_time.assign(d.conn.size() / 4, 0.0);
+                    for (i++; i < n && !lines[i].empty() && lines[i][0] != '*'; i++) {
+                        auto f = split(lines[i]);
+                        if (f.size() < 3) die("an *INITINTVARS line has element, position, value", (int)i + 1);
+                        long long e = atoll(f[0].c_str()) - 1, pos = atoll(f[1].c_str()) - 1;
+                        if (e < 0 || e >= (long long)d.act_time.size()) die("*INITINTVARS element out of range", (int)i + 1);
+                        if (pos != 0) die("Position of an internal variable not valid", (int)i + 1);
+                        if (!d.elem_mat.empty() && d.elem_mat[e] != id) die("Element on INITINTVARS list not valid", (int)i + 1);
+                        d.act_time[e] = atof(f[2].c_str());
+                    }
                 } else if (starts(K, "*List of Elements")) {
                     if (d.elem_mat.size() != d.conn.size() / 4) d.elem_mat.assign(d.conn.size() / 4, -1);
                     if (starts(lines[i + 1], "All")) {
@@ -340,6 +358,9 @@ Deck parse(const std::string &path)
                         b.value = atof(f[2].c_str());
                         s.bcs.push_back(b);
                     }
+                } else if (starts(K, "*ACTIVATION")) {
+                    s.activation = true;   // IO/inputFile.cpp:2332-2334
+                    i++;
                 } else if (starts(K, "*Forces")) {
                     if (i + 1 >= n) die("*Forces needs a frequency", (int)i + 1);
                     s.force_freq = atof(lines[i + 1].c_str());
@@ -644,6 +665,9 @@ int main(int argc, char **argv)
             }
             st = msx_next_solver(h, s.bcs.data(), (int64_t)s.bcs.size(), &o);
         }
+        // element birth: the activation times once, the block's *ACTIVATION flag each block
+        if (st == MSX_OK && !d.act_time.empty())
+            st = msx_set_activation(h, k == 0 ? d.act_time.data() : nullptr, s.activation ? 1 : 0);
         if (st != MSX_OK) {
             fprintf(stderr, "msx_deck: %s\n", msx_last_error());
             return 1;

@@ -186,6 +186,15 @@ __device__ __forceinline__ const MatParams &mat_of(const Problem &p, long long e
     return p.mats[p.mat ? p.mat[e] : 0];
 }
 
+// Element birth (the reference's *ACTIVATION option: solvers.cpp:403-433 with
+// the laws' checkActivation): a St-Venant-Kirchhoff or linear-elastic element
+// is alive once its activation time is <= t; a dead element adds no internal
+// force (solverExplicit.cpp:370-371).  act_t is null without the option.
+__device__ __forceinline__ bool elem_dead(const Problem &p, long long e, double t)
+{
+    return p.act_t && mat_of(p, e).law >= 2 && t < p.act_t[e];
+}
+
 // Block-wide min of a positive double, then one integer atomicMin on its bit
 // pattern (monotone for non-negative doubles; exact and order independent).
 __device__ __forceinline__ void block_min_to(double v, unsigned long long *slot)
@@ -718,6 +727,7 @@ __device__ __forceinline__ double elem_body_exact(const Problem &p, long long e,
         // constitutiveAlgorithms.cpp:46-56
         double wJ = p.wJ[e];
         double *fe = p.fe + e * 12;
+        const bool dead = !FORCE_ONLY && elem_dead(p, e, p.ctrl[parity].t);
 #pragma unroll
         for (int a = 0; a < 4; a++)
 #pragma unroll
@@ -725,7 +735,7 @@ __device__ __forceinline__ double elem_body_exact(const Problem &p, long long e,
                 double f = 0;
 #pragma unroll
                 for (int J = 0; J < 3; J++) f += wJ * P[i * 3 + J] * dphi[a * 3 + J];
-                fe[a * 3 + i] = 0 + f;
+                fe[a * 3 + i] = dead ? 0.0 : 0 + f;
             }
         if (!FORCE_ONLY) {
             // solvers.cpp:304-317: deformed inscribed sphere
@@ -969,6 +979,9 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
             f[a * 3 + i] = P[i * 3] * G[(a - 1) * 3] + P[i * 3 + 1] * G[(a - 1) * 3 + 1] + P[i * 3 + 2] * G[(a - 1) * 3 + 2];
 #pragma unroll
     for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
+    if (!FORCE_ONLY && elem_dead(p, e, p.ctrl[parity].t))
+#pragma unroll
+        for (int k = 0; k < 12; k++) f[k] = 0.0;
     const int4 sl = __ldg(p.slot + e);
     const int ks[4] = {sl.x, sl.y, sl.z, sl.w};
 #pragma unroll
@@ -1127,6 +1140,9 @@ __device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, 
                                P[i * 3 + 2] * G[(a - 1) * 3 + 2];
 #pragma unroll
         for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
+        if (!FORCE_ONLY && elem_dead(p, e, p.ctrl[parity].t))
+#pragma unroll
+            for (int k = 0; k < 12; k++) f[k] = 0.f;
         // one 16-byte store per corner (a padded slot) rather than three scalar ones
         const int4 sl = __ldg(p.slot + e);
         float4 *fe = reinterpret_cast<float4 *>(p.fe32);
@@ -1443,6 +1459,9 @@ __device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int
                                    G[(a - 1) * 3 + 2], 0.0f);
 #pragma unroll
     for (int i = 0; i < 3; i++) f[i] = dw_neg(dw_add_sloppy(dw_add_sloppy(f[3 + i], f[6 + i]), f[9 + i]));
+    if (!FORCE_ONLY && elem_dead(p, e, p.ctrl[parity].t))
+#pragma unroll
+        for (int k = 0; k < 12; k++) f[k] = make_float2(0.f, 0.f);
     const int4 sl = __ldg(p.slot + e);
     const int ks[4] = {sl.x, sl.y, sl.z, sl.w};
     float2 *fe = reinterpret_cast<float2 *>(p.fe);
@@ -1936,10 +1955,19 @@ __global__ void __launch_bounds__(kElemBlock) initial_cfl_kernel(Problem p, cons
 // Cauchy (NH: the law's sigma, hyperElasticNeoHookean.cpp:113-124; other laws
 // P F^T / J, maths.cpp:1250-1254), Green-Lagrange E (maths.cpp:1227-1243) and
 // von Mises (maths.cpp:1261-1271).
-__global__ void element_fields_kernel(Problem p, double *cauchy, double *gl, double *vms)
+__global__ void element_fields_kernel(Problem p, double t, double *cauchy, double *gl, double *vms)
 {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= p.ne) return;
+    if (elem_dead(p, e, t)) {   // never updated: the Gauss point's initial, zero state
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            if (cauchy) cauchy[e * 9 + k] = 0.0;
+            if (gl) gl[e * 9 + k] = 0.0;
+        }
+        if (vms) vms[e] = 0.0;
+        return;
+    }
     const long long ne = p.ne, nn = p.nn;
     int4 cn = p.conn[e];
     int nd[4] = {cn.x, cn.y, cn.z, cn.w};
@@ -2033,8 +2061,9 @@ __global__ void element_fields_kernel(Problem p, double *cauchy, double *gl, dou
 // centroid, where every shape function is 0.25 (dataExtraction.cpp:626-688),
 // and volume's wJ det F (:690-748).  The internal variables read zero: no law
 // here has more than one (getValueAtGP wants more than k for INVAR k).
-__device__ double element_quantity_ref(const Problem &p, int q, long long e)
+__device__ double element_quantity_ref(const Problem &p, int q, long long e, double t)
 {
+    if (elem_dead(p, e, t)) return 0.0;   // dataExtraction.cpp:510
     if (q >= MSX_ELEM_INVAR1 && q <= MSX_ELEM_INVAR6) return 0.0;
     const long long ne = p.ne, nn = p.nn;
     const int4 cn = p.conn[e];
@@ -2108,10 +2137,10 @@ __device__ double element_quantity_ref(const Problem &p, int q, long long e)
     return q == MSX_ELEM_KVM ? svm * detF : svm;
 }
 
-__global__ void element_values_kernel(Problem p, int q, const int *elems, long long n, double *out)
+__global__ void element_values_kernel(Problem p, int q, const int *elems, long long n, double t, double *out)
 {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < n) out[j] = element_quantity_ref(p, q, elems ? elems[j] : j);
+    if (j < n) out[j] = element_quantity_ref(p, q, elems ? elems[j] : j, t);
 }
 
 // The element-extraction reduction in two fixed-shape passes, so the result
@@ -2163,7 +2192,10 @@ __global__ void __launch_bounds__(kReduceThreads) element_reduce_kernel(Problem 
             continue;
         }
         const long long e = elems ? elems[j] : j;
-        const double v = element_quantity_ref(p, q, e), dV = p.wJ[e];
+        // the energies and the volume skip dead Gauss points altogether (:577-578, 644-645, 706-707)
+        if ((q == MSX_ELEM_DEFO_ENERGY || q == MSX_ELEM_KIN_ENERGY || q == MSX_ELEM_VOLUME) && elem_dead(p, e, t))
+            continue;
+        const double v = element_quantity_ref(p, q, e, t), dV = p.wJ[e];
         fold_pair(op, s, w, q == MSX_ELEM_VOLUME || op == MSX_OP_MAX || op == MSX_OP_MIN ? v : v * dV, dV);
     }
     block_fold(op, s, w);

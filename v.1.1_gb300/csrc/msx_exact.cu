@@ -59,14 +59,15 @@ void launch_setup_gravity(const Problem &p, double g, double *grav_e, double *gr
     setup_gravity_node_kernel<<<grid_for(p.nn, 256), 256, 0, s>>>(p, grav_e, grav_n);
 }
 
-void launch_element_fields(const Problem &p, double *cauchy, double *gl, double *vms, cudaStream_t s)
+void launch_element_fields(const Problem &p, double t, double *cauchy, double *gl, double *vms, cudaStream_t s)
 {
-    element_fields_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, cauchy, gl, vms);
+    element_fields_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, t, cauchy, gl, vms);
 }
 
-void launch_element_values(const Problem &p, int quantity, const int *elems, long long n, double *out, cudaStream_t s)
+void launch_element_values(const Problem &p, int quantity, const int *elems, long long n, double t, double *out,
+                           cudaStream_t s)
 {
-    if (n > 0) element_values_kernel<<<grid_for(n, 128), 128, 0, s>>>(p, quantity, elems, n, out);
+    if (n > 0) element_values_kernel<<<grid_for(n, 128), 128, 0, s>>>(p, quantity, elems, n, t, out);
 }
 
 void launch_element_reduce(const Problem &p, int quantity, int op, const int *elems, long long n, double t,

@@ -86,6 +86,7 @@ struct Problem {
     const float *Eref32;      // 9*ne reference edge vectors X_a - X_0 (FP32 CFL screen of the FP64 mode)
     const float *G32lo, *wJ32lo;  // low words: G32 + G32lo and wJ32 + wJ32lo as double-words (double-word mode)
     const unsigned char *mat; // per-element material id, or nullptr
+    const double *act_t;      // per-element activation time under *ACTIVATION, or nullptr
     int nmat;
     MatParams mats[kMaxMats];
     // nodes (SoA, dof = node + c*nn)
@@ -185,12 +186,13 @@ void launch_face_loads(const Problem &p, int parity, bool mixed, cudaStream_t s)
 void launch_node_values(const Problem &p, int mode, int field, int comp, const int *nodes, long long n, double t,
                         double *out, cudaStream_t s);
 // Cauchy, Green-Lagrange (9 per element, row-major) and von Mises of the current u
-void launch_element_fields(const Problem &p, double *cauchy, double *gl, double *vms, cudaStream_t s);
+void launch_element_fields(const Problem &p, double t, double *cauchy, double *gl, double *vms, cudaStream_t s);
 // Element data extraction: per-element values of a msx_element_quantity, and
 // the reduction one extraction row writes (quantity, op as in msx.h), from the
 // current u, v and, for the external energy, the loads at time t.  part holds
 // element_reduce_scratch() - 1 doubles of partials, out one.
-void launch_element_values(const Problem &p, int quantity, const int *elems, long long n, double *out, cudaStream_t s);
+void launch_element_values(const Problem &p, int quantity, const int *elems, long long n, double t, double *out,
+                           cudaStream_t s);
 void launch_element_reduce(const Problem &p, int quantity, int op, const int *elems, long long n, double t,
                            double *part, double *out, cudaStream_t s);
 long long element_reduce_scratch();

@@ -129,6 +129,8 @@ struct msx_handle {
     launch_fn node = nullptr, elem = nullptr;   // reference-order kernels (exact mode)
     bool tiled = false;                          // FP64 / mixed: the shared tiled step kernels
     DBuf<Problem> d_desc;
+    DBuf<double> act;                    // activation times (element birth), when set
+    bool act_enabled = false;
     DBuf<Tile> d_etiles, d_ntiles;
     int tile_elems = 0;                 // element-tile size of d_etiles
     DBuf<int> d_counts;
@@ -225,6 +227,7 @@ static msx_status build_bcs(long long nn, const msx_bc *bcs, long long nbc, doub
 static void bind_problem(msx_handle *h)
 {
     Problem &P = h->P;
+    P.act_t = h->act_enabled ? h->act.p : nullptr;
     P.conn = h->conn.p;
     P.G = h->G.p;
     P.wJ = h->wJ.p;
@@ -613,6 +616,7 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     for (auto *b : {&h->node_ptr, &h->node_inc, &h->node_bc, &h->flags}) b->release();
     h->bc_rec.release();
     h->bcs.release();
+    h->act.release();
     h->grav_e.release();
     h->grav_n.release();
     h->fcon.release();
@@ -880,6 +884,27 @@ extern "C" msx_status msx_set_load_blocks(msx_handle *h, const msx_load_block *b
     return MSX_OK;
 }
 
+extern "C" msx_status msx_set_activation(msx_handle *h, const double *activation_time, int32_t enabled)
+{
+    if (!h) return fail(MSX_ERR_ARG, "NULL handle");
+    if (activation_time) {
+        if (!h->act.p) MSX_CUDA(h->act.alloc(h->P.ne));
+        MSX_CUDA(cudaMemcpyAsync(h->act.p, activation_time, sizeof(double) * h->P.ne, cudaMemcpyHostToDevice,
+                                 h->stream));
+    }
+    if (enabled && !h->act.p) return fail(MSX_ERR_STATE, "activation enabled before any activation times were set");
+    h->act_enabled = enabled != 0;
+    bind_problem(h);
+    msx_status st = upload_tiled(h);
+    if (st != MSX_OK) return st;
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->graph) {   // the exact mode's captured launches hold the Problem by value
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    return MSX_OK;
+}
+
 extern "C" msx_status msx_set_loads(msx_handle *h, const msx_nodal_force *forces, int64_t num_forces, double gravity,
                                     int32_t gravity_first)
 {
@@ -1011,7 +1036,7 @@ extern "C" msx_status msx_element_values(msx_handle *h, int32_t quantity, const 
         return fail(MSX_ERR_OOM, "element value scratch");
     }
     bind_problem(h);
-    launch_element_values(h->P, quantity, elems ? de.p : nullptr, n, dv.p, h->stream);
+    launch_element_values(h->P, quantity, elems ? de.p : nullptr, n, h->last_t, dv.p, h->stream);
     cudaMemcpyAsync(out, dv.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream);
     const cudaError_t err = cudaStreamSynchronize(h->stream);
     de.release();
@@ -1228,7 +1253,7 @@ extern "C" msx_status msx_element_fields(msx_handle *h, double *cauchy, double *
         return fail(MSX_ERR_OOM, "element field buffers");
     }
     bind_problem(h);
-    launch_element_fields(h->P, dc.p, dg.p, dv.p, h->stream);
+    launch_element_fields(h->P, h->last_t, dc.p, dg.p, dv.p, h->stream);
     if (cauchy) cudaMemcpyAsync(cauchy, dc.p, sizeof(double) * 9 * ne, cudaMemcpyDeviceToHost, h->stream);
     if (green_lagrange) cudaMemcpyAsync(green_lagrange, dg.p, sizeof(double) * 9 * ne, cudaMemcpyDeviceToHost, h->stream);
     if (von_mises) cudaMemcpyAsync(von_mises, dv.p, sizeof(double) * ne, cudaMemcpyDeviceToHost, h->stream);

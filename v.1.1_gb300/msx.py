@@ -103,7 +103,8 @@ SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_
            "msx_stream", "msx_set_device", "msx_pool_create", "msx_pool_submit", "msx_pool_step",
            "msx_pool_poll", "msx_pool_fetch", "msx_pool_wait", "msx_pool_destroy", "msx_pool_stats_get",
            "msx_internal_force_noalloc", "msx_initial_dt", "msx_element_fields", "msx_set_loads",
-           "msx_set_load_blocks", "msx_node_values", "msx_element_values", "msx_element_reduce"]
+           "msx_set_load_blocks", "msx_node_values", "msx_element_values", "msx_element_reduce",
+           "msx_set_activation"]
 
 _lib = None
 
@@ -136,6 +137,7 @@ def load(path: str = LIB_PATH):
         "msx_set_load_blocks": [vp, vp, i64],
         "msx_node_values": [vp, i32, i32, vp, i64, vp],
         "msx_element_values": [vp, i32, vp, i64, vp],
+        "msx_set_activation": [vp, vp, i32],
         "msx_element_reduce": [vp, i32, i32, vp, i64, vp],
     }
     for name, args in sig.items():
@@ -303,6 +305,14 @@ class Solver:
         out = np.zeros(len(n))
         _check(load().msx_node_values(self.h, int(field), int(comp), _p(n), len(n), _p(out)))
         return out
+
+    def set_activation(self, activation_time=None, enabled=True):
+        """Element birth (*ACTIVATION): per-element activation times (None keeps the
+        current ones) and whether the current and later blocks use them."""
+        t = None if activation_time is None else np.ascontiguousarray(activation_time, dtype=np.float64)
+        if t is not None and t.shape != (self.ne,):
+            raise ValueError("one activation time per element")
+        _check(load().msx_set_activation(self.h, _p(t), 1 if enabled else 0))
 
     def element_values(self, quantity, elems=None):
         """Per-element value of an element-extraction quantity (a name of
