@@ -73,7 +73,8 @@ def test_double_word_mode_matches_reference(name):
     assert rel(v, vr) <= 1e-10
 
 
-@pytest.mark.parametrize("name", [n for n in names() if n.startswith("cube10")] + ["cube4_le_ramp"])
+@pytest.mark.parametrize("name", [n for n in names() if n.startswith("cube10")] +
+                         ["cube4_le_ramp", "cube3_stvk_activation", "cube3_le_activation_chain"])
 def test_mixed_mode_error_bound(name):
     (u, v, a), (ur, vr, ar), steps, ref_steps = run_case(name, msx.MIXED)
     assert abs(steps - ref_steps) <= 1
