@@ -945,8 +945,8 @@ __device__ __forceinline__ float cfl_screen(const Problem &p, long long e, const
 // the 4th corner force as minus the sum of the other three.  Same algebra as
 // the reference, about half its FP64 operations.  Returns the FP32 CFL screen
 // value (see cfl_screen).
-template <bool FORCE_ONLY>
-__device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, int parity)
+template <bool FORCE_ONLY, bool ACT = false>
+__device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, int parity, double t = 0.0)
 {
     const long long ne = p.ne, nn = p.nn;
     int4 cn = p.conn[e];
@@ -979,7 +979,7 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
             f[a * 3 + i] = P[i * 3] * G[(a - 1) * 3] + P[i * 3 + 1] * G[(a - 1) * 3 + 1] + P[i * 3 + 2] * G[(a - 1) * 3 + 2];
 #pragma unroll
     for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
-    if (!FORCE_ONLY && elem_dead(p, e, p.ctrl[parity].t))
+    if (ACT && elem_dead(p, e, t))
 #pragma unroll
         for (int k = 0; k < 12; k++) f[k] = 0.0;
     const int4 sl = __ldg(p.slot + e);
@@ -1083,8 +1083,8 @@ __device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H,
     }
 }
 
-template <bool FORCE_ONLY>
-__device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, int parity, int4 cn)
+template <bool FORCE_ONLY, bool ACT = false>
+__device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, int parity, int4 cn, double t = 0.0)
 {
     const long long ne = p.ne, nn = p.nn;
     float vmin = INFINITY;
@@ -1140,7 +1140,7 @@ __device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, 
                                P[i * 3 + 2] * G[(a - 1) * 3 + 2];
 #pragma unroll
         for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
-        if (!FORCE_ONLY && elem_dead(p, e, p.ctrl[parity].t))
+        if (ACT && elem_dead(p, e, t))
 #pragma unroll
             for (int k = 0; k < 12; k++) f[k] = 0.f;
         // one 16-byte store per corner (a padded slot) rather than three scalar ones
@@ -1427,8 +1427,8 @@ static __device__ __noinline__ double cfl_dw(const Problem &p, long long e)
     return ((dist < Lr) ? dist : Lr) / mat_of(p, e).c;
 }
 
-template <bool FORCE_ONLY>
-__device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int parity, int4 cn)
+template <bool FORCE_ONLY, bool ACT = false>
+__device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int parity, int4 cn, double t = 0.0)
 {
     const long long ne = p.ne, nn = p.nn;
     int nd[4] = {cn.x, cn.y, cn.z, cn.w};
@@ -1459,7 +1459,7 @@ __device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int
                                    G[(a - 1) * 3 + 2], 0.0f);
 #pragma unroll
     for (int i = 0; i < 3; i++) f[i] = dw_neg(dw_add_sloppy(dw_add_sloppy(f[3 + i], f[6 + i]), f[9 + i]));
-    if (!FORCE_ONLY && elem_dead(p, e, p.ctrl[parity].t))
+    if (ACT && elem_dead(p, e, t))
 #pragma unroll
         for (int k = 0; k < 12; k++) f[k] = make_float2(0.f, 0.f);
     const int4 sl = __ldg(p.slot + e);
@@ -1659,12 +1659,41 @@ __global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *
     q.finish();
 }
 
+// The elements of one tile for the tiled element kernel: each thread's
+// elements in turn, FP32 CFL screen values into sdt (FP64 and double-word);
+// returns the thread's FP32 minimum.  The mixed and double-word bodies take the
+// element's connectivity loaded one element ahead, so their node gathers wait
+// for one memory latency instead of two (connectivity, then the nodes).  ACT:
+// element birth is on, and the step's time decides which elements are dead.
+template <int MODE, bool ACT>
+__device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl, int parity, float *sdt)
+{
+    float v32 = INFINITY;
+    const double t = ACT ? p.ctrl[parity].t : 0.0;
+    long long e = tl.begin + threadIdx.x;
+    int4 cn_next = make_int4(0, 0, 0, 0);
+    if (MODE == MODE_MIXED || MODE == MODE_DW) {
+        if (e < tl.end) cn_next = p.conn[e];
+    }
+    for (; e < tl.end; e += blockDim.x) {
+        const int4 cn = cn_next;
+        if ((MODE == MODE_MIXED || MODE == MODE_DW) && e + blockDim.x < tl.end) cn_next = p.conn[e + blockDim.x];
+        float d = MODE == MODE_MIXED ? elem_body_mixed<false, ACT>(p, e, parity, cn, t)
+                                     : (MODE == MODE_DW ? elem_body_dw<false, ACT>(p, e, parity, cn, t)
+                                                        : elem_body_fp64<false, ACT>(p, e, parity, t));
+        if (MODE != MODE_MIXED) sdt[e - tl.begin] = d;
+        if (d >= 0.0f) v32 = fminf(v32, d);
+    }
+    return v32;
+}
+
 // Element kernel over tiles.  FP64 and double-word: every element's FP32 CFL
 // screen value is kept in shared memory; after the tile's FP32 minimum is
 // known, elements within 2^-8 of it (and slivers) recompute the exact FP64
 // value, whose minimum goes to the solve's CFL slot.  Mixed: the FP32 minimum
-// itself.
-template <int MODE>
+// itself.  ACT: the instantiation with element birth (single solves whose block
+// has it on); the other one carries no trace of it.
+template <int MODE, bool ACT = false>
 __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE == MODE_DW ? 3 : 2)) pool_elem_kernel(const Problem *__restrict__ descs,
                                                                  const Tile *__restrict__ tiles,
                                                                  int *__restrict__ sched, int parity)
@@ -1683,24 +1712,7 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
         const Problem &p = descs[tl.solve];
         if (p.ctrl[parity].ran) {
             if (MODE != MODE_MIXED && threadIdx.x == 0) s_ncand = 0;
-            float v32 = INFINITY;
-            // the mixed and double-word bodies take the element's connectivity
-            // loaded one element ahead, so their node gathers wait for one memory
-            // latency instead of two (connectivity, then the nodes)
-            long long e = tl.begin + threadIdx.x;
-            int4 cn_next = make_int4(0, 0, 0, 0);
-            if (MODE == MODE_MIXED || MODE == MODE_DW) {
-                if (e < tl.end) cn_next = p.conn[e];
-            }
-            for (; e < tl.end; e += blockDim.x) {
-                const int4 cn = cn_next;
-                if ((MODE == MODE_MIXED || MODE == MODE_DW) && e + blockDim.x < tl.end) cn_next = p.conn[e + blockDim.x];
-                float d = MODE == MODE_MIXED ? elem_body_mixed<false>(p, e, parity, cn)
-                                             : (MODE == MODE_DW ? elem_body_dw<false>(p, e, parity, cn)
-                                                                : elem_body_fp64<false>(p, e, parity));
-                if (MODE != MODE_MIXED) sdt[e - tl.begin] = d;
-                if (d >= 0.0f) v32 = fminf(v32, d);
-            }
+            const float v32 = tile_elements<MODE, ACT>(p, tl, parity, sdt);
             float bmin = block_min_bcast(v32);   // also orders the sdt writes before the reads below
             if (MODE == MODE_MIXED) {
                 if (threadIdx.x == 0 && bmin < INFINITY)

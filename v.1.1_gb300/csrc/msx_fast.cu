@@ -35,14 +35,17 @@ void launch_tiled_node(const Problem *descs, const Tile *ntiles, int *counts, in
 }
 
 void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, int mode, int parity, int grid,
-                       int threads, cudaStream_t s)
+                       int threads, cudaStream_t s, bool act)
 {
     if (mode == MODE_MIXED)
-        pool_elem_kernel<MODE_MIXED><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
+        act ? pool_elem_kernel<MODE_MIXED, true><<<grid, threads, 0, s>>>(descs, etiles, counts, parity)
+            : pool_elem_kernel<MODE_MIXED><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
     else if (mode == MODE_DW)
-        pool_elem_kernel<MODE_DW><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
+        act ? pool_elem_kernel<MODE_DW, true><<<grid, threads, 0, s>>>(descs, etiles, counts, parity)
+            : pool_elem_kernel<MODE_DW><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
     else
-        pool_elem_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
+        act ? pool_elem_kernel<MODE_FP64, true><<<grid, threads, 0, s>>>(descs, etiles, counts, parity)
+            : pool_elem_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
 }
 
 __global__ void state_split_kernel(Problem p)
