@@ -319,3 +319,29 @@ def test_element_reduce_matches_oracle(precision):
     with pytest.raises(msx.MsxError):
         S.element_values("EXTERNAL_ENERGY")
     S.close()
+
+
+def test_activation_api_errors_and_dead_elements():
+    """msx_set_activation refuses to switch on without times; with every element
+    dead the internal force is zero, so without loads the free DOFs stay at rest."""
+    mesh, mats, solvers, _, _ = load("cube3_stvk_activation")
+    s0 = solvers[0]
+    m = [(x.law, x.young, x.nu, x.rho) for x in mats]
+    S = msx.Solver(mesh.X, mesh.conn, m, s0.bcs, s0.t0, s0.tf, s0.scale_factor)
+    with pytest.raises(msx.MsxError):
+        S.set_activation(None, True)
+    with pytest.raises(ValueError):
+        S.set_activation(np.zeros(3), True)
+    S.set_activation(np.full(mesh.ne, 1e9), True)   # nobody is born in this block
+    S.run(5)
+    nodes = np.arange(mesh.nn, dtype=np.int32)
+    for c in range(3):
+        assert not S.node_values(msx.FIELD_INTERNAL_FORCE, c, nodes).any()
+    u = S.state()[0]
+    fixed = np.zeros(3 * mesh.nn, bool)
+    fixed[[b[0] for b in s0.bcs]] = True
+    assert not u[~fixed].any() and u[fixed].any()
+    S.set_activation(None, False)                   # everyone alive again
+    S.run(1)
+    assert any(S.node_values(msx.FIELD_INTERNAL_FORCE, c, nodes).any() for c in range(3))
+    S.close()
