@@ -692,7 +692,33 @@ __global__ void __launch_bounds__(kNodeBlock) node_kernel(Problem p, int parity)
 // ---------------------------------------------------------------------------
 
 // Reference operation order (used with contraction off).
-template <bool FORCE_ONLY>
+__device__ __forceinline__ float f32_trunc(double x);
+__device__ __forceinline__ float cfl_screen(const Problem &p, long long e, const float *du, const MatParams &m);
+
+// Exact CFL value of one element, min(L_ref, L(X+u)) / c, in the reference's
+// order (solvers.cpp:304-317: deformed inscribed sphere).
+__device__ __forceinline__ double cfl_exact_ref(const Problem &p, long long e)
+{
+    const long long nn = p.nn;
+    const int4 cn = p.conn[e];
+    const int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    double x[12];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            x[a * 3 + k] = p.X[k * nn + nd[a]];
+            x[a * 3 + k] += p.u[nd[a] + k * nn];
+        }
+    double dist = char_length_ref(x);
+    double Lr = p.Lref[e];
+    double mlen = (dist < Lr) ? dist : Lr;
+    return mlen / mat_of(p, e).c;
+}
+
+// SCREEN: return the FP32 screen value of the CFL (cfl_screen) instead of the
+// exact one; the caller rechecks the elements near its block's minimum.
+template <bool FORCE_ONLY, bool SCREEN = false>
 __device__ __forceinline__ double elem_body_exact(const Problem &p, long long e, int parity)
 {
     const long long ne = p.ne, nn = p.nn;
@@ -737,7 +763,15 @@ __device__ __forceinline__ double elem_body_exact(const Problem &p, long long e,
                 for (int J = 0; J < 3; J++) f += wJ * P[i * 3 + J] * dphi[a * 3 + J];
                 fe[a * 3 + i] = dead ? 0.0 : 0 + f;
             }
-        if (!FORCE_ONLY) {
+        if (!FORCE_ONLY && SCREEN) {
+            float du32[9];
+#pragma unroll
+            for (int a = 1; a < 4; a++)
+#pragma unroll
+                for (int i = 0; i < 3; i++) du32[(a - 1) * 3 + i] = f32_trunc(ue[a * 3 + i] - ue[i]);
+            vmin = (double)cfl_screen(p, e, du32, m);
+            if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
+        } else if (!FORCE_ONLY) {
             // solvers.cpp:304-317: deformed inscribed sphere
             double x[12];
 #pragma unroll
@@ -1581,6 +1615,23 @@ __device__ __forceinline__ void node_quad_dw(const Problem &p, long long i, bool
 }
 
 // Block-wide min of a float, returned to every thread of the block.
+__device__ __forceinline__ float block_min_bcast(float v);
+
+// Reference-order element kernel with the FP32 CFL screen: forces in the
+// reference's order for every element, the exact reference-order CFL value only
+// for the elements of the block within 2^-8 of its FP32 minimum (and slivers),
+// a set that always holds the block's exact minimum, so dt is the reference's.
+static __global__ void __launch_bounds__(kElemBlock) elem_kernel_exact_screened(Problem p, int parity)
+{
+    if (!p.ctrl[parity].ran) return;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const float d = e < p.ne ? (float)elem_body_exact<false, true>(p, e, parity) : INFINITY;
+    const float bmin = block_min_bcast(d >= 0.0f ? d : INFINITY);
+    double v = INFINITY;
+    if (e < p.ne && (d < 0.0f || d <= bmin * (1.0f + 1.0f / 256.0f))) v = cfl_exact_ref(p, e);
+    block_min_to(v, p.dtmin + (parity ^ 1));
+}
+
 __device__ __forceinline__ float block_min_bcast(float v)
 {
     __shared__ float wm[32];

@@ -15,7 +15,7 @@ void launch_node_exact(const Problem &p, int parity, cudaStream_t s)
 
 void launch_elem_exact(const Problem &p, int parity, cudaStream_t s)
 {
-    elem_kernel_exact<false><<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, parity);
+    elem_kernel_exact_screened<<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, parity);
 }
 
 void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s)
