@@ -2,10 +2,12 @@
 // the C ABI, as `MuPhiSim -input <deck>` runs it through the reference's
 // solver chain (src/main.cpp:37-217).
 //
-//   msx_deck -input deck.inp [-inputDir d] [-outputDir o] [-precision fp64|exact|mixed]
+//   msx_deck -input deck.inp [-inputDir d] [-outputDir o] [-precision fp64|exact|mixed|dword]
 //            [-dump final.bin] [-csv final.csv] [-parse-only]
 //
-// With -outputDir, VTK files MuPhiSimOutputs_0_.<k>.vtk and the series index
+// -inputDir defaults to "input" and the extraction and *Forces files go to
+// -outputDir, by default "output", as in the reference (IO/commandLine.cpp).
+// With -outputDir given, VTK files MuPhiSimOutputs_0_.<k>.vtk and the series index
 // allOutputs_0.vtk.series are written at the reference's *Outputs cadence
 // (solverExplicit.cpp:171-174, 310-321): at t0 when t0 < 1e-12, then every
 // long(long((tf - t0)/dt0)/outputs) steps and when the block ends at tf; the
@@ -15,10 +17,14 @@
 // Keyword subset (src/IO/inputFile.cpp): *Node (:20-108), *Element, type=C3D4
 // (:118-323), *FEM Nodes / *FEM Elements, *MATERIAL with *Density,
 // *HyperElastic {Neo-Hookean | 3D-Compressible-Neo-Hookean |
-// St-Venant-Kirchhoff} and *List of Elements (:838-1029, 2010-2053),
-// *SOLVER, EXPLICIT ... *END SOLVER with *Scale Factor, *Outputs, *Time and
-// *BOUNDARY, TYPE=DISPLACEMENT RAMP|INST (:2253-2831, 2960-3218).  Other
-// keywords belong to paths this library does not implement and are refused.
+// St-Venant-Kirchhoff}, *Linear-Elastic, *INITINTVARS and *List of Elements
+// (:838-1029, 2010-2111), *SOLVER, EXPLICIT ... *END SOLVER with *ACTIVATION,
+// *Scale Factor, *Outputs, *Time, *Forces and *BOUNDARY, TYPE=DISPLACEMENT
+// RAMP|INST (:2253-2831, 2960-3218, 4830-4886), the Neumann blocks *BOUNDARY,
+// TYPE=FORCE | TRACTION INST|RAMP | PRESSURE INST|RAMP and *GRAVITY
+// (:4705-4760, 2841-2945), and *EXTRACTION, NODE | ELEMENT (:4950-5111).
+// Other keywords belong to paths this library does not implement and are
+// refused.
 // As in the reference, a RAMP BC stores U/(tf - t0) with the *Time read so
 // far, and once an INST block has been read every later displacement block
 // is instantaneous (the flag is not reset between solvers).
@@ -556,7 +562,7 @@ struct ForcePrinter {
 
 int main(int argc, char **argv)
 {
-    std::string input, dir = ".", dump, csv, outdir;
+    std::string input, dir = "input", dump, csv, outdir;
     int precision = MSX_PREC_FP64;
     bool parse_only = false;
     for (int k = 1; k < argc; k++) {
@@ -576,8 +582,8 @@ int main(int argc, char **argv)
         }
     }
     if (input.empty()) {
-        fprintf(stderr, "usage: msx_deck -input deck.inp [-inputDir d] [-precision fp64|exact|mixed] "
-                        "[-dump f.bin] [-csv f.csv] [-parse-only]\n");
+        fprintf(stderr, "usage: msx_deck -input deck.inp [-inputDir d] [-outputDir o] "
+                        "[-precision fp64|exact|mixed|dword] [-dump f.bin] [-csv f.csv] [-parse-only]\n");
         return 2;
     }
     Deck d = parse(dir + "/" + input);
