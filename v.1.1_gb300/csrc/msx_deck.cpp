@@ -406,7 +406,7 @@ Deck parse(const std::string &path)
 // One output file in the reference's VTK layout (src/IO/output.cpp:296-700):
 // undeformed points, C3D4 cells, nodal displacement / velocity /
 // acceleration, element Cauchy, Green-Lagrange and von Mises.
-bool write_vtk(const std::string &dir, int index, double t, const std::vector<double> &X, const std::vector<int32_t> &conn,
+bool write_vtk(const std::string &dir, int index, const std::vector<double> &X, const std::vector<int32_t> &conn,
                msx_handle *h)
 {
     const long long nn = (long long)X.size() / 3, ne = (long long)conn.size() / 4;
@@ -697,7 +697,7 @@ int main(int argc, char **argv)
             long long sampler = s.outputs > 0 ? numStepsT / s.outputs : numStepsT;
             const long long every = sampler > 0 ? sampler : 1;
             auto emit = [&](double t) {
-                if (!write_vtk(outdir, (int)outputs.size(), t, X, d.conn, h)) return false;
+                if (!write_vtk(outdir, (int)outputs.size(), X, d.conn, h)) return false;
                 outputs.push_back({"MuPhiSimOutputs_0_." + std::to_string(outputs.size()) + ".vtk", t});
                 write_series(outdir, outputs);
                 return true;
