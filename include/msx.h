@@ -351,8 +351,20 @@ msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const msx_material
 /* Advance every resident solve by up to `steps` steps (graph replays of
  * steps_per_launch steps).  Keeps one replay in flight: waits for the previous
  * one, collects its finished solves, launches the next and returns without
- * waiting for it, so the caller's next admissions overlap it. */
+ * waiting for it, so the caller's next admissions overlap it.
+ * MSX_ERR_STATE while the pool is serving. */
 msx_status msx_pool_step(msx_pool *p, int64_t steps);
+/* Serving mode on (enabled != 0) or off.  On: a thread of the library launches
+ * replays back to back while any solve is resident and sleeps while none is;
+ * msx_pool_submit admits new solves between replays, msx_pool_poll returns the
+ * finished ones, msx_pool_wait blocks until a ticket is done.  Admissions build
+ * their tables and upload their data without holding the pool's lock, so they
+ * overlap the running replays.  Off: waits for the replay in flight and stops
+ * the thread; msx_pool_step drives the pool again.  A CUDA failure in the
+ * serving thread stops the stepping and is returned by the next poll or wait
+ * (and by turning serving off).  Results are the same as with msx_pool_step:
+ * only the host-side driving differs. */
+msx_status msx_pool_serve(msx_pool *p, int32_t enabled);
 /* Finished solves collected so far (never waits; takes in the replay in flight
  * if it has completed): fills up to max results, returns the count in *n.
  * u, v, a of a solve are copied out by msx_pool_fetch. */

@@ -103,3 +103,71 @@ def test_wait_for_one_ticket():
     with pytest.raises(msx.MsxError):
         P.wait(tickets[1])   # already fetched
     P.close()
+
+
+@pytest.mark.parametrize("precision", [msx.MIXED, msx.DOUBLE_WORD])
+def test_serving_mode_concurrent_admission(precision):
+    """Serving mode: the library's thread steps the pool while two host threads
+    admit solves, one of them staggered so its admissions land while replays
+    run.  Every result equals the solve alone; msx_pool_step is refused while
+    serving; msx_pool_wait blocks on the serving thread; after serving is
+    turned off the pool is stepped by hand again."""
+    import threading
+    import time
+    rng = np.random.default_rng(23)
+    cases = [case(int(n), float(E), float(nu), float(v), 40 + s)
+             for s, (n, E, nu, v) in enumerate(zip(rng.integers(3, 10, 10), 10 ** rng.uniform(5, 7, 10),
+                                                   rng.uniform(0.25, 0.45, 10), rng.uniform(0.01, 0.2, 10)))]
+    steps = [int(x) for x in rng.integers(30, 160, len(cases))]
+    P = msx.Pool(max_slots=6, precision=precision, steps_per_launch=4)
+    P.serve(True)
+    P.serve(True)   # already serving: no second thread
+    with pytest.raises(msx.MsxError):
+        P.step(4)
+    tickets = {}
+    lock = threading.Lock()
+
+    def client(ks, pause):
+        for k in ks:
+            X, c, m, b = cases[k]
+            while True:
+                t = P.submit(X, c, m, b, steps[k])
+                if t is not None:
+                    break
+                time.sleep(0.002)   # slots full: the serving thread frees them
+            with lock:
+                tickets[t] = k
+            time.sleep(pause)
+
+    th = [threading.Thread(target=client, args=(list(range(0, 10, 2)), 0.01)),
+          threading.Thread(target=client, args=(list(range(1, 10, 2)), 0.0))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    done = {}
+    first = next(iter(tickets))
+    r = P.wait(first)
+    assert r["ticket"] == first and r["status"] == 0
+    done[first] = r
+    deadline = time.time() + 120
+    while len(done) < len(cases) and time.time() < deadline:
+        for q in P.poll():
+            done[q["ticket"]] = q
+        time.sleep(0.001)
+    assert len(done) == len(cases)
+    for t, q in done.items():
+        k = tickets[t]
+        assert q["status"] == 0 and q["steps"] == steps[k]
+        ua, va, aa = alone(*cases[k], steps[k], precision)
+        u, v, a = P.fetch(t)
+        assert np.array_equal(u, ua) and np.array_equal(v, va) and np.array_equal(a, aa)
+    P.serve(False)
+    X, c, m, b = cases[0]
+    t = P.submit(X, c, m, b, 17)
+    for _ in range(10):
+        P.step()
+    got = {q["ticket"]: q for q in P.poll()}
+    assert got[t]["steps"] == 17
+    assert np.array_equal(P.fetch(t)[0], alone(X, c, m, b, 17, precision)[0])
+    P.close()

@@ -8,10 +8,14 @@
 // solve), captured as a CUDA graph of `steps_per_launch` steps.  Admission is
 // by HBM footprint; finished solves are copied out, freed and replaced
 // between graph replays (continuous batching).  Tile size, CTA size and grid
-// size are picked by timing candidates on the resident work.
+// size are picked by timing candidates on the resident work.  In serving mode
+// (msx_pool_serve) a library thread launches the replays back to back while
+// any solve is resident; admissions build their host tables and upload their
+// data without holding the pool's lock, so they overlap the replays.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
 #include <deque>
@@ -19,6 +23,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/msx.h"
@@ -68,6 +73,7 @@ double now_ms()
 
 struct Slot {
     bool active = false;
+    bool reserved = false;   // taken by an admission whose uploads are still being enqueued
     bool launched = false;   // a replay ordered after the solve's admission has run on it
     long long ticket = -1;
     long long nn = 0, ne = 0;
@@ -119,6 +125,13 @@ struct msx_pool {
     std::deque<long long> done_order;
     long long elem_steps_finished = 0;   // element-steps of solves already collected
     long long elem_steps_active = 0;     // element-steps of resident solves at the last read
+    // serving mode
+    std::thread server;
+    std::condition_variable cv_work;   // to the serving thread: a solve was admitted, or stop
+    std::condition_variable cv_done;   // to msx_pool_wait: a replay was collected, or serving failed
+    bool serving = false, serve_stop = false;
+    msx_status serve_status = MSX_OK;
+    std::string serve_error;
 };
 
 // ------------------------------------------------------------------ helpers
@@ -262,7 +275,10 @@ static msx_status collect(msx_pool *p)
         p->done_order.push_back(t);
         changed = true;
     }
-    if (changed) rebuild_tiles(p);
+    if (changed) {
+        rebuild_tiles(p);
+        p->cv_done.notify_all();   // msx_pool_wait callers in serving mode
+    }
     return MSX_OK;
 }
 
@@ -384,6 +400,39 @@ static msx_status autotune(msx_pool *p)
     return MSX_OK;
 }
 
+// Serving thread: while any solve is resident, launch a replay, wait for it
+// without the lock (admissions, polls and fetches go on meanwhile), collect it.
+// Sleeps while the pool is empty.  A failure stops the stepping; msx_pool_poll
+// and msx_pool_wait report it.
+static void serve_loop(msx_pool *p)
+{
+    cudaSetDevice(p->device);
+    std::unique_lock<std::mutex> lk(p->mu);
+    while (!p->serve_stop) {
+        if (p->serve_status != MSX_OK || !any_active(p)) {
+            p->cv_work.wait(lk);
+            continue;
+        }
+        msx_status st = MSX_OK;
+        if (!p->tuned) st = autotune(p);
+        if (st == MSX_OK && any_active(p)) st = launch_replay(p);
+        if (st == MSX_OK && p->inflight) {
+            const cudaEvent_t ev = p->ev_step;
+            lk.unlock();
+            cudaEventSynchronize(ev);   // errors are read again by finish_inflight
+            lk.lock();
+            st = finish_inflight(p);
+        }
+        if (st != MSX_OK) {
+            p->serve_status = st;
+            p->serve_error = msx_last_error();
+        }
+        p->cv_done.notify_all();
+    }
+}
+
+static msx_status serve_failure(msx_pool *p) { return pfail(p->serve_status, "pool serving thread: " + p->serve_error); }
+
 // ------------------------------------------------------------------ C ABI
 extern "C" msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out)
 {
@@ -448,6 +497,7 @@ extern "C" msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out)
 extern "C" msx_status msx_pool_destroy(msx_pool *p)
 {
     if (!p) return MSX_OK;
+    msx_pool_serve(p, 0);
     if (p->upload) cudaStreamSynchronize(p->upload);
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (Slot &s : p->slots)
@@ -469,7 +519,6 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
                                       int64_t num_bcs, const msx_solver_opts *o, int64_t *ticket)
 {
     if (!p || !mesh || !mat || !o || !ticket) return pfail(MSX_ERR_ARG, "NULL argument");
-    std::lock_guard<std::mutex> lk(p->mu);
     const long long nn = mesh->num_nodes, ne = mesh->num_elems;
     if (!mesh->X || !mesh->conn || nn < 4 || ne < 1 || nn >= (1LL << 31) || 4 * ne >= (1LL << 31))
         return pfail(MSX_ERR_ARG, "bad mesh");
@@ -481,17 +530,17 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     MatParams mp;
     msx_status st = make_mat(*mat, mp);
     if (st != MSX_OK) return st;
-    int slot = -1;
-    for (size_t s = 0; s < p->slots.size(); s++)
-        if (!p->slots[s].active) {
-            slot = (int)s;
-            break;
-        }
     const int prec = p->opts.precision;
-    size_t bytes = footprint(nn, ne, num_bcs, prec);
-    if (slot < 0 || p->used + bytes > p->budget) return pfail(MSX_ERR_BUSY, "pool full (slots or HBM budget)");
+    const size_t bytes = footprint(nn, ne, num_bcs, prec);
+    {   // cheap early refusal; the slot is taken below, after the host tables
+        std::lock_guard<std::mutex> lk(p->mu);
+        bool free_slot = false;
+        for (const Slot &q : p->slots) free_slot |= !q.active && !q.reserved;
+        if (!free_slot || p->used + bytes > p->budget) return pfail(MSX_ERR_BUSY, "pool full (slots or HBM budget)");
+    }
 
-    // host tables: CSR in element order and Dirichlet records (as the single-solve path)
+    // host tables, without the pool's lock: CSR in element order and Dirichlet
+    // records (as the single-solve path)
     std::vector<int> ptr(nn + 1, 0), inc(4 * ne), slots(4 * ne), node_bc(nn, -1);
     for (long long k = 0; k < 4 * ne; k++) ptr[mesh->conn[k] + 1]++;
     for (long long i = 0; i < nn; i++) ptr[i + 1] += ptr[i];
@@ -529,120 +578,184 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
         ent.push_back(e);
     }
 
+    int slot = -1;
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        for (size_t q = 0; q < p->slots.size(); q++)
+            if (!p->slots[q].active && !p->slots[q].reserved) {
+                slot = (int)q;
+                break;
+            }
+        if (slot < 0 || p->used + bytes > p->budget) return pfail(MSX_ERR_BUSY, "pool full (slots or HBM budget)");
+        p->slots[slot].reserved = true;
+        p->used += bytes;
+    }
     Slot sl;
     sl.nn = nn;
     sl.ne = ne;
     sl.bytes = bytes;
-    PCUDA(cudaMallocAsync(&sl.arena, bytes, p->upload));
-    char *q = (char *)sl.arena;
-    auto carve = [&](size_t b) {
-        char *r = q;
-        q += align256(b);
-        return (void *)r;
+    // Device uploads and set-up kernels, enqueued on the upload stream without
+    // the pool's lock: a replay in flight keeps running, and the serving thread
+    // can launch the next one meanwhile.  Replays touch only the tiles of
+    // active solves, so none reads this slot's arrays or control entries yet.
+    auto upload_solve = [&]() -> msx_status {
+        PCUDA(cudaMallocAsync(&sl.arena, bytes, p->upload));
+        char *q = (char *)sl.arena;
+        auto carve = [&](size_t b) {
+            char *r = q;
+            q += align256(b);
+            return (void *)r;
+        };
+        Problem &P = sl.P;
+        memset(&P, 0, sizeof(P));
+        P.nn = nn;
+        P.ne = ne;
+        P.nmat = 1;
+        P.mats[0] = mp;
+        P.mat = nullptr;
+        P.conn = (int4 *)carve(sizeof(int4) * ne);
+        P.G = (double *)carve(sizeof(double) * 9 * ne);
+        P.wJ = (double *)carve(sizeof(double) * ne);
+        P.Lref = (double *)carve(sizeof(double) * ne);
+        P.G32 = (float *)carve(sizeof(float) * 9 * ne);
+        P.Eref32 = (float *)carve(sizeof(float) * 9 * ne);
+        P.wJ32 = (float *)carve(sizeof(float) * ne);
+        P.Lref32 = (float *)carve(sizeof(float) * ne);
+        if (prec == MSX_PREC_DOUBLE_WORD) {
+            P.G32lo = (float *)carve(sizeof(float) * 9 * ne);
+            P.wJ32lo = (float *)carve(sizeof(float) * ne);
+        }
+        double *X = (double *)carve(sizeof(double) * 3 * nn);
+        P.X = X;
+        P.u = (double *)carve(sizeof(double) * 3 * nn);
+        P.v = (double *)carve(sizeof(double) * 3 * nn);
+        P.a = (double *)carve(sizeof(double) * 3 * nn);
+        double *mass = (double *)carve(sizeof(double) * nn), *minv = (double *)carve(sizeof(double) * nn);
+        P.mass = mass;
+        P.minv = minv;
+        P.uhl = (float2 *)carve(sizeof(float2) * 3 * nn);
+        float2 *minv2 = nullptr;
+        if (pair_state(prec)) {
+            P.vhl = (float2 *)carve(sizeof(float2) * 3 * nn);
+            P.ahl = (float2 *)carve(sizeof(float2) * 3 * nn);
+            minv2 = (float2 *)carve(sizeof(float2) * nn);
+            P.minv2 = minv2;
+        }
+        if (prec == MSX_PREC_MIXED) P.fe32 = (float *)carve(sizeof(float) * 16 * ne);
+        else P.fe = (double *)carve(sizeof(double) * 12 * ne);
+        int *d_ptr = (int *)carve(sizeof(int) * (nn + 1)), *d_inc = (int *)carve(sizeof(int) * 4 * ne);
+        int *d_nbc = (int *)carve(sizeof(int) * nn);
+        int4 *d_slot = (int4 *)carve(sizeof(int4) * ne);
+        int2 *d_rec = (int2 *)carve(sizeof(int2) * 3 * nn);
+        BCEntry *d_ent = (BCEntry *)carve(sizeof(BCEntry) * (num_bcs > 0 ? num_bcs : 1));
+        if ((size_t)(q - (char *)sl.arena) > bytes)   // the footprint must cover every array carved above
+            return pfail(MSX_ERR_CUDA, "internal: solve arena smaller than its arrays");
+        P.node_ptr = d_ptr;
+        P.node_inc = d_inc;
+        P.slot = d_slot;
+        P.node_bc = d_nbc;
+        P.bc_rec = d_rec;
+        P.bcs = d_ent;
+        P.ctrl = p->d_ctrl + 2 * slot;
+        P.dtmin = p->d_dtmin + 2 * slot;
+        P.flags = p->d_flags + 2 * slot;
+        P.sf = o->scale_factor;
+        P.tf = o->tf;
+        // everything on the upload stream: a replay in flight on the main stream
+        // keeps running; the next replay waits for ev_upload
+        cudaStream_t s = p->upload;
+        PCUDA(cudaMemcpyAsync((void *)P.conn, mesh->conn, sizeof(int4) * ne, cudaMemcpyHostToDevice, s));
+        PCUDA(cudaMemcpyAsync(X, mesh->X, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, s));
+        PCUDA(cudaMemcpyAsync(d_ptr, ptr.data(), sizeof(int) * (nn + 1), cudaMemcpyHostToDevice, s));
+        PCUDA(cudaMemcpyAsync(d_inc, inc.data(), sizeof(int) * 4 * ne, cudaMemcpyHostToDevice, s));
+        PCUDA(cudaMemcpyAsync(d_slot, slots.data(), sizeof(int4) * ne, cudaMemcpyHostToDevice, s));
+        PCUDA(cudaMemcpyAsync(d_nbc, node_bc.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, s));
+        if (!rec.empty()) PCUDA(cudaMemcpyAsync(d_rec, rec.data(), sizeof(int2) * rec.size(), cudaMemcpyHostToDevice, s));
+        if (!ent.empty()) PCUDA(cudaMemcpyAsync(d_ent, ent.data(), sizeof(BCEntry) * ent.size(), cudaMemcpyHostToDevice, s));
+        PCUDA(cudaMemsetAsync(P.u, 0, sizeof(double) * 3 * nn, s));
+        PCUDA(cudaMemsetAsync(P.v, 0, sizeof(double) * 3 * nn, s));
+        PCUDA(cudaMemsetAsync(P.a, 0, sizeof(double) * 3 * nn, s));
+        PCUDA(cudaMemsetAsync(P.uhl, 0, sizeof(float2) * 3 * nn, s));
+        if (pair_state(prec)) {
+            PCUDA(cudaMemsetAsync(P.vhl, 0, sizeof(float2) * 3 * nn, s));
+            PCUDA(cudaMemsetAsync(P.ahl, 0, sizeof(float2) * 3 * nn, s));
+        }
+        launch_setup_elements(P, X, s);
+        launch_setup_mass(P, mass, minv, s);
+        if (pair_state(prec)) launch_minv_split(minv, minv2, nn, s);
+        unsigned long long inf2[2] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL};
+        PCUDA(cudaMemcpyAsync(P.dtmin, inf2, sizeof(inf2), cudaMemcpyHostToDevice, s));
+        launch_initial_cfl(P, nullptr, 0, s);
+        launch_initial_cfl(P, nullptr, 1, s);   // u = 0: the deformed CFL equals the undeformed one
+        long long limit = o->max_steps > 0 ? o->max_steps : (1LL << 62);
+        pool_init_ctrl<<<1, 1, 0, s>>>(P, o->t0, limit);
+        PCUDA(cudaGetLastError());
+        PCUDA(cudaMemcpyAsync(p->d_descs + slot, &P, sizeof(Problem), cudaMemcpyHostToDevice, s));
+        return MSX_OK;
     };
-    Problem &P = sl.P;
-    memset(&P, 0, sizeof(P));
-    P.nn = nn;
-    P.ne = ne;
-    P.nmat = 1;
-    P.mats[0] = mp;
-    P.mat = nullptr;
-    P.conn = (int4 *)carve(sizeof(int4) * ne);
-    P.G = (double *)carve(sizeof(double) * 9 * ne);
-    P.wJ = (double *)carve(sizeof(double) * ne);
-    P.Lref = (double *)carve(sizeof(double) * ne);
-    P.G32 = (float *)carve(sizeof(float) * 9 * ne);
-    P.Eref32 = (float *)carve(sizeof(float) * 9 * ne);
-    P.wJ32 = (float *)carve(sizeof(float) * ne);
-    P.Lref32 = (float *)carve(sizeof(float) * ne);
-    if (prec == MSX_PREC_DOUBLE_WORD) {
-        P.G32lo = (float *)carve(sizeof(float) * 9 * ne);
-        P.wJ32lo = (float *)carve(sizeof(float) * ne);
+    st = upload_solve();
+
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (st == MSX_OK) {
+        // recorded under the lock: the next replay launch waits for everything
+        // enqueued on the upload stream up to here, this solve's uploads included
+        const cudaError_t e = cudaEventRecord(p->ev_upload, p->upload);
+        if (e != cudaSuccess) st = pfail(MSX_ERR_CUDA, std::string("admission event: ") + cudaGetErrorString(e));
     }
-    double *X = (double *)carve(sizeof(double) * 3 * nn);
-    P.X = X;
-    P.u = (double *)carve(sizeof(double) * 3 * nn);
-    P.v = (double *)carve(sizeof(double) * 3 * nn);
-    P.a = (double *)carve(sizeof(double) * 3 * nn);
-    double *mass = (double *)carve(sizeof(double) * nn), *minv = (double *)carve(sizeof(double) * nn);
-    P.mass = mass;
-    P.minv = minv;
-    P.uhl = (float2 *)carve(sizeof(float2) * 3 * nn);
-    float2 *minv2 = nullptr;
-    if (pair_state(prec)) {
-        P.vhl = (float2 *)carve(sizeof(float2) * 3 * nn);
-        P.ahl = (float2 *)carve(sizeof(float2) * 3 * nn);
-        minv2 = (float2 *)carve(sizeof(float2) * nn);
-        P.minv2 = minv2;
+    if (st != MSX_OK) {
+        if (sl.arena) cudaFreeAsync(sl.arena, p->upload);
+        p->slots[slot].reserved = false;
+        p->used -= bytes;
+        return st;
     }
-    if (prec == MSX_PREC_MIXED) P.fe32 = (float *)carve(sizeof(float) * 16 * ne);
-    else P.fe = (double *)carve(sizeof(double) * 12 * ne);
-    int *d_ptr = (int *)carve(sizeof(int) * (nn + 1)), *d_inc = (int *)carve(sizeof(int) * 4 * ne);
-    int *d_nbc = (int *)carve(sizeof(int) * nn);
-    int4 *d_slot = (int4 *)carve(sizeof(int4) * ne);
-    int2 *d_rec = (int2 *)carve(sizeof(int2) * 3 * nn);
-    BCEntry *d_ent = (BCEntry *)carve(sizeof(BCEntry) * (num_bcs > 0 ? num_bcs : 1));
-    if ((size_t)(q - (char *)sl.arena) > bytes) {   // the footprint must cover every array carved above
-        cudaFreeAsync(sl.arena, p->upload);
-        return pfail(MSX_ERR_CUDA, "internal: solve arena smaller than its arrays");
-    }
-    P.node_ptr = d_ptr;
-    P.node_inc = d_inc;
-    P.slot = d_slot;
-    P.node_bc = d_nbc;
-    P.bc_rec = d_rec;
-    P.bcs = d_ent;
-    P.ctrl = p->d_ctrl + 2 * slot;
-    P.dtmin = p->d_dtmin + 2 * slot;
-    P.flags = p->d_flags + 2 * slot;
-    P.sf = o->scale_factor;
-    P.tf = o->tf;
-    // everything on the upload stream: a replay in flight on the main stream
-    // keeps running; the next replay waits for ev_upload
-    cudaStream_t s = p->upload;
-    PCUDA(cudaMemcpyAsync((void *)P.conn, mesh->conn, sizeof(int4) * ne, cudaMemcpyHostToDevice, s));
-    PCUDA(cudaMemcpyAsync(X, mesh->X, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, s));
-    PCUDA(cudaMemcpyAsync(d_ptr, ptr.data(), sizeof(int) * (nn + 1), cudaMemcpyHostToDevice, s));
-    PCUDA(cudaMemcpyAsync(d_inc, inc.data(), sizeof(int) * 4 * ne, cudaMemcpyHostToDevice, s));
-    PCUDA(cudaMemcpyAsync(d_slot, slots.data(), sizeof(int4) * ne, cudaMemcpyHostToDevice, s));
-    PCUDA(cudaMemcpyAsync(d_nbc, node_bc.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, s));
-    if (!rec.empty()) PCUDA(cudaMemcpyAsync(d_rec, rec.data(), sizeof(int2) * rec.size(), cudaMemcpyHostToDevice, s));
-    if (!ent.empty()) PCUDA(cudaMemcpyAsync(d_ent, ent.data(), sizeof(BCEntry) * ent.size(), cudaMemcpyHostToDevice, s));
-    PCUDA(cudaMemsetAsync(P.u, 0, sizeof(double) * 3 * nn, s));
-    PCUDA(cudaMemsetAsync(P.v, 0, sizeof(double) * 3 * nn, s));
-    PCUDA(cudaMemsetAsync(P.a, 0, sizeof(double) * 3 * nn, s));
-    PCUDA(cudaMemsetAsync(P.uhl, 0, sizeof(float2) * 3 * nn, s));
-    if (pair_state(prec)) {
-        PCUDA(cudaMemsetAsync(P.vhl, 0, sizeof(float2) * 3 * nn, s));
-        PCUDA(cudaMemsetAsync(P.ahl, 0, sizeof(float2) * 3 * nn, s));
-    }
-    launch_setup_elements(P, X, s);
-    launch_setup_mass(P, mass, minv, s);
-    if (pair_state(prec)) launch_minv_split(minv, minv2, nn, s);
-    unsigned long long inf2[2] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL};
-    PCUDA(cudaMemcpyAsync(P.dtmin, inf2, sizeof(inf2), cudaMemcpyHostToDevice, s));
-    launch_initial_cfl(P, nullptr, 0, s);
-    launch_initial_cfl(P, nullptr, 1, s);   // u = 0: the deformed CFL equals the undeformed one
-    long long limit = o->max_steps > 0 ? o->max_steps : (1LL << 62);
-    pool_init_ctrl<<<1, 1, 0, s>>>(P, o->t0, limit);
-    PCUDA(cudaGetLastError());
-    PCUDA(cudaMemcpyAsync(p->d_descs + slot, &P, sizeof(Problem), cudaMemcpyHostToDevice, s));
-    PCUDA(cudaEventRecord(p->ev_upload, s));
     p->uploads_pending = true;
     sl.active = true;
     sl.ticket = p->next_ticket++;
     sl.submit_ms = now_ms();
     p->slots[slot] = sl;
-    p->used += bytes;
     rebuild_tiles(p);
     *ticket = sl.ticket;
+    if (p->serving) p->cv_work.notify_one();
     return MSX_OK;
+}
+
+extern "C" msx_status msx_pool_serve(msx_pool *p, int32_t enabled)
+{
+    if (!p) return pfail(MSX_ERR_ARG, "NULL pool");
+    if (enabled) {
+        std::lock_guard<std::mutex> lk(p->mu);
+        if (p->serving) return MSX_OK;
+        msx_status st = finish_inflight(p);   // the serving thread starts with no replay in flight
+        if (st != MSX_OK) return st;
+        p->serve_stop = false;
+        p->serve_status = MSX_OK;
+        p->serve_error.clear();
+        try {
+            p->server = std::thread(serve_loop, p);
+        } catch (...) {
+            return pfail(MSX_ERR_STATE, "cannot start the pool's serving thread");
+        }
+        p->serving = true;
+        return MSX_OK;
+    }
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        if (!p->serving) return MSX_OK;
+        p->serve_stop = true;
+    }
+    p->cv_work.notify_all();
+    p->server.join();   // its last replay was collected before it saw the stop
+    std::lock_guard<std::mutex> lk(p->mu);
+    p->serving = false;
+    p->cv_done.notify_all();
+    return p->serve_status == MSX_OK ? MSX_OK : serve_failure(p);
 }
 
 extern "C" msx_status msx_pool_step(msx_pool *p, int64_t steps)
 {
     if (!p) return pfail(MSX_ERR_ARG, "NULL pool");
     std::lock_guard<std::mutex> lk(p->mu);
+    if (p->serving) return pfail(MSX_ERR_STATE, "the pool's serving thread drives the steps");
     msx_status st;
     if ((st = finish_inflight(p)) != MSX_OK) return st;
     if (!p->tuned && any_active(p) && (st = autotune(p)) != MSX_OK) return st;
@@ -680,7 +793,10 @@ extern "C" msx_status msx_pool_poll(msx_pool *p, msx_pool_result *results, int32
 {
     if (!p || !n || (max > 0 && !results)) return pfail(MSX_ERR_ARG, "NULL argument");
     std::lock_guard<std::mutex> lk(p->mu);
-    if (p->inflight) {   // never waits: collect only a replay that has finished
+    *n = 0;
+    if (p->serving) {
+        if (p->serve_status != MSX_OK) return serve_failure(p);
+    } else if (p->inflight) {   // never waits: collect only a replay that has finished
         const cudaError_t q = cudaEventQuery(p->ev_step);
         if (q == cudaSuccess) {
             msx_status st = finish_inflight(p);
@@ -706,7 +822,7 @@ extern "C" msx_status msx_pool_poll(msx_pool *p, msx_pool_result *results, int32
 extern "C" msx_status msx_pool_wait(msx_pool *p, int64_t ticket, msx_pool_result *result)
 {
     if (!p || !result) return pfail(MSX_ERR_ARG, "NULL argument");
-    std::lock_guard<std::mutex> lk(p->mu);
+    std::unique_lock<std::mutex> lk(p->mu);
     auto resident = [&] {
         for (const Slot &s : p->slots)
             if (s.active && s.ticket == ticket) return true;
@@ -714,13 +830,18 @@ extern "C" msx_status msx_pool_wait(msx_pool *p, int64_t ticket, msx_pool_result
     };
     msx_status st;
     for (;;) {
-        if ((st = finish_inflight(p)) != MSX_OK) return st;
+        if (!p->serving && (st = finish_inflight(p)) != MSX_OK) return st;
         auto it = p->done.find(ticket);
         if (it != p->done.end()) {
             *result = it->second.res;
             return MSX_OK;
         }
         if (!resident()) return pfail(MSX_ERR_ARG, "unknown or already fetched ticket");
+        if (p->serving) {   // the serving thread steps; wake up at each collected replay
+            if (p->serve_status != MSX_OK) return serve_failure(p);
+            p->cv_done.wait(lk);
+            continue;
+        }
         if (!p->tuned && (st = autotune(p)) != MSX_OK) return st;
         if ((st = launch_replay(p)) != MSX_OK) return st;
     }

@@ -100,7 +100,7 @@ class PoolResult_(C.Structure):
 # every entry point declared in include/msx.h
 SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_solver", "msx_destroy",
            "msx_last_error", "msx_internal_force", "msx_get_element_data", "msx_profile", "msx_mesh_cube",
-           "msx_stream", "msx_set_device", "msx_pool_create", "msx_pool_submit", "msx_pool_step",
+           "msx_stream", "msx_set_device", "msx_pool_create", "msx_pool_submit", "msx_pool_step", "msx_pool_serve",
            "msx_pool_poll", "msx_pool_fetch", "msx_pool_wait", "msx_pool_destroy", "msx_pool_stats_get",
            "msx_internal_force_noalloc", "msx_initial_dt", "msx_element_fields", "msx_set_loads",
            "msx_set_load_blocks", "msx_node_values", "msx_element_values", "msx_element_reduce",
@@ -178,17 +178,26 @@ def cube_bcs(n: int, top_value: float, mode: int = BC_RAMP, ramp_steps: int = 0)
     nn = m ** 3
     bottom = BC_INST if mode == BC_INST else BC_RAMP
     ij = np.arange(m * m)
-    dof_b = np.concatenate([[(node + c * nn) for c in range(3)] for node in ij])
+    dof_b = (ij[:, None] + nn * np.arange(3)[None, :]).ravel()
     dof_t = ij + m * m * n + 2 * nn
-    rows = [(int(d), bottom, 0.0, 0) for d in dof_b] + [(int(d), mode, top_value, ramp_steps) for d in dof_t]
-    return rows
+    return ([(d, bottom, 0.0, 0) for d in dof_b.tolist()] +
+            [(d, mode, top_value, ramp_steps) for d in dof_t.tolist()])
+
+
+_BC_DTYPE = np.dtype({"names": [f for f, _ in BC_._fields_], "formats": ["<i8", "<i4", "<i4", "<f8"],
+                      "offsets": [getattr(BC_, f).offset for f, _ in BC_._fields_], "itemsize": C.sizeof(BC_)})
 
 
 def _bc_array(bcs):
-    arr = (BC_ * max(1, len(bcs)))()
-    for i, (dof, mode, value, ramp) in enumerate(bcs):
-        arr[i] = BC_(int(dof), int(mode), int(ramp), float(value))
-    return arr
+    """(dof, mode, value, ramp_steps) rows as an msx_bc array (at least one entry)."""
+    out = np.zeros(max(1, len(bcs)), _BC_DTYPE)
+    if len(bcs):
+        rows = np.array(bcs, dtype=[("dof", "<i8"), ("mode", "<i4"), ("value", "<f8"), ("ramp", "<i4")])
+        out["dof"][:] = rows["dof"]
+        out["mode"][:] = rows["mode"]
+        out["ramp_steps"][:] = rows["ramp"]
+        out["value"][:] = rows["value"]
+    return out
 
 
 def _opts(t0, tf, sf, max_steps, precision, spg):
@@ -226,7 +235,7 @@ class Solver:
         opts = _opts(t0, tf, scale_factor, max_steps, precision, steps_per_graph)
         h = C.c_void_p()
         _check(L.msx_create(C.byref(mesh), C.cast(mats, C.c_void_p), len(materials),
-                            C.cast(barr, C.c_void_p), len(bcs), C.byref(opts), C.byref(h)))
+                            _p(barr), len(bcs), C.byref(opts), C.byref(h)))
         self.h = h
 
     def run(self, max_steps: int = 0) -> Report:
@@ -240,7 +249,7 @@ class Solver:
     def next_solver(self, bcs, t0, tf, scale_factor, max_steps=0, precision=FP64, steps_per_graph=0):
         barr = _bc_array(bcs)
         opts = _opts(t0, tf, scale_factor, max_steps, precision, steps_per_graph)
-        _check(load().msx_next_solver(self.h, C.cast(barr, C.c_void_p), len(bcs), C.byref(opts)))
+        _check(load().msx_next_solver(self.h, _p(barr), len(bcs), C.byref(opts)))
 
     def state(self):
         u, v, a = (np.zeros(3 * self.nn) for _ in range(3))
@@ -377,6 +386,7 @@ class Pool:
                            ("msx_pool_submit", [C.c_void_p, C.POINTER(Mesh_), C.POINTER(Material_), C.c_void_p,
                                                 C.c_int64, C.POINTER(Opts_), C.POINTER(C.c_int64)]),
                            ("msx_pool_step", [C.c_void_p, C.c_int64]),
+                           ("msx_pool_serve", [C.c_void_p, C.c_int32]),
                            ("msx_pool_poll", [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
                            ("msx_pool_fetch", [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
                            ("msx_pool_wait", [C.c_void_p, C.c_int64, C.c_void_p]),
@@ -403,7 +413,7 @@ class Pool:
         barr = _bc_array(bcs)
         opts = Opts_(t0, tf, scale_factor, max_steps, 0, 0)
         t = C.c_int64()
-        st = load().msx_pool_submit(self.h, C.byref(mesh), C.byref(mat), C.cast(barr, C.c_void_p), len(bcs),
+        st = load().msx_pool_submit(self.h, C.byref(mesh), C.byref(mat), _p(barr), len(bcs),
                                     C.byref(opts), C.byref(t))
         if st == 9:
             return None
@@ -413,6 +423,11 @@ class Pool:
 
     def step(self, steps=0):
         _check(load().msx_pool_step(self.h, steps))
+
+    def serve(self, enabled=True):
+        """Serving mode: a library thread steps the pool while solves are resident
+        (submit, poll, wait and fetch keep working; step is refused)."""
+        _check(load().msx_pool_serve(self.h, 1 if enabled else 0))
 
     def poll(self, max_results=4096):
         arr = (PoolResult_ * max_results)()
