@@ -320,12 +320,27 @@ static msx_status upload_tiled(msx_handle *h)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
     h->tgrid = sms * tiled_ctas_per_sm(tiled_mode(h), h->tthreads);
     h->tgrid_node = sms * tiled_ctas_per_sm(tiled_mode(h), h->tthreads, true);
-    // Element tiles: the FP64 and double-word kernels close each tile with
-    // block-wide CFL reductions, so they take large tiles, halved while the
-    // grid would get fewer than two tiles per CTA; the mixed kernel's tiles
-    // are cheap to close and 1024 balances best.
-    int te = h->precision == MSX_PREC_MIXED ? 1024 : kMaxTileElems;
-    while (te > 256 && h->P.ne / te < 2LL * h->tgrid) te /= 2;
+    // Element tiles of P whole CTA passes (P * threads elements).  Spread over
+    // the grid, the busiest CTA runs ceil(tiles / grid) tiles; P minimises that
+    // count times (P + 1/2), the half pass standing for a tile's close (the
+    // FP64 and double-word kernels end each tile with block-wide CFL
+    // reductions), so the last wave of tiles fills the grid instead of
+    // leaving most CTAs idle.  P is capped at 4096 elements for those two
+    // kernels and at 1024 for the mixed one, whose tiles balance best small.
+    const int thr = h->tthreads;
+    const int pmax = (h->precision == MSX_PREC_MIXED ? 1024 : kMaxTileElems) / thr;
+    const long long passes = (h->P.ne + thr - 1) / thr;
+    int bestp = pmax;
+    double best = 1e300;
+    for (int P = pmax; P >= 1; P--) {
+        const long long rounds = ((passes + P - 1) / P + h->tgrid - 1) / h->tgrid;
+        const double cost = (double)rounds * (P + 0.5);
+        if (cost < best) {
+            best = cost;
+            bestp = P;
+        }
+    }
+    const int te = bestp * thr;
     const int tn = 128;
     if (!h->d_desc.p || te != h->tile_elems) {
         std::vector<Tile> et, nt;
