@@ -44,7 +44,9 @@ enum { MSX_LAW_NEO_HOOKEAN = 0,             /* *HyperElastic, Neo-Hookean       
 
 enum { MSX_BC_RAMP = 0,      /* *BOUNDARY, TYPE=DISPLACEMENT RAMP: value reached at tf         */
        MSX_BC_INST = 1,      /* *BOUNDARY, TYPE=DISPLACEMENT INST: value applied at first step */
-       MSX_BC_VEL_RAMP = 2 };/* extension: velocity ramped linearly to `value` over ramp_steps */
+       MSX_BC_VEL_RAMP = 2,  /* extension: velocity ramped linearly to `value` over ramp_steps */
+       MSX_BC_RAMP_RATE = 3 };/* a ramp given by its rate U/(tf - t0), the value a ramped
+                                 classDirichlet stores (getUU(), classNodes.cpp:66-73)     */
 
 enum { MSX_PREC_FP64 = 0,        /* plain FP64, FMA-contracted, algebraically simplified laws */
        MSX_PREC_FP64_EXACT = 1,  /* FP64 in the reference's operation order, no contraction   */

@@ -111,3 +111,35 @@ def test_large_compression(law, precision):
     assert steps == ref.steps
     assert np.abs(u).max() > 0.2          # the top really moved
     assert rel(u, ref.u) <= 1e-10, rel(u, ref.u)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [msx.FP64_EXACT, msx.FP64, msx.MIXED, msx.DOUBLE_WORD])
+def test_ramp_given_by_its_rate(precision):
+    """MSX_BC_RAMP_RATE takes the rate a ramped classDirichlet stores
+    (U / (tf - t0)); given the same division it is bit for bit MSX_BC_RAMP,
+    in a two-block chain (rates of each block's own duration) and in the pool."""
+    n, t0, t1, t2 = 4, 0.0, 0.013, 0.029
+    X, conn = msx.mesh_cube(n, seed=5)
+    ramp1, ramp2 = msx.cube_bcs(n, 0.002), msx.cube_bcs(n, 0.005)
+    rate = lambda bcs, d: [(dof, msx.BC_RAMP_RATE, value / d, 0) for dof, _, value, _ in bcs]
+    out = []
+    for b1, b2 in ((ramp1, ramp2), (rate(ramp1, t1 - t0), rate(ramp2, t2 - t1))):
+        S = msx.Solver(X, conn, [(msx.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0)], b1, t0, t1, 0.5, precision=precision)
+        S.run()
+        S.next_solver(b2, t1, t2, 0.5, precision=precision)
+        S.run()
+        out.append(S.state())
+        S.close()
+    for x, y in zip(*out):
+        assert np.array_equal(x, y)
+    if precision in (msx.FP64, msx.MIXED, msx.DOUBLE_WORD):
+        P = msx.Pool(max_slots=2, precision=precision, steps_per_launch=4)
+        ta = P.submit(X, conn, (msx.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0), ramp1, 0, t0, t1)
+        tb = P.submit(X, conn, (msx.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0), rate(ramp1, t1 - t0), 0, t0, t1)
+        P.wait(ta)
+        P.wait(tb)
+        ua, ub = P.fetch(ta), P.fetch(tb)
+        P.close()
+        for x, y in zip(ua, ub):
+            assert np.array_equal(x, y)

@@ -556,7 +556,7 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     std::vector<long long> order(num_bcs);
     std::iota(order.begin(), order.end(), 0);
     for (long long k = 0; k < num_bcs; k++) {
-        if (bcs[k].dof < 0 || bcs[k].dof >= 3 * nn || bcs[k].mode < 0 || bcs[k].mode > 2)
+        if (bcs[k].dof < 0 || bcs[k].dof >= 3 * nn || bcs[k].mode < 0 || bcs[k].mode > 3)
             return pfail(MSX_ERR_ARG, "bad boundary condition entry");
         if (bcs[k].mode == MSX_BC_RAMP && !(o->tf - o->t0 != 0)) return pfail(MSX_ERR_ARG, "ramp BC needs tf != t0");
     }
@@ -565,7 +565,8 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     std::vector<BCEntry> ent;
     for (long long k = 0; k < num_bcs; k++) {
         const msx_bc &b = bcs[order[k]];
-        BCEntry e{b.mode, b.ramp_steps, b.mode == MSX_BC_RAMP ? b.value / (o->tf - o->t0) : b.value};
+        BCEntry e{b.mode == MSX_BC_RAMP_RATE ? MSX_BC_RAMP : b.mode, b.ramp_steps,
+                  b.mode == MSX_BC_RAMP ? b.value / (o->tf - o->t0) : b.value};
         long long node = b.dof % nn;
         int comp = (int)(b.dof / nn);
         if (node_bc[node] < 0) {

@@ -195,7 +195,7 @@ static msx_status build_bcs(long long nn, const msx_bc *bcs, long long nbc, doub
     std::iota(order.begin(), order.end(), 0);
     for (long long k = 0; k < nbc; k++) {
         if (bcs[k].dof < 0 || bcs[k].dof >= 3 * nn) return fail(MSX_ERR_ARG, "BC dof out of range");
-        if (bcs[k].mode < 0 || bcs[k].mode > 2) return fail(MSX_ERR_ARG, "unknown BC mode");
+        if (bcs[k].mode < 0 || bcs[k].mode > 3) return fail(MSX_ERR_ARG, "unknown BC mode");
         if (bcs[k].mode == MSX_BC_RAMP && !(tf - t0 != 0)) return fail(MSX_ERR_ARG, "ramp BC needs tf != t0");
     }
     std::stable_sort(order.begin(), order.end(), [&](long long x, long long y) { return bcs[x].dof < bcs[y].dof; });
@@ -206,7 +206,7 @@ static msx_status build_bcs(long long nn, const msx_bc *bcs, long long nbc, doub
     for (long long k = 0; k < nbc; k++) {
         const msx_bc &b = bcs[order[k]];
         BCEntry e;
-        e.mode = b.mode;
+        e.mode = b.mode == MSX_BC_RAMP_RATE ? MSX_BC_RAMP : b.mode;
         e.ramp_steps = b.ramp_steps;
         // classNodes.cpp:58-74: a ramp stores U/duration, an instant BC stores U
         e.val = b.mode == MSX_BC_RAMP ? b.value / (tf - t0) : b.value;

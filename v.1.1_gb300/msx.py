@@ -19,7 +19,7 @@ OK = 0
 ERR = {0: "OK", 1: "ARG", 2: "CUDA", 3: "NEG_JACOBIAN", 4: "NAN", 5: "OOM", 6: "STATE",
        7: "NO_DEVICE", 8: "TIMEOUT", 9: "BUSY"}
 NEO_HOOKEAN, COMPRESSIBLE_NH, STVK, LINEAR_ELASTIC = 0, 1, 2, 3
-BC_RAMP, BC_INST, BC_VEL_RAMP = 0, 1, 2
+BC_RAMP, BC_INST, BC_VEL_RAMP, BC_RAMP_RATE = 0, 1, 2, 3
 FP64, FP64_EXACT, MIXED, DOUBLE_WORD = 0, 1, 2, 3
 
 
