@@ -1,6 +1,7 @@
 """Edge cases of the explicit step on the GPU, against the oracle: a single
 tet, a mesh whose every DOF is prescribed, a solver chain that changes
-precision between blocks, a block of zero length, malformed meshes."""
+precision between blocks, a block of zero length, malformed meshes, ramps
+given by their rate, nodes shared by 100 and 1100 elements."""
 import numpy as np
 import pytest
 
@@ -143,3 +144,38 @@ def test_ramp_given_by_its_rate(precision):
         P.close()
         for x, y in zip(ua, ub):
             assert np.array_equal(x, y)
+
+
+def fan_mesh(m):
+    """m tets sharing an apex (node 0) and a base centre (node 1) over a ring of
+    m nodes: two nodes of degree m, the ring nodes of degree 2."""
+    ang = 2 * np.pi * np.arange(m) / m
+    X = np.zeros((3, m + 2))
+    X[2, 0] = 1.0
+    X[0, 2:], X[1, 2:] = np.cos(ang), np.sin(ang)
+    conn = np.array([[0, 1, 2 + i, 2 + (i + 1) % m] for i in range(m)], np.int32)
+    return O.Mesh(X, conn)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m", [100, 1100])
+def test_high_degree_nodes(m):
+    """Node lists far longer than a tet mesh's ~24: 100 (sorted on the device)
+    and 1100 (above the device builder's limit: built on the host).  Element
+    order of every node's sum is kept: the reference-order mode equals the
+    oracle bit for bit (St-Venant-Kirchhoff), the FP64 mode within 1e-10."""
+    mesh = fan_mesh(m)
+    bcs = [(i + c * mesh.nn, O.BC_RAMP, 0.0, 0) for i in range(2, mesh.nn) for c in range(3)]
+    bcs += [(0 + 2 * mesh.nn, O.BC_RAMP, -0.01, 0)]
+    solvers = [O.Solver(0.0, 1.0, 0.5, bcs, max_steps=6)]
+    ref = O.run(mesh, [O.Material(O.STVK)], solvers)
+    for precision, tol in ((msx.FP64_EXACT, 0.0), (msx.FP64, 1e-10)):
+        S = msx.Solver(mesh.X, mesh.conn, [(msx.STVK, 1e6, 0.3, 1000.0)], bcs, 0.0, 1.0, 0.5, max_steps=6,
+                       precision=precision)
+        assert S.run().steps == ref.steps == 6
+        u, v, a = S.state()
+        S.close()
+        if tol == 0.0:
+            assert np.array_equal(u, ref.u) and np.array_equal(v, ref.v) and np.array_equal(a, ref.a)
+        else:
+            assert rel(u, ref.u) <= tol and rel(a, ref.a) <= tol

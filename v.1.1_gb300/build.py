@@ -25,6 +25,7 @@ UNITS = {
     "msx_runtime.cu": [],
     "msx_pool.cu": [],
     "msx_noalloc.cu": ["--fmad=false"],
+    "msx_csr.cu": [],
 }
 DECK = os.path.join(OUT, "msx_deck")
 

@@ -2,6 +2,7 @@
 // host runtime of the explicit C3D4 step.
 #pragma once
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "../../include/msx.h"
@@ -204,5 +205,14 @@ void launch_internal_force_mixed(const Problem &p, double *fint, cudaStream_t s)
 void launch_internal_force_dw(const Problem &p, double *fint, cudaStream_t s);
 // Law parameters of one material, FP64 and the FP32 / double-word copies; false if invalid.
 bool material_params(const msx_material &m, MatParams &o);
+
+// Node -> (element, corner) lists in element order (node_ptr[nn + 1],
+// node_inc[4 ne], slot[ne]) built on the device from the uploaded conn;
+// synchronises s once.  MSX_ERR_ARG (message in err) when a node id is out of
+// range; lists with a node in more than kCsrMaxDegree elements are built on the
+// host from conn_host instead.
+constexpr int kCsrMaxDegree = 1024;
+msx_status build_node_csr(const int4 *conn, const int *conn_host, long long ne, long long nn, int *node_ptr,
+                          int *node_inc, int4 *slot, cudaStream_t s, std::string &err);
 
 }  // namespace msx

@@ -539,20 +539,9 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
         if (!free_slot || p->used + bytes > p->budget) return pfail(MSX_ERR_BUSY, "pool full (slots or HBM budget)");
     }
 
-    // host tables, without the pool's lock: CSR in element order and Dirichlet
-    // records (as the single-solve path)
-    std::vector<int> ptr(nn + 1, 0), inc(4 * ne), slots(4 * ne), node_bc(nn, -1);
-    for (long long k = 0; k < 4 * ne; k++) ptr[mesh->conn[k] + 1]++;
-    for (long long i = 0; i < nn; i++) ptr[i + 1] += ptr[i];
-    {
-        std::vector<int> fill(ptr.begin(), ptr.end() - 1);
-        for (long long e = 0; e < ne; e++)
-            for (int q = 0; q < 4; q++) {
-                int k = fill[mesh->conn[e * 4 + q]]++;
-                inc[k] = (int)(e * 4 + q);
-                slots[e * 4 + q] = k;
-            }
-    }
+    // host tables, without the pool's lock: Dirichlet records (as the
+    // single-solve path); the node -> corner lists are built on the device
+    std::vector<int> node_bc(nn, -1);
     std::vector<long long> order(num_bcs);
     std::iota(order.begin(), order.end(), 0);
     for (long long k = 0; k < num_bcs; k++) {
@@ -667,9 +656,11 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
         cudaStream_t s = p->upload;
         PCUDA(cudaMemcpyAsync((void *)P.conn, mesh->conn, sizeof(int4) * ne, cudaMemcpyHostToDevice, s));
         PCUDA(cudaMemcpyAsync(X, mesh->X, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, s));
-        PCUDA(cudaMemcpyAsync(d_ptr, ptr.data(), sizeof(int) * (nn + 1), cudaMemcpyHostToDevice, s));
-        PCUDA(cudaMemcpyAsync(d_inc, inc.data(), sizeof(int) * 4 * ne, cudaMemcpyHostToDevice, s));
-        PCUDA(cudaMemcpyAsync(d_slot, slots.data(), sizeof(int4) * ne, cudaMemcpyHostToDevice, s));
+        {
+            std::string err;
+            const msx_status cst = build_node_csr(P.conn, mesh->conn, ne, nn, d_ptr, d_inc, d_slot, s, err);
+            if (cst != MSX_OK) return pfail(cst, err);
+        }
         PCUDA(cudaMemcpyAsync(d_nbc, node_bc.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, s));
         if (!rec.empty()) PCUDA(cudaMemcpyAsync(d_rec, rec.data(), sizeof(int2) * rec.size(), cudaMemcpyHostToDevice, s));
         if (!ent.empty()) PCUDA(cudaMemcpyAsync(d_ent, ent.data(), sizeof(BCEntry) * ent.size(), cudaMemcpyHostToDevice, s));

@@ -501,8 +501,6 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(MSX_ERR_NO_DEVICE, "no CUDA device");
     const long long nn = mesh->num_nodes, ne = mesh->num_elems;
-    for (long long k = 0; k < 4 * ne; k++)
-        if (mesh->conn[k] < 0 || mesh->conn[k] >= nn) return fail(MSX_ERR_ARG, "connectivity index out of range");
     if (mesh->elem_material)
         for (long long e = 0; e < ne; e++)
             if (mesh->elem_material[e] < 0 || mesh->elem_material[e] >= num_mats)
@@ -534,23 +532,6 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     cudaEventCreateWithFlags(&h->evc[1], cudaEventDisableTiming);
     if (cudaMallocHost((void **)&h->h_ctrl, 2 * sizeof(Ctrl)) != cudaSuccess)
         return bail(fail(MSX_ERR_OOM, "pinned control buffer"));
-
-    // node -> (element, corner) CSR in element order: the per-node summation
-    // order of classSolverExplicit::computeInternalForce (solverExplicit.cpp:363-379)
-    // (slots: where each corner sits in that list; the FP64 and mixed element
-    // kernels write corner forces there, so the node kernel reads them in a run)
-    std::vector<int> ptr(nn + 1, 0), inc(4 * ne), slots(4 * ne);
-    for (long long k = 0; k < 4 * ne; k++) ptr[mesh->conn[k] + 1]++;
-    for (long long i = 0; i < nn; i++) ptr[i + 1] += ptr[i];
-    {
-        std::vector<int> fill(ptr.begin(), ptr.end() - 1);
-        for (long long e = 0; e < ne; e++)
-            for (int q = 0; q < 4; q++) {
-                int k = fill[mesh->conn[e * 4 + q]]++;
-                inc[k] = (int)(e * 4 + q);
-                slots[e * 4 + q] = k;
-            }
-    }
 
 #define ALLOC(buf, n) \
     if (cudaError_t e_ = buf.alloc(n)) return bail(fail(MSX_ERR_OOM, std::string("device allocation: ") + cudaGetErrorString(e_)))
@@ -594,9 +575,13 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return bail(fail(MSX_ERR_CUDA, "upload failed"))
     UP(h->conn.p, mesh->conn, sizeof(int4) * ne);
     UP(h->X.p, mesh->X, sizeof(double) * 3 * nn);
-    UP(h->node_ptr.p, ptr.data(), sizeof(int) * (nn + 1));
-    UP(h->node_inc.p, inc.data(), sizeof(int) * 4 * ne);
-    UP(h->slot.p, slots.data(), sizeof(int4) * ne);
+    {   // node -> (element, corner) lists in element order, built on the device;
+        // this also range-checks the connectivity before any kernel reads it
+        std::string err;
+        if ((st = build_node_csr(h->conn.p, mesh->conn, ne, nn, h->node_ptr.p, h->node_inc.p, h->slot.p, s, err)) !=
+            MSX_OK)
+            return bail(fail(st, err.c_str()));
+    }
     if (h->mat.p) UP(h->mat.p, mids.data(), ne);
 #undef UP
     cudaMemsetAsync(h->fe.p, 0, sizeof(double) * 12 * ne, s);
