@@ -161,12 +161,22 @@ def dword_roofline(ne, nn, prof, ms_per_step):
 
 def run_e2e(X, conn, bcs, steps):
     """Whole job through the C ABI from host buffers: upload, set-up, K steps,
-    read back u, v, a.  Inputs come from pinned host memory."""
+    read back u, v, a.  The mesh is in page-locked host memory before the
+    clock starts and the state is read back into page-locked buffers."""
     import msx
+    import torch
+
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+
+    Xp, cp = pinned(X.shape, torch.float64), pinned(conn.shape, torch.int32)
+    Xp[...] = X
+    cp[...] = conn
+    out = tuple(pinned((X.size,), torch.float64) for _ in range(3))
     t0 = time.perf_counter()
-    S = msx.Solver(X, conn, [MATERIAL], bcs, 0.0, 1e30, 0.5, max_steps=0, precision=msx.FP64)
+    S = msx.Solver(Xp, cp, [MATERIAL], bcs, 0.0, 1e30, 0.5, max_steps=0, precision=msx.FP64)
     rep = S.run(steps)
-    u, v, a = S.state()
+    u, v, a = S.state(out)
     wall = time.perf_counter() - t0
     S.close()
     h2d = X.nbytes + conn.nbytes + len(bcs) * 24

@@ -251,8 +251,15 @@ class Solver:
         opts = _opts(t0, tf, scale_factor, max_steps, precision, steps_per_graph)
         _check(load().msx_next_solver(self.h, _p(barr), len(bcs), C.byref(opts)))
 
-    def state(self):
-        u, v, a = (np.zeros(3 * self.nn) for _ in range(3))
+    def state(self, out=None):
+        """u, v, a of the last step, into `out` (three contiguous float64 arrays
+        of 3*nn, e.g. in page-locked memory) when given."""
+        if out is None:
+            out = tuple(np.zeros(3 * self.nn) for _ in range(3))
+        for x in out:
+            if x.dtype != np.float64 or x.size != 3 * self.nn or not x.flags.c_contiguous:
+                raise ValueError("state buffers must be contiguous float64 arrays of 3*nn")
+        u, v, a = out
         _check(load().msx_get_state(self.h, _p(u), _p(v), _p(a)))
         return u, v, a
 
