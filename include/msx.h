@@ -346,7 +346,8 @@ typedef struct {
 } msx_pool_result;
 
 msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out);
-/* Admit a solve (copies host inputs); MSX_ERR_BUSY if slots/HBM are full. */
+/* Admit a solve (copies host inputs); MSX_ERR_BUSY if slots/HBM are full
+ * (a finished solve frees its slot at once, its HBM when it is fetched). */
 msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const msx_material *mat,
                            const msx_bc *bcs, int64_t num_bcs, const msx_solver_opts *opts,
                            int64_t *ticket);
@@ -371,6 +372,11 @@ msx_status msx_pool_serve(msx_pool *p, int32_t enabled);
  * if it has completed): fills up to max results, returns the count in *n.
  * u, v, a of a solve are copied out by msx_pool_fetch. */
 msx_status msx_pool_poll(msx_pool *p, msx_pool_result *results, int32_t max, int32_t *n);
+/* Copy a finished solve's u, v, a (host buffers of 3*num_nodes doubles, any
+ * may be NULL; page-locked buffers copy fastest) and release its device memory.
+ * The result stays on the device until then, counted against the HBM budget.
+ * The copies run on a stream of their own without the pool's lock, so the
+ * replays, admissions and polls of other threads go on meanwhile. */
 msx_status msx_pool_fetch(msx_pool *p, int64_t ticket, double *u, double *v, double *a);
 /* Step the pool until solve `ticket` has finished and fill its result (the
  * other resident solves advance too; their results are kept for poll/fetch).

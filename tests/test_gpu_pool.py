@@ -60,7 +60,7 @@ def test_continuous_admission_and_budget():
     probe.close()
     # a budget that fits two solves of this size but not three
     P = msx.Pool(max_slots=64, precision=msx.MIXED, hbm_budget_bytes=int(2.5 * one), steps_per_launch=4)
-    admitted, waiting, done = [], list(range(6)), {}
+    admitted, waiting, done, got = [], list(range(6)), {}, {}
     while waiting or admitted:
         while waiting:
             t = P.submit(X, c, m, b, 30 + 4 * waiting[0])
@@ -71,11 +71,15 @@ def test_continuous_admission_and_budget():
         P.step()
         for r in P.poll():
             done[r["ticket"]] = r
+            if waiting and len(admitted) == 2:
+                # a finished solve holds its HBM until it is fetched
+                assert P.submit(X, c, m, b, 1) is None
+            got[r["ticket"]] = P.fetch(r["ticket"])[0]
             admitted = [(tt, s) for tt, s in admitted if tt != r["ticket"]]
     assert len(done) == 6 and all(r["status"] == 0 for r in done.values())
     ref = {s: alone(X, c, m, b, s, msx.MIXED)[0] for s in {r["steps"] for r in done.values()}}
     for t, r in done.items():
-        assert np.array_equal(P.fetch(t)[0], ref[r["steps"]])
+        assert np.array_equal(got[t], ref[r["steps"]])
     P.close()
 
 

@@ -83,9 +83,16 @@ struct Slot {
     double submit_ms = 0;
 };
 
+// A finished solve: its result, and its arena, kept on the device until
+// msx_pool_fetch copies u, v, a out (ready: recorded after the last replay
+// and, for the pair-state modes, the merge of u, v, a back to FP64).
 struct Finished {
     msx_pool_result res;
-    std::vector<double> u, v, a;
+    void *arena = nullptr;
+    size_t bytes = 0;
+    long long nn = 0;
+    const double *u = nullptr, *v = nullptr, *a = nullptr;
+    cudaEvent_t ready = nullptr;
 };
 
 struct Sched {
@@ -102,6 +109,7 @@ struct msx_pool {
     int device = 0, sms = 152;
     cudaStream_t stream = nullptr;   // graph replays and result copies
     cudaStream_t upload = nullptr;   // admissions: uploads and set-up kernels, overlapping a replay
+    cudaStream_t fetch = nullptr;    // msx_pool_fetch: result copies, overlapping a replay
     cudaEvent_t ev_upload = nullptr, ev_step = nullptr;
     bool uploads_pending = false;    // admissions since the last replay launch
     bool inflight = false;           // a replay launched by msx_pool_step not yet collected
@@ -257,19 +265,19 @@ static msx_status collect(msx_pool *p)
         f.res.reserved = 0;
         f.res.steps = c.step;
         f.res.t = c.t;
-        size_t bytes = sizeof(double) * 3 * sl.nn;
+        // no copy here: the result stays in the solve's arena until it is
+        // fetched, so the next replay is not held up by device-to-host copies
         if (pair_state(p->opts.precision)) launch_state_merge(sl.P, p->stream);
-        f.u.resize(3 * sl.nn);
-        f.v.resize(3 * sl.nn);
-        f.a.resize(3 * sl.nn);
-        PCUDA(cudaMemcpyAsync(f.u.data(), sl.P.u, bytes, cudaMemcpyDeviceToHost, p->stream));
-        PCUDA(cudaMemcpyAsync(f.v.data(), sl.P.v, bytes, cudaMemcpyDeviceToHost, p->stream));
-        PCUDA(cudaMemcpyAsync(f.a.data(), sl.P.a, bytes, cudaMemcpyDeviceToHost, p->stream));
-        PCUDA(cudaStreamSynchronize(p->stream));
+        PCUDA(cudaEventCreateWithFlags(&f.ready, cudaEventDisableTiming));
+        PCUDA(cudaEventRecord(f.ready, p->stream));
+        f.arena = sl.arena;
+        f.bytes = sl.bytes;   // still counted in p->used until the fetch
+        f.nn = sl.nn;
+        f.u = sl.P.u;
+        f.v = sl.P.v;
+        f.a = sl.P.a;
         f.res.submit_to_done_ms = now_ms() - sl.submit_ms;
-        PCUDA(cudaFreeAsync(sl.arena, p->stream));
-        p->used -= sl.bytes;
-        sl = Slot();
+        sl = Slot();   // the slot and its control entries can take a new solve
         const long long t = f.res.ticket;
         p->done[t] = std::move(f);
         p->done_order.push_back(t);
@@ -476,6 +484,7 @@ extern "C" msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out)
     };
     if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&p->upload, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&p->fetch, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&p->ev_upload, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&p->ev_step, cudaEventDisableTiming) != cudaSuccess)
         return bail(pfail(MSX_ERR_CUDA, "streams"));
@@ -500,8 +509,13 @@ extern "C" msx_status msx_pool_destroy(msx_pool *p)
     msx_pool_serve(p, 0);
     if (p->upload) cudaStreamSynchronize(p->upload);
     if (p->stream) cudaStreamSynchronize(p->stream);
+    if (p->fetch) cudaStreamSynchronize(p->fetch);
     for (Slot &s : p->slots)
         if (s.arena) cudaFree(s.arena);
+    for (auto &d : p->done) {   // results never fetched
+        if (d.second.arena) cudaFree(d.second.arena);
+        if (d.second.ready) cudaEventDestroy(d.second.ready);
+    }
     if (p->graph) cudaGraphExecDestroy(p->graph);
     for (void *q : {(void *)p->d_descs, (void *)p->d_ctrl, (void *)p->d_dtmin, (void *)p->d_flags, (void *)p->d_counts,
                     (void *)p->d_etiles, (void *)p->d_ntiles})
@@ -509,6 +523,7 @@ extern "C" msx_status msx_pool_destroy(msx_pool *p)
     if (p->h_ctrl) cudaFreeHost(p->h_ctrl);
     if (p->stream) cudaStreamDestroy(p->stream);
     if (p->upload) cudaStreamDestroy(p->upload);
+    if (p->fetch) cudaStreamDestroy(p->fetch);
     for (cudaEvent_t e : {p->ev_upload, p->ev_step})
         if (e) cudaEventDestroy(e);
     delete p;
@@ -842,14 +857,30 @@ extern "C" msx_status msx_pool_wait(msx_pool *p, int64_t ticket, msx_pool_result
 extern "C" msx_status msx_pool_fetch(msx_pool *p, int64_t ticket, double *u, double *v, double *a)
 {
     if (!p) return pfail(MSX_ERR_ARG, "NULL pool");
-    std::lock_guard<std::mutex> lk(p->mu);
-    auto it = p->done.find(ticket);
-    if (it == p->done.end()) return pfail(MSX_ERR_STATE, "ticket not finished or already fetched");
-    const Finished &f = it->second;
-    if (u) memcpy(u, f.u.data(), sizeof(double) * f.u.size());
-    if (v) memcpy(v, f.v.data(), sizeof(double) * f.v.size());
-    if (a) memcpy(a, f.a.data(), sizeof(double) * f.a.size());
-    p->done.erase(it);
+    Finished f;
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        auto it = p->done.find(ticket);
+        if (it == p->done.end()) return pfail(MSX_ERR_STATE, "ticket not finished or already fetched");
+        f = it->second;
+        p->done.erase(it);
+    }
+    // copies on the fetch stream without the pool's lock: replays, admissions
+    // and polls go on meanwhile
+    const size_t bytes = sizeof(double) * 3 * f.nn;
+    cudaError_t e = cudaStreamWaitEvent(p->fetch, f.ready, 0);
+    if (e == cudaSuccess && u) e = cudaMemcpyAsync(u, f.u, bytes, cudaMemcpyDeviceToHost, p->fetch);
+    if (e == cudaSuccess && v) e = cudaMemcpyAsync(v, f.v, bytes, cudaMemcpyDeviceToHost, p->fetch);
+    if (e == cudaSuccess && a) e = cudaMemcpyAsync(a, f.a, bytes, cudaMemcpyDeviceToHost, p->fetch);
+    const cudaError_t es = cudaStreamSynchronize(p->fetch);
+    if (e == cudaSuccess) e = es;
+    cudaFreeAsync(f.arena, p->fetch);
+    cudaEventDestroy(f.ready);
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        p->used -= f.bytes;
+    }
+    if (e != cudaSuccess) return pfail(MSX_ERR_CUDA, std::string("pool fetch: ") + cudaGetErrorString(e));
     return MSX_OK;
 }
 

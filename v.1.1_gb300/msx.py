@@ -449,10 +449,18 @@ class Pool:
         _check(load().msx_pool_wait(self.h, ticket, C.byref(r)))
         return dict(ticket=r.ticket, status=r.status, steps=r.steps, t=r.t, latency_ms=r.submit_to_done_ms)
 
-    def fetch(self, ticket):
-        nn = self.sizes.pop(ticket)
-        u, v, a = (np.zeros(3 * nn) for _ in range(3))
+    def fetch(self, ticket, out=None):
+        """u, v, a of a finished solve (into `out`, three contiguous float64 arrays
+        of 3*nn, when given); releases its device memory."""
+        nn = self.sizes[ticket]
+        if out is None:
+            out = tuple(np.zeros(3 * nn) for _ in range(3))
+        for x in out:
+            if x.dtype != np.float64 or x.size != 3 * nn or not x.flags.c_contiguous:
+                raise ValueError("result buffers must be contiguous float64 arrays of 3*nn")
+        u, v, a = out
         _check(load().msx_pool_fetch(self.h, ticket, _p(u), _p(v), _p(a)))
+        del self.sizes[ticket]
         return u, v, a
 
     def stats(self):
