@@ -510,6 +510,34 @@ __device__ __forceinline__ double node_fext(const Problem &p, long long i, int q
     return ext_force_dof(p, i + (long long)q * p.nn, ns.t);
 }
 
+// Biased exponent field of a double (0: zero or subnormal, 0x7FF: Inf or NaN).
+__device__ __forceinline__ int dexp_field(double x) { return (__double2hiint(x) >> 20) & 0x7FF; }
+
+// x as an integer multiple of 2^(max(E,1) - 1075 - H), truncated toward zero;
+// E is at least x's exponent field and not 0x7FF, 0 <= H <= 10.
+__device__ __forceinline__ long long dfixed(double x, int E, int H)
+{
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7FF);
+    unsigned long long m = (unsigned long long)b & 0xFFFFFFFFFFFFFull;
+    if (ex) m |= 1ull << 52;
+    const int d = max(E, 1) - max(ex, 1);
+    const unsigned long long t = d > 63 ? 0ull : (m << H) >> d;
+    return b < 0 ? -(long long)t : (long long)t;
+}
+
+// x * 2^k for an integer-valued x (|x| < 2^63) and -1085 <= k <= 971: exact
+// unless the product is subnormal, then rounded once (the first factor of the
+// two-step case keeps x * 2^-600 normal and exact).
+__device__ __forceinline__ double pow2_scale(double x, int k)
+{
+    if (k < -1022) {
+        x *= __longlong_as_double((long long)(1023 - 600) << 52);
+        k += 600;
+    }
+    return x * __longlong_as_double((long long)(k + 1023) << 52);
+}
+
 __device__ __forceinline__ void node_quad_fp64(const Problem &p, long long i, bool valid, const NodeStep &ns)
 {
     const int q = threadIdx.x & 3;
@@ -530,33 +558,71 @@ __device__ __forceinline__ void node_quad_fp64(const Problem &p, long long i, bo
         k0 = p.node_ptr[i];
         k1 = p.node_ptr[i + 1];
     }
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-    int k = k0 + q;
-    if (k < k1) {
+    // The node's f_int per component as one exact integer sum, rounded once:
+    // each term's 53-bit significand aligned to the largest exponent E of that
+    // component among the node's terms, with H guard bits below it, summed in
+    // int64 on the integer pipes instead of ~24 dependent FP64 additions.  With
+    // n terms, H = 10 - ceil(log2 n) keeps the sum below 2^63; bits below the
+    // guard bits are truncated (at most one unit of 2^(E - 1075 - H) per term).
+    // The sum does not depend on the order of the terms.  Nodes with an
+    // infinite or NaN term, or too many terms for H >= 0 (and the other nodes of
+    // their warp), add in FP64.
+    const int n = k1 - k0;   // the same for the node's four lanes
+    int e0 = 0, e1 = 0, e2 = 0;
+    for (int k = k0 + q; k < k1; k += 4) {
         const double *f = p.fe + (long long)k * 3;
-        s0 = f[0];
-        s1 = f[1];
-        s2 = f[2];
-        k += 4;
+        e0 = max(e0, dexp_field(__ldg(f)));
+        e1 = max(e1, dexp_field(__ldg(f + 1)));
+        e2 = max(e2, dexp_field(__ldg(f + 2)));
     }
-    for (; k < k1; k += 4) {
-        const double *f = p.fe + (long long)k * 3;
-        s0 += f[0];
-        s1 += f[1];
-        s2 += f[2];
+#pragma unroll
+    for (int o = 1; o <= 2; o <<= 1) {
+        e0 = max(e0, __shfl_xor_sync(0xffffffffu, e0, o));
+        e1 = max(e1, __shfl_xor_sync(0xffffffffu, e1, o));
+        e2 = max(e2, __shfl_xor_sync(0xffffffffu, e2, o));
     }
-    // pairs (0,1), (2,3): even lanes need components 0 and 2, odd lanes 1
-    double x = __shfl_xor_sync(0xffffffffu, odd ? s0 : s1, 1), y = __shfl_xor_sync(0xffffffffu, s2, 1);
-    if (odd) {
-        s1 += x;
+    const int H = 10 - (n > 1 ? 32 - __clz(n - 1) : 0);
+    // one path for the whole warp: both use shuffles over all 32 lanes (lanes
+    // past the tile's end have no terms and vote for the integer path)
+    const bool fixed = __all_sync(0xffffffffu, H >= 0 && max(e0, max(e1, e2)) < 0x7FF);
+    double s;
+    if (fixed) {
+        long long a0 = 0, a1 = 0, a2 = 0;
+        for (int k = k0 + q; k < k1; k += 4) {
+            const double *f = p.fe + (long long)k * 3;
+            a0 += dfixed(__ldg(f), e0, H);
+            a1 += dfixed(__ldg(f + 1), e1, H);
+            a2 += dfixed(__ldg(f + 2), e2, H);
+        }
+#pragma unroll
+        for (int o = 1; o <= 2; o <<= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+            a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+        }
+        if (!own) return;
+        s = pow2_scale(__ll2double_rn(pick3(q, a0, a1, a2)), max(pick3(q, e0, e1, e2), 1) - 1075 - H);
     } else {
-        s0 += x;
-        s2 += y;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        for (int k = k0 + q; k < k1; k += 4) {
+            const double *f = p.fe + (long long)k * 3;
+            s0 += f[0];
+            s1 += f[1];
+            s2 += f[2];
+        }
+        // pairs (0,1), (2,3): even lanes need components 0 and 2, odd lanes 1
+        double x = __shfl_xor_sync(0xffffffffu, odd ? s0 : s1, 1), y = __shfl_xor_sync(0xffffffffu, s2, 1);
+        if (odd) {
+            s1 += x;
+        } else {
+            s0 += x;
+            s2 += y;
+        }
+        // across pairs: lanes 0 <-> 2 exchange components 2 / 0, lane 1 <- 3 component 1
+        double z = __shfl_xor_sync(0xffffffffu, odd ? s1 : (q == 0 ? s2 : s0), 2);
+        if (!own) return;
+        s = pick3(q, s0, s1, s2) + z;
     }
-    // across pairs: lanes 0 <-> 2 exchange components 2 / 0, lane 1 <- 3 component 1
-    double z = __shfl_xor_sync(0xffffffffu, odd ? s1 : (q == 0 ? s2 : s0), 2);
-    if (!own) return;
-    const double s = pick3(q, s0, s1, s2) + z;
     const int2 br = rec >= 0 ? p.bc_rec[rec * 3 + q] : make_int2(0, 0);
     const bool act = br.y == 0;
     bool changed = false;
