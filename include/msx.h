@@ -301,20 +301,24 @@ msx_status msx_set_device(int32_t device);
  * host application that owns all device memory through its own allocator,
  * code that must not trigger the device synchronisation cudaMalloc/cudaFree
  * can cause, or work enqueued while a stream is being captured into a graph).
- * It computes f_int(u) for one material in the reference's operation order,
- * bit-identical to msx_internal_force on an MSX_PREC_FP64_EXACT handle.
+ * It computes f_int(u) for one material (any of the four laws) in the
+ * reference's operation order, bit-identical to msx_internal_force on an
+ * MSX_PREC_FP64_EXACT handle.
  * Every array is DEVICE memory owned by the caller: X[3*num_nodes] (SoA),
- * conn[4*num_elems] (16-byte aligned), node_ptr[num_nodes+1] and
- * node_inc[4*num_elems] (for each node, e*4+corner of its incident elements in
- * increasing element order), u[3*num_nodes] in, fint[3*num_nodes] out.  Work
- * is enqueued on `stream` (a cudaStream_t, NULL for the default stream) and
- * is not waited for.  The corner forces go to a fixed scratch array inside
- * the library, so num_elems above MSX_NOALLOC_MAX_ELEMS is rejected with
- * MSX_ERR_ARG.  The first call on each device looks up that array's device
- * address (cudaGetSymbolAddress) with the device current: make that first
- * call before capturing a stream.  All calls share the one array, which keeps
- * the last call's contents; each call writes every entry it reads, but calls
- * whose work overlaps on the GPU race on it. */
+ * conn[4*num_elems], node_ptr[num_nodes+1] and node_inc[4*num_elems] (for
+ * each node, e*4+corner of its incident elements in increasing element order),
+ * u[3*num_nodes] in, fint[3*num_nodes] out.  conn must be 16-byte aligned,
+ * X, u and fint 8-byte aligned, node_ptr and node_inc 4-byte aligned; other
+ * pointers are rejected with MSX_ERR_ARG.  Work is enqueued on `stream` (a
+ * cudaStream_t, NULL for the default stream) and is not waited for.  The
+ * corner forces go to a fixed scratch array inside the library, so num_elems
+ * above MSX_NOALLOC_MAX_ELEMS is rejected with MSX_ERR_ARG.  Each call looks
+ * up that array's device address (cudaGetSymbolAddress) with the device
+ * current, so a device reset between calls is harmless; the first call on a
+ * device may load the library's device code, so make it before capturing a
+ * stream.  All calls share the one array, which keeps the last call's
+ * contents; each call writes every entry it reads, but calls whose work
+ * overlaps on the GPU race on it. */
 msx_status msx_internal_force_noalloc(const double *X, const int32_t *conn, int64_t num_nodes,
                                       int64_t num_elems, const int32_t *node_ptr,
                                       const int32_t *node_inc, const msx_material *material,

@@ -77,8 +77,47 @@ def test_double_word_mode_matches_reference(name):
                          ["cube4_le_ramp", "cube3_stvk_activation", "cube3_le_activation_chain"])
 def test_mixed_mode_error_bound(name):
     (u, v, a), (ur, vr, ar), steps, ref_steps = run_case(name, msx.MIXED)
-    assert abs(steps - ref_steps) <= 1
+    # the stable dt is the FP64 minimum (FP32 screen + FP64 recheck), so the
+    # mixed run takes the reference's steps
+    assert steps == ref_steps
     assert rel(u, ur) <= 1e-5, rel(u, ur)
+
+
+def cfl_dt_host(X, conn, u, Lref, c, sf):
+    """sf * min_e min(Lref_e, 2 r(X + u)_e) / c in FP64 on the host: the
+    inscribed-sphere diameter 2 |e1.(e2 x e3)| / (sum of face areas)
+    (geometry.cpp:264-301, solvers.cpp:296-320)."""
+    nn = X.shape[1]
+    x = X + u.reshape(3, nn)
+    p = [x[:, conn[:, k]].T for k in range(4)]
+    e1, e2, e3 = p[1] - p[0], p[2] - p[0], p[3] - p[0]
+    A, B, Cc = np.cross(e1, e2), np.cross(e1, e3), np.cross(e2, e3)
+    D = Cc + A - B
+    s = sum(np.sqrt((q * q).sum(1)) for q in (A, B, Cc, D))
+    dist = 2 * np.abs((e1 * Cc).sum(1)) / s
+    return sf * (np.minimum(dist, Lref) / c).min()
+
+
+@pytest.mark.parametrize("law", [msx.COMPRESSIBLE_NH, msx.STVK])
+def test_mixed_dt_is_the_fp64_cfl_of_its_state(law):
+    """Each mixed step's dt is sf times the FP64 CFL minimum over the mesh at
+    the mixed state (the FP32 screen only picks which elements to evaluate in
+    FP64): after 150 steps of a deforming 10^3 cube, the next dt equals the
+    host's FP64 evaluation to rounding (an FP32 CFL minimum would be ~1e-8 off)."""
+    X, conn = msx.mesh_cube(10, seed=3)
+    bcs = msx.cube_bcs(10, 0.5, msx.BC_VEL_RAMP, 20)
+    E, nu, rho = 1e6, 0.3, 1000.0
+    S = msx.Solver(X, conn, [(law, E, nu, rho)], bcs, 0.0, 1e30, 0.5, precision=msx.MIXED)
+    S.run(150)
+    u = S.state()[0]
+    _, _, Lref, _ = S.element_data()
+    dt = S.run(1).dt
+    S.close()
+    lam, mu = E * nu / ((1 + nu) * (1 - 2 * nu)), 0.5 * E / (1 + nu)
+    c = np.sqrt(E / rho) if law == msx.STVK else np.sqrt((lam + 2 * mu) / rho)
+    ref = cfl_dt_host(X, conn, u, Lref, c, 0.5)
+    assert np.abs(u).max() > 1e-3
+    assert abs(dt - ref) <= 1e-13 * ref, (dt, ref, dt / ref - 1)
 
 
 def test_graph_chunk_size_does_not_change_results():

@@ -6,17 +6,17 @@ cudaMalloc/cudaFree can trigger, or work enqueued during stream capture.
 Collected last (file name) so that a run stopping at the first failure has run
 every other test.  The test itself allocates the device buffers it passes in;
 the entry point keeps its corner forces in a fixed array inside the library.
-It checks the result against msx_internal_force on an FP64_EXACT handle, with
-the exact-mode tolerance of the other tests, on two calls in a row with
-different displacements (the second call finds the first call's scratch)."""
+It checks the result against msx_internal_force on an FP64_EXACT handle, bit
+for bit (both run the reference's operation order), on two calls in a row with
+different displacements (the second call finds the first call's scratch).  The
+argument checks (sizes, alignment) run before any CUDA call and are tested on
+the CPU as well."""
 import ctypes as C
 
 import numpy as np
 import pytest
 
 import msx
-
-pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope="module")
@@ -78,7 +78,8 @@ def csr(conn, nn):
     return np.cumsum(ptr).astype(np.int32), inc[order].astype(np.int32)
 
 
-@pytest.mark.parametrize("law", [msx.COMPRESSIBLE_NH, msx.NEO_HOOKEAN, msx.STVK])
+@pytest.mark.gpu
+@pytest.mark.parametrize("law", [msx.COMPRESSIBLE_NH, msx.NEO_HOOKEAN, msx.STVK, msx.LINEAR_ELASTIC])
 def test_noalloc_internal_force_matches_handle_twice(lib, law):
     X, conn = msx.mesh_cube(8, seed=21)          # 3072 elements
     nn, ne = X.shape[1], conn.shape[0]
@@ -100,8 +101,9 @@ def test_noalloc_internal_force_matches_handle_twice(lib, law):
             f = dev.get(dfint, 3 * nn)
             ref = S.internal_force(u)
             assert np.isfinite(ref).all()
-            rel = np.linalg.norm(f - ref) / np.linalg.norm(ref)
-            assert rel <= 1e-12, (call, rel)
+            # the same operation order on both paths: equal bits
+            assert np.array_equal(f.view(np.uint64), ref.view(np.uint64)), \
+                (call, np.abs(f - ref).max() / np.abs(ref).max())
     finally:
         dev.free()
         S.close()
@@ -113,3 +115,35 @@ def test_noalloc_rejects_sizes_beyond_scratch(lib):
     st = lib.msx_internal_force_noalloc(fake, fake, 10, 65537, fake, fake, C.byref(m), fake, fake, None)
     assert st == 1
     assert b"exceed the scratch maximum of 65536" in lib.msx_last_error()
+
+
+@pytest.mark.parametrize("arg,addr,msg", [
+    ("conn", 264, b"conn must be 16-byte aligned"),
+    ("X", 260, b"X, u and fint must be 8-byte aligned"),
+    ("u", 260, b"X, u and fint must be 8-byte aligned"),
+    ("fint", 252, b"X, u and fint must be 8-byte aligned"),
+    ("node_ptr", 258, b"node_ptr and node_inc must be 4-byte aligned"),
+    ("node_inc", 257, b"node_ptr and node_inc must be 4-byte aligned"),
+])
+def test_noalloc_rejects_misaligned_pointers(lib, arg, addr, msg):
+    """A caller's own allocator may hand out sub-allocations at any offset:
+    misaligned arrays come back as MSX_ERR_ARG before anything touches the
+    GPU (the fake addresses are never dereferenced)."""
+    m = msx.Material_(1, 0, 1e6, 0.3, 1000.0)
+    args = {k: C.c_void_p(256) for k in ("X", "conn", "node_ptr", "node_inc", "u", "fint")}
+    args[arg] = C.c_void_p(addr)
+    st = lib.msx_internal_force_noalloc(args["X"], args["conn"], 10, 8, args["node_ptr"], args["node_inc"],
+                                        C.byref(m), args["u"], args["fint"], None)
+    assert st == 1
+    assert msg in lib.msx_last_error()
+
+
+def test_noalloc_takes_every_law_and_rejects_bad_materials(lib):
+    """The law parameters come from the same routine as every other entry
+    point: an unknown law or an invalid constant is refused up front."""
+    fake = C.c_void_p(256)
+    for bad in (msx.Material_(4, 0, 1e6, 0.3, 1000.0), msx.Material_(1, 0, -1.0, 0.3, 1000.0),
+                msx.Material_(2, 0, 1e6, 0.5, 1000.0)):
+        st = lib.msx_internal_force_noalloc(fake, fake, 10, 8, fake, fake, C.byref(bad), fake, fake, None)
+        assert st == 1
+        assert b"material needs law 0..3" in lib.msx_last_error()

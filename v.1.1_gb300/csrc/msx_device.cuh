@@ -1109,7 +1109,9 @@ static __global__ void __launch_bounds__(kElemBlock) elem_force_kernel_fp64(Prob
 // ---------------------------------------------------------------------------
 // Mixed precision: FP32 kinematics, stress and B^T P written in terms of the
 // displacement gradient H = F - I (no 1 - 1 cancellation in FP32); J - 1 and
-// ln J in FP64; FP32 corner forces; FP32 CFL length with the dt min in FP64.
+// ln J in FP32 with an exactly summed trace; FP32 corner forces; an FP32
+// screen of the CFL values whose near-minimum elements are recomputed in FP64
+// (cfl_dw), so the stable dt is the FP64 minimum.
 // cof(I + H) = I + D with D = (tr H + I2) I - (1 + tr H) H^T + (H^2)^T.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H, float Jm1, float lnJ,
@@ -1272,9 +1274,20 @@ __device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, 
                 e2[i] = C[3 + i] * idet + du[3 + i];
                 e3[i] = C[6 + i] * idet + du[6 + i];
             }
+            // FP32 screen of the CFL value, as cfl_screen: slivers (6V below
+            // 0.063 |e1||e2||e3|, where the FP32 edges lose accuracy) and
+            // reference slivers (a negative Lref32, set at set-up) come back
+            // negative, so the caller recomputes them in FP64
+            const float C0 = e2[1] * e3[2] - e2[2] * e3[1], C1 = e2[2] * e3[0] - e2[0] * e3[2],
+                        C2 = e2[0] * e3[1] - e2[1] * e3[0];
+            const float v6 = fabsf(e1[0] * C0 + e1[1] * C1 + e1[2] * C2);
+            const float l1 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+            const float l2 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+            const float l3 = e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2];
             float dist = char_length_edges<float>(e1, e2, e3);
             float Lr = __ldg(p.Lref32 + e);
             vmin = ((dist < Lr) ? dist : Lr) * m.inv_c_f;
+            if (!(v6 * v6 >= 4e-3f * l1 * l2 * l3) || !(vmin > 0.0f)) vmin = -1.0f;
             if (e == 0 && !isfinite(p.uhl[1].x)) atomicOr(p.flags + (parity ^ 1), 1);
         }
     }
@@ -1777,7 +1790,7 @@ __global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *
 }
 
 // The elements of one tile for the tiled element kernel: each thread's
-// elements in turn, FP32 CFL screen values into sdt (FP64 and double-word);
+// elements in turn, FP32 CFL screen values into sdt;
 // returns the thread's FP32 minimum.  The mixed and double-word bodies take the
 // element's connectivity loaded one element ahead, so their node gathers wait
 // for one memory latency instead of two (connectivity, then the nodes).  ACT:
@@ -1798,26 +1811,33 @@ __device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl,
         float d = MODE == MODE_MIXED ? elem_body_mixed<false, ACT>(p, e, parity, cn, t)
                                      : (MODE == MODE_DW ? elem_body_dw<false, ACT>(p, e, parity, cn, t)
                                                         : elem_body_fp64<false, ACT>(p, e, parity, t));
-        if (MODE != MODE_MIXED) sdt[e - tl.begin] = d;
+        sdt[e - tl.begin] = d;
         if (d >= 0.0f) v32 = fminf(v32, d);
     }
     return v32;
 }
 
-// Element kernel over tiles.  FP64 and double-word: every element's FP32 CFL
-// screen value is kept in shared memory; after the tile's FP32 minimum is
-// known, elements within 2^-8 of it (and slivers) recompute the exact FP64
-// value, whose minimum goes to the solve's CFL slot.  Mixed: the FP32 minimum
-// itself.  ACT: the instantiation with element birth (single solves whose block
-// has it on); the other one carries no trace of it.
+// Element kernel over tiles.  Every element's FP32 CFL screen value is kept in
+// shared memory; after the tile's FP32 minimum is known, elements within 2^-8
+// of it (and slivers) recompute the exact FP64 value, whose minimum goes to
+// the solve's CFL slot.  The screen's error stays far below 2^-9 outside
+// slivers, so that set always holds the tile's exact minimum.  FP64 and
+// double-word list the candidates and recompute them by consecutive threads;
+// mixed tiles have a candidate or two, which each thread recomputes among its
+// own elements (no list, no extra barrier), and keep their screen values in
+// dynamic shared memory of 4 bytes per tile element.  ACT: the instantiation
+// with element birth (single solves whose block has it on); the other one
+// carries no trace of it.
 template <int MODE, bool ACT = false>
 __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE == MODE_DW ? 3 : 2)) pool_elem_kernel(const Problem *__restrict__ descs,
                                                                  const Tile *__restrict__ tiles,
                                                                  int *__restrict__ sched, int parity)
 {
-    __shared__ float sdt[MODE == MODE_MIXED ? 1 : kMaxTileElems];
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    __shared__ float sdt_static[MODE == MODE_MIXED ? 1 : kMaxTileElems];
     __shared__ unsigned short scand[MODE == MODE_MIXED ? 1 : kMaxTileElems];
     __shared__ int s_tile, s_ncand;
+    float *sdt = MODE == MODE_MIXED ? reinterpret_cast<float *>(dyn_smem) : sdt_static;
     TileQueue q{sched, sched[0]};
     if (threadIdx.x == 0) s_tile = q.claim();
     __syncthreads();
@@ -1832,8 +1852,15 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
             const float v32 = tile_elements<MODE, ACT>(p, tl, parity, sdt);
             float bmin = block_min_bcast(v32);   // also orders the sdt writes before the reads below
             if (MODE == MODE_MIXED) {
-                if (threadIdx.x == 0 && bmin < INFINITY)
-                    atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong((double)bmin));
+                // a thread reads back only the entries it wrote itself
+                const float thr = bmin * (1.0f + 1.0f / 256.0f);
+                double v = INFINITY;
+                for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
+                    const float d = sdt[e - tl.begin];
+                    if (d < 0.0f || d <= thr) v = fmin(v, cfl_dw(p, e));
+                }
+                if (v >= 0.0 && v < INFINITY)
+                    atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
             } else {
                 // the tile's candidates are listed first and then recomputed by
                 // consecutive threads, so a few candidates take one warp, not several
@@ -1908,7 +1935,26 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
     if (p.wJ32lo) const_cast<float *>(p.wJ32lo)[e] = (float)(w - (double)(float)w);
     double L = char_length_ref(pts);
     Lref[e] = L;
-    Lref32[e] = (float)L;
+    // A reference sliver (6V below 0.063 |e1||e2||e3|) gets a negative FP32
+    // length: the FP32 CFL screens then always recompute it in FP64 (the mixed
+    // screen rebuilds the reference edges from G in FP32, which loses accuracy
+    // on such a tet).  Lref itself is unchanged.
+    {
+        double e1[3], e2[3], e3[3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            e1[i] = pts[3 + i] - pts[i];
+            e2[i] = pts[6 + i] - pts[i];
+            e3[i] = pts[9 + i] - pts[i];
+        }
+        const double v6 = e1[0] * (e2[1] * e3[2] - e2[2] * e3[1]) + e1[1] * (e2[2] * e3[0] - e2[0] * e3[2]) +
+                          e1[2] * (e2[0] * e3[1] - e2[1] * e3[0]);
+        const double l1 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+        const double l2 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+        const double l3 = e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2];
+        const bool sliver = !(v6 * v6 >= 4e-3 * l1 * l2 * l3);
+        Lref32[e] = sliver ? -(float)L : (float)L;
+    }
 #pragma unroll
     for (int a = 1; a < 4; a++)
 #pragma unroll

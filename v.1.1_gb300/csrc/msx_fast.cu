@@ -35,11 +35,12 @@ void launch_tiled_node(const Problem *descs, const Tile *ntiles, int *counts, in
 }
 
 void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, int mode, int parity, int grid,
-                       int threads, cudaStream_t s, bool act)
+                       int threads, int tile_elems, cudaStream_t s, bool act)
 {
+    const size_t smem = sizeof(float) * (size_t)tile_elems;   // mixed: FP32 CFL screen values of a tile
     if (mode == MODE_MIXED)
-        act ? pool_elem_kernel<MODE_MIXED, true><<<grid, threads, 0, s>>>(descs, etiles, counts, parity)
-            : pool_elem_kernel<MODE_MIXED><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
+        act ? pool_elem_kernel<MODE_MIXED, true><<<grid, threads, smem, s>>>(descs, etiles, counts, parity)
+            : pool_elem_kernel<MODE_MIXED><<<grid, threads, smem, s>>>(descs, etiles, counts, parity);
     else if (mode == MODE_DW)
         act ? pool_elem_kernel<MODE_DW, true><<<grid, threads, 0, s>>>(descs, etiles, counts, parity)
             : pool_elem_kernel<MODE_DW><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
@@ -93,7 +94,8 @@ int tiled_ctas_per_sm(int mode, int threads, bool node)
     int a = 0;
     if (mode == MODE_MIXED)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, node ? (const void *)pool_node_kernel<MODE_MIXED>
-                                                               : (const void *)pool_elem_kernel<MODE_MIXED>, threads, 0);
+                                                               : (const void *)pool_elem_kernel<MODE_MIXED>, threads,
+                                                      node ? 0 : sizeof(float) * kMaxTileElems);
     else if (mode == MODE_DW)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, node ? (const void *)pool_node_kernel<MODE_DW>
                                                                : (const void *)pool_elem_kernel<MODE_DW>, threads, 0);

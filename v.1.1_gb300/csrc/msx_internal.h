@@ -154,9 +154,11 @@ constexpr int kMaxTileElems = 4096; // upper bound on the elements of one tile
 constexpr int kTileSched = 6;
 void launch_tiled_node(const Problem *descs, const Tile *ntiles, int *counts, int mode, int parity, int grid,
                        int threads, cudaStream_t s);
-// act: the instantiation with element birth (Problem::act_t set)
+// tile_elems: the largest tile of etiles (the mixed kernel keeps 4 bytes of
+// shared memory per tile element); act: the instantiation with element birth
+// (Problem::act_t set)
 void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, int mode, int parity, int grid,
-                       int threads, cudaStream_t s, bool act = false);
+                       int threads, int tile_elems, cudaStream_t s, bool act = false);
 // CTAs of the tiled element kernel (node kernel when `node` is true) that fit on one SM
 int tiled_ctas_per_sm(int mode, int threads, bool node = false);
 // Mixed-mode state conversions: u, v, a (FP64) -> uhl, vhl, ahl, and back

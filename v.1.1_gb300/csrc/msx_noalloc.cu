@@ -7,7 +7,6 @@
 // live in g_corner_scratch below, a fixed array in the library's own device
 // memory: every GPU that loads the library holds its 6 MiB until the process
 // exits, and the entry point never calls cudaMalloc or cudaFree.
-#include <mutex>
 #include <string>
 
 #include "../../include/msx.h"
@@ -23,10 +22,6 @@ constexpr long long kNoAllocMaxElems = 65536;   // MSX_NOALLOC_MAX_ELEMS in incl
 // is only a stand-in for the device array: its device address comes from
 // cudaGetSymbolAddress (set-up below), never from taking its address here.
 static __device__ __align__(256) double g_corner_scratch[12 * kNoAllocMaxElems];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-double *g_scratch_ptr[kMaxDevices] = {};
 
 // Element pass: the reference's set-up of dphi and wJ from X
 // (classLinearTetrahedra.cpp:171-268, classGPs.cpp:27), F (constitutiveManager.cpp:
@@ -123,25 +118,24 @@ msx_status nfail(msx_status st, const std::string &m)
     return st;
 }
 
-// Device address of the scratch array for the current device, looked up once
-// per device with that device current.
+// Device address of the scratch array on the current device.  Looked up on
+// every call with that device current (the lookup allocates nothing): an
+// address kept from an earlier call would go stale if the application reset
+// the device, which reloads the library's module at a new address.
 msx_status scratch_for_current_device(double **out)
 {
     int dev = -1;
     cudaError_t err = cudaGetDevice(&dev);
     if (err != cudaSuccess) return nfail(MSX_ERR_NO_DEVICE, std::string("cudaGetDevice: ") + cudaGetErrorString(err));
-    if (dev < 0 || dev >= kMaxDevices) return nfail(MSX_ERR_NO_DEVICE, "device ordinal beyond 64");
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-        void *ptr = nullptr;
-        err = cudaGetSymbolAddress(&ptr, g_corner_scratch);
-        if (err != cudaSuccess || !ptr)
-            return nfail(MSX_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(err));
-        g_scratch_ptr[dev] = (double *)ptr;
-    }
-    *out = g_scratch_ptr[dev];
+    void *ptr = nullptr;
+    err = cudaGetSymbolAddress(&ptr, g_corner_scratch);
+    if (err != cudaSuccess || !ptr)
+        return nfail(MSX_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(err));
+    *out = (double *)ptr;
     return MSX_OK;
 }
+
+bool aligned(const void *p, uintptr_t a) { return (uintptr_t)p % a == 0; }
 
 }  // namespace
 
@@ -157,21 +151,15 @@ extern "C" msx_status msx_internal_force_noalloc(const double *X, const int32_t 
         return nfail(MSX_ERR_ARG, "msx_internal_force_noalloc: " + std::to_string(num_elems) +
                                       " elements exceed the scratch maximum of " + std::to_string(kNoAllocMaxElems));
     if (num_nodes >= (1LL << 31)) return nfail(MSX_ERR_ARG, "msx_internal_force_noalloc: too many nodes");
-    if ((uintptr_t)conn % 16 != 0) return nfail(MSX_ERR_ARG, "msx_internal_force_noalloc: conn must be 16-byte aligned");
-    const msx_material &mt = *material;
-    if (mt.law < 0 || mt.law > 2 || !(mt.young > 0) || !(mt.rho > 0) || !(mt.nu > -1.0) || !(mt.nu < 0.5))
-        return nfail(MSX_ERR_ARG, "msx_internal_force_noalloc: bad material");
+    if (!aligned(conn, 16)) return nfail(MSX_ERR_ARG, "msx_internal_force_noalloc: conn must be 16-byte aligned");
+    if (!aligned(X, 8) || !aligned(u, 8) || !aligned(fint, 8))
+        return nfail(MSX_ERR_ARG, "msx_internal_force_noalloc: X, u and fint must be 8-byte aligned");
+    if (!aligned(node_ptr, 4) || !aligned(node_inc, 4))
+        return nfail(MSX_ERR_ARG, "msx_internal_force_noalloc: node_ptr and node_inc must be 4-byte aligned");
+    // the same law parameters as every other entry point (all four laws)
     MatParams m{};
-    const double E = mt.young, nu = mt.nu;
-    m.law = mt.law;
-    m.young = E;
-    m.nu = nu;
-    m.rho = mt.rho;
-    m.lambda = (E * nu) / ((1. + nu) * (1. - 2. * nu));
-    m.mu = 0.5 * E / (1. + nu);
-    m.K1 = E / (3 * (1 - 2 * nu));
-    m.mu2 = E / (1. + nu);
-    m.lam_stvk = E * nu / ((1. + nu) * (1. - (2 * nu)));
+    if (!material_params(*material, m))
+        return nfail(MSX_ERR_ARG, "msx_internal_force_noalloc: material needs law 0..3, E > 0, rho > 0, -1 < nu < 0.5");
     double *scratch = nullptr;
     msx_status st = scratch_for_current_device(&scratch);
     if (st != MSX_OK) return st;

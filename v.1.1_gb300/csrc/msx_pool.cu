@@ -232,7 +232,8 @@ static msx_status build_pool_graph(msx_pool *p, int steps)
     for (int i = 0; i < steps; i++) {
         int parity = (i & 1) ? 0 : 1;
         launch_tiled_node(p->d_descs, p->d_ntiles, p->d_counts, mode, parity, node_grid, threads, p->stream);
-        launch_tiled_elem(p->d_descs, p->d_etiles, p->d_counts, mode, parity, grid, threads, p->stream);
+        launch_tiled_elem(p->d_descs, p->d_etiles, p->d_counts, mode, parity, grid, threads, p->sched.tile_elems,
+                          p->stream);
     }
     cudaError_t err = cudaStreamEndCapture(p->stream, &g);
     if (err != cudaSuccess) return pfail(MSX_ERR_CUDA, std::string("pool graph capture: ") + cudaGetErrorString(err));
@@ -730,7 +731,9 @@ extern "C" msx_status msx_pool_serve(msx_pool *p, int32_t enabled)
 {
     if (!p) return pfail(MSX_ERR_ARG, "NULL pool");
     if (enabled) {
-        std::lock_guard<std::mutex> lk(p->mu);
+        std::unique_lock<std::mutex> lk(p->mu);
+        // a stop in progress on another thread completes first
+        p->cv_done.wait(lk, [p] { return !(p->serving && p->serve_stop); });
         if (p->serving) return MSX_OK;
         msx_status st = finish_inflight(p);   // the serving thread starts with no replay in flight
         if (st != MSX_OK) return st;
@@ -745,13 +748,20 @@ extern "C" msx_status msx_pool_serve(msx_pool *p, int32_t enabled)
         p->serving = true;
         return MSX_OK;
     }
+    std::thread server;
     {
-        std::lock_guard<std::mutex> lk(p->mu);
+        std::unique_lock<std::mutex> lk(p->mu);
         if (!p->serving) return MSX_OK;
+        if (p->serve_stop) {
+            // another thread is stopping it: wait until that thread has joined it
+            p->cv_done.wait(lk, [p] { return !p->serving; });
+            return p->serve_status == MSX_OK ? MSX_OK : serve_failure(p);
+        }
         p->serve_stop = true;
+        server = std::move(p->server);   // the one caller that joins the thread
     }
     p->cv_work.notify_all();
-    p->server.join();   // its last replay was collected before it saw the stop
+    server.join();   // its last replay was collected before it saw the stop
     std::lock_guard<std::mutex> lk(p->mu);
     p->serving = false;
     p->cv_done.notify_all();

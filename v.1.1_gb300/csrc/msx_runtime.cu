@@ -307,7 +307,7 @@ static void launch_step(msx_handle *h, int parity)
     if (h->nfaces) launch_face_loads(h->P, parity, pair_state(h), h->stream);
     if (h->tiled)
         launch_tiled_elem(h->d_desc.p, h->d_etiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
-                          h->stream, h->P.act_t != nullptr);
+                          h->tile_elems, h->stream, h->P.act_t != nullptr);
     else
         h->elem(h->P, parity, h->stream);
 }
@@ -1198,7 +1198,7 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
         cudaEventRecord(ev[3 * i + 1], h->stream);
         if (h->tiled)
             launch_tiled_elem(h->d_desc.p, h->d_etiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
-                              h->stream, h->P.act_t != nullptr);
+                              h->tile_elems, h->stream, h->P.act_t != nullptr);
         else
             h->elem(h->P, parity, h->stream);
         cudaEventRecord(ev[3 * i + 2], h->stream);
