@@ -231,49 +231,100 @@ def reference_arm(args):
             "e2e": {"value": value, "unit": "element-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def accuracy_sample(ns, nus, k=8, seed=0):
+    """Indices of the solves whose results are checked against FP64: the
+    largest and the smallest cube, the highest and the lowest nu, then seeded
+    picks up to k."""
+    pick = [int(np.argmax(ns)), int(np.argmin(ns)), int(np.argmax(nus)), int(np.argmin(nus))]
+    for i in np.random.default_rng(seed).permutation(len(ns)):
+        if len(set(pick)) >= k:
+            break
+        pick.append(int(i))
+    return sorted(set(pick))
+
+
+def fp64_alone(X, conn, material, bcs, steps):
+    """u after `steps` steps of one solve run by itself in the plain FP64 path."""
+    import msx
+    S = msx.Solver(X, conn, [material], bcs, 0.0, 1e30, 0.5, max_steps=steps, precision=msx.FP64)
+    rep = S.run()
+    u = S.state()[0]
+    S.close()
+    assert rep.steps == steps and rep.status == 0, rep
+    return u
+
+
+def accuracy_summary(cases, bar):
+    e = [c["rel_l2_u_vs_fp64"] for c in cases]
+    return {"solves_checked": len(e), "max_rel_l2_u_vs_fp64": max(e), "median_rel_l2_u_vs_fp64": float(np.median(e)),
+            "bar": bar, "within_bar": bool(max(e) <= bar),
+            "how": "each sampled solve re-run alone in the plain FP64 path for the same steps; relative L2 of u",
+            "cases": cases}
+
+
 def batched_variant(seed=7, count=256, steps=1000, warmup=3, precision=None, cache=None):
     """256 independent solves (cube side n log-uniform in [8, 48], E log-uniform
     in [1e5, 1e7], nu uniform in [0.25, 0.45], top velocity uniform in
     [0.01, 0.2]) stepped together by the pool, 1000 steps each: mixed (FP32
     elements, double-word nodes) by default, or another pool precision.  The
     timed region starts after admission, autotuning and warm-up and ends when
-    the last solve finishes."""
+    the last solve's result is in host memory.  Afterwards a sample of the
+    solves (largest and smallest n, extreme nu, seeded picks) runs alone in
+    FP64 and the fetched displacements are compared with it."""
     import msx
+    precision = msx.MIXED if precision is None else precision
     rng = np.random.default_rng(seed)
     ns = np.floor(np.exp(rng.uniform(np.log(8), np.log(49), count))).astype(int)
     Es = np.exp(rng.uniform(np.log(1e5), np.log(1e7), count))
     nus = rng.uniform(0.25, 0.45, count)
     vs = rng.uniform(0.01, 0.2, count)
+    sample = accuracy_sample(ns, nus)
+
+    def case(k):
+        X, conn = msx.mesh_cube(int(ns[k]), SEED + k, 0.1)
+        return X, conn, (1, float(Es[k]), float(nus[k]), 1000.0), \
+            msx.cube_bcs(int(ns[k]), float(vs[k]), msx.BC_VEL_RAMP, RAMP_STEPS)
+
     cache = cache or TUNE_CACHE
     if os.path.exists(cache):
         os.remove(cache)
-    P = msx.Pool(max_slots=count, precision=msx.MIXED if precision is None else precision, steps_per_launch=32,
-                 tune_cache=cache)
-    total_elems = 0
+    P = msx.Pool(max_slots=count, precision=precision, steps_per_launch=32, tune_cache=cache)
+    total_elems, owner = 0, {}
     t0 = time.perf_counter()
     for k in range(count):
-        X, conn = msx.mesh_cube(int(ns[k]), SEED + k, 0.1)
-        t = P.submit(X, conn, (1, float(Es[k]), float(nus[k]), 1000.0),
-                     msx.cube_bcs(int(ns[k]), float(vs[k]), msx.BC_VEL_RAMP, RAMP_STEPS), steps)
+        X, conn, mat, bcs = case(k)
+        t = P.submit(X, conn, mat, bcs, steps)
         assert t is not None, "batched workload does not fit"
+        owner[t] = k
         total_elems += conn.shape[0]
     admit_s = time.perf_counter() - t0
     P.step(warmup)   # autotunes the schedule on the resident work, then warms up
     before = P.stats()
     t1 = time.perf_counter()
-    res = []
+    res, kept = [], {}
     while len(res) < count:
         P.step(steps)
         for r in P.poll():   # every result is read back to the host inside the timed region
-            P.fetch(r["ticket"])
+            u = P.fetch(r["ticket"])[0]
+            if owner[r["ticket"]] in sample:
+                kept[owner[r["ticket"]]] = u
             res.append(r)
     wall = time.perf_counter() - t1
     after = P.stats()
     P.close()
     timed = after["element_steps"] - before["element_steps"]
+    cases = []
+    for k in sample:
+        X, conn, mat, bcs = case(k)
+        ref = fp64_alone(X, conn, mat, bcs, steps)
+        cases.append({"solve": k, "n": int(ns[k]), "num_elems": int(conn.shape[0]), "E": float(Es[k]),
+                      "nu": float(nus[k]), "v_top": float(vs[k]),
+                      "rel_l2_u_vs_fp64": float(np.linalg.norm(kept[k] - ref) / max(np.linalg.norm(ref), 1e-300))})
+    bar = 1e-10 if precision == msx.DOUBLE_WORD else 1e-5
     return {"value": timed / wall, "unit": "element-steps/s", "solves": count, "total_elems": int(total_elems),
             "steps_per_solve": steps, "wall_s": wall, "admit_s": admit_s,
             "all_ok": all(r["status"] == 0 and r["steps"] == steps for r in res),
+            "accuracy": accuracy_summary(cases, bar),
             "schedule": {"threads": before["threads"], "tile_elems": before["tile_elems"],
                          "ctas_per_sm": before["ctas_per_sm"], "steps_per_graph": before["steps_per_launch"]}}
 
@@ -281,15 +332,12 @@ def batched_variant(seed=7, count=256, steps=1000, warmup=3, precision=None, cac
 TUNE_CACHE = os.path.join(os.environ.get("TMPDIR", "/tmp"), "msx_pool_schedule.txt")
 
 
-def serving_variant(lam, count=64, seed=11, max_slots=64):
-    """Request stream with Poisson arrivals at rate `lam` per second; each
-    request is a seeded cube of side n log-uniform in [8, 64], compressible
-    neo-Hookean with E log-uniform in [1e5, 1e7] and nu uniform in
-    [0.25, 0.45], and a step count uniform in [200, 2000].  Requests are
-    admitted into the pool as slots and HBM free up (continuous batching) while
-    the pool's serving thread steps the resident solves; latency runs from a
-    request's arrival to its result in host memory."""
-    import msx
+def serving_requests(lam, count, seed=11):
+    """The seeded request stream of the serving configuration: Poisson
+    arrivals at rate lam per second; cube side n log-uniform in [8, 64];
+    compressible neo-Hookean with E log-uniform in [1e5, 1e7] and nu uniform
+    in [0.25, 0.45]; top velocity uniform in [0.01, 0.2]; a step count uniform
+    in [200, 2000]."""
     rng = np.random.default_rng(seed + int(lam))
     arrivals = np.cumsum(rng.exponential(1.0 / lam, count))
     ns = np.floor(np.exp(rng.uniform(np.log(8), np.log(65), count))).astype(int)
@@ -297,7 +345,25 @@ def serving_variant(lam, count=64, seed=11, max_slots=64):
     Es = np.exp(rng.uniform(np.log(1e5), np.log(1e7), count))
     nus = rng.uniform(0.25, 0.45, count)
     vs = rng.uniform(0.01, 0.2, count)
+    return arrivals, ns, steps, Es, nus, vs
+
+
+def serving_variant(lam, count=64, seed=11, max_slots=64, capacity=None):
+    """Requests of serving_requests() arriving in real time are admitted into
+    the pool as slots and HBM free up (continuous batching) while the pool's
+    serving thread steps the resident solves.  Latency runs from a request's
+    arrival to its result in host memory and is split into the wait before
+    admission (the client building the request, then waiting for a slot) and
+    the time in the pool (admission to completion, sharing the GPU).  The
+    offered load is the requests' element-steps over their arrival span; with
+    `capacity` (the batched rate of the same kernels) it is also given as a
+    fraction of it, and a rate above it is marked saturated: its latencies
+    then measure how fast the backlog drains.  A sample of the requests
+    (largest n, extreme nu, seeded picks) is re-run alone in FP64."""
+    import msx
+    arrivals, ns, steps, Es, nus, vs = serving_requests(lam, count, seed)
     work = sum(6 * int(n) ** 3 * int(st) for n, st in zip(ns, steps))
+    sample = accuracy_sample(ns, nus, seed=int(lam))
 
     def request(k):
         X, conn = msx.mesh_cube(int(ns[k]), SEED + 1000 + k, 0.1)
@@ -309,8 +375,8 @@ def serving_variant(lam, count=64, seed=11, max_slots=64):
     P = msx.Pool(max_slots=max_slots, precision=msx.MIXED, steps_per_launch=16, tune_cache=TUNE_CACHE)
     P.serve(True)
     start = time.perf_counter()
-    nxt, owner, lat, ready = 0, {}, {}, None
-    while len(lat) < count:
+    nxt, owner, wait, inpool, kept, ready = 0, {}, {}, {}, {}, None
+    while len(inpool) < count:
         if ready is None and nxt < count and arrivals[nxt] <= time.perf_counter() - start:
             ready = (nxt, request(nxt))
             nxt += 1
@@ -318,33 +384,49 @@ def serving_variant(lam, count=64, seed=11, max_slots=64):
         if ready is not None:
             t = P.submit(*ready[1])
             if t is not None:
-                owner[t] = (ready[0], time.perf_counter() - start)
+                k = ready[0]
+                owner[t] = k
+                wait[k] = time.perf_counter() - start - arrivals[k]
                 ready, admitted = None, True
         for r in P.poll():
-            # finished = admitted + the pool's own submit-to-completion time
-            k, at = owner.pop(r["ticket"])
-            lat[k] = at + 1e-3 * r["latency_ms"] - arrivals[k]
-            P.fetch(r["ticket"])
+            k = owner.pop(r["ticket"])
+            inpool[k] = 1e-3 * r["latency_ms"]   # the pool's own admission-to-completion time
+            u = P.fetch(r["ticket"])[0]
+            if k in sample:
+                kept[k] = u
         if not admitted:
-            wait = 0.001 if ready is not None or nxt >= count else arrivals[nxt] - (time.perf_counter() - start)
-            time.sleep(max(0.0, min(0.001, wait)))
+            w = 0.001 if ready is not None or nxt >= count else arrivals[nxt] - (time.perf_counter() - start)
+            time.sleep(max(0.0, min(0.001, w)))
     wall = time.perf_counter() - start
     P.close()
-    L = np.array([lat[k] for k in range(count)]) * 1e3
-    return {"lambda_per_s": lam, "requests": count, "value": work / wall, "unit": "element-steps/s",
-            "p50_ms": float(np.percentile(L, 50)), "p99_ms": float(np.percentile(L, 99)), "wall_s": wall}
+    W = np.array([wait[k] for k in range(count)]) * 1e3
+    G = np.array([inpool[k] for k in range(count)]) * 1e3
+    L = W + G
+    offered = work / arrivals[-1]
+    out = {"lambda_per_s": lam, "requests": count, "value": work / wall, "unit": "element-steps/s",
+           "p50_ms": float(np.percentile(L, 50)), "p99_ms": float(np.percentile(L, 99)), "wall_s": wall,
+           "arrival_span_s": float(arrivals[-1]), "offered_element_steps_per_s": offered,
+           "wait_p50_ms": float(np.percentile(W, 50)), "wait_p99_ms": float(np.percentile(W, 99)),
+           "in_pool_p50_ms": float(np.percentile(G, 50)), "in_pool_p99_ms": float(np.percentile(G, 99))}
+    if capacity:
+        out.update({"capacity_element_steps_per_s": capacity, "offered_fraction_of_capacity": offered / capacity,
+                    "utilisation": (work / wall) / capacity, "saturated": bool(offered > capacity),
+                    "capacity_note": "capacity = the batched mixed rate of the same kernels (variants.batched)"})
+    cases = []
+    for k in sample:
+        X, conn, mat, bcs, st = request(k)
+        ref = fp64_alone(X, conn, mat, bcs, st)
+        cases.append({"request": k, "n": int(ns[k]), "num_elems": int(conn.shape[0]), "steps": st,
+                      "nu": float(nus[k]), "E": float(Es[k]),
+                      "rel_l2_u_vs_fp64": float(np.linalg.norm(kept[k] - ref) / max(np.linalg.norm(ref), 1e-300))})
+    out["accuracy"] = accuracy_summary(cases, 1e-5)
+    return out
 
 
 def serving_sequential_fp64(lam, count=64, seed=11):
     """The same request stream served one solve at a time by the plain FP64 path."""
     import msx
-    rng = np.random.default_rng(seed + int(lam))
-    arrivals = np.cumsum(rng.exponential(1.0 / lam, count))
-    ns = np.floor(np.exp(rng.uniform(np.log(8), np.log(65), count))).astype(int)
-    steps = rng.integers(200, 2001, count)
-    Es = np.exp(rng.uniform(np.log(1e5), np.log(1e7), count))
-    nus = rng.uniform(0.25, 0.45, count)
-    vs = rng.uniform(0.01, 0.2, count)
+    arrivals, ns, steps, Es, nus, vs = serving_requests(lam, count, seed)
     work = sum(6 * int(n) ** 3 * int(st) for n, st in zip(ns, steps))
     start = time.perf_counter()
     lat = []
@@ -364,6 +446,52 @@ def serving_sequential_fp64(lam, count=64, seed=11):
     L = np.array(lat) * 1e3
     return {"lambda_per_s": lam, "requests": count, "value": work / wall, "unit": "element-steps/s",
             "p50_ms": float(np.percentile(L, 50)), "p99_ms": float(np.percentile(L, 99)), "wall_s": wall}
+
+
+def precision_sweep(cube=N_CUBE, steps=5000, every=100):
+    """Precision variant: the 6M-tet cube with St-Venant-Kirchhoff and
+    compressible neo-Hookean, nu in {0.3, 0.45, 0.49}, 5000 steps, run side by
+    side in the plain FP64 path and the mixed path (FP32 element kinematics,
+    stress and B^T P; double-word nodal state; FP64 stable dt).  Every `every`
+    steps: the relative L2 displacement error of the mixed run against the FP64
+    run, and the largest von Mises difference over the largest von Mises
+    stress.  The FP64 path stands in for the oracle here (it equals the oracle
+    to ~1e-15 on this mesh after 2000 steps, tests/test_gpu_large.py; the CPU
+    oracle needs ~0.1 s per step at this size)."""
+    import msx
+    X, conn = msx.mesh_cube(cube, SEED, 0.1)
+    bcs = msx.cube_bcs(cube, V_TOP, msx.BC_VEL_RAMP, RAMP_STEPS)
+    runs = []
+    t0 = time.perf_counter()
+    for law, lname in ((msx.STVK, "St-Venant-Kirchhoff"), (msx.COMPRESSIBLE_NH, "3D-Compressible-Neo-Hookean")):
+        for nu in (0.3, 0.45, 0.49):
+            mat = (law, 1e6, nu, 1000.0)
+            A = msx.Solver(X, conn, [mat], bcs, 0.0, 1e30, 0.5, max_steps=steps, precision=msx.FP64)
+            B = msx.Solver(X, conn, [mat], bcs, 0.0, 1e30, 0.5, max_steps=steps, precision=msx.MIXED)
+            eu, ev, done, same_t = [], [], 0, True
+            while done < steps:
+                k = min(every, steps - done)
+                ra, rb = A.run(k), B.run(k)
+                assert ra.steps == k and rb.steps == k and ra.status == 0 and rb.status == 0, (ra, rb)
+                done += k
+                same_t &= abs(ra.t - rb.t) <= 1e-9 * abs(ra.t)
+                ua, ub = A.state()[0], B.state()[0]
+                eu.append(float(np.linalg.norm(ub - ua) / max(np.linalg.norm(ua), 1e-300)))
+                va, vb = A.von_mises(), B.von_mises()
+                ev.append(float(np.abs(vb - va).max() / max(np.abs(va).max(), 1e-300)))
+            A.close()
+            B.close()
+            runs.append({"law": lname, "nu": nu, "max_rel_l2_u": max(eu), "final_rel_l2_u": eu[-1],
+                         "max_rel_vms": max(ev), "final_rel_vms": ev[-1], "times_agree_1e-9": bool(same_t),
+                         "rel_l2_u_every": [float("%.3g" % x) for x in eu],
+                         "rel_vms_every": [float("%.3g" % x) for x in ev]})
+    return {"num_elems": int(conn.shape[0]), "steps": steps, "every": every, "bar": 1e-5,
+            "worst_rel_l2_u": max(r["max_rel_l2_u"] for r in runs),
+            "worst_rel_vms": max(r["max_rel_vms"] for r in runs),
+            "within_bar": bool(max(max(r["max_rel_l2_u"], r["max_rel_vms"]) for r in runs) <= 1e-5),
+            "wall_s": time.perf_counter() - t0,
+            "vms_metric": "max over elements |vm_mixed - vm_fp64| / max over elements |vm_fp64|",
+            "runs": runs}
 
 
 def dist_env():
@@ -399,6 +527,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-pool", action="store_true", help="skip the batched and serving variants")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the precision sweep (6 x 5000 steps)")
+    ap.add_argument("--sweep-steps", type=int, default=5000)
     ap.add_argument("--cube", type=int, default=N_CUBE, help="hexes per cube edge (profiling runs only)")
     ap.add_argument("--only", choices=["fp64", "mixed", "fp64_exact", "dword"], default=None,
                     help="time a single variant (profiling runs only)")
@@ -446,8 +576,14 @@ def main():
     if not args.no_pool and args.only is None and args.cube == N_CUBE:
         variants["batched"] = batched_variant()
         variants["batched_double_word"] = batched_variant(precision=msx.DOUBLE_WORD, cache=TUNE_CACHE + ".dw")
-        variants["serving"] = [serving_variant(lam) for lam in (50, 200, 800)]
+        cap = variants["batched"]["value"]
+        # lambda = 50 per s is below the pool's capacity: 500 requests (~10 s of
+        # arrivals) give steady-state latencies; 200 and 800 per s exceed it
+        variants["serving"] = [serving_variant(50, count=500, capacity=cap)] + \
+            [serving_variant(lam, capacity=cap) for lam in (200, 800)]
         variants["serving_one_at_a_time_fp64"] = serving_sequential_fp64(200)
+    if not args.no_sweep and args.only is None and args.cube == N_CUBE:
+        variants["precision_sweep"] = precision_sweep(steps=args.sweep_steps)
     e2e = None
     if not args.no_e2e and args.only is None:
         wall, r3, h2d, d2h = run_e2e(X, conn, bcs, args.steps)

@@ -50,7 +50,10 @@ enum { MSX_BC_RAMP = 0,      /* *BOUNDARY, TYPE=DISPLACEMENT RAMP: value reached
 
 enum { MSX_PREC_FP64 = 0,        /* plain FP64, FMA-contracted, algebraically simplified laws */
        MSX_PREC_FP64_EXACT = 1,  /* FP64 in the reference's operation order, no contraction   */
-       MSX_PREC_MIXED = 2,       /* FP32 element kinematics/stress/B^T P; FP64 nodes, J-1, dt  */
+       MSX_PREC_MIXED = 2,       /* FP32 element kinematics, stress, B^T P, J-1 and ln J (trace
+                                    summed exactly); nodal u, v, a as double-word FP32 pairs
+                                    (~48 bits); the stable dt is the FP64 CFL minimum (FP32
+                                    screen, FP64 recheck of the near-minimum elements)         */
        MSX_PREC_DOUBLE_WORD = 3  /* MSX_PREC_FP64's algebra in double-word (FP32 pair, ~48-bit)
                                     arithmetic on the FP32 pipe, state and corner forces too;
                                     FP64 CFL check.  Values must stay inside FP32's exponent
@@ -176,6 +179,20 @@ typedef struct {
  * (boundaryConditions.cpp:370-452).  Replaces any loads set before (by either
  * call); takes effect from the next step. */
 msx_status msx_set_load_blocks(msx_handle *h, const msx_load_block *blocks, int64_t num_blocks);
+
+/* The Neumann blocks of an input deck, read from the file by the library:
+ * one msx_load_block per *BOUNDARY, TYPE=FORCE | TRACTION INST|RAMP |
+ * PRESSURE INST|RAMP and *GRAVITY block, in file order, as
+ * NeumannCommonManagement (IO/inputFile.cpp:4705-4760) scans the whole file
+ * and builds one classNeumannBCs per block.  For a solver plugin inside the
+ * reference, which holds the deck's path (GeneralOptions::getInputFilePath)
+ * but whose load objects keep their t0, tf and amounts private.  Force
+ * entries: dof = node + comp * num_nodes, value = F_comp * Ff; surface loads:
+ * 0-based bulk tets.  The blocks stay valid until msx_deck_loads_free. */
+typedef struct msx_deck_loads msx_deck_loads;
+msx_status msx_deck_read_loads(const char *path, int64_t num_nodes, msx_deck_loads **out);
+msx_status msx_deck_loads_blocks(const msx_deck_loads *loads, const msx_load_block **blocks, int64_t *num_blocks);
+msx_status msx_deck_loads_free(msx_deck_loads *loads);
 
 /* Element birth: the reference's *ACTIVATION option of a solver block
  * (solvers.cpp:403-433, called each step at solverExplicit.cpp:259-264) with the
@@ -398,6 +415,14 @@ typedef struct {
 
 /* Counters of the pool (reads the device control table). */
 msx_status msx_pool_stats_get(msx_pool *p, msx_pool_stats *stats);
+
+/* Fault injection for tests of the admission path (no counterpart in the
+ * reference): the next `count` calls of msx_pool_submit fail their device
+ * allocation as if cudaMallocAsync had run out of memory, after the slot and
+ * its HBM were reserved, so they take the same release path as a real
+ * failure and return MSX_ERR_OOM.  Resident solves are not touched.
+ * count = 0 disarms it. */
+msx_status msx_pool_inject_alloc_failures(msx_pool *p, int32_t count);
 
 #ifdef __cplusplus
 }

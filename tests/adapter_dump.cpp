@@ -4,7 +4,10 @@
  * and prints, instead of running the solvers, what the GPU solver plugin
  * (v.1.1_gb300/integration/solverExplicitGPU.h) would hand to msx_create for
  * it: coordinates, connectivity, each element's msx_material, its activation
- * time, and each solver block's msx_bc entries.  Numbers as %.17g.
+ * time, each solver block's msx_bc entries, and the Neumann blocks the plugin
+ * reads from the deck file and checks against the reference's load objects.
+ * Numbers as %.17g.  With -drop-last-load the last of the reference's load
+ * objects is left out before that check (which must then refuse the deck).
  */
 #include "solverExplicitGPU.h"
 #include "commandLine.h"
@@ -15,6 +18,14 @@
 
 int main(int argc, char **argv)
 {
+    bool drop_last_load = false;
+    std::vector<char *> args;
+    for (int k = 0; k < argc; k++) {
+        if (std::string(argv[k]) == "-drop-last-load") drop_last_load = true;
+        else args.push_back(argv[k]);
+    }
+    argc = (int)args.size();
+    argv = args.data();
     GeneralOptions::initialise(argc, argv);
     vector<classNodes *> nod;
     vector<classElements *> elem, geoShape;
@@ -55,6 +66,29 @@ int main(int argc, char **argv)
             const msx_bc c = msx_binding::bc_of(*b);
             printf("B %zu %lld %d %.17g\n", k, (long long)c.dof, c.mode, c.value);
         }
+    }
+    if (!NeumannBCs.empty()) {
+        if (drop_last_load) NeumannBCs.pop_back();
+        msx_deck_loads *keep = nullptr;
+        const msx_load_block *blocks = nullptr;
+        int64_t nb = 0;
+        const std::string why =
+            msx_binding::loads_of(GeneralOptions::getInputFilePath(), NeumannBCs, nn, keep, blocks, nb);
+        if (!why.empty()) {
+            printf("LX %s\n", why.c_str());
+            msx_deck_loads_free(keep);
+            return 4;
+        }
+        for (int64_t k = 0; k < nb; k++) {
+            const msx_load_block &b = blocks[k];
+            printf("L %lld %d %d %.17g %.17g %.17g %.17g %.17g %lld %lld\n", (long long)k, b.kind, b.face, b.t0,
+                   b.tf, b.value[0], b.value[1], b.value[2], (long long)b.num_elems, (long long)b.num_forces);
+            for (int64_t e = 0; e < b.num_elems; e++) printf("LE %lld %d\n", (long long)k, b.elems[e]);
+            for (int64_t f = 0; f < b.num_forces; f++)
+                printf("LF %lld %lld %.17g %.17g %.17g\n", (long long)k, (long long)b.forces[f].dof, b.forces[f].t0,
+                       b.forces[f].tf, b.forces[f].value);
+        }
+        msx_deck_loads_free(keep);
     }
     return 0;
 }

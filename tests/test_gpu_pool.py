@@ -175,3 +175,109 @@ def test_serving_mode_concurrent_admission(precision):
     assert got[t]["steps"] == 17
     assert np.array_equal(P.fetch(t)[0], alone(X, c, m, b, 17, precision)[0])
     P.close()
+
+
+def collapsed_case(seed):
+    """A cube with one element flattened to zero volume: its CFL length is 0,
+    so the solve's first step stops with dt < 1e-20 ("Negative jacobian",
+    solverExplicit.cpp:270-273), status 3."""
+    X, c, m, b = case(3, 1e6, 0.3, 0.1, seed)
+    X = X.copy()
+    X[:, c[5][3]] = X[:, c[5][0]]
+    return X, c, m, b
+
+
+def nan_case(seed):
+    """A cube whose input puts a NaN into u[1] (an instantaneous Dirichlet
+    entry of value NaN on DOF 1): the NaN check of solverExplicit.cpp:306-308
+    stops it with status 4."""
+    X, c, m, b = case(4, 1e6, 0.3, 0.1, seed)
+    return X, c, m, b + [(1, msx.BC_INST, float("nan"), 0)]
+
+
+@pytest.mark.parametrize("precision", [msx.MIXED, msx.FP64, msx.DOUBLE_WORD])
+def test_failed_solves_leave_the_others_unchanged(precision):
+    """Solves that fail inside the pool report their own status and leave it;
+    the healthy solves stepped in the same replays equal their runs alone bit
+    for bit (failure isolation: no state is shared between solves)."""
+    healthy = [case(4, 1e6, 0.3, 0.1, 1), case(5, 3e6, 0.4, 0.05, 2), case(3, 2e5, 0.25, 0.2, 3)]
+    steps = [60, 45, 70]
+    P = msx.Pool(max_slots=8, precision=precision, steps_per_launch=4)
+    tb = P.submit(*collapsed_case(4), 50)
+    tickets = [P.submit(X, c, m, b, st) for (X, c, m, b), st in zip(healthy, steps)]
+    tn = P.submit(*nan_case(5), 50)
+    assert None not in tickets + [tb, tn]
+    for _ in range(40):
+        P.step()
+    res = {r["ticket"]: r for r in P.poll()}
+    assert set(res) == set(tickets + [tb, tn])
+    assert res[tb]["status"] == 3 and res[tb]["steps"] == 0
+    assert res[tn]["status"] == 4 and 1 <= res[tn]["steps"] <= 2
+    for t in (tb, tn):
+        P.fetch(t)          # a failed solve's memory is released like any other
+    for t, (X, c, m, b), st in zip(tickets, healthy, steps):
+        assert res[t]["status"] == 0 and res[t]["steps"] == st
+        got = P.fetch(t)
+        ref = alone(X, c, m, b, st, precision)
+        assert all(np.array_equal(x, y) for x, y in zip(got, ref))
+    assert P.stats()["used_bytes"] == 0
+    P.close()
+
+
+def test_admission_allocation_failure_leaves_the_pool_intact():
+    """An admission whose device allocation fails (injected on the host, as
+    cudaMallocAsync running out of memory) returns MSX_ERR_OOM and releases
+    its reservation; the resident solves run on unchanged, and the next
+    admission succeeds."""
+    A, B, Cc = case(5, 1e6, 0.3, 0.1, 7), case(4, 2e6, 0.35, 0.08, 8), case(3, 5e5, 0.3, 0.15, 9)
+    P = msx.Pool(max_slots=4, precision=msx.MIXED, steps_per_launch=4)
+    ta, tb = P.submit(*A, 120), P.submit(*B, 90)
+    P.step(8)
+    before = P.stats()
+    P.inject_alloc_failures(1)
+    with pytest.raises(msx.MsxError) as ei:
+        P.submit(*Cc, 50)
+    assert ei.value.status == 5 and b"injected" in msx.load().msx_last_error()
+    after = P.stats()
+    assert after["used_bytes"] == before["used_bytes"] and after["active"] == 2
+    tc = P.submit(*Cc, 50)
+    assert tc is not None
+    out = {}
+    for t in (ta, tb, tc):
+        r = P.wait(t)
+        assert r["status"] == 0
+        out[t] = P.fetch(t)
+    P.close()
+    for t, (X, c, m, b), st in ((ta, A, 120), (tb, B, 90), (tc, Cc, 50)):
+        ref = alone(X, c, m, b, st, msx.MIXED)
+        assert all(np.array_equal(x, y) for x, y in zip(out[t], ref))
+
+
+def test_concurrent_serving_stop_joins_once():
+    """Two threads turning serving off at the same time: one joins the
+    library's serving thread, the other waits for it; both return OK and the
+    pool is stepped by msx_pool_step afterwards."""
+    import threading
+    X, c, m, b = case(4, 1e6, 0.3, 0.1, 12)
+    P = msx.Pool(max_slots=2, precision=msx.MIXED, steps_per_launch=4)
+    P.serve(True)
+    t = P.submit(X, c, m, b, 400)
+    errs = []
+
+    def stop():
+        try:
+            P.serve(False)
+        except Exception as e:   # noqa: BLE001
+            errs.append(e)
+
+    th = [threading.Thread(target=stop) for _ in range(2)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    assert not errs
+    r = P.wait(t)
+    assert r["status"] == 0 and r["steps"] == 400
+    u = P.fetch(t)[0]
+    P.close()
+    assert np.array_equal(u, alone(X, c, m, b, 400, msx.MIXED)[0])

@@ -87,6 +87,106 @@ def dump_exe(tmp_path_factory):
     return _link(d, os.path.join(ROOT, "tests", "adapter_dump.cpp"), d / "adapter_dump")
 
 
+def _parse_loads(text):
+    """The L / LE / LF lines of the dump: [(kind, face, t0, tf, values, elems, forces)]."""
+    blocks = []
+    for line in text.splitlines():
+        f = line.split()
+        if not f:
+            continue
+        if f[0] == "L":
+            blocks.append([int(f[2]), int(f[3]), float(f[4]), float(f[5]), tuple(float(x) for x in f[6:9]), [], []])
+        elif f[0] == "LE":
+            blocks[int(f[1])][5].append(int(f[2]))
+        elif f[0] == "LF":
+            blocks[int(f[1])][6].append((int(f[2]), float(f[3]), float(f[4]), float(f[5])))
+    return blocks
+
+
+def _expected_blocks(items, nn):
+    """msx_load_block contents for the deck's load items, as the deck reader
+    builds them (force entries: dof = node + comp * nn, value = F_comp * Ff)."""
+    kinds = {"force": 0, "gravity": 1, "traction_inst": 2, "traction_ramp": 3, "pressure_inst": 4, "pressure_ramp": 5}
+    out = []
+    for it in items:
+        if it[0] == "force":
+            _, t0, tf, Ff, rows = it
+            forces = [(node + c * nn, t0, tf, F[c] * Ff) for node, *F in rows for c in range(3)]
+            out.append([0, 0, 0.0, 0.0, (0.0, 0.0, 0.0), [], forces])
+        elif it[0] == "gravity":
+            out.append([1, 0, 0.0, 0.0, (float(it[1]), 0.0, 0.0), [], []])
+        else:
+            kind, t0, tf, val, S, elems = it
+            vals = (float(val), 0.0, 0.0) if kind.startswith("pressure") else tuple(float(x) for x in val)
+            out.append([kinds[kind], S, t0, tf, vals, list(elems), []])
+    return out
+
+
+LOAD_DECKS = ["cube3_cnh_traction_pressure", "cube3_nh_loads_mixed", "cube3_cnh_force_gravity",
+              "cube3_nh_gravity_force", "cube4_stvk_pressure_ramp"]
+
+
+def _write_load_deck(tmp_path, name):
+    import numpy as np
+    import oracle as O
+    from golden_cases import load, load_loads
+    mesh, mats, solvers, _, _ = load(name)
+    mat_elems = None
+    if mesh.elem_mat is not None:
+        mat_elems = [np.nonzero(mesh.elem_mat == k)[0] for k in range(len(mats))]
+    items = load_loads(name).items
+    O.write_deck(str(tmp_path / "deck.inp"), mesh, mats, solvers, mat_elems, load_loads(name))
+    (tmp_path / "out").mkdir()
+    return mesh, items
+
+
+@needs_ref
+@pytest.mark.parametrize("name", LOAD_DECKS)
+def test_adapter_maps_the_reference_loads(tmp_path, dump_exe, name):
+    """Neumann loads through the plugin: with the deck read by the reference's
+    own readers (one classNeumannBCs per block), the plugin's load blocks --
+    read from the same file by the library and checked against each reference
+    object's class, node ids, face count and amount at tf -- are the deck's
+    blocks in deck order, bit for bit what msx_deck hands to
+    msx_set_load_blocks (boundaryConditions.cpp:75-138 applies them in that
+    order)."""
+    mesh, items = _write_load_deck(tmp_path, name)
+    r = subprocess.run([str(dump_exe), "-input", "deck.inp", "-inputDir", ".", "-outputDir", "out"],
+                       cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.stdout[-1000:], r.stderr[-2000:])
+    got = _parse_loads(r.stdout)
+    want = _expected_blocks(items, mesh.nn)
+    assert len(got) == len(want)
+    for g, w in zip(got, want):
+        assert g[0] == w[0] and g[5] == w[5] and g[6] == w[6], (g[:5], w[:5])
+        if w[0] >= 2:           # surface loads: face, t0, tf, values
+            assert (g[1], g[2], g[3], g[4]) == (w[1], w[2], w[3], w[4])
+        if w[0] == 1:
+            assert g[4][0] == w[4][0]
+    # the front end's own view of the same file
+    import build as msx_build
+    deck = os.path.join(os.path.dirname(msx_build.LIB), "msx_deck")
+    p = subprocess.run([deck, "-input", "deck.inp", "-inputDir", str(tmp_path), "-parse-only"],
+                       capture_output=True, text=True, timeout=60)
+    assert p.returncode == 0, p.stderr
+    import json
+    d = json.loads(p.stdout)
+    assert [(b["kind"], b["elements"], b["entries"]) for b in d["loads"]] == \
+        [({0: "FORCE", 1: "GRAVITY", 2: "TRACTION INST", 3: "TRACTION RAMP", 4: "PRESSURE INST",
+           5: "PRESSURE RAMP"}[g[0]], len(g[5]), len(g[6])) for g in got]
+
+
+@needs_ref
+def test_adapter_refuses_a_deck_that_does_not_match_the_model(tmp_path, dump_exe):
+    """If the reference's load objects and the deck file disagree (here: one
+    object fewer), the plugin stops the block instead of loading the deck."""
+    _write_load_deck(tmp_path, "cube3_nh_loads_mixed")
+    r = subprocess.run([str(dump_exe), "-input", "deck.inp", "-inputDir", ".", "-outputDir", "out",
+                        "-drop-last-load"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 4
+    assert "Neumann blocks, the model" in r.stdout
+
+
 def _parse_dump(text):
     X, C, M, A, S, B = {}, {}, {}, {}, [], {}
     for line in text.splitlines():

@@ -26,6 +26,7 @@ UNITS = {
     "msx_pool.cu": [],
     "msx_noalloc.cu": ["--fmad=false"],
     "msx_csr.cu": [],
+    "msx_deckio.cpp": [],
 }
 DECK = os.path.join(OUT, "msx_deck")
 

@@ -57,16 +57,7 @@ struct SolverBlock {
 
 struct Deck {
     std::vector<double> xyz;          // node-major while reading
-    struct Force { long long node; int comp; double t0, tf, value; };
-    // Neumann blocks in deck order (the reference's NeumannBCs list)
-    struct Load {
-        int kind;                     // MSX_LOAD_*
-        int face = 0;
-        double t0 = 0, tf = 0, value[3] = {0, 0, 0};
-        std::vector<Force> forces;    // FORCE entries
-        std::vector<int32_t> elems;   // traction / pressure: bulk tets, 0-based
-    };
-    std::vector<Load> loads;
+    bool has_loads = false;           // Neumann blocks present (read by msx_deck_read_loads)
     // *EXTRACTION, NODE blocks (IO/inputFile.cpp:4950-5026): "name, type, operation, comp";
     // *EXTRACTION, ELEMENT blocks (:5028-5111): "name,type,operation", then All or elements
     struct Extraction {
@@ -152,47 +143,16 @@ Deck parse(const std::string &path)
                 if (f.size() != 5) die("a C3D4 line has id and 4 nodes", (int)i + 1);
                 for (int c = 1; c < 5; c++) d.conn.push_back(atoi(f[c].c_str()) - 1);
             }
-        } else if (starts(L, "*BOUNDARY, TYPE=FORCE")) {
-            // src/IO/inputFile.cpp:2841-2945: "t0, tf, Ff" then "node, Fx, Fy, Fz"
-            auto h = split(lines[i + 1]);
-            if (h.size() != 3) die("a force block starts with t0, tf, Ff", (int)i + 2);
-            double t0 = atof(h[0].c_str()), tf = atof(h[1].c_str()), Ff = atof(h[2].c_str());
-            Deck::Load B;
-            B.kind = MSX_LOAD_FORCE;
+        } else if (starts(L, "*BOUNDARY, TYPE=FORCE") || starts(L, "*BOUNDARY, TYPE=TRACTION RAMP") ||
+                   starts(L, "*BOUNDARY, TYPE=TRACTION INST") || starts(L, "*BOUNDARY, TYPE=PRESSURE RAMP") ||
+                   starts(L, "*BOUNDARY, TYPE=PRESSURE INST")) {
+            // Neumann blocks: read by the library (msx_deck_read_loads); skipped here
             for (i += 2; data_line(i); i++) {
-                auto f = split(lines[i]);
-                if (f.size() != 4) die("a force line has node, Fx, Fy, Fz", (int)i + 1);
-                long long node = atoll(f[0].c_str()) - 1;
-                if (node < 0 || node >= (long long)d.xyz.size() / 3) die("force node out of range", (int)i + 1);
-                for (int c = 0; c < 3; c++) B.forces.push_back({node, c, t0, tf, atof(f[c + 1].c_str()) * Ff});
             }
-            d.loads.push_back(B);
-        } else if (starts(L, "*BOUNDARY, TYPE=TRACTION RAMP") || starts(L, "*BOUNDARY, TYPE=TRACTION INST") ||
-                   starts(L, "*BOUNDARY, TYPE=PRESSURE RAMP") || starts(L, "*BOUNDARY, TYPE=PRESSURE INST")) {
-            // src/IO/inputFile.cpp:3229-3700: "t0, tf, Tx, Ty, Tz, S" (traction) or
-            // "t0, tf, P, S" (pressure), then one bulk element per line; face S of each
-            const bool pressure = L.find("PRESSURE") != std::string::npos, ramp = L.find("RAMP") != std::string::npos;
-            Deck::Load B;
-            B.kind = pressure ? (ramp ? MSX_LOAD_PRESSURE_RAMP : MSX_LOAD_PRESSURE_INST)
-                              : (ramp ? MSX_LOAD_TRACTION_RAMP : MSX_LOAD_TRACTION_INST);
-            auto h = split(lines[i + 1]);
-            const size_t nv = pressure ? 1 : 3;
-            if (h.size() != nv + 3) die(pressure ? "a pressure block starts with t0, tf, P, S"
-                                                 : "a traction block starts with t0, tf, Tx, Ty, Tz, S", (int)i + 2);
-            B.t0 = atof(h[0].c_str());
-            B.tf = atof(h[1].c_str());
-            for (size_t k = 0; k < nv; k++) B.value[k] = atof(h[2 + k].c_str());
-            B.face = (int)atof(h[2 + nv].c_str());
-            if (B.face < 1 || B.face > 4) die("the face of a C3D4 surface load is 1..4", (int)i + 2);
-            for (i += 2; data_line(i); i++) B.elems.push_back(atoi(lines[i].c_str()) - 1);
-            d.loads.push_back(B);
+            d.has_loads = true;
         } else if (starts(L, "*GRAVITY")) {
-            // src/IO/inputFile.cpp:4723-4735
-            Deck::Load B;
-            B.kind = MSX_LOAD_GRAVITY;
-            B.value[0] = atof(lines[i + 1].c_str());
-            d.loads.push_back(B);
             i += 2;
+            d.has_loads = true;
         } else if (starts(L, "*EXTRACTION, NODE")) {
             // data extraction of nodal values written every step (solvers/dataExtraction.cpp)
             auto h = split(lines[i + 1]);
@@ -588,6 +548,15 @@ int main(int argc, char **argv)
     }
     Deck d = parse(dir + "/" + input);
     const long long nn = (long long)d.xyz.size() / 3, ne = (long long)d.conn.size() / 4;
+    // the Neumann blocks, as the library reads them for any caller
+    msx_deck_loads *loads = nullptr;
+    const msx_load_block *blocks = nullptr;
+    int64_t nblocks = 0;
+    if (d.has_loads && (msx_deck_read_loads((dir + "/" + input).c_str(), nn, &loads) != MSX_OK ||
+                        msx_deck_loads_blocks(loads, &blocks, &nblocks) != MSX_OK)) {
+        fprintf(stderr, "msx_deck: %s\n", msx_last_error());
+        return 2;
+    }
     std::vector<double> X(3 * nn);
     for (long long i = 0; i < nn; i++)
         for (int c = 0; c < 3; c++) X[c * nn + i] = d.xyz[3 * i + c];
@@ -599,8 +568,9 @@ int main(int argc, char **argv)
         size_t nforces = 0;
         double gravity = 0;
         int gravity_first = 0;
-        for (const auto &B : d.loads) {
-            if (B.kind == MSX_LOAD_FORCE) nforces += B.forces.size();
+        for (int64_t k = 0; k < nblocks; k++) {
+            const msx_load_block &B = blocks[k];
+            if (B.kind == MSX_LOAD_FORCE) nforces += (size_t)B.num_forces;
             if (B.kind == MSX_LOAD_GRAVITY) {
                 if (nforces == 0 && gravity == 0) gravity_first = 1;
                 gravity = B.value[0];
@@ -620,9 +590,10 @@ int main(int argc, char **argv)
         }
         printf("]");
         printf(", \"loads\": [");
-        for (size_t k = 0; k < d.loads.size(); k++)
-            printf("%s{\"kind\": \"%s\", \"face\": %d, \"elements\": %zu, \"entries\": %zu}", k ? ", " : "",
-                   names[d.loads[k].kind], d.loads[k].face, d.loads[k].elems.size(), d.loads[k].forces.size());
+        for (int64_t k = 0; k < nblocks; k++)
+            printf("%s{\"kind\": \"%s\", \"face\": %d, \"elements\": %lld, \"entries\": %lld}", k ? ", " : "",
+                   names[blocks[k].kind], blocks[k].face, (long long)blocks[k].num_elems,
+                   (long long)blocks[k].num_forces);
         printf("]");
         printf(", \"blocks\": [");
         for (size_t k = 0; k < d.solvers.size(); k++)
@@ -651,18 +622,7 @@ int main(int argc, char **argv)
         msx_status st;
         if (k == 0) {
             st = msx_create(&mesh, d.mats.data(), (int32_t)d.mats.size(), s.bcs.data(), (int64_t)s.bcs.size(), &o, &h);
-            if (st == MSX_OK && !d.loads.empty()) {
-                std::vector<std::vector<msx_nodal_force>> nf(d.loads.size());
-                std::vector<msx_load_block> blocks(d.loads.size());
-                for (size_t k = 0; k < d.loads.size(); k++) {
-                    const Deck::Load &B = d.loads[k];
-                    for (const auto &f : B.forces) nf[k].push_back({f.node + f.comp * nn, f.t0, f.tf, f.value});
-                    blocks[k] = msx_load_block{B.kind, B.face, B.t0, B.tf, {B.value[0], B.value[1], B.value[2]},
-                                               B.elems.data(), (int64_t)B.elems.size(), nf[k].data(),
-                                               (int64_t)nf[k].size()};
-                }
-                st = msx_set_load_blocks(h, blocks.data(), (int64_t)blocks.size());
-            }
+            if (st == MSX_OK && nblocks > 0) st = msx_set_load_blocks(h, blocks, nblocks);
         } else {
             // src/main.cpp:171-179: time continuity between solvers
             if (s.t0 - d.solvers[k - 1].tf > 1E-12) {
@@ -765,5 +725,6 @@ int main(int argc, char **argv)
     for (auto &E : d.extractions)
         if (E.file) fclose(E.file);
     msx_destroy(h);
+    msx_deck_loads_free(loads);
     return 0;
 }

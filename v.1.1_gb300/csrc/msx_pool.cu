@@ -13,6 +13,7 @@
 // any solve is resident; admissions build their host tables and upload their
 // data without holding the pool's lock, so they overlap the replays.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -112,6 +113,7 @@ struct msx_pool {
     cudaStream_t fetch = nullptr;    // msx_pool_fetch: result copies, overlapping a replay
     cudaEvent_t ev_upload = nullptr, ev_step = nullptr;
     bool uploads_pending = false;    // admissions since the last replay launch
+    std::atomic<int> inject_alloc_failures{0};   // msx_pool_inject_alloc_failures
     bool inflight = false;           // a replay launched by msx_pool_step not yet collected
     std::vector<Slot> slots;
     Problem *d_descs = nullptr;
@@ -289,6 +291,15 @@ static msx_status collect(msx_pool *p)
         p->cv_done.notify_all();   // msx_pool_wait callers in serving mode
     }
     return MSX_OK;
+}
+
+// One armed admission failure, if any is left (msx_pool_inject_alloc_failures).
+static bool take_injected_failure(msx_pool *p)
+{
+    int n = p->inject_alloc_failures.load();
+    while (n > 0 && !p->inject_alloc_failures.compare_exchange_weak(n, n - 1)) {
+    }
+    return n > 0;
 }
 
 static bool any_active(const msx_pool *p)
@@ -605,6 +616,8 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     // can launch the next one meanwhile.  Replays touch only the tiles of
     // active solves, so none reads this slot's arrays or control entries yet.
     auto upload_solve = [&]() -> msx_status {
+        if (take_injected_failure(p))
+            return pfail(MSX_ERR_OOM, "cudaMallocAsync(solve arena): out of memory (injected failure)");
         PCUDA(cudaMallocAsync(&sl.arena, bytes, p->upload));
         char *q = (char *)sl.arena;
         auto carve = [&](size_t b) {
@@ -766,6 +779,13 @@ extern "C" msx_status msx_pool_serve(msx_pool *p, int32_t enabled)
     p->serving = false;
     p->cv_done.notify_all();
     return p->serve_status == MSX_OK ? MSX_OK : serve_failure(p);
+}
+
+extern "C" msx_status msx_pool_inject_alloc_failures(msx_pool *p, int32_t count)
+{
+    if (!p || count < 0) return pfail(MSX_ERR_ARG, "msx_pool_inject_alloc_failures: NULL pool or negative count");
+    p->inject_alloc_failures.store(count);
+    return MSX_OK;
 }
 
 extern "C" msx_status msx_pool_step(msx_pool *p, int64_t steps)

@@ -9,9 +9,14 @@
 // the arguments classSolverExplicit gets plus a precision (MSX_PREC_*), and
 // links with -lmsx.  It covers decks of C3D4 elements with the Neo-Hookean,
 // compressible Neo-Hookean, St-Venant-Kirchhoff and linear-elastic laws,
-// Dirichlet BCs and element birth (*ACTIVATION).  Neumann loads need getters
-// the reference's load classes do not have (their t0, tf and amounts are
-// private): with loads present the block stops with an error naming them.
+// Dirichlet BCs, element birth (*ACTIVATION) and the Neumann loads of the
+// explicit path (nodal forces, gravity, traction and pressure, instantaneous
+// and ramped).  The reference's load classes keep their t0, tf and amounts
+// private, so the loads are read from the deck file itself by the library
+// (msx_deck_read_loads on GeneralOptions::getInputFilePath()), and each block
+// is checked against the reference's own load object through its public
+// getters (class, node ids, element count, amount at the block's tf): a deck
+// that does not match the loaded model stops the block with an error.
 // The state hand-off is the reference's own: initValues() before calculate,
 // getFinalValues() after, through the protected _u, _v, _a.
 //
@@ -29,6 +34,7 @@
 #include "classGPs.h"
 #include "classNeumannBCs.h"
 #include "classNodes.h"
+#include "commandLine.h"
 #include "configuration.h"
 #include "hyperElasticNeoHookean.h"
 #include "hyperElasticStVenantKirchhoff.h"
@@ -94,6 +100,99 @@ inline msx_bc bc_of(const classDirichlet &d)
     return b;
 }
 
+// Whether block B (read from the deck by the library) is the reference's load
+// object L, as far as L's public getters show: the class for the kind, then
+// the node ids and the amount at B's tf computed as L computes it
+// (classNodes.h:101-109 for nodal forces: F / (tf - t0) * t; classNeumannBCs.h
+// for tractions and pressures), the number of faces of a surface load (one
+// per listed tet in a serial run) and g.  Empty when they agree, else why not.
+inline std::string load_mismatch(const msx_load_block &B, classNeumannBCs *L, int64_t nn)
+{
+    const std::type_info &t = typeid(*L);
+    const double tf = B.tf, dt = 0.0;
+    switch (B.kind) {
+    case MSX_LOAD_FORCE: {
+        if (t != typeid(classNodalForces)) return "a nodal-force block where the model has " + L->getType();
+        vector<classNeumann *> &nodes = static_cast<classNodalForces *>(L)->getListOfNodes();
+        if ((int64_t)nodes.size() * 3 != B.num_forces) return "a different number of force nodes";
+        for (size_t i = 0; i < nodes.size(); i++) {
+            const msx_nodal_force *f = B.forces + 3 * i;
+            if (f[0].dof != nodes[i]->getMe()) return "a different force node";
+            const vector<double> F = nodes[i]->getTracAmount(f[0].tf, dt);
+            for (int c = 0; c < 3; c++)
+                if (F[c] != f[c].value / (f[c].tf - f[c].t0) * f[c].tf) return "a different nodal force";
+        }
+        return "";
+    }
+    case MSX_LOAD_GRAVITY:
+        if (t != typeid(classGravity)) return "a gravity block where the model has " + L->getType();
+        return static_cast<classGravity *>(L)->getGravity() == B.value[0] ? "" : "a different g";
+    case MSX_LOAD_TRACTION_INST:
+    case MSX_LOAD_TRACTION_RAMP: {
+        const bool ramp = B.kind == MSX_LOAD_TRACTION_RAMP;
+        double T[3] = {0, 0, 0};
+        size_t faces = 0;
+        if (!ramp && t == typeid(classTractionInst)) {
+            auto *x = static_cast<classTractionInst *>(L);
+            x->getTraction(tf, dt, T[0], T[1], T[2]);
+            faces = x->getListOfElements().size();
+        } else if (ramp && t == typeid(classTractionRamp)) {
+            auto *x = static_cast<classTractionRamp *>(L);
+            x->getTraction(tf, dt, T[0], T[1], T[2]);
+            faces = x->getListOfElements().size();
+        } else {
+            return std::string("a traction block where the model has ") + L->getType();
+        }
+        if ((int64_t)faces != B.num_elems) return "a different number of traction faces";
+        for (int c = 0; c < 3; c++) {
+            const double want = ramp ? B.value[c] / (B.tf - B.t0) * (tf - B.t0) : B.value[c];
+            if (T[c] != want) return "a different traction";
+        }
+        return "";
+    }
+    case MSX_LOAD_PRESSURE_INST:
+    case MSX_LOAD_PRESSURE_RAMP: {
+        const bool ramp = B.kind == MSX_LOAD_PRESSURE_RAMP;
+        double P = 0;
+        size_t faces = 0;
+        if (!ramp && t == typeid(classPressureInst)) {
+            auto *x = static_cast<classPressureInst *>(L);
+            P = x->getPressure(tf, dt);
+            faces = x->getListOfElements().size();
+        } else if (ramp && t == typeid(classPressureRamp)) {
+            auto *x = static_cast<classPressureRamp *>(L);
+            P = x->getPressure(tf, dt);
+            faces = x->getListOfElements().size();
+        } else {
+            return std::string("a pressure block where the model has ") + L->getType();
+        }
+        if ((int64_t)faces != B.num_elems) return "a different number of pressure faces";
+        const double want = ramp ? B.value[0] / (B.tf - B.t0) * (tf - B.t0) : B.value[0];
+        return P == want ? "" : "a different pressure";
+    }
+    default:
+        return "an unknown load kind";
+    }
+}
+
+// The model's Neumann loads as msx_load_blocks read from the deck file, each
+// checked against the reference's object; `keep` owns the blocks.
+inline std::string loads_of(const std::string &deck, vector<classNeumannBCs *> &NeumannBCs, int64_t nn,
+                            msx_deck_loads *&keep, const msx_load_block *&blocks, int64_t &nblocks)
+{
+    keep = nullptr;
+    if (msx_deck_read_loads(deck.c_str(), nn, &keep) != MSX_OK || msx_deck_loads_blocks(keep, &blocks, &nblocks) != MSX_OK)
+        return msx_last_error();
+    if (nblocks != (int64_t)NeumannBCs.size())
+        return "the deck " + deck + " has " + std::to_string(nblocks) + " Neumann blocks, the model " +
+               std::to_string(NeumannBCs.size());
+    for (int64_t k = 0; k < nblocks; k++) {
+        const std::string why = load_mismatch(blocks[k], NeumannBCs[k], nn);
+        if (!why.empty()) return "Neumann block " + std::to_string(k + 1) + " of " + deck + ": " + why;
+    }
+    return "";
+}
+
 }  // namespace msx_binding
 
 class classSolverExplicitGPU : public solvers {
@@ -119,9 +218,6 @@ class classSolverExplicitGPU : public solvers {
         if (_ndim != 3 || (int64_t)_u.size() != 3 * nn || (int64_t)_v.size() != 3 * nn ||
             (int64_t)_a.size() != 3 * nn)
             stop("EXPLICIT GPU: 3D mechanics only (3 DOFs per node, no extra fields)");
-        if (!NeumannBCs.empty())
-            stop("EXPLICIT GPU: Neumann loads need getters for their t0, tf and amounts "
-                 "(classNodalForces, classGravity, classTractionInst/Ramp, classPressureInst/Ramp)");
         // mesh: X[c*Nn + node], conn[4e + a], one material id per element
         std::vector<double> X(3 * nn);
         for (int64_t i = 0; i < nn; i++)
@@ -161,6 +257,21 @@ class classSolverExplicitGPU : public solvers {
         msx_handle *h = nullptr;
         check(msx_create(&mesh, mats.data(), (int32_t)mats.size(), bcs.data(), (int64_t)bcs.size(), &o, &h), h);
         check(msx_set_state(h, _u.data(), _v.data(), _a.data()), h);
+        if (!NeumannBCs.empty()) {
+            msx_deck_loads *loads = nullptr;
+            const msx_load_block *blocks = nullptr;
+            int64_t nblocks = 0;
+            const std::string why =
+                msx_binding::loads_of(GeneralOptions::getInputFilePath(), NeumannBCs, nn, loads, blocks, nblocks);
+            if (!why.empty()) {
+                msx_deck_loads_free(loads);
+                msx_destroy(h);
+                stop("EXPLICIT GPU: " + why);
+            }
+            const msx_status st = msx_set_load_blocks(h, blocks, nblocks);
+            msx_deck_loads_free(loads);
+            check(st, h);
+        }
         if (_flagActivation) check(msx_set_activation(h, act.data(), 1), h);
         msx_run_report r{};
         check(msx_run(h, 0, &r), h);

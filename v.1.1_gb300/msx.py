@@ -104,7 +104,8 @@ SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_
            "msx_pool_poll", "msx_pool_fetch", "msx_pool_wait", "msx_pool_destroy", "msx_pool_stats_get",
            "msx_internal_force_noalloc", "msx_initial_dt", "msx_element_fields", "msx_set_loads",
            "msx_set_load_blocks", "msx_node_values", "msx_element_values", "msx_element_reduce",
-           "msx_set_activation"]
+           "msx_set_activation", "msx_pool_inject_alloc_failures", "msx_deck_read_loads", "msx_deck_loads_blocks",
+           "msx_deck_loads_free"]
 
 _lib = None
 
@@ -360,6 +361,12 @@ class Solver:
         _check(load().msx_element_fields(self.h, _p(c), _p(g), _p(v)))
         return c.reshape(-1, 3, 3), g.reshape(-1, 3, 3), v
 
+    def von_mises(self):
+        """Von Mises stress (ne,) of the current state (the other fields are not copied)."""
+        v = np.zeros(self.ne)
+        _check(load().msx_element_fields(self.h, None, None, _p(v)))
+        return v
+
     def element_data(self):
         G, wJ, L, m = np.zeros(9 * self.ne), np.zeros(self.ne), np.zeros(self.ne), np.zeros(self.nn)
         _check(load().msx_get_element_data(self.h, _p(G), _p(wJ), _p(L), _p(m)))
@@ -398,7 +405,8 @@ class Pool:
                            ("msx_pool_fetch", [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
                            ("msx_pool_wait", [C.c_void_p, C.c_int64, C.c_void_p]),
                            ("msx_pool_destroy", [C.c_void_p]),
-                           ("msx_pool_stats_get", [C.c_void_p, C.POINTER(PoolStats_)])):
+                           ("msx_pool_stats_get", [C.c_void_p, C.POINTER(PoolStats_)]),
+                           ("msx_pool_inject_alloc_failures", [C.c_void_p, C.c_int32])):
             f = getattr(L, name)
             f.argtypes = args
             f.restype = C.c_int
@@ -462,6 +470,10 @@ class Pool:
         _check(load().msx_pool_fetch(self.h, ticket, _p(u), _p(v), _p(a)))
         del self.sizes[ticket]
         return u, v, a
+
+    def inject_alloc_failures(self, count):
+        """Make the next `count` submits fail their device allocation (MSX_ERR_OOM)."""
+        _check(load().msx_pool_inject_alloc_failures(self.h, int(count)))
 
     def stats(self):
         st = PoolStats_()
