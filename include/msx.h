@@ -209,6 +209,27 @@ msx_status msx_deck_loads_free(msx_deck_loads *loads);
  * available in msx_pool_*. */
 msx_status msx_set_activation(msx_handle *h, const double *activation_time, int32_t enabled);
 
+/* Artificial viscosity of the explicit solver: *Bulk viscosity (kind
+ * MSX_VISC_BULK) and *Dev viscosity (MSX_VISC_DEV) with the "c1, cl" the
+ * deck gives (defaults 0.06, 1.2 and 1, 0.5: IO/inputFile.cpp:2462-2511), the
+ * second pass of classSolverExplicit::computeInternalForce
+ * (solverExplicit.cpp:381-421).  Bulk: per element trD = tr(F - F_prev)/dt
+ * (F_prev: the element's F at the previous step, the handed-over state's at a
+ * block start), qBV = rho/J h (c1^2 h |trD| min(0, trD) + cl c0 trD) and the
+ * viscous Piola stress J qBV F^-T, integrated as wJ B^T P (bulkViscosity,
+ * :514-541).  h and c0 are the reference's solvers::_elementSize and _c0
+ * (solvers.h:53-54), which it never assigns: its builds run with 0, which
+ * makes the viscous force zero, and element_size = 0 here does the same
+ * (results bit for bit those without viscosity).  A nonzero element_size
+ * applies the formula with the given h and c0.  Deviatoric: the reference
+ * scales the deviatoric rate but maps the still-zero Cauchy tensor to P
+ * (:469-502), so it adds nothing, whatever its parameters; here too.
+ * MSX_VISC_NONE turns it off.  Applies from the next step, also to later
+ * solver blocks (the reference's flag stays set); msx_internal_force leaves it
+ * out.  Not together with element birth, not in msx_pool_*. */
+enum { MSX_VISC_NONE = 0, MSX_VISC_BULK = 1, MSX_VISC_DEV = 2 };
+msx_status msx_set_viscosity(msx_handle *h, int32_t kind, double c1, double cl, double element_size, double c0);
+
 /* Nodal values of the current state for the reference's node data extraction
  * (*EXTRACTION, NODE: solvers/dataExtraction.cpp:778-840, written every step by
  * classSolverExplicit::calculate, solverExplicit.cpp:325).  field: displacement
@@ -270,7 +291,9 @@ const char *msx_last_error(void);
 
 /* Internal force f_int(u) for host u (3*num_nodes), host fint out: one element
  * pass plus the CSR gather (classSolverExplicit::computeInternalForce,
- * src/solvers/solverExplicit.cpp:363-379).  Leaves the solver state untouched. */
+ * src/solvers/solverExplicit.cpp:363-379; the elastic part: artificial
+ * viscosity depends on the previous step and is left out).  Leaves the solver
+ * state untouched. */
 msx_status msx_internal_force(msx_handle *h, const double *u, double *fint);
 
 /* Per-element set-up data and per-node lumped mass: G[9*num_elems] (rows of

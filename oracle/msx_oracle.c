@@ -344,6 +344,79 @@ int orc_element_fields(int64_t nn, int64_t ne, const int32_t *conn, const double
     return ORC_OK;
 }
 
+/* classSolverExplicit::bulkViscosity (solverExplicit.cpp:514-541): the
+ * viscous first Piola stress from the current and previous F of one Gauss
+ * point, in the reference's operation order (sumTensorTensor with factor -1,
+ * multiSTensorScalar by 1/dt, getTrace, maths.cpp:1169-1175, 1604-1610,
+ * 2257-2286).  The quadratic term takes |trD| as fabs; std::min(0., trD) is
+ * (trD < 0) ? trD : 0. */
+static void bulk_viscosity(double h, double c1, double cl, double c0, const double *F1, const double *F0,
+                           double rho, double dt, double *P)
+{
+    double Fdot[9];
+    if (dt == 0) {
+        for (int k = 0; k < 9; k++) Fdot[k] = 0.;
+    } else {
+        for (int k = 0; k < 9; k++) Fdot[k] = F1[k] + (-1) * F0[k];
+        for (int k = 0; k < 9; k++) Fdot[k] = Fdot[k] * (1 / dt);
+    }
+    double trD = 0;
+    for (int i = 0; i < 3; i++) trD += Fdot[i * 3 + i];
+    double J1 = det3(F1);
+    double Rho_1 = rho / J1;
+    double qBV = Rho_1 * h * (c1 * c1 * h * fabs(trD) * ((trD < 0.) ? trD : 0.) + cl * c0 * trD);
+    double Cv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, iF[9];
+    for (int i = 0; i < 3; i++) Cv[i + i * 3] = -1 * qBV;
+    inverse3(F1, iF);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            P[i * 3 + j] = 0;
+            for (int k = 0; k < 3; k++) P[i * 3 + j] += Cv[i * 3 + k] * iF[j * 3 + k];
+        }
+    for (int k = 0; k < 9; k++) P[k] = P[k] * (-1 * J1);
+}
+
+/* classSolverExplicit::artificialViscosity (solverExplicit.cpp:469-502): its
+ * scaled deviatoric rate is never stored in the Cauchy tensor it maps, so the
+ * Piola stress is that zero tensor times F^-T, times J (the rest of the
+ * routine has no effect on the result). */
+static void dev_viscosity(const double *F1, double *P)
+{
+    double Cv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, iF[9];
+    double J1 = det3(F1);
+    inverse3(F1, iF);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            P[i * 3 + j] = 0;
+            for (int k = 0; k < 3; k++) P[i * 3 + j] += Cv[i * 3 + k] * iF[j * 3 + k];
+        }
+    for (int k = 0; k < 9; k++) P[k] = P[k] * J1;
+}
+
+/* The viscous pass of computeInternalForce (solverExplicit.cpp:381-421): after
+ * the elastic scatter, per Gauss point in element order, fint += wJ P_vis dphi
+ * term by term.  F1: the elements' current F; F0: their previous F. */
+static void viscous_force(const orc_problem *p, const double *dphi, const double *wJ, const double *F1,
+                          const double *F0, double dt, double t, double *fint)
+{
+    const int64_t nn = p->nn;
+    for (int64_t e = 0; e < p->ne; e++) {
+        if (!gp_active(p, e, t)) continue;
+        const orc_material *m = &p->mats[p->elem_mat ? p->elem_mat[e] : 0];
+        double P[9];
+        if (p->viscosity == 1)
+            bulk_viscosity(p->visc_h, p->visc_c1, p->visc_cl, p->visc_c0, F1 + 9 * e, F0 + 9 * e, m->rho, dt, P);
+        else
+            dev_viscosity(F1 + 9 * e, P);
+        const double *dp = dphi + 12 * e;
+        for (int a = 0; a < 4; a++)
+            for (int i = 0; i < 3; i++) {
+                const int64_t d = p->conn[e * 4 + a] + nn * i;
+                for (int J = 0; J < 3; J++) fint[d] += wJ[e] * P[i * 3 + J] * dp[a * 3 + J];
+            }
+    }
+}
+
 /* solverExplicit.cpp:363-379 computeInternalForce: scatter in element order. */
 static int internal_force(int64_t nn, int64_t ne, const int32_t *conn, const double *dphi,
                           const double *wJ, const int32_t *elem_mat, const orc_material *mats,
@@ -619,9 +692,12 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
     double *uK = malloc(sizeof(double) * (size_t)ndof), *aprev = malloc(sizeof(double) * (size_t)ndof);
     double *fext = malloc(sizeof(double) * (size_t)ndof), *absJ = malloc(sizeof(double) * (size_t)ne);
     char *cons = calloc((size_t)ndof, 1);
+    const int visc = p->viscosity == 1 || p->viscosity == 2;
+    double *Fcur = visc ? malloc(sizeof(double) * 9 * (size_t)ne) : NULL;
     int32_t *flag = malloc(sizeof(int32_t) * (size_t)(p->nbc > 0 ? p->nbc : 1));
     double *UU = malloc(sizeof(double) * (size_t)(p->nbc > 0 ? p->nbc : 1));
-    if (!dphi || !wJ || !Lref || !cel || !mass || !fint || !uK || !aprev || !cons || !flag || !UU || !fext || !absJ) {
+    if (!dphi || !wJ || !Lref || !cel || !mass || !fint || !uK || !aprev || !cons || !flag || !UU || !fext || !absJ ||
+        (visc && (!Fcur || !p->F_prev))) {
         rc = ORC_ERR_ARG;
         goto done;
     }
@@ -684,7 +760,8 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
             v[d] = Ud;
             a[d] = 0.;
         }
-        internal_force(nn, ne, p->conn, dphi, wJ, p->elem_mat, p->mats, u, fint, 0, 0, p->nthreads, p, t);
+        internal_force(nn, ne, p->conn, dphi, wJ, p->elem_mat, p->mats, u, fint, Fcur, 0, p->nthreads, p, t);
+        if (visc) viscous_force(p, dphi, wJ, Fcur, p->F_prev, dt, t, fint);
         external_force(p, absJ, dphi, u, t, fext);
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static) num_threads(p->nthreads > 0 ? p->nthreads : 1)
@@ -700,6 +777,8 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
         memcpy(uK, u, sizeof(double) * (size_t)ndof);
         if (!isfinite(uK[1])) { rc = ORC_ERR_NAN; break; }
         memcpy(aprev, a, sizeof(double) * (size_t)ndof);
+        /* solvers.cpp:328-343 nextStep: the Gauss points' previous state <- current */
+        if (visc) memcpy(p->F_prev, Fcur, sizeof(double) * 9 * (size_t)ne);
     }
     if (res) {
         res->steps = step; res->t = t; res->dt_last = dt; res->status = rc;
@@ -711,7 +790,7 @@ int orc_run(const orc_problem *p, double *u, double *v, double *a,
     }
 done:
     free(dphi); free(wJ); free(Lref); free(cel); free(mass); free(fint);
-    free(uK); free(aprev); free(cons); free(flag); free(UU); free(fext); free(absJ);
+    free(uK); free(aprev); free(cons); free(flag); free(UU); free(fext); free(absJ); free(Fcur);
     return rc;
 }
 

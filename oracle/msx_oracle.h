@@ -67,6 +67,14 @@ typedef struct {
     const double *act_time;   /* ne activation times (first internal variable), or NULL  */
     int32_t activation;       /* 1: the block's *ACTIVATION option (element birth)       */
     double time;              /* element extraction: the time the element states are at */
+    /* Artificial viscosity of the explicit solver (solverExplicit.cpp:381-421, 469-541):
+     * 0 none, 1 *Bulk viscosity, 2 *Dev viscosity; c1, cl as the keyword reads them
+     * (inputFile.cpp:2462-2511).  visc_h and visc_c0 stand for solvers::_elementSize and
+     * _c0 (solvers.h:53-54), which the reference never assigns (0 in its builds). */
+    int32_t viscosity;
+    double visc_c1, visc_cl, visc_h, visc_c0;
+    double *F_prev;           /* 9*ne: each element's F at the previous step (the Gauss
+                                 point's previous state), in/out; needed with viscosity */
 } orc_problem;
 
 typedef struct { int64_t steps; double t, dt_last, dt_init; int32_t status; double loop_seconds; } orc_result;

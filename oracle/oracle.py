@@ -27,6 +27,7 @@ NEO_HOOKEAN, COMPRESSIBLE_NH, STVK, LINEAR_ELASTIC = 0, 1, 2, 3
 LAW_NAMES = {NEO_HOOKEAN: "Neo-Hookean", COMPRESSIBLE_NH: "3D-Compressible-Neo-Hookean",
              STVK: "St-Venant-Kirchhoff"}
 BC_RAMP, BC_INST, BC_VEL_RAMP = 0, 1, 2
+VISC_NONE, VISC_BULK, VISC_DEV = 0, 1, 2
 
 
 class _Mat(C.Structure):
@@ -60,7 +61,9 @@ class _Problem(C.Structure):
                 ("first_step_zero_uK", C.c_int32), ("nthreads", C.c_int32),
                 ("forces", C.c_void_p), ("nforces", C.c_int64), ("gravity", C.c_double),
                 ("gravity_first", C.c_int32), ("loads", C.c_void_p), ("nloads", C.c_int64),
-                ("act_time", C.c_void_p), ("activation", C.c_int32), ("time", C.c_double)]
+                ("act_time", C.c_void_p), ("activation", C.c_int32), ("time", C.c_double),
+                ("viscosity", C.c_int32), ("visc_c1", C.c_double), ("visc_cl", C.c_double),
+                ("visc_h", C.c_double), ("visc_c0", C.c_double), ("F_prev", C.c_void_p)]
 
 
 class _Result(C.Structure):
@@ -212,6 +215,9 @@ class Solver:
     forces_out: tuple = None                  # *Forces: (frequency, [(node, direction), ...])
     outputs: int = 1                          # *Outputs: number of VTK outputs of the block
     activation: bool = False                  # *ACTIVATION: element birth at the activation times
+    # artificial viscosity (kind, c1, cl, h, c0): kind VISC_BULK (*Bulk viscosity) or VISC_DEV
+    # (*Dev viscosity); h and c0 stand for solvers::_elementSize and _c0, 0 in the reference
+    viscosity: tuple = None
 
 
 def cube_mesh(n: int, seed: int = 1234, jitter: float = 0.1) -> Mesh:
@@ -449,7 +455,17 @@ def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int 
         farr[i] = _Force(*f)
     larr, nl, _keep = loads.blocks(nn) if loads else (None, 0, None)
     act = None if mesh.act_time is None else np.ascontiguousarray(mesh.act_time, np.float64)
+    F_prev = None
     for k, s in enumerate(solvers):
+        visc = s.viscosity if s.viscosity and s.viscosity[0] in (VISC_BULK, VISC_DEV) else None
+        if visc is None:
+            F_prev = None
+        elif F_prev is None:
+            # the Gauss points' previous F: that of the current state (F = I from rest)
+            F_prev, f_scratch = np.zeros(9 * mesh.ne), np.zeros(3 * nn)
+            dphi, wJ, _ = precompute(mesh)
+            lib().orc_internal_force(nn, mesh.ne, _p(conn), _p(dphi), _p(wJ), _p(em), C.cast(marr, C.c_void_p),
+                                     _p(u), _p(f_scratch), _p(F_prev), None, 1)
         barr = (_BC * max(1, len(s.bcs)))()
         for i, (dof, mode, value, ramp) in enumerate(s.bcs):
             barr[i] = _BC(dof, mode, ramp, value)
@@ -458,7 +474,8 @@ def run(mesh: Mesh, mats, solvers, nthreads: int = 1, state=None, max_hist: int 
                         0, nthreads, C.cast(farr, C.c_void_p), len(fl),
                         loads.gravity() if loads else 0.0, loads.gravity_first() if loads else 0,
                         C.cast(larr, C.c_void_p) if nl else None, nl,
-                        _p(act), 1 if s.activation else 0, 0.0)
+                        _p(act), 1 if s.activation else 0, 0.0,
+                        visc[0] if visc else 0, *(visc[1:5] if visc else (0.0, 0.0, 0.0, 0.0)), _p(F_prev))
         hist = np.zeros(max(1, max_hist))
         rc = lib().orc_run(C.byref(prob), _p(u), _p(v), _p(a), _p(hist), max_hist, C.byref(res))
         total += res.steps
@@ -513,6 +530,7 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Load
         name, dtype, op, comp, nodes = ex
         lines += ["*EXTRACTION, NODE", "%s,%s,%s,%d" % (name, dtype, op, comp)]
         lines += ["%d" % (int(nd) + 1) for nd in nodes]
+    visc_seen = False
     for s in solvers:
         if any(b[1] == BC_VEL_RAMP for b in s.bcs):
             raise ValueError("the reference has no velocity-ramp boundary condition")
@@ -521,6 +539,15 @@ def write_deck(path: str, mesh: Mesh, mats, solvers, mat_elems=None, loads: Load
             raise ValueError("one *BOUNDARY block per solver: a single mode only")
         mode = modes.pop() if modes else BC_RAMP
         lines += ["*SOLVER, EXPLICIT"] + (["*ACTIVATION"] if s.activation else [])
+        if s.viscosity:
+            # the reader has no element size or c0 for these (solvers.h:53-54)
+            kind, c1, cl, h, c0 = s.viscosity
+            if h != 0 or c0 != 0:
+                raise ValueError("the reference has no element size or c0 for its artificial viscosity")
+            lines += ["*Bulk viscosity" if kind == VISC_BULK else "*Dev viscosity", "%.17g, %.17g" % (c1, cl)]
+        elif visc_seen:
+            raise ValueError("the reference keeps artificial viscosity on in later solver blocks")
+        visc_seen = visc_seen or bool(s.viscosity)
         lines += ["*Scale Factor", "%.17g" % s.scale_factor,
                   "*Outputs", "%d" % s.outputs, "*Time", "%.17g, %.17g" % (s.t0, s.tf),
                   "*BOUNDARY, TYPE=DISPLACEMENT " + ("INST" if mode == BC_INST else "RAMP")]

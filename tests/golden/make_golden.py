@@ -180,6 +180,16 @@ def cases(ref_src):
     out["cube4_stvk_pressure_ramp"] = (
         m4, [O.Material(stvk)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(4, 0.001))],
         O.Loads([("pressure_ramp", 0.0, 0.02, 8e3, S, el) for S, el in side4]))
+    # artificial viscosity: *Bulk viscosity in the first of two blocks (the reader
+    # keeps it on in the second) and *Dev viscosity; the reference runs them with
+    # its never-assigned element size and c0, which are 0 in its builds
+    bulk = (O.VISC_BULK, 0.5, 2.0, 0.0, 0.0)
+    out["cube3_cnh_bulk_viscosity"] = (
+        m3, [O.Material(cnh)], [O.Solver(0.0, 0.01, 0.5, O.cube_bcs(3, 0.002), viscosity=bulk),
+                                O.Solver(0.01, 0.02, 0.45, O.cube_bcs(3, 0.004), viscosity=bulk)])
+    out["cube3_stvk_dev_viscosity"] = (
+        m3, [O.Material(stvk)], [O.Solver(0.0, 0.02, 0.5, O.cube_bcs(3, 0.002),
+                                          viscosity=(O.VISC_DEV, 1.0, 0.5, 0.0, 0.0))])
     m10 = O.cube_mesh(10)
     for name, law in (("cnh", cnh), ("nh", nh), ("stvk", stvk)):
         out["cube10_%s_S" % name] = (m10, [O.Material(law)], [O.Solver(0.0, 0.5, 0.5, O.cube_bcs(10, 0.05))])
@@ -204,6 +214,8 @@ def pack(mesh, mats, solvers, ref, orc, loads=None, extractions=()):
         d["activation"] = np.array([int(s.activation) for s in solvers])
     if any(s.outputs != 1 for s in solvers):
         d["outputs"] = np.array([s.outputs for s in solvers])
+    if any(s.viscosity for s in solvers):
+        d["viscosity"] = np.array([s.viscosity or (0, 0.0, 0.0, 0.0, 0.0) for s in solvers], dtype=np.float64)
     if any(s.forces_out for s in solvers):
         import json
         d["forces_out_json"] = np.array(json.dumps([s.forces_out for s in solvers]))

@@ -32,6 +32,9 @@ def load(name):
     if "outputs" in d:
         for s, k in zip(solvers, d["outputs"]):
             s.outputs = int(k)
+    if "viscosity" in d:
+        for s, v in zip(solvers, d["viscosity"]):
+            s.viscosity = (int(v[0]),) + tuple(float(x) for x in v[1:]) if int(v[0]) else None
     if "forces_out_json" in d:
         import json
         for s, fo in zip(solvers, json.loads(str(d["forces_out_json"]))):

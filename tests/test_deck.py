@@ -107,6 +107,26 @@ def test_deck_outputs_follow_reference_cadence(tmp_path, name):
         assert np.all(np.abs(mine - refv) <= 6e-6 * np.abs(refv) + 1e-6 * scale)
 
 
+@pytest.mark.parametrize("param,c1,cl", [("0.5, 2", 0.5, 2.0), ("3", 0.06, 3.0), ("", 0.06, 1.2)])
+def test_parse_viscosity_keywords(tmp_path, param, c1, cl):
+    """*Bulk viscosity in the first of two solver blocks: the reader keeps it on
+    in the second (the reference never resets its flag) and reads "c1, cl" as
+    the reference's character scan does (a lone number is cl; defaults
+    0.06, 1.2)."""
+    write(tmp_path, "cube3_cnh_bulk_viscosity")
+    text = (tmp_path / "deck.inp").read_text()
+    first = text.index("*Bulk viscosity")
+    second = text.index("*Bulk viscosity", first + 1)
+    end = text.index("\n", text.index("\n", second) + 1) + 1
+    text = text[:second] + text[end:]                         # only the first block names it
+    text = text.replace("*Bulk viscosity\n0.5, 2\n", "*Bulk viscosity\n%s\n" % param)
+    (tmp_path / "deck.inp").write_text(text)
+    r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-parse-only"],
+                       capture_output=True, text=True, check=True)
+    blocks = json.loads(r.stdout)["blocks"]
+    assert [(b["visc"], b["visc_c1"], b["visc_cl"]) for b in blocks] == [(1, c1, cl)] * 2
+
+
 def test_parse_node_extractions(tmp_path):
     write(tmp_path, "cube3_cnh_extraction")
     r = subprocess.run([DECK, "-input", "deck.inp", "-inputDir", str(tmp_path), "-parse-only"],

@@ -34,11 +34,14 @@ def run_case(name, precision, spg=0):
         S.set_load_blocks(L.items)
     if mesh.act_time is not None:
         S.set_activation(mesh.act_time, s0.activation)
+    if s0.viscosity:
+        S.set_viscosity(*s0.viscosity)
     total = S.run().steps
     for s in solvers[1:]:
         S.next_solver(s.bcs, s.t0, s.tf, s.scale_factor, precision=precision, steps_per_graph=spg)
         if mesh.act_time is not None:
             S.set_activation(None, s.activation)
+        S.set_viscosity(*(s.viscosity or (msx.VISC_NONE,)))
         total += S.run().steps
     out = S.state()
     S.close()
@@ -383,4 +386,88 @@ def test_activation_api_errors_and_dead_elements():
     S.set_activation(None, False)                   # everyone alive again
     S.run(1)
     assert any(S.node_values(msx.FIELD_INTERNAL_FORCE, c, nodes).any() for c in range(3))
+    S.close()
+
+
+VISC = (msx.VISC_BULK, 1.5, 0.8, 0.05, 40.0)   # kind, c1, cl, element size, c0
+
+
+@pytest.mark.parametrize("law", [msx.COMPRESSIBLE_NH, msx.STVK])
+@pytest.mark.parametrize("precision,tol", [(msx.FP64_EXACT, 1e-12), (msx.FP64, 1e-10), (msx.DOUBLE_WORD, 1e-10),
+                                           (msx.MIXED, 1e-5)])
+def test_bulk_viscosity_matches_oracle(law, precision, tol):
+    """Bulk viscosity with an element size and c0 given (the reference leaves
+    both unset): a cube compressed over a two-block chain, the viscosity kept
+    on in the second block as the reference keeps it, against the oracle's
+    restatement of the reference's formula; the result differs from the
+    inviscid one by far more than the tolerance."""
+    mesh = O.cube_mesh(4)
+    solvers = [O.Solver(0.0, 0.01, 0.5, O.cube_bcs(4, -0.004), viscosity=VISC),
+               O.Solver(0.01, 0.02, 0.45, O.cube_bcs(4, -0.006), viscosity=VISC)]
+    ref = O.run(mesh, [O.Material(law)], solvers)
+    plain = O.run(mesh, [O.Material(law)], [O.Solver(s.t0, s.tf, s.scale_factor, s.bcs) for s in solvers])
+    assert rel(ref.u, plain.u) > 1e-3
+    S = msx.Solver(mesh.X, mesh.conn, [(law, 1e6, 0.3, 1000.0)], solvers[0].bcs, 0.0, 0.01, 0.5,
+                   precision=precision)
+    S.set_viscosity(*VISC)
+    steps = S.run().steps
+    S.next_solver(solvers[1].bcs, 0.01, 0.02, 0.45, precision=precision)
+    steps += S.run().steps
+    u, v, a = S.state()
+    S.close()
+    assert steps == ref.steps
+    assert rel(u, ref.u) <= tol, rel(u, ref.u)
+    assert rel(v, ref.v) <= 10 * tol
+
+
+def test_bulk_viscosity_across_a_precision_change():
+    """FP64, mixed, FP64 blocks with bulk viscosity: each block starts from the
+    handed-over state's F as the previous one, whatever the precision before."""
+    mesh = O.cube_mesh(4)
+    solvers = [O.Solver(0.0, 0.01, 0.5, O.cube_bcs(4, -0.004), viscosity=VISC),
+               O.Solver(0.01, 0.02, 0.5, O.cube_bcs(4, -0.006), viscosity=VISC),
+               O.Solver(0.02, 0.03, 0.5, O.cube_bcs(4, -0.007), viscosity=VISC)]
+    ref = O.run(mesh, [O.Material(O.COMPRESSIBLE_NH)], solvers)
+    S = msx.Solver(mesh.X, mesh.conn, [(msx.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0)], solvers[0].bcs, 0.0, 0.01, 0.5,
+                   precision=msx.FP64)
+    S.set_viscosity(*VISC)
+    steps = S.run().steps
+    for s, prec in zip(solvers[1:], (msx.MIXED, msx.FP64)):
+        S.next_solver(s.bcs, s.t0, s.tf, s.scale_factor, precision=prec)
+        steps += S.run().steps
+    u = S.state()[0]
+    S.close()
+    assert steps == ref.steps
+    assert rel(u, ref.u) <= 1e-5
+
+
+def test_zero_element_size_viscosity_is_bitwise_inviscid():
+    """The reference's own setting (element size and c0 never assigned, 0):
+    bulk and deviatoric viscosity leave the FP64 run bit for bit unchanged."""
+    X, conn = msx.mesh_cube(4, seed=3)
+    bcs = msx.cube_bcs(4, 0.002)
+    out = []
+    for visc in (None, (msx.VISC_BULK, 0.06, 1.2, 0.0, 0.0), (msx.VISC_DEV, 1.0, 0.5, 0.0, 0.0)):
+        S = msx.Solver(X, conn, [(msx.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0)], bcs, 0.0, 0.02, 0.5)
+        if visc:
+            S.set_viscosity(*visc)
+        S.run()
+        out.append(S.state())
+        S.close()
+    for o in out[1:]:
+        assert all(np.array_equal(x, y) for x, y in zip(o, out[0]))
+
+
+def test_bulk_viscosity_and_element_birth_are_refused_together():
+    X, conn = msx.mesh_cube(2)
+    S = msx.Solver(X, conn, [(msx.STVK, 1e6, 0.3, 1000.0)], [], 0.0, 0.01, 0.5)
+    S.set_activation(np.zeros(S.ne), True)
+    with pytest.raises(msx.MsxError) as ei:
+        S.set_viscosity(*VISC)
+    assert ei.value.status == 6
+    S.set_activation(None, False)
+    S.set_viscosity(*VISC)
+    with pytest.raises(msx.MsxError) as ei:
+        S.set_activation(None, True)
+    assert ei.value.status == 6
     S.close()

@@ -233,3 +233,53 @@ def test_print_forces_pinned_to_reference():
             if r.t >= s.tf - 1e-12:
                 break
         assert rows[1:] == expect, name
+
+
+def test_viscosity_keywords_leave_the_reference_unchanged():
+    """*Bulk viscosity and *Dev viscosity: the reference multiplies by its
+    element size and c0, which it never assigns (0 in its builds), and its
+    deviatoric branch maps a zero tensor, so its results with the keywords are
+    bit for bit those without them (golden fixtures from the reference)."""
+    for name in ("cube3_cnh_bulk_viscosity", "cube3_stvk_dev_viscosity"):
+        mesh, mats, solvers, (u, v, a), steps = load(name)
+        assert all(s.viscosity for s in solvers)
+        plain = [O.Solver(s.t0, s.tf, s.scale_factor, s.bcs) for s in solvers]
+        r = O.run(mesh, mats, plain)
+        assert r.steps == steps
+        assert np.array_equal(r.u, u) and np.array_equal(r.v, v) and np.array_equal(r.a, a)
+
+
+@pytest.mark.parametrize("law", [O.COMPRESSIBLE_NH, O.STVK])
+def test_bulk_viscosity_force_matches_its_formula(law):
+    """One step from rest with bulk viscosity (element size and c0 given): the
+    acceleration changes by -f_vis/m on the free DOFs against the same step
+    without it, with f_vis = wJ B^T P_vis, P_vis = J qBV F^-T,
+    qBV = rho/J h (c1^2 h |trD| min(0, trD) + cl c0 trD) and trD = tr(F - I)/dt
+    (solverExplicit.cpp:381-421, 514-541), evaluated here in numpy."""
+    mesh = O.cube_mesh(3)
+    bcs = O.cube_bcs(3, -0.004)             # the top moves down: trD < 0 near it
+    mat = O.Material(law)
+    h, c1, cl, c0 = 0.05, 1.5, 0.8, 40.0
+    base = O.run(mesh, [mat], [O.Solver(0.0, 1.0, 0.5, bcs, max_steps=1)])
+    vis = O.run(mesh, [mat], [O.Solver(0.0, 1.0, 0.5, bcs, max_steps=1, viscosity=(O.VISC_BULK, c1, cl, h, c0))])
+    assert np.array_equal(base.u, vis.u) and base.dt_last == vis.dt_last
+    dt, nn = vis.dt_last, mesh.nn
+    dphi, wJ, _ = O.precompute(mesh)
+    f = np.zeros(3 * nn)
+    for e in range(mesh.ne):
+        nd = mesh.conn[e]
+        g = dphi[e].reshape(4, 3)
+        F = np.eye(3) + sum(np.outer(vis.u[nd[a] + nn * np.arange(3)], g[a]) for a in range(4))
+        trD = np.trace(F - np.eye(3)) / dt
+        J = np.linalg.det(F)
+        q = mat.rho / J * h * (c1 * c1 * h * abs(trD) * min(0.0, trD) + cl * c0 * trD)
+        P = J * q * np.linalg.inv(F).T
+        for a in range(4):
+            f[nd[a] + nn * np.arange(3)] += wJ[e] * P @ g[a]
+    m = O.lumped_mass(mesh, [mat], wJ)
+    free = np.ones(3 * nn, bool)
+    free[[b[0] for b in bcs]] = False
+    want = -f[free] / np.tile(m, 3)[free]
+    got = (vis.a - base.a)[free]
+    assert np.abs(want).max() > 0
+    assert np.abs(got - want).max() <= 1e-9 * np.abs(want).max()

@@ -20,7 +20,8 @@
 // St-Venant-Kirchhoff}, *Linear-Elastic, *INITINTVARS and *List of Elements
 // (:838-1029, 2010-2111), *SOLVER, EXPLICIT ... *END SOLVER with *ACTIVATION,
 // *Scale Factor, *Outputs, *Time, *Forces and *BOUNDARY, TYPE=DISPLACEMENT
-// RAMP|INST (:2253-2831, 2960-3218, 4830-4886), the Neumann blocks *BOUNDARY,
+// RAMP|INST and *Bulk viscosity / *Dev viscosity (:2253-2831, 2960-3218,
+// 4830-4886), the Neumann blocks *BOUNDARY,
 // TYPE=FORCE | TRACTION INST|RAMP | PRESSURE INST|RAMP and *GRAVITY
 // (:4705-4760, 2841-2945), and *EXTRACTION, NODE | ELEMENT (:4950-5111).
 // Other keywords belong to paths this library does not implement and are
@@ -53,6 +54,10 @@ struct SolverBlock {
     double force_freq = 0;
     std::vector<std::pair<int32_t, int>> force_out;
     bool activation = false;          // *ACTIVATION (element birth)
+    // *Bulk viscosity / *Dev viscosity (IO/inputFile.cpp:2462-2511): kind and "c1, cl";
+    // once read, later blocks keep it (the reader never resets its flag)
+    int visc = MSX_VISC_NONE;
+    double visc_c1 = 0, visc_cl = 0;
 };
 
 struct Deck {
@@ -121,6 +126,8 @@ Deck parse(const std::string &path)
     for (std::string l; std::getline(in, l);) lines.push_back(trim(l));
     Deck d;
     bool instantaneous = false;
+    int visc = MSX_VISC_NONE;         // the artificial viscosity read so far (kept across blocks)
+    double visc_c1 = 0, visc_cl = 0;
     const size_t n = lines.size();
     size_t i = 0;
     auto data_line = [&](size_t k) { return k < n && !lines[k].empty() && lines[k][0] != '*'; };
@@ -327,6 +334,31 @@ Deck parse(const std::string &path)
                 } else if (starts(K, "*ACTIVATION")) {
                     s.activation = true;   // IO/inputFile.cpp:2332-2334
                     i++;
+                } else if (starts(K, "*Bulk viscosity") || starts(K, "*Dev viscosity")) {
+                    // IO/inputFile.cpp:2462-2511: defaults (0.06, 1.2) and (1, 0.5); the next
+                    // line is always consumed and read as "c1, cl": spaces are skipped, each
+                    // comma sets c1 from the characters before it, the line's last character
+                    // closes cl, and a '*' ends the scan (no parameters)
+                    const bool bulk = starts(K, "*Bulk");
+                    visc = bulk ? MSX_VISC_BULK : MSX_VISC_DEV;
+                    visc_c1 = bulk ? 0.06 : 1.0;
+                    visc_cl = bulk ? 1.2 : 0.5;
+                    if (i + 1 < n) {
+                        const std::string &T = lines[i + 1];
+                        std::string tok;
+                        for (size_t c = 0; c < T.size(); c++) {
+                            if (T[c] == '*') break;
+                            if (T[c] == ' ') continue;
+                            if (T[c] == ',') {
+                                visc_c1 = atof(tok.c_str());
+                                tok.clear();
+                            } else {
+                                tok += T[c];
+                                if (c == T.size() - 1) visc_cl = atof(tok.c_str());
+                            }
+                        }
+                    }
+                    i += 2;
                 } else if (starts(K, "*Forces")) {
                     if (i + 1 >= n) die("*Forces needs a frequency", (int)i + 1);
                     s.force_freq = atof(lines[i + 1].c_str());
@@ -347,6 +379,9 @@ Deck parse(const std::string &path)
                 }
             }
             if (s.outputs < 0) die("*Outputs is required in an explicit solver block", ln);
+            s.visc = visc;
+            s.visc_c1 = visc_c1;
+            s.visc_cl = visc_cl;
             d.solvers.push_back(s);
             i++;
         } else if (starts(L, "*END")) {
@@ -598,10 +633,11 @@ int main(int argc, char **argv)
         printf(", \"blocks\": [");
         for (size_t k = 0; k < d.solvers.size(); k++)
             printf("%s{\"t0\": %.17g, \"tf\": %.17g, \"sf\": %.17g, \"bcs\": %zu, \"inst\": %d, "
-                   "\"force_freq\": %.17g, \"force_out\": %zu}", k ? ", " : "",
+                   "\"force_freq\": %.17g, \"force_out\": %zu, \"visc\": %d, \"visc_c1\": %.17g, "
+                   "\"visc_cl\": %.17g}", k ? ", " : "",
                    d.solvers[k].t0, d.solvers[k].tf, d.solvers[k].sf, d.solvers[k].bcs.size(),
                    d.solvers[k].bcs.empty() ? 0 : d.solvers[k].bcs[0].mode == MSX_BC_INST, d.solvers[k].force_freq,
-                   d.solvers[k].force_out.size());
+                   d.solvers[k].force_out.size(), d.solvers[k].visc, d.solvers[k].visc_c1, d.solvers[k].visc_cl);
         printf("]}\n");
         return 0;
     }
@@ -631,6 +667,9 @@ int main(int argc, char **argv)
             }
             st = msx_next_solver(h, s.bcs.data(), (int64_t)s.bcs.size(), &o);
         }
+        // artificial viscosity with the element size and c0 the reference runs with: 0
+        // (solvers.h:53-54 are never assigned), which makes its force zero
+        if (st == MSX_OK) st = msx_set_viscosity(h, s.visc, s.visc_c1, s.visc_cl, 0.0, 0.0);
         // element birth: the activation times once, the block's *ACTIVATION flag each block
         if (st == MSX_OK && !d.act_time.empty())
             st = msx_set_activation(h, k == 0 ? d.act_time.data() : nullptr, s.activation ? 1 : 0);

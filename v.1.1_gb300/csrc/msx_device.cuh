@@ -11,6 +11,8 @@
 namespace msx {
 
 #define MSX_INF_BITS 0x7FF0000000000000ULL
+// FP32 +infinity as the running minimum of the CFL screen (dtmin[2..3])
+constexpr unsigned long long kScreenInfBits = 0x7F800000ULL;
 
 // ---------------------------------------------------------------------------
 // Reference-order arithmetic (src/mathematics/maths.cpp, geometry.cpp and the
@@ -739,6 +741,7 @@ __device__ __forceinline__ void publish_step(const Problem &p, const StepDecisio
 {
     p.ctrl[parity] = d.next;
     p.dtmin[parity ^ 1] = MSX_INF_BITS;
+    p.dtmin[2 + (parity ^ 1)] = kScreenInfBits;
     p.flags[parity ^ 1] = 0;
 }
 
@@ -784,7 +787,7 @@ __device__ __forceinline__ double cfl_exact_ref(const Problem &p, long long e)
 
 // SCREEN: return the FP32 screen value of the CFL (cfl_screen) instead of the
 // exact one; the caller rechecks the elements near its block's minimum.
-template <bool FORCE_ONLY, bool SCREEN = false>
+template <bool FORCE_ONLY, bool SCREEN = false, bool VISC = false>
 __device__ __forceinline__ double elem_body_exact(const Problem &p, long long e, int parity)
 {
     const long long ne = p.ne, nn = p.nn;
@@ -820,6 +823,43 @@ __device__ __forceinline__ double elem_body_exact(const Problem &p, long long e,
         double wJ = p.wJ[e];
         double *fe = p.fe + e * 12;
         const bool dead = !FORCE_ONLY && elem_dead(p, e, p.ctrl[parity].t);
+        double Pv[9];
+        if (VISC && !FORCE_ONLY) {
+            // bulkViscosity in the reference's order (solverExplicit.cpp:514-541; sumTensorTensor,
+            // multiSTensorScalar, getTrace, multSTensor3SecondTranspose: maths.cpp:1169-1175,
+            // 1604-1610, 2257-2286); F_prev's diagonal rolls to F's
+            double *f0 = p.visc_f0;
+            const double dt = p.ctrl[parity].dt;
+            double Fd[3] = {0., 0., 0.};
+            if (dt != 0) {
+                const double r = 1 / dt;
+#pragma unroll
+                for (int c = 0; c < 3; c++) Fd[c] = (F[c * 4] + (-1) * f0[c * ne + e]) * r;
+            }
+            double trD = 0;
+#pragma unroll
+            for (int c = 0; c < 3; c++) trD += Fd[c];
+#pragma unroll
+            for (int c = 0; c < 3; c++) f0[c * ne + e] = F[c * 4];
+            const double J1 = det3_ref(F);
+            const double Rho_1 = m.rho / J1;
+            const double qBV = Rho_1 * p.visc_h *
+                               (p.visc_c1 * p.visc_c1 * p.visc_h * fabs(trD) * ((trD < 0.) ? trD : 0.) +
+                                p.visc_cl * p.visc_c0 * trD);
+            double Cv[9], iF[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) Cv[k] = (k % 4 == 0) ? -1 * qBV : 0.0;
+            inv3_ref(F, iF);
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    double s = 0;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) s += Cv[i * 3 + k] * iF[j * 3 + k];
+                    Pv[i * 3 + j] = s * (-1 * J1);
+                }
+        }
 #pragma unroll
         for (int a = 0; a < 4; a++)
 #pragma unroll
@@ -827,7 +867,11 @@ __device__ __forceinline__ double elem_body_exact(const Problem &p, long long e,
                 double f = 0;
 #pragma unroll
                 for (int J = 0; J < 3; J++) f += wJ * P[i * 3 + J] * dphi[a * 3 + J];
-                fe[a * 3 + i] = dead ? 0.0 : 0 + f;
+                f = 0 + f;
+                if (VISC && !FORCE_ONLY)   // the viscous pass's terms, as computeInternalForce adds them
+#pragma unroll
+                    for (int J = 0; J < 3; J++) f += wJ * Pv[i * 3 + J] * dphi[a * 3 + J];
+                fe[a * 3 + i] = dead ? 0.0 : f;
             }
         if (!FORCE_ONLY && SCREEN) {
             float du32[9];
@@ -881,6 +925,38 @@ __device__ __forceinline__ void cofactor(const double *F, double *K)
     K[6] = F[1] * F[5] - F[2] * F[4];
     K[7] = F[2] * F[3] - F[0] * F[5];
     K[8] = F[0] * F[4] - F[1] * F[3];
+}
+
+// Artificial bulk viscosity (the second pass of computeInternalForce,
+// solverExplicit.cpp:381-421, with bulkViscosity, :514-541): the viscous
+// Cauchy stress -qBV I maps to the Piola stress J qBV F^-T = qBV cof(F), with
+// qBV = rho/J h (c1^2 h |trD| min(0, trD) + cl c0 trD) and trD = tr(Fdot),
+// Fdot = (F - F_prev)/dt.  Only F_prev's diagonal enters, so that is what an
+// element keeps; h and c0 stand for the reference's solvers::_elementSize and
+// _c0.  FP64 form; the mixed and reference-order forms sit in their bodies.
+__device__ __forceinline__ double visc_q(const Problem &p, double rho, double J, double trD)
+{
+    return rho / J * p.visc_h * (p.visc_c1 * p.visc_c1 * p.visc_h * fabs(trD) * fmin(0.0, trD) +
+                                 p.visc_cl * p.visc_c0 * trD);
+}
+
+// P += wJ qBV cof(F) for F in FP64 (FP64 and double-word modes); rolls the
+// element's F_prev diagonal to F's.
+__device__ __forceinline__ void visc_bulk_fp64(const Problem &p, long long e, const double *F, double wJ, double rho,
+                                               double idt, double *Pv)
+{
+    const long long ne = p.ne;
+    double *f0 = p.visc_f0;
+    const double trD = ((F[0] - f0[e]) + (F[4] - f0[ne + e]) + (F[8] - f0[2 * ne + e])) * idt;
+    f0[e] = F[0];
+    f0[ne + e] = F[4];
+    f0[2 * ne + e] = F[8];
+    double K[9];
+    cofactor(F, K);
+    const double J = F[0] * K[0] + F[1] * K[1] + F[2] * K[2];
+    const double w = wJ * visc_q(p, rho, J, trD);
+#pragma unroll
+    for (int k = 0; k < 9; k++) Pv[k] = w * K[k];
 }
 
 // ln J for J = det F in FP64.  For |J - 1| < 2^-7 (the usual case) the
@@ -1045,8 +1121,9 @@ __device__ __forceinline__ float cfl_screen(const Problem &p, long long e, const
 // the 4th corner force as minus the sum of the other three.  Same algebra as
 // the reference, about half its FP64 operations.  Returns the FP32 CFL screen
 // value (see cfl_screen).
-template <bool FORCE_ONLY, bool ACT = false>
-__device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, int parity, double t = 0.0)
+template <bool FORCE_ONLY, bool ACT = false, bool VISC = false>
+__device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, int parity, double t = 0.0,
+                                                double idt = 0.0)
 {
     const long long ne = p.ne, nn = p.nn;
     int4 cn = p.conn[e];
@@ -1071,6 +1148,12 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
                                                                              : du[6 + i] * G[6 + j]));
     const MatParams &m = mat_of(p, e);
     stress_fast(m, F, __ldg(p.wJ + e), P);
+    if (VISC && !FORCE_ONLY) {
+        double Pv[9];
+        visc_bulk_fp64(p, e, F, __ldg(p.wJ + e), m.rho, idt, Pv);
+#pragma unroll
+        for (int k = 0; k < 9; k++) P[k] += Pv[k];
+    }
     double f[12];
 #pragma unroll
     for (int a = 1; a < 4; a++)
@@ -1185,8 +1268,9 @@ __device__ __forceinline__ void stress_mixed(const MatParams &m, const float *H,
     }
 }
 
-template <bool FORCE_ONLY, bool ACT = false>
-__device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, int parity, int4 cn, double t = 0.0)
+template <bool FORCE_ONLY, bool ACT = false, bool VISC = false>
+__device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, int parity, int4 cn, double t = 0.0,
+                                                 float idtf = 0.0f)
 {
     const long long ne = p.ne, nn = p.nn;
     float vmin = INFINITY;
@@ -1230,6 +1314,25 @@ __device__ __forceinline__ float elem_body_mixed(const Problem &p, long long e, 
         const MatParams &m = mat_of(p, e);
         float P[9];
         stress_mixed(m, H, Jm1, lnJ, tf, I2f, P);
+        if (VISC && !FORCE_ONLY) {
+            // bulk viscosity in FP32: P += qBV cof(I + H) = qBV (I + D), D as in stress_mixed
+            float *h0 = p.visc_h0;
+            const float trD = ((H[0] - h0[e]) + (H[4] - h0[ne + e]) + (H[8] - h0[2 * ne + e])) * idtf;
+            h0[e] = H[0];
+            h0[ne + e] = H[4];
+            h0[2 * ne + e] = H[8];
+            const float q = m.rho_f / (1.0f + Jm1) * p.visc_hf *
+                            (p.visc_c1sq_hf * fabsf(trD) * fminf(0.0f, trD) + p.visc_clc0f * trD);
+            const float a0 = tf + I2f, a1 = 1.0f + tf;
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    const float h2 = H[j * 3] * H[i] + H[j * 3 + 1] * H[3 + i] + H[j * 3 + 2] * H[6 + i];
+                    const float Dij = (i == j ? a0 : 0.0f) - a1 * H[j * 3 + i] + h2;
+                    P[i * 3 + j] += q * ((i == j ? 1.0f : 0.0f) + Dij);
+                }
+        }
         float wJ = __ldg(p.wJ32 + e);
 #pragma unroll
         for (int k = 0; k < 9; k++) P[k] *= wJ;
@@ -1540,8 +1643,9 @@ static __device__ __noinline__ double cfl_dw(const Problem &p, long long e)
     return ((dist < Lr) ? dist : Lr) / mat_of(p, e).c;
 }
 
-template <bool FORCE_ONLY, bool ACT = false>
-__device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int parity, int4 cn, double t = 0.0)
+template <bool FORCE_ONLY, bool ACT = false, bool VISC = false>
+__device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int parity, int4 cn, double t = 0.0,
+                                              double idt = 0.0)
 {
     const long long ne = p.ne, nn = p.nn;
     int nd[4] = {cn.x, cn.y, cn.z, cn.w};
@@ -1563,6 +1667,15 @@ __device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int
             F[i * 3 + j] = dw_dot3(du[i], G[j], du[3 + i], G[3 + j], du[6 + i], G[6 + j], i == j ? 1.0f : 0.0f);
     const MatParams &m = mat_of(p, e);
     stress_dw(m, F, make_float2(__ldg(p.wJ32 + e), __ldg(p.wJ32lo + e)), P);
+    if (VISC && !FORCE_ONLY) {
+        // bulk viscosity in FP64 from the double-word F (exact as doubles), added as double-words
+        double Fd[9], Pv[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) Fd[k] = (double)F[k].x + (double)F[k].y;
+        visc_bulk_fp64(p, e, Fd, (double)__ldg(p.wJ32 + e) + (double)__ldg(p.wJ32lo + e), m.rho, idt, Pv);
+#pragma unroll
+        for (int k = 0; k < 9; k++) P[k] = dw_add(P[k], dw_from(Pv[k]));
+    }
     float2 f[12];
 #pragma unroll
     for (int a = 1; a < 4; a++)
@@ -1700,11 +1813,12 @@ __device__ __forceinline__ float block_min_bcast(float v);
 // reference's order for every element, the exact reference-order CFL value only
 // for the elements of the block within 2^-8 of its FP32 minimum (and slivers),
 // a set that always holds the block's exact minimum, so dt is the reference's.
-static __global__ void __launch_bounds__(kElemBlock) elem_kernel_exact_screened(Problem p, int parity)
+template <bool VISC>
+__global__ void __launch_bounds__(kElemBlock) elem_kernel_exact_screened(Problem p, int parity)
 {
     if (!p.ctrl[parity].ran) return;
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const float d = e < p.ne ? (float)elem_body_exact<false, true>(p, e, parity) : INFINITY;
+    const float d = e < p.ne ? (float)elem_body_exact<false, true, VISC>(p, e, parity) : INFINITY;
     const float bmin = block_min_bcast(d >= 0.0f ? d : INFINITY);
     double v = INFINITY;
     if (e < p.ne && (d < 0.0f || d <= bmin * (1.0f + 1.0f / 256.0f))) v = cfl_exact_ref(p, e);
@@ -1795,11 +1909,13 @@ __global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *
 // element's connectivity loaded one element ahead, so their node gathers wait
 // for one memory latency instead of two (connectivity, then the nodes).  ACT:
 // element birth is on, and the step's time decides which elements are dead.
-template <int MODE, bool ACT>
+template <int MODE, bool ACT, bool VISC>
 __device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl, int parity, float *sdt)
 {
     float v32 = INFINITY;
     const double t = ACT ? p.ctrl[parity].t : 0.0;
+    const double idt = VISC ? 1.0 / p.ctrl[parity].dt : 0.0;   // the step's dt (bulk viscosity)
+    const float idtf = (float)idt;
     long long e = tl.begin + threadIdx.x;
     int4 cn_next = make_int4(0, 0, 0, 0);
     if (MODE == MODE_MIXED || MODE == MODE_DW) {
@@ -1808,9 +1924,9 @@ __device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl,
     for (; e < tl.end; e += blockDim.x) {
         const int4 cn = cn_next;
         if ((MODE == MODE_MIXED || MODE == MODE_DW) && e + blockDim.x < tl.end) cn_next = p.conn[e + blockDim.x];
-        float d = MODE == MODE_MIXED ? elem_body_mixed<false, ACT>(p, e, parity, cn, t)
-                                     : (MODE == MODE_DW ? elem_body_dw<false, ACT>(p, e, parity, cn, t)
-                                                        : elem_body_fp64<false, ACT>(p, e, parity, t));
+        float d = MODE == MODE_MIXED ? elem_body_mixed<false, ACT, VISC>(p, e, parity, cn, t, idtf)
+                                     : (MODE == MODE_DW ? elem_body_dw<false, ACT, VISC>(p, e, parity, cn, t, idt)
+                                                        : elem_body_fp64<false, ACT, VISC>(p, e, parity, t, idt));
         sdt[e - tl.begin] = d;
         if (d >= 0.0f) v32 = fminf(v32, d);
     }
@@ -1819,16 +1935,17 @@ __device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl,
 
 // Element kernel over tiles.  Every element's FP32 CFL screen value is kept in
 // shared memory; after the tile's FP32 minimum is known, elements within 2^-8
-// of it (and slivers) recompute the exact FP64 value, whose minimum goes to
-// the solve's CFL slot.  The screen's error stays far below 2^-9 outside
-// slivers, so that set always holds the tile's exact minimum.  FP64 and
+// of the solve's running FP32 minimum (and slivers) recompute the exact FP64
+// value, whose minimum goes to the solve's CFL slot.  The screen's error stays
+// far below 2^-9 outside slivers, so that set always holds the step's exact
+// minimum.  FP64 and
 // double-word list the candidates and recompute them by consecutive threads;
 // mixed tiles have a candidate or two, which each thread recomputes among its
 // own elements (no list, no extra barrier), and keep their screen values in
 // dynamic shared memory of 4 bytes per tile element.  ACT: the instantiation
-// with element birth (single solves whose block has it on); the other one
-// carries no trace of it.
-template <int MODE, bool ACT = false>
+// with element birth (single solves whose block has it on), VISC the one with
+// artificial bulk viscosity; the plain one carries no trace of either.
+template <int MODE, bool ACT = false, bool VISC = false>
 __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE == MODE_DW ? 3 : 2)) pool_elem_kernel(const Problem *__restrict__ descs,
                                                                  const Tile *__restrict__ tiles,
                                                                  int *__restrict__ sched, int parity)
@@ -1837,6 +1954,7 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
     __shared__ float sdt_static[MODE == MODE_MIXED ? 1 : kMaxTileElems];
     __shared__ unsigned short scand[MODE == MODE_MIXED ? 1 : kMaxTileElems];
     __shared__ int s_tile, s_ncand;
+    __shared__ float s_thr;
     float *sdt = MODE == MODE_MIXED ? reinterpret_cast<float *>(dyn_smem) : sdt_static;
     TileQueue q{sched, sched[0]};
     if (threadIdx.x == 0) s_tile = q.claim();
@@ -1849,11 +1967,27 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
         const Problem &p = descs[tl.solve];
         if (p.ctrl[parity].ran) {
             if (MODE != MODE_MIXED && threadIdx.x == 0) s_ncand = 0;
-            const float v32 = tile_elements<MODE, ACT>(p, tl, parity, sdt);
-            float bmin = block_min_bcast(v32);   // also orders the sdt writes before the reads below
+            const float v32 = tile_elements<MODE, ACT, VISC>(p, tl, parity, sdt);
+            const float bmin = block_min_bcast(v32);   // also orders the sdt writes before the reads below
+            if (threadIdx.x == 0) {
+                // g: the solve's smallest FP32 screen value over the tiles closed
+                // so far in this step, this one included.  g >= the step's FP32
+                // minimum m, and the exact minimum's screen value is <= m (1 + 2^-8)
+                // (screen error below 2^-9 outside slivers), so elements above
+                // g (1 + 2^-8) are never the exact minimum: most tiles skip the
+                // FP64 recheck, whichever order they close in.
+                float g = bmin;
+                if (bmin < INFINITY) {
+                    const unsigned long long old =
+                        atomicMin(p.dtmin + 2 + (parity ^ 1), (unsigned long long)__float_as_uint(bmin));
+                    g = old >= kScreenInfBits ? bmin : fminf(__uint_as_float((unsigned)old), bmin);
+                }
+                s_thr = g * (1.0f + 1.0f / 256.0f);
+            }
+            __syncthreads();
+            const float thr = s_thr;
             if (MODE == MODE_MIXED) {
                 // a thread reads back only the entries it wrote itself
-                const float thr = bmin * (1.0f + 1.0f / 256.0f);
                 double v = INFINITY;
                 for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
                     const float d = sdt[e - tl.begin];
@@ -1864,19 +1998,20 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
             } else {
                 // the tile's candidates are listed first and then recomputed by
                 // consecutive threads, so a few candidates take one warp, not several
-                const float thr = bmin * (1.0f + 1.0f / 256.0f);
                 for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
                     float d = sdt[e - tl.begin];
                     if (d < 0.0f || d <= thr) scand[atomicAdd(&s_ncand, 1)] = (unsigned short)(e - tl.begin);
                 }
                 __syncthreads();
                 const int nc = s_ncand;
-                double v = INFINITY;
-                for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-                    const long long e = tl.begin + scand[c];
-                    v = fmin(v, MODE == MODE_DW ? cfl_dw(p, e) : cfl_fp64(p, e));
+                if (nc > 0) {   // uniform across the block
+                    double v = INFINITY;
+                    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+                        const long long e = tl.begin + scand[c];
+                        v = fmin(v, MODE == MODE_DW ? cfl_dw(p, e) : cfl_fp64(p, e));
+                    }
+                    block_min_to(v, p.dtmin + (parity ^ 1));
                 }
-                block_min_to(v, p.dtmin + (parity ^ 1));
             }
         }
         __syncthreads();
@@ -1959,6 +2094,33 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
     for (int a = 1; a < 4; a++)
 #pragma unroll
         for (int i = 0; i < 3; i++) Eref32[((a - 1) * 3 + i) * ne + e] = (float)(pts[a * 3 + i] - pts[i]);
+}
+
+// Previous-step F diagonal for the bulk viscosity, from displacement u, in the
+// reference's order of F (constitutiveManager.cpp:151-164): what the Gauss
+// points' previous state holds at the start of a block (the last step's F, or
+// I from rest).
+__global__ void visc_init_kernel(Problem p, const double *u)
+{
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.ne) return;
+    const long long ne = p.ne, nn = p.nn;
+    const int4 cn = p.conn[e];
+    const int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    double dphi[12];
+#pragma unroll
+    for (int k = 0; k < 9; k++) dphi[3 + k] = p.G[k * ne + e];
+#pragma unroll
+    for (int j = 0; j < 3; j++) dphi[j] = (-dphi[3 + j] - dphi[6 + j]) - dphi[9 + j];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        double F = 0.;
+        F += 1.;
+#pragma unroll
+        for (int a = 0; a < 4; a++) F += dphi[a * 3 + i] * u[nd[a] + i * nn];
+        if (p.visc_f0) p.visc_f0[i * ne + e] = F;
+        if (p.visc_h0) p.visc_h0[i * ne + e] = (float)(F - 1.0);
+    }
 }
 
 // constitutiveAlgorithms.cpp:191-205 (rho wJ phi_a phi_b summed over b) and

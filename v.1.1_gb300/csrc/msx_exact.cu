@@ -15,7 +15,10 @@ void launch_node_exact(const Problem &p, int parity, cudaStream_t s)
 
 void launch_elem_exact(const Problem &p, int parity, cudaStream_t s)
 {
-    elem_kernel_exact_screened<<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, parity);
+    if (p.visc)
+        elem_kernel_exact_screened<true><<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, parity);
+    else
+        elem_kernel_exact_screened<false><<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, parity);
 }
 
 void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s)
@@ -24,6 +27,11 @@ void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s)
         p, X, const_cast<double *>(p.G), const_cast<double *>(p.wJ), const_cast<double *>(p.Lref),
         const_cast<float *>(p.G32), const_cast<float *>(p.wJ32), const_cast<float *>(p.Lref32),
         const_cast<float *>(p.Eref32));
+}
+
+void launch_visc_init(const Problem &p, const double *u, cudaStream_t s)
+{
+    visc_init_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, u);
 }
 
 void launch_setup_mass(const Problem &p, double *mass, double *minv, cudaStream_t s)

@@ -34,19 +34,29 @@ void launch_tiled_node(const Problem *descs, const Tile *ntiles, int *counts, in
         pool_node_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, ntiles, counts + 3, parity);
 }
 
-void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, int mode, int parity, int grid,
-                       int threads, int tile_elems, cudaStream_t s, bool act)
+template <int MODE>
+static void launch_elem_variant(const Problem *descs, const Tile *etiles, int *counts, int parity, int grid,
+                                int threads, size_t smem, cudaStream_t s, bool act, bool visc)
 {
-    const size_t smem = sizeof(float) * (size_t)tile_elems;   // mixed: FP32 CFL screen values of a tile
-    if (mode == MODE_MIXED)
-        act ? pool_elem_kernel<MODE_MIXED, true><<<grid, threads, smem, s>>>(descs, etiles, counts, parity)
-            : pool_elem_kernel<MODE_MIXED><<<grid, threads, smem, s>>>(descs, etiles, counts, parity);
-    else if (mode == MODE_DW)
-        act ? pool_elem_kernel<MODE_DW, true><<<grid, threads, 0, s>>>(descs, etiles, counts, parity)
-            : pool_elem_kernel<MODE_DW><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
+    // element birth and bulk viscosity are separate instantiations (never both: the host refuses that)
+    if (act)
+        pool_elem_kernel<MODE, true><<<grid, threads, smem, s>>>(descs, etiles, counts, parity);
+    else if (visc)
+        pool_elem_kernel<MODE, false, true><<<grid, threads, smem, s>>>(descs, etiles, counts, parity);
     else
-        act ? pool_elem_kernel<MODE_FP64, true><<<grid, threads, 0, s>>>(descs, etiles, counts, parity)
-            : pool_elem_kernel<MODE_FP64><<<grid, threads, 0, s>>>(descs, etiles, counts, parity);
+        pool_elem_kernel<MODE><<<grid, threads, smem, s>>>(descs, etiles, counts, parity);
+}
+
+void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, int mode, int parity, int grid,
+                       int threads, int tile_elems, cudaStream_t s, bool act, bool visc)
+{
+    if (mode == MODE_MIXED)   // the mixed kernel keeps its FP32 CFL screen values in dynamic shared memory
+        launch_elem_variant<MODE_MIXED>(descs, etiles, counts, parity, grid, threads,
+                                        sizeof(float) * (size_t)tile_elems, s, act, visc);
+    else if (mode == MODE_DW)
+        launch_elem_variant<MODE_DW>(descs, etiles, counts, parity, grid, threads, 0, s, act, visc);
+    else
+        launch_elem_variant<MODE_FP64>(descs, etiles, counts, parity, grid, threads, 0, s, act, visc);
 }
 
 __global__ void state_split_kernel(Problem p)

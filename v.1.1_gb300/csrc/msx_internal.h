@@ -24,7 +24,7 @@ struct MatParams {
     double lambda, mu, K1;        // NH / compressible NH
     double mu2, lam_stvk;         // StVK: E/(1+nu), E nu/((1+nu)(1-2nu))
     double c;                     // sound speed used by the CFL
-    float lambda_f, mu_f, K1_f, mu2_f, lam_stvk_f, inv_c_f;
+    float lambda_f, mu_f, K1_f, mu2_f, lam_stvk_f, inv_c_f, rho_f;
     float2 lambda_w, mu_w, K1_w, mu2_w, lam_stvk_w, mu3_w;   // double-word copies (mu3 = mu/3)
 };
 
@@ -129,9 +129,22 @@ struct Problem {
     double *fcon;
     const FaceLoad *faces;
     int nfaces;
+    // Artificial bulk viscosity (*Bulk viscosity with a nonzero element size;
+    // solverExplicit.cpp:381-421, 514-541).  visc != 0: the element kernels add
+    // the viscous stress qBV cof(F), qBV = rho/J h (c1^2 h |trD| min(0, trD) +
+    // cl c0 trD), trD = tr(F - F_prev)/dt, and roll each element's F_prev
+    // diagonal: visc_f0 (3*ne, F_ii, FP64, exact and double-word modes) or
+    // visc_h0 (3*ne, H_ii = F_ii - 1, mixed mode), SoA by component.
+    int visc;
+    double *visc_f0;
+    float *visc_h0;
+    double visc_h, visc_c1, visc_cl, visc_c0;
+    float visc_hf, visc_c1sq_hf, visc_clc0f;   // h, c1^2 h and cl c0 in FP32 (mixed mode)
     // control
     Ctrl *ctrl;                       // [2]
-    unsigned long long *dtmin;        // [2] bit patterns of positive doubles
+    unsigned long long *dtmin;        // [4]: [0..1] bit patterns of positive doubles (the CFL
+                                      // minimum by step parity); [2..3] FP32 bit patterns of the
+                                      // running minimum of the elements' FP32 CFL screen
     int *flags;                       // [2] NaN flag raised by the element kernel
     double sf, tf;
 };
@@ -156,9 +169,9 @@ void launch_tiled_node(const Problem *descs, const Tile *ntiles, int *counts, in
                        int threads, cudaStream_t s);
 // tile_elems: the largest tile of etiles (the mixed kernel keeps 4 bytes of
 // shared memory per tile element); act: the instantiation with element birth
-// (Problem::act_t set)
+// (Problem::act_t set); visc: the one with bulk viscosity (Problem::visc set)
 void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, int mode, int parity, int grid,
-                       int threads, int tile_elems, cudaStream_t s, bool act = false);
+                       int threads, int tile_elems, cudaStream_t s, bool act = false, bool visc = false);
 // CTAs of the tiled element kernel (node kernel when `node` is true) that fit on one SM
 int tiled_ctas_per_sm(int mode, int threads, bool node = false);
 // Mixed-mode state conversions: u, v, a (FP64) -> uhl, vhl, ahl, and back
@@ -177,6 +190,8 @@ void launch_elem_exact(const Problem &p, int parity, cudaStream_t s);
 // set-up (exact operation order)
 void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s);
 void launch_setup_mass(const Problem &p, double *mass, double *minv, cudaStream_t s);
+// bulk viscosity: the elements' previous-step F diagonal from displacement u
+void launch_visc_init(const Problem &p, const double *u, cudaStream_t s);
 // min over elements of Lref/c (undeformed) or min(Lref, L(X+u))/c, into dtmin[slot]
 void launch_initial_cfl(const Problem &p, const double *uK, int slot, cudaStream_t s);
 // gravity terms per element and their per-node sums (reference order)

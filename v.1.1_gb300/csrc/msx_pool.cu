@@ -502,7 +502,7 @@ extern "C" msx_status msx_pool_create(const msx_pool_opts *opts, msx_pool **out)
         return bail(pfail(MSX_ERR_CUDA, "streams"));
     size_t n = opts->max_slots;
     if (cudaMalloc(&p->d_descs, sizeof(Problem) * n) != cudaSuccess || cudaMalloc(&p->d_ctrl, sizeof(Ctrl) * 2 * n) != cudaSuccess ||
-        cudaMalloc(&p->d_dtmin, sizeof(unsigned long long) * 2 * n) != cudaSuccess ||
+        cudaMalloc(&p->d_dtmin, sizeof(unsigned long long) * 4 * n) != cudaSuccess ||
         cudaMalloc(&p->d_flags, sizeof(int) * 2 * n) != cudaSuccess || cudaMalloc(&p->d_counts, sizeof(int) * kTileSched) != cudaSuccess ||
         cudaMallocHost(&p->h_ctrl, sizeof(Ctrl) * 2 * n) != cudaSuccess)
         return bail(pfail(MSX_ERR_OOM, "pool tables"));
@@ -676,7 +676,7 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
         P.bc_rec = d_rec;
         P.bcs = d_ent;
         P.ctrl = p->d_ctrl + 2 * slot;
-        P.dtmin = p->d_dtmin + 2 * slot;
+        P.dtmin = p->d_dtmin + 4 * slot;
         P.flags = p->d_flags + 2 * slot;
         P.sf = o->scale_factor;
         P.tf = o->tf;
@@ -704,7 +704,8 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
         launch_setup_elements(P, X, s);
         launch_setup_mass(P, mass, minv, s);
         if (pair_state(prec)) launch_minv_split(minv, minv2, nn, s);
-        unsigned long long inf2[2] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL};
+        // CFL minima (double bits) and the screen's running minima (FP32 bits)
+        unsigned long long inf2[4] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL, 0x7F800000ULL, 0x7F800000ULL};
         PCUDA(cudaMemcpyAsync(P.dtmin, inf2, sizeof(inf2), cudaMemcpyHostToDevice, s));
         launch_initial_cfl(P, nullptr, 0, s);
         launch_initial_cfl(P, nullptr, 1, s);   // u = 0: the deformed CFL equals the undeformed one

@@ -131,6 +131,12 @@ struct msx_handle {
     DBuf<Problem> d_desc;
     DBuf<double> act;                    // activation times (element birth), when set
     bool act_enabled = false;
+    // artificial viscosity (msx_set_viscosity): kind and parameters; the
+    // elements' previous-step F diagonal while bulk viscosity runs
+    int visc_kind = MSX_VISC_NONE;
+    double visc_c1 = 0, visc_cl = 0, visc_h = 0, visc_c0 = 0;
+    DBuf<double> visc_f0;
+    DBuf<float> visc_h0;
     DBuf<Tile> d_etiles, d_ntiles;
     int tile_elems = 0;                 // element-tile size of d_etiles
     DBuf<int> d_counts;
@@ -168,6 +174,7 @@ bool msx::material_params(const msx_material &m, MatParams &o)
     o.mu2_f = (float)o.mu2;
     o.lam_stvk_f = (float)o.lam_stvk;
     o.inv_c_f = (float)(1.0 / o.c);
+    o.rho_f = (float)m.rho;
     auto dw = [](double x) { const float hi = (float)x; return make_float2(hi, (float)(x - (double)hi)); };
     o.lambda_w = dw(o.lambda);
     o.mu_w = dw(o.mu);
@@ -224,9 +231,23 @@ static msx_status build_bcs(long long nn, const msx_bc *bcs, long long nbc, doub
     return MSX_OK;
 }
 
+// Bulk viscosity with a nonzero element size changes the forces; the
+// deviatoric kind and a zero size add exact zeros, as in the reference.
+static bool visc_running(const msx_handle *h) { return h->visc_kind == MSX_VISC_BULK && h->visc_h != 0.0; }
+
 static void bind_problem(msx_handle *h)
 {
     Problem &P = h->P;
+    P.visc = visc_running(h) ? 1 : 0;
+    P.visc_f0 = P.visc ? h->visc_f0.p : nullptr;
+    P.visc_h0 = P.visc ? h->visc_h0.p : nullptr;
+    P.visc_h = h->visc_h;
+    P.visc_c1 = h->visc_c1;
+    P.visc_cl = h->visc_cl;
+    P.visc_c0 = h->visc_c0;
+    P.visc_hf = (float)h->visc_h;
+    P.visc_c1sq_hf = (float)(h->visc_c1 * h->visc_c1 * h->visc_h);
+    P.visc_clc0f = (float)(h->visc_cl * h->visc_c0);
     P.act_t = h->act_enabled ? h->act.p : nullptr;
     P.conn = h->conn.p;
     P.G = h->G.p;
@@ -307,7 +328,7 @@ static void launch_step(msx_handle *h, int parity)
     if (h->nfaces) launch_face_loads(h->P, parity, pair_state(h), h->stream);
     if (h->tiled)
         launch_tiled_elem(h->d_desc.p, h->d_etiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
-                          h->tile_elems, h->stream, h->P.act_t != nullptr);
+                          h->tile_elems, h->stream, h->P.act_t != nullptr, h->P.visc != 0);
     else
         h->elem(h->P, parity, h->stream);
 }
@@ -422,7 +443,8 @@ static msx_status init_block(msx_handle *h)
     msx_status tst = upload_tiled(h);
     if (tst != MSX_OK) return tst;
     const Problem &P = h->P;
-    unsigned long long inf[2] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL};
+    // CFL minima (double bits) and the screen's running minima (FP32 bits)
+    unsigned long long inf[4] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL, 0x7F800000ULL, 0x7F800000ULL};
     MSX_CUDA(cudaMemcpyAsync(h->dtmin.p, inf, sizeof(inf), cudaMemcpyHostToDevice, h->stream));
     launch_initial_cfl(P, nullptr, 0, h->stream);
     launch_initial_cfl(P, h->t0 < 1E-12 ? h->u.p : nullptr, 1, h->stream);
@@ -431,6 +453,11 @@ static msx_status init_block(msx_handle *h)
     MSX_CUDA(cudaGetLastError());
     if (pair_state(h)) {
         launch_state_split(P, h->stream);   // the running state of a mixed or double-word block
+        MSX_CUDA(cudaGetLastError());
+    }
+    if (P.visc) {
+        // the Gauss points' previous F at a block start: that of the handed-over state
+        launch_visc_init(P, h->u.p, h->stream);
         MSX_CUDA(cudaGetLastError());
     }
     MSX_CUDA(cudaMemcpyAsync(h->h_ctrl, h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
@@ -561,7 +588,7 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     ALLOC(h->node_ptr, nn + 1);
     ALLOC(h->node_inc, 4 * ne);
     ALLOC(h->ctrl, 2);
-    ALLOC(h->dtmin, 2);
+    ALLOC(h->dtmin, 4);
     ALLOC(h->flags, 2);
     if (mesh->elem_material && num_mats > 1) ALLOC(h->mat, ne);
 #undef ALLOC
@@ -617,6 +644,8 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     h->bc_rec.release();
     h->bcs.release();
     h->act.release();
+    h->visc_f0.release();
+    h->visc_h0.release();
     h->grav_e.release();
     h->grav_n.release();
     h->fcon.release();
@@ -893,12 +922,50 @@ extern "C" msx_status msx_set_activation(msx_handle *h, const double *activation
                                  h->stream));
     }
     if (enabled && !h->act.p) return fail(MSX_ERR_STATE, "activation enabled before any activation times were set");
+    if (enabled && visc_running(h))
+        return fail(MSX_ERR_STATE, "element birth and bulk viscosity together are not supported");
     h->act_enabled = enabled != 0;
     bind_problem(h);
     msx_status st = upload_tiled(h);
     if (st != MSX_OK) return st;
     MSX_CUDA(cudaStreamSynchronize(h->stream));
     if (h->graph) {   // the exact mode's captured launches hold the Problem by value
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    return MSX_OK;
+}
+
+extern "C" msx_status msx_set_viscosity(msx_handle *h, int32_t kind, double c1, double cl, double element_size,
+                                        double c0)
+{
+    if (!h) return fail(MSX_ERR_ARG, "NULL handle");
+    if (kind < MSX_VISC_NONE || kind > MSX_VISC_DEV) return fail(MSX_ERR_ARG, "unknown artificial viscosity kind");
+    if (!std::isfinite(c1) || !std::isfinite(cl) || !std::isfinite(element_size) || !std::isfinite(c0) ||
+        element_size < 0)
+        return fail(MSX_ERR_ARG, "viscosity parameters must be finite and the element size >= 0");
+    const bool was = visc_running(h);
+    const bool on = kind == MSX_VISC_BULK && element_size != 0.0;
+    if (on && h->act_enabled) return fail(MSX_ERR_STATE, "element birth and bulk viscosity together are not supported");
+    if (on && !h->visc_f0.p) {
+        MSX_CUDA(h->visc_f0.alloc(3 * h->P.ne));
+        MSX_CUDA(h->visc_h0.alloc(3 * h->P.ne));
+    }
+    h->visc_kind = kind;
+    h->visc_c1 = c1;
+    h->visc_cl = cl;
+    h->visc_h = element_size;
+    h->visc_c0 = c0;
+    bind_problem(h);
+    if (on && !was) {
+        // from here on the previous step's F is that of the current state
+        launch_visc_init(h->P, h->u.p, h->stream);
+        MSX_CUDA(cudaGetLastError());
+    }
+    msx_status st = upload_tiled(h);
+    if (st != MSX_OK) return st;
+    MSX_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->graph) {   // another element-kernel instantiation, and the exact mode's launches hold the Problem
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
     }
@@ -1198,7 +1265,7 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
         cudaEventRecord(ev[3 * i + 1], h->stream);
         if (h->tiled)
             launch_tiled_elem(h->d_desc.p, h->d_etiles.p, h->d_counts.p, tiled_mode(h), parity, h->tgrid, h->tthreads,
-                              h->tile_elems, h->stream, h->P.act_t != nullptr);
+                              h->tile_elems, h->stream, h->P.act_t != nullptr, h->P.visc != 0);
         else
             h->elem(h->P, parity, h->stream);
         cudaEventRecord(ev[3 * i + 2], h->stream);

@@ -19,6 +19,7 @@ OK = 0
 ERR = {0: "OK", 1: "ARG", 2: "CUDA", 3: "NEG_JACOBIAN", 4: "NAN", 5: "OOM", 6: "STATE",
        7: "NO_DEVICE", 8: "TIMEOUT", 9: "BUSY"}
 NEO_HOOKEAN, COMPRESSIBLE_NH, STVK, LINEAR_ELASTIC = 0, 1, 2, 3
+VISC_NONE, VISC_BULK, VISC_DEV = 0, 1, 2
 BC_RAMP, BC_INST, BC_VEL_RAMP, BC_RAMP_RATE = 0, 1, 2, 3
 FP64, FP64_EXACT, MIXED, DOUBLE_WORD = 0, 1, 2, 3
 
@@ -105,7 +106,7 @@ SYMBOLS = ["msx_create", "msx_run", "msx_get_state", "msx_set_state", "msx_next_
            "msx_internal_force_noalloc", "msx_initial_dt", "msx_element_fields", "msx_set_loads",
            "msx_set_load_blocks", "msx_node_values", "msx_element_values", "msx_element_reduce",
            "msx_set_activation", "msx_pool_inject_alloc_failures", "msx_deck_read_loads", "msx_deck_loads_blocks",
-           "msx_deck_loads_free"]
+           "msx_deck_loads_free", "msx_set_viscosity"]
 
 _lib = None
 
@@ -314,6 +315,13 @@ class Solver:
             blocks.append(B)
         arr = (LoadBlock_ * max(1, len(blocks)))(*blocks)
         _check(load().msx_set_load_blocks(self.h, C.cast(arr, C.c_void_p), len(blocks)))
+
+    def set_viscosity(self, kind, c1=0.06, cl=1.2, element_size=0.0, c0=0.0):
+        """Artificial viscosity (VISC_NONE, VISC_BULK, VISC_DEV); element_size and c0 are
+        the reference's never-set solvers::_elementSize and _c0 (0 there)."""
+        load().msx_set_viscosity.argtypes = [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                             C.c_double]
+        _check(load().msx_set_viscosity(self.h, int(kind), float(c1), float(cl), float(element_size), float(c0)))
 
     def node_values(self, field, comp, nodes):
         """Component comp of FIELD_DISPLACEMENT / FIELD_EXTERNAL_FORCE /
