@@ -57,7 +57,9 @@ enum { MSX_PREC_FP64 = 0,        /* plain FP64, FMA-contracted, algebraically si
        MSX_PREC_DOUBLE_WORD = 3  /* MSX_PREC_FP64's algebra in double-word (FP32 pair, ~48-bit)
                                     arithmetic on the FP32 pipe, state and corner forces too;
                                     FP64 CFL check.  Values must stay inside FP32's exponent
-                                    range (|x| < 3e38, and near 1e-38 only as zeros). */ };
+                                    range: msx_create, msx_next_solver and msx_pool_submit
+                                    refuse (MSX_ERR_ARG) material constants or nonzero
+                                    coordinates outside [2^-100, 2^100] for this mode. */ };
 
 typedef struct {
     int64_t num_nodes, num_elems;

@@ -179,3 +179,31 @@ def test_high_degree_nodes(m):
             assert np.array_equal(u, ref.u) and np.array_equal(v, ref.v) and np.array_equal(a, ref.a)
         else:
             assert rel(u, ref.u) <= tol and rel(a, ref.a) <= tol
+
+
+@pytest.mark.gpu
+def test_double_word_refuses_values_outside_its_range():
+    """The double-word mode's low words need FP32's normal range: material
+    constants or nonzero coordinates outside [2^-100, 2^100] are refused
+    (MSX_ERR_ARG) by msx_create, msx_next_solver and msx_pool_submit; the
+    other modes take them."""
+    X, conn = msx.mesh_cube(2)
+    tiny = X * 2.0 ** -110                       # a mesh in absurd units
+    bcs = msx.cube_bcs(2, 0.0)
+    mat = (msx.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0)
+    for Xc, m in ((tiny, mat), (X, (msx.COMPRESSIBLE_NH, 1e35, 0.3, 1000.0))):
+        with pytest.raises(msx.MsxError) as ei:
+            msx.Solver(Xc, conn, [m], bcs, 0.0, 1.0, 0.5, precision=msx.DOUBLE_WORD)
+        assert ei.value.status == 1 and b"double-word" in msx.load().msx_last_error()
+        S = msx.Solver(Xc, conn, [m], bcs, 0.0, 1.0, 0.5, precision=msx.FP64)
+        with pytest.raises(msx.MsxError) as ei:
+            S.next_solver(bcs, 1.0, 2.0, 0.5, precision=msx.DOUBLE_WORD)
+        assert ei.value.status == 1
+        S.close()
+        P = msx.Pool(max_slots=2, precision=msx.DOUBLE_WORD)
+        with pytest.raises(msx.MsxError) as ei:
+            P.submit(Xc, conn, m, bcs, 5)
+        assert ei.value.status == 1
+        P.close()
+    S = msx.Solver(X, conn, [mat], bcs, 0.0, 1.0, 0.5, precision=msx.DOUBLE_WORD)   # ordinary units
+    S.close()

@@ -31,8 +31,10 @@ int main(int argc, char **argv)
     classPrintForces *forces = nullptr;
     vector<int> none;
     string petsc_solver, petsc_precon;
+    vector<double> para_AV = {0.06, 1.2};
     solvers *s = new classSolverExplicitGPU(nod, 3, 0, dnod, 0.5, outputs, 0.0, 1.0, "EXPLICIT", none, none, none,
-                                            forces, false, petsc_solver, petsc_precon, false, MSX_PREC_FP64);
+                                            1, para_AV, forces, false, petsc_solver, petsc_precon, false,
+                                            MSX_PREC_FP64);
     vector<classNeumannBCs *> loads;
     vector<classGPs *> gps;
     vector<classElements *> elem, geo;

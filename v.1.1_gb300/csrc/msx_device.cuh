@@ -1945,6 +1945,67 @@ __device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl,
 // dynamic shared memory of 4 bytes per tile element.  ACT: the instantiation
 // with element birth (single solves whose block has it on), VISC the one with
 // artificial bulk viscosity; the plain one carries no trace of either.
+// The mixed kernel's tile loop, two CTA barriers per tile: one inside the
+// tile's FP32 minimum (warp minima to shared memory), one after thread 0 has
+// posted the recheck threshold and the next tile index.  The running screen
+// minimum is read at the tile's start (its latency hidden by the tile's work)
+// and the tile's minimum posted without waiting for the old value: the
+// threshold min(g0, tile min) (1 + 2^-8) is still >= the step's FP32 minimum
+// times (1 + 2^-8), which is all the recheck needs.  Shared slots alternate by
+// iteration, so thread 0 never overwrites a value another thread has yet to read.
+template <bool ACT, bool VISC>
+__device__ __forceinline__ void mixed_tile_loop(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
+                                                TileQueue &q, int parity, float *sdt)
+{
+    __shared__ int s_tile[2];
+    __shared__ float s_thr[2];
+    __shared__ float wm[32];
+    if (threadIdx.x == 0) s_tile[0] = q.claim();
+    __syncthreads();
+    int t = s_tile[0];
+    for (int it = 1; t < q.n; it ^= 1) {
+        int next = 0;
+        if (threadIdx.x == 0) next = q.claim();
+        const Tile tl = tiles[t];
+        const Problem &p = descs[tl.solve];
+        const bool ran = p.ctrl[parity].ran;   // the same for the whole block
+        if (ran) {
+            unsigned long long *slot = p.dtmin + 2 + (parity ^ 1);
+            const unsigned long long g0 = threadIdx.x == 0 ? __ldcg(slot) : 0ULL;
+            float v = tile_elements<MODE_MIXED, ACT, VISC>(p, tl, parity, sdt);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+            if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = v;
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                const int nw = (blockDim.x + 31) >> 5;
+                float b = threadIdx.x < nw ? wm[threadIdx.x] : INFINITY;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) b = fminf(b, __shfl_xor_sync(0xffffffffu, b, o));
+                if (threadIdx.x == 0) {
+                    if (b < INFINITY) atomicMin(slot, (unsigned long long)__float_as_uint(b));
+                    const float g = g0 >= kScreenInfBits ? b : fminf(__uint_as_float((unsigned)g0), b);
+                    s_thr[it] = g * (1.0f + 1.0f / 256.0f);
+                }
+            }
+        }
+        if (threadIdx.x == 0) s_tile[it] = next;
+        __syncthreads();   // s_thr, s_tile posted; wm read by warp 0 before it
+        if (ran) {
+            // a thread reads back only the screen values it wrote itself
+            const float thr = s_thr[it];
+            double v = INFINITY;
+            for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
+                const float d = sdt[e - tl.begin];
+                if (d < 0.0f || d <= thr) v = fmin(v, cfl_dw(p, e));
+            }
+            if (v >= 0.0 && v < INFINITY)
+                atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
+        }
+        t = s_tile[it];
+    }
+}
+
 template <int MODE, bool ACT = false, bool VISC = false>
 __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE == MODE_DW ? 3 : 2)) pool_elem_kernel(const Problem *__restrict__ descs,
                                                                  const Tile *__restrict__ tiles,
@@ -1957,6 +2018,11 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
     __shared__ float s_thr;
     float *sdt = MODE == MODE_MIXED ? reinterpret_cast<float *>(dyn_smem) : sdt_static;
     TileQueue q{sched, sched[0]};
+    if constexpr (MODE == MODE_MIXED) {
+        mixed_tile_loop<ACT, VISC>(descs, tiles, q, parity, sdt);
+        q.finish();
+        return;
+    }
     if (threadIdx.x == 0) s_tile = q.claim();
     __syncthreads();
     int t = s_tile;

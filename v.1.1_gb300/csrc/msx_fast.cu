@@ -99,6 +99,40 @@ void launch_minv_split(const double *minv, float2 *minv2, long long nn, cudaStre
     minv_split_kernel<<<grid_for(nn, 256), 256, 0, s>>>(minv, minv2, nn);
 }
 
+__global__ void abs_range_kernel(const double *x, long long n, unsigned long long *mm)
+{
+    unsigned long long lo = ~0ULL, hi = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(x[i]));
+        if (b != 0) {
+            lo = b < lo ? b : lo;
+            hi = b > hi ? b : hi;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, lo, o), h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        lo = l2 < lo ? l2 : lo;
+        hi = h2 > hi ? h2 : hi;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(mm, lo);
+        atomicMax(mm + 1, hi);
+    }
+}
+
+__global__ void abs_range_init_kernel(unsigned long long *mm)
+{
+    mm[0] = ~0ULL;
+    mm[1] = 0;
+}
+
+void launch_abs_range(const double *x, long long n, unsigned long long *mm, cudaStream_t s)
+{
+    abs_range_init_kernel<<<1, 1, 0, s>>>(mm);
+    abs_range_kernel<<<256, 256, 0, s>>>(x, n, mm);
+}
+
 int tiled_ctas_per_sm(int mode, int threads, bool node)
 {
     int a = 0;

@@ -223,6 +223,16 @@ void launch_internal_force_dw(const Problem &p, double *fint, cudaStream_t s);
 // Law parameters of one material, FP64 and the FP32 / double-word copies; false if invalid.
 bool material_params(const msx_material &m, MatParams &o);
 
+// The double-word mode holds values as FP32 (hi, lo) pairs, whose low word
+// needs FP32's normal range: material constants and nonzero coordinates must
+// lie within [2^-100, 2^100] (a margin for the products the kernels form).
+constexpr int kDwExpLimit = 100;
+bool dw_in_range(double x);   // x == 0 or 2^-100 <= |x| <= 2^100
+bool dw_material_ok(const MatParams &m);
+// min nonzero |x| and max |x| over x[0..n) on the device, as the bit patterns
+// of non-negative doubles in mm[0], mm[1] (device memory, set here)
+void launch_abs_range(const double *x, long long n, unsigned long long *mm, cudaStream_t s);
+
 // Node -> (element, corner) lists in element order (node_ptr[nn + 1],
 // node_inc[4 ne], slot[ne]) built on the device from the uploaded conn;
 // synchronises s once.  MSX_ERR_ARG (message in err) when a node id is out of

@@ -558,6 +558,13 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
     msx_status st = make_mat(*mat, mp);
     if (st != MSX_OK) return st;
     const int prec = p->opts.precision;
+    if (prec == MSX_PREC_DOUBLE_WORD) {   // the range the double-word kernels need (dw_in_range)
+        if (!dw_material_ok(mp))
+            return pfail(MSX_ERR_ARG, "double-word pool: a material constant lies outside [2^-100, 2^100]");
+        for (long long i = 0; i < 3 * nn; i++)
+            if (!dw_in_range(mesh->X[i]))
+                return pfail(MSX_ERR_ARG, "double-word pool: a nonzero coordinate lies outside [2^-100, 2^100]");
+    }
     const size_t bytes = footprint(nn, ne, num_bcs, prec);
     {   // cheap early refusal; the slot is taken below, after the host tables
         std::lock_guard<std::mutex> lk(p->mu);

@@ -144,6 +144,7 @@ struct msx_handle {
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc[2] = {nullptr, nullptr};
     std::vector<int> h_node_bc;   // host copies for next_solver rebuilds
+    bool dw_coords_checked = false, dw_coords_ok = false;   // double-word range of the coordinates
 };
 
 // ------------------------------------------------------------------ host helpers
@@ -182,6 +183,19 @@ bool msx::material_params(const msx_material &m, MatParams &o)
     o.mu2_w = dw(o.mu2);
     o.lam_stvk_w = dw(o.lam_stvk);
     o.mu3_w = dw(o.mu / 3.0);
+    return true;
+}
+
+bool msx::dw_in_range(double x)
+{
+    const double a = std::fabs(x);
+    return a == 0.0 || (a >= std::ldexp(1.0, -kDwExpLimit) && a <= std::ldexp(1.0, kDwExpLimit));
+}
+
+bool msx::dw_material_ok(const MatParams &m)
+{
+    for (double x : {m.young, m.rho, m.lambda, m.mu, m.K1, m.mu2, m.lam_stvk})
+        if (!dw_in_range(x)) return false;
     return true;
 }
 
@@ -410,6 +424,33 @@ static msx_status upload_bcs(msx_handle *h, const msx_bc *bcs, long long nbc)
     return MSX_OK;
 }
 
+// Inputs of a double-word block (see dw_in_range): the materials, and the
+// coordinates through one device reduction (once per handle).
+static msx_status check_double_word(msx_handle *h)
+{
+    for (int k = 0; k < h->P.nmat; k++)
+        if (!dw_material_ok(h->P.mats[k]))
+            return fail(MSX_ERR_ARG, "double-word mode: a material constant lies outside [2^-100, 2^100]");
+    if (!h->dw_coords_checked) {
+        DBuf<unsigned long long> mm;
+        MSX_CUDA(mm.alloc(2));
+        launch_abs_range(h->X.p, 3 * h->P.nn, mm.p, h->stream);
+        unsigned long long r[2] = {0, 0};
+        cudaError_t e = cudaMemcpyAsync(r, mm.p, sizeof(r), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        mm.release();
+        if (e != cudaSuccess) return fail(MSX_ERR_CUDA, std::string("coordinate range: ") + cudaGetErrorString(e));
+        double lo, hi;
+        memcpy(&lo, &r[0], sizeof lo);
+        memcpy(&hi, &r[1], sizeof hi);
+        h->dw_coords_ok = (r[0] == ~0ULL || dw_in_range(lo)) && dw_in_range(hi);
+        h->dw_coords_checked = true;
+    }
+    if (!h->dw_coords_ok)
+        return fail(MSX_ERR_ARG, "double-word mode: a nonzero coordinate lies outside [2^-100, 2^100]");
+    return MSX_OK;
+}
+
 static msx_status set_opts(msx_handle *h, const msx_solver_opts *o)
 {
     if (!o) return fail(MSX_ERR_ARG, "solver options required");
@@ -623,6 +664,7 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     launch_minv_split(h->minv.p, h->minv2.p, nn, s);
     if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
         return bail(fail(MSX_ERR_CUDA, "set-up kernels failed"));
+    if (h->precision == MSX_PREC_DOUBLE_WORD && (st = check_double_word(h)) != MSX_OK) return bail(st);
     if ((st = upload_bcs(h, bcs, num_bcs)) != MSX_OK) return bail(st);
     bind_problem(h);
     *out = h;
@@ -1182,6 +1224,7 @@ extern "C" msx_status msx_next_solver(msx_handle *h, const msx_bc *bcs, int64_t 
 {
     if (!h) return fail(MSX_ERR_ARG, "NULL handle");
     msx_status st;
+    if (opts && opts->precision == MSX_PREC_DOUBLE_WORD && (st = check_double_word(h)) != MSX_OK) return st;
     if ((st = set_opts(h, opts)) != MSX_OK) return st;
     if ((st = upload_bcs(h, bcs, num_bcs)) != MSX_OK) return st;
     if (h->graph) {

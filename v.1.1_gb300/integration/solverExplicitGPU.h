@@ -9,7 +9,8 @@
 // the arguments classSolverExplicit gets plus a precision (MSX_PREC_*), and
 // links with -lmsx.  It covers decks of C3D4 elements with the Neo-Hookean,
 // compressible Neo-Hookean, St-Venant-Kirchhoff and linear-elastic laws,
-// Dirichlet BCs, element birth (*ACTIVATION) and the Neumann loads of the
+// Dirichlet BCs, element birth (*ACTIVATION), artificial viscosity (the
+// factory's flag_AV and para_AV, as classSolverExplicit gets them) and the Neumann loads of the
 // explicit path (nodal forces, gravity, traction and pressure, instantaneous
 // and ramped).  The reference's load classes keep their t0, tf and amounts
 // private, so the loads are read from the deck file itself by the library
@@ -197,14 +198,19 @@ inline std::string loads_of(const std::string &deck, vector<classNeumannBCs *> &
 
 class classSolverExplicitGPU : public solvers {
   public:
+    // The arguments of classSolverExplicit's constructor (solverExplicit.h), with
+    // flag_AV and para_AV = {c1, cl} of *Bulk viscosity (1) / *Dev viscosity (2),
+    // plus the precision.
     classSolverExplicitGPU(vector<classNodes *> &nod, int ndim, int numDof, vector<classDirichlet *> &DNod,
                            double scaleFactor, classOutputs *&outputs, double t0, double tf, string solverType,
                            const vector<int> &activeDofMapLocal, const vector<int> &nActiveDof,
-                           const vector<int> &ISactiveDof, classPrintForces *&forceOutputs, bool flagActivation,
-                           string &petsc_solver, string &petsc_precon, bool flagFSI, int precision)
+                           const vector<int> &ISactiveDof, int flag_AV, const vector<double> &para_AV,
+                           classPrintForces *&forceOutputs, bool flagActivation, string &petsc_solver,
+                           string &petsc_precon, bool flagFSI, int precision)
         : solvers(nod, ndim, numDof, DNod, scaleFactor, outputs, t0, tf, solverType, activeDofMapLocal, nActiveDof,
                   ISactiveDof, forceOutputs, flagActivation, petsc_solver, petsc_precon, flagFSI),
-          _precision(precision)
+          _precision(precision), _flagAV(flag_AV), _c1(para_AV.size() > 0 ? para_AV[0] : 0.0),
+          _cl(para_AV.size() > 1 ? para_AV[1] : 0.0)
     {
     }
 
@@ -273,6 +279,10 @@ class classSolverExplicitGPU : public solvers {
             check(st, h);
         }
         if (_flagActivation) check(msx_set_activation(h, act.data(), 1), h);
+        // artificial viscosity with the element size and c0 the reference computes with: it
+        // never assigns solvers::_elementSize and _c0 (0 in its builds), so pass 0
+        if (_flagAV == 1 || _flagAV == 2)
+            check(msx_set_viscosity(h, _flagAV == 1 ? MSX_VISC_BULK : MSX_VISC_DEV, _c1, _cl, 0.0, 0.0), h);
         msx_run_report r{};
         check(msx_run(h, 0, &r), h);
         check(msx_get_state(h, _u.data(), _v.data(), _a.data()), h);   // read back by getFinalValues()
@@ -282,6 +292,8 @@ class classSolverExplicitGPU : public solvers {
 
   private:
     int _precision;
+    int _flagAV;
+    double _c1, _cl;
 
     static void stop(const std::string &msg)
     {
