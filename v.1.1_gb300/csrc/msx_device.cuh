@@ -1904,13 +1904,15 @@ __global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *
 }
 
 // The elements of one tile for the tiled element kernel: each thread's
-// elements in turn, FP32 CFL screen values into sdt;
-// returns the thread's FP32 minimum.  The mixed and double-word bodies take the
-// element's connectivity loaded one element ahead, so their node gathers wait
-// for one memory latency instead of two (connectivity, then the nodes).  ACT:
-// element birth is on, and the step's time decides which elements are dead.
+// elements in turn; returns the thread's FP32 minimum of the CFL screen.  The
+// FP64 and double-word kernels keep every screen value in sdt; the mixed one
+// only notes in `neg` whether one of its elements was a sliver (a negative
+// screen value).  The mixed and double-word bodies take the element's
+// connectivity loaded one element ahead, so their node gathers wait for one
+// memory latency instead of two (connectivity, then the nodes).  ACT: element
+// birth is on, and the step's time decides which elements are dead.
 template <int MODE, bool ACT, bool VISC>
-__device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl, int parity, float *sdt)
+__device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl, int parity, float *sdt, bool &neg)
 {
     float v32 = INFINITY;
     const double t = ACT ? p.ctrl[parity].t : 0.0;
@@ -1927,99 +1929,127 @@ __device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl,
         float d = MODE == MODE_MIXED ? elem_body_mixed<false, ACT, VISC>(p, e, parity, cn, t, idtf)
                                      : (MODE == MODE_DW ? elem_body_dw<false, ACT, VISC>(p, e, parity, cn, t, idt)
                                                         : elem_body_fp64<false, ACT, VISC>(p, e, parity, t, idt));
-        sdt[e - tl.begin] = d;
+        if (MODE == MODE_MIXED) neg |= d < 0.0f;
+        else sdt[e - tl.begin] = d;
         if (d >= 0.0f) v32 = fminf(v32, d);
     }
     return v32;
 }
 
-// Element kernel over tiles.  Every element's FP32 CFL screen value is kept in
-// shared memory; after the tile's FP32 minimum is known, elements within 2^-8
-// of the solve's running FP32 minimum (and slivers) recompute the exact FP64
-// value, whose minimum goes to the solve's CFL slot.  The screen's error stays
-// far below 2^-9 outside slivers, so that set always holds the step's exact
-// minimum.  FP64 and
-// double-word list the candidates and recompute them by consecutive threads;
-// mixed tiles have a candidate or two, which each thread recomputes among its
-// own elements (no list, no extra barrier), and keep their screen values in
-// dynamic shared memory of 4 bytes per tile element.  ACT: the instantiation
-// with element birth (single solves whose block has it on), VISC the one with
-// artificial bulk viscosity; the plain one carries no trace of either.
-// The mixed kernel's tile loop, two CTA barriers per tile: one inside the
-// tile's FP32 minimum (warp minima to shared memory), one after thread 0 has
-// posted the recheck threshold and the next tile index.  The running screen
-// minimum is read at the tile's start (its latency hidden by the tile's work)
-// and the tile's minimum posted without waiting for the old value: the
-// threshold min(g0, tile min) (1 + 2^-8) is still >= the step's FP32 minimum
-// times (1 + 2^-8), which is all the recheck needs.  Shared slots alternate by
-// iteration, so thread 0 never overwrites a value another thread has yet to read.
+constexpr int kMixedPending = 64;   // deferred FP64 rechecks a mixed CTA can hold
+
+// FP64 CFL values (cfl_dw) of one thread's elements of a mixed tile, their
+// minimum into the solve's CFL slot (a full pending list).
+__device__ __forceinline__ void mixed_recheck(const Problem &p, const Tile &tl, int lane, int parity)
+{
+    double v = INFINITY;
+    for (long long e = tl.begin + lane; e < tl.end; e += blockDim.x) v = fmin(v, cfl_dw(p, e));
+    if (v >= 0.0 && v < INFINITY) atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
+}
+
+// The mixed kernel's tile loop.  Each tile's FP32 screen minimum goes to the
+// solve's running minimum (an integer atomicMin on its bit pattern, nothing
+// waited for); a thread whose own minimum lies within 2^-8 of the tile's, or
+// that met a sliver, posts (tile, thread, own minimum) to a per-CTA list.  Once
+// the CTA has run out of tiles, every entry whose minimum is still within
+// 2^-8 of the solve's running minimum -- by then nearly the step's FP32
+// minimum m -- has that thread's elements of that tile recomputed in FP64,
+// one element per thread of the CTA.  An element x near the exact minimum has
+// d(x) <= m (1 + 2^-8) <= (tile minimum) (1 + 2^-8), so its thread posted, and
+// the entry's minimum is <= d(x) <= (running minimum) (1 + 2^-8), so it is
+// rechecked.  A full list rechecks at once.
 template <bool ACT, bool VISC>
 __device__ __forceinline__ void mixed_tile_loop(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
-                                                TileQueue &q, int parity, float *sdt)
+                                                TileQueue &q, int parity)
 {
-    __shared__ int s_tile[2];
-    __shared__ float s_thr[2];
-    __shared__ float wm[32];
-    if (threadIdx.x == 0) s_tile[0] = q.claim();
+    __shared__ int s_tile, s_npend;
+    __shared__ int2 s_pend[kMixedPending];      // (tile, thread)
+    __shared__ float s_pendv[kMixedPending];    // the thread's minimum, -1 for a sliver
+    if (threadIdx.x == 0) {
+        s_tile = q.claim();
+        s_npend = 0;
+    }
     __syncthreads();
-    int t = s_tile[0];
-    for (int it = 1; t < q.n; it ^= 1) {
+    int t = s_tile;
+    while (t < q.n) {
         int next = 0;
         if (threadIdx.x == 0) next = q.claim();
         const Tile tl = tiles[t];
         const Problem &p = descs[tl.solve];
-        const bool ran = p.ctrl[parity].ran;   // the same for the whole block
-        if (ran) {
-            unsigned long long *slot = p.dtmin + 2 + (parity ^ 1);
-            const unsigned long long g0 = threadIdx.x == 0 ? __ldcg(slot) : 0ULL;
-            float v = tile_elements<MODE_MIXED, ACT, VISC>(p, tl, parity, sdt);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-            if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = v;
-            __syncthreads();
-            if (threadIdx.x < 32) {
-                const int nw = (blockDim.x + 31) >> 5;
-                float b = threadIdx.x < nw ? wm[threadIdx.x] : INFINITY;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) b = fminf(b, __shfl_xor_sync(0xffffffffu, b, o));
-                if (threadIdx.x == 0) {
-                    if (b < INFINITY) atomicMin(slot, (unsigned long long)__float_as_uint(b));
-                    const float g = g0 >= kScreenInfBits ? b : fminf(__uint_as_float((unsigned)g0), b);
-                    s_thr[it] = g * (1.0f + 1.0f / 256.0f);
+        if (p.ctrl[parity].ran) {
+            bool neg = false;
+            const float mine = tile_elements<MODE_MIXED, ACT, VISC>(p, tl, parity, nullptr, neg);
+            const float bmin = block_min_bcast(mine);
+            if (threadIdx.x == 0 && bmin < INFINITY)
+                atomicMin(p.dtmin + 2 + (parity ^ 1), (unsigned long long)__float_as_uint(bmin));
+            if (neg || (mine < INFINITY && mine <= bmin * (1.0f + 1.0f / 256.0f))) {
+                const int k = atomicAdd(&s_npend, 1);
+                if (k < kMixedPending) {
+                    s_pend[k] = make_int2(t, (int)threadIdx.x);
+                    s_pendv[k] = neg ? -1.0f : mine;
+                } else {
+                    mixed_recheck(p, tl, threadIdx.x, parity);
                 }
             }
         }
-        if (threadIdx.x == 0) s_tile[it] = next;
-        __syncthreads();   // s_thr, s_tile posted; wm read by warp 0 before it
-        if (ran) {
-            // a thread reads back only the screen values it wrote itself
-            const float thr = s_thr[it];
-            double v = INFINITY;
-            for (long long e = tl.begin + threadIdx.x; e < tl.end; e += blockDim.x) {
-                const float d = sdt[e - tl.begin];
-                if (d < 0.0f || d <= thr) v = fmin(v, cfl_dw(p, e));
-            }
-            if (v >= 0.0 && v < INFINITY)
-                atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
-        }
-        t = s_tile[it];
+        __syncthreads();
+        if (threadIdx.x == 0) s_tile = next;
+        __syncthreads();
+        t = s_tile;
     }
+    // every entry was posted before the loop's last barrier
+    const int np = min(s_npend, kMixedPending);
+    if (np == 0) return;
+    const int per = (kMaxTileElems + blockDim.x - 1) / blockDim.x;   // elements of one thread in one tile, at most
+    double v = INFINITY;
+    const Problem *last = nullptr;
+    for (int idx = threadIdx.x; idx < np * per; idx += blockDim.x) {
+        const int j = idx % np, k = idx / np;
+        const Tile tl = tiles[s_pend[j].x];
+        const long long e = tl.begin + s_pend[j].y + (long long)k * blockDim.x;
+        if (e >= tl.end) continue;
+        const Problem &p = descs[tl.solve];
+        const float mine = s_pendv[j];
+        if (!(mine < 0.0f)) {
+            const unsigned long long g = __ldcg(p.dtmin + 2 + (parity ^ 1));
+            if (g < kScreenInfBits && mine > __uint_as_float((unsigned)g) * (1.0f + 1.0f / 256.0f)) continue;
+        }
+        const double c = cfl_dw(p, e);
+        if (&p != last && v < INFINITY) {   // another solve: flush this one's minimum
+            atomicMin(last->dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
+            v = INFINITY;
+        }
+        last = &p;
+        v = fmin(v, c);
+    }
+    if (last && v >= 0.0 && v < INFINITY)
+        atomicMin(last->dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
 }
 
+// Element kernel over tiles.  Each element's FP32 CFL screen value is
+// compared with the solve's running FP32 minimum of the screen (a per-step
+// slot that every tile lowers by an integer atomicMin on its bit pattern):
+// elements within 2^-8 of it, and slivers, recompute the exact FP64 value,
+// whose minimum goes to the solve's CFL slot.  The screen's error stays far
+// below 2^-9 outside slivers, so that set always holds the step's exact
+// minimum.  FP64 and double-word keep the tile's screen values in shared
+// memory, list the candidates and recompute them by consecutive threads; the
+// mixed kernel defers its few rechecks to the end of the CTA's tiles
+// (mixed_tile_loop).  ACT: the instantiation with element birth (single
+// solves whose block has it on), VISC the one with artificial bulk viscosity;
+// the plain one carries no trace of either.
 template <int MODE, bool ACT = false, bool VISC = false>
 __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE == MODE_DW ? 3 : 2)) pool_elem_kernel(const Problem *__restrict__ descs,
                                                                  const Tile *__restrict__ tiles,
                                                                  int *__restrict__ sched, int parity)
 {
-    extern __shared__ __align__(16) unsigned char dyn_smem[];
-    __shared__ float sdt_static[MODE == MODE_MIXED ? 1 : kMaxTileElems];
+    __shared__ float sdt[MODE == MODE_MIXED ? 1 : kMaxTileElems];
     __shared__ unsigned short scand[MODE == MODE_MIXED ? 1 : kMaxTileElems];
     __shared__ int s_tile, s_ncand;
     __shared__ float s_thr;
-    float *sdt = MODE == MODE_MIXED ? reinterpret_cast<float *>(dyn_smem) : sdt_static;
     TileQueue q{sched, sched[0]};
     if constexpr (MODE == MODE_MIXED) {
-        mixed_tile_loop<ACT, VISC>(descs, tiles, q, parity, sdt);
+        mixed_tile_loop<ACT, VISC>(descs, tiles, q, parity);
         q.finish();
         return;
     }
@@ -2033,7 +2063,8 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
         const Problem &p = descs[tl.solve];
         if (p.ctrl[parity].ran) {
             if (MODE != MODE_MIXED && threadIdx.x == 0) s_ncand = 0;
-            const float v32 = tile_elements<MODE, ACT, VISC>(p, tl, parity, sdt);
+            bool neg = false;   // slivers are listed from sdt below
+            const float v32 = tile_elements<MODE, ACT, VISC>(p, tl, parity, sdt, neg);
             const float bmin = block_min_bcast(v32);   // also orders the sdt writes before the reads below
             if (threadIdx.x == 0) {
                 // g: the solve's smallest FP32 screen value over the tiles closed

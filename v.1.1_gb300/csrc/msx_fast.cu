@@ -50,9 +50,9 @@ static void launch_elem_variant(const Problem *descs, const Tile *etiles, int *c
 void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, int mode, int parity, int grid,
                        int threads, int tile_elems, cudaStream_t s, bool act, bool visc)
 {
-    if (mode == MODE_MIXED)   // the mixed kernel keeps its FP32 CFL screen values in dynamic shared memory
-        launch_elem_variant<MODE_MIXED>(descs, etiles, counts, parity, grid, threads,
-                                        sizeof(float) * (size_t)tile_elems, s, act, visc);
+    (void)tile_elems;
+    if (mode == MODE_MIXED)
+        launch_elem_variant<MODE_MIXED>(descs, etiles, counts, parity, grid, threads, 0, s, act, visc);
     else if (mode == MODE_DW)
         launch_elem_variant<MODE_DW>(descs, etiles, counts, parity, grid, threads, 0, s, act, visc);
     else
@@ -138,8 +138,7 @@ int tiled_ctas_per_sm(int mode, int threads, bool node)
     int a = 0;
     if (mode == MODE_MIXED)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, node ? (const void *)pool_node_kernel<MODE_MIXED>
-                                                               : (const void *)pool_elem_kernel<MODE_MIXED>, threads,
-                                                      node ? 0 : sizeof(float) * kMaxTileElems);
+                                                               : (const void *)pool_elem_kernel<MODE_MIXED>, threads, 0);
     else if (mode == MODE_DW)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, node ? (const void *)pool_node_kernel<MODE_DW>
                                                                : (const void *)pool_elem_kernel<MODE_DW>, threads, 0);

@@ -167,8 +167,8 @@ constexpr int kMaxTileElems = 4096; // upper bound on the elements of one tile
 constexpr int kTileSched = 6;
 void launch_tiled_node(const Problem *descs, const Tile *ntiles, int *counts, int mode, int parity, int grid,
                        int threads, cudaStream_t s);
-// tile_elems: the largest tile of etiles (the mixed kernel keeps 4 bytes of
-// shared memory per tile element); act: the instantiation with element birth
+// tile_elems: the largest tile of etiles (unused: every kernel's shared memory
+// is static); act: the instantiation with element birth
 // (Problem::act_t set); visc: the one with bulk viscosity (Problem::visc set)
 void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, int mode, int parity, int grid,
                        int threads, int tile_elems, cudaStream_t s, bool act = false, bool visc = false);

@@ -145,6 +145,7 @@ struct msx_handle {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc[2] = {nullptr, nullptr};
     std::vector<int> h_node_bc;   // host copies for next_solver rebuilds
     bool dw_coords_checked = false, dw_coords_ok = false;   // double-word range of the coordinates
+    bool u_zero = true;   // u is still the all-zero state msx_create set (no step run, no state set)
 };
 
 // ------------------------------------------------------------------ host helpers
@@ -488,7 +489,14 @@ static msx_status init_block(msx_handle *h)
     unsigned long long inf[4] = {0x7FF0000000000000ULL, 0x7FF0000000000000ULL, 0x7F800000ULL, 0x7F800000ULL};
     MSX_CUDA(cudaMemcpyAsync(h->dtmin.p, inf, sizeof(inf), cudaMemcpyHostToDevice, h->stream));
     launch_initial_cfl(P, nullptr, 0, h->stream);
-    launch_initial_cfl(P, h->t0 < 1E-12 ? h->u.p : nullptr, 1, h->stream);
+    if (h->t0 < 1E-12 && !h->u_zero) {
+        launch_initial_cfl(P, h->u.p, 1, h->stream);
+    } else {
+        // the undeformed lengths again (u is zero: X + u reproduces X bit for bit, so the
+        // deformed inscribed spheres are the reference ones)
+        MSX_CUDA(cudaMemcpyAsync(h->dtmin.p + 1, h->dtmin.p, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                                 h->stream));
+    }
     long long limit = h->max_steps > 0 ? h->max_steps : (1LL << 62);
     init_block_kernel<<<1, 1, 0, h->stream>>>(P, h->t0, limit);
     MSX_CUDA(cudaGetLastError());
@@ -1067,6 +1075,7 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     h->block_steps = fin.step;
     h->last_t = fin.t;
+    if (fin.step > 0) h->u_zero = false;
     if (rep) {
         rep->steps = fin.step - start_steps;
         rep->total_steps = fin.step;
@@ -1212,7 +1221,10 @@ extern "C" msx_status msx_set_state(msx_handle *h, const double *u, const double
     if (!h) return fail(MSX_ERR_ARG, "NULL handle");
     if (h->block_steps > 0) return fail(MSX_ERR_STATE, "state can only be set before a block's first step");
     size_t bytes = sizeof(double) * 3 * h->P.nn;
-    if (u) MSX_CUDA(cudaMemcpyAsync(h->u.p, u, bytes, cudaMemcpyHostToDevice, h->stream));
+    if (u) {
+        MSX_CUDA(cudaMemcpyAsync(h->u.p, u, bytes, cudaMemcpyHostToDevice, h->stream));
+        h->u_zero = false;
+    }
     if (v) MSX_CUDA(cudaMemcpyAsync(h->v.p, v, bytes, cudaMemcpyHostToDevice, h->stream));
     if (a) MSX_CUDA(cudaMemcpyAsync(h->a.p, a, bytes, cudaMemcpyHostToDevice, h->stream));
     MSX_CUDA(cudaStreamSynchronize(h->stream));

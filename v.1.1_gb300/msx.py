@@ -190,9 +190,12 @@ _BC_DTYPE = np.dtype({"names": [f for f, _ in BC_._fields_], "formats": ["<i8", 
                       "offsets": [getattr(BC_, f).offset for f, _ in BC_._fields_], "itemsize": C.sizeof(BC_)})
 
 
-def _bc_array(bcs):
-    """(dof, mode, value, ramp_steps) rows as an msx_bc array (at least one entry)."""
-    out = np.zeros(max(1, len(bcs)), _BC_DTYPE)
+def bc_array(bcs):
+    """(dof, mode, value, ramp_steps) rows as an msx_bc array.  Solver,
+    next_solver and Pool.submit take such an array in place of the rows."""
+    if isinstance(bcs, np.ndarray) and bcs.dtype == _BC_DTYPE:
+        return bcs
+    out = np.zeros(len(bcs), _BC_DTYPE)
     if len(bcs):
         rows = np.array(bcs, dtype=[("dof", "<i8"), ("mode", "<i4"), ("value", "<f8"), ("ramp", "<i4")])
         out["dof"][:] = rows["dof"]
@@ -233,11 +236,11 @@ class Solver:
         for k, m in enumerate(materials):
             law, E, nu, rho = m
             mats[k] = Material_(int(law), 0, float(E), float(nu), float(rho))
-        barr = _bc_array(bcs)
+        barr = bc_array(bcs)
         opts = _opts(t0, tf, scale_factor, max_steps, precision, steps_per_graph)
         h = C.c_void_p()
         _check(L.msx_create(C.byref(mesh), C.cast(mats, C.c_void_p), len(materials),
-                            _p(barr), len(bcs), C.byref(opts), C.byref(h)))
+                            _p(barr), len(barr), C.byref(opts), C.byref(h)))
         self.h = h
 
     def run(self, max_steps: int = 0) -> Report:
@@ -249,9 +252,9 @@ class Solver:
         return rep
 
     def next_solver(self, bcs, t0, tf, scale_factor, max_steps=0, precision=FP64, steps_per_graph=0):
-        barr = _bc_array(bcs)
+        barr = bc_array(bcs)
         opts = _opts(t0, tf, scale_factor, max_steps, precision, steps_per_graph)
-        _check(load().msx_next_solver(self.h, _p(barr), len(bcs), C.byref(opts)))
+        _check(load().msx_next_solver(self.h, _p(barr), len(barr), C.byref(opts)))
 
     def state(self, out=None):
         """u, v, a of the last step, into `out` (three contiguous float64 arrays
@@ -433,10 +436,10 @@ class Pool:
         mesh = Mesh_(X.shape[1], conn.shape[0], _p(X), _p(conn), None)
         law, E, nu, rho = material
         mat = Material_(int(law), 0, float(E), float(nu), float(rho))
-        barr = _bc_array(bcs)
+        barr = bc_array(bcs)
         opts = Opts_(t0, tf, scale_factor, max_steps, 0, 0)
         t = C.c_int64()
-        st = load().msx_pool_submit(self.h, C.byref(mesh), C.byref(mat), _p(barr), len(bcs),
+        st = load().msx_pool_submit(self.h, C.byref(mesh), C.byref(mat), _p(barr), len(barr),
                                     C.byref(opts), C.byref(t))
         if st == 9:
             return None
