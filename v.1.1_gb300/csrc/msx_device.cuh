@@ -1906,13 +1906,13 @@ __global__ void __launch_bounds__(kStepThreads) pool_node_kernel(const Problem *
 // The elements of one tile for the tiled element kernel: each thread's
 // elements in turn; returns the thread's FP32 minimum of the CFL screen.  The
 // FP64 and double-word kernels keep every screen value in sdt; the mixed one
-// only notes in `neg` whether one of its elements was a sliver (a negative
-// screen value).  The mixed and double-word bodies take the element's
+// keeps none and returns -1 once one of its elements was a sliver (a negative
+// screen value), so no other register stays live.  The mixed and double-word bodies take the element's
 // connectivity loaded one element ahead, so their node gathers wait for one
 // memory latency instead of two (connectivity, then the nodes).  ACT: element
 // birth is on, and the step's time decides which elements are dead.
 template <int MODE, bool ACT, bool VISC>
-__device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl, int parity, float *sdt, bool &neg)
+__device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl, int parity, float *sdt)
 {
     float v32 = INFINITY;
     const double t = ACT ? p.ctrl[parity].t : 0.0;
@@ -1929,14 +1929,17 @@ __device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl,
         float d = MODE == MODE_MIXED ? elem_body_mixed<false, ACT, VISC>(p, e, parity, cn, t, idtf)
                                      : (MODE == MODE_DW ? elem_body_dw<false, ACT, VISC>(p, e, parity, cn, t, idt)
                                                         : elem_body_fp64<false, ACT, VISC>(p, e, parity, t, idt));
-        if (MODE == MODE_MIXED) neg |= d < 0.0f;
-        else sdt[e - tl.begin] = d;
-        if (d >= 0.0f) v32 = fminf(v32, d);
+        if (MODE == MODE_MIXED) {
+            v32 = d < 0.0f ? -1.0f : fminf(v32, d);   // -1 sticks: fminf(-1, d) = -1 for d >= 0
+        } else {
+            sdt[e - tl.begin] = d;
+            if (d >= 0.0f) v32 = fminf(v32, d);
+        }
     }
     return v32;
 }
 
-constexpr int kMixedPending = 64;   // deferred FP64 rechecks a mixed CTA can hold
+constexpr int kMixedPending = 256;  // deferred FP64 rechecks a mixed CTA can hold
 
 // FP64 CFL values (cfl_dw) of one thread's elements of a mixed tile, their
 // minimum into the solve's CFL slot (a full pending list).
@@ -1947,17 +1950,20 @@ __device__ __forceinline__ void mixed_recheck(const Problem &p, const Tile &tl, 
     if (v >= 0.0 && v < INFINITY) atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
 }
 
-// The mixed kernel's tile loop.  Each tile's FP32 screen minimum goes to the
-// solve's running minimum (an integer atomicMin on its bit pattern, nothing
-// waited for); a thread whose own minimum lies within 2^-8 of the tile's, or
-// that met a sliver, posts (tile, thread, own minimum) to a per-CTA list.  Once
+// The mixed kernel's tile loop.  Each tile's FP32 screen minimum (over the
+// threads that met no sliver) goes to the solve's running minimum (an integer
+// atomicMin on its bit pattern, nothing waited for); a thread whose own
+// minimum lies within 2^-8 of the tile's, or that met a sliver, posts (tile,
+// thread, own minimum) to a per-CTA list.  Once
 // the CTA has run out of tiles, every entry whose minimum is still within
 // 2^-8 of the solve's running minimum -- by then nearly the step's FP32
-// minimum m -- has that thread's elements of that tile recomputed in FP64,
-// one element per thread of the CTA.  An element x near the exact minimum has
-// d(x) <= m (1 + 2^-8) <= (tile minimum) (1 + 2^-8), so its thread posted, and
-// the entry's minimum is <= d(x) <= (running minimum) (1 + 2^-8), so it is
-// rechecked.  A full list rechecks at once.
+// minimum m -- has that thread's elements of that tile recomputed in FP64 by
+// one warp of the CTA.  An element x near the exact minimum has
+// d(x) <= m (1 + 2^-8) <= (tile minimum) (1 + 2^-8) (the tile minimum, taken
+// over part of the elements, is >= m), so its thread posted unless it met a
+// sliver, and then it posted anyway; the entry's minimum is <= d(x) <=
+// (running minimum) (1 + 2^-8), so it is rechecked.  A full list rechecks at
+// once.
 template <bool ACT, bool VISC>
 __device__ __forceinline__ void mixed_tile_loop(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
                                                 TileQueue &q, int parity)
@@ -1977,9 +1983,9 @@ __device__ __forceinline__ void mixed_tile_loop(const Problem *__restrict__ desc
         const Tile tl = tiles[t];
         const Problem &p = descs[tl.solve];
         if (p.ctrl[parity].ran) {
-            bool neg = false;
-            const float mine = tile_elements<MODE_MIXED, ACT, VISC>(p, tl, parity, nullptr, neg);
-            const float bmin = block_min_bcast(mine);
+            const float mine = tile_elements<MODE_MIXED, ACT, VISC>(p, tl, parity, nullptr);
+            const bool neg = mine < 0.0f;
+            const float bmin = block_min_bcast(neg ? INFINITY : mine);
             if (threadIdx.x == 0 && bmin < INFINITY)
                 atomicMin(p.dtmin + 2 + (parity ^ 1), (unsigned long long)__float_as_uint(bmin));
             if (neg || (mine < INFINITY && mine <= bmin * (1.0f + 1.0f / 256.0f))) {
@@ -1997,33 +2003,28 @@ __device__ __forceinline__ void mixed_tile_loop(const Problem *__restrict__ desc
         __syncthreads();
         t = s_tile;
     }
-    // every entry was posted before the loop's last barrier
+    // every entry was posted before the loop's last barrier.  One warp per
+    // entry, its lanes over the posting thread's elements of that tile (one
+    // each when the tile has at most 32 per thread, as kMaxTileElems / 128 does)
     const int np = min(s_npend, kMixedPending);
-    if (np == 0) return;
-    const int per = (kMaxTileElems + blockDim.x - 1) / blockDim.x;   // elements of one thread in one tile, at most
-    double v = INFINITY;
-    const Problem *last = nullptr;
-    for (int idx = threadIdx.x; idx < np * per; idx += blockDim.x) {
-        const int j = idx % np, k = idx / np;
-        const Tile tl = tiles[s_pend[j].x];
-        const long long e = tl.begin + s_pend[j].y + (long long)k * blockDim.x;
-        if (e >= tl.end) continue;
+    const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+    for (int j = threadIdx.x >> 5; j < np; j += nwarp) {
+        const int2 pe = s_pend[j];
+        const Tile tl = tiles[pe.x];
         const Problem &p = descs[tl.solve];
         const float mine = s_pendv[j];
         if (!(mine < 0.0f)) {
             const unsigned long long g = __ldcg(p.dtmin + 2 + (parity ^ 1));
             if (g < kScreenInfBits && mine > __uint_as_float((unsigned)g) * (1.0f + 1.0f / 256.0f)) continue;
         }
-        const double c = cfl_dw(p, e);
-        if (&p != last && v < INFINITY) {   // another solve: flush this one's minimum
-            atomicMin(last->dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
-            v = INFINITY;
-        }
-        last = &p;
-        v = fmin(v, c);
+        double v = INFINITY;
+        for (long long e = tl.begin + pe.y + (long long)lane * blockDim.x; e < tl.end; e += 32LL * blockDim.x)
+            v = fmin(v, cfl_dw(p, e));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0 && v >= 0.0 && v < INFINITY)
+            atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
     }
-    if (last && v >= 0.0 && v < INFINITY)
-        atomicMin(last->dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
 }
 
 // Element kernel over tiles.  Each element's FP32 CFL screen value is
@@ -2063,8 +2064,7 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
         const Problem &p = descs[tl.solve];
         if (p.ctrl[parity].ran) {
             if (MODE != MODE_MIXED && threadIdx.x == 0) s_ncand = 0;
-            bool neg = false;   // slivers are listed from sdt below
-            const float v32 = tile_elements<MODE, ACT, VISC>(p, tl, parity, sdt, neg);
+            const float v32 = tile_elements<MODE, ACT, VISC>(p, tl, parity, sdt);
             const float bmin = block_min_bcast(v32);   // also orders the sdt writes before the reads below
             if (threadIdx.x == 0) {
                 // g: the solve's smallest FP32 screen value over the tiles closed
@@ -2158,12 +2158,12 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
     for (int k = 0; k < 9; k++) {
         double g = 0.0 + iJ[k];
         G[k * ne + e] = g;
-        G32[k * ne + e] = (float)g;
+        if (G32) G32[k * ne + e] = (float)g;
         if (p.G32lo) const_cast<float *>(p.G32lo)[k * ne + e] = (float)(g - (double)(float)g);
     }
     double w = 0.166666666667 * fabs(J);
     wJ[e] = w;
-    wJ32[e] = (float)w;
+    if (wJ32) wJ32[e] = (float)w;
     if (p.wJ32lo) const_cast<float *>(p.wJ32lo)[e] = (float)(w - (double)(float)w);
     double L = char_length_ref(pts);
     Lref[e] = L;
@@ -2190,7 +2190,36 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
 #pragma unroll
     for (int a = 1; a < 4; a++)
 #pragma unroll
-        for (int i = 0; i < 3; i++) Eref32[((a - 1) * 3 + i) * ne + e] = (float)(pts[a * 3 + i] - pts[i]);
+        for (int i = 0; i < 3; i++)
+            if (Eref32) Eref32[((a - 1) * 3 + i) * ne + e] = (float)(pts[a * 3 + i] - pts[i]);
+}
+
+// The FP32 element arrays of a precision mode that a handle starts using after
+// its set-up (a later solver block in another mode), from the FP64 set-up data
+// and X: the same conversions setup_elements_kernel makes, so the same bits.
+__global__ void mode_arrays_kernel(Problem p, const double *X, float *G32, float *wJ32, float *G32lo, float *wJ32lo,
+                                   float *Eref32)
+{
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.ne) return;
+    const long long ne = p.ne, nn = p.nn;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const double g = p.G[k * ne + e];
+        if (G32) G32[k * ne + e] = (float)g;
+        if (G32lo) G32lo[k * ne + e] = (float)(g - (double)(float)g);
+    }
+    const double w = p.wJ[e];
+    if (wJ32) wJ32[e] = (float)w;
+    if (wJ32lo) wJ32lo[e] = (float)(w - (double)(float)w);
+    if (Eref32) {
+        const int4 cn = p.conn[e];
+        const int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+#pragma unroll
+        for (int a = 1; a < 4; a++)
+#pragma unroll
+            for (int i = 0; i < 3; i++) Eref32[((a - 1) * 3 + i) * ne + e] = (float)(X[i * nn + nd[a]] - X[i * nn + nd[0]]);
+    }
 }
 
 // Previous-step F diagonal for the bulk viscosity, from displacement u, in the

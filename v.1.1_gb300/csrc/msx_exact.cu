@@ -29,6 +29,12 @@ void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s)
         const_cast<float *>(p.Eref32));
 }
 
+void launch_mode_arrays(const Problem &p, const double *X, float *G32, float *wJ32, float *G32lo, float *wJ32lo,
+                        float *Eref32, cudaStream_t s)
+{
+    mode_arrays_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, X, G32, wJ32, G32lo, wJ32lo, Eref32);
+}
+
 void launch_visc_init(const Problem &p, const double *u, cudaStream_t s)
 {
     visc_init_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, u);

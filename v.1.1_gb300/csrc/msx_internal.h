@@ -190,6 +190,9 @@ void launch_elem_exact(const Problem &p, int parity, cudaStream_t s);
 // set-up (exact operation order)
 void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s);
 void launch_setup_mass(const Problem &p, double *mass, double *minv, cudaStream_t s);
+// a precision mode's FP32 element arrays (any pointer may be null) from G, wJ and X
+void launch_mode_arrays(const Problem &p, const double *X, float *G32, float *wJ32, float *G32lo, float *wJ32lo,
+                        float *Eref32, cudaStream_t s);
 // bulk viscosity: the elements' previous-step F diagonal from displacement u
 void launch_visc_init(const Problem &p, const double *u, cudaStream_t s);
 // min over elements of Lref/c (undeformed) or min(Lref, L(X+u))/c, into dtmin[slot]

@@ -122,6 +122,7 @@ struct msx_handle {
     long long max_steps = 0;
     int precision = MSX_PREC_FP64;
     int spg = 64;
+    int graph_steps = 0;   // steps captured in `graph` (spg, or fewer for a short first call)
     bool block_ready = false;
     double last_t = 0;   // time of the last step run (external force of node extraction)
     long long block_steps = 0;
@@ -425,6 +426,61 @@ static msx_status upload_bcs(msx_handle *h, const msx_bc *bcs, long long nbc)
     return MSX_OK;
 }
 
+// The arrays only some precision modes read, allocated the first time a block
+// runs in such a mode (an FP64 handle of the 6M-tet cube saves ~0.95 GB and its
+// allocation time): FP32 G and wJ (mixed, double-word), their low words
+// (double-word), the FP32 reference edges of the CFL screen (every mode but
+// mixed), the (hi, lo) nodal state and 1/m (mixed, double-word), and the corner
+// forces as FP64 (or double-word) or FP32 slots.  With `fill`, derived arrays
+// are converted from the FP64 set-up data (a later block in a new mode); at
+// msx_create the set-up kernels fill them.
+static msx_status mode_buffers(msx_handle *h, int precision, bool fill)
+{
+    const long long ne = h->P.ne, nn = h->P.nn;
+    const bool mixed = precision == MSX_PREC_MIXED, dw = precision == MSX_PREC_DOUBLE_WORD;
+    float *G32 = nullptr, *wJ32 = nullptr, *G32lo = nullptr, *wJ32lo = nullptr, *Eref32 = nullptr;
+    bool minv2 = false;
+    if ((mixed || dw) && !h->G32.p) {
+        MSX_CUDA(h->G32.alloc(9 * ne));
+        MSX_CUDA(h->wJ32.alloc(ne));
+        G32 = h->G32.p;
+        wJ32 = h->wJ32.p;
+    }
+    if (dw && !h->G32lo.p) {
+        MSX_CUDA(h->G32lo.alloc(9 * ne));
+        MSX_CUDA(h->wJ32lo.alloc(ne));
+        G32lo = h->G32lo.p;
+        wJ32lo = h->wJ32lo.p;
+    }
+    if (!mixed && !h->Eref32.p) {
+        MSX_CUDA(h->Eref32.alloc(9 * ne));
+        Eref32 = h->Eref32.p;
+    }
+    if ((mixed || dw) && !h->uhl.p) {
+        MSX_CUDA(h->uhl.alloc(3 * nn));
+        MSX_CUDA(h->vhl.alloc(3 * nn));
+        MSX_CUDA(h->ahl.alloc(3 * nn));
+        MSX_CUDA(h->minv2.alloc(nn));
+        minv2 = true;
+    }
+    if (mixed && !h->fe32.p) {
+        MSX_CUDA(h->fe32.alloc(16 * ne));
+        MSX_CUDA(cudaMemsetAsync(h->fe32.p, 0, sizeof(float) * 16 * ne, h->stream));
+    }
+    if (!mixed && !h->fe.p) {
+        MSX_CUDA(h->fe.alloc(12 * ne));
+        MSX_CUDA(cudaMemsetAsync(h->fe.p, 0, sizeof(double) * 12 * ne, h->stream));
+    }
+    bind_problem(h);
+    if (fill) {
+        if (G32 || G32lo || Eref32) launch_mode_arrays(h->P, h->X.p, G32, wJ32, G32lo, wJ32lo, Eref32, h->stream);
+        if (minv2) launch_minv_split(h->minv.p, h->minv2.p, nn, h->stream);
+        MSX_CUDA(cudaGetLastError());
+        MSX_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    return MSX_OK;
+}
+
 // Inputs of a double-word block (see dw_in_range): the materials, and the
 // coordinates through one device reduction (once per handle).
 static msx_status check_double_word(msx_handle *h)
@@ -516,7 +572,8 @@ static msx_status init_block(msx_handle *h)
     return MSX_OK;
 }
 
-static msx_status build_graph(msx_handle *h)
+// Captures `steps` (even) steps: replays start on parity 1 and keep it.
+static msx_status build_graph(msx_handle *h, int steps)
 {
     if (h->graph) {
         cudaGraphExecDestroy(h->graph);
@@ -524,8 +581,9 @@ static msx_status build_graph(msx_handle *h)
     }
     bind_problem(h);
     cudaGraph_t g;
+    h->graph_steps = steps;
     MSX_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < h->spg; i++) launch_step(h, (i & 1) ? 0 : 1);
+    for (int i = 0; i < steps; i++) launch_step(h, (i & 1) ? 0 : 1);
     cudaError_t err = cudaStreamEndCapture(h->stream, &g);
     if (err != cudaSuccess) return fail(MSX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(err));
     err = cudaGraphInstantiate(&h->graph, g, 0);
@@ -615,24 +673,13 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     ALLOC(h->G, 9 * ne);
     ALLOC(h->wJ, ne);
     ALLOC(h->Lref, ne);
-    ALLOC(h->G32, 9 * ne);
-    ALLOC(h->wJ32, ne);
     ALLOC(h->Lref32, ne);
-    ALLOC(h->Eref32, 9 * ne);
-    ALLOC(h->G32lo, 9 * ne);
-    ALLOC(h->wJ32lo, ne);
     ALLOC(h->X, 3 * nn);
     ALLOC(h->u, 3 * nn);
     ALLOC(h->v, 3 * nn);
     ALLOC(h->a, 3 * nn);
     ALLOC(h->mass, nn);
     ALLOC(h->minv, nn);
-    ALLOC(h->uhl, 3 * nn);
-    ALLOC(h->vhl, 3 * nn);
-    ALLOC(h->ahl, 3 * nn);
-    ALLOC(h->minv2, nn);
-    ALLOC(h->fe, 12 * ne);
-    ALLOC(h->fe32, 16 * ne);
     ALLOC(h->slot, ne);
     ALLOC(h->node_ptr, nn + 1);
     ALLOC(h->node_inc, 4 * ne);
@@ -641,6 +688,8 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     ALLOC(h->flags, 2);
     if (mesh->elem_material && num_mats > 1) ALLOC(h->mat, ne);
 #undef ALLOC
+    // the first block's mode's own arrays, filled by the set-up kernels below
+    if ((st = mode_buffers(h, h->precision, false)) != MSX_OK) return bail(st);
     cudaStream_t s = h->stream;
     std::vector<unsigned char> mids;
     if (h->mat.p) {
@@ -660,8 +709,6 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     }
     if (h->mat.p) UP(h->mat.p, mids.data(), ne);
 #undef UP
-    cudaMemsetAsync(h->fe.p, 0, sizeof(double) * 12 * ne, s);
-    cudaMemsetAsync(h->fe32.p, 0, sizeof(float) * 16 * ne, s);
     cudaMemsetAsync(h->u.p, 0, sizeof(double) * 3 * nn, s);
     cudaMemsetAsync(h->v.p, 0, sizeof(double) * 3 * nn, s);
     cudaMemsetAsync(h->a.p, 0, sizeof(double) * 3 * nn, s);
@@ -669,7 +716,7 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     h->P.mat = h->mat.p;
     launch_setup_elements(h->P, h->X.p, s);
     launch_setup_mass(h->P, h->mass.p, h->minv.p, s);
-    launch_minv_split(h->minv.p, h->minv2.p, nn, s);
+    if (h->minv2.p) launch_minv_split(h->minv.p, h->minv2.p, nn, s);
     if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
         return bail(fail(MSX_ERR_CUDA, "set-up kernels failed"));
     if (h->precision == MSX_PREC_DOUBLE_WORD && (st = check_double_word(h)) != MSX_OK) return bail(st);
@@ -1045,7 +1092,6 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
     if (!h) return fail(MSX_ERR_ARG, "NULL handle");
     msx_status st;
     if (!h->block_ready && (st = init_block(h)) != MSX_OK) return st;
-    if (!h->graph && (st = build_graph(h)) != MSX_OK) return st;
     long long start_steps = 0;
     if ((st = arm_block(h, max_steps, &start_steps)) != MSX_OK) return st;
     Ctrl latest = h->h_ctrl[0];
@@ -1053,7 +1099,14 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
     // limit's last step is post-updated, and the stop raised, by one more node
     // kernel, so room + 1 node kernels in all
     const long long room = latest.limit - latest.step;
-    const long long needed = room >= (1LL << 61) ? (1LL << 62) : (room + 1 + h->spg - 1) / h->spg;
+    // The graph holds steps_per_graph steps; a handle's first call that needs
+    // fewer captures only those (even), and a later call that needs more than a
+    // short graph holds captures the full length once.
+    const long long want = room >= (1LL << 61) ? h->spg : std::min<long long>(h->spg, (room + 2) & ~1LL);
+    if (!h->graph || (h->graph_steps < h->spg && want > h->graph_steps))
+        if ((st = build_graph(h, h->graph ? h->spg : (int)want)) != MSX_OK) return st;
+    const long long gs = h->graph_steps;
+    const long long needed = room >= (1LL << 61) ? (1LL << 62) : (room + 1 + gs - 1) / gs;
     MSX_CUDA(cudaEventRecord(h->ev0, h->stream));
     // two replays in flight: check the older one's control slot
     long long k = 0;
@@ -1084,7 +1137,7 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
         rep->dt_init = h->dt_init;
         rep->status = fin.status;
         rep->device_ms = ms;
-        rep->kernel_launches = (k + 1) * 2LL * h->spg;
+        rep->kernel_launches = (k + 1) * 2LL * h->graph_steps;
     }
     if (fin.status == MSX_ERR_NEG_JACOBIAN) return fail(MSX_ERR_NEG_JACOBIAN, "Negative jacobian: dt < 1e-20");
     if (fin.status == MSX_ERR_NAN) return fail(MSX_ERR_NAN, "There are NANs in the displacements");
@@ -1238,6 +1291,7 @@ extern "C" msx_status msx_next_solver(msx_handle *h, const msx_bc *bcs, int64_t 
     msx_status st;
     if (opts && opts->precision == MSX_PREC_DOUBLE_WORD && (st = check_double_word(h)) != MSX_OK) return st;
     if ((st = set_opts(h, opts)) != MSX_OK) return st;
+    if ((st = mode_buffers(h, h->precision, true)) != MSX_OK) return st;
     if ((st = upload_bcs(h, bcs, num_bcs)) != MSX_OK) return st;
     if (h->graph) {
         cudaGraphExecDestroy(h->graph);
