@@ -53,16 +53,16 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profiled(key, name="element_kernel_fp64_cube.md"):
-    """A per-element figure of an element kernel from its committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", name)
+def profiled(key, kernel="pool_elem_kernel<FP64>"):
+    """A per-element figure of a kernel from the committed ncu captures
+    (profiles/ncu_figures.json: DRAM bytes per element from one --set full
+    capture on the 64^3 cube, FP64 instructions per element, the FP64 peak
+    measured with a DFMA loop), or None."""
     try:
-        for line in open(path):
-            if line.startswith(key + ":"):
-                return float(line.split(":")[1].split()[0])
-    except OSError:
-        pass
-    return None
+        with open(os.path.join(ROOT, "profiles", "ncu_figures.json")) as f:
+            return float(json.load(f)[kernel][key])
+    except (OSError, KeyError, ValueError, TypeError):
+        return None
 
 
 class Clocks:
@@ -136,7 +136,7 @@ def mixed_roofline(ne, nn, prof, ms_per_step):
     alg_elem, alg_step = 72.0 * ne, 72.0 * ne + 176.0 * nn
     ach = alg_elem / (prof.element_ms * 1e-3) / 1e9
     step = alg_step / (ms_per_step * 1e-3) / 1e9
-    tr = profiled("dram_bytes_per_element", "element_kernel_mixed_cube.md")
+    tr = profiled("dram_bytes_per_element", "pool_elem_kernel<MIXED>")
     return {"bound": "hbm", "kernel": "pool_elem_kernel<MIXED>", "achieved": ach, "peak": peak, "unit": "GB/s",
             "frac": ach / peak, "peak_kind": peak_kind, "traffic": tr * ne if tr else None,
             "alg_bytes_per_launch": alg_elem,
@@ -150,7 +150,7 @@ def dword_roofline(ne, nn, prof, ms_per_step):
     alg_elem, alg_step = 100.0 * ne, 100.0 * ne + 176.0 * nn
     ach = alg_elem / (prof.element_ms * 1e-3) / 1e9
     step = alg_step / (ms_per_step * 1e-3) / 1e9
-    tr = profiled("dram_bytes_per_element", "element_kernel_dword_cube.md")
+    tr = profiled("dram_bytes_per_element", "pool_elem_kernel<DW>")
     return {"bound": "hbm", "kernel": "pool_elem_kernel<DW>", "achieved": ach, "peak": peak, "unit": "GB/s",
             "frac": ach / peak, "peak_kind": peak_kind, "traffic": tr * ne if tr else None,
             "alg_bytes_per_launch": alg_elem,
@@ -616,7 +616,7 @@ def main():
                 "fp64_pipe": None if not ops else {
                     "achieved_gops": ops * ne / (prof.element_ms * 1e-3) / 1e9, "peak_gops": opk,
                     "frac": ops * ne / (prof.element_ms * 1e-3) / 1e9 / opk, "ops_per_element": ops,
-                    "note": "FP64 ops/element from ncu counters (profiles/element_kernel_fp64_cube.md); "
+                    "note": "FP64 ops/element from ncu counters (profiles/ncu_figures.json); "
                             "peak from a DFMA/DADD loop on this GPU"},
                 "note": "the kernel is bound by the FP64 pipe, not by HBM; both fractions are reported"}
     line = {"metric": METRIC, "value": value, "unit": "element-steps/s", "n_gpus": ws, "steps": args.steps,

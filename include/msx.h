@@ -85,7 +85,7 @@ typedef struct {
     double t0, tf, scale_factor;  /* *Time t0, tf and *Scale Factor                        */
     int64_t max_steps;            /* 0: run to tf like the reference; >0: stop after N     */
     int32_t precision;            /* MSX_PREC_*                                            */
-    int32_t steps_per_graph;      /* steps per captured CUDA graph; 0 = default (64)       */
+    int32_t steps_per_graph;      /* steps per full CUDA-graph chunk; 0 = default (64)     */
 } msx_solver_opts;
 
 typedef struct {

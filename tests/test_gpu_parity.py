@@ -129,6 +129,31 @@ def test_graph_chunk_size_does_not_change_results():
     assert all(np.array_equal(x, y) for x, y in zip(r1, r2))
 
 
+@pytest.mark.parametrize("precision", [msx.FP64, msx.MIXED])
+def test_split_calls_replay_at_most_one_idle_step(precision):
+    """Calls of any length run full chunks plus power-of-two remainders: the
+    state after calls of 1, 2, 5, 20, 64 and 13 steps is bitwise that of one
+    105-step call, and each call launches at most K + 2 step pairs."""
+    X, conn = msx.mesh_cube(4, seed=3)
+    bcs = msx.cube_bcs(4, 0.5, msx.BC_VEL_RAMP, 50)
+    mat = [(msx.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0)]
+
+    def solver():
+        return msx.Solver(X, conn, mat, bcs, 0.0, 1e30, 0.5, max_steps=0, precision=precision,
+                          steps_per_graph=16)
+
+    A = solver()
+    for k in (1, 2, 5, 20, 64, 13):
+        rep = A.run(k)
+        assert rep.steps == k
+        assert k + 1 <= rep.kernel_launches // 2 <= k + 2, (k, rep.kernel_launches)
+    B = solver()
+    assert B.run(105).steps == 105
+    assert all(np.array_equal(x, y) for x, y in zip(A.state(), B.state()))
+    A.close()
+    B.close()
+
+
 def test_setup_data_bitwise_equal_to_oracle():
     mesh, mats, solvers, _, _ = load("cube4_stvk_ramp")
     S = msx.Solver(mesh.X, mesh.conn, [(m.law, m.young, m.nu, m.rho) for m in mats], solvers[0].bcs,

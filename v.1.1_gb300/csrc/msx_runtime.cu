@@ -122,7 +122,6 @@ struct msx_handle {
     long long max_steps = 0;
     int precision = MSX_PREC_FP64;
     int spg = 64;
-    int graph_steps = 0;   // steps captured in `graph` (spg, or fewer for a short first call)
     bool block_ready = false;
     double last_t = 0;   // time of the last step run (external force of node extraction)
     long long block_steps = 0;
@@ -142,12 +141,17 @@ struct msx_handle {
     int tile_elems = 0;                 // element-tile size of d_etiles
     DBuf<int> d_counts;
     int tgrid = 0, tgrid_node = 0, tthreads = kStepThreads;
+    // captured step chunks: `graph` holds spg steps; part[k] (k >= 1) holds 2^k
+    // steps and runs a call's remainder, so a call replays at most one idle step
     cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t part[31] = {};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc[2] = {nullptr, nullptr};
     std::vector<int> h_node_bc;   // host copies for next_solver rebuilds
     bool dw_coords_checked = false, dw_coords_ok = false;   // double-word range of the coordinates
     bool u_zero = true;   // u is still the all-zero state msx_create set (no step run, no state set)
 };
+
+static void drop_graphs(msx_handle *h);
 
 // ------------------------------------------------------------------ host helpers
 // Law parameters of one material (shared by single solves and the pool);
@@ -394,10 +398,7 @@ static msx_status upload_tiled(msx_handle *h)
         MSX_CUDA(cudaMemcpyAsync(h->d_ntiles.p, nt.data(), sizeof(Tile) * nt.size(), cudaMemcpyHostToDevice, h->stream));
         MSX_CUDA(cudaMemcpyAsync(h->d_counts.p, counts, sizeof(counts), cudaMemcpyHostToDevice, h->stream));
         h->tile_elems = te;
-        if (h->graph) {   // the captured launches name the old tile lists
-            cudaGraphExecDestroy(h->graph);
-            h->graph = nullptr;
-        }
+        drop_graphs(h);   // the captured launches name the old tile lists
     }
     MSX_CUDA(cudaMemcpyAsync(h->d_desc.p, &h->P, sizeof(Problem), cudaMemcpyHostToDevice, h->stream));
     MSX_CUDA(cudaStreamSynchronize(h->stream));
@@ -572,23 +573,33 @@ static msx_status init_block(msx_handle *h)
     return MSX_OK;
 }
 
-// Captures `steps` (even) steps: replays start on parity 1 and keep it.
-static msx_status build_graph(msx_handle *h, int steps)
+// Destroys the captured step chunks (their launches name the tile lists, the
+// kernel instantiation and, in the exact mode, the Problem by value).
+static void drop_graphs(msx_handle *h)
 {
-    if (h->graph) {
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+    for (auto &g : h->part) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
     }
+}
+
+// Captures `steps` (even) steps into *out: replays start on parity 1 and keep it.
+static msx_status build_graph(msx_handle *h, int steps, cudaGraphExec_t *out)
+{
     bind_problem(h);
     cudaGraph_t g;
-    h->graph_steps = steps;
     MSX_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     for (int i = 0; i < steps; i++) launch_step(h, (i & 1) ? 0 : 1);
     cudaError_t err = cudaStreamEndCapture(h->stream, &g);
     if (err != cudaSuccess) return fail(MSX_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(err));
-    err = cudaGraphInstantiate(&h->graph, g, 0);
+    err = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
-    if (err != cudaSuccess) return fail(MSX_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(err));
+    if (err != cudaSuccess) {
+        *out = nullptr;
+        return fail(MSX_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(err));
+    }
     return MSX_OK;
 }
 
@@ -730,7 +741,7 @@ extern "C" msx_status msx_destroy(msx_handle *h)
 {
     if (!h) return MSX_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
-    if (h->graph) cudaGraphExecDestroy(h->graph);
+    drop_graphs(h);
     DBuf<int4> *b4[] = {&h->conn, &h->slot};
     for (auto *b : b4) b->release();
     for (auto *b : {&h->G, &h->wJ, &h->Lref, &h->X, &h->u, &h->v, &h->a, &h->mass, &h->minv, &h->fe}) b->release();
@@ -1003,10 +1014,7 @@ extern "C" msx_status msx_set_load_blocks(msx_handle *h, const msx_load_block *b
     msx_status st = upload_tiled(h);
     if (st != MSX_OK) return st;
     MSX_CUDA(cudaStreamSynchronize(h->stream));
-    if (h->graph) {   // the step's kernel list (face kernel) and the exact mode's Problem changed
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;
-    }
+    drop_graphs(h);   // the step's kernel list (face kernel) and the exact mode's Problem changed
     return MSX_OK;
 }
 
@@ -1026,10 +1034,7 @@ extern "C" msx_status msx_set_activation(msx_handle *h, const double *activation
     msx_status st = upload_tiled(h);
     if (st != MSX_OK) return st;
     MSX_CUDA(cudaStreamSynchronize(h->stream));
-    if (h->graph) {   // the exact mode's captured launches hold the Problem by value
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;
-    }
+    drop_graphs(h);   // the exact mode's captured launches hold the Problem by value
     return MSX_OK;
 }
 
@@ -1062,10 +1067,7 @@ extern "C" msx_status msx_set_viscosity(msx_handle *h, int32_t kind, double c1, 
     msx_status st = upload_tiled(h);
     if (st != MSX_OK) return st;
     MSX_CUDA(cudaStreamSynchronize(h->stream));
-    if (h->graph) {   // another element-kernel instantiation, and the exact mode's launches hold the Problem
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;
-    }
+    drop_graphs(h);   // another element-kernel instantiation, and the exact mode's launches hold the Problem
     return MSX_OK;
 }
 
@@ -1099,19 +1101,31 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
     // limit's last step is post-updated, and the stop raised, by one more node
     // kernel, so room + 1 node kernels in all
     const long long room = latest.limit - latest.step;
-    // The graph holds steps_per_graph steps; a handle's first call that needs
-    // fewer captures only those (even), and a later call that needs more than a
-    // short graph holds captures the full length once.
-    const long long want = room >= (1LL << 61) ? h->spg : std::min<long long>(h->spg, (room + 2) & ~1LL);
-    if (!h->graph || (h->graph_steps < h->spg && want > h->graph_steps))
-        if ((st = build_graph(h, h->graph ? h->spg : (int)want)) != MSX_OK) return st;
-    const long long gs = h->graph_steps;
-    const long long needed = room >= (1LL << 61) ? (1LL << 62) : (room + 1 + gs - 1) / gs;
+    // Full chunks of steps_per_graph steps, then the remainder (rounded up to
+    // even) as power-of-two chunks, largest first; an open-ended block
+    // replays full chunks until the device raises the stop.
+    const bool open = room >= (1LL << 61);
+    long long full = open ? (1LL << 62) : (room + 1) / h->spg;
+    long long rest = open ? 0 : ((room + 1 - full * h->spg) + 1) & ~1LL;
+    if (rest >= h->spg) {
+        full++;
+        rest = 0;
+    }
+    int parts[31], nparts = 0;
+    for (int b = 30; b >= 1; b--)
+        if (rest & (1LL << b)) parts[nparts++] = b;
+    if (full == 0 && nparts == 0) parts[nparts++] = 1;   // a stopped block: one short replay reports it
+    if (full > 0 && !h->graph && (st = build_graph(h, h->spg, &h->graph)) != MSX_OK) return st;
+    for (int j = 0; j < nparts; j++)
+        if (!h->part[parts[j]] && (st = build_graph(h, 1 << parts[j], &h->part[parts[j]])) != MSX_OK) return st;
+    const long long needed = full + nparts;
     MSX_CUDA(cudaEventRecord(h->ev0, h->stream));
     // two replays in flight: check the older one's control slot
-    long long k = 0;
+    long long k = 0, replayed = 0;
     for (;; k++) {
-        MSX_CUDA(cudaGraphLaunch(h->graph, h->stream));
+        const bool whole = k < full;
+        MSX_CUDA(cudaGraphLaunch(whole ? h->graph : h->part[parts[k - full]], h->stream));
+        replayed += whole ? h->spg : (1LL << parts[k - full]);
         MSX_CUDA(cudaMemcpyAsync(h->h_ctrl + (k & 1), h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
         MSX_CUDA(cudaEventRecord(h->evc[k & 1], h->stream));
         if (latest.stop || k + 1 >= needed) break;
@@ -1137,7 +1151,7 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
         rep->dt_init = h->dt_init;
         rep->status = fin.status;
         rep->device_ms = ms;
-        rep->kernel_launches = (k + 1) * 2LL * h->graph_steps;
+        rep->kernel_launches = 2 * replayed;
     }
     if (fin.status == MSX_ERR_NEG_JACOBIAN) return fail(MSX_ERR_NEG_JACOBIAN, "Negative jacobian: dt < 1e-20");
     if (fin.status == MSX_ERR_NAN) return fail(MSX_ERR_NAN, "There are NANs in the displacements");
@@ -1293,10 +1307,7 @@ extern "C" msx_status msx_next_solver(msx_handle *h, const msx_bc *bcs, int64_t 
     if ((st = set_opts(h, opts)) != MSX_OK) return st;
     if ((st = mode_buffers(h, h->precision, true)) != MSX_OK) return st;
     if ((st = upload_bcs(h, bcs, num_bcs)) != MSX_OK) return st;
-    if (h->graph) {
-        cudaGraphExecDestroy(h->graph);
-        h->graph = nullptr;
-    }
+    drop_graphs(h);
     return MSX_OK;
 }
 
