@@ -2132,6 +2132,11 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
     if (e >= p.ne) return;
     const long long nn = p.nn, ne = p.ne;
     int4 cn = p.conn[e];
+    // an out-of-range node id: the node-list build queued after this kernel
+    // rejects the mesh
+    if ((unsigned long long)(unsigned)cn.x >= (unsigned long long)nn || (unsigned long long)(unsigned)cn.y >= (unsigned long long)nn ||
+        (unsigned long long)(unsigned)cn.z >= (unsigned long long)nn || (unsigned long long)(unsigned)cn.w >= (unsigned long long)nn)
+        return;
     int nd[4] = {cn.x, cn.y, cn.z, cn.w};
     double xyz[12], pts[12];
 #pragma unroll

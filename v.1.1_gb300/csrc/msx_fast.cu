@@ -99,6 +99,18 @@ void launch_minv_split(const double *minv, float2 *minv2, long long nn, cudaStre
     minv_split_kernel<<<grid_for(nn, 256), 256, 0, s>>>(minv, minv2, nn);
 }
 
+__global__ void node_bc_scatter_kernel(int *node_bc, const int2 *nodes, long long n)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) node_bc[nodes[k].x] = nodes[k].y;
+}
+
+void launch_node_bc_scatter(int *node_bc, long long nn, const int2 *nodes, long long n, cudaStream_t s)
+{
+    cudaMemsetAsync(node_bc, 0xFF, sizeof(int) * nn, s);   // -1: no entry
+    if (n > 0) node_bc_scatter_kernel<<<grid_for(n, 256), 256, 0, s>>>(node_bc, nodes, n);
+}
+
 __global__ void abs_range_kernel(const double *x, long long n, unsigned long long *mm)
 {
     unsigned long long lo = ~0ULL, hi = 0;

@@ -3,6 +3,7 @@
 #pragma once
 #include <cstdint>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "../../include/msx.h"
@@ -244,5 +245,20 @@ void launch_abs_range(const double *x, long long n, unsigned long long *mm, cuda
 constexpr int kCsrMaxDegree = 1024;
 msx_status build_node_csr(const int4 *conn, const int *conn_host, long long ne, long long nn, int *node_ptr,
                           int *node_inc, int4 *slot, cudaStream_t s, std::string &err);
+
+// The Dirichlet tables of one solve, built on the host in O(nbc log nbc)
+// (nothing per node): `nodes` holds (node, record) for each node with an
+// entry, ascending by node; `rec` three (first entry, count) records per such
+// node, one per component; `ent` the entries grouped by DOF, each DOF's in
+// input order (the order the reference applies them in).  MSX_ERR_ARG with
+// the reason in err for a bad entry.
+struct BCTables {
+    std::vector<int2> nodes, rec;
+    std::vector<BCEntry> ent;
+};
+msx_status build_bc_tables(long long nn, const msx_bc *bcs, long long nbc, double t0, double tf, BCTables &t,
+                           std::string &err);
+// node_bc[nn] = -1 except node_bc[nodes[k].x] = nodes[k].y (device arrays)
+void launch_node_bc_scatter(int *node_bc, long long nn, const int2 *nodes, long long n, cudaStream_t s);
 
 }  // namespace msx

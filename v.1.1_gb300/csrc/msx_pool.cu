@@ -170,7 +170,8 @@ static size_t footprint(long long nn, long long ne, long long nbc, int precision
     b += precision == MSX_PREC_MIXED ? align256(sizeof(float) * 16 * ne) : align256(sizeof(double) * 12 * ne);
     b += align256(sizeof(int) * (nn + 1)) + align256(sizeof(int) * 4 * ne) + align256(sizeof(int) * nn);
     b += align256(sizeof(int4) * ne);                                                // corner slots
-    b += align256(sizeof(int2) * 3 * nn) + align256(sizeof(BCEntry) * (nbc > 0 ? nbc : 1));
+    const long long nbcn = std::max(1LL, std::min(nn, nbc));   // nodes with Dirichlet entries, at most
+    b += align256(sizeof(int2) * 3 * nbcn) + align256(sizeof(int2) * nbcn) + align256(sizeof(BCEntry) * (nbc > 0 ? nbc : 1));
     return b;
 }
 
@@ -575,31 +576,11 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
 
     // host tables, without the pool's lock: Dirichlet records (as the
     // single-solve path); the node -> corner lists are built on the device
-    std::vector<int> node_bc(nn, -1);
-    std::vector<long long> order(num_bcs);
-    std::iota(order.begin(), order.end(), 0);
-    for (long long k = 0; k < num_bcs; k++) {
-        if (bcs[k].dof < 0 || bcs[k].dof >= 3 * nn || bcs[k].mode < 0 || bcs[k].mode > 3)
-            return pfail(MSX_ERR_ARG, "bad boundary condition entry");
-        if (bcs[k].mode == MSX_BC_RAMP && !(o->tf - o->t0 != 0)) return pfail(MSX_ERR_ARG, "ramp BC needs tf != t0");
-    }
-    std::stable_sort(order.begin(), order.end(), [&](long long x, long long y) { return bcs[x].dof < bcs[y].dof; });
-    std::vector<int2> rec;
-    std::vector<BCEntry> ent;
-    for (long long k = 0; k < num_bcs; k++) {
-        const msx_bc &b = bcs[order[k]];
-        BCEntry e{b.mode == MSX_BC_RAMP_RATE ? MSX_BC_RAMP : b.mode, b.ramp_steps,
-                  b.mode == MSX_BC_RAMP ? b.value / (o->tf - o->t0) : b.value};
-        long long node = b.dof % nn;
-        int comp = (int)(b.dof / nn);
-        if (node_bc[node] < 0) {
-            node_bc[node] = (int)(rec.size() / 3);
-            rec.resize(rec.size() + 3, make_int2(0, 0));
-        }
-        int2 &r = rec[node_bc[node] * 3 + comp];
-        if (r.y == 0) r.x = (int)ent.size();
-        r.y++;
-        ent.push_back(e);
+    BCTables bt;
+    {
+        std::string err;
+        if (build_bc_tables(nn, bcs, num_bcs, o->t0, o->tf, bt, err) != MSX_OK)
+            return pfail(MSX_ERR_ARG, "bad boundary condition entry: " + err);
     }
 
     int slot = -1;
@@ -672,7 +653,9 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
         int *d_ptr = (int *)carve(sizeof(int) * (nn + 1)), *d_inc = (int *)carve(sizeof(int) * 4 * ne);
         int *d_nbc = (int *)carve(sizeof(int) * nn);
         int4 *d_slot = (int4 *)carve(sizeof(int4) * ne);
-        int2 *d_rec = (int2 *)carve(sizeof(int2) * 3 * nn);
+        const long long nbcn = std::max(1LL, std::min(nn, (long long)num_bcs));
+        int2 *d_rec = (int2 *)carve(sizeof(int2) * 3 * nbcn);
+        int2 *d_bcn = (int2 *)carve(sizeof(int2) * nbcn);
         BCEntry *d_ent = (BCEntry *)carve(sizeof(BCEntry) * (num_bcs > 0 ? num_bcs : 1));
         if ((size_t)(q - (char *)sl.arena) > bytes)   // the footprint must cover every array carved above
             return pfail(MSX_ERR_CUDA, "internal: solve arena smaller than its arrays");
@@ -697,9 +680,13 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
             const msx_status cst = build_node_csr(P.conn, mesh->conn, ne, nn, d_ptr, d_inc, d_slot, s, err);
             if (cst != MSX_OK) return pfail(cst, err);
         }
-        PCUDA(cudaMemcpyAsync(d_nbc, node_bc.data(), sizeof(int) * nn, cudaMemcpyHostToDevice, s));
-        if (!rec.empty()) PCUDA(cudaMemcpyAsync(d_rec, rec.data(), sizeof(int2) * rec.size(), cudaMemcpyHostToDevice, s));
-        if (!ent.empty()) PCUDA(cudaMemcpyAsync(d_ent, ent.data(), sizeof(BCEntry) * ent.size(), cudaMemcpyHostToDevice, s));
+        if (!bt.nodes.empty())
+            PCUDA(cudaMemcpyAsync(d_bcn, bt.nodes.data(), sizeof(int2) * bt.nodes.size(), cudaMemcpyHostToDevice, s));
+        launch_node_bc_scatter(d_nbc, nn, d_bcn, (long long)bt.nodes.size(), s);
+        if (!bt.rec.empty())
+            PCUDA(cudaMemcpyAsync(d_rec, bt.rec.data(), sizeof(int2) * bt.rec.size(), cudaMemcpyHostToDevice, s));
+        if (!bt.ent.empty())
+            PCUDA(cudaMemcpyAsync(d_ent, bt.ent.data(), sizeof(BCEntry) * bt.ent.size(), cudaMemcpyHostToDevice, s));
         PCUDA(cudaMemsetAsync(P.u, 0, sizeof(double) * 3 * nn, s));
         PCUDA(cudaMemsetAsync(P.v, 0, sizeof(double) * 3 * nn, s));
         PCUDA(cudaMemsetAsync(P.a, 0, sizeof(double) * 3 * nn, s));

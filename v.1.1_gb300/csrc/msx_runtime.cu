@@ -102,6 +102,7 @@ struct msx_handle {
     DBuf<float2> uhl, vhl, ahl, minv2;
     DBuf<unsigned char> mat;
     DBuf<int> node_ptr, node_inc, node_bc;
+    DBuf<int2> bc_nodes;   // (node, record) of the nodes with Dirichlet entries
     DBuf<int2> bc_rec;
     DBuf<BCEntry> bcs;
     // Neumann loads: term lists per DOF, nodal-force entries, gravity terms per
@@ -146,7 +147,6 @@ struct msx_handle {
     cudaGraphExec_t graph = nullptr;
     cudaGraphExec_t part[31] = {};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc[2] = {nullptr, nullptr};
-    std::vector<int> h_node_bc;   // host copies for next_solver rebuilds
     bool dw_coords_checked = false, dw_coords_ok = false;   // double-word range of the coordinates
     bool u_zero = true;   // u is still the all-zero state msx_create set (no step run, no state set)
 };
@@ -214,39 +214,50 @@ static msx_status make_material(const msx_material &m, MatParams &o)
 
 // Dirichlet tables: entries grouped by DOF in input order, one record per
 // constrained node with (first, count) per component.
-static msx_status build_bcs(long long nn, const msx_bc *bcs, long long nbc, double t0, double tf,
-                            std::vector<int> &node_bc, std::vector<int2> &rec, std::vector<BCEntry> &ent)
+msx_status msx::build_bc_tables(long long nn, const msx_bc *bcs, long long nbc, double t0, double tf, BCTables &t,
+                                std::string &err)
 {
-    if (nbc < 0 || (nbc > 0 && !bcs)) return fail(MSX_ERR_ARG, "bad boundary-condition array");
-    std::vector<long long> order(nbc);
-    std::iota(order.begin(), order.end(), 0);
-    for (long long k = 0; k < nbc; k++) {
-        if (bcs[k].dof < 0 || bcs[k].dof >= 3 * nn) return fail(MSX_ERR_ARG, "BC dof out of range");
-        if (bcs[k].mode < 0 || bcs[k].mode > 3) return fail(MSX_ERR_ARG, "unknown BC mode");
-        if (bcs[k].mode == MSX_BC_RAMP && !(tf - t0 != 0)) return fail(MSX_ERR_ARG, "ramp BC needs tf != t0");
+    t.nodes.clear();
+    t.rec.clear();
+    t.ent.clear();
+    if (nbc < 0 || (nbc > 0 && !bcs) || nbc >= (1LL << 31)) {
+        err = "bad boundary-condition array";
+        return MSX_ERR_ARG;
     }
-    std::stable_sort(order.begin(), order.end(), [&](long long x, long long y) { return bcs[x].dof < bcs[y].dof; });
-    node_bc.assign(nn, -1);
-    rec.clear();
-    ent.clear();
-    ent.reserve(nbc);
+    // key = (3 node + component) << 31 | input index (3 node + component <
+    // 3 * 2^31, so the key fits 64 bits): sorting the keys groups the entries
+    // by node and component and keeps each DOF's entries in input order
+    std::vector<unsigned long long> key(nbc);
     for (long long k = 0; k < nbc; k++) {
-        const msx_bc &b = bcs[order[k]];
+        const msx_bc &b = bcs[k];
+        if (b.dof < 0 || b.dof >= 3 * nn) err = "BC dof out of range";
+        else if (b.mode < 0 || b.mode > 3) err = "unknown BC mode";
+        else if (b.mode == MSX_BC_RAMP && !(tf - t0 != 0)) err = "ramp BC needs tf != t0";
+        if (!err.empty()) return MSX_ERR_ARG;
+        const unsigned long long node = (unsigned long long)(b.dof % nn), comp = (unsigned long long)(b.dof / nn);
+        key[k] = ((3 * node + comp) << 31) | (unsigned long long)k;
+    }
+    std::sort(key.begin(), key.end());
+    t.ent.reserve(nbc);
+    long long cur = -1;
+    for (long long j = 0; j < nbc; j++) {
+        const msx_bc &b = bcs[(long long)(key[j] & 0x7FFFFFFFULL)];
+        const unsigned long long nc = key[j] >> 31;
+        const long long node = (long long)(nc / 3);
+        if (node != cur) {
+            t.nodes.push_back(make_int2((int)node, (int)(t.rec.size() / 3)));
+            t.rec.resize(t.rec.size() + 3, make_int2(0, 0));
+            cur = node;
+        }
+        int2 &r = t.rec[t.rec.size() - 3 + (int)(nc % 3)];
+        if (r.y == 0) r.x = (int)t.ent.size();
+        r.y++;
         BCEntry e;
         e.mode = b.mode == MSX_BC_RAMP_RATE ? MSX_BC_RAMP : b.mode;
         e.ramp_steps = b.ramp_steps;
         // classNodes.cpp:58-74: a ramp stores U/duration, an instant BC stores U
         e.val = b.mode == MSX_BC_RAMP ? b.value / (tf - t0) : b.value;
-        long long node = b.dof % nn;
-        int comp = (int)(b.dof / nn);
-        if (node_bc[node] < 0) {
-            node_bc[node] = (int)(rec.size() / 3);
-            rec.resize(rec.size() + 3, make_int2(0, 0));
-        }
-        int2 &r = rec[node_bc[node] * 3 + comp];
-        if (r.y == 0) r.x = (int)ent.size();
-        r.y++;
-        ent.push_back(e);
+        t.ent.push_back(e);
     }
     return MSX_OK;
 }
@@ -405,25 +416,39 @@ static msx_status upload_tiled(msx_handle *h)
     return MSX_OK;
 }
 
-static msx_status upload_bcs(msx_handle *h, const msx_bc *bcs, long long nbc)
+// The Dirichlet tables on the device (enqueued on the handle's stream; the
+// host vectors may go once this returns).
+static msx_status upload_bc_tables(msx_handle *h, const BCTables &t)
 {
-    std::vector<int> node_bc;
-    std::vector<int2> rec;
-    std::vector<BCEntry> ent;
-    msx_status st = build_bcs(h->P.nn, bcs, nbc, h->t0, h->tf, node_bc, rec, ent);
-    if (st != MSX_OK) return st;
     h->bc_rec.release();
     h->bcs.release();
+    h->bc_nodes.release();
     if (!h->node_bc.p) MSX_CUDA(h->node_bc.alloc(h->P.nn));
-    MSX_CUDA(h->bc_rec.alloc(rec.size()));
-    MSX_CUDA(h->bcs.alloc(ent.size()));
-    MSX_CUDA(cudaMemcpyAsync(h->node_bc.p, node_bc.data(), sizeof(int) * node_bc.size(), cudaMemcpyHostToDevice, h->stream));
-    if (!rec.empty())
-        MSX_CUDA(cudaMemcpyAsync(h->bc_rec.p, rec.data(), sizeof(int2) * rec.size(), cudaMemcpyHostToDevice, h->stream));
-    if (!ent.empty())
-        MSX_CUDA(cudaMemcpyAsync(h->bcs.p, ent.data(), sizeof(BCEntry) * ent.size(), cudaMemcpyHostToDevice, h->stream));
+    MSX_CUDA(h->bc_rec.alloc(t.rec.size()));
+    MSX_CUDA(h->bcs.alloc(t.ent.size()));
+    MSX_CUDA(h->bc_nodes.alloc(t.nodes.size()));
+    if (!t.nodes.empty())
+        MSX_CUDA(cudaMemcpyAsync(h->bc_nodes.p, t.nodes.data(), sizeof(int2) * t.nodes.size(), cudaMemcpyHostToDevice,
+                                 h->stream));
+    launch_node_bc_scatter(h->node_bc.p, h->P.nn, h->bc_nodes.p, (long long)t.nodes.size(), h->stream);
+    if (!t.rec.empty())
+        MSX_CUDA(cudaMemcpyAsync(h->bc_rec.p, t.rec.data(), sizeof(int2) * t.rec.size(), cudaMemcpyHostToDevice,
+                                 h->stream));
+    if (!t.ent.empty())
+        MSX_CUDA(cudaMemcpyAsync(h->bcs.p, t.ent.data(), sizeof(BCEntry) * t.ent.size(), cudaMemcpyHostToDevice,
+                                 h->stream));
+    MSX_CUDA(cudaGetLastError());
+    return MSX_OK;
+}
+
+static msx_status upload_bcs(msx_handle *h, const msx_bc *bcs, long long nbc)
+{
+    BCTables t;
+    std::string err;
+    if (build_bc_tables(h->P.nn, bcs, nbc, h->t0, h->tf, t, err) != MSX_OK) return fail(MSX_ERR_ARG, err);
+    msx_status st = upload_bc_tables(h, t);
+    if (st != MSX_OK) return st;
     MSX_CUDA(cudaStreamSynchronize(h->stream));
-    h->h_node_bc.swap(node_bc);
     return MSX_OK;
 }
 
@@ -658,8 +683,10 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     };
     msx_status st;
     cudaGetDevice(&h->device);
-    cudaDeviceProp prop;
-    if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess || prop.major * 10 + prop.minor != 103) {
+    int cc_major = 0, cc_minor = 0;
+    if (cudaDeviceGetAttribute(&cc_major, cudaDevAttrComputeCapabilityMajor, h->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&cc_minor, cudaDevAttrComputeCapabilityMinor, h->device) != cudaSuccess ||
+        cc_major * 10 + cc_minor != 103) {
         delete h;
         return fail(MSX_ERR_NO_DEVICE, "the library is built for sm_103 (GB300) only");
     }
@@ -702,36 +729,45 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     // the first block's mode's own arrays, filled by the set-up kernels below
     if ((st = mode_buffers(h, h->precision, false)) != MSX_OK) return bail(st);
     cudaStream_t s = h->stream;
-    std::vector<unsigned char> mids;
-    if (h->mat.p) {
-        mids.resize(ne);
-        for (long long e = 0; e < ne; e++) mids[e] = (unsigned char)mesh->elem_material[e];
-    }
 #define UP(dst, src, bytes) \
     if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return bail(fail(MSX_ERR_CUDA, "upload failed"))
     UP(h->conn.p, mesh->conn, sizeof(int4) * ne);
     UP(h->X.p, mesh->X, sizeof(double) * 3 * nn);
-    {   // node -> (element, corner) lists in element order, built on the device;
-        // this also range-checks the connectivity before any kernel reads it
+    bind_problem(h);
+    h->P.mat = h->mat.p;
+    // The element set-up (FP64-bound, the longest set-up kernel) is queued
+    // first, and the host builds the Dirichlet tables while it runs.  The
+    // node-list build after it range-checks conn; the set-up kernel skips an
+    // element with an out-of-range node id, and msx_create then fails on the
+    // check (every exit waits for the stream: msx_destroy synchronises it).
+    launch_setup_elements(h->P, h->X.p, s);
+    BCTables bt;
+    {
+        std::string err;
+        if (build_bc_tables(nn, bcs, num_bcs, h->t0, h->tf, bt, err) != MSX_OK) return bail(fail(MSX_ERR_ARG, err));
+    }
+    std::vector<unsigned char> mids;
+    if (h->mat.p) {
+        mids.resize(ne);
+        for (long long e = 0; e < ne; e++) mids[e] = (unsigned char)mesh->elem_material[e];
+        UP(h->mat.p, mids.data(), ne);
+    }
+#undef UP
+    cudaMemsetAsync(h->u.p, 0, sizeof(double) * 3 * nn, s);
+    cudaMemsetAsync(h->v.p, 0, sizeof(double) * 3 * nn, s);
+    cudaMemsetAsync(h->a.p, 0, sizeof(double) * 3 * nn, s);
+    {   // node -> (element, corner) lists in element order, built on the device
         std::string err;
         if ((st = build_node_csr(h->conn.p, mesh->conn, ne, nn, h->node_ptr.p, h->node_inc.p, h->slot.p, s, err)) !=
             MSX_OK)
             return bail(fail(st, err.c_str()));
     }
-    if (h->mat.p) UP(h->mat.p, mids.data(), ne);
-#undef UP
-    cudaMemsetAsync(h->u.p, 0, sizeof(double) * 3 * nn, s);
-    cudaMemsetAsync(h->v.p, 0, sizeof(double) * 3 * nn, s);
-    cudaMemsetAsync(h->a.p, 0, sizeof(double) * 3 * nn, s);
-    bind_problem(h);
-    h->P.mat = h->mat.p;
-    launch_setup_elements(h->P, h->X.p, s);
     launch_setup_mass(h->P, h->mass.p, h->minv.p, s);
     if (h->minv2.p) launch_minv_split(h->minv.p, h->minv2.p, nn, s);
+    if ((st = upload_bc_tables(h, bt)) != MSX_OK) return bail(st);
     if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
         return bail(fail(MSX_ERR_CUDA, "set-up kernels failed"));
     if (h->precision == MSX_PREC_DOUBLE_WORD && (st = check_double_word(h)) != MSX_OK) return bail(st);
-    if ((st = upload_bcs(h, bcs, num_bcs)) != MSX_OK) return bail(st);
     bind_problem(h);
     *out = h;
     return MSX_OK;
@@ -751,6 +787,7 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     for (auto *b : {&h->node_ptr, &h->node_inc, &h->node_bc, &h->flags}) b->release();
     h->bc_rec.release();
     h->bcs.release();
+    h->bc_nodes.release();
     h->act.release();
     h->visc_f0.release();
     h->visc_h0.release();
