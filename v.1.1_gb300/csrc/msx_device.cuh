@@ -651,6 +651,7 @@ __device__ __forceinline__ void node_quad_fp64(const Problem &p, long long i, bo
         p.u[dof] = ui;
         p.v[dof] = vi;
         p.a[dof] = ai;
+        if (p.u4) p.u4[4LL * i + q] = ui;
     }
 }
 
@@ -1132,12 +1133,27 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
 #pragma unroll
     for (int k = 0; k < 9; k++) G[k] = __ldg(p.G + k * ne + e);
     double u0[3], du[9];
+    if (!FORCE_ONLY && p.u4) {
+        double ua[4][3];
 #pragma unroll
-    for (int i = 0; i < 3; i++) u0[i] = p.u[nd[0] + i * nn];
+        for (int a = 0; a < 4; a++) {
+            const double2 xy = __ldg(reinterpret_cast<const double2 *>(p.u4) + 2LL * nd[a]);
+            ua[a][0] = xy.x;
+            ua[a][1] = xy.y;
+            ua[a][2] = __ldg(p.u4 + 4LL * nd[a] + 2);
+        }
 #pragma unroll
-    for (int a = 1; a < 4; a++)
+        for (int a = 1; a < 4; a++)
 #pragma unroll
-        for (int i = 0; i < 3; i++) du[(a - 1) * 3 + i] = p.u[nd[a] + i * nn] - u0[i];
+            for (int i = 0; i < 3; i++) du[(a - 1) * 3 + i] = ua[a][i] - ua[0][i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < 3; i++) u0[i] = p.u[nd[0] + i * nn];
+#pragma unroll
+        for (int a = 1; a < 4; a++)
+#pragma unroll
+            for (int i = 0; i < 3; i++) du[(a - 1) * 3 + i] = p.u[nd[a] + i * nn] - u0[i];
+    }
     double F[9], P[9];
 #pragma unroll
     for (int i = 0; i < 3; i++)

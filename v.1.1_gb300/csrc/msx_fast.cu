@@ -78,6 +78,19 @@ __global__ void state_merge_kernel(Problem p)
     p.a[i] = (double)a.x + (double)a.y;
 }
 
+__global__ void u4_from_u_kernel(const double *u, double *u4, long long nn)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    reinterpret_cast<double2 *>(u4)[2 * i] = make_double2(u[i], u[nn + i]);
+    reinterpret_cast<double2 *>(u4)[2 * i + 1] = make_double2(u[2 * nn + i], 0.0);
+}
+
+void launch_u4_from_u(const double *u, double *u4, long long nn, cudaStream_t s)
+{
+    u4_from_u_kernel<<<grid_for(nn, 256), 256, 0, s>>>(u, u4, nn);
+}
+
 __global__ void minv_split_kernel(const double *minv, float2 *minv2, long long nn)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

@@ -94,6 +94,11 @@ struct Problem {
     // nodes (SoA, dof = node + c*nn)
     const double *X;
     double *u, *v, *a;
+    // plain FP64 mode: a node-major copy of u, one 32-byte record per node
+    // (x, y, z, zero pad), kept by the node kernel beside u; the element
+    // kernel gathers a node with two loads of one sector instead of three
+    // 8-byte loads from three rows.  Null in the other modes.
+    double *u4;
     const double *mass;       // lumped mass per node
     const double *minv;       // 1/mass per node
     // mixed mode: u, v, a as FP32 (hi, lo) pairs (value hi + lo) while a block
@@ -180,6 +185,8 @@ int tiled_ctas_per_sm(int mode, int threads, bool node = false);
 void launch_state_split(const Problem &p, cudaStream_t s);
 void launch_state_merge(const Problem &p, cudaStream_t s);
 void launch_minv_split(const double *minv, float2 *minv2, long long nn, cudaStream_t s);
+// u (SoA) -> the plain FP64 mode's node-major copy u4
+void launch_u4_from_u(const double *u, double *u4, long long nn, cudaStream_t s);
 
 // records the message returned by msx_last_error() on this host thread
 void msx_set_error(const char *msg);

@@ -165,6 +165,7 @@ static size_t footprint(long long nn, long long ne, long long nbc, int precision
     b += align256(sizeof(float2) * 3 * nn);                                          // uhl
     if (pair_state(precision))                                                       // vhl, ahl, minv2
         b += 2 * align256(sizeof(float2) * 3 * nn) + align256(sizeof(float2) * nn);
+    if (precision == MSX_PREC_FP64) b += align256(sizeof(double) * 4 * nn);          // u4 (node-major u)
     if (precision == MSX_PREC_DOUBLE_WORD)                                           // G32lo, wJ32lo
         b += align256(sizeof(float) * 9 * ne) + align256(sizeof(float) * ne);
     b += precision == MSX_PREC_MIXED ? align256(sizeof(float) * 16 * ne) : align256(sizeof(double) * 12 * ne);
@@ -641,6 +642,7 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
         P.mass = mass;
         P.minv = minv;
         P.uhl = (float2 *)carve(sizeof(float2) * 3 * nn);
+        if (prec == MSX_PREC_FP64) P.u4 = (double *)carve(sizeof(double) * 4 * nn);
         float2 *minv2 = nullptr;
         if (pair_state(prec)) {
             P.vhl = (float2 *)carve(sizeof(float2) * 3 * nn);
@@ -691,6 +693,7 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
         PCUDA(cudaMemsetAsync(P.v, 0, sizeof(double) * 3 * nn, s));
         PCUDA(cudaMemsetAsync(P.a, 0, sizeof(double) * 3 * nn, s));
         PCUDA(cudaMemsetAsync(P.uhl, 0, sizeof(float2) * 3 * nn, s));
+        if (P.u4) PCUDA(cudaMemsetAsync(P.u4, 0, sizeof(double) * 4 * nn, s));
         if (pair_state(prec)) {
             PCUDA(cudaMemsetAsync(P.vhl, 0, sizeof(float2) * 3 * nn, s));
             PCUDA(cudaMemsetAsync(P.ahl, 0, sizeof(float2) * 3 * nn, s));

@@ -100,6 +100,7 @@ struct msx_handle {
     DBuf<double> G, wJ, Lref, X, u, v, a, mass, minv, fe;
     DBuf<float> G32, wJ32, Lref32, Eref32, fe32, G32lo, wJ32lo;
     DBuf<float2> uhl, vhl, ahl, minv2;
+    DBuf<double> u4;   // plain FP64 mode: node-major copy of u (Problem::u4)
     DBuf<unsigned char> mat;
     DBuf<int> node_ptr, node_inc, node_bc;
     DBuf<int2> bc_nodes;   // (node, record) of the nodes with Dirichlet entries
@@ -297,6 +298,7 @@ static void bind_problem(msx_handle *h)
     P.mass = h->mass.p;
     P.minv = h->minv.p;
     P.uhl = h->uhl.p;
+    P.u4 = h->precision == MSX_PREC_FP64 ? h->u4.p : nullptr;
     P.vhl = h->vhl.p;
     P.ahl = h->ahl.p;
     P.minv2 = h->minv2.p;
@@ -493,6 +495,7 @@ static msx_status mode_buffers(msx_handle *h, int precision, bool fill)
         MSX_CUDA(h->fe32.alloc(16 * ne));
         MSX_CUDA(cudaMemsetAsync(h->fe32.p, 0, sizeof(float) * 16 * ne, h->stream));
     }
+    if (precision == MSX_PREC_FP64 && !h->u4.p) MSX_CUDA(h->u4.alloc(4 * nn));   // filled at each block start
     if (!mixed && !h->fe.p) {
         MSX_CUDA(h->fe.alloc(12 * ne));
         MSX_CUDA(cudaMemsetAsync(h->fe.p, 0, sizeof(double) * 12 * ne, h->stream));
@@ -582,6 +585,7 @@ static msx_status init_block(msx_handle *h)
     long long limit = h->max_steps > 0 ? h->max_steps : (1LL << 62);
     init_block_kernel<<<1, 1, 0, h->stream>>>(P, h->t0, limit);
     MSX_CUDA(cudaGetLastError());
+    if (P.u4) launch_u4_from_u(P.u, P.u4, P.nn, h->stream);   // the element gathers' copy of u
     if (pair_state(h)) {
         launch_state_split(P, h->stream);   // the running state of a mixed or double-word block
         MSX_CUDA(cudaGetLastError());
@@ -783,6 +787,7 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     for (auto *b : {&h->G, &h->wJ, &h->Lref, &h->X, &h->u, &h->v, &h->a, &h->mass, &h->minv, &h->fe}) b->release();
     for (auto *b : {&h->G32, &h->wJ32, &h->Lref32, &h->Eref32, &h->fe32, &h->G32lo, &h->wJ32lo}) b->release();
     for (auto *b : {&h->uhl, &h->vhl, &h->ahl, &h->minv2}) b->release();
+    h->u4.release();
     h->mat.release();
     for (auto *b : {&h->node_ptr, &h->node_inc, &h->node_bc, &h->flags}) b->release();
     h->bc_rec.release();
