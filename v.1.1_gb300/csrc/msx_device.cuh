@@ -763,7 +763,8 @@ __global__ void __launch_bounds__(kNodeBlock) node_kernel(Problem p, int parity)
 
 // Reference operation order (used with contraction off).
 __device__ __forceinline__ float f32_trunc(double x);
-__device__ __forceinline__ float cfl_screen(const Problem &p, long long e, const float *du, const MatParams &m);
+__device__ __forceinline__ float cfl_screen(const Problem &p, long long e, const float *g, const float *du,
+                                            const MatParams &m);
 
 // Exact CFL value of one element, min(L_ref, L(X+u)) / c, in the reference's
 // order (solvers.cpp:304-317: deformed inscribed sphere).
@@ -880,7 +881,10 @@ __device__ __forceinline__ double elem_body_exact(const Problem &p, long long e,
             for (int a = 1; a < 4; a++)
 #pragma unroll
                 for (int i = 0; i < 3; i++) du32[(a - 1) * 3 + i] = f32_trunc(ue[a * 3 + i] - ue[i]);
-            vmin = (double)cfl_screen(p, e, du32, m);
+            float g32[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) g32[k] = f32_trunc(dphi[3 + k]);
+            vmin = (double)cfl_screen(p, e, g32, du32, m);
             if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
         } else if (!FORCE_ONLY) {
             // solvers.cpp:304-317: deformed inscribed sphere
@@ -1091,29 +1095,45 @@ __device__ __forceinline__ float f32_trunc(double x)
     return __uint_as_float(r);
 }
 
-// FP32 estimate of an element's CFL value from the FP32 reference edges plus
-// the displacement differences.  Its relative error stays below ~3e-4 unless
-// the tet is a sliver (6V < 4e-3 |e1||e2||e3|); slivers are returned negated
-// so that the caller always recomputes them in FP64.
-__device__ __forceinline__ float cfl_screen(const Problem &p, long long e, const float *du, const MatParams &m)
+// FP32 estimate of an element's CFL value: the reference edges X_b - X_0 are
+// the columns of G^-1 (g: the rows of G, the gradients of shape functions
+// 1-3, in FP32), cof(G)^T / det G, plus the displacement differences du.  Its
+// relative error stays below ~3e-4 unless the tet is a sliver (6V below
+// 0.063 |e1||e2||e3|, where the FP32 inverse loses accuracy) or a reference
+// sliver (a negative Lref32, set at set-up); those are returned as -1 so that
+// the caller always recomputes them in FP64.  The same screen as the mixed
+// kernel's, with no streamed edge data.
+__device__ __forceinline__ float cfl_screen(const Problem &p, long long e, const float *g, const float *du,
+                                            const MatParams &m)
 {
-    const long long ne = p.ne;
+    float C[9];
+    C[0] = g[4] * g[8] - g[5] * g[7];
+    C[1] = g[5] * g[6] - g[3] * g[8];
+    C[2] = g[3] * g[7] - g[4] * g[6];
+    C[3] = g[2] * g[7] - g[1] * g[8];
+    C[4] = g[0] * g[8] - g[2] * g[6];
+    C[5] = g[1] * g[6] - g[0] * g[7];
+    C[6] = g[1] * g[5] - g[2] * g[4];
+    C[7] = g[2] * g[3] - g[0] * g[5];
+    C[8] = g[0] * g[4] - g[1] * g[3];
+    const float idet = 1.0f / (g[0] * C[0] + g[1] * C[1] + g[2] * C[2]);
     float e1[3], e2[3], e3[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        e1[i] = __ldg(p.Eref32 + i * ne + e) + du[i];
-        e2[i] = __ldg(p.Eref32 + (3 + i) * ne + e) + du[3 + i];
-        e3[i] = __ldg(p.Eref32 + (6 + i) * ne + e) + du[6 + i];
+        e1[i] = C[i] * idet + du[i];
+        e2[i] = C[3 + i] * idet + du[3 + i];
+        e3[i] = C[6 + i] * idet + du[6 + i];
     }
-    float C0 = e2[1] * e3[2] - e2[2] * e3[1], C1 = e2[2] * e3[0] - e2[0] * e3[2], C2 = e2[0] * e3[1] - e2[1] * e3[0];
-    float v6 = fabsf(e1[0] * C0 + e1[1] * C1 + e1[2] * C2);
-    float l1 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
-    float l2 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
-    float l3 = e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2];
-    float dist = char_length_edges<float>(e1, e2, e3);
-    float Lr = __ldg(p.Lref32 + e);
-    float dt = ((dist < Lr) ? dist : Lr) * m.inv_c_f;
-    bool sliver = !(v6 * v6 >= 1.6e-5f * l1 * l2 * l3) || !(dt > 0.0f);
+    const float C0 = e2[1] * e3[2] - e2[2] * e3[1], C1 = e2[2] * e3[0] - e2[0] * e3[2],
+                C2 = e2[0] * e3[1] - e2[1] * e3[0];
+    const float v6 = fabsf(e1[0] * C0 + e1[1] * C1 + e1[2] * C2);
+    const float l1 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+    const float l2 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+    const float l3 = e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2];
+    const float dist = char_length_edges<float>(e1, e2, e3);
+    const float Lr = __ldg(p.Lref32 + e);
+    const float dt = ((dist < Lr) ? dist : Lr) * m.inv_c_f;
+    const bool sliver = !(v6 * v6 >= 4e-3f * l1 * l2 * l3) || !(dt > 0.0f);
     return sliver ? -1.0f : dt;
 }
 
@@ -1192,10 +1212,13 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
     }
     if (FORCE_ONLY) return 0.0f;
     if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
-    float du32[9];
+    float du32[9], g32[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) du32[k] = f32_trunc(du[k]);
-    return cfl_screen(p, e, du32, m);
+    for (int k = 0; k < 9; k++) {
+        du32[k] = f32_trunc(du[k]);
+        g32[k] = f32_trunc(G[k]);
+    }
+    return cfl_screen(p, e, g32, du32, m);
 }
 
 // corner forces only (internal-force hook)
@@ -1716,10 +1739,13 @@ __device__ __forceinline__ float elem_body_dw(const Problem &p, long long e, int
     }
     if (FORCE_ONLY) return 0.0f;
     if (e == 0 && !isfinite(p.uhl[1].x)) atomicOr(p.flags + (parity ^ 1), 1);
-    float du32[9];
+    float du32[9], g32[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) du32[k] = du[k].x;
-    return cfl_screen(p, e, du32, m);
+    for (int k = 0; k < 9; k++) {
+        du32[k] = du[k].x;
+        g32[k] = G[k].x;
+    }
+    return cfl_screen(p, e, g32, du32, m);
 }
 
 // corner forces only (internal-force hook)
@@ -2142,7 +2168,7 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
 // classLinearTetrahedra.cpp:171-268 (Jacobian, inverse, dphi), classGPs.cpp:27
 // (wJ = 0.166666666667 |J|), classLinearTetrahedra.cpp:129-140 (charLength).
 __global__ void setup_elements_kernel(Problem p, const double *X, double *G, double *wJ, double *Lref,
-                                      float *G32, float *wJ32, float *Lref32, float *Eref32)
+                                      float *G32, float *wJ32, float *Lref32)
 {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= p.ne) return;
@@ -2208,22 +2234,16 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
         const bool sliver = !(v6 * v6 >= 4e-3 * l1 * l2 * l3);
         Lref32[e] = sliver ? -(float)L : (float)L;
     }
-#pragma unroll
-    for (int a = 1; a < 4; a++)
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-            if (Eref32) Eref32[((a - 1) * 3 + i) * ne + e] = (float)(pts[a * 3 + i] - pts[i]);
 }
 
 // The FP32 element arrays of a precision mode that a handle starts using after
 // its set-up (a later solver block in another mode), from the FP64 set-up data
 // and X: the same conversions setup_elements_kernel makes, so the same bits.
-__global__ void mode_arrays_kernel(Problem p, const double *X, float *G32, float *wJ32, float *G32lo, float *wJ32lo,
-                                   float *Eref32)
+__global__ void mode_arrays_kernel(Problem p, float *G32, float *wJ32, float *G32lo, float *wJ32lo)
 {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= p.ne) return;
-    const long long ne = p.ne, nn = p.nn;
+    const long long ne = p.ne;
 #pragma unroll
     for (int k = 0; k < 9; k++) {
         const double g = p.G[k * ne + e];
@@ -2233,14 +2253,6 @@ __global__ void mode_arrays_kernel(Problem p, const double *X, float *G32, float
     const double w = p.wJ[e];
     if (wJ32) wJ32[e] = (float)w;
     if (wJ32lo) wJ32lo[e] = (float)(w - (double)(float)w);
-    if (Eref32) {
-        const int4 cn = p.conn[e];
-        const int nd[4] = {cn.x, cn.y, cn.z, cn.w};
-#pragma unroll
-        for (int a = 1; a < 4; a++)
-#pragma unroll
-            for (int i = 0; i < 3; i++) Eref32[((a - 1) * 3 + i) * ne + e] = (float)(X[i * nn + nd[a]] - X[i * nn + nd[0]]);
-    }
 }
 
 // Previous-step F diagonal for the bulk viscosity, from displacement u, in the

@@ -25,14 +25,12 @@ void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s)
 {
     setup_elements_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(
         p, X, const_cast<double *>(p.G), const_cast<double *>(p.wJ), const_cast<double *>(p.Lref),
-        const_cast<float *>(p.G32), const_cast<float *>(p.wJ32), const_cast<float *>(p.Lref32),
-        const_cast<float *>(p.Eref32));
+        const_cast<float *>(p.G32), const_cast<float *>(p.wJ32), const_cast<float *>(p.Lref32));
 }
 
-void launch_mode_arrays(const Problem &p, const double *X, float *G32, float *wJ32, float *G32lo, float *wJ32lo,
-                        float *Eref32, cudaStream_t s)
+void launch_mode_arrays(const Problem &p, float *G32, float *wJ32, float *G32lo, float *wJ32lo, cudaStream_t s)
 {
-    mode_arrays_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, X, G32, wJ32, G32lo, wJ32lo, Eref32);
+    mode_arrays_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, G32, wJ32, G32lo, wJ32lo);
 }
 
 void launch_visc_init(const Problem &p, const double *u, cudaStream_t s)

@@ -85,7 +85,6 @@ struct Problem {
     const double *wJ;
     const double *Lref;
     const float *G32, *wJ32, *Lref32;       // FP32 copies (mixed mode)
-    const float *Eref32;      // 9*ne reference edge vectors X_a - X_0 (FP32 CFL screen of the FP64 mode)
     const float *G32lo, *wJ32lo;  // low words: G32 + G32lo and wJ32 + wJ32lo as double-words (double-word mode)
     const unsigned char *mat; // per-element material id, or nullptr
     const double *act_t;      // per-element activation time under *ACTIVATION, or nullptr
@@ -199,8 +198,7 @@ void launch_elem_exact(const Problem &p, int parity, cudaStream_t s);
 void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s);
 void launch_setup_mass(const Problem &p, double *mass, double *minv, cudaStream_t s);
 // a precision mode's FP32 element arrays (any pointer may be null) from G, wJ and X
-void launch_mode_arrays(const Problem &p, const double *X, float *G32, float *wJ32, float *G32lo, float *wJ32lo,
-                        float *Eref32, cudaStream_t s);
+void launch_mode_arrays(const Problem &p, float *G32, float *wJ32, float *G32lo, float *wJ32lo, cudaStream_t s);
 // bulk viscosity: the elements' previous-step F diagonal from displacement u
 void launch_visc_init(const Problem &p, const double *u, cudaStream_t s);
 // min over elements of Lref/c (undeformed) or min(Lref, L(X+u))/c, into dtmin[slot]

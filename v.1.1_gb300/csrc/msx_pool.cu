@@ -160,7 +160,7 @@ static size_t footprint(long long nn, long long ne, long long nbc, int precision
     size_t b = 0;
     b += align256(sizeof(int4) * ne) + align256(sizeof(double) * 9 * ne);           // conn, G
     b += 2 * align256(sizeof(double) * ne);                                         // wJ, Lref
-    b += 2 * align256(sizeof(float) * 9 * ne) + 2 * align256(sizeof(float) * ne);    // G32, Eref32, wJ32, Lref32
+    b += align256(sizeof(float) * 9 * ne) + 2 * align256(sizeof(float) * ne);        // G32, wJ32, Lref32
     b += 4 * align256(sizeof(double) * 3 * nn) + 2 * align256(sizeof(double) * nn);  // X, u, v, a, mass, minv
     b += align256(sizeof(float2) * 3 * nn);                                          // uhl
     if (pair_state(precision))                                                       // vhl, ahl, minv2
@@ -626,7 +626,6 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
         P.wJ = (double *)carve(sizeof(double) * ne);
         P.Lref = (double *)carve(sizeof(double) * ne);
         P.G32 = (float *)carve(sizeof(float) * 9 * ne);
-        P.Eref32 = (float *)carve(sizeof(float) * 9 * ne);
         P.wJ32 = (float *)carve(sizeof(float) * ne);
         P.Lref32 = (float *)carve(sizeof(float) * ne);
         if (prec == MSX_PREC_DOUBLE_WORD) {

@@ -98,7 +98,7 @@ struct msx_handle {
     // owned device storage
     DBuf<int4> conn, slot;
     DBuf<double> G, wJ, Lref, X, u, v, a, mass, minv, fe;
-    DBuf<float> G32, wJ32, Lref32, Eref32, fe32, G32lo, wJ32lo;
+    DBuf<float> G32, wJ32, Lref32, fe32, G32lo, wJ32lo;
     DBuf<float2> uhl, vhl, ahl, minv2;
     DBuf<double> u4;   // plain FP64 mode: node-major copy of u (Problem::u4)
     DBuf<unsigned char> mat;
@@ -288,7 +288,6 @@ static void bind_problem(msx_handle *h)
     P.G32 = h->G32.p;
     P.wJ32 = h->wJ32.p;
     P.Lref32 = h->Lref32.p;
-    P.Eref32 = h->Eref32.p;
     P.G32lo = h->G32lo.p;
     P.wJ32lo = h->wJ32lo.p;
     P.X = h->X.p;
@@ -455,18 +454,18 @@ static msx_status upload_bcs(msx_handle *h, const msx_bc *bcs, long long nbc)
 }
 
 // The arrays only some precision modes read, allocated the first time a block
-// runs in such a mode (an FP64 handle of the 6M-tet cube saves ~0.95 GB and its
+// runs in such a mode (an FP64 handle of the 6M-tet cube saves ~0.5 GB and its
 // allocation time): FP32 G and wJ (mixed, double-word), their low words
-// (double-word), the FP32 reference edges of the CFL screen (every mode but
-// mixed), the (hi, lo) nodal state and 1/m (mixed, double-word), and the corner
-// forces as FP64 (or double-word) or FP32 slots.  With `fill`, derived arrays
+// (double-word), the (hi, lo) nodal state and 1/m (mixed, double-word), the
+// node-major copy of u (plain FP64), and the corner forces as FP64 (or
+// double-word) or FP32 slots.  With `fill`, derived arrays
 // are converted from the FP64 set-up data (a later block in a new mode); at
 // msx_create the set-up kernels fill them.
 static msx_status mode_buffers(msx_handle *h, int precision, bool fill)
 {
     const long long ne = h->P.ne, nn = h->P.nn;
     const bool mixed = precision == MSX_PREC_MIXED, dw = precision == MSX_PREC_DOUBLE_WORD;
-    float *G32 = nullptr, *wJ32 = nullptr, *G32lo = nullptr, *wJ32lo = nullptr, *Eref32 = nullptr;
+    float *G32 = nullptr, *wJ32 = nullptr, *G32lo = nullptr, *wJ32lo = nullptr;
     bool minv2 = false;
     if ((mixed || dw) && !h->G32.p) {
         MSX_CUDA(h->G32.alloc(9 * ne));
@@ -479,10 +478,6 @@ static msx_status mode_buffers(msx_handle *h, int precision, bool fill)
         MSX_CUDA(h->wJ32lo.alloc(ne));
         G32lo = h->G32lo.p;
         wJ32lo = h->wJ32lo.p;
-    }
-    if (!mixed && !h->Eref32.p) {
-        MSX_CUDA(h->Eref32.alloc(9 * ne));
-        Eref32 = h->Eref32.p;
     }
     if ((mixed || dw) && !h->uhl.p) {
         MSX_CUDA(h->uhl.alloc(3 * nn));
@@ -502,7 +497,7 @@ static msx_status mode_buffers(msx_handle *h, int precision, bool fill)
     }
     bind_problem(h);
     if (fill) {
-        if (G32 || G32lo || Eref32) launch_mode_arrays(h->P, h->X.p, G32, wJ32, G32lo, wJ32lo, Eref32, h->stream);
+        if (G32 || G32lo) launch_mode_arrays(h->P, G32, wJ32, G32lo, wJ32lo, h->stream);
         if (minv2) launch_minv_split(h->minv.p, h->minv2.p, nn, h->stream);
         MSX_CUDA(cudaGetLastError());
         MSX_CUDA(cudaStreamSynchronize(h->stream));
@@ -785,7 +780,7 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     DBuf<int4> *b4[] = {&h->conn, &h->slot};
     for (auto *b : b4) b->release();
     for (auto *b : {&h->G, &h->wJ, &h->Lref, &h->X, &h->u, &h->v, &h->a, &h->mass, &h->minv, &h->fe}) b->release();
-    for (auto *b : {&h->G32, &h->wJ32, &h->Lref32, &h->Eref32, &h->fe32, &h->G32lo, &h->wJ32lo}) b->release();
+    for (auto *b : {&h->G32, &h->wJ32, &h->Lref32, &h->fe32, &h->G32lo, &h->wJ32lo}) b->release();
     for (auto *b : {&h->uhl, &h->vhl, &h->ahl, &h->minv2}) b->release();
     h->u4.release();
     h->mat.release();
