@@ -1981,15 +1981,33 @@ __device__ __forceinline__ float tile_elements(const Problem &p, const Tile &tl,
     return v32;
 }
 
-constexpr int kMixedPending = 256;  // deferred FP64 rechecks a mixed CTA can hold
+constexpr int kMixedPending = 2 * kStepThreads;  // deferred FP64 rechecks a mixed CTA can hold
 
-// FP64 CFL values (cfl_dw) of one thread's elements of a mixed tile, their
-// minimum into the solve's CFL slot (a full pending list).
-__device__ __forceinline__ void mixed_recheck(const Problem &p, const Tile &tl, int lane, int parity)
+// The pending entries of a mixed CTA (all posted before the caller's last
+// barrier): one warp per entry, its lanes over the posting thread's elements
+// of that tile (one each when the tile has at most 32 per thread), skipping
+// entries above 2^-8 of the solve's running screen minimum.
+static __device__ __noinline__ void mixed_flush(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
+                                          const int2 *pend, const float *pendv, int np, int parity)
 {
-    double v = INFINITY;
-    for (long long e = tl.begin + lane; e < tl.end; e += blockDim.x) v = fmin(v, cfl_dw(p, e));
-    if (v >= 0.0 && v < INFINITY) atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
+    const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+    for (int j = threadIdx.x >> 5; j < np; j += nwarp) {
+        const int2 pe = pend[j];
+        const Tile tl = tiles[pe.x];
+        const Problem &p = descs[tl.solve];
+        const float mine = pendv[j];
+        if (!(mine < 0.0f)) {
+            const unsigned long long g = __ldcg(p.dtmin + 2 + (parity ^ 1));
+            if (g < kScreenInfBits && mine > __uint_as_float((unsigned)g) * (1.0f + 1.0f / 256.0f)) continue;
+        }
+        double v = INFINITY;
+        for (long long e = tl.begin + pe.y + (long long)lane * blockDim.x; e < tl.end; e += 32LL * blockDim.x)
+            v = fmin(v, cfl_dw(p, e));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0 && v >= 0.0 && v < INFINITY)
+            atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
+    }
 }
 
 // The mixed kernel's tile loop.  Each tile's FP32 screen minimum (over the
@@ -2004,8 +2022,10 @@ __device__ __forceinline__ void mixed_recheck(const Problem &p, const Tile &tl, 
 // d(x) <= m (1 + 2^-8) <= (tile minimum) (1 + 2^-8) (the tile minimum, taken
 // over part of the elements, is >= m), so its thread posted unless it met a
 // sliver, and then it posted anyway; the entry's minimum is <= d(x) <=
-// (running minimum) (1 + 2^-8), so it is rechecked.  A full list rechecks at
-// once.
+// (running minimum) (1 + 2^-8), so it is rechecked.  A tile adds at most one
+// entry per thread, so the list is flushed at a tile boundary once it holds
+// more than kMixedPending - blockDim entries, and never overflows; the element
+// loop itself calls no FP64 code.
 template <bool ACT, bool VISC>
 __device__ __forceinline__ void mixed_tile_loop(const Problem *__restrict__ descs, const Tile *__restrict__ tiles,
                                                 TileQueue &q, int parity)
@@ -2031,42 +2051,23 @@ __device__ __forceinline__ void mixed_tile_loop(const Problem *__restrict__ desc
             if (threadIdx.x == 0 && bmin < INFINITY)
                 atomicMin(p.dtmin + 2 + (parity ^ 1), (unsigned long long)__float_as_uint(bmin));
             if (neg || (mine < INFINITY && mine <= bmin * (1.0f + 1.0f / 256.0f))) {
-                const int k = atomicAdd(&s_npend, 1);
-                if (k < kMixedPending) {
-                    s_pend[k] = make_int2(t, (int)threadIdx.x);
-                    s_pendv[k] = neg ? -1.0f : mine;
-                } else {
-                    mixed_recheck(p, tl, threadIdx.x, parity);
-                }
+                const int k = atomicAdd(&s_npend, 1);   // < kMixedPending: flushed below in time
+                s_pend[k] = make_int2(t, (int)threadIdx.x);
+                s_pendv[k] = neg ? -1.0f : mine;
             }
         }
         __syncthreads();
         if (threadIdx.x == 0) s_tile = next;
         __syncthreads();
+        if (s_npend > kMixedPending - (int)blockDim.x) {   // the same value in every thread
+            mixed_flush(descs, tiles, s_pend, s_pendv, s_npend, parity);
+            __syncthreads();
+            if (threadIdx.x == 0) s_npend = 0;
+            __syncthreads();
+        }
         t = s_tile;
     }
-    // every entry was posted before the loop's last barrier.  One warp per
-    // entry, its lanes over the posting thread's elements of that tile (one
-    // each when the tile has at most 32 per thread, as kMaxTileElems / 128 does)
-    const int np = min(s_npend, kMixedPending);
-    const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-    for (int j = threadIdx.x >> 5; j < np; j += nwarp) {
-        const int2 pe = s_pend[j];
-        const Tile tl = tiles[pe.x];
-        const Problem &p = descs[tl.solve];
-        const float mine = s_pendv[j];
-        if (!(mine < 0.0f)) {
-            const unsigned long long g = __ldcg(p.dtmin + 2 + (parity ^ 1));
-            if (g < kScreenInfBits && mine > __uint_as_float((unsigned)g) * (1.0f + 1.0f / 256.0f)) continue;
-        }
-        double v = INFINITY;
-        for (long long e = tl.begin + pe.y + (long long)lane * blockDim.x; e < tl.end; e += 32LL * blockDim.x)
-            v = fmin(v, cfl_dw(p, e));
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if (lane == 0 && v >= 0.0 && v < INFINITY)
-            atomicMin(p.dtmin + (parity ^ 1), (unsigned long long)__double_as_longlong(v));
-    }
+    mixed_flush(descs, tiles, s_pend, s_pendv, s_npend, parity);   // posted before the loop's last barrier
 }
 
 // Element kernel over tiles.  Each element's FP32 CFL screen value is
