@@ -10,6 +10,7 @@
 // are bit for bit those of the sequential construction on the host.  A node
 // with more than kCsrMaxDegree incidences is left to the host (the per-node
 // insertion sort is quadratic in the degree).
+#include <climits>
 #include <algorithm>
 #include <string>
 #include <vector>
@@ -136,14 +137,39 @@ __global__ void csr_fill_kernel(const int *conn, long long n4, const int *node_p
     }
 }
 
-// Each node's list in increasing incidence order (insertion sort: the lists
-// are short, at most kCsrMaxDegree long).
+// Each node's list in increasing incidence order.  Lists of at most 32 (a
+// tet mesh's usual degree is about 24) are sorted in registers by a bitonic
+// network, padded with INT_MAX; longer ones (at most kCsrMaxDegree) by
+// insertion sort in place.
 __global__ void csr_sort_kernel(const int *node_ptr, long long nn, int *inc)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
     int *l = inc + node_ptr[i];
     const int d = node_ptr[i + 1] - node_ptr[i];
+    if (d <= 32) {
+        int v[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) v[j] = j < d ? l[j] : INT_MAX;
+#pragma unroll
+        for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+            for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+                for (int a = 0; a < 32; a++) {
+                    const int b = a ^ j;
+                    if (b > a) {
+                        const int lo = min(v[a], v[b]), hi = max(v[a], v[b]);
+                        const bool up = (a & k) == 0;
+                        v[a] = up ? lo : hi;
+                        v[b] = up ? hi : lo;
+                    }
+                }
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+            if (j < d) l[j] = v[j];
+        return;
+    }
     for (int x = 1; x < d; x++) {
         const int key = l[x];
         int y = x - 1;
