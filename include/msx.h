@@ -51,9 +51,10 @@ enum { MSX_BC_RAMP = 0,      /* *BOUNDARY, TYPE=DISPLACEMENT RAMP: value reached
 enum { MSX_PREC_FP64 = 0,        /* plain FP64, FMA-contracted, algebraically simplified laws */
        MSX_PREC_FP64_EXACT = 1,  /* FP64 in the reference's operation order, no contraction   */
        MSX_PREC_MIXED = 2,       /* FP32 element kinematics, stress, B^T P, J-1 and ln J (trace
-                                    summed exactly); nodal u, v, a as double-word FP32 pairs
-                                    (~48 bits); the stable dt is the FP64 CFL minimum (FP32
-                                    screen, FP64 recheck of the near-minimum elements)         */
+                                    summed exactly); nodal u, v as double-word FP32 pairs
+                                    (~48 bits), a in FP32; the stable dt is the FP64 CFL
+                                    minimum (FP32 screen, FP64 recheck of the near-minimum
+                                    elements)                                                  */
        MSX_PREC_DOUBLE_WORD = 3  /* MSX_PREC_FP64's algebra in double-word (FP32 pair, ~48-bit)
                                     arithmetic on the FP32 pipe, state and corner forces too;
                                     FP64 CFL check.  Values must stay inside FP32's exponent

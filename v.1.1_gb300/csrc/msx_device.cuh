@@ -655,6 +655,11 @@ __device__ __forceinline__ void node_quad_fp64(const Problem &p, long long i, bo
     }
 }
 
+// The mixed mode's acceleration, one FP32 per DOF in the storage of ahl: a is
+// recomputed every step from the FP32 corner forces (compensated sum / m), so
+// FP32 holds all it carries; u and v, the accumulated state, stay double-words.
+__device__ __forceinline__ float *mixed_a32(const Problem &p) { return reinterpret_cast<float *>(p.ahl); }
+
 __device__ __forceinline__ void node_quad_mixed(const Problem &p, long long i, bool valid, const NodeStep &ns)
 {
     const int q = threadIdx.x & 3;
@@ -666,7 +671,7 @@ __device__ __forceinline__ void node_quad_mixed(const Problem &p, long long i, b
     if (own) {
         uq = p.uhl[dof];
         vq = p.vhl[dof];
-        aq = p.ahl[dof];
+        aq = make_float2(mixed_a32(p)[dof], 0.f);
         minv = p.minv2[i];
         rec = p.node_bc[i];
     }
@@ -714,7 +719,7 @@ __device__ __forceinline__ void node_quad_mixed(const Problem &p, long long i, b
         const float2 f = ns.loads ? df_add(df_from(node_fext(p, i, q, ns)), df_neg(s)) : df_neg(s);
         const float2 an = df_mul(f, minv);
         vq = df_add(vq, df_mul(ns.hdt2, df_add(aq, an)));
-        aq = an;
+        aq = make_float2(__fadd_rn(an.x, an.y), 0.f);   // as stored: the prediction uses what a later call reads
         changed = true;
     }
     if (ns.run) {
@@ -733,7 +738,7 @@ __device__ __forceinline__ void node_quad_mixed(const Problem &p, long long i, b
     if (changed) {
         p.uhl[dof] = uq;
         p.vhl[dof] = vq;
-        p.ahl[dof] = aq;
+        mixed_a32(p)[dof] = aq.x;
     }
 }
 

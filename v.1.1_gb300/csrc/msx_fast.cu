@@ -59,23 +59,30 @@ void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, in
         launch_elem_variant<MODE_FP64>(descs, etiles, counts, parity, grid, threads, 0, s, act, visc);
 }
 
-__global__ void state_split_kernel(Problem p)
+// a32: the mixed mode, whose acceleration is one FP32 per DOF (mixed_a32)
+__global__ void state_split_kernel(Problem p, bool a32)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 3 * p.nn) return;
     p.uhl[i] = df_from(p.u[i]);
     p.vhl[i] = df_from(p.v[i]);
-    p.ahl[i] = df_from(p.a[i]);
+    if (a32) mixed_a32(p)[i] = (float)p.a[i];
+    else p.ahl[i] = df_from(p.a[i]);
 }
 
-__global__ void state_merge_kernel(Problem p)
+__global__ void state_merge_kernel(Problem p, bool a32)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 3 * p.nn) return;
-    float2 u = p.uhl[i], v = p.vhl[i], a = p.ahl[i];
+    float2 u = p.uhl[i], v = p.vhl[i];
     p.u[i] = (double)u.x + (double)u.y;
     p.v[i] = (double)v.x + (double)v.y;
-    p.a[i] = (double)a.x + (double)a.y;
+    if (a32) {
+        p.a[i] = (double)mixed_a32(p)[i];
+    } else {
+        const float2 a = p.ahl[i];
+        p.a[i] = (double)a.x + (double)a.y;
+    }
 }
 
 __global__ void u4_from_u_kernel(const double *u, double *u4, long long nn)
@@ -97,14 +104,14 @@ __global__ void minv_split_kernel(const double *minv, float2 *minv2, long long n
     if (i < nn) minv2[i] = df_from(minv[i]);
 }
 
-void launch_state_split(const Problem &p, cudaStream_t s)
+void launch_state_split(const Problem &p, bool mixed, cudaStream_t s)
 {
-    state_split_kernel<<<grid_for(3 * p.nn, 256), 256, 0, s>>>(p);
+    state_split_kernel<<<grid_for(3 * p.nn, 256), 256, 0, s>>>(p, mixed);
 }
 
-void launch_state_merge(const Problem &p, cudaStream_t s)
+void launch_state_merge(const Problem &p, bool mixed, cudaStream_t s)
 {
-    state_merge_kernel<<<grid_for(3 * p.nn, 256), 256, 0, s>>>(p);
+    state_merge_kernel<<<grid_for(3 * p.nn, 256), 256, 0, s>>>(p, mixed);
 }
 
 void launch_minv_split(const double *minv, float2 *minv2, long long nn, cudaStream_t s)

@@ -102,7 +102,7 @@ struct Problem {
     const double *minv;       // 1/mass per node
     // mixed mode: u, v, a as FP32 (hi, lo) pairs (value hi + lo) while a block
     // runs; u, v, a above hold the state between calls (state_merge)
-    float2 *uhl, *vhl, *ahl;  // 3*nn each
+    float2 *uhl, *vhl, *ahl;  // 3*nn each (the mixed mode keeps a as one FP32 per DOF: mixed_a32)
     const float2 *minv2;      // 1/mass as an (hi, lo) pair
     // corner forces.  Reference-order mode: fe[(e*4 + a)*3 + i] (element
     // order).  FP64 and mixed modes: in the node's CSR slot k = slot[e].a,
@@ -181,8 +181,8 @@ void launch_tiled_elem(const Problem *descs, const Tile *etiles, int *counts, in
 int tiled_ctas_per_sm(int mode, int threads, bool node = false);
 // Mixed-mode state conversions: u, v, a (FP64) -> uhl, vhl, ahl, and back
 // (hi + lo, exact unless the pair spans more than 53 bits); minv -> minv2.
-void launch_state_split(const Problem &p, cudaStream_t s);
-void launch_state_merge(const Problem &p, cudaStream_t s);
+void launch_state_split(const Problem &p, bool mixed, cudaStream_t s);
+void launch_state_merge(const Problem &p, bool mixed, cudaStream_t s);
 void launch_minv_split(const double *minv, float2 *minv2, long long nn, cudaStream_t s);
 // u (SoA) -> the plain FP64 mode's node-major copy u4
 void launch_u4_from_u(const double *u, double *u4, long long nn, cudaStream_t s);

@@ -272,7 +272,7 @@ static msx_status collect(msx_pool *p)
         f.res.t = c.t;
         // no copy here: the result stays in the solve's arena until it is
         // fetched, so the next replay is not held up by device-to-host copies
-        if (pair_state(p->opts.precision)) launch_state_merge(sl.P, p->stream);
+        if (pair_state(p->opts.precision)) launch_state_merge(sl.P, p->opts.precision == MSX_PREC_MIXED, p->stream);
         PCUDA(cudaEventCreateWithFlags(&f.ready, cudaEventDisableTiming));
         PCUDA(cudaEventRecord(f.ready, p->stream));
         f.arena = sl.arena;

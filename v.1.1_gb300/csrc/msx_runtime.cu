@@ -582,7 +582,7 @@ static msx_status init_block(msx_handle *h)
     MSX_CUDA(cudaGetLastError());
     if (P.u4) launch_u4_from_u(P.u, P.u4, P.nn, h->stream);   // the element gathers' copy of u
     if (pair_state(h)) {
-        launch_state_split(P, h->stream);   // the running state of a mixed or double-word block
+        launch_state_split(P, h->precision == MSX_PREC_MIXED, h->stream);   // the running state of a mixed or double-word block
         MSX_CUDA(cudaGetLastError());
     }
     if (P.visc) {
@@ -1171,7 +1171,7 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
             if (h->h_ctrl[(k - 1) & 1].stop) break;
         }
     }
-    if (pair_state(h)) launch_state_merge(h->P, h->stream);   // u, v, a for the caller
+    if (pair_state(h)) launch_state_merge(h->P, h->precision == MSX_PREC_MIXED, h->stream);   // u, v, a for the caller
     MSX_CUDA(cudaEventRecord(h->ev1, h->stream));
     MSX_CUDA(cudaStreamSynchronize(h->stream));
     Ctrl fin = h->h_ctrl[k & 1];
@@ -1427,7 +1427,7 @@ extern "C" msx_status msx_profile(msx_handle *h, int64_t steps, msx_profile_repo
             h->elem(h->P, parity, h->stream);
         cudaEventRecord(ev[3 * i + 2], h->stream);
     }
-    if (pair_state(h)) launch_state_merge(h->P, h->stream);
+    if (pair_state(h)) launch_state_merge(h->P, h->precision == MSX_PREC_MIXED, h->stream);
     cudaError_t err = cudaStreamSynchronize(h->stream);
     double tn = 0, te = 0;
     for (long long i = 0; i < n; i++) {
