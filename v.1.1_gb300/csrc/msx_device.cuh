@@ -540,6 +540,28 @@ __device__ __forceinline__ double pow2_scale(double x, int k)
     return x * __longlong_as_double((long long)(k + 1023) << 52);
 }
 
+// A 24-byte corner slot of the FP64 layout (slot k at byte 24 k: 16-byte
+// aligned for even k) in one 16-byte and one 8-byte access instead of three
+// 8-byte ones: the 16-byte half holds values 0-1 of an even slot, 1-2 of an
+// odd one.  The selects keep the warp on one path.
+__device__ __forceinline__ void ld_slot24(const double *base, long long k, double &x, double &y, double &z)
+{
+    const bool odd = k & 1;
+    const double *s = base + 3 * k;
+    const double2 v = __ldg(reinterpret_cast<const double2 *>(s + (odd ? 1 : 0)));
+    const double w = __ldg(s + (odd ? 0 : 2));
+    x = odd ? w : v.x;
+    y = odd ? v.x : v.y;
+    z = odd ? v.y : w;
+}
+__device__ __forceinline__ void st_slot24(double *base, long long k, double x, double y, double z)
+{
+    const bool odd = k & 1;
+    double *s = base + 3 * k;
+    *reinterpret_cast<double2 *>(s + (odd ? 1 : 0)) = odd ? make_double2(y, z) : make_double2(x, y);
+    s[odd ? 0 : 2] = odd ? x : z;
+}
+
 __device__ __forceinline__ void node_quad_fp64(const Problem &p, long long i, bool valid, const NodeStep &ns)
 {
     const int q = threadIdx.x & 3;
@@ -572,10 +594,11 @@ __device__ __forceinline__ void node_quad_fp64(const Problem &p, long long i, bo
     const int n = k1 - k0;   // the same for the node's four lanes
     int e0 = 0, e1 = 0, e2 = 0;
     for (int k = k0 + q; k < k1; k += 4) {
-        const double *f = p.fe + (long long)k * 3;
-        e0 = max(e0, dexp_field(__ldg(f)));
-        e1 = max(e1, dexp_field(__ldg(f + 1)));
-        e2 = max(e2, dexp_field(__ldg(f + 2)));
+        double f0, f1, f2;
+        ld_slot24(p.fe, k, f0, f1, f2);
+        e0 = max(e0, dexp_field(f0));
+        e1 = max(e1, dexp_field(f1));
+        e2 = max(e2, dexp_field(f2));
     }
 #pragma unroll
     for (int o = 1; o <= 2; o <<= 1) {
@@ -591,10 +614,11 @@ __device__ __forceinline__ void node_quad_fp64(const Problem &p, long long i, bo
     if (fixed) {
         long long a0 = 0, a1 = 0, a2 = 0;
         for (int k = k0 + q; k < k1; k += 4) {
-            const double *f = p.fe + (long long)k * 3;
-            a0 += dfixed(__ldg(f), e0, H);
-            a1 += dfixed(__ldg(f + 1), e1, H);
-            a2 += dfixed(__ldg(f + 2), e2, H);
+            double f0, f1, f2;
+            ld_slot24(p.fe, k, f0, f1, f2);
+            a0 += dfixed(f0, e0, H);
+            a1 += dfixed(f1, e1, H);
+            a2 += dfixed(f2, e2, H);
         }
 #pragma unroll
         for (int o = 1; o <= 2; o <<= 1) {
@@ -1209,12 +1233,7 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
     const int4 sl = __ldg(p.slot + e);
     const int ks[4] = {sl.x, sl.y, sl.z, sl.w};
 #pragma unroll
-    for (int a = 0; a < 4; a++) {
-        double *fk = p.fe + (long long)ks[a] * 3;
-        fk[0] = f[a * 3];
-        fk[1] = f[a * 3 + 1];
-        fk[2] = f[a * 3 + 2];
-    }
+    for (int a = 0; a < 4; a++) st_slot24(p.fe, ks[a], f[a * 3], f[a * 3 + 1], f[a * 3 + 2]);
     if (FORCE_ONLY) return 0.0f;
     if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
     float du32[9], g32[9];
