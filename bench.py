@@ -65,6 +65,21 @@ def profiled(key, kernel="pool_elem_kernel<FP64>"):
         return None
 
 
+def fp64_peak():
+    """The FP64 pipe's DFMA rate on this GPU in G op/s, measured now by the
+    library's probe (v.1.1_gb300/_build/msx_fp64_peak, built with the library),
+    else the figure in profiles/ncu_figures.json; and which of the two."""
+    exe = os.path.join(ROOT, "v.1.1_gb300", "_build", "msx_fp64_peak")
+    try:
+        r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+        for line in r.stdout.splitlines():
+            if r.returncode == 0 and line.startswith("fp64_dfma_gops"):
+                return float(line.split()[1]), "measured"
+    except (OSError, subprocess.SubprocessError, ValueError):
+        pass
+    return profiled("fp64_peak_gops"), "recorded"
+
+
 class Clocks:
     """nvidia-smi samples during a timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -610,7 +625,8 @@ def main():
     alg_step = 128.0 * ne + 176.0 * nn
     achieved = alg_elem / (prof.element_ms * 1e-3) / 1e9
     tr = profiled("dram_bytes_per_element")
-    ops, opk = profiled("fp64_ops_per_element"), profiled("fp64_peak_gops")
+    ops = profiled("fp64_ops_per_element")
+    opk, opk_kind = fp64_peak()
     step_gbs = alg_step / (secs / args.steps) / 1e9
     roofline = {"bound": "hbm", "kernel": "pool_elem_kernel<FP64>", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
@@ -622,8 +638,9 @@ def main():
                 "fp64_pipe": None if not ops else {
                     "achieved_gops": ops * ne / (prof.element_ms * 1e-3) / 1e9, "peak_gops": opk,
                     "frac": ops * ne / (prof.element_ms * 1e-3) / 1e9 / opk, "ops_per_element": ops,
-                    "note": "FP64 ops/element from ncu counters (profiles/ncu_figures.json); "
-                            "peak from a DFMA/DADD loop on this GPU"},
+                    "peak_kind": opk_kind,
+                    "note": "FP64 ops/element from ncu counters (profiles/ncu_figures.json); peak: DFMA "
+                            "rate with eight independent chains per thread on this GPU (msx_fp64_peak)"},
                 "note": "the kernel is bound by the FP64 pipe, not by HBM; both fractions are reported"}
     # a profiling run of one other precision reports that precision's kernel
     if args.only == "mixed":

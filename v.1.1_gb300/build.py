@@ -75,6 +75,11 @@ def build(force=False):
                         "-lmsx", "-Wl,-rpath,$ORIGIN"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("msx_deck build failed:\n" + r.stderr)
+    # the FP64 pipe's DFMA rate (the denominator of bench.py's FP64-pipe roofline)
+    r = subprocess.run([nvcc(), *ARCH, "-O3", os.path.join(CSRC, "msx_fp64_peak.cu"), "-o", os.path.join(OUT, "msx_fp64_peak")],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("msx_fp64_peak build failed:\n" + r.stderr)
     return LIB
 
 
