@@ -187,7 +187,11 @@ static void rebuild_tiles(msx_pool *p)
 {
     p->h_etiles.clear();
     p->h_ntiles.clear();
-    const int te = p->sched.tile_elems, tn = p->sched.threads / 2;   // node tiles: two passes of four lanes per node
+    // node tiles of eight passes of a CTA's threads / 4 nodes: a pooled step has
+    // many solves and millions of nodes, and tiles of two passes spent ~6 % of
+    // the batched step on claims and barriers (256 solves: 1.81e10 -> 1.92e10
+    // element-steps/s with eight passes)
+    const int te = p->sched.tile_elems, tn = p->sched.threads * 2;
     for (int s = 0; s < (int)p->slots.size(); s++) {
         const Slot &sl = p->slots[s];
         if (!sl.active) continue;
