@@ -1212,6 +1212,16 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
             F[i * 3 + j] = fma(du[i], G[j], fma(du[3 + i], G[3 + j], i == j ? fma(du[6 + i], G[6 + j], 1.0)
                                                                              : du[6 + i] * G[6 + j]));
     const MatParams &m = mat_of(p, e);
+    float scr = 0.0f;
+    if (!FORCE_ONLY) {   // the CFL screen first, so du dies before the stress
+        float du32[9], g32[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            du32[k] = f32_trunc(du[k]);
+            g32[k] = f32_trunc(G[k]);
+        }
+        scr = cfl_screen(p, e, g32, du32, m);
+    }
     stress_fast(m, F, __ldg(p.wJ + e), P);
     if (VISC && !FORCE_ONLY) {
         double Pv[9];
@@ -1236,13 +1246,7 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
     for (int a = 0; a < 4; a++) st_slot24(p.fe, ks[a], f[a * 3], f[a * 3 + 1], f[a * 3 + 2]);
     if (FORCE_ONLY) return 0.0f;
     if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
-    float du32[9], g32[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-        du32[k] = f32_trunc(du[k]);
-        g32[k] = f32_trunc(G[k]);
-    }
-    return cfl_screen(p, e, g32, du32, m);
+    return scr;
 }
 
 // corner forces only (internal-force hook)
