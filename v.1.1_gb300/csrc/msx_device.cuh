@@ -51,8 +51,10 @@ __device__ __forceinline__ double area_tri_ref(const double *p, const double *q,
     return 0.5 * sqrt(C0 * C0 + C1 * C1 + C2 * C2);
 }
 
-// geometry.cpp:264-301 inscribedSphere x 2 (classLinearTetrahedra.cpp:146-163)
-__device__ __forceinline__ double char_length_ref(const double *x)
+// geometry.cpp:264-301 inscribedSphere x 2 (classLinearTetrahedra.cpp:146-163);
+// *det_edges (when given) receives the determinant of the edge rows p1-p0,
+// p2-p0, p3-p0 that the volume comes from.
+__device__ __forceinline__ double char_length_ref(const double *x, double *det_edges = nullptr)
 {
     const double *p0 = x, *p1 = x + 3, *p2 = x + 6, *p3 = x + 9;
     double s1 = area_tri_ref(p0, p1, p2);
@@ -62,7 +64,9 @@ __device__ __forceinline__ double char_length_ref(const double *x)
     double A = fabs(s1) + fabs(s2) + fabs(s3) + fabs(s4);
     double M[9] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], p2[0] - p0[0], p2[1] - p0[1],
                    p2[2] - p0[2], p3[0] - p0[0], p3[1] - p0[1], p3[2] - p0[2]};
-    double V = 1.0 / 6.0 * fabs(det3_ref(M));
+    const double D = det3_ref(M);
+    if (det_edges) *det_edges = D;
+    double V = 1.0 / 6.0 * fabs(D);
     double r = 3.0 * V / A;
     return 2 * r;
 }
@@ -2217,17 +2221,34 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
             xyz[i * 4 + k] = X[i * nn + nd[k]];
             pts[k * 3 + i] = X[i * nn + nd[k]];
         }
-    const double natDev[12] = {-1.0, -1.0, -1.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
     double Jac[9], iJ[9];
+    // Jac_ij = 0 + sum_k x_ik natDev_kj in corner order, natDev's entries -1, 0
+    // and 1.  For finite coordinates that sum is (0 - x_i0) + x_i(j+1) bit for
+    // bit: 0 - x_i0 is never -0, and the products with 0 add signed zeros to a
+    // partial sum that is never -0, which leaves it unchanged.  A non-finite
+    // coordinate (x * 0 is NaN) takes the full sum.
+    bool finite = true;
 #pragma unroll
-    for (int i = 0; i < 3; i++)
+    for (int k = 0; k < 12; k++) finite &= isfinite(xyz[k]);
+    if (finite) {
 #pragma unroll
-        for (int j = 0; j < 3; j++) {
-            double c = 0;
+        for (int i = 0; i < 3; i++) {
+            const double y0 = 0.0 - xyz[i * 4];
 #pragma unroll
-            for (int k = 0; k < 4; k++) c += xyz[i * 4 + k] * natDev[k * 3 + j];
-            Jac[i * 3 + j] = c;
+            for (int j = 0; j < 3; j++) Jac[i * 3 + j] = y0 + xyz[i * 4 + j + 1];
         }
+    } else {
+        const double natDev[12] = {-1.0, -1.0, -1.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++) c += xyz[i * 4 + k] * natDev[k * 3 + j];
+                Jac[i * 3 + j] = c;
+            }
+    }
     double J = det3_ref(Jac);
     inv3_ref(Jac, iJ);
 #pragma unroll
@@ -2241,7 +2262,8 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
     wJ[e] = w;
     if (wJ32) wJ32[e] = (float)w;
     if (p.wJ32lo) const_cast<float *>(p.wJ32lo)[e] = (float)(w - (double)(float)w);
-    double L = char_length_ref(pts);
+    double v6;   // 6V, signed: the edge determinant of the inscribed-sphere volume
+    double L = char_length_ref(pts, &v6);
     Lref[e] = L;
     // A reference sliver (6V below 0.063 |e1||e2||e3|) gets a negative FP32
     // length: the FP32 CFL screens then always recompute it in FP64 (the mixed
@@ -2255,8 +2277,6 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
             e2[i] = pts[6 + i] - pts[i];
             e3[i] = pts[9 + i] - pts[i];
         }
-        const double v6 = e1[0] * (e2[1] * e3[2] - e2[2] * e3[1]) + e1[1] * (e2[2] * e3[0] - e2[0] * e3[2]) +
-                          e1[2] * (e2[0] * e3[1] - e2[1] * e3[0]);
         const double l1 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
         const double l2 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
         const double l3 = e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2];
@@ -2319,13 +2339,25 @@ __global__ void setup_mass_kernel(Problem p, double *mass, double *minv)
     if (i >= p.nn) return;
     const double phi = -1.0 * 0.25 - 1.0 * 0.25 - 1.0 * 0.25 + 1.0;
     double m = 0;
-    for (int k = p.node_ptr[i]; k < p.node_ptr[i + 1]; k++) {
-        long long e = p.node_inc[k] >> 2;
-        double rho = mat_of(p, e).rho;
-        double me = 0;
+    const int k1 = p.node_ptr[i + 1];
+    // the incidences' loads eight at a time, then their sums in element order
+    for (int k = p.node_ptr[i]; k < k1; k += 8) {
+        double w[8], r[8];
 #pragma unroll
-        for (int b = 0; b < 4; b++) me += p.wJ[e] * rho * phi * phi;
-        m += me;
+        for (int j = 0; j < 8; j++)
+            if (k + j < k1) {
+                const long long e = p.node_inc[k + j] >> 2;
+                w[j] = p.wJ[e];
+                r[j] = mat_of(p, e).rho;
+            }
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            if (k + j < k1) {
+                double me = 0;
+#pragma unroll
+                for (int b = 0; b < 4; b++) me += w[j] * r[j] * phi * phi;
+                m += me;
+            }
     }
     mass[i] = m;
     minv[i] = 1.0 / m;

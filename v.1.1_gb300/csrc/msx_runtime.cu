@@ -676,7 +676,25 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
                 return fail(MSX_ERR_ARG, "element material id out of range");
 
     msx_handle *h = new msx_handle();
+    // The node lists are built on a second stream while the element set-up runs
+    // (they need only conn); its work is synchronised before any exit.
+    struct SideStream {
+        cudaStream_t s = nullptr;
+        cudaEvent_t conn = nullptr, lists = nullptr;
+        void finish()
+        {
+            if (s) cudaStreamSynchronize(s);
+        }
+        ~SideStream()
+        {
+            finish();
+            if (s) cudaStreamDestroy(s);
+            for (cudaEvent_t e : {conn, lists})
+                if (e) cudaEventDestroy(e);
+        }
+    } side;
     auto bail = [&](msx_status st) {
+        side.finish();
         msx_destroy(h);
         return st;
     };
@@ -695,7 +713,10 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     for (int k = 0; k < num_mats; k++)
         if ((st = make_material(mats[k], h->P.mats[k])) != MSX_OK) return bail(st);
     if ((st = set_opts(h, opts)) != MSX_OK) return bail(st);
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&side.conn, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&side.lists, cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(MSX_ERR_CUDA, "stream creation failed"));
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
@@ -731,20 +752,35 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
 #define UP(dst, src, bytes) \
     if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return bail(fail(MSX_ERR_CUDA, "upload failed"))
     UP(h->conn.p, mesh->conn, sizeof(int4) * ne);
+    if (cudaEventRecord(side.conn, s) != cudaSuccess || cudaStreamWaitEvent(side.s, side.conn, 0) != cudaSuccess)
+        return bail(fail(MSX_ERR_CUDA, "stream ordering failed"));
     UP(h->X.p, mesh->X, sizeof(double) * 3 * nn);
     bind_problem(h);
     h->P.mat = h->mat.p;
     // The element set-up (FP64-bound, the longest set-up kernel) is queued
     // first, and the host builds the Dirichlet tables while it runs.  The
-    // node-list build after it range-checks conn; the set-up kernel skips an
-    // element with an out-of-range node id, and msx_create then fails on the
-    // check (every exit waits for the stream: msx_destroy synchronises it).
+    // node-list build on the side stream range-checks conn; the set-up kernel
+    // skips an element with an out-of-range node id, and msx_create then fails
+    // on the check (every exit waits for both streams).
     launch_setup_elements(h->P, h->X.p, s);
     BCTables bt;
     {
         std::string err;
         if (build_bc_tables(nn, bcs, num_bcs, h->t0, h->tf, bt, err) != MSX_OK) return bail(fail(MSX_ERR_ARG, err));
     }
+    cudaMemsetAsync(h->u.p, 0, sizeof(double) * 3 * nn, side.s);
+    cudaMemsetAsync(h->v.p, 0, sizeof(double) * 3 * nn, side.s);
+    cudaMemsetAsync(h->a.p, 0, sizeof(double) * 3 * nn, side.s);
+    {   // node -> (element, corner) lists in element order, built on the device
+        // (its range check waits for the side stream only)
+        std::string err;
+        if ((st = build_node_csr(h->conn.p, mesh->conn, ne, nn, h->node_ptr.p, h->node_inc.p, h->slot.p, side.s,
+                                 err)) != MSX_OK)
+            return bail(fail(st, err.c_str()));
+    }
+    if (cudaEventRecord(side.lists, side.s) != cudaSuccess || cudaStreamWaitEvent(s, side.lists, 0) != cudaSuccess)
+        return bail(fail(MSX_ERR_CUDA, "stream ordering failed"));
+    // the material ids (pageable: the copy may wait for the set-up) after the lists are queued
     std::vector<unsigned char> mids;
     if (h->mat.p) {
         mids.resize(ne);
@@ -752,15 +788,6 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
         UP(h->mat.p, mids.data(), ne);
     }
 #undef UP
-    cudaMemsetAsync(h->u.p, 0, sizeof(double) * 3 * nn, s);
-    cudaMemsetAsync(h->v.p, 0, sizeof(double) * 3 * nn, s);
-    cudaMemsetAsync(h->a.p, 0, sizeof(double) * 3 * nn, s);
-    {   // node -> (element, corner) lists in element order, built on the device
-        std::string err;
-        if ((st = build_node_csr(h->conn.p, mesh->conn, ne, nn, h->node_ptr.p, h->node_inc.p, h->slot.p, s, err)) !=
-            MSX_OK)
-            return bail(fail(st, err.c_str()));
-    }
     launch_setup_mass(h->P, h->mass.p, h->minv.p, s);
     if (h->minv2.p) launch_minv_split(h->minv.p, h->minv2.p, nn, s);
     if ((st = upload_bc_tables(h, bt)) != MSX_OK) return bail(st);
@@ -1152,19 +1179,31 @@ extern "C" msx_status msx_run(msx_handle *h, int64_t max_steps, msx_run_report *
     for (int b = 30; b >= 1; b--)
         if (rest & (1LL << b)) parts[nparts++] = b;
     if (full == 0 && nparts == 0) parts[nparts++] = 1;   // a stopped block: one short replay reports it
-    if (full > 0 && !h->graph && (st = build_graph(h, h->spg, &h->graph)) != MSX_OK) return st;
-    for (int j = 0; j < nparts; j++)
-        if (!h->part[parts[j]] && (st = build_graph(h, 1 << parts[j], &h->part[parts[j]])) != MSX_OK) return st;
     const long long needed = full + nparts;
     MSX_CUDA(cudaEventRecord(h->ev0, h->stream));
     // two replays in flight: check the older one's control slot
     long long k = 0, replayed = 0;
     for (;; k++) {
         const bool whole = k < full;
-        MSX_CUDA(cudaGraphLaunch(whole ? h->graph : h->part[parts[k - full]], h->stream));
-        replayed += whole ? h->spg : (1LL << parts[k - full]);
+        const int n = whole ? h->spg : 1 << parts[k - full];
+        cudaGraphExec_t *gx = whole ? &h->graph : &h->part[parts[k - full]];
+        // A chunk whose graph is not captured yet is launched step by step, and
+        // its graph captured while the device runs it: the first call of a
+        // handle does not wait for the captures.
+        const bool direct = !*gx;
+        if (direct) {
+            bind_problem(h);
+            for (int i = 0; i < n; i++) launch_step(h, (i & 1) ? 0 : 1);
+        } else
+            MSX_CUDA(cudaGraphLaunch(*gx, h->stream));
+        MSX_CUDA(cudaGetLastError());
+        replayed += n;
         MSX_CUDA(cudaMemcpyAsync(h->h_ctrl + (k & 1), h->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
         MSX_CUDA(cudaEventRecord(h->evc[k & 1], h->stream));
+        if (direct && (st = build_graph(h, n, gx)) != MSX_OK) {
+            cudaStreamSynchronize(h->stream);
+            return st;
+        }
         if (latest.stop || k + 1 >= needed) break;
         if (k >= 1) {
             MSX_CUDA(cudaEventSynchronize(h->evc[(k - 1) & 1]));
