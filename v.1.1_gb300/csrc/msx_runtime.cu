@@ -713,8 +713,13 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     for (int k = 0; k < num_mats; k++)
         if ((st = make_material(mats[k], h->P.mats[k])) != MSX_OK) return bail(st);
     if ((st = set_opts(h, opts)) != MSX_OK) return bail(st);
+    // The side stream has the greatest priority: the block scheduler then
+    // dispatches the short list-building kernels as soon as set-up blocks retire
+    // instead of after the set-up grid's last block.
+    int prio_least = 0, prio_greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&side.s, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
         cudaEventCreateWithFlags(&side.conn, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&side.lists, cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(MSX_ERR_CUDA, "stream creation failed"));
