@@ -2201,10 +2201,10 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
 // classLinearTetrahedra.cpp:171-268 (Jacobian, inverse, dphi), classGPs.cpp:27
 // (wJ = 0.166666666667 |J|), classLinearTetrahedra.cpp:129-140 (charLength).
 __global__ void setup_elements_kernel(Problem p, const double *X, double *G, double *wJ, double *Lref,
-                                      float *G32, float *wJ32, float *Lref32)
+                                      float *G32, float *wJ32, float *Lref32, long long e0, long long e1)
 {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= p.ne) return;
+    const long long e = e0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;   // elements [e0, e1)
+    if (e >= e1) return;
     const long long nn = p.nn, ne = p.ne;
     int4 cn = p.conn[e];
     // an out-of-range node id: the node-list build queued after this kernel
@@ -2353,10 +2353,12 @@ __global__ void setup_mass_kernel(Problem p, double *mass, double *minv)
 #pragma unroll
         for (int j = 0; j < 8; j++)
             if (k + j < k1) {
-                double me = 0;
-#pragma unroll
-                for (int b = 0; b < 4; b++) me += w[j] * r[j] * phi * phi;
-                m += me;
+                // me = 0 + z + z + z + z over the four corners b, z = ((wJ rho) phi) phi:
+                // that sum is (3z) + z bit for bit (0 + z = z and z + z = 2z are exact,
+                // 2z + z rounds 3z once); a z of -0 gives -0 instead of +0, which adds
+                // to m the same way
+                const double z = w[j] * r[j] * phi * phi;
+                m += __dadd_rn(__dmul_rn(3.0, z), z);
             }
     }
     mass[i] = m;

@@ -21,11 +21,13 @@ void launch_elem_exact(const Problem &p, int parity, cudaStream_t s)
         elem_kernel_exact_screened<false><<<grid_for(p.ne, kElemBlock), kElemBlock, 0, s>>>(p, parity);
 }
 
-void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s)
+void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s, long long e0, long long e1)
 {
-    setup_elements_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(
+    if (e1 < 0) e1 = p.ne;
+    if (e1 <= e0) return;
+    setup_elements_kernel<<<grid_for(e1 - e0, 256), 256, 0, s>>>(
         p, X, const_cast<double *>(p.G), const_cast<double *>(p.wJ), const_cast<double *>(p.Lref),
-        const_cast<float *>(p.G32), const_cast<float *>(p.wJ32), const_cast<float *>(p.Lref32));
+        const_cast<float *>(p.G32), const_cast<float *>(p.wJ32), const_cast<float *>(p.Lref32), e0, e1);
 }
 
 void launch_mode_arrays(const Problem &p, float *G32, float *wJ32, float *G32lo, float *wJ32lo, cudaStream_t s)

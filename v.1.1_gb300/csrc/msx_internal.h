@@ -195,7 +195,8 @@ void launch_node_exact(const Problem &p, int parity, cudaStream_t s);
 void launch_elem_exact(const Problem &p, int parity, cudaStream_t s);
 
 // set-up (exact operation order)
-void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s);
+// the element set-up of elements [e0, e1) (e1 < 0: to the last element)
+void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s, long long e0 = 0, long long e1 = -1);
 void launch_setup_mass(const Problem &p, double *mass, double *minv, cudaStream_t s);
 // a precision mode's FP32 element arrays (any pointer may be null) from G, wJ and X
 void launch_mode_arrays(const Problem &p, float *G32, float *wJ32, float *G32lo, float *wJ32lo, cudaStream_t s);

@@ -419,8 +419,13 @@ static msx_status upload_tiled(msx_handle *h)
 
 // The Dirichlet tables on the device (enqueued on the handle's stream; the
 // host vectors may go once this returns).
-static msx_status upload_bc_tables(msx_handle *h, const BCTables &t)
+// pieces of the connectivity upload that the element set-up follows (meshes of
+// 2^20 elements and more)
+constexpr int kSetupChunks = 4;
+
+static msx_status upload_bc_tables(msx_handle *h, const BCTables &t, cudaStream_t strm = nullptr)
 {
+    if (!strm) strm = h->stream;
     h->bc_rec.release();
     h->bcs.release();
     h->bc_nodes.release();
@@ -430,14 +435,14 @@ static msx_status upload_bc_tables(msx_handle *h, const BCTables &t)
     MSX_CUDA(h->bc_nodes.alloc(t.nodes.size()));
     if (!t.nodes.empty())
         MSX_CUDA(cudaMemcpyAsync(h->bc_nodes.p, t.nodes.data(), sizeof(int2) * t.nodes.size(), cudaMemcpyHostToDevice,
-                                 h->stream));
-    launch_node_bc_scatter(h->node_bc.p, h->P.nn, h->bc_nodes.p, (long long)t.nodes.size(), h->stream);
+                                 strm));
+    launch_node_bc_scatter(h->node_bc.p, h->P.nn, h->bc_nodes.p, (long long)t.nodes.size(), strm);
     if (!t.rec.empty())
         MSX_CUDA(cudaMemcpyAsync(h->bc_rec.p, t.rec.data(), sizeof(int2) * t.rec.size(), cudaMemcpyHostToDevice,
-                                 h->stream));
+                                 strm));
     if (!t.ent.empty())
         MSX_CUDA(cudaMemcpyAsync(h->bcs.p, t.ent.data(), sizeof(BCEntry) * t.ent.size(), cudaMemcpyHostToDevice,
-                                 h->stream));
+                                 strm));
     MSX_CUDA(cudaGetLastError());
     return MSX_OK;
 }
@@ -676,11 +681,13 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
                 return fail(MSX_ERR_ARG, "element material id out of range");
 
     msx_handle *h = new msx_handle();
-    // The node lists are built on a second stream while the element set-up runs
-    // (they need only conn); its work is synchronised before any exit.
+    // A second stream uploads the mesh (conn in chunks), builds the node lists
+    // (they need only conn) and uploads the Dirichlet tables while the element
+    // set-up runs chunk by chunk on the handle's stream; its work is
+    // synchronised before any exit.
     struct SideStream {
         cudaStream_t s = nullptr;
-        cudaEvent_t conn = nullptr, lists = nullptr;
+        cudaEvent_t chunk[kSetupChunks] = {}, lists = nullptr;
         void finish()
         {
             if (s) cudaStreamSynchronize(s);
@@ -689,8 +696,9 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
         {
             finish();
             if (s) cudaStreamDestroy(s);
-            for (cudaEvent_t e : {conn, lists})
+            for (cudaEvent_t e : chunk)
                 if (e) cudaEventDestroy(e);
+            if (lists) cudaEventDestroy(lists);
         }
     } side;
     auto bail = [&](msx_status st) {
@@ -720,9 +728,11 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithPriority(&side.s, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
-        cudaEventCreateWithFlags(&side.conn, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&side.lists, cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(MSX_ERR_CUDA, "stream creation failed"));
+    for (cudaEvent_t &e : side.chunk)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(MSX_ERR_CUDA, "event creation failed"));
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
     cudaEventCreateWithFlags(&h->evc[0], cudaEventDisableTiming);
@@ -754,20 +764,30 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     // the first block's mode's own arrays, filled by the set-up kernels below
     if ((st = mode_buffers(h, h->precision, false)) != MSX_OK) return bail(st);
     cudaStream_t s = h->stream;
-#define UP(dst, src, bytes) \
-    if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return bail(fail(MSX_ERR_CUDA, "upload failed"))
-    UP(h->conn.p, mesh->conn, sizeof(int4) * ne);
-    if (cudaEventRecord(side.conn, s) != cudaSuccess || cudaStreamWaitEvent(side.s, side.conn, 0) != cudaSuccess)
-        return bail(fail(MSX_ERR_CUDA, "stream ordering failed"));
-    UP(h->X.p, mesh->X, sizeof(double) * 3 * nn);
+#define UP(dst, src, bytes, strm) \
+    if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, strm) != cudaSuccess) return bail(fail(MSX_ERR_CUDA, "upload failed"))
+    // X, then conn in chunks on the side stream; the element set-up (FP64-bound,
+    // the longest set-up kernel) of a chunk runs on the handle's stream while
+    // the next chunk uploads.  The node-list build after the uploads
+    // range-checks conn; the set-up kernel skips an element with an
+    // out-of-range node id, and msx_create then fails on the check (every exit
+    // waits for both streams).
+    UP(h->X.p, mesh->X, sizeof(double) * 3 * nn, side.s);
     bind_problem(h);
     h->P.mat = h->mat.p;
-    // The element set-up (FP64-bound, the longest set-up kernel) is queued
-    // first, and the host builds the Dirichlet tables while it runs.  The
-    // node-list build on the side stream range-checks conn; the set-up kernel
-    // skips an element with an out-of-range node id, and msx_create then fails
-    // on the check (every exit waits for both streams).
-    launch_setup_elements(h->P, h->X.p, s);
+    {
+        const int nchunk = ne >= (1LL << 20) ? kSetupChunks : 1;
+        const long long csz = (ne + nchunk - 1) / nchunk;
+        for (int c = 0; c < nchunk; c++) {
+            const long long e0 = c * csz, e1 = std::min(ne, e0 + csz);
+            if (e1 <= e0) break;
+            UP(h->conn.p + e0, mesh->conn + 4 * e0, sizeof(int4) * (e1 - e0), side.s);
+            if (cudaEventRecord(side.chunk[c], side.s) != cudaSuccess || cudaStreamWaitEvent(s, side.chunk[c], 0) != cudaSuccess)
+                return bail(fail(MSX_ERR_CUDA, "stream ordering failed"));
+            launch_setup_elements(h->P, h->X.p, s, e0, e1);
+        }
+    }
+    // the host builds the Dirichlet tables while the set-up runs
     BCTables bt;
     {
         std::string err;
@@ -783,19 +803,19 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
                                  err)) != MSX_OK)
             return bail(fail(st, err.c_str()));
     }
-    if (cudaEventRecord(side.lists, side.s) != cudaSuccess || cudaStreamWaitEvent(s, side.lists, 0) != cudaSuccess)
-        return bail(fail(MSX_ERR_CUDA, "stream ordering failed"));
-    // the material ids (pageable: the copy may wait for the set-up) after the lists are queued
+    if ((st = upload_bc_tables(h, bt, side.s)) != MSX_OK) return bail(st);
+    // the material ids (pageable: the copy may wait for the side stream's work)
     std::vector<unsigned char> mids;
     if (h->mat.p) {
         mids.resize(ne);
         for (long long e = 0; e < ne; e++) mids[e] = (unsigned char)mesh->elem_material[e];
-        UP(h->mat.p, mids.data(), ne);
+        UP(h->mat.p, mids.data(), ne, side.s);
     }
 #undef UP
+    if (cudaEventRecord(side.lists, side.s) != cudaSuccess || cudaStreamWaitEvent(s, side.lists, 0) != cudaSuccess)
+        return bail(fail(MSX_ERR_CUDA, "stream ordering failed"));
     launch_setup_mass(h->P, h->mass.p, h->minv.p, s);
     if (h->minv2.p) launch_minv_split(h->minv.p, h->minv2.p, nn, s);
-    if ((st = upload_bc_tables(h, bt)) != MSX_OK) return bail(st);
     if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
         return bail(fail(MSX_ERR_CUDA, "set-up kernels failed"));
     if (h->precision == MSX_PREC_DOUBLE_WORD && (st = check_double_word(h)) != MSX_OK) return bail(st);
