@@ -466,8 +466,9 @@ static msx_status upload_bcs(msx_handle *h, const msx_bc *bcs, long long nbc)
 // double-word) or FP32 slots.  With `fill`, derived arrays
 // are converted from the FP64 set-up data (a later block in a new mode); at
 // msx_create the set-up kernels fill them.
-static msx_status mode_buffers(msx_handle *h, int precision, bool fill)
+static msx_status mode_buffers(msx_handle *h, int precision, bool fill, cudaStream_t strm = nullptr)
 {
+    if (!strm) strm = h->stream;
     const long long ne = h->P.ne, nn = h->P.nn;
     const bool mixed = precision == MSX_PREC_MIXED, dw = precision == MSX_PREC_DOUBLE_WORD;
     float *G32 = nullptr, *wJ32 = nullptr, *G32lo = nullptr, *wJ32lo = nullptr;
@@ -493,12 +494,12 @@ static msx_status mode_buffers(msx_handle *h, int precision, bool fill)
     }
     if (mixed && !h->fe32.p) {
         MSX_CUDA(h->fe32.alloc(16 * ne));
-        MSX_CUDA(cudaMemsetAsync(h->fe32.p, 0, sizeof(float) * 16 * ne, h->stream));
+        MSX_CUDA(cudaMemsetAsync(h->fe32.p, 0, sizeof(float) * 16 * ne, strm));
     }
     if (precision == MSX_PREC_FP64 && !h->u4.p) MSX_CUDA(h->u4.alloc(4 * nn));   // filled at each block start
     if (!mixed && !h->fe.p) {
         MSX_CUDA(h->fe.alloc(12 * ne));
-        MSX_CUDA(cudaMemsetAsync(h->fe.p, 0, sizeof(double) * 12 * ne, h->stream));
+        MSX_CUDA(cudaMemsetAsync(h->fe.p, 0, sizeof(double) * 12 * ne, strm));
     }
     bind_problem(h);
     if (fill) {
@@ -742,27 +743,22 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
 
 #define ALLOC(buf, n) \
     if (cudaError_t e_ = buf.alloc(n)) return bail(fail(MSX_ERR_OOM, std::string("device allocation: ") + cudaGetErrorString(e_)))
+    // what the element set-up reads and writes (with the FP32 copies of G and
+    // wJ of a mixed or double-word handle); the rest is allocated while it runs
     ALLOC(h->conn, ne);
     ALLOC(h->G, 9 * ne);
     ALLOC(h->wJ, ne);
     ALLOC(h->Lref, ne);
     ALLOC(h->Lref32, ne);
     ALLOC(h->X, 3 * nn);
-    ALLOC(h->u, 3 * nn);
-    ALLOC(h->v, 3 * nn);
-    ALLOC(h->a, 3 * nn);
-    ALLOC(h->mass, nn);
-    ALLOC(h->minv, nn);
-    ALLOC(h->slot, ne);
-    ALLOC(h->node_ptr, nn + 1);
-    ALLOC(h->node_inc, 4 * ne);
-    ALLOC(h->ctrl, 2);
-    ALLOC(h->dtmin, 4);
-    ALLOC(h->flags, 2);
-    if (mesh->elem_material && num_mats > 1) ALLOC(h->mat, ne);
-#undef ALLOC
-    // the first block's mode's own arrays, filled by the set-up kernels below
-    if ((st = mode_buffers(h, h->precision, false)) != MSX_OK) return bail(st);
+    if (h->precision == MSX_PREC_MIXED || h->precision == MSX_PREC_DOUBLE_WORD) {
+        ALLOC(h->G32, 9 * ne);
+        ALLOC(h->wJ32, ne);
+    }
+    if (h->precision == MSX_PREC_DOUBLE_WORD) {
+        ALLOC(h->G32lo, 9 * ne);
+        ALLOC(h->wJ32lo, ne);
+    }
     cudaStream_t s = h->stream;
 #define UP(dst, src, bytes, strm) \
     if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, strm) != cudaSuccess) return bail(fail(MSX_ERR_CUDA, "upload failed"))
@@ -787,6 +783,23 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
             launch_setup_elements(h->P, h->X.p, s, e0, e1);
         }
     }
+    ALLOC(h->u, 3 * nn);
+    ALLOC(h->v, 3 * nn);
+    ALLOC(h->a, 3 * nn);
+    ALLOC(h->mass, nn);
+    ALLOC(h->minv, nn);
+    ALLOC(h->slot, ne);
+    ALLOC(h->node_ptr, nn + 1);
+    ALLOC(h->node_inc, 4 * ne);
+    ALLOC(h->ctrl, 2);
+    ALLOC(h->dtmin, 4);
+    ALLOC(h->flags, 2);
+    if (mesh->elem_material && num_mats > 1) ALLOC(h->mat, ne);
+#undef ALLOC
+    // the rest of the first block's mode's own arrays (zero fills on the side stream)
+    if ((st = mode_buffers(h, h->precision, false, side.s)) != MSX_OK) return bail(st);
+    bind_problem(h);
+    h->P.mat = h->mat.p;
     // the host builds the Dirichlet tables while the set-up runs
     BCTables bt;
     {
