@@ -165,6 +165,33 @@ def test_setup_data_bitwise_equal_to_oracle():
     assert np.array_equal(mass, O.lumped_mass(mesh, mats, wJo))
 
 
+def test_setup_data_bitwise_equal_to_oracle_large_two_materials():
+    """A mesh of 2^20 elements or more takes the chunked connectivity upload,
+    with the element set-up following each piece and the material ids and node
+    lists on the second stream: its set-up data stay bit for bit the oracle's,
+    with signed zeros among the coordinates (the Jacobian's (0 - x0) + x1 form)
+    and two materials (the lumped mass's (3z) + z sum)."""
+    n = 60
+    X, conn = msx.mesh_cube(n, seed=5, jitter=0.1)
+    assert conn.shape[0] >= 1 << 20
+    X = X.copy()
+    flat = X.reshape(-1)
+    zeros = np.nonzero(flat == 0.0)[0]
+    assert zeros.size > 100
+    flat[zeros[::2]] = -0.0
+    em = (np.arange(conn.shape[0]) % 3 == 0).astype(np.int32)
+    mats = [O.Material(O.COMPRESSIBLE_NH, 1e6, 0.3, 1000.0), O.Material(O.STVK, 3e6, 0.25, 2500.0)]
+    mesh = O.Mesh(X, conn, elem_mat=em)
+    S = msx.Solver(X, conn, [(m.law, m.young, m.nu, m.rho) for m in mats],
+                   msx.cube_bcs(n, 0.1, msx.BC_VEL_RAMP, 200), 0.0, 0.02, 0.5, elem_material=em)
+    G, wJ, L, mass = S.element_data()
+    S.close()
+    dphi, wJo, Lo = O.precompute(mesh)
+    assert np.array_equal(G.T.reshape(-1, 3, 3), dphi.reshape(-1, 4, 3)[:, 1:, :])
+    assert np.array_equal(wJ, wJo) and np.array_equal(L, Lo)
+    assert np.array_equal(mass, O.lumped_mass(mesh, mats, wJo))
+
+
 @pytest.mark.parametrize("law", [msx.NEO_HOOKEAN, msx.COMPRESSIBLE_NH, msx.STVK, msx.LINEAR_ELASTIC])
 @pytest.mark.parametrize("precision,tol", [(msx.FP64_EXACT, 0.0), (msx.FP64, 1e-12), (msx.MIXED, 2e-5),
                                            (msx.DOUBLE_WORD, 1e-11)])
