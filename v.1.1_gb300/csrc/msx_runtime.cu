@@ -738,39 +738,21 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
     cudaEventCreate(&h->ev1);
     cudaEventCreateWithFlags(&h->evc[0], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&h->evc[1], cudaEventDisableTiming);
-    if (cudaMallocHost((void **)&h->h_ctrl, 2 * sizeof(Ctrl)) != cudaSuccess)
-        return bail(fail(MSX_ERR_OOM, "pinned control buffer"));
-
 #define ALLOC(buf, n) \
     if (cudaError_t e_ = buf.alloc(n)) return bail(fail(MSX_ERR_OOM, std::string("device allocation: ") + cudaGetErrorString(e_)))
-    // what the element set-up reads and writes (with the FP32 copies of G and
-    // wJ of a mixed or double-word handle); the rest is allocated while it runs
     ALLOC(h->conn, ne);
-    ALLOC(h->G, 9 * ne);
-    ALLOC(h->wJ, ne);
-    ALLOC(h->Lref, ne);
-    ALLOC(h->Lref32, ne);
     ALLOC(h->X, 3 * nn);
-    if (h->precision == MSX_PREC_MIXED || h->precision == MSX_PREC_DOUBLE_WORD) {
-        ALLOC(h->G32, 9 * ne);
-        ALLOC(h->wJ32, ne);
-    }
-    if (h->precision == MSX_PREC_DOUBLE_WORD) {
-        ALLOC(h->G32lo, 9 * ne);
-        ALLOC(h->wJ32lo, ne);
-    }
     cudaStream_t s = h->stream;
 #define UP(dst, src, bytes, strm) \
     if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, strm) != cudaSuccess) return bail(fail(MSX_ERR_CUDA, "upload failed"))
     // X, then conn in chunks on the side stream; the element set-up (FP64-bound,
     // the longest set-up kernel) of a chunk runs on the handle's stream while
-    // the next chunk uploads.  The node-list build after the uploads
+    // the next chunk uploads, and the arrays it writes are allocated while X
+    // and the first chunk upload.  The node-list build after the uploads
     // range-checks conn; the set-up kernel skips an element with an
     // out-of-range node id, and msx_create then fails on the check (every exit
     // waits for both streams).
     UP(h->X.p, mesh->X, sizeof(double) * 3 * nn, side.s);
-    bind_problem(h);
-    h->P.mat = h->mat.p;
     {
         const int nchunk = ne >= (1LL << 20) ? kSetupChunks : 1;
         const long long csz = (ne + nchunk - 1) / nchunk;
@@ -778,11 +760,32 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
             const long long e0 = c * csz, e1 = std::min(ne, e0 + csz);
             if (e1 <= e0) break;
             UP(h->conn.p + e0, mesh->conn + 4 * e0, sizeof(int4) * (e1 - e0), side.s);
-            if (cudaEventRecord(side.chunk[c], side.s) != cudaSuccess || cudaStreamWaitEvent(s, side.chunk[c], 0) != cudaSuccess)
+            if (cudaEventRecord(side.chunk[c], side.s) != cudaSuccess)
+                return bail(fail(MSX_ERR_CUDA, "stream ordering failed"));
+            if (c == 0) {
+                // what the set-up writes (with the FP32 copies of G and wJ of a
+                // mixed or double-word handle); the rest is allocated while it runs
+                ALLOC(h->G, 9 * ne);
+                ALLOC(h->wJ, ne);
+                ALLOC(h->Lref, ne);
+                ALLOC(h->Lref32, ne);
+                if (h->precision == MSX_PREC_MIXED || h->precision == MSX_PREC_DOUBLE_WORD) {
+                    ALLOC(h->G32, 9 * ne);
+                    ALLOC(h->wJ32, ne);
+                }
+                if (h->precision == MSX_PREC_DOUBLE_WORD) {
+                    ALLOC(h->G32lo, 9 * ne);
+                    ALLOC(h->wJ32lo, ne);
+                }
+                bind_problem(h);
+            }
+            if (cudaStreamWaitEvent(s, side.chunk[c], 0) != cudaSuccess)
                 return bail(fail(MSX_ERR_CUDA, "stream ordering failed"));
             launch_setup_elements(h->P, h->X.p, s, e0, e1);
         }
     }
+    if (cudaMallocHost((void **)&h->h_ctrl, 2 * sizeof(Ctrl)) != cudaSuccess)
+        return bail(fail(MSX_ERR_OOM, "pinned control buffer"));
     ALLOC(h->u, 3 * nn);
     ALLOC(h->v, 3 * nn);
     ALLOC(h->a, 3 * nn);
