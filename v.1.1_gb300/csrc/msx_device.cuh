@@ -1136,6 +1136,22 @@ __device__ __forceinline__ float f32_trunc(double x)
 // sliver (a negative Lref32, set at set-up); those are returned as -1 so that
 // the caller always recomputes them in FP64.  The same screen as the mixed
 // kernel's, with no streamed edge data.
+__device__ __forceinline__ float cfl_screen_edges(const Problem &p, long long e, const float *e1, const float *e2,
+                                                  const float *e3, const MatParams &m)
+{
+    const float C0 = e2[1] * e3[2] - e2[2] * e3[1], C1 = e2[2] * e3[0] - e2[0] * e3[2],
+                C2 = e2[0] * e3[1] - e2[1] * e3[0];
+    const float v6 = fabsf(e1[0] * C0 + e1[1] * C1 + e1[2] * C2);
+    const float l1 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+    const float l2 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+    const float l3 = e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2];
+    const float dist = char_length_edges<float>(e1, e2, e3);
+    const float Lr = __ldg(p.Lref32 + e);
+    const float dt = ((dist < Lr) ? dist : Lr) * m.inv_c_f;
+    const bool sliver = !(v6 * v6 >= 4e-3f * l1 * l2 * l3) || !(dt > 0.0f);
+    return sliver ? -1.0f : dt;
+}
+
 __device__ __forceinline__ float cfl_screen(const Problem &p, long long e, const float *g, const float *du,
                                             const MatParams &m)
 {
@@ -1157,17 +1173,91 @@ __device__ __forceinline__ float cfl_screen(const Problem &p, long long e, const
         e2[i] = C[3 + i] * idet + du[3 + i];
         e3[i] = C[6 + i] * idet + du[6 + i];
     }
-    const float C0 = e2[1] * e3[2] - e2[2] * e3[1], C1 = e2[2] * e3[0] - e2[0] * e3[2],
-                C2 = e2[0] * e3[1] - e2[1] * e3[0];
-    const float v6 = fabsf(e1[0] * C0 + e1[1] * C1 + e1[2] * C2);
-    const float l1 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
-    const float l2 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
-    const float l3 = e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2];
-    const float dist = char_length_edges<float>(e1, e2, e3);
-    const float Lr = __ldg(p.Lref32 + e);
-    const float dt = ((dist < Lr) ? dist : Lr) * m.inv_c_f;
-    const bool sliver = !(v6 * v6 >= 4e-3f * l1 * l2 * l3) || !(dt > 0.0f);
-    return sliver ? -1.0f : dt;
+    return cfl_screen_edges(p, e, e1, e2, e3, m);
+}
+
+// Plain FP64, compressible neo-Hookean, without forming F: with the deformed
+// edges e_b = E_b + (u_b - u_0) (b = 1..3, E_b the reference edges), the
+// corner force of node a = 1..3 is
+//   f_a = wJ P g_a = wJ mu F g_a + wJ (lambda ln J - mu) F^-T g_a,
+//   F g_a = sum_b M_ab e_b        (F = I + du G and E G = I give F = e G, and
+//                                  G g_a = (g_b . g_a)_b = M_a),
+//   F^-T g_a = (e_c x e_d) / det e   (the rows of e^-1: e2 x e3, e3 x e1, e1 x e2),
+//   J = det e / det E,
+// and f_0 = -(f_1 + f_2 + f_3): about 113 FP64 operations per element instead
+// of the cofactor form's 130.  The CFL screen takes the deformed edges
+// directly (truncated to FP32).
+template <bool ACT>
+__device__ __forceinline__ float elem_body_fp64_cnh(const Problem &p, long long e, int parity, double t,
+                                                    const MatParams &m, const int *nd)
+{
+    const long long ne = p.ne, nn = p.nn;
+    double ua[4][3];
+    if (p.u4) {
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            const double2 xy = __ldg(reinterpret_cast<const double2 *>(p.u4) + 2LL * nd[a]);
+            ua[a][0] = xy.x;
+            ua[a][1] = xy.y;
+            ua[a][2] = __ldg(p.u4 + 4LL * nd[a] + 2);
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int i = 0; i < 3; i++) ua[a][i] = p.u[nd[a] + i * nn];
+    }
+    double ed[9];   // ed[(b-1)*3 + i]: component i of the deformed edge e_b
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) ed[b * 3 + i] = __ldg(p.Eref + (b * 3 + i) * ne + e) + (ua[b + 1][i] - ua[0][i]);
+    float scr;
+    {
+        float e32[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) e32[k] = f32_trunc(ed[k]);
+        scr = cfl_screen_edges(p, e, e32, e32 + 3, e32 + 6, m);
+    }
+    const double *e1 = ed, *e2 = ed + 3, *e3 = ed + 6;
+    double cr[9];   // cr[(a-1)*3 + i] = det(e) (F^-T g_a)_i
+    cr[0] = e2[1] * e3[2] - e2[2] * e3[1];
+    cr[1] = e2[2] * e3[0] - e2[0] * e3[2];
+    cr[2] = e2[0] * e3[1] - e2[1] * e3[0];
+    cr[3] = e3[1] * e1[2] - e3[2] * e1[1];
+    cr[4] = e3[2] * e1[0] - e3[0] * e1[2];
+    cr[5] = e3[0] * e1[1] - e3[1] * e1[0];
+    cr[6] = e1[1] * e2[2] - e1[2] * e2[1];
+    cr[7] = e1[2] * e2[0] - e1[0] * e2[2];
+    cr[8] = e1[0] * e2[1] - e1[1] * e2[0];
+    const double dete = e1[0] * cr[0] + e1[1] * cr[1] + e1[2] * cr[2];
+    const double J = dete * __ldg(p.rdetE + e);
+    const double wJ = __ldg(p.wJ + e);
+    const double c1 = m.mu * wJ;
+    const double c2 = (m.lambda * log_near1(J) - m.mu) * (wJ / dete);
+    double Mv[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) Mv[k] = __ldg(p.Mg + k * ne + e);
+    const int mi[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};   // M_ab at Mv[mi[(a-1)*3 + (b-1)]]
+    double f[12];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const double Fg = e1[i] * Mv[mi[a * 3]] + e2[i] * Mv[mi[a * 3 + 1]] + e3[i] * Mv[mi[a * 3 + 2]];
+            f[(a + 1) * 3 + i] = c1 * Fg + c2 * cr[a * 3 + i];
+        }
+#pragma unroll
+    for (int i = 0; i < 3; i++) f[i] = -(f[3 + i] + f[6 + i] + f[9 + i]);
+    if (ACT && elem_dead(p, e, t))
+#pragma unroll
+        for (int k = 0; k < 12; k++) f[k] = 0.0;
+    const int4 sl = __ldg(p.slot + e);
+    const int ks[4] = {sl.x, sl.y, sl.z, sl.w};
+#pragma unroll
+    for (int a = 0; a < 4; a++) st_slot24(p.fe, ks[a], f[a * 3], f[a * 3 + 1], f[a * 3 + 2]);
+    if (e == 0 && !isfinite(p.u[1])) atomicOr(p.flags + (parity ^ 1), 1);
+    return scr;
 }
 
 // Plain FP64 with contraction: H from node differences, laws through the
@@ -1182,6 +1272,8 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
     const long long ne = p.ne, nn = p.nn;
     int4 cn = p.conn[e];
     int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    const MatParams &m = mat_of(p, e);
+    if (!FORCE_ONLY && !VISC && p.Eref && m.law == 1) return elem_body_fp64_cnh<ACT>(p, e, parity, t, m, nd);
     double G[9];
 #pragma unroll
     for (int k = 0; k < 9; k++) G[k] = __ldg(p.G + k * ne + e);
@@ -1215,7 +1307,6 @@ __device__ __forceinline__ float elem_body_fp64(const Problem &p, long long e, i
             // the identity enters the FMA chain (no separate 0 + x or 1 + x)
             F[i * 3 + j] = fma(du[i], G[j], fma(du[3 + i], G[3 + j], i == j ? fma(du[6 + i], G[6 + j], 1.0)
                                                                              : du[6 + i] * G[6 + j]));
-    const MatParams &m = mat_of(p, e);
     float scr = 0.0f;
     if (!FORCE_ONLY) {   // the CFL screen first, so du dies before the stress
         float du32[9], g32[9];
@@ -2194,10 +2285,64 @@ __global__ void __launch_bounds__(kStepThreads, MODE == MODE_MIXED ? 4 : (MODE =
     q.finish();
 }
 
-#ifdef MSX_SETUP_KERNELS
 // ---------------------------------------------------------------------------
 // Set-up kernels (reference operation order), built in the exact unit only
 // ---------------------------------------------------------------------------
+#ifdef MSX_SETUP_KERNELS
+// Reference Jacobian of a tet from xyz[i*4 + k] (coordinate i of corner k):
+// Jac_ij = 0 + sum_k x_ik natDev_kj in corner order, natDev's entries -1, 0
+// and 1 (classLinearTetrahedra.cpp:171-268).  For finite coordinates that sum
+// is (0 - x_i0) + x_i(j+1) bit for bit: 0 - x_i0 is never -0, and the products
+// with 0 add signed zeros to a partial sum that is never -0, which leaves it
+// unchanged.  A non-finite coordinate (x * 0 is NaN) takes the full sum.
+__device__ __forceinline__ void ref_jacobian(const double *xyz, double *Jac)
+{
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k < 12; k++) finite &= isfinite(xyz[k]);
+    if (finite) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const double y0 = 0.0 - xyz[i * 4];
+#pragma unroll
+            for (int j = 0; j < 3; j++) Jac[i * 3 + j] = y0 + xyz[i * 4 + j + 1];
+        }
+    } else {
+        const double natDev[12] = {-1.0, -1.0, -1.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                double c = 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++) c += xyz[i * 4 + k] * natDev[k * 3 + j];
+                Jac[i * 3 + j] = c;
+            }
+    }
+}
+
+// The plain FP64 mode's compressible neo-Hookean element data of element e
+// (Problem::Eref, Mg, rdetE) from its corner coordinates pts[k*3 + i], the
+// stored gradients g (G's nine entries) and the reference Jacobian's
+// determinant.
+__device__ __forceinline__ void write_cnh_arrays(const Problem &p, long long e, const double *pts, const double *g,
+                                                 double Jref)
+{
+    const long long ne = p.ne;
+    double *Er = const_cast<double *>(p.Eref), *Mw = const_cast<double *>(p.Mg);
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) Er[(b * 3 + i) * ne + e] = pts[(b + 1) * 3 + i] - pts[i];
+    int k = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = a; b < 3; b++, k++)
+            Mw[k * ne + e] = g[a * 3] * g[b * 3] + g[a * 3 + 1] * g[b * 3 + 1] + g[a * 3 + 2] * g[b * 3 + 2];
+    const_cast<double *>(p.rdetE)[e] = 1.0 / Jref;
+}
+
 // classLinearTetrahedra.cpp:171-268 (Jacobian, inverse, dphi), classGPs.cpp:27
 // (wJ = 0.166666666667 |J|), classLinearTetrahedra.cpp:129-140 (charLength).
 __global__ void setup_elements_kernel(Problem p, const double *X, double *G, double *wJ, double *Lref,
@@ -2222,38 +2367,14 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
             pts[k * 3 + i] = X[i * nn + nd[k]];
         }
     double Jac[9], iJ[9];
-    // Jac_ij = 0 + sum_k x_ik natDev_kj in corner order, natDev's entries -1, 0
-    // and 1.  For finite coordinates that sum is (0 - x_i0) + x_i(j+1) bit for
-    // bit: 0 - x_i0 is never -0, and the products with 0 add signed zeros to a
-    // partial sum that is never -0, which leaves it unchanged.  A non-finite
-    // coordinate (x * 0 is NaN) takes the full sum.
-    bool finite = true;
-#pragma unroll
-    for (int k = 0; k < 12; k++) finite &= isfinite(xyz[k]);
-    if (finite) {
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            const double y0 = 0.0 - xyz[i * 4];
-#pragma unroll
-            for (int j = 0; j < 3; j++) Jac[i * 3 + j] = y0 + xyz[i * 4 + j + 1];
-        }
-    } else {
-        const double natDev[12] = {-1.0, -1.0, -1.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-            for (int j = 0; j < 3; j++) {
-                double c = 0;
-#pragma unroll
-                for (int k = 0; k < 4; k++) c += xyz[i * 4 + k] * natDev[k * 3 + j];
-                Jac[i * 3 + j] = c;
-            }
-    }
+    ref_jacobian(xyz, Jac);
     double J = det3_ref(Jac);
     inv3_ref(Jac, iJ);
+    double gst[9];   // G as stored
 #pragma unroll
     for (int k = 0; k < 9; k++) {
         double g = 0.0 + iJ[k];
+        gst[k] = g;
         G[k * ne + e] = g;
         if (G32) G32[k * ne + e] = (float)g;
         if (p.G32lo) const_cast<float *>(p.G32lo)[k * ne + e] = (float)(g - (double)(float)g);
@@ -2265,6 +2386,7 @@ __global__ void setup_elements_kernel(Problem p, const double *X, double *G, dou
     double v6;   // 6V, signed: the edge determinant of the inscribed-sphere volume
     double L = char_length_ref(pts, &v6);
     Lref[e] = L;
+    if (p.Eref) write_cnh_arrays(p, e, pts, gst, J);
     // A reference sliver (6V below 0.063 |e1||e2||e3|) gets a negative FP32
     // length: the FP32 CFL screens then always recompute it in FP64 (the mixed
     // screen rebuilds the reference edges from G in FP32, which loses accuracy
@@ -2302,6 +2424,29 @@ __global__ void mode_arrays_kernel(Problem p, float *G32, float *wJ32, float *G3
     const double w = p.wJ[e];
     if (wJ32) wJ32[e] = (float)w;
     if (wJ32lo) wJ32lo[e] = (float)(w - (double)(float)w);
+}
+
+// Problem::Eref, Mg and rdetE of a handle whose FP64 block starts after its
+// set-up: the same operations as setup_elements_kernel, from X and the stored G.
+__global__ void cnh_arrays_kernel(Problem p)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.ne) return;
+    const long long nn = p.nn, ne = p.ne;
+    const int4 cn = p.conn[e];
+    const int nd[4] = {cn.x, cn.y, cn.z, cn.w};
+    double xyz[12], pts[12], g[9], Jac[9];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            xyz[i * 4 + k] = p.X[i * nn + nd[k]];
+            pts[k * 3 + i] = p.X[i * nn + nd[k]];
+        }
+    ref_jacobian(xyz, Jac);
+#pragma unroll
+    for (int k = 0; k < 9; k++) g[k] = p.G[k * ne + e];
+    write_cnh_arrays(p, e, pts, g, det3_ref(Jac));
 }
 
 // Previous-step F diagonal for the bulk viscosity, from displacement u, in the

@@ -35,6 +35,11 @@ void launch_mode_arrays(const Problem &p, float *G32, float *wJ32, float *G32lo,
     mode_arrays_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, G32, wJ32, G32lo, wJ32lo);
 }
 
+void launch_cnh_arrays(const Problem &p, cudaStream_t s)
+{
+    cnh_arrays_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p);
+}
+
 void launch_visc_init(const Problem &p, const double *u, cudaStream_t s)
 {
     visc_init_kernel<<<grid_for(p.ne, 256), 256, 0, s>>>(p, u);

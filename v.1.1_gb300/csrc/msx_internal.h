@@ -98,6 +98,14 @@ struct Problem {
     // kernel gathers a node with two loads of one sector instead of three
     // 8-byte loads from three rows.  Null in the other modes.
     double *u4;
+    // plain FP64 mode, compressible neo-Hookean elements: the reference edges
+    // X_b - X_0 (9*ne: Eref[(3(b-1) + i)*ne + e], b = 1..3), the metric
+    // M_ab = g_a . g_b of the shape-function gradients g_1..g_3 (6*ne, in the
+    // order 11 12 13 22 23 33) and 1/det of the reference Jacobian (ne).  The
+    // element kernel then takes F g_a = sum_b M_ab e_b and cof(F) g_a from the
+    // cross products of the deformed edges e_b, without forming F.  Null in the
+    // other modes and in pooled solves.
+    const double *Eref, *Mg, *rdetE;
     const double *mass;       // lumped mass per node
     const double *minv;       // 1/mass per node
     // mixed mode: u, v, a as FP32 (hi, lo) pairs (value hi + lo) while a block
@@ -200,6 +208,8 @@ void launch_setup_elements(const Problem &p, const double *X, cudaStream_t s, lo
 void launch_setup_mass(const Problem &p, double *mass, double *minv, cudaStream_t s);
 // a precision mode's FP32 element arrays (any pointer may be null) from G, wJ and X
 void launch_mode_arrays(const Problem &p, float *G32, float *wJ32, float *G32lo, float *wJ32lo, cudaStream_t s);
+// Problem::Eref, Mg and rdetE from X and G (the same values the set-up writes)
+void launch_cnh_arrays(const Problem &p, cudaStream_t s);
 // bulk viscosity: the elements' previous-step F diagonal from displacement u
 void launch_visc_init(const Problem &p, const double *u, cudaStream_t s);
 // min over elements of Lref/c (undeformed) or min(Lref, L(X+u))/c, into dtmin[slot]

@@ -155,9 +155,11 @@ static int pool_mode(int precision)
 // modes whose running state is the (hi, lo) FP32 pairs uhl, vhl, ahl
 static bool pair_state(int precision) { return precision == MSX_PREC_MIXED || precision == MSX_PREC_DOUBLE_WORD; }
 
-static size_t footprint(long long nn, long long ne, long long nbc, int precision)
+static size_t footprint(long long nn, long long ne, long long nbc, int precision, bool cnh)
 {
     size_t b = 0;
+    if (cnh)   // plain FP64, compressible neo-Hookean: Eref, Mg, rdetE
+        b += align256(sizeof(double) * 9 * ne) + align256(sizeof(double) * 6 * ne) + align256(sizeof(double) * ne);
     b += align256(sizeof(int4) * ne) + align256(sizeof(double) * 9 * ne);           // conn, G
     b += 2 * align256(sizeof(double) * ne);                                         // wJ, Lref
     b += align256(sizeof(float) * 9 * ne) + 2 * align256(sizeof(float) * ne);        // G32, wJ32, Lref32
@@ -571,7 +573,8 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
             if (!dw_in_range(mesh->X[i]))
                 return pfail(MSX_ERR_ARG, "double-word pool: a nonzero coordinate lies outside [2^-100, 2^100]");
     }
-    const size_t bytes = footprint(nn, ne, num_bcs, prec);
+    const bool cnh = prec == MSX_PREC_FP64 && mp.law == 1;   // the FP64 element kernel's F-free path
+    const size_t bytes = footprint(nn, ne, num_bcs, prec, cnh);
     {   // cheap early refusal; the slot is taken below, after the host tables
         std::lock_guard<std::mutex> lk(p->mu);
         bool free_slot = false;
@@ -646,6 +649,11 @@ extern "C" msx_status msx_pool_submit(msx_pool *p, const msx_mesh *mesh, const m
         P.minv = minv;
         P.uhl = (float2 *)carve(sizeof(float2) * 3 * nn);
         if (prec == MSX_PREC_FP64) P.u4 = (double *)carve(sizeof(double) * 4 * nn);
+        if (cnh) {   // written by the element set-up, as for a single solve
+            P.Eref = (double *)carve(sizeof(double) * 9 * ne);
+            P.Mg = (double *)carve(sizeof(double) * 6 * ne);
+            P.rdetE = (double *)carve(sizeof(double) * ne);
+        }
         float2 *minv2 = nullptr;
         if (pair_state(prec)) {
             P.vhl = (float2 *)carve(sizeof(float2) * 3 * nn);

@@ -101,6 +101,9 @@ struct msx_handle {
     DBuf<float> G32, wJ32, Lref32, fe32, G32lo, wJ32lo;
     DBuf<float2> uhl, vhl, ahl, minv2;
     DBuf<double> u4;   // plain FP64 mode: node-major copy of u (Problem::u4)
+    // plain FP64 mode with a compressible neo-Hookean material: reference
+    // edges, gradient metric and 1/det of the reference Jacobian (Problem::Eref, Mg, rdetE)
+    DBuf<double> Eref, Mg, rdetE;
     DBuf<unsigned char> mat;
     DBuf<int> node_ptr, node_inc, node_bc;
     DBuf<int2> bc_nodes;   // (node, record) of the nodes with Dirichlet entries
@@ -298,6 +301,9 @@ static void bind_problem(msx_handle *h)
     P.minv = h->minv.p;
     P.uhl = h->uhl.p;
     P.u4 = h->precision == MSX_PREC_FP64 ? h->u4.p : nullptr;
+    P.Eref = h->precision == MSX_PREC_FP64 ? h->Eref.p : nullptr;
+    P.Mg = h->precision == MSX_PREC_FP64 ? h->Mg.p : nullptr;
+    P.rdetE = h->precision == MSX_PREC_FP64 ? h->rdetE.p : nullptr;
     P.vhl = h->vhl.p;
     P.ahl = h->ahl.p;
     P.minv2 = h->minv2.p;
@@ -466,6 +472,15 @@ static msx_status upload_bcs(msx_handle *h, const msx_bc *bcs, long long nbc)
 // double-word) or FP32 slots.  With `fill`, derived arrays
 // are converted from the FP64 set-up data (a later block in a new mode); at
 // msx_create the set-up kernels fill them.
+// A material of the compressible neo-Hookean law (the plain FP64 mode's
+// F-free element path).
+static bool has_cnh(const msx_handle *h)
+{
+    for (int k = 0; k < h->P.nmat; k++)
+        if (h->P.mats[k].law == 1) return true;
+    return false;
+}
+
 static msx_status mode_buffers(msx_handle *h, int precision, bool fill, cudaStream_t strm = nullptr)
 {
     if (!strm) strm = h->stream;
@@ -497,6 +512,13 @@ static msx_status mode_buffers(msx_handle *h, int precision, bool fill, cudaStre
         MSX_CUDA(cudaMemsetAsync(h->fe32.p, 0, sizeof(float) * 16 * ne, strm));
     }
     if (precision == MSX_PREC_FP64 && !h->u4.p) MSX_CUDA(h->u4.alloc(4 * nn));   // filled at each block start
+    bool cnh = false;
+    if (precision == MSX_PREC_FP64 && has_cnh(h) && !h->Eref.p) {
+        MSX_CUDA(h->Eref.alloc(9 * ne));
+        MSX_CUDA(h->Mg.alloc(6 * ne));
+        MSX_CUDA(h->rdetE.alloc(ne));
+        cnh = true;
+    }
     if (!mixed && !h->fe.p) {
         MSX_CUDA(h->fe.alloc(12 * ne));
         MSX_CUDA(cudaMemsetAsync(h->fe.p, 0, sizeof(double) * 12 * ne, strm));
@@ -504,6 +526,7 @@ static msx_status mode_buffers(msx_handle *h, int precision, bool fill, cudaStre
     bind_problem(h);
     if (fill) {
         if (G32 || G32lo) launch_mode_arrays(h->P, G32, wJ32, G32lo, wJ32lo, h->stream);
+        if (cnh) launch_cnh_arrays(h->P, h->stream);
         if (minv2) launch_minv_split(h->minv.p, h->minv2.p, nn, h->stream);
         MSX_CUDA(cudaGetLastError());
         MSX_CUDA(cudaStreamSynchronize(h->stream));
@@ -777,6 +800,11 @@ extern "C" msx_status msx_create(const msx_mesh *mesh, const msx_material *mats,
                     ALLOC(h->G32lo, 9 * ne);
                     ALLOC(h->wJ32lo, ne);
                 }
+                if (h->precision == MSX_PREC_FP64 && has_cnh(h)) {
+                    ALLOC(h->Eref, 9 * ne);
+                    ALLOC(h->Mg, 6 * ne);
+                    ALLOC(h->rdetE, ne);
+                }
                 bind_problem(h);
             }
             if (cudaStreamWaitEvent(s, side.chunk[c], 0) != cudaSuccess)
@@ -851,6 +879,7 @@ extern "C" msx_status msx_destroy(msx_handle *h)
     for (auto *b : {&h->G32, &h->wJ32, &h->Lref32, &h->fe32, &h->G32lo, &h->wJ32lo}) b->release();
     for (auto *b : {&h->uhl, &h->vhl, &h->ahl, &h->minv2}) b->release();
     h->u4.release();
+    for (auto *b : {&h->Eref, &h->Mg, &h->rdetE}) b->release();
     h->mat.release();
     for (auto *b : {&h->node_ptr, &h->node_inc, &h->node_bc, &h->flags}) b->release();
     h->bc_rec.release();
